@@ -1,0 +1,199 @@
+/*
+ * libvkdt_cuda: GB300 (sm_103a) CUDA backend for the raw development hot path
+ * of vkdt:  denoise -> hilite -> demosaic -> colour -> filmcurv -> llap
+ * over a 16-bit Bayer (rggb) or X-Trans mosaic.
+ *
+ * The library replaces, for those nodes, vkdt's Vulkan device layer (src/qvk)
+ * and the modules' .comp shaders. Module names, parameters (the `params` files
+ * of each module), connector formats (rggb:ui16 in, rgba:f16 out) and the .cfg
+ * graph syntax are those of the reference. Every call returns an int that uses
+ * the VkResult numbering the reference scheduler propagates with QVKR
+ * (src/qvk/qvk.h): 0 success, negative errors, VK_INCOMPLETE (5) for a graph
+ * the library cannot run. Nothing in the library aborts or exits.
+ *
+ * Threading: a graph is used by one thread at a time (src/pipe/graph.h:67-69);
+ * different graphs may run concurrently on different streams.
+ */
+#ifndef VKDT_CUDA_H
+#define VKDT_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VKDT_CUDA_API_VERSION 1
+
+/* 8 character token packed into an int64, as src/pipe/token.h:15 */
+typedef uint64_t dt_token_t;
+
+/* return codes (VkResult numbering) */
+#define VKDT_CUDA_SUCCESS                        0
+#define VKDT_CUDA_NOT_READY                      1   /* VK_NOT_READY: job still running */
+#define VKDT_CUDA_TIMEOUT                        2   /* VK_TIMEOUT: bounded wait ran out */
+#define VKDT_CUDA_INCOMPLETE                     5   /* VK_INCOMPLETE: unconnected/unsupported graph */
+#define VKDT_CUDA_ERROR_OUT_OF_HOST_MEMORY     (-1)
+#define VKDT_CUDA_ERROR_OUT_OF_DEVICE_MEMORY   (-2)  /* allocation or admission failed */
+#define VKDT_CUDA_ERROR_INITIALIZATION_FAILED  (-3)
+#define VKDT_CUDA_ERROR_DEVICE_LOST            (-4)  /* device error or a device-side status word */
+#define VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED  (-11)  /* bad sizes / parameters */
+#define VKDT_CUDA_ERROR_UNKNOWN               (-13)
+
+/* run flags: the s_graph_run_* bits of src/pipe/modules/api.h:25-37 */
+#define VKDT_CUDA_RUN_ROI            (1u<<0)
+#define VKDT_CUDA_RUN_CREATE_NODES   (1u<<1)
+#define VKDT_CUDA_RUN_ALLOC          (1u<<2)
+#define VKDT_CUDA_RUN_RECORD_CMD_BUF (1u<<3)
+#define VKDT_CUDA_RUN_UPLOAD_SOURCE  (1u<<4)
+#define VKDT_CUDA_RUN_DOWNLOAD_SINK  (1u<<5)
+#define VKDT_CUDA_RUN_WAIT_DONE      (1u<<6)
+#define VKDT_CUDA_RUN_ALL            (0xffffffffu)
+
+/* image metadata the raw input module sets on its output
+ * (dt_image_params_t, src/pipe/module.h:72-109; filled in
+ * src/pipe/modules/i-raw/main.c:138-259) */
+typedef struct vkdt_cuda_img_param_t
+{
+  float    black[4];           /* black level, raw DN */
+  float    white[4];           /* white level, raw DN */
+  float    whitebalance[4];    /* camera coefficients, normalised to green = 1 */
+  uint32_t filters;            /* 0 rgb, 9 x-trans 6x6, else bayer rggb */
+  uint32_t crop_aabb[4];       /* x0 y0 x1 y1 of the active area */
+  float    cam_to_rec2020[9];  /* row major camera rgb -> linear rec2020 */
+  float    noise_a;            /* noise profile, gaussian part (normalised units) */
+  float    noise_b;            /* noise profile, poissonian part (normalised units) */
+}
+vkdt_cuda_img_param_t;
+
+/* one node of the expanded graph, as the modules' create_nodes emit them
+ * (dt_node_t, src/pipe/node.h:19-52): identity and dispatch size */
+typedef struct vkdt_cuda_node_info_t
+{
+  dt_token_t name;     /* module directory, e.g. "hilite" */
+  dt_token_t kernel;   /* kernel, e.g. "reduce" */
+  uint32_t   wd, ht, dp;
+  uint32_t   fused;    /* index of the CUDA kernel launch that computes this node */
+}
+vkdt_cuda_node_info_t;
+
+typedef struct vkdt_cuda_graph_t vkdt_cuda_graph_t;
+
+/* ---- device layer (replaces qvk_init/qvk_cleanup, src/cli/main.c:101,157) */
+
+/* select and initialise a CUDA device. flags: reserved, pass 0 */
+int  vkdt_cuda_init(int device_id, uint32_t flags);
+void vkdt_cuda_cleanup(void);
+/* 1 if the library runs node (name, kernel), e.g. ("llap", "assemble"):
+ * the question dt_graph_create_shader_module asks (src/pipe/graph.c:303-343) */
+int  vkdt_cuda_supports(dt_token_t name, dt_token_t kernel);
+
+/* ---- graph (dt_graph_init/dt_graph_cleanup, src/pipe/graph.h:176-194) */
+
+int  vkdt_cuda_graph_create(vkdt_cuda_graph_t **graph);
+void vkdt_cuda_graph_destroy(vkdt_cuda_graph_t *graph);
+
+/* read a .cfg graph (the text of e.g. bin/default-darkroom.i-raw) with the
+ * line syntax of dt_graph_read_config_ascii (src/pipe/graph-io.c:232-282):
+ * module:<name>:<inst>, connect:..., param:<name>:<inst>:<param>:<values>.
+ * modules outside the path are recorded and reported by
+ * vkdt_cuda_graph_unsupported(); the path must be connected i-raw:main ->
+ * denoise -> hilite -> demosaic -> [crop] -> colour -> filmcurv -> llap. */
+int  vkdt_cuda_graph_read_config(vkdt_cuda_graph_t *graph, const char *cfg, size_t len);
+/* number of modules in the cfg the library does not run; names written as
+ * tokens to `names` (up to max) */
+int  vkdt_cuda_graph_unsupported(vkdt_cuda_graph_t *graph, dt_token_t *names, int max);
+
+/* set/get a module parameter by name (dt_module_set_param_*, the values of a
+ * `param:` cfg line). bytes must match count*4 of the params file entry. */
+int  vkdt_cuda_graph_set_param(vkdt_cuda_graph_t *graph, dt_token_t module, dt_token_t inst,
+    dt_token_t param, const void *value, size_t bytes);
+int  vkdt_cuda_graph_get_param(vkdt_cuda_graph_t *graph, dt_token_t module, dt_token_t inst,
+    dt_token_t param, void *value, size_t bytes);
+
+/* source metadata: what i-raw's modify_roi_out provides (full size + img_param) */
+int  vkdt_cuda_graph_set_input(vkdt_cuda_graph_t *graph, int wd, int ht, const vkdt_cuda_img_param_t *ip);
+/* requested size of the output (the sink's roi). 0,0 = full size. a scale of
+ * >= 3 (bayer) switches demosaic to its half-size + resample path */
+int  vkdt_cuda_graph_set_output_size(vkdt_cuda_graph_t *graph, int wd, int ht);
+/* llap pyramid depth override (0 = automatic as llap/main.c:44-89) */
+int  vkdt_cuda_graph_set_llap_levels(vkdt_cuda_graph_t *graph, int levels);
+
+/* run modify_roi/create_nodes for every module (no device work): the node
+ * list becomes available through vkdt_cuda_graph_node*. */
+int  vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *graph);
+/* run create_nodes for every module and allocate device memory
+ * (dt_graph_run_modules + dt_graph_run_nodes_allocate, src/pipe/graph.c:747-806).
+ * *device_bytes (may be 0) receives the bytes allocated. */
+int  vkdt_cuda_graph_alloc(vkdt_cuda_graph_t *graph, uint64_t *device_bytes);
+/* the node list create_nodes produced (for inspection and per-node timing) */
+int  vkdt_cuda_graph_node_count(vkdt_cuda_graph_t *graph);
+int  vkdt_cuda_graph_node(vkdt_cuda_graph_t *graph, int i, vkdt_cuda_node_info_t *info);
+/* output size after alloc */
+int  vkdt_cuda_graph_output_size(vkdt_cuda_graph_t *graph, int *wd, int *ht);
+
+/* pinned host staging, valid until destroy (vkMapMemory of the staging
+ * buffers, src/pipe/graph-run-nodes-upload.h:60-80, -download.h:17-26):
+ * source = wd*ht uint16 mosaic, sink = out_wd*out_ht*4 IEEE half rgba */
+void *vkdt_cuda_graph_map_source(vkdt_cuda_graph_t *graph, size_t *bytes);
+void *vkdt_cuda_graph_map_sink(vkdt_cuda_graph_t *graph, size_t *bytes);
+/* the resident device buffers behind source and sink */
+int  vkdt_cuda_graph_device_buffers(vkdt_cuda_graph_t *graph, void **d_source, void **d_sink);
+
+/* run the graph on `stream` (a cudaStream_t, 0 = the graph's own stream):
+ * upload source (if flagged), all kernels, download sink (if flagged), wait
+ * (if flagged). the dt_graph_run sequence of src/pipe/graph.c:719-936. */
+int  vkdt_cuda_graph_run(vkdt_cuda_graph_t *graph, void *stream, uint32_t run_flags);
+/* bounded wait for the last run: VKDT_CUDA_TIMEOUT after timeout_ms */
+int  vkdt_cuda_graph_wait(vkdt_cuda_graph_t *graph, uint32_t timeout_ms);
+/* develop from a device mosaic into a device rgba f16 buffer (resident data,
+ * no host copies). both buffers as the graph's source/sink layouts. */
+int  vkdt_cuda_graph_develop(vkdt_cuda_graph_t *graph, const void *d_mosaic, void *d_rgba, void *stream);
+
+/* per-launch device times of the last run with timing enabled (the -d perf
+ * output of src/pipe/graph.c:881-932): names are "module:kernel" tokens of
+ * the fused launch. returns the count. */
+int  vkdt_cuda_graph_set_timing(vkdt_cuda_graph_t *graph, int enable);
+int  vkdt_cuda_graph_query_times(vkdt_cuda_graph_t *graph, float *ms, dt_token_t *names, dt_token_t *kernels, int max);
+
+/* 257 bin histogram the filmcurv module feeds to its display
+ * (OpenDRT/hist.comp): bins 0..255 and the count in [256]. enable before run. */
+int  vkdt_cuda_graph_set_hist(vkdt_cuda_graph_t *graph, int enable);
+int  vkdt_cuda_graph_hist(vkdt_cuda_graph_t *graph, uint32_t *hist257);
+
+/* standalone OpenDRT/hist.comp over a device rgba f16 image into a device u32[257]
+ * (cleared by the call) */
+int  vkdt_cuda_hist_rgba_f16(const void *d_rgba, int wd, int ht, uint32_t *d_hist257, void *stream);
+
+/* debug: copy an intermediate image of the last run to host floats.
+ * stage 0 denoise output (1 ch), 1 hilite output (1 ch), 2 filmcurv output (4 ch).
+ * requires vkdt_cuda_graph_set_debug(graph, 1) before alloc. */
+int  vkdt_cuda_graph_set_debug(vkdt_cuda_graph_t *graph, int enable);
+int  vkdt_cuda_graph_debug_stage(vkdt_cuda_graph_t *graph, int stage, float *out, size_t count);
+
+/* ---- synthetic raw scenes (the seeded mosaics the benchmarks are quoted on) */
+
+typedef struct vkdt_cuda_scene_t
+{
+  int32_t  wd, ht;
+  uint32_t seed, image_id;
+  uint32_t filters;           /* cfa of the mosaic (bayer rggb or 9) */
+  float    black, white;      /* DN */
+  float    noise_a, noise_b;  /* DN: variance = a + b * signal */
+  float    wb[3];             /* camera rgb = scene / wb */
+  float    pan_x, pan_y;      /* scene offset in pixels (video panning) */
+}
+vkdt_cuda_scene_t;
+
+/* fill a device (or host) u16 mosaic with the seeded scene */
+int  vkdt_cuda_scene_generate(const vkdt_cuda_scene_t *scene, void *d_mosaic, void *stream);
+int  vkdt_cuda_scene_generate_host(const vkdt_cuda_scene_t *scene, uint16_t *mosaic);
+
+/* last error message of this thread (static storage) */
+const char *vkdt_cuda_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,164 @@
+"""CPU oracle for the raw development path (test infrastructure only).
+
+Restatement of the reference shaders in C++ (oracle.cpp), loaded with ctypes.
+Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg use it,
+as the checker; the product library never touches it.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+# the oracle's OpenMP loops are short; spinning workers starve each other on
+# shared hosts, so they sleep while idle (read once, when the runtime loads)
+os.environ.setdefault("OMP_WAIT_POLICY", "PASSIVE")
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SO = os.path.join(HERE, "liboracle.so")
+
+
+def build(force=False):
+    src = os.path.join(HERE, "oracle.cpp")
+    hdr = os.path.join(HERE, "oracle.h")
+    if not force and os.path.exists(SO) and os.path.getmtime(SO) >= max(os.path.getmtime(src), os.path.getmtime(hdr)):
+        return SO
+    # no contraction: the oracle's operation order is the reference's
+    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-o", SO, src]
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+    if r.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + r.stdout.decode())
+    return SO
+
+
+class ImgParam(C.Structure):
+    _fields_ = [
+        ("black", C.c_float * 4), ("white", C.c_float * 4), ("whitebalance", C.c_float * 4),
+        ("filters", C.c_uint32), ("crop_aabb", C.c_uint32 * 4), ("cam_to_rec2020", C.c_float * 9),
+        ("noise_a", C.c_float), ("noise_b", C.c_float),
+    ]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("dn_strength", C.c_float), ("dn_luma", C.c_float), ("dn_detail", C.c_float), ("dn_pad", C.c_float),
+        ("dn_edges", C.c_float * 4), ("dn_gainmap", C.c_int32),
+        ("hl_white", C.c_float), ("hl_desat", C.c_float), ("hl_soft", C.c_float),
+        ("dm_colour", C.c_int32), ("dm_method", C.c_int32),
+        ("co_exposure", C.c_float), ("co_sat", C.c_float), ("co_matrix", C.c_int32), ("co_white", C.c_float * 4),
+        ("fc_light", C.c_float), ("fc_contrast", C.c_float), ("fc_bias", C.c_float), ("fc_colour", C.c_int32),
+        ("fc_chroma", C.c_float), ("fc_rolloff", C.c_float), ("fc_red", C.c_float), ("fc_yellow", C.c_float),
+        ("fc_blue", C.c_float), ("fc_shadows", C.c_float),
+        ("ll_sigma", C.c_float), ("ll_shadows", C.c_float), ("ll_hilights", C.c_float), ("ll_clarity", C.c_float),
+        ("ll_levels", C.c_int32), ("out_wd", C.c_int32), ("out_ht", C.c_int32),
+    ]
+
+
+class Stages(C.Structure):
+    _fields_ = [
+        ("denoise", C.POINTER(C.c_float)), ("hilite", C.POINTER(C.c_float)), ("demosaic", C.POINTER(C.c_float)),
+        ("colour", C.POINTER(C.c_float)), ("filmcurv", C.POINTER(C.c_float)), ("hist", C.POINTER(C.c_uint32)),
+        ("llap", C.POINTER(C.c_float)), ("out_wd", C.c_int32), ("out_ht", C.c_int32),
+        ("llap_levels", C.c_int32), ("hilite_levels", C.c_int32),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        l = C.CDLL(SO)
+        l.oracle_default_params.argtypes = [C.POINTER(Params)]
+        for f in (l.oracle_develop_f32, l.oracle_develop_f64):
+            f.restype = C.c_int
+            f.argtypes = [C.POINTER(C.c_uint16), C.c_int, C.c_int, C.POINTER(ImgParam), C.POINTER(Params), C.POINTER(Stages)]
+        l.oracle_noop.argtypes = [C.POINTER(C.c_uint16), C.c_int, C.c_int, C.POINTER(ImgParam), C.POINTER(C.c_float)]
+        l.oracle_hist.argtypes = [C.POINTER(C.c_float), C.c_int, C.c_int, C.POINTER(C.c_uint32)]
+        l.oracle_hist_bin.restype = C.c_uint32
+        l.oracle_hist_bin.argtypes = [C.c_float, C.c_float, C.c_float]
+        l.oracle_cfa_colour.restype = C.c_int
+        l.oracle_cfa_colour.argtypes = [C.c_uint32, C.c_int, C.c_int]
+        l.oracle_f16.restype = C.c_float
+        l.oracle_f16.argtypes = [C.c_float]
+        _lib = l
+    return _lib
+
+
+def default_params():
+    p = Params()
+    lib().oracle_default_params(C.byref(p))
+    return p
+
+
+def img_param(src):
+    """Copy a vkdt_gb300.ImgParam (same layout) into the oracle's struct."""
+    ip = ImgParam()
+    C.memmove(C.byref(ip), C.byref(src), C.sizeof(ImgParam))
+    return ip
+
+
+def _fptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def develop(mosaic, ip, params=None, double=False, stages=("llap",)):
+    """Run the oracle on a u16 mosaic; returns a dict of the requested stage images."""
+    mosaic = np.ascontiguousarray(mosaic, dtype=np.uint16)
+    ht, wd = mosaic.shape
+    params = params or default_params()
+    W = ip.crop_aabb[2] - ip.crop_aabb[0]
+    H = ip.crop_aabb[3] - ip.crop_aabb[1]
+    ow = params.out_wd or W
+    oh = params.out_ht or H
+    st = Stages()
+    bufs = {}
+    for name in stages:
+        if name in ("denoise", "hilite"):
+            bufs[name] = np.zeros((H, W), np.float32)
+        elif name == "hist":
+            bufs[name] = np.zeros(257, np.uint32)
+        else:
+            bufs[name] = np.zeros((oh, ow, 4), np.float32)
+        if name == "hist":
+            st.hist = bufs[name].ctypes.data_as(C.POINTER(C.c_uint32))
+        else:
+            setattr(st, name, _fptr(bufs[name]))
+    f = lib().oracle_develop_f64 if double else lib().oracle_develop_f32
+    r = f(mosaic.ctypes.data_as(C.POINTER(C.c_uint16)), wd, ht, C.byref(ip), C.byref(params), C.byref(st))
+    if r != 0:
+        raise RuntimeError("oracle develop failed with %d" % r)
+    bufs["llap_levels"] = st.llap_levels
+    bufs["hilite_levels"] = st.hilite_levels
+    return bufs
+
+
+def noop(mosaic, ip):
+    mosaic = np.ascontiguousarray(mosaic, dtype=np.uint16)
+    ht, wd = mosaic.shape
+    W = ip.crop_aabb[2] - ip.crop_aabb[0]
+    H = ip.crop_aabb[3] - ip.crop_aabb[1]
+    out = np.zeros((H, W), np.float32)
+    lib().oracle_noop(mosaic.ctypes.data_as(C.POINTER(C.c_uint16)), wd, ht, C.byref(ip), _fptr(out))
+    return out
+
+
+def hist(rgba):
+    rgba = np.ascontiguousarray(rgba, dtype=np.float32)
+    h = np.zeros(257, np.uint32)
+    lib().oracle_hist(_fptr(rgba), rgba.shape[1], rgba.shape[0], h.ctypes.data_as(C.POINTER(C.c_uint32)))
+    return h
+
+
+def hist_bin(r, g, b):
+    return lib().oracle_hist_bin(r, g, b)
+
+
+def cfa_colour(filters, x, y):
+    return lib().oracle_cfa_colour(filters, x, y)
+
+
+def f16(v):
+    return lib().oracle_f16(v)

@@ -1,0 +1,1431 @@
+// CPU oracle (test infrastructure only): restatement of the vkdt raw
+// development shaders. See oracle.h for the rules of use.
+//
+// Conventions shared by every node below (the reference's sampler and storage
+// semantics, src/qvk/qvk.c:596-611, src/pipe/graph-run-nodes-allocate.h:39-96):
+// - texture()/textureLod() use LINEAR filtering with MIRRORED_REPEAT wrap and
+//   normalised coordinates. At texel centres this is the texel itself, which
+//   is how the restatement reads it (fetch_m). Elsewhere the bilinear weights
+//   are evaluated exactly in the arithmetic type (tex_bilinear).
+// - texelFetch() has no wrap; out-of-range reads are undefined in the
+//   reference and read as 0 here (fetch_z).
+// - textureGather(.., 0) returns component 0 of the 2x2 quad in the order
+//   (i0,j1) (i1,j1) (i1,j0) (i0,j0).
+// - a one-channel image reads as (r, 0, 0, 1).
+// - every imageStore to an f16 image rounds to IEEE half (RTNE).
+// - min/max/clamp follow IEEE minNum/maxNum: a NaN operand yields the other
+//   operand, as the min/max instructions of GPUs do.
+// - R16_UNORM decodes as v/65535.
+#include "oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#ifdef _OPENMP
+#define OMP_FOR _Pragma("omp parallel for schedule(static)")
+#else
+#define OMP_FOR
+#endif
+
+namespace {
+
+// ------------------------------------------------------------------ helpers
+
+template<class T> static inline T f16r(T v)
+{ // round to IEEE binary16, round to nearest even, and back
+  if(std::isnan(v)) return v;
+  T a = std::fabs(v);
+  if(std::isinf(a)) return v;
+  if(a >= T(65520.0)) return std::copysign(T(INFINITY), v);
+  if(a < T(6.103515625e-05))
+  { // subnormal half: integer multiples of 2^-24
+    T m = std::nearbyint(std::ldexp(a, 24));
+    return std::copysign(std::ldexp(m, -24), v);
+  }
+  int e;
+  T f = std::frexp(a, &e);           // a = f * 2^e, f in [0.5, 1)
+  T m = std::nearbyint(std::ldexp(f, 11)); // 11 significant bits
+  return std::copysign(std::ldexp(m, e - 11), v);
+}
+
+template<class T> static inline T gmax(T a, T b) { return std::fmax(a, b); }
+template<class T> static inline T gmin(T a, T b) { return std::fmin(a, b); }
+template<class T> static inline T gclamp(T x, T lo, T hi) { return gmin(gmax(x, lo), hi); }
+template<class T> static inline T gmix(T x, T y, T a) { return x * (T(1) - a) + y * a; }
+template<class T> static inline T gsign(T x) { return x > T(0) ? T(1) : (x < T(0) ? T(-1) : T(0)); }
+template<class T> static inline T smoothstep(T e0, T e1, T x)
+{
+  T t = gclamp((x - e0) / (e1 - e0), T(0), T(1));
+  return t * t * (T(3) - T(2) * t);
+}
+template<class T> static inline T lum2020(T r, T g, T b)
+{ // shared.glsl:150-154 luminance_rec2020
+  return T(2.62700212e-01) * r + T(6.77998072e-01) * g + T(5.93017165e-02) * b;
+}
+
+static inline int mirror(int i, int n)
+{ // VK_SAMPLER_ADDRESS_MODE_MIRRORED_REPEAT
+  const int m = 2 * n;
+  int t = i % m;
+  if(t < 0) t += m;
+  return t < n ? t : m - 1 - t;
+}
+
+template<class T> struct img_t
+{
+  int w = 0, h = 0, c = 0;
+  std::vector<T> d;
+  img_t() {}
+  img_t(int w_, int h_, int c_) : w(w_), h(h_), c(c_), d((size_t)w_ * h_ * c_, T(0)) {}
+  T *px(int x, int y) { return d.data() + ((size_t)y * w + x) * c; }
+  const T *px(int x, int y) const { return d.data() + ((size_t)y * w + x) * c; }
+  T ch(int x, int y, int k) const
+  { // channel read with the (r,0,0,1) rule of one-channel formats
+    if(k < c) return px(x, y)[k];
+    return k == 3 ? T(1) : T(0);
+  }
+  void store(int x, int y, const T *v, int n)
+  { // imageStore into an f16 image
+    T *p = px(x, y);
+    for(int k = 0; k < c && k < n; k++) p[k] = f16r(v[k]);
+  }
+};
+
+// texelFetch: no wrap, undefined out of range -> 0
+template<class T> static inline T fetch_z(const img_t<T> &im, int x, int y, int k)
+{
+  if(x < 0 || y < 0 || x >= im.w || y >= im.h) return T(0);
+  return im.ch(x, y, k);
+}
+// texture() at a texel centre: mirrored texel
+template<class T> static inline T fetch_m(const img_t<T> &im, int x, int y, int k)
+{
+  return im.ch(mirror(x, im.w), mirror(y, im.h), k);
+}
+// texture() anywhere: x,y are texel-space coordinates (normalised * size)
+template<class T> static inline void tex_bilinear(const img_t<T> &im, T x, T y, T out[4])
+{
+  const T xs = x - T(0.5), ys = y - T(0.5);
+  const T fx = std::floor(xs), fy = std::floor(ys);
+  const int x0 = (int)fx, y0 = (int)fy;
+  const T ax = xs - fx, ay = ys - fy;
+  const int X0 = mirror(x0, im.w), X1 = mirror(x0 + 1, im.w);
+  const int Y0 = mirror(y0, im.h), Y1 = mirror(y0 + 1, im.h);
+  for(int k = 0; k < 4; k++)
+  {
+    const T t00 = im.ch(X0, Y0, k), t10 = im.ch(X1, Y0, k);
+    const T t01 = im.ch(X0, Y1, k), t11 = im.ch(X1, Y1, k);
+    out[k] = (t00 * (T(1) - ax) + t10 * ax) * (T(1) - ay) + (t01 * (T(1) - ax) + t11 * ax) * ay;
+  }
+}
+
+// CFA colour index (0 r, 1 g, 2 b) of an absolute mosaic position.
+// bayer: demosaic/splat.comp:197-222 (rggb at 0,0); x-trans: splat.comp:167-195.
+static inline int cfa_bayer(int x, int y)
+{
+  const int ox = x & 1, oy = y & 1;
+  if((ox == 0 && oy == 1) || (ox == 1 && oy == 0)) return 1;
+  if(ox == 0 && oy == 0) return 0;
+  return 2;
+}
+static inline int cfa_xtrans(int x, int y)
+{ // expects non-negative coordinates (callers add the 6 px margin)
+  const bool blue_top = ((x / 3 + y / 3) & 1) > 0;
+  const int px = x - (x / 3) * 3, py = y - (y / 3) * 3;
+  if(((px + py) & 1) == 0) return 1;
+  if(blue_top ^ (py == 1)) return 2;
+  return 0;
+}
+
+// shared.glsl:244-293 evd2x2 (after christoph peters). M = (m00, m10, m11)
+template<class T> static inline void evd2x2(T eval[2], T evec0[2], T evec1[2], T a, T b, T c)
+{
+  const T pHalf = T(-0.5) * (a + c);
+  const T q = a * c - b * b;
+  const T dr = std::sqrt(pHalf * pHalf - q);
+  eval[0] = -pHalf + dr;
+  eval[1] = -pHalf - dr;
+  const T a0 = a - eval[0], b0 = b, c0 = c - eval[0];
+  const T sl0 = a0 * a0 + b0 * b0;
+  const T sl1 = b0 * b0 + c0 * c0;
+  T sl;
+  if(sl0 > sl1) { evec1[0] = a0; evec1[1] = b0; sl = sl0; }
+  else          { evec1[0] = b0; evec1[1] = c0; sl = sl1; }
+  evec1[0] = (sl == T(0)) ? T(1) : evec1[0];
+  sl = (sl == T(0)) ? T(1) : sl;
+  const T inv = T(1) / std::sqrt(sl);
+  evec1[0] *= inv;
+  evec1[1] *= inv;
+  evec0[0] = evec1[1];
+  evec0[1] = -evec1[0];
+}
+
+// ------------------------------------------------------------------ colour matrices (src/pipe/modules/matrices.h, row major)
+static const double M_cat16_Mi[9] = { 1.86206786, -1.01125463,  0.14918677, 0.38752654,  0.62144744, -0.00897398, -0.01584150, -0.03412294,  1.04996444 };
+static const double M_cat16_M[9]  = { 0.401288, 0.650173, -0.051461, -0.250268, 1.204414,  0.045854, -0.002079, 0.048952,  0.953127 };
+static const double M_rec2020_to_xyz[9] = { 0.636958048301290991, 0.144616903586208406, 0.168880975164172054, 0.26270021201126692, 0.677998071518871148, 0.0593017164698619384, 4.9999999999999999e-17, 0.0280726930490874452, 1.06098505771079066 };
+static const double M_xyz_to_rec2020[9] = { 1.71665119, -0.35567078, -0.25336628, -0.66668435,  1.61648124,  0.01576855, 0.01763986, -0.04277061, 0.94210312 };
+static const double M_rec709_to_rec2020[9] = { 0.62750375, 0.32927542, 0.04330266, 0.06910828, 0.91951916, 0.0113596, 0.01639406, 0.08801125, 0.89538035 };
+static const double M_rec2020_to_rec709[9] = { 1.66022677, -0.58754761, -0.07283825, -0.12455334,  1.13292605, -0.00834963, -0.01815514, -0.10060303,  1.11899817 };
+static const double M_rec709_to_yuv[9] = { 0.299, 0.587, 0.114, -0.147, -0.289, 0.436, 0.615, -0.515, -0.100 };
+static const double M_yuv_to_rec709[9] = { 1.0, -3.94570707e-05, 1.13982797, 1.0, -3.94610164e-01, -5.80500316e-01, 1.0, 2.03199968, -4.81376263e-04 };
+
+template<class T> struct m3 { T m[9]; };
+template<class T> static m3<T> m3_load(const double *a) { m3<T> r; for(int i = 0; i < 9; i++) r.m[i] = T(a[i]); return r; }
+template<class T> static m3<T> m3_mul(const m3<T> &A, const m3<T> &B)
+{ // glsl A*B with column-major storage evaluates the same sums as row-major A*B
+  m3<T> r;
+  for(int i = 0; i < 3; i++) for(int j = 0; j < 3; j++)
+    r.m[3 * i + j] = A.m[3 * i + 0] * B.m[0 + j] + A.m[3 * i + 1] * B.m[3 + j] + A.m[3 * i + 2] * B.m[6 + j];
+  return r;
+}
+template<class T> static inline void m3_apply(const m3<T> &A, const T v[3], T o[3])
+{ // glsl mat3*vec3: col0*v.x + col1*v.y + col2*v.z
+  T r[3];
+  for(int i = 0; i < 3; i++) r[i] = A.m[3 * i + 0] * v[0] + A.m[3 * i + 1] * v[1] + A.m[3 * i + 2] * v[2];
+  o[0] = r[0]; o[1] = r[1]; o[2] = r[2];
+}
+
+// ------------------------------------------------------------------ denoise
+
+// denoise/noop.comp:36-57 (gain map absent on the synthetic input)
+template<class T> static img_t<T> denoise_noop(const img_t<T> &in, int wd, int ht,
+    const int crop[4], const T black[4], const T white[4])
+{
+  img_t<T> out(wd, ht, 4);
+  OMP_FOR
+  for(int y = 0; y < ht; y++) for(int x = 0; x < wd; x++)
+  {
+    T col[4];
+    for(int k = 0; k < 3; k++)
+      col[k] = gmax(T(0), (fetch_z(in, x + crop[0], y + crop[1], k) - black[k]) / (white[k] - black[k]));
+    col[3] = T(1);
+    out.store(x, y, col, 4);
+  }
+  return out;
+}
+
+// denoise/noise.glsl:1-11 (edges applied per channel)
+template<class T> static inline void noise_sigma(T out[3], T na, T nb, T black, T white, const T edges[4], T val)
+{
+  const T s = std::sqrt(na + gmax(T(0), (val - black) / (white - black)) * nb);
+  for(int k = 0; k < 3; k++)
+    out[k] = gclamp(std::exp2(T(12) * edges[k] + edges[3]) * s, T(1e-3), T(1e3));
+}
+
+// denoise/half.comp:24-74
+template<class T> static img_t<T> denoise_half(const img_t<T> &in, int wd, int ht,
+    const int crop[4], T white_g, uint32_t filters)
+{
+  img_t<T> out(wd, ht, 4);
+  OMP_FOR
+  for(int y = 0; y < ht; y++) for(int x = 0; x < wd; x++)
+  {
+    T rgba[4];
+    if(filters == 9)
+    {
+      const int bx = crop[0] + 3 * x, by = crop[1] + 3 * y;
+      T c[9];
+      for(int i = 0; i < 3; i++) for(int j = 0; j < 3; j++) c[3 * i + j] = fetch_z(in, bx + i, by + j, 0);
+      const T c0 = (c[1] + c[7]) * T(0.5), c1 = (c[3] + c[5]) * T(0.5);
+      if(((x + y + crop[0] + crop[1]) & 1) > 0) { rgba[0] = c0; rgba[2] = c1; }
+      else                                      { rgba[2] = c0; rgba[0] = c1; }
+      rgba[1] = (c[0] + c[2] + c[4] + c[6] + c[8]) * T(1.0) / T(5.0);
+      rgba[3] = T(1);
+    }
+    else
+    {
+      const int i0 = crop[0] + 2 * x, j0 = crop[1] + 2 * y;
+      T cx = fetch_m(in, i0, j0 + 1, 0), cy = fetch_m(in, i0 + 1, j0 + 1, 0);
+      T cz = fetch_m(in, i0 + 1, j0, 0), cw = fetch_m(in, i0, j0, 0);
+      if(cx >= white_g) cx = cz;
+      if(cz >= white_g) cz = cx;
+      rgba[0] = cw; rgba[1] = (cx + cz) / T(2); rgba[2] = cy; rgba[3] = T(1);
+    }
+    out.store(x, y, rgba, 4);
+  }
+  return out;
+}
+
+// denoise/cov.glsl:159-276 response(). p in texel coordinates of img.
+template<class T> static void denoise_response(const img_t<T> &img, int px_, int py_, T res_out[3], T cov[4])
+{
+  T mw[2] = {0, 0}, mb[2] = {0, 0}, smw = 0, smb = 0, mean_b = 0;
+  T Sw00 = 0, Sw01 = 0, Sw10 = 0, Sw11 = 0, Sb00 = 0, Sb01 = 0, Sb10 = 0, Sb11 = 0, sw = 0, sb = 0;
+  const T w = T(1);
+  for(int j = -2; j <= 2; j++) for(int i = -2; i <= 2; i++)
+  {
+    const T px = lum2020(fetch_m(img, px_ + i, py_ + j, 0), fetch_m(img, px_ + i, py_ + j, 1), fetch_m(img, px_ + i, py_ + j, 2));
+    const T p[2] = { T(i), T(j) };
+    mw[0] += p[0] * px * w; mw[1] += p[1] * px * w;
+    smw += px * w;
+    mb[0] += p[0] / px * w; mb[1] += p[1] / px * w;
+    smb += T(1) / px * w;
+  }
+  mw[0] /= smw; mw[1] /= smw;
+  mb[0] /= smb; mb[1] /= smb;
+  for(int j = -2; j <= 2; j++) for(int i = -2; i <= 2; i++)
+  {
+    const T px = lum2020(fetch_m(img, px_ + i, py_ + j, 0), fetch_m(img, px_ + i, py_ + j, 1), fetch_m(img, px_ + i, py_ + j, 2));
+    mean_b += px / T(25);
+    T p2 = px * px * w;
+    T p[2] = { T(i) - mw[0], T(j) - mw[1] };
+    Sw00 += p2 * p[0] * p[0]; Sw01 += p2 * p[0] * p[1]; Sw10 += p2 * p[1] * p[0]; Sw11 += p2 * p[1] * p[1];
+    sw += p2;
+    p[0] = T(i) - mb[0]; p[1] = T(j) - mb[1];
+    p2 = T(1) / (px * px) * w;
+    Sb00 += p2 * p[0] * p[0]; Sb01 += p2 * p[0] * p[1]; Sb10 += p2 * p[1] * p[0]; Sb11 += p2 * p[1] * p[1];
+    sb += p2;
+  }
+  Sw00 /= sw; Sw01 /= sw; Sw10 /= sw; Sw11 /= sw;
+  Sb00 /= sb; Sb01 /= sb; Sb10 /= sb; Sb11 /= sb;
+  const T detw = Sw00 * Sw11 - Sw10 * Sw01, detb = Sb00 * Sb11 - Sb10 * Sb01;
+  const bool usew = detw < detb;
+  T eval[2], evec0[2], evec1[2];
+  if(usew) evd2x2(eval, evec0, evec1, Sw00, Sw10, Sw11);
+  else     evd2x2(eval, evec0, evec1, Sb00, Sb10, Sb11);
+  eval[0] *= T(1.0); eval[1] *= T(0.05);
+  eval[0] = gclamp(eval[0], T(0.01), T(25)); eval[1] = gclamp(eval[1], T(0.01), T(25));
+  cov[0] = eval[0]; cov[1] = eval[1]; cov[2] = evec0[0]; cov[3] = evec0[1];
+  T res[3] = {0, 0, 0}, wt = 0;
+  for(int j = -2; j <= 2; j++) for(int i = -2; i <= 2; i++)
+  {
+    const T pr = fetch_m(img, px_ + i, py_ + j, 0), pg = fetch_m(img, px_ + i, py_ + j, 1), pb = fetch_m(img, px_ + i, py_ + j, 2);
+    if(pr > T(2) * mean_b) continue;
+    const T x0 = T(i) * evec0[0] + T(j) * evec0[1];
+    const T x1 = T(i) * evec1[0] + T(j) * evec1[1];
+    const T ww = gmax(T(1e-9), std::exp(T(-0.5) * (x0 / eval[0] * x0 + x1 / eval[1] * x1)));
+    res[0] += ww * pr; res[1] += ww * pg; res[2] += ww * pb;
+    wt += ww;
+  }
+  const T d = gmax(wt, T(1e-8));
+  res_out[0] = res[0] / d; res_out[1] = res[1] / d; res_out[2] = res[2] / d;
+}
+
+static inline void swz(int &x, int &y, int w, int h)
+{ // denoise/down.comp:102-104 decimated write position
+  const int ox = (x & 1) * (w + 1) / 2, oy = (y & 1) * (h + 1) / 2;
+  x = x / 2 + ox; y = y / 2 + oy;
+}
+
+// denoise/downcov.comp:41-63
+template<class T> static img_t<T> denoise_downcov(const img_t<T> &in, int wd, int ht, const int crop[4])
+{
+  img_t<T> out(wd, ht, 4);
+  OMP_FOR
+  for(int y = 0; y < ht; y++) for(int x = 0; x < wd; x++)
+  {
+    T rgb[3], cov[4];
+    denoise_response(in, x + crop[0], y + crop[1], rgb, cov);
+    T edge = gclamp(T(75) * gmax(T(0), cov[1] - T(0.09)), T(0), T(1));
+    edge = smoothstep(T(0.4), T(0.75), edge);
+    edge = gclamp(T(0.02) + edge, T(0), T(1));
+    int X = x, Y = y;
+    swz(X, Y, wd, ht);
+    const T v[4] = { rgb[0], rgb[1], rgb[2], edge };
+    out.store(X, Y, v, 4);
+  }
+  return out;
+}
+
+// denoise/down.comp:59-108 (level >= 0 branch)
+template<class T> static img_t<T> denoise_down(const img_t<T> &in, int wd, int ht, const int crop[4],
+    T black_g, T white_g, T na, T nb, const T edges[4], int level, int block_i)
+{
+  img_t<T> out(wd, ht, 4);
+  const T t = T(0.2);
+  const T block = (block_i == 3) ? T(2.23607) : (block_i == 2 ? T(1.414213) : T(1.0));
+  const T offs[4][2] = {
+    { T(0.5) + T(1.2), T(0.5) + T(0.4) }, { T(0.5) - T(1.2), T(0.5) - T(0.4) },
+    { T(0.5) + T(0.4), T(0.5) - T(1.2) }, { T(0.5) - T(0.4), T(0.5) + T(1.2) } };
+  OMP_FOR
+  for(int y = 0; y < ht; y++) for(int x = 0; x < wd; x++)
+  {
+    T rgb[3];
+    for(int k = 0; k < 3; k++) rgb[k] = fetch_m(in, x + crop[0], y + crop[1], k);
+    T sum[3], wgt[3];
+    for(int k = 0; k < 3; k++) { sum[k] = t * rgb[k]; wgt[k] = t; }
+    T ns[3];
+    noise_sigma(ns, na, nb, black_g, white_g, edges, rgb[0]);
+    const T pl = std::pow(T(0.7), T(level));
+    T wc[3];
+    for(int k = 0; k < 3; k++) { const T sigma = pl * ns[k] / block; wc[k] = T(1) / sigma; }
+    for(int o = 0; o < 4; o++)
+    {
+      T col[4];
+      tex_bilinear(in, T(x + crop[0]) + offs[o][0], T(y + crop[1]) + offs[o][1], col);
+      for(int k = 0; k < 3; k++)
+      {
+        const T g0 = col[k] < T(0) ? col[k] : std::pow(col[k], T(0.8));
+        const T g1 = rgb[k] < T(0) ? rgb[k] : std::pow(rgb[k], T(0.8));
+        const T e = gclamp(T(1) - T(0.5) * (wc[k] * std::fabs(g0 - g1)), T(0), T(1));
+        const T w = e * (T(1) - t) / T(4);
+        sum[k] += w * col[k];
+        wgt[k] += w;
+      }
+    }
+    for(int k = 0; k < 3; k++) rgb[k] = sum[k] / wgt[k];
+    int X = x, Y = y;
+    swz(X, Y, wd, ht);
+    const T v[4] = { rgb[0], rgb[1], rgb[2], T(1) };
+    out.store(X, Y, v, 4);
+  }
+  return out;
+}
+
+// denoise/assemble.comp:151-273
+template<class T> static img_t<T> denoise_assemble(const img_t<T> *s, int wd, int ht, const int crop[4],
+    const T wb[4], const T black[4], const T white[4], T na, T nb, uint32_t filters,
+    T strength, T luma, const T edges[4])
+{
+  img_t<T> out(wd, ht, 4);
+  const m3<T> rgb_to_yuv = m3_mul(m3_load<T>(M_rec709_to_yuv), m3_load<T>(M_rec2020_to_rec709));
+  const m3<T> yuv_to_rgb = m3_mul(m3_load<T>(M_rec709_to_rec2020), m3_load<T>(M_yuv_to_rec709));
+  const int szx = s[1].w + 1, szy = s[1].h + 1;
+  OMP_FOR
+  for(int y = 0; y < ht; y++) for(int x = 0; x < wd; x++)
+  {
+    T orig[3], d[5][3];
+    for(int k = 0; k < 3; k++) orig[k] = fetch_z(s[0], x + crop[0], y + crop[1], k);
+    int ex = x, ey = y;
+    for(int k = 0; k < 3; k++) d[0][k] = orig[k];
+    T test;
+    for(int l = 1; l <= 4; l++)
+    {
+      ex = ex / 2 + (ex & 1) * szx / 2;
+      ey = ey / 2 + (ey & 1) * szy / 2;
+      for(int k = 0; k < 3; k++) d[l][k] = fetch_z(s[l], ex, ey, k);
+      if(l == 1) test = fetch_z(s[1], ex, ey, 3);
+    }
+    T sigma[3];
+    noise_sigma(sigma, na, nb, black[1], white[1], edges, gmax(d[2][0], T(0)));
+    const T block = filters == 0u ? T(1.0) : (filters == 9u ? T(2.23607) : T(1.414213));
+    const T b[4] = { T(0.7000) / block, T(0.4900) / block, T(0.3430) / block, T(0.2401) / block };
+    for(int l = 0; l < 4; l++) for(int k = 0; k < 3; k++) d[l][k] = (d[l][k] - d[l + 1][k]) / (sigma[k] * b[l]);
+    T len[4];
+    for(int l = 0; l < 4; l++) len[l] = std::sqrt(d[l][0] * d[l][0] + d[l][1] * d[l][1] + d[l][2] * d[l][2]);
+    const T d0 = len[0], d1 = len[1], d2 = len[2], d3 = len[3];
+    const T slope = ((d3 - d0) / T(3.0) + (d2 - d1) / T(1.0) + (d1 - d0) / T(1.0) + (d3 - d2) / T(1.0) + (d2 - d0) / T(2.0) + (d3 - d1) / T(2.0)) / T(6.0);
+    test = gmax(T(0), -slope);
+    test = gmax(T(0), T(1) - test);
+    test = std::pow(test, T(16));
+    test = gclamp(T(1.5) * test, T(0), T(1));
+    const T thrs0 = std::pow(strength, T(4));
+    const T ht_ = T(10);
+    for(int l = 3; l >= 0; l--)
+    {
+      const T thrs = (std::fabs(d[l][0]) > ht_) ? T(10000) : thrs0;
+      for(int k = 0; k < 3; k++)
+      {
+        const T a = std::fabs(d[l][k]);
+        const T tt = gmin(T(1), a / (T(2) * thrs));
+        d[4][k] += sigma[k] * b[l] * gsign(d[l][k]) * gmix(gmax(a - thrs, T(0)), a, tt);
+      }
+    }
+    T v4[3], vo[3];
+    for(int k = 0; k < 3; k++)
+    {
+      v4[k] = (d[4][k] - black[k]) / (white[k] - black[k]) * wb[k];
+      vo[k] = (orig[k] - black[k]) / (white[k] - black[k]) * wb[k];
+    }
+    T yuv[3], yuvo[3];
+    m3_apply(rgb_to_yuv, v4, yuv);
+    m3_apply(rgb_to_yuv, vo, yuvo);
+    yuv[0] = gmix(yuvo[0], yuv[0], luma);
+    T rgb[3];
+    m3_apply(yuv_to_rgb, yuv, rgb);
+    T o[4];
+    for(int k = 0; k < 3; k++) o[k] = rgb[k] / wb[k] * (white[k] - black[k]) + black[k];
+    o[3] = test;
+    out.store(x, y, o, 4);
+  }
+  return out;
+}
+
+// denoise/doub.comp:35-116 (gain map absent)
+template<class T> static img_t<T> denoise_doub(const img_t<T> &orig, const img_t<T> &crs0, const img_t<T> &crs1,
+    int wd, int ht, const int crop[4], const T black4[4], const T white4[4], uint32_t filters,
+    T na, T nb, T strength, T luma, T detail, const T edges[4])
+{
+  img_t<T> out(wd, ht, 1);
+  OMP_FOR
+  for(int y = 0; y < ht; y++) for(int x = 0; x < wd; x++)
+  {
+    T upsm[4], down[4];
+    const T ux = (T(x) + T(0.5)) / T(wd), uy = (T(y) + T(0.5)) / T(ht);
+    tex_bilinear(crs0, ux * T(crs0.w), uy * T(crs0.h), upsm);
+    tex_bilinear(crs1, ux * T(crs1.w), uy * T(crs1.h), down);
+    T black = black4[1], white = white4[1], crs = upsm[1], crs1v = down[1];
+    T Tt = T(0.5) * strength * upsm[3], blendw = luma;
+    int col;
+    if(filters == 9) col = cfa_xtrans(x, y);
+    else             col = cfa_bayer(x, y);
+    if(col != 1)
+    {
+      black = black4[col]; white = white4[col];
+      crs = upsm[col]; crs1v = down[col]; blendw = T(1);
+      if(filters == 9) Tt /= gmax(T(1e-4), upsm[3]);
+    }
+    T sigma[3];
+    noise_sigma(sigma, na, nb, black, white, edges, crs);
+    T val = fetch_m(orig, x + crop[0], y + crop[1], 0);
+    blendw = T(0.5) * (blendw + T(1));
+    if(val < white)
+    {
+      const T wav = (val - crs1v) / gmax(sigma[0] + sigma[2], T(1e-8));
+      const T tt = gmin(T(1), wav / gmax(T(2) * Tt, T(1e-8)));
+      T uw = std::pow(gmin(T(1), T(1) * upsm[3]), T(4));
+      uw = T(1) - (T(1) - uw) * detail;
+      const T aw = std::fabs(wav);
+      val = gmix(val, gmax(T(0), crs + sigma[1] * gsign(wav) * gmix(gmax(T(0), aw - Tt), aw, tt)), uw * blendw);
+    }
+    val = gmax(T(0), (val - black) / (white - black));
+    const T v[1] = { val };
+    out.store(x, y, v, 1);
+  }
+  return out;
+}
+
+// ------------------------------------------------------------------ hilite
+
+// hilite/half.comp:21-72
+template<class T> static img_t<T> hilite_half(const img_t<T> &in, int wd, int ht, T white, uint32_t filters)
+{
+  img_t<T> out(wd, ht, 4);
+  OMP_FOR
+  for(int y = 0; y < ht; y++) for(int x = 0; x < wd; x++)
+  {
+    T rgba[4];
+    if(filters == 9)
+    {
+      T c[9];
+      for(int i = 0; i < 3; i++) for(int j = 0; j < 3; j++) c[3 * i + j] = fetch_z(in, 3 * x + i, 3 * y + j, 0);
+      if(c[1] >= white) c[1] = c[7];
+      if(c[7] >= white) c[7] = c[1];
+      if(c[3] >= white) c[3] = c[5];
+      if(c[5] >= white) c[5] = c[3];
+      const T maxg = gmax(gmax(gmax(c[0], c[2]), c[4]), gmax(c[6], c[8]));
+      if(maxg >= white) c[0] = c[2] = c[4] = c[6] = c[8] = T(1);
+      const T c0 = (c[1] + c[7]) * T(0.5), c1 = (c[3] + c[5]) * T(0.5);
+      if(((x + y) & 1) > 0) { rgba[0] = c0; rgba[2] = c1; }
+      else                  { rgba[2] = c0; rgba[0] = c1; }
+      rgba[1] = (c[0] + c[2] + c[4] + c[6] + c[8]) / T(5.0);
+      rgba[3] = T(1);
+    }
+    else
+    {
+      T cx = fetch_m(in, 2 * x, 2 * y + 1, 0), cy = fetch_m(in, 2 * x + 1, 2 * y + 1, 0);
+      T cz = fetch_m(in, 2 * x + 1, 2 * y, 0), cw = fetch_m(in, 2 * x, 2 * y, 0);
+      if(cx >= white) cx = cz;
+      if(cz >= white) cz = cx;
+      rgba[0] = cw; rgba[1] = (cx + cz) / T(2); rgba[2] = cy; rgba[3] = T(1);
+    }
+    out.store(x, y, rgba, 4);
+  }
+  return out;
+}
+
+// hilite/reduce.comp:21-61
+template<class T> static img_t<T> hilite_reduce(const img_t<T> &in, int wd, int ht, const T wb4[4], T white_p, T desat)
+{
+  img_t<T> out(wd, ht, 4);
+  T white = white_p;
+  if(!(white > T(0))) white = T(1);
+  const T w[5] = { T(1.0) / T(16.0), T(4.0) / T(16.0), T(6.0) / T(16.0), T(4.0) / T(16.0), T(1.0) / T(16.0) };
+  const T sw[5] = { T(1), T(2), T(0), T(-2), T(-1) };
+  T wb[3] = { wb4[0], wb4[1], wb4[2] };
+  if(!(wb[0] * wb[0] + wb[1] * wb[1] + wb[2] * wb[2] > T(1e-3))) wb[0] = wb[1] = wb[2] = T(1);
+  OMP_FOR
+  for(int y = 0; y < ht; y++) for(int x = 0; x < wd; x++)
+  {
+    T edge[2] = {0, 0}, col[3] = {0, 0, 0}, wgt = 0;
+    for(int jj = -2; jj <= 2; jj++) for(int ii = -2; ii <= 2; ii++)
+    {
+      T rgb[3];
+      for(int k = 0; k < 3; k++) rgb[k] = fetch_m(in, 2 * x + ii, 2 * y + jj, k);
+      const T l = lum2020(rgb[0], rgb[1], rgb[2]);
+      edge[0] += w[jj + 2] * sw[ii + 2] * l;
+      edge[1] += w[ii + 2] * sw[jj + 2] * l;
+      const T u = w[ii + 2] * w[jj + 2];
+      const T rw = rgb[0] * wb[0], gw = rgb[1] * wb[1], bw = rgb[2] * wb[2];
+      const T cmax = gmax(rw, gmax(gw, bw));
+      const T cmin = gmin(rw, gmin(gw, bw));
+      const T sat = (cmax - cmin) / gmax(T(1e-3), cmax);
+      if(rgb[0] < white && rgb[1] < white && rgb[2] < white)
+      {
+        const T s = smoothstep(T(0.2), T(1.0), gmax(rgb[0], gmax(rgb[1], rgb[2])) / white);
+        T t = smoothstep(T(0.15), T(0.9), sat);
+        const T ds = desat * desat;
+        t = gclamp(T(5) * ds * ds * s * t, T(0), T(1));
+        for(int k = 0; k < 3; k++)
+        {
+          rgb[k] = gmix(rgb[k], (cmax + cmin) / wb[k] * T(0.5), t);
+          col[k] += rgb[k] * u;
+        }
+        wgt += u;
+      }
+    }
+    T o[4];
+    if(wgt == T(0)) { o[0] = o[1] = o[2] = T(1); }
+    else for(int k = 0; k < 3; k++) o[k] = col[k] / wgt;
+    o[3] = std::sqrt(edge[0] * edge[0] + edge[1] * edge[1]);
+    out.store(x, y, o, 4);
+  }
+  return out;
+}
+
+// hilite/assemble.comp:23-81 gauss_expand
+template<class T> static void hilite_expand(const img_t<T> &im, int ox, int oy, T c[3])
+{
+  const T w[5] = { T(1.0) / T(16.0), T(4.0) / T(16.0), T(6.0) / T(16.0), T(4.0) / T(16.0), T(1.0) / T(16.0) };
+  c[0] = c[1] = c[2] = T(0);
+  T wgt = T(0);
+  const int ix = ox / 2, iy = oy / 2;
+  const int d = (ox & 1) + 2 * (oy & 1);
+  const int i0 = (d & 1) ? 0 : -1, j0 = (d & 2) ? 0 : -1;
+  for(int ii = i0; ii <= 1; ii++) for(int jj = j0; jj <= 1; jj++)
+  {
+    const T wy = (d & 2) ? w[2 * jj + 1] : w[2 * jj + 2];
+    const T wx = (d & 1) ? w[2 * ii + 1] : w[2 * ii + 2];
+    for(int k = 0; k < 3; k++) c[k] += fetch_m(im, ix + ii, iy + jj, k) * wy * wx;
+    wgt += wy * wx;
+  }
+  if(wgt == T(0)) { c[0] = 0; c[1] = 1; c[2] = 1; return; }
+  for(int k = 0; k < 3; k++) c[k] /= wgt;
+}
+
+// hilite/assemble.comp:83-119
+template<class T> static img_t<T> hilite_assemble(const img_t<T> &fine, const img_t<T> &coarse, int wd, int ht, T white, T soft)
+{
+  img_t<T> out(wd, ht, 4);
+  OMP_FOR
+  for(int y = 0; y < ht; y++) for(int x = 0; x < wd; x++)
+  {
+    T upsm[3];
+    hilite_expand(coarse, x, y, upsm);
+    T f[4];
+    for(int k = 0; k < 4; k++) f[k] = fetch_z(fine, x, y, k);
+    const T sr = f[0] / gmax(T(0.001), upsm[0]);
+    const T sg = f[1] / gmax(T(0.001), upsm[1]);
+    const T sb = f[2] / gmax(T(0.001), upsm[2]);
+    const T wr = std::exp(upsm[0] - gmax(upsm[1], upsm[2]));
+    const T wg = std::exp(upsm[1] - gmax(upsm[0], upsm[2]));
+    const T wbb = std::exp(upsm[2] - gmax(upsm[0], upsm[1]));
+    const T scale = (sr * wr + sg * wg + sb * wbb) / (wr + wg + wbb);
+    T rec[3];
+    for(int k = 0; k < 3; k++) rec[k] = gclamp(upsm[k] * scale, T(-65535.0), T(65535.0));
+    T t = soft;
+    if(f[0] >= white || f[1] >= white || f[2] >= white) t = T(1);
+    if(std::isnan(f[3])) f[3] = T(0);
+    t = gclamp(gmix(t, T(1), std::sqrt(gmax(T(0), f[3]))), T(0), T(1));
+    T o[4];
+    for(int k = 0; k < 3; k++) o[k] = gmix(f[k], rec[k], t);
+    o[3] = T(1);
+    out.store(x, y, o, 4);
+  }
+  return out;
+}
+
+// hilite/doub.comp:141-241. out is the full mosaic.
+template<class T> static void hilite_doub(const img_t<T> &in, const img_t<T> &coarse, int wd, int ht, T white,
+    uint32_t filters, img_t<T> &out)
+{
+  OMP_FOR
+  for(int y = 0; y < ht; y++) for(int x = 0; x < wd; x++)
+  {
+    T up[3];
+    for(int k = 0; k < 3; k++) up[k] = fetch_z(coarse, x, y, k);
+    if(filters == 9)
+    {
+      if(((x + y) & 1) == 0) std::swap(up[0], up[2]);
+      T c[9];
+      for(int i = 0; i < 3; i++) for(int j = 0; j < 3; j++) c[3 * i + j] = fetch_z(in, 3 * x + i, 3 * y + j, 0);
+      const T minr = gmin(c[1], c[7]), minb = gmin(c[3], c[5]);
+      const T ming = gmin(gmin(gmin(c[0], c[2]), c[4]), gmin(c[6], c[8]));
+      const T sr = minr / gmax(T(0.001), up[0]);
+      const T sg = ming / gmax(T(0.001), up[1]);
+      const T sb = minb / gmax(T(0.001), up[2]);
+      const T wr = std::exp(up[0] - gmax(up[1], up[2]));
+      const T wg = std::exp(up[1] - gmax(up[0], up[2]));
+      const T wbb = std::exp(up[2] - gmax(up[0], up[1]));
+      const T scale = (sr * wr + sg * wg + sb * wbb) / (wr + wg + wbb);
+      const T maxr = gmax(c[1], c[7]), maxb = gmax(c[3], c[5]);
+      const T maxg = gmax(gmax(gmax(c[0], c[2]), c[4]), gmax(c[6], c[8]));
+      const T softw = T(0.97) * white;
+      const T maxrgb = gmax(maxr, gmax(maxg, maxb));
+      if(maxrgb > softw)
+      {
+        T t = smoothstep(softw, white, maxrgb);
+        c[1] = gmix(c[1], up[0] * scale, t);
+        c[7] = gmix(c[7], up[0] * scale, t);
+        c[3] = gmix(c[3], up[2] * scale, t);
+        c[5] = gmix(c[5], up[2] * scale, t);
+        t = smoothstep(softw, white, ming);
+        c[0] = gmix(c[0], up[1] * scale, t);
+        c[2] = gmix(c[2], up[1] * scale, t);
+        c[4] = gmix(c[4], up[1] * scale, t);
+        c[6] = gmix(c[6], up[1] * scale, t);
+        c[8] = gmix(c[8], up[1] * scale, t);
+      }
+      for(int i = 0; i < 3; i++) for(int j = 0; j < 3; j++)
+      {
+        const int X = 3 * x + i, Y = 3 * y + j;
+        if(X < out.w && Y < out.h) { const T v[1] = { c[3 * i + j] }; out.store(X, Y, v, 1); }
+      }
+    }
+    else
+    {
+      T cx = fetch_m(in, 2 * x, 2 * y + 1, 0), cy = fetch_m(in, 2 * x + 1, 2 * y + 1, 0);
+      T cz = fetch_m(in, 2 * x + 1, 2 * y, 0), cw = fetch_m(in, 2 * x, 2 * y, 0);
+      const T ming = gmin(cx, cz);
+      const T sr = cw / gmax(T(0.001), up[0]);
+      const T sg = ming / gmax(T(0.001), up[1]);
+      const T sb = cy / gmax(T(0.001), up[2]);
+      const T wr = std::exp(up[0] - gmax(up[1], up[2]));
+      const T wg = std::exp(up[1] - gmax(up[0], up[2]));
+      const T wbb = std::exp(up[2] - gmax(up[0], up[1]));
+      const T scale = (sr * wr + sg * wg + sb * wbb) / (wr + wg + wbb);
+      const T softw = T(0.97) * white;
+      const T maxrgb = gmax(gmax(cx, cy), gmax(cz, cw));
+      if(maxrgb > softw)
+      {
+        const T t = smoothstep(softw, white, maxrgb);
+        cx = gmix(cx, scale * up[1], t);
+        cy = gmix(cy, scale * up[2], t);
+        cz = gmix(cz, scale * up[1], t);
+        cw = gmix(cw, scale * up[0], t);
+      }
+      const T vw[1] = { cw }, vz[1] = { cz }, vx[1] = { cx }, vy[1] = { cy };
+      if(2 * x < out.w && 2 * y < out.h) out.store(2 * x, 2 * y, vw, 1);
+      if(2 * x + 1 < out.w && 2 * y < out.h) out.store(2 * x + 1, 2 * y, vz, 1);
+      if(2 * x < out.w && 2 * y + 1 < out.h) out.store(2 * x, 2 * y + 1, vx, 1);
+      if(2 * x + 1 < out.w && 2 * y + 1 < out.h) out.store(2 * x + 1, 2 * y + 1, vy, 1);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ demosaic
+
+// demosaic/gauss.comp:19-126
+template<class T> static img_t<T> demosaic_gauss(const img_t<T> &orig, int wd, int ht, uint32_t filters)
+{
+  img_t<T> out(wd, ht, 4);
+  const int blk = filters == 9 ? 3 : 2;
+  const int j0 = filters == 9 ? 0 : -1, j1 = filters == 9 ? 3 : 3;
+  OMP_FOR
+  for(int y = 0; y < ht; y++) for(int x = 0; x < wd; x++)
+  {
+    T mw[2] = {0, 0}, mb[2] = {0, 0}, smw = 0, smb = 0;
+    T Sw00 = 0, Sw01 = 0, Sw10 = 0, Sw11 = 0, Sb00 = 0, Sb01 = 0, Sb10 = 0, Sb11 = 0, sw = 0, sb = 0;
+    auto skip = [&](int i, int j) { return filters == 9 ? (((j + i) & 1) == 1) : (((j + i) & 1) != 1); };
+    for(int j = j0; j < j1; j++) for(int i = j0; i < j1; i++)
+    {
+      if(skip(i, j)) continue;
+      const T px = fetch_m(orig, blk * x + i, blk * y + j, 0);
+      mw[0] += T(i) * px; mw[1] += T(j) * px;
+      smw += px;
+      mb[0] += T(i) / px; mb[1] += T(j) / px;
+      smb += T(1) / px;
+    }
+    mw[0] /= smw; mw[1] /= smw;
+    mb[0] /= smb; mb[1] /= smb;
+    for(int j = j0; j < j1; j++) for(int i = j0; i < j1; i++)
+    {
+      if(skip(i, j)) continue;
+      const T px = fetch_m(orig, blk * x + i, blk * y + j, 0);
+      T p2 = px * px;
+      T p[2] = { T(i) - mw[0], T(j) - mw[1] };
+      Sw00 += p2 * p[0] * p[0]; Sw01 += p2 * p[0] * p[1]; Sw10 += p2 * p[1] * p[0]; Sw11 += p2 * p[1] * p[1];
+      sw += p2;
+      p[0] = T(i) - mb[0]; p[1] = T(j) - mb[1];
+      p2 = T(1) / p2;
+      Sb00 += p2 * p[0] * p[0]; Sb01 += p2 * p[0] * p[1]; Sb10 += p2 * p[1] * p[0]; Sb11 += p2 * p[1] * p[1];
+      sb += p2;
+    }
+    Sw00 /= sw; Sw01 /= sw; Sw10 /= sw; Sw11 /= sw;
+    Sb00 /= sb; Sb01 /= sb; Sb10 /= sb; Sb11 /= sb;
+    const T detw = Sw00 * Sw11 - Sw10 * Sw01, detb = Sb00 * Sb11 - Sb10 * Sb01;
+    T eval[2], evec0[2], evec1[2];
+    if(detw < detb) evd2x2(eval, evec0, evec1, Sw00, Sw10, Sw11);
+    else            evd2x2(eval, evec0, evec1, Sb00, Sb10, Sb11);
+    if(filters != 9)
+    {
+      eval[0] *= T(0.2); eval[1] *= T(0.2);
+      if(std::fabs(evec0[0]) > std::fabs(evec0[1])) { evec0[0] = 1; evec0[1] = 0; }
+      else                                          { evec0[0] = 0; evec0[1] = 1; }
+    }
+    else
+    {
+      eval[0] *= T(0.4); eval[1] *= T(0.4);
+      if(std::fabs(evec0[0]) > T(2) * std::fabs(evec0[1]))      { evec0[0] = 1; evec0[1] = 0; }
+      else if(std::fabs(evec0[1]) > T(2) * std::fabs(evec0[0])) { evec0[0] = 0; evec0[1] = 1; }
+      else { eval[0] = T(0.1); eval[1] = T(0.1); }
+    }
+    const T v[4] = { eval[0], eval[1], evec0[0], evec0[1] };
+    out.store(x, y, v, 4);
+  }
+  return out;
+}
+
+// demosaic/splat.comp:142-266
+template<class T> static img_t<T> demosaic_splat(const img_t<T> &in, const img_t<T> &gauss, int wd, int ht, uint32_t filters)
+{
+  img_t<T> out(wd, ht, 1);
+  const int r = filters == 9 ? 2 : 1;
+  OMP_FOR
+  for(int y = 0; y < ht; y++) for(int x = 0; x < wd; x++)
+  {
+    T cov[4];
+    for(int k = 0; k < 4; k++)
+      cov[k] = filters == 9 ? fetch_z(gauss, x / 3, y / 3, k) : fetch_z(gauss, (x + 1) / 2, (y + 1) / 2, k);
+    T rgb[3] = {0, 0, 0}, w[3] = {0, 0, 0};
+    for(int j = -r; j <= r; j++) for(int i = -r; i <= r; i++)
+    {
+      int px = x + i, py = y + j;
+      if(px < 0) px += 6;
+      if(py < 0) py += 6;
+      if(px >= in.w) px -= 6;
+      if(py >= in.h) py -= 6;
+      const T col = fetch_z(in, px, py, 0);
+      const T e0 = gclamp(cov[0], T(0.01), T(25)), e1 = gclamp(cov[1], T(0.01), T(25));
+      const T of0 = cov[2] * T(i) + cov[3] * T(j);
+      const T of1 = -cov[3] * T(i) + cov[2] * T(j);
+      T weight = gclamp(std::exp(T(-0.5) * (of0 / e0 * of0 + of1 / e1 * of1)), T(1e-4), T(1.0));
+      if(i == 0 && j == 0) weight = T(666.0);
+      int c;
+      if(filters == 9) c = cfa_xtrans(x + i + 6, y + j + 6);
+      else             c = cfa_bayer(x + i, y + j);
+      if(filters == 9) rgb[c] += col * weight;
+      else             rgb[c] += col * weight;
+      w[c] += weight;
+    }
+    const T g = rgb[1] / gmax(T(1e-8), w[1]);
+    const T v[1] = { g };
+    out.store(x, y, v, 1);
+  }
+  return out;
+}
+
+// demosaic/fix.comp:21-135
+template<class T> static img_t<T> demosaic_fix(const img_t<T> &in, const img_t<T> &g, const img_t<T> &cov_img,
+    int wd, int ht, uint32_t filters, int fixup)
+{
+  img_t<T> out(wd, ht, 4);
+  OMP_FOR
+  for(int y = 0; y < ht; y++) for(int x = 0; x < wd; x++)
+  {
+    T rgb[3] = {0, 0, 0}, w[3] = {0, 0, 0};
+    const T gc = fetch_m(g, x, y, 0);
+    T cov[4];
+    int r;
+    T scale;
+    if(filters == 9)
+    {
+      for(int k = 0; k < 4; k++) cov[k] = fetch_z(cov_img, (x + 1) / 3, (y + 1) / 3, k);
+      cov[0] = gclamp(cov[0], T(1.), T(10.)); cov[1] = gclamp(cov[1], T(1.), T(10.));
+      r = std::min(std::max(fixup + 2, 2), 3);
+      scale = T(3);
+    }
+    else
+    {
+      for(int k = 0; k < 4; k++) cov[k] = fetch_z(cov_img, (x + 1) / 2, (y + 1) / 2, k);
+      cov[0] = gclamp(cov[0], T(1.0), T(49)); cov[1] = gclamp(cov[1], T(1.0), T(49));
+      r = std::min(std::max(fixup + 1, 1), 2);
+      scale = T(2);
+    }
+    for(int j = -r; j <= r; j++) for(int i = -r; i <= r; i++)
+    {
+      const T gh = fetch_m(g, x + i, y + j, 0);
+      const T col = fetch_m(in, x + i, y + j, 0);
+      int c;
+      if(filters == 9)
+      { // write_xtrans2: the pattern is evaluated on the unshifted position
+        const int px = x + i, py = y + j;
+        const bool blue_top = ((px / 3 + py / 3) & 1) > 0;
+        const int qx = px - (px / 3) * 3, qy = py - (py / 3) * 3;
+        if(((qx + qy) & 1) == 0) c = 1;
+        else if(blue_top ^ (qy == 1)) c = 2;
+        else c = 0;
+      }
+      else c = cfa_bayer(x + i, y + j);
+      if(c == 1) { rgb[1] = gc; w[1] = T(1); continue; }
+      // eval_gauss(vec4(scale*cov.xy, cov.zw), (i,j))
+      const T e0 = scale * cov[0], e1 = scale * cov[1];
+      const T of0 = cov[2] * T(i) + cov[3] * T(j);
+      const T of1 = -cov[3] * T(i) + cov[2] * T(j);
+      const T weight = gclamp(std::exp(T(-0.5) * (of0 / e0 * of0 + of1 / e1 * of1)), T(1e-3), T(1.0));
+      if(filters == 9)
+      {
+        const T corr = (T(1e-4) + gc) / (T(1e-4) + gh);
+        rgb[c] += col * corr * weight;
+      }
+      else rgb[c] += col * (T(1e-4) + gc) / (T(1e-4) + gh) * weight;
+      w[c] += weight;
+    }
+    T o[4];
+    for(int k = 0; k < 3; k++) o[k] = rgb[k] / gmax(T(1e-8), w[k]);
+    o[3] = T(1);
+    out.store(x, y, o, 4);
+  }
+  return out;
+}
+
+// demosaic/halfsize.comp:155-187
+template<class T> static img_t<T> demosaic_halfsize(const img_t<T> &in, int wd, int ht, uint32_t filters)
+{
+  img_t<T> out(wd, ht, 4);
+  OMP_FOR
+  for(int y = 0; y < ht; y++) for(int x = 0; x < wd; x++)
+  {
+    T rgba[4];
+    if(filters == 9)
+    {
+      T c[9];
+      for(int i = 0; i < 3; i++) for(int j = 0; j < 3; j++) c[3 * i + j] = fetch_z(in, 3 * x + i, 3 * y + j, 0);
+      rgba[1] = (c[0] + c[2] + c[4] + c[6] + c[8]) * T(1.0) / T(5.0);
+      const T c0 = (c[1] + c[7]) * T(0.5), c1 = (c[3] + c[5]) * T(.5);
+      if(((x + y) & 1) > 0) { rgba[0] = c0; rgba[2] = c1; }
+      else                  { rgba[2] = c0; rgba[0] = c1; }
+      rgba[3] = T(1); // not written by the shader: the f16 target holds whatever, use 1
+    }
+    else
+    {
+      const T cx = fetch_m(in, 2 * x, 2 * y + 1, 0), cy = fetch_m(in, 2 * x + 1, 2 * y + 1, 0);
+      const T cz = fetch_m(in, 2 * x + 1, 2 * y, 0), cw = fetch_m(in, 2 * x, 2 * y, 0);
+      rgba[0] = cw; rgba[1] = (cx + cz) / T(2); rgba[2] = cy; rgba[3] = T(1);
+    }
+    out.store(x, y, rgba, 4);
+  }
+  return out;
+}
+
+// shared/resample.comp:213-224 with shared.glsl:47-96 sample_catmull_rom
+template<class T> static img_t<T> shared_resample(const img_t<T> &in, int wd, int ht)
+{
+  img_t<T> out(wd, ht, 4);
+  OMP_FOR
+  for(int y = 0; y < ht; y++) for(int x = 0; x < wd; x++)
+  {
+    const T sp[2] = { (T(x) + T(0.5)) / T(wd) * T(in.w), (T(y) + T(0.5)) / T(ht) * T(in.h) };
+    T t0[2], t12[2], t3[2], w0[2], w12[2], w3[2];
+    for(int k = 0; k < 2; k++)
+    {
+      const T tp1 = std::floor(sp[k] - T(0.5)) + T(0.5);
+      const T f = sp[k] - tp1;
+      w0[k] = f * (T(-0.5) + f * (T(1.0) - T(0.5) * f));
+      const T w1 = T(1.0) + f * f * (T(-2.5) + T(1.5) * f);
+      const T w2 = f * (T(0.5) + f * (T(2.0) - T(1.5) * f));
+      w3[k] = f * f * (T(-0.5) + T(0.5) * f);
+      w12[k] = w1 + w2;
+      const T off12 = w2 / (w1 + w2);
+      t0[k] = tp1 - T(1.0); t3[k] = tp1 + T(2.0); t12[k] = tp1 + off12;
+    }
+    const T *tx[3] = { &t0[0], &t12[0], &t3[0] }, *ty[3] = { &t0[1], &t12[1], &t3[1] };
+    const T wx[3] = { w0[0], w12[0], w3[0] }, wy[3] = { w0[1], w12[1], w3[1] };
+    T res[4] = {0, 0, 0, 0};
+    for(int j = 0; j < 3; j++) for(int i = 0; i < 3; i++)
+    {
+      T v[4];
+      tex_bilinear(in, *tx[i], *ty[j], v);
+      for(int k = 0; k < 4; k++) res[k] += v[k] * wx[i] * wy[j];
+    }
+    out.store(x, y, res, 4);
+  }
+  return out;
+}
+
+// ------------------------------------------------------------------ colour
+
+// colour/main.c:219-292 commit_params (matrix path) + main-impl.glsl:200-341
+template<class T> static img_t<T> colour_main(const img_t<T> &in, const oracle_img_param_t *ip, const oracle_params_t *p)
+{
+  // host side: p_wb from the camera coefficients when white = 0 (main.c:241-253)
+  float p_wb[3] = { p->co_white[0], p->co_white[1], p->co_white[2] };
+  if(p_wb[0] == 0.0f && p_wb[1] == 0.0f && p_wb[2] == 0.0f)
+  {
+    float w0[3] = {0}, w[] = { ip->whitebalance[0], ip->whitebalance[1], ip->whitebalance[2] };
+    for(int j = 0; j < 3; j++) for(int i = 0; i < 3; i++) w0[j] += ip->cam_to_rec2020[3 * j + i] / w[i];
+    w0[0] /= w0[1]; w0[2] /= w0[1]; w0[1] = 1.0f;
+    p_wb[0] = 1 / w0[0]; p_wb[1] = 1; p_wb[2] = 1 / w0[2];
+  }
+  if(!(p_wb[0] == p_wb[0]) || p_wb[0] == 0.0f || p_wb[1] == 0.0f || p_wb[2] == 0.0f)
+    p_wb[0] = p_wb[1] = p_wb[2] = 1.0f;
+  const float mulf[4] = { p_wb[0] / p_wb[1], 1.0f, p_wb[2] / p_wb[1], powf(2.0f, p->co_exposure) };
+  m3<T> cam;
+  if(p->co_matrix == 1) for(int i = 0; i < 9; i++) cam.m[i] = T(ip->cam_to_rec2020[i]);
+  else for(int i = 0; i < 9; i++) cam.m[i] = T(i % 4 == 0 ? 1 : 0);
+  // cat16(rgb, vec3(1), mul.rgb): the matrix products fold at compile time
+  const m3<T> P = m3_mul(m3_load<T>(M_cat16_M), m3_load<T>(M_rec2020_to_xyz));
+  const m3<T> Q = m3_mul(m3_load<T>(M_xyz_to_rec2020), m3_load<T>(M_cat16_Mi));
+  const T one[3] = { 1, 1, 1 }, mul3[3] = { T(mulf[0]), T(mulf[1]), T(mulf[2]) };
+  T cl_src[3], cl_dst[3];
+  m3_apply(P, one, cl_src);
+  m3_apply(P, mul3, cl_dst);
+  img_t<T> out(in.w, in.h, 4);
+  OMP_FOR
+  for(int y = 0; y < in.h; y++) for(int x = 0; x < in.w; x++)
+  {
+    T rgb[3];
+    for(int k = 0; k < 3; k++) rgb[k] = fetch_m(in, x, y, k);
+    m3_apply(cam, rgb, rgb);           // decode_colour: primaries custom, trc linear
+    T cl[3];
+    m3_apply(P, rgb, cl);
+    for(int k = 0; k < 3; k++) cl[k] *= cl_dst[k] / cl_src[k];
+    m3_apply(Q, cl, rgb);
+    T o[4];
+    for(int k = 0; k < 3; k++) o[k] = gclamp(rgb[k] * T(mulf[3]), T(-65535.0), T(65535.0));
+    o[3] = T(1);
+    out.store(x, y, o, 4);
+  }
+  return out;
+}
+
+// ------------------------------------------------------------------ filmcurv
+
+template<class T> static inline T weibull_cdf(T x, T il, T k)
+{ // filmcurv/params.glsl:15-34
+  return T(1.0) - std::exp(-std::pow(gmax(x, T(1e-7)) * il, k));
+}
+
+// shared.glsl:371-387 adjust_colour_dng
+template<class T> static void adjust_colour_dng(T c0[3], T c1[3])
+{
+  bool fx = false, fy = false, fz = false;
+  if(c0[2] > c0[1]) { std::swap(c0[2], c0[1]); std::swap(c1[2], c1[1]); fx = true; }
+  if(c0[1] > c0[0]) { std::swap(c0[0], c0[1]); std::swap(c1[0], c1[1]); fy = true; }
+  if(c0[2] > c0[1]) { std::swap(c0[2], c0[1]); std::swap(c1[2], c1[1]); fz = true; }
+  c1[1] = gmix(c1[2], c1[0], (c0[1] - c0[2] + T(1e-6)) / (c0[0] - c0[2] + T(1e-6)));
+  if(fz) std::swap(c1[2], c1[1]);
+  if(fy) std::swap(c1[0], c1[1]);
+  if(fx) std::swap(c1[2], c1[1]);
+}
+
+// filmcurv/main.comp:106-205 (colour modes 1 and 3)
+template<class T> static img_t<T> filmcurv_main(const img_t<T> &in, const oracle_params_t *p)
+{
+  img_t<T> out(in.w, in.h, 4);
+  const T il = gmax(T(5e-3), T(p->fc_light));
+  const T k = gmax(T(1e-4), T(p->fc_contrast));
+  OMP_FOR
+  for(int y = 0; y < in.h; y++) for(int x = 0; x < in.w; x++)
+  {
+    T c0[3], c1[3];
+    for(int j = 0; j < 3; j++) c0[j] = fetch_z(in, x, y, j) + T(p->fc_bias);
+    for(int j = 0; j < 3; j++) c1[j] = weibull_cdf(c0[j], il, k);
+    if(p->fc_colour == 3) adjust_colour_dng(c0, c1);  // mode 1: per channel curve
+    const T o[4] = { c1[0], c1[1], c1[2], T(1) };
+    out.store(x, y, o, 4);
+  }
+  return out;
+}
+
+// ------------------------------------------------------------------ histogram
+
+// natural logarithm used by the histogram bin index. the reference calls the
+// GPU's log(); bin counts are integer results and must agree bit for bit
+// between this oracle and the kernel, so both evaluate the same published
+// method with the same operation order and no contraction:
+// x = 2^e * m with m in [sqrt(1/2), sqrt(2)), s = (m-1)/(m+1),
+// log(m) = 2 atanh(s) = 2 (s + s^3/3 + s^5/5 + ... + s^13/13) (series of the
+// inverse hyperbolic tangent, cf. Cody & Waite, "Software manual for the
+// elementary functions", 1980, ch. 5), log(x) = e ln2 + log(m).
+static float hist_log(float x)
+{
+  if(!(x > 0.0f)) return x == 0.0f ? -INFINITY : NAN;
+  if(x == INFINITY) return INFINITY;
+  uint32_t u; memcpy(&u, &x, 4);
+  int e = (int)((u >> 23) & 0xff);
+  if(e == 0) { x *= 8388608.0f; memcpy(&u, &x, 4); e = (int)((u >> 23) & 0xff) - 23; }
+  e -= 127;
+  u = (u & 0x007fffffu) | 0x3f800000u;
+  float m; memcpy(&m, &u, 4);
+  if(m > 1.41421356f) { m *= 0.5f; e += 1; }
+  volatile float num = m - 1.0f, den = m + 1.0f;
+  const float s = num / den;
+  const float s2 = s * s;
+  float poly = 1.0f / 13.0f;
+  poly = poly * s2; poly = poly + 1.0f / 11.0f;
+  poly = poly * s2; poly = poly + 1.0f / 9.0f;
+  poly = poly * s2; poly = poly + 1.0f / 7.0f;
+  poly = poly * s2; poly = poly + 1.0f / 5.0f;
+  poly = poly * s2; poly = poly + 1.0f / 3.0f;
+  poly = poly * s2; poly = poly + 1.0f;
+  const float lm = 2.0f * s * poly;
+  const float fe = (float)e;
+  const float hi = fe * 0.693145752f;       // ln2 split: hi part exact in 16 bits
+  const float lo = fe * 1.42860677e-06f;    // ln2 - hi
+  return (hi + (lo + lm));
+}
+
+} // namespace
+
+extern "C" uint32_t oracle_hist_bin(float r, float g, float b)
+{ // OpenDRT/hist.comp:15-20 get_bin, shared/oetf.glsl:13-15 eotf_filmlight_tlog
+  const float p0 = 2.62700212e-01f * r, p1 = 6.77998072e-01f * g, p2 = 5.93017165e-02f * b;
+  const float v = (p0 + p1) + p2;
+  float l;
+  if(v < 0.0f) { const float t = v * 16.184376489665897f; l = t + 0.075f; }
+  else
+  {
+    const float a = v + 0.0057048244042473785f;
+    const float t = hist_log(a) * 0.09232902596577353f;
+    l = t + 0.5520126568606655f;
+  }
+  const float f = 256.0f * l;
+  const float fb = f + 0.5f;
+  uint32_t bin;
+  if(!(fb > 0.0f)) bin = 0;                 // negative and NaN saturate to 0
+  else if(fb >= 4294967295.0f) bin = 0xffffffffu;
+  else bin = (uint32_t)fb;
+  return bin > 255u ? 255u : bin;
+}
+
+namespace {
+
+template<class T> static void hist(const img_t<T> &in, uint32_t *h)
+{
+  for(int i = 0; i < 257; i++) h[i] = 0;
+  for(int y = 0; y < in.h; y++) for(int x = 0; x < in.w; x++)
+  {
+    const uint32_t bin = oracle_hist_bin((float)fetch_z(in, x, y, 0), (float)fetch_z(in, x, y, 1), (float)fetch_z(in, x, y, 2));
+    if(bin > 0) { h[bin]++; h[256]++; }
+  }
+}
+
+// ------------------------------------------------------------------ llap
+
+static const int NUM_GAMMA = 10; // llap/config.h:2
+
+template<class T> static inline T gamma_from_i(int i)
+{ // llap/llap.glsl:3-14
+  return T(i) / (T(NUM_GAMMA) - T(1.0));
+}
+template<class T> static inline int gamma_hi_from_v(T v)
+{ // llap/llap.glsl:16-21
+  int hi = 1;
+  for(; hi < NUM_GAMMA - 1 && gamma_from_i<T>(hi) <= v; hi++);
+  return hi;
+}
+
+// llap/curve.comp:39-63
+template<class T> static inline T llap_curve_fn(T x, T g, T sigma, T shadows, T highlights, T clarity)
+{
+  const T c = x - g;
+  T val;
+  const T ssigma = c > T(0) ? sigma : -sigma;
+  const T shadhi = c > T(0) ? shadows : highlights;
+  if(std::fabs(c) > T(2) * sigma) val = g + ssigma + shadhi * (c - ssigma);
+  else
+  {
+    const T t = gclamp(c / (T(2.0) * ssigma), T(0.0), T(1.0));
+    const T t2 = t * t;
+    const T mt = T(1.0) - t;
+    val = g + ssigma * T(2.0) * mt * t + t2 * (ssigma + ssigma * shadhi);
+  }
+  val += clarity * c * std::exp(-c * c / (T(2.0) * sigma * sigma / T(3.0)));
+  return val;
+}
+
+// llap/curve.comp:65-79: 11 planes (NUM_GAMMA curves + grey)
+template<class T> static std::vector<img_t<T>> llap_curve(const img_t<T> &in, const oracle_params_t *p)
+{
+  std::vector<img_t<T>> out(NUM_GAMMA + 1, img_t<T>(in.w, in.h, 1));
+  OMP_FOR
+  for(int y = 0; y < in.h; y++) for(int x = 0; x < in.w; x++)
+  {
+    T rgb[3];
+    for(int k = 0; k < 3; k++) rgb[k] = gclamp(fetch_z(in, x, y, k), T(-1000.0), T(1000.0));
+    const T yv = lum2020(rgb[0], rgb[1], rgb[2]);
+    for(int i = 0; i < NUM_GAMMA; i++)
+    {
+      const T v[1] = { llap_curve_fn(yv, gamma_from_i<T>(i), T(p->ll_sigma), T(p->ll_shadows), T(p->ll_hilights), T(p->ll_clarity)) };
+      out[i].store(x, y, v, 1);
+    }
+    const T v[1] = { yv };
+    out[NUM_GAMMA].store(x, y, v, 1);
+  }
+  return out;
+}
+
+// one bilinear tap at half-texel offsets (texel-space coordinate x of the sampler)
+template<class T> static inline T tap(const img_t<T> &im, T x, T y)
+{
+  T v[4];
+  tex_bilinear(im, x, y, v);
+  return v[0];
+}
+
+// llap/reduce.comp:17-35 with shared.glsl:130-148 sample_semisoft
+template<class T> static img_t<T> llap_reduce(const img_t<T> &in, int wd, int ht)
+{
+  img_t<T> out(wd, ht, 1);
+  OMP_FOR
+  for(int y = 0; y < ht; y++) for(int x = 0; x < wd; x++)
+  {
+    const T cx = T(2 * x) + T(0.5), cy = T(2 * y) + T(0.5);
+    T r = T(0);
+    r += tap(in, cx - T(.5), cy - T(.5));
+    r += tap(in, cx + T(.5), cy - T(.5));
+    r += tap(in, cx - T(.5), cy + T(.5));
+    r += tap(in, cx + T(.5), cy + T(.5));
+    const T v[1] = { r / T(4.0) };
+    out.store(x, y, v, 1);
+  }
+  return out;
+}
+
+// llap/assemble.comp:54-58 gauss_expand via shared.glsl:99-127 sample_soft
+template<class T> static inline T llap_expand(const img_t<T> &im, int ox, int oy)
+{
+  const T sx = T(ox) * T(0.5) + T(0.5), sy = T(oy) * T(0.5) + T(0.5);
+  const T tx[3] = { sx - T(1.5), sx, sx + T(1.5) }, ty[3] = { sy - T(1.5), sy, sy + T(1.5) };
+  T r = T(0);
+  for(int j = 0; j < 3; j++) for(int i = 0; i < 3; i++) r += tap(im, tx[i], ty[j]);
+  return r / T(9.0);
+}
+
+// llap/assemble.comp:89-123
+template<class T> static img_t<T> llap_assemble(const img_t<T> &coarse, const std::vector<img_t<T>> &l0,
+    const std::vector<img_t<T>> &l1, int first, int wd, int ht)
+{
+  img_t<T> out(wd, ht, 1);
+  OMP_FOR
+  for(int y = 0; y < ht; y++) for(int x = 0; x < wd; x++)
+  {
+    T res;
+    if(first > 0) res = llap_expand(l1[NUM_GAMMA], x, y);
+    else          res = llap_expand(coarse, x, y);
+    const T v = fetch_z(l0[NUM_GAMMA], x, y, 0);
+    const int hi = gamma_hi_from_v(v);
+    const int lo = hi - 1;
+    const T glo = gamma_from_i<T>(lo), ghi = gamma_from_i<T>(hi);
+    const T a = gclamp((v - glo) / (ghi - glo), T(0.0), T(1.0));
+    const T la = fetch_z(l0[hi - 1], x, y, 0) - llap_expand(l1[hi - 1], x, y);
+    const T lb = fetch_z(l0[hi], x, y, 0) - llap_expand(l1[hi], x, y);
+    const T o[1] = { res + la * (T(1.0) - a) + lb * a };
+    out.store(x, y, o, 1);
+  }
+  return out;
+}
+
+// llap/colour.comp:141-160
+template<class T> static img_t<T> llap_colour(const img_t<T> &yimg, const img_t<T> &org)
+{
+  img_t<T> out(org.w, org.h, 4);
+  OMP_FOR
+  for(int y = 0; y < org.h; y++) for(int x = 0; x < org.w; x++)
+  {
+    T yv = fetch_z(yimg, x, y, 0);
+    T rgb[3];
+    for(int k = 0; k < 3; k++) rgb[k] = fetch_z(org, x, y, k);
+    const T yo = gmax(lum2020(rgb[0], rgb[1], rgb[2]), T(1e-8));
+    const T c = T(1.0);
+    if(yv < yo) yv = yo * std::exp(c * (yv - yo));
+    T o[4];
+    for(int k = 0; k < 3; k++) o[k] = gmax(T(0), rgb[k] * yv / yo);
+    o[3] = T(1);
+    out.store(x, y, o, 4);
+  }
+  return out;
+}
+
+// ------------------------------------------------------------------ graph
+
+template<class T> static void to_float(const img_t<T> &im, float *dst)
+{
+  if(!dst) return;
+  for(size_t i = 0; i < im.d.size(); i++) dst[i] = (float)im.d[i];
+}
+template<class T> static void to_float_ch(const img_t<T> &im, int ch, float *dst)
+{ // first ch channels of every pixel
+  if(!dst) return;
+  OMP_FOR
+  for(int y = 0; y < im.h; y++) for(int x = 0; x < im.w; x++)
+    for(int k = 0; k < ch; k++) dst[((size_t)y * im.w + x) * ch + k] = (float)im.ch(x, y, k);
+}
+
+template<class T> static int develop(const uint16_t *mosaic, int wd, int ht,
+    const oracle_img_param_t *ip, const oracle_params_t *p, oracle_stages_t *st)
+{
+  if(wd <= 0 || ht <= 0 || !mosaic || !ip || !p) return 1;
+  const uint32_t filters = ip->filters;
+  if(filters == 0) return 2; // the path starts on a mosaic
+  // i-raw output: R16_UNORM
+  img_t<T> raw(wd, ht, 1);
+  for(size_t i = 0; i < (size_t)wd * ht; i++) raw.d[i] = T(mosaic[i]) / T(65535);
+
+  // ---- denoise (denoise/main.c:133-333). crop window and black/white in unorm units
+  T black[4], white[4], wb[4];
+  for(int k = 0; k < 4; k++)
+  {
+    black[k] = T(ip->black[k] / 65535.0f);
+    white[k] = T(ip->white[k] / 65535.0f);
+    wb[k] = T(ip->whitebalance[k]);
+  }
+  const int cw = (int)(ip->crop_aabb[2] - ip->crop_aabb[0]), ch = (int)(ip->crop_aabb[3] - ip->crop_aabb[1]);
+  if(cw <= 0 || ch <= 0 || (int)ip->crop_aabb[2] > wd || (int)ip->crop_aabb[3] > ht) return 3;
+  const int crop[4] = { (int)ip->crop_aabb[0], (int)ip->crop_aabb[1], (int)ip->crop_aabb[2], (int)ip->crop_aabb[3] };
+  const int W = cw, H = ch; // module output roi
+  const T edges[4] = { T(p->dn_edges[0]), T(p->dn_edges[1]), T(p->dn_edges[2]), T(p->dn_edges[3]) };
+  img_t<T> dn;
+  if(p->dn_strength <= 0.0f)
+  {
+    dn = denoise_noop(raw, W, H, crop, black, white);
+  }
+  else
+  {
+    const int block = filters == 9u ? 3 : 2;
+    const int hw = W / block, hh = H / block;
+    img_t<T> half = denoise_half(raw, hw, hh, crop, white[1], filters);
+    const int zc[4] = { 0, 0, 0, 0 };
+    img_t<T> s[5];
+    s[0] = half;
+    s[1] = denoise_downcov(half, hw, hh, zc);
+    for(int i = 1; i < 4; i++)
+      s[i + 1] = denoise_down(s[i], hw, hh, zc, black[1], white[1], T(ip->noise_a), T(ip->noise_b), edges, i, block);
+    img_t<T> as = denoise_assemble(s, hw, hh, zc, wb, black, white, T(ip->noise_a), T(ip->noise_b), filters,
+        T(p->dn_strength), T(p->dn_luma), edges);
+    dn = denoise_doub(raw, as, half, W, H, crop, black, white, filters, T(ip->noise_a), T(ip->noise_b),
+        T(p->dn_strength), T(p->dn_luma), T(p->dn_detail), edges);
+  }
+  if(st) to_float_ch(dn, 1, st->denoise);
+
+  // ---- hilite (hilite/main.c:5-90)
+  const int block = filters == 9u ? 3 : 2;
+  img_t<T> hl(W, H, 1);
+  {
+    const T hwhite = T(p->hl_white);
+    const int hw = W / block, hh = H / block;
+    img_t<T> h0 = hilite_half(dn, hw, hh, hwhite, filters);
+    std::vector<img_t<T>> red;   // reduce outputs r_1..r_n
+    std::vector<int> rw, rh;
+    int cwd = (hw - 1) / 2 + 1, cht = (hh - 1) / 2 + 1;
+    const int max_nl = 15;
+    const img_t<T> *fine = &h0;
+    red.reserve(max_nl);
+    for(int l = 1; l < max_nl; l++)
+    {
+      red.push_back(hilite_reduce(*fine, cwd, cht, wb, hwhite, T(p->hl_desat)));
+      fine = &red.back();
+      const int nwd = (cwd - 1) / 2 + 1, nht = (cht - 1) / 2 + 1;
+      cwd = nwd; cht = nht;
+      if(cwd <= 1 || cht <= 1 || l + 1 == max_nl) break;
+    }
+    if(st) st->hilite_levels = (int)red.size();
+    // assemble from the coarsest: the last assemble takes the last reduce as coarse
+    img_t<T> up = red.back();
+    for(int l = (int)red.size() - 1; l >= 0; l--)
+    {
+      const img_t<T> &f = l == 0 ? h0 : red[l - 1];
+      up = hilite_assemble(f, up, f.w, f.h, hwhite, T(p->hl_soft));
+    }
+    hilite_doub(dn, up, hw, hh, hwhite, filters, hl);
+  }
+  if(st) to_float_ch(hl, 1, st->hilite);
+
+  // ---- demosaic (demosaic/main.c:18-203)
+  const int ow = p->out_wd > 0 ? p->out_wd : W, oh = p->out_ht > 0 ? p->out_ht : H;
+  const float scale = (float)W / (float)ow;
+  const int halfsize = (scale >= 1.5 * block) || (p->dm_method == 2);
+  img_t<T> rgb;
+  if(halfsize)
+  {
+    img_t<T> hs = demosaic_halfsize(hl, W / block, H / block, filters);
+    if(block != scale) rgb = shared_resample(hs, ow, oh);
+    else rgb = hs;
+  }
+  else
+  {
+    if(ow != W || oh != H) return 4; // resample after full-size demosaic not covered
+    img_t<T> cov = demosaic_gauss(hl, W / block, H / block, filters);
+    img_t<T> g = demosaic_splat(hl, cov, W, H, filters);
+    rgb = demosaic_fix(hl, g, cov, W, H, filters, p->dm_colour);
+  }
+  if(st) { to_float(rgb, st->demosaic); st->out_wd = rgb.w; st->out_ht = rgb.h; }
+
+  // ---- colour, filmcurv (+ histogram of its input), llap
+  if(p->fc_colour != 1 && p->fc_colour != 3) return 5; // filmcurv colour modes restated: 1, 3
+  if(p->co_sat != 1.0f) return 6;                       // colour saturation path not restated
+  img_t<T> col = colour_main(rgb, ip, p);
+  if(st) to_float(col, st->colour);
+  if(st && st->hist) hist(col, st->hist);
+  img_t<T> fc = filmcurv_main(col, p);
+  if(st) to_float(fc, st->filmcurv);
+
+  // llap (llap/main.c:6-106)
+  std::vector<std::vector<img_t<T>>> lev;
+  lev.push_back(llap_curve(fc, p));
+  int rcw = (fc.w - 1) / 2 + 1, rch = (fc.h - 1) / 2 + 1;
+  int nl = 12;
+  for(int l = 1; l < nl; l++)
+  {
+    std::vector<img_t<T>> r;
+    for(int i = 0; i <= NUM_GAMMA; i++) r.push_back(llap_reduce(lev[l - 1][i], rcw, rch));
+    lev.push_back(r);
+    rcw = (rcw - 1) / 2 + 1; rch = (rch - 1) / 2 + 1;
+    if(rcw <= 1 || rch <= 1) { nl = l + 1; break; }
+    if(p->ll_levels > 0 && l + 1 == p->ll_levels) { nl = l + 1; break; }
+  }
+  if(st) st->llap_levels = nl;
+  img_t<T> up;
+  for(int l = nl - 1; l >= 1; l--)
+    up = llap_assemble(up, lev[l - 1], lev[l], l == nl - 1, lev[l - 1][0].w, lev[l - 1][0].h);
+  img_t<T> outimg = llap_colour(up, fc);
+  if(st) to_float(outimg, st->llap);
+  return 0;
+}
+
+} // namespace
+
+extern "C" {
+
+void oracle_default_params(oracle_params_t *p)
+{
+  memset(p, 0, sizeof(*p));
+  p->dn_strength = 0.0f; p->dn_luma = 0.6f; p->dn_detail = 1.0f; p->dn_gainmap = 1;   // denoise/params:1-6
+  p->hl_white = 0.985f; p->hl_desat = 0.3f; p->hl_soft = 0.6f;                        // hilite/params:1-3
+  p->dm_colour = 0; p->dm_method = 0;                                                  // demosaic/params:1-2
+  p->co_exposure = 0.0f; p->co_sat = 1.0f; p->co_matrix = 1;                           // colour/params:1-9
+  p->fc_light = 3.0f; p->fc_contrast = 1.2f; p->fc_bias = 0.0f; p->fc_colour = 3;      // filmcurv/params:1-10
+  p->fc_chroma = 1.0f;
+  p->ll_sigma = 0.12f; p->ll_shadows = 1.0f; p->ll_hilights = 1.0f; p->ll_clarity = 0.2f; // default-darkroom.i-raw:29-32
+}
+
+int oracle_develop_f32(const uint16_t *mosaic, int wd, int ht,
+    const oracle_img_param_t *ip, const oracle_params_t *p, oracle_stages_t *out)
+{ return develop<float>(mosaic, wd, ht, ip, p, out); }
+
+int oracle_develop_f64(const uint16_t *mosaic, int wd, int ht,
+    const oracle_img_param_t *ip, const oracle_params_t *p, oracle_stages_t *out)
+{ return develop<double>(mosaic, wd, ht, ip, p, out); }
+
+void oracle_noop(const uint16_t *mosaic, int wd, int ht, const oracle_img_param_t *ip, float *out)
+{
+  img_t<float> raw(wd, ht, 1);
+  for(size_t i = 0; i < (size_t)wd * ht; i++) raw.d[i] = float(mosaic[i]) / 65535.0f;
+  float black[4], white[4];
+  for(int k = 0; k < 4; k++) { black[k] = ip->black[k] / 65535.0f; white[k] = ip->white[k] / 65535.0f; }
+  const int crop[4] = { (int)ip->crop_aabb[0], (int)ip->crop_aabb[1], (int)ip->crop_aabb[2], (int)ip->crop_aabb[3] };
+  img_t<float> o = denoise_noop(raw, (int)(crop[2] - crop[0]), (int)(crop[3] - crop[1]), crop, black, white);
+  to_float_ch(o, 1, out);
+}
+
+void oracle_hist(const float *rgba, int wd, int ht, uint32_t *h)
+{
+  img_t<float> im(wd, ht, 4);
+  memcpy(im.d.data(), rgba, sizeof(float) * 4 * (size_t)wd * ht);
+  hist(im, h);
+}
+
+int oracle_cfa_colour(uint32_t filters, int x, int y)
+{
+  if(filters == 9) return cfa_xtrans(x + 6, y + 6);
+  return cfa_bayer(x, y);
+}
+
+float oracle_f16(float v) { return f16r(v); }
+
+} // extern "C"

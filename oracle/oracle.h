@@ -1,0 +1,109 @@
+/*
+ * CPU oracle for the raw-development hot path of vkdt
+ * (denoise -> hilite -> demosaic -> colour -> filmcurv -> llap).
+ *
+ * TEST INFRASTRUCTURE ONLY. This is a line-by-line restatement of the
+ * reference GLSL compute shaders in plain C++, used as the checker for the
+ * CUDA library. Only tests/, __graft_entry__.smoke() and the cpu_baseline leg
+ * of bench.py may load it. The product library never links it.
+ *
+ * Every node function cites the shader (path within the vkdt project) it
+ * restates. The whole file is templated on the arithmetic type so the same
+ * code gives the FP32 build (the timed CPU baseline and the parity checker)
+ * and the FP64 build (the error reference). f16 storage is emulated at the
+ * exact points where the reference stores an image (every node output).
+ *
+ * Parity pinning: the reference ships no golden vectors for this path. The
+ * restatement is pinned against the reference's own shader sources compiled
+ * for the CPU (oracle/glsl, built into oracle/_ref) where that build exists.
+ */
+#pragma once
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* subset of dt_image_params_t (src/pipe/module.h:72-109) that the path reads */
+typedef struct oracle_img_param_t
+{
+  float    black[4];           /* raw DN */
+  float    white[4];           /* raw DN */
+  float    whitebalance[4];    /* normalised to green = 1 (i-raw/main.c:214-218) */
+  uint32_t filters;            /* 0 rgb, 9 x-trans, else bayer rggb */
+  uint32_t crop_aabb[4];       /* x0 y0 x1 y1 */
+  float    cam_to_rec2020[9];  /* row major */
+  float    noise_a, noise_b;   /* vkdt normalised noise profile */
+}
+oracle_img_param_t;
+
+/* module parameters in the order of each module's `params` file */
+typedef struct oracle_params_t
+{
+  /* denoise/params */
+  float   dn_strength, dn_luma, dn_detail, dn_pad, dn_edges[4];
+  int32_t dn_gainmap;
+  /* hilite/params */
+  float   hl_white, hl_desat, hl_soft;
+  /* demosaic/params */
+  int32_t dm_colour, dm_method;
+  /* colour/params (the parts read by the matrix path) */
+  float   co_exposure, co_sat;
+  int32_t co_matrix;
+  float   co_white[4];
+  /* filmcurv/params */
+  float   fc_light, fc_contrast, fc_bias;
+  int32_t fc_colour;
+  float   fc_chroma, fc_rolloff, fc_red, fc_yellow, fc_blue, fc_shadows;
+  /* llap/params */
+  float   ll_sigma, ll_shadows, ll_hilights, ll_clarity;
+  /* pyramid depth override: 0 = automatic as llap/main.c:44-89 */
+  int32_t ll_levels;
+  /* requested output size of the demosaic module (0 = full size). a smaller
+   * size switches to the half-size demosaic + resample (demosaic/main.c:93-111) */
+  int32_t out_wd, out_ht;
+}
+oracle_params_t;
+
+/* optional stage outputs, any pointer may be 0. float arrays, row major. */
+typedef struct oracle_stages_t
+{
+  float    *denoise;   /* denoise module output, W*H, 1 channel (mosaic) */
+  float    *hilite;    /* hilite module output, W*H, 1 channel (mosaic) */
+  float    *demosaic;  /* demosaic output, ow*oh*4 */
+  float    *colour;    /* colour output, ow*oh*4 */
+  float    *filmcurv;  /* filmcurv output, ow*oh*4 */
+  uint32_t *hist;      /* OpenDRT/hist of the filmcurv input, 257 counts */
+  float    *llap;      /* llap output (module output of the path), ow*oh*4 */
+  int32_t   out_wd, out_ht; /* written: size of the rgb stages */
+  int32_t   llap_levels;    /* written: pyramid depth used */
+  int32_t   hilite_levels;  /* written: number of hilite reduce nodes */
+}
+oracle_stages_t;
+
+/* the default parameters of the six modules plus the darkroom .cfg values
+ * (bin/default-darkroom.i-raw:28-32) */
+void oracle_default_params(oracle_params_t *p);
+
+/* run the whole path on one u16 mosaic. returns 0 on success. */
+int oracle_develop_f32(const uint16_t *mosaic, int wd, int ht,
+    const oracle_img_param_t *ip, const oracle_params_t *p, oracle_stages_t *out);
+int oracle_develop_f64(const uint16_t *mosaic, int wd, int ht,
+    const oracle_img_param_t *ip, const oracle_params_t *p, oracle_stages_t *out);
+
+/* single-node entry points for unit tests */
+/* denoise/noop.comp on the whole mosaic -> W*H normalised f16 values */
+void oracle_noop(const uint16_t *mosaic, int wd, int ht, const oracle_img_param_t *ip, float *out);
+/* OpenDRT/hist.comp over an rgba image (float values, already f16) */
+void oracle_hist(const float *rgba, int wd, int ht, uint32_t *hist257);
+/* the bin index the histogram assigns to a luminance (bit exact with the kernel) */
+uint32_t oracle_hist_bin(float r, float g, float b);
+/* CFA colour index at a pixel: 0 red, 1 green, 2 blue (demosaic/splat.comp:167-222) */
+int oracle_cfa_colour(uint32_t filters, int x, int y);
+/* round to IEEE half (RTNE) and back */
+float oracle_f16(float v);
+
+#ifdef __cplusplus
+}
+#endif

@@ -1,0 +1,117 @@
+"""CPU tests of the C-ABI library: it loads, exports every declared entry
+point, and its host side (cfg reading, parameters, create_nodes) behaves like
+the reference's module layer. No compute calls (no GPU here)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import vkdt_gb300 as v
+from vkdt_gb300 import _lib
+
+
+def test_library_exports_every_declared_symbol():
+    l = _lib.lib()
+    declared = _lib.declared_symbols()
+    assert len(declared) >= 30
+    for name in declared:
+        assert hasattr(l, name), name
+        assert name in _lib._SIGS, name
+
+
+def test_token_packing():
+    # src/pipe/token.h: little endian chars, at most 8
+    assert v.token("llap") == ord("l") | ord("l") << 8 | ord("a") << 16 | ord("p") << 24
+    assert v.token_str(v.token("demosaic")) == "demosaic"
+    assert v.token("toolongname") == v.token("toolongn")
+
+
+def test_supports():
+    for n, k in [("denoise", "noop"), ("hilite", "reduce"), ("demosaic", "splat"), ("llap", "assemble"), ("OpenDRT", "hist")]:
+        assert v.supports(n, k)
+    assert not v.supports("crop", "main")
+    assert not v.supports("demosaic", "rcd_fill")
+
+
+def test_default_params_and_cfg_overrides():
+    g = v.Graph()
+    assert np.isclose(g.get_param("denoise", "strength")[0], 0.0)
+    assert np.isclose(g.get_param("hilite", "white")[0], 0.985)
+    assert np.isclose(g.get_param("filmcurv", "light")[0], 3.0)
+    assert g.get_param("filmcurv", "colour", dtype=np.int32)[0] == 3
+    assert np.isclose(g.get_param("llap", "clarity")[0], 0.2)   # the cfg line
+    assert np.isclose(g.get_param("llap", "sigma")[0], 0.12)
+    g.set_param("colour", "exposure", 0.5)
+    assert np.isclose(g.get_param("colour", "exposure")[0], 0.5)
+    g.set_param("denoise", "edges", [0.1, 0.2, 0.3, 0.4])
+    assert np.allclose(g.get_param("denoise", "edges", 4), [0.1, 0.2, 0.3, 0.4])
+    with pytest.raises(_lib.VkdtError) as e:
+        g.set_param("colour", "nosuch", 1.0)
+    assert e.value.code == _lib.ERROR_FORMAT_NOT_SUPPORTED
+    with pytest.raises(_lib.VkdtError):
+        g.set_param("denoise", "edges", 1.0)    # wrong count
+    g.close()
+
+
+FULL_CFG = v.DARKROOM_CFG.replace(
+    "connect:demosaic:01:output:colour:01:input\n",
+    "module:crop:01:743:400\nmodule:grade:01:1444:400\nmodule:display:main:1545:400\n"
+    "connect:demosaic:01:output:crop:01:input\nconnect:crop:01:output:colour:01:input\n"
+    "connect:llap:01:output:grade:01:input\nconnect:grade:01:output:display:main:input\n") + "param:grade:01:vib:1\n"
+
+
+def test_cfg_with_modules_outside_the_path():
+    g = v.Graph(FULL_CFG)
+    assert sorted(g.unsupported()) == ["crop", "display", "grade"]
+    g.close()
+
+
+def test_cfg_errors():
+    broken = v.DARKROOM_CFG.replace("connect:hilite:01:output:demosaic:01:input\n", "")
+    with pytest.raises(_lib.VkdtError) as e:
+        v.Graph(broken)
+    assert e.value.code == _lib.INCOMPLETE
+    with pytest.raises(_lib.VkdtError) as e:
+        v.Graph(v.DARKROOM_CFG + "bogus line\n")
+    assert e.value.code == _lib.ERROR_FORMAT_NOT_SUPPORTED
+
+
+def _nodes(wd, ht, levels=0):
+    g = v.Graph()
+    g.set_input(wd, ht, v.default_img_param(wd=wd, ht=ht))
+    if levels:
+        g.set_llap_levels(levels)
+    g.create_nodes()
+    n = g.nodes()
+    g.close()
+    return n
+
+
+def test_create_nodes_24mp():
+    n = _nodes(6000, 4000)
+    kinds = [(a, b) for a, b, *_ in n]
+    # hilite/main.c: reduce/assemble pairs until a level has one pixel row or column
+    assert kinds.count(("hilite", "reduce")) == 10 and kinds.count(("hilite", "assemble")) == 10
+    # llap/main.c: 12 levels at 24 MP (11 reduce + 11 assemble nodes)
+    assert kinds.count(("llap", "reduce")) == 11 and kinds.count(("llap", "assemble")) == 11
+    red = [x for x in n if x[0] == "llap" and x[1] == "reduce"]
+    assert red[0][2:5] == (3000, 2000, 11) and red[-1][2:4] == (3, 2)
+    hred = [x for x in n if x[0] == "hilite" and x[1] == "reduce"]
+    assert hred[0][2:4] == (1500, 1000) and hred[-1][2:4] == (3, 2)
+    for name, kernel, *_ in n:
+        assert v.supports(name, kernel), (name, kernel)
+
+
+def test_create_nodes_forced_depth():
+    n = _nodes(6000, 4000, levels=6)
+    kinds = [(a, b) for a, b, *_ in n]
+    assert kinds.count(("llap", "reduce")) == 5
+
+
+def test_create_nodes_rejects_bad_input():
+    g = v.Graph()
+    ip = v.default_img_param(wd=101, ht=100)
+    g.set_input(101, 100, ip)
+    with pytest.raises(_lib.VkdtError):
+        g.create_nodes()
+    g.close()

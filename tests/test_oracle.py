@@ -1,0 +1,120 @@
+"""CPU tests of the oracle: known-answer tests on its integer and storage
+semantics, and agreement of its FP32 and FP64 builds."""
+import numpy as np
+import pytest
+
+import oracle
+import vkdt_gb300 as v
+
+from metrics import delta_e2000, delta_e2000_lab, summary
+
+
+def test_f16_rounding_kat():
+    # IEEE binary16 round to nearest even, including subnormals and overflow
+    kat = {
+        0.0: 0.0, 1.0: 1.0, 65504.0: 65504.0, 65519.0: 65504.0, 65520.0: np.inf, -65520.0: -np.inf,
+        1.0 + 2 ** -11: 1.0,                     # tie -> even
+        1.0 + 3 * 2 ** -11: 1.0 + 2 ** -9,       # tie -> even (up)
+        2 ** -24: 2 ** -24, 2 ** -25: 0.0,       # smallest subnormal, tie to even zero
+        3 * 2 ** -26: 2 ** -24,
+        0.1: float(np.float16(0.1)), 1e-5: float(np.float16(1e-5)),
+    }
+    for x, want in kat.items():
+        assert oracle.f16(np.float32(x)) == np.float32(want), x
+
+
+def test_f16_rounding_matches_numpy():
+    rng = np.random.default_rng(1)
+    x = np.concatenate([rng.uniform(-70000, 70000, 20000), rng.uniform(-1e-4, 1e-4, 20000),
+                        rng.uniform(-2, 2, 20000)]).astype(np.float32)
+    got = np.array([oracle.f16(float(a)) for a in x], np.float32)
+    assert np.array_equal(got, x.astype(np.float16).astype(np.float32))
+
+
+def test_noop_exhaustive_u16():
+    # denoise/noop.comp: max(0, (v/65535 - b)/(w - b)) stored as f16, all 65536 codes
+    codes = np.arange(65536, dtype=np.uint16).reshape(256, 256)
+    for black, white in ((512.0, 16383.0), (256.0, 4095.0), (0.0, 65535.0), (2048.0, 15000.0)):
+        ip = oracle.img_param(v.default_img_param(black=black, white=white, wd=256, ht=256))
+        got = oracle.noop(codes, ip)
+        b = np.float32(black / np.float32(65535.0))
+        w = np.float32(white / np.float32(65535.0))
+        x = codes.astype(np.float32) / np.float32(65535.0)
+        want = np.maximum(np.float32(0), (x - b) / (w - b)).astype(np.float16).astype(np.float32)
+        assert np.array_equal(got, want), (black, white)
+
+
+def test_cfa_pattern():
+    # bayer rggb at (0,0)
+    for y in range(-4, 8):
+        for x in range(-4, 8):
+            want = 0 if (x % 2 == 0 and y % 2 == 0) else (2 if (x % 2 == 1 and y % 2 == 1) else 1)
+            assert oracle.cfa_colour(0x94949494, x, y) == want
+    # x-trans 6x6 as demosaic/splat.comp:229-235 draws it (r . b = red, blue; g elsewhere)
+    rows = ["GRGGBG", "BGBRGR", "GRGGBG", "GBGGRG", "RGRBGB", "GBGGRG"]
+    idx = {"R": 0, "G": 1, "B": 2}
+    for y in range(12):
+        for x in range(12):
+            assert oracle.cfa_colour(9, x, y) == idx[rows[y % 6][x % 6]], (x, y)
+
+
+def test_hist_bins_constructed():
+    # luminances placed at bin centres: l = eotf_filmlight_tlog(lum), bin = uint(256 l + 0.5)
+    for b in list(range(1, 256, 7)) + [255]:
+        l = b / 256.0
+        lum = np.exp((l - 0.5520126568606655) / 0.09232902596577353) - 0.0057048244042473785
+        if lum < 0:
+            lum = (l - 0.075) / 16.184376489665897
+        assert oracle.hist_bin(float(lum), float(lum), float(lum)) == b, b
+    assert oracle.hist_bin(-10.0, -10.0, -10.0) == 0
+    assert oracle.hist_bin(1e6, 1e6, 1e6) == 255
+    # counts on a constructed image: each bin value repeated (bin) times
+    vals, want = [], np.zeros(257, np.uint32)
+    for b in range(1, 256):
+        l = b / 256.0
+        lum = np.exp((l - 0.5520126568606655) / 0.09232902596577353) - 0.0057048244042473785
+        if lum < 0:
+            lum = (l - 0.075) / 16.184376489665897
+        vals += [lum] * (b % 5 + 1)
+        want[b] += b % 5 + 1
+    want[256] = want[:256].sum()
+    n = len(vals)
+    img = np.zeros((1, n, 4), np.float32)
+    img[0, :, 0] = img[0, :, 1] = img[0, :, 2] = vals
+    assert np.array_equal(oracle.hist(img), want)
+
+
+def _scene(wd, ht, seed=0):
+    s = v.make_scene(wd, ht, seed=seed)
+    m = v.scene_host(s)
+    ip = v.default_img_param(wd=wd, ht=ht, noise_a=2.0 / (16383 - 512) ** 2, noise_b=0.4 / (16383 - 512))
+    return m, ip
+
+
+def test_scene_recipe():
+    m, _ = _scene(512, 384)
+    assert m.dtype == np.uint16
+    clipped = (m == 16383).mean()
+    assert 0.01 < clipped < 0.03          # the seeded 2% at white
+    assert m[m < 16383].max() < 16383
+    assert m.min() >= 0
+
+
+def test_fp32_matches_fp64():
+    m, ip = _scene(192, 128, seed=3)
+    oip = oracle.img_param(ip)
+    a = oracle.develop(m, oip, stages=("colour", "filmcurv", "llap"))
+    b = oracle.develop(m, oip, double=True, stages=("colour", "filmcurv", "llap"))
+    s = summary(a["colour"], b["colour"])
+    assert s["mean"] < 1e-4 and s["flipped_frac"] < 1e-3, s
+    de = delta_e2000(a["llap"], b["llap"])
+    assert np.percentile(de, 99.9) < 0.5, de.max()
+
+
+@pytest.mark.parametrize("wd,ht,nl,nh", [(6000, 4000, 12, 10), (2048, 1536, 11, 9), (256, 192, 8, 6)])
+def test_pyramid_depths(wd, ht, nl, nh):
+    m = np.zeros((ht, wd), np.uint16) + 4000 if wd * ht < 100000 else None
+    if m is None:
+        pytest.skip("depth arithmetic checked through the library for large sizes")
+    r = oracle.develop(m, oracle.img_param(v.default_img_param(wd=wd, ht=ht)), stages=())
+    assert r["llap_levels"] == nl and r["hilite_levels"] == nh

@@ -1,0 +1,244 @@
+"""vkdt_gb300: the raw development hot path of vkdt on GB300 (sm_103a CUDA).
+
+Python mirror of the drop-in C-ABI (include/vkdt_cuda.h). The graph object
+follows the reference's graph API: read a .cfg, set module parameters by
+name, set the source image metadata, allocate, run, read the sink.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _lib
+from ._lib import ImgParam, Scene, check, token, token_str, RUN_ALL, RUN_UPLOAD_SOURCE, RUN_DOWNLOAD_SINK, RUN_WAIT_DONE
+
+__all__ = ["Graph", "ImgParam", "Scene", "init", "default_img_param", "scene_host", "scene_device",
+           "DARKROOM_CFG", "CAM_TO_REC2020", "supports"]
+
+# the synthetic camera: camera rgb -> rec2020, rows sum to one
+CAM_TO_REC2020 = (1.20, -0.15, -0.05,
+                  -0.10, 1.25, -0.15,
+                  0.02, -0.22, 1.20)
+
+# bin/default-darkroom.i-raw restricted to the modules of the path plus
+# the crop between demosaic and colour, with the cfg's parameter lines
+DARKROOM_CFG = """module:i-raw:main:43:400
+module:denoise:01:218:400
+module:hilite:01:393:400
+module:demosaic:01:568:400
+module:colour:01:931:400
+module:filmcurv:01:1094:400
+module:llap:01:1269:400
+connect:i-raw:main:output:denoise:01:input
+connect:denoise:01:output:hilite:01:input
+connect:hilite:01:output:demosaic:01:input
+connect:demosaic:01:output:colour:01:input
+connect:colour:01:output:filmcurv:01:input
+connect:filmcurv:01:output:llap:01:input
+param:colour:01:exposure:0
+param:llap:01:sigma:0.12
+param:llap:01:shadows:1
+param:llap:01:hilights:1
+param:llap:01:clarity:0.2
+"""
+
+_inited = None
+
+
+def init(device=0):
+    """vkdt_cuda_init (replaces qvk_init)."""
+    global _inited
+    if _inited == device:
+        return
+    check(_lib.lib().vkdt_cuda_init(device, 0), "vkdt_cuda_init")
+    _inited = device
+
+
+def supports(name, kernel):
+    return bool(_lib.lib().vkdt_cuda_supports(token(name), token(kernel)))
+
+
+def default_img_param(black=512.0, white=16383.0, wb=(2.0, 1.0, 1.6), filters=0x94949494, wd=0, ht=0,
+                      noise_a=0.0, noise_b=0.0, cam=CAM_TO_REC2020):
+    ip = ImgParam()
+    for k in range(4):
+        ip.black[k] = black
+        ip.white[k] = white
+    ip.whitebalance[0], ip.whitebalance[1], ip.whitebalance[2], ip.whitebalance[3] = wb[0], wb[1], wb[2], 1.0
+    ip.filters = filters
+    ip.crop_aabb[0], ip.crop_aabb[1], ip.crop_aabb[2], ip.crop_aabb[3] = 0, 0, wd, ht
+    for i in range(9):
+        ip.cam_to_rec2020[i] = cam[i]
+    ip.noise_a = noise_a
+    ip.noise_b = noise_b
+    return ip
+
+
+def make_scene(wd, ht, seed=0, image_id=0, black=512.0, white=16383.0, a=2.0, b=0.4, wb=(2.0, 1.0, 1.6),
+               filters=0x94949494, pan=(0.0, 0.0)):
+    s = Scene()
+    s.wd, s.ht, s.seed, s.image_id, s.filters = wd, ht, seed, image_id, filters
+    s.black, s.white, s.noise_a, s.noise_b = black, white, a, b
+    s.wb[0], s.wb[1], s.wb[2] = wb
+    s.pan_x, s.pan_y = pan
+    return s
+
+
+def scene_host(scene):
+    """The seeded mosaic, generated on the host (uint16 numpy array)."""
+    out = np.empty((scene.ht, scene.wd), dtype=np.uint16)
+    check(_lib.lib().vkdt_cuda_scene_generate_host(C.byref(scene), out.ctypes.data_as(C.POINTER(C.c_uint16))),
+          "vkdt_cuda_scene_generate_host")
+    return out
+
+
+def scene_device(scene, d_ptr, stream=0):
+    """Fill a device buffer (pointer) with the seeded mosaic."""
+    check(_lib.lib().vkdt_cuda_scene_generate(C.byref(scene), C.c_void_p(d_ptr), C.c_void_p(stream)),
+          "vkdt_cuda_scene_generate")
+
+
+class Graph:
+    """A vkdt processing graph restricted to the development path."""
+
+    def __init__(self, cfg=DARKROOM_CFG):
+        self._l = _lib.lib()
+        self._g = C.c_void_p()
+        check(self._l.vkdt_cuda_graph_create(C.byref(self._g)), "vkdt_cuda_graph_create")
+        if cfg is not None:
+            b = cfg.encode()
+            check(self._l.vkdt_cuda_graph_read_config(self._g, b, len(b)), "vkdt_cuda_graph_read_config")
+        self.wd = self.ht = 0
+        self.out_wd = self.out_ht = 0
+
+    def close(self):
+        if self._g:
+            self._l.vkdt_cuda_graph_destroy(self._g)
+            self._g = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- parameters
+    def set_param(self, module, param, value, inst="01"):
+        arr = np.atleast_1d(np.asarray(value))
+        kind = np.int32 if np.issubdtype(arr.dtype, np.integer) else np.float32
+        arr = np.ascontiguousarray(arr.astype(kind))
+        check(self._l.vkdt_cuda_graph_set_param(self._g, token(module), token(inst), token(param),
+                                                arr.ctypes.data, arr.nbytes), "set_param %s:%s" % (module, param))
+
+    def get_param(self, module, param, count=1, dtype=np.float32, inst="01"):
+        arr = np.zeros(count, dtype=dtype)
+        check(self._l.vkdt_cuda_graph_get_param(self._g, token(module), token(inst), token(param),
+                                                arr.ctypes.data, arr.nbytes), "get_param %s:%s" % (module, param))
+        return arr
+
+    def unsupported(self):
+        n = self._l.vkdt_cuda_graph_unsupported(self._g, None, 0)
+        buf = (C.c_uint64 * max(n, 1))()
+        self._l.vkdt_cuda_graph_unsupported(self._g, buf, n)
+        return [token_str(buf[i]) for i in range(n)]
+
+    def set_input(self, wd, ht, img_param):
+        self.wd, self.ht = wd, ht
+        check(self._l.vkdt_cuda_graph_set_input(self._g, wd, ht, C.byref(img_param)), "set_input")
+
+    def set_llap_levels(self, n):
+        check(self._l.vkdt_cuda_graph_set_llap_levels(self._g, n), "set_llap_levels")
+
+    def set_output_size(self, wd, ht):
+        check(self._l.vkdt_cuda_graph_set_output_size(self._g, wd, ht), "set_output_size")
+
+    def set_hist(self, on=True):
+        check(self._l.vkdt_cuda_graph_set_hist(self._g, 1 if on else 0), "set_hist")
+
+    def set_timing(self, on=True):
+        check(self._l.vkdt_cuda_graph_set_timing(self._g, 1 if on else 0), "set_timing")
+
+    def set_debug(self, on=True):
+        check(self._l.vkdt_cuda_graph_set_debug(self._g, 1 if on else 0), "set_debug")
+
+    # ---- allocation and nodes
+    def create_nodes(self):
+        check(self._l.vkdt_cuda_graph_create_nodes(self._g), "create_nodes")
+
+    def alloc(self):
+        nbytes = C.c_uint64(0)
+        check(self._l.vkdt_cuda_graph_alloc(self._g, C.byref(nbytes)), "alloc")
+        w, h = C.c_int(), C.c_int()
+        check(self._l.vkdt_cuda_graph_output_size(self._g, C.byref(w), C.byref(h)), "output_size")
+        self.out_wd, self.out_ht = w.value, h.value
+        return nbytes.value
+
+    def nodes(self):
+        out = []
+        info = _lib.NodeInfo()
+        for i in range(self._l.vkdt_cuda_graph_node_count(self._g)):
+            check(self._l.vkdt_cuda_graph_node(self._g, i, C.byref(info)), "node")
+            out.append((token_str(info.name), token_str(info.kernel), info.wd, info.ht, info.dp, info.fused))
+        return out
+
+    def device_buffers(self):
+        s, d = C.c_void_p(), C.c_void_p()
+        check(self._l.vkdt_cuda_graph_device_buffers(self._g, C.byref(s), C.byref(d)), "device_buffers")
+        return s.value, d.value
+
+    # ---- running
+    def source(self):
+        n = C.c_size_t()
+        p = self._l.vkdt_cuda_graph_map_source(self._g, C.byref(n))
+        if not p:
+            raise RuntimeError("graph not allocated")
+        return np.ctypeslib.as_array(C.cast(p, C.POINTER(C.c_uint16)), shape=(self.ht, self.wd))
+
+    def sink(self):
+        n = C.c_size_t()
+        p = self._l.vkdt_cuda_graph_map_sink(self._g, C.byref(n))
+        if not p:
+            raise RuntimeError("graph not allocated")
+        return np.ctypeslib.as_array(C.cast(p, C.POINTER(C.c_uint16)), shape=(self.out_ht, self.out_wd, 4)).view(np.float16)
+
+    def run(self, mosaic=None, flags=RUN_ALL, stream=0):
+        """Upload `mosaic` (if given), run, download and return the rgba f16 output."""
+        if mosaic is not None:
+            self.source()[...] = mosaic
+        check(self._l.vkdt_cuda_graph_run(self._g, C.c_void_p(stream), flags), "run")
+        if flags & RUN_DOWNLOAD_SINK and flags & RUN_WAIT_DONE:
+            return self.sink().copy()
+        return None
+
+    def wait(self, timeout_ms=600000):
+        check(self._l.vkdt_cuda_graph_wait(self._g, timeout_ms), "wait")
+
+    def develop(self, d_mosaic, d_rgba, stream=0):
+        check(self._l.vkdt_cuda_graph_develop(self._g, C.c_void_p(d_mosaic), C.c_void_p(d_rgba), C.c_void_p(stream)),
+              "develop")
+
+    def times(self):
+        n = self._l.vkdt_cuda_graph_query_times(self._g, None, None, None, 0)
+        ms = (C.c_float * max(n, 1))()
+        nm = (C.c_uint64 * max(n, 1))()
+        kn = (C.c_uint64 * max(n, 1))()
+        self._l.vkdt_cuda_graph_query_times(self._g, ms, nm, kn, n)
+        return [("%s:%s" % (token_str(nm[i]), token_str(kn[i])), ms[i]) for i in range(n)]
+
+    def hist(self):
+        h = (C.c_uint32 * 257)()
+        check(self._l.vkdt_cuda_graph_hist(self._g, h), "hist")
+        return np.array(h[:], dtype=np.uint32)
+
+    def debug_stage(self, stage):
+        ch = 4 if stage == 2 else 1
+        out = np.empty((self.ht, self.wd, ch), dtype=np.float32) if stage != 2 else np.empty((self.ht, self.wd, 4), np.float32)
+        check(self._l.vkdt_cuda_graph_debug_stage(self._g, stage, out.ctypes.data_as(C.POINTER(C.c_float)), out.size),
+              "debug_stage")
+        return out if ch == 4 else out[..., 0]

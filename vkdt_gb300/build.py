@@ -1,0 +1,84 @@
+"""Build libvkdt_cuda.so in-tree for sm_103a (nvcc + g++, parallel, no cmake).
+
+The kernels are compiled without floating point contraction (-fmad=false) so
+that every expression evaluates in the same order as the CPU oracle, which
+keeps data dependent branches (edge snapping, clipping tests, llap gamma
+selection, histogram bins) on the same side as the reference arithmetic.
+"""
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libvkdt_cuda.so")
+ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+CU_SOURCES = ["k_hilite.cu", "k_develop.cu", "k_llap.cu", "k_misc.cu"]
+CPP_SOURCES = ["graph.cpp"]
+
+
+def _cuda_home():
+    for c in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
+        if c and os.path.exists(os.path.join(c, "bin", "nvcc")):
+            return c
+    nv = shutil.which("nvcc")
+    if nv:
+        return os.path.dirname(os.path.dirname(nv))
+    raise RuntimeError("nvcc not found")
+
+
+def _newer(src_list, out):
+    if not os.path.exists(out):
+        return True
+    t = os.path.getmtime(out)
+    return any(os.path.getmtime(s) > t for s in src_list)
+
+
+def build(verbose=False, force=False):
+    cuda = _cuda_home()
+    nvcc = os.path.join(cuda, "bin", "nvcc")
+    os.makedirs(BUILD, exist_ok=True)
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    headers.append(os.path.join(ROOT, "include", "vkdt_cuda.h"))
+    inc = ["-I" + CSRC, "-I" + os.path.join(ROOT, "include")]
+    jobs, objs = [], []
+    for f in CU_SOURCES:
+        src = os.path.join(CSRC, f)
+        obj = os.path.join(BUILD, f + ".o")
+        objs.append(obj)
+        if force or _newer([src] + headers, obj):
+            cmd = [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--expt-relaxed-constexpr",
+                   "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills"] + inc + ["-c", src, "-o", obj]
+            jobs.append(cmd)
+    for f in CPP_SOURCES:
+        src = os.path.join(CSRC, f)
+        obj = os.path.join(BUILD, f + ".o")
+        objs.append(obj)
+        if force or _newer([src] + headers, obj):
+            cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-fvisibility=hidden",
+                   "-I" + os.path.join(cuda, "include")] + inc + ["-c", src, "-o", obj]
+            jobs.append(cmd)
+    procs = [(c, subprocess.Popen(c, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)) for c in jobs]
+    err = False
+    for c, p in procs:
+        out = p.communicate()[0].decode()
+        if p.returncode != 0:
+            err = True
+            sys.stderr.write("FAILED: %s\n%s\n" % (" ".join(c), out))
+        elif verbose and out.strip():
+            sys.stderr.write(out)
+    if err:
+        raise RuntimeError("libvkdt_cuda build failed")
+    if force or _newer(objs, LIB):
+        cmd = [nvcc, ARCH, "-shared", "-o", LIB] + objs + ["-lcudart_static", "-lpthread", "-ldl", "-lrt"]
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+        if r.returncode != 0:
+            raise RuntimeError("link failed:\n" + r.stdout.decode())
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose=True, force="--force" in sys.argv))

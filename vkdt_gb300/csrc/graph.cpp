@@ -1,0 +1,1007 @@
+// libvkdt_cuda host side: the module layer of the path (parameters, .cfg
+// reading, the node lists each module's create_nodes emits, commit_params),
+// device memory, the launch sequence, staging copies and the C-ABI of
+// include/vkdt_cuda.h.
+#include "vkdt_cuda.h"
+#include "kernels.h"
+#include "scene.h"
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdarg>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+namespace {
+
+thread_local char g_err[512] = "";
+int g_device = -1;
+
+int fail(int code, const char *fmt, ...) __attribute__((format(printf, 2, 3)));
+int fail(int code, const char *fmt, ...)
+{
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+int cuda_code(cudaError_t e)
+{
+  if(e == cudaErrorMemoryAllocation) return VKDT_CUDA_ERROR_OUT_OF_DEVICE_MEMORY;
+  if(e == cudaErrorInvalidValue || e == cudaErrorInvalidConfiguration) return VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED;
+  return VKDT_CUDA_ERROR_DEVICE_LOST;
+}
+#define CU(x) do { cudaError_t e_ = (x); if(e_ != cudaSuccess) return fail(cuda_code(e_), "%s: %s (%s:%d)", #x, cudaGetErrorString(e_), __FILE__, __LINE__); } while(0)
+
+dt_token_t tkn(const char *s)
+{ // src/pipe/token.h dt_token: up to 8 chars, little endian packed
+  uint64_t t = 0;
+  for(int i = 0; i < 8 && s[i]; i++) t |= ((uint64_t)(uint8_t)s[i]) << (8 * i);
+  return t;
+}
+std::string tstr(dt_token_t t)
+{
+  char c[9] = {0};
+  memcpy(c, &t, 8);
+  return std::string(c);
+}
+
+// ------------------------------------------------------------------ module parameter tables
+// name:type:count:defaults of each module's `params` file
+struct param_def_t { const char *name; char type; int cnt; std::vector<float> def; };
+struct module_def_t { const char *name; std::vector<param_def_t> params; };
+
+const std::vector<module_def_t> &module_defs()
+{
+  static const std::vector<module_def_t> defs = {
+    { "i-raw", {                                                  // i-raw/params
+      { "noise a", 'f', 1, { 0.0f } }, { "noise b", 'f', 1, { 0.0f } }, { "startid", 'i', 1, { 0 } } } },
+    { "denoise", {                                                // denoise/params:1-6
+      { "strength", 'f', 1, { 0.0f } }, { "luma", 'f', 1, { 0.6f } }, { "detail", 'f', 1, { 1.0f } },
+      { "pad", 'f', 1, { 0.0f } }, { "edges", 'f', 4, { 0, 0, 0, 0 } }, { "gainmap", 'i', 1, { 1 } } } },
+    { "hilite", {                                                 // hilite/params:1-3
+      { "white", 'f', 1, { 0.985f } }, { "desat", 'f', 1, { 0.3f } }, { "soft", 'f', 1, { 0.6f } } } },
+    { "demosaic", {                                               // demosaic/params:1-2
+      { "colour", 'i', 1, { 0 } }, { "method", 'i', 1, { 0 } } } },
+    { "colour", {                                                 // colour/params:1-13 (rbmap/import omitted)
+      { "exposure", 'f', 1, { 0.0f } }, { "sat", 'f', 1, { 1.0f } }, { "picked", 'i', 1, { 0 } },
+      { "matrix", 'i', 1, { 1 } }, { "gamut", 'i', 1, { 0 } }, { "clip", 'i', 1, { 0 } },
+      { "clipmax", 'f', 1, { 1.0f } }, { "temp", 'f', 1, { 6504.0f } }, { "white", 'f', 4, { 0, 0, 0, 0 } },
+      { "mat", 'f', 9, { -1, -1, -1, -1, -1, -1, -1, -1, -1 } }, { "mode", 'i', 1, { 0 } }, { "cnt", 'i', 1, { 4 } } } },
+    { "filmcurv", {                                               // filmcurv/params:1-10
+      { "light", 'f', 1, { 3.0f } }, { "contrast", 'f', 1, { 1.2f } }, { "bias", 'f', 1, { 0.0f } },
+      { "colour", 'i', 1, { 3 } }, { "chroma", 'f', 1, { 1.0f } }, { "rolloff", 'f', 1, { 0.0f } },
+      { "red", 'f', 1, { 0.0f } }, { "yellow", 'f', 1, { 0.0f } }, { "blue", 'f', 1, { 0.0f } },
+      { "shadows", 'f', 1, { 0.0f } } } },
+    { "llap", {                                                   // llap/params:1-4
+      { "sigma", 'f', 1, { 0.12f } }, { "shadows", 'f', 1, { 1.0f } }, { "hilights", 'f', 1, { 1.0f } },
+      { "clarity", 'f', 1, { 0.0f } } } },
+  };
+  return defs;
+}
+
+const module_def_t *find_def(dt_token_t name)
+{
+  for(auto &d : module_defs()) if(tkn(d.name) == name) return &d;
+  return nullptr;
+}
+
+struct module_t
+{
+  dt_token_t name = 0, inst = 0;
+  const module_def_t *def = nullptr;
+  std::vector<uint32_t> param; // 4 bytes per value, params file order
+  int offset(dt_token_t p, int *cnt, char *type) const
+  {
+    int off = 0;
+    for(auto &pd : def->params)
+    {
+      if(tkn(pd.name) == p) { if(cnt) *cnt = pd.cnt; if(type) *type = pd.type; return off; }
+      off += pd.cnt;
+    }
+    return -1;
+  }
+  float f(const char *p, int i = 0) const { int o = offset(tkn(p), 0, 0); float v; memcpy(&v, &param[o + i], 4); return v; }
+  int   n(const char *p, int i = 0) const { int o = offset(tkn(p), 0, 0); int32_t v; memcpy(&v, &param[o + i], 4); return v; }
+  void  setf(const char *p, int i, float v) { int o = offset(tkn(p), 0, 0); memcpy(&param[o + i], &v, 4); }
+  void init(const module_def_t *d, dt_token_t nm, dt_token_t in)
+  {
+    def = d; name = nm; inst = in;
+    param.clear();
+    for(auto &pd : d->params) for(int i = 0; i < pd.cnt; i++)
+    {
+      const float dv = pd.def[std::min<int>(i, (int)pd.def.size() - 1)];
+      uint32_t u;
+      if(pd.type == 'i') { int32_t iv = (int32_t)dv; memcpy(&u, &iv, 4); }
+      else memcpy(&u, &dv, 4);
+      param.push_back(u);
+    }
+  }
+};
+
+// ------------------------------------------------------------------ device buffers
+struct level_t { int w = 0, h = 0; size_t off = 0; };
+
+} // namespace
+
+struct vkdt_cuda_graph_t
+{
+  std::vector<module_t> modules;
+  std::vector<dt_token_t> unsupported;
+  std::vector<std::pair<std::string, std::string>> connects; // "mod:inst:conn" pairs
+  // input
+  int in_wd = 0, in_ht = 0;
+  vkdt_cuda_img_param_t ip;
+  bool have_input = false;
+  int req_wd = 0, req_ht = 0;
+  int llap_levels_req = 0;
+  bool timing = false, want_hist = false, debug = false, use_graph = true;
+  // derived by alloc
+  bool allocated = false, nodes_ready = false;
+  int W = 0, H = 0, out_w = 0, out_h = 0;
+  int hw = 0, hh = 0;
+  std::vector<level_t> hr, hb;   // hilite reduce outputs r[1..L] (index 0 = r1), assembled B[1..L-1]
+  std::vector<level_t> lp, la;   // llap planes level 1..nl-1 (index 0 = level 1), assembled A[1..nl-2]
+  int nl = 0;
+  size_t off_src = 0, off_rgbf = 0, off_out = 0, off_hist = 0, off_dbg0 = 0, off_dbg1 = 0, arena_bytes = 0;
+  unsigned char *arena = nullptr;
+  void *h_src = nullptr, *h_sink = nullptr;
+  size_t src_bytes = 0, sink_bytes = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+  std::vector<vkdt_cuda_node_info_t> nodes;
+  // launch list (fused kernels) and timing
+  struct launch_t { dt_token_t name, kernel; };
+  std::vector<launch_t> launches;
+  std::vector<cudaEvent_t> ev;
+  std::vector<float> times;
+  cudaGraphExec_t gexec = nullptr;
+  bool graph_dirty = true;
+  const void *ext_src = nullptr;  // device buffers bound for the current run
+  void *ext_dst = nullptr;
+
+  module_t *mod(const char *name)
+  {
+    for(auto &m : modules) if(m.name == tkn(name)) return &m;
+    return nullptr;
+  }
+  template<class T> T *at(size_t off) { return reinterpret_cast<T *>(arena + off); }
+};
+
+namespace {
+
+module_t *ensure_module(vkdt_cuda_graph_t *g, const char *name)
+{
+  module_t *m = g->mod(name);
+  if(m) return m;
+  module_t nm;
+  nm.init(find_def(tkn(name)), tkn(name), tkn("01"));
+  g->modules.push_back(nm);
+  return &g->modules.back();
+}
+
+void default_modules(vkdt_cuda_graph_t *g)
+{
+  const char *path[] = { "i-raw", "denoise", "hilite", "demosaic", "colour", "filmcurv", "llap" };
+  for(const char *p : path) ensure_module(g, p);
+  // the darkroom graph's llap values (bin/default-darkroom.i-raw:29-32)
+  g->mod("llap")->setf("clarity", 0, 0.2f);
+}
+
+void add_node(vkdt_cuda_graph_t *g, const char *name, const char *kernel, int wd, int ht, int dp, int fused)
+{
+  vkdt_cuda_node_info_t n;
+  n.name = tkn(name); n.kernel = tkn(kernel);
+  n.wd = wd; n.ht = ht; n.dp = dp; n.fused = fused;
+  g->nodes.push_back(n);
+}
+
+// 3x3 helpers in float with the same summation order as the shader constant folding
+void m3_mul(const double *A, const double *B, float *r)
+{
+  float a[9], b[9];
+  for(int i = 0; i < 9; i++) { a[i] = (float)A[i]; b[i] = (float)B[i]; }
+  for(int i = 0; i < 3; i++) for(int j = 0; j < 3; j++)
+  {
+    volatile float s = a[3 * i + 0] * b[0 + j];
+    s = s + a[3 * i + 1] * b[3 + j];
+    s = s + a[3 * i + 2] * b[6 + j];
+    r[3 * i + j] = s;
+  }
+}
+void m3_apply(const float *A, const float *v, float *o)
+{
+  for(int i = 0; i < 3; i++)
+  {
+    volatile float s = A[3 * i + 0] * v[0];
+    s = s + A[3 * i + 1] * v[1];
+    s = s + A[3 * i + 2] * v[2];
+    o[i] = s;
+  }
+}
+
+// colour matrices (src/pipe/modules/matrices.h, row major)
+const double M_cat16_Mi[9] = { 1.86206786, -1.01125463,  0.14918677, 0.38752654,  0.62144744, -0.00897398, -0.01584150, -0.03412294,  1.04996444 };
+const double M_cat16_M[9]  = { 0.401288, 0.650173, -0.051461, -0.250268, 1.204414,  0.045854, -0.002079, 0.048952,  0.953127 };
+const double M_rec2020_to_xyz[9] = { 0.636958048301290991, 0.144616903586208406, 0.168880975164172054, 0.26270021201126692, 0.677998071518871148, 0.0593017164698619384, 4.9999999999999999e-17, 0.0280726930490874452, 1.06098505771079066 };
+const double M_xyz_to_rec2020[9] = { 1.71665119, -0.35567078, -0.25336628, -0.66668435,  1.61648124,  0.01576855, 0.01763986, -0.04277061, 0.94210312 };
+
+// colour/main.c:219-292 commit_params (matrix path): writes p_wb back into the
+// module's params when it was derived from the camera coefficients
+void colour_commit(vkdt_cuda_graph_t *g, dev_image_t &d)
+{
+  module_t *m = g->mod("colour");
+  float p_wb[3] = { m->f("white", 0), m->f("white", 1), m->f("white", 2) };
+  if(p_wb[0] == 0.0f && p_wb[1] == 0.0f && p_wb[2] == 0.0f)
+  {
+    float w0[3] = {0}, w[] = { g->ip.whitebalance[0], g->ip.whitebalance[1], g->ip.whitebalance[2] };
+    for(int j = 0; j < 3; j++) for(int i = 0; i < 3; i++) w0[j] += g->ip.cam_to_rec2020[3 * j + i] / w[i];
+    w0[0] /= w0[1]; w0[2] /= w0[1]; w0[1] = 1.0f;
+    p_wb[0] = 1 / w0[0]; p_wb[1] = 1; p_wb[2] = 1 / w0[2];
+  }
+  if(!(p_wb[0] == p_wb[0]) || p_wb[0] == 0.0f || p_wb[1] == 0.0f || p_wb[2] == 0.0f)
+    p_wb[0] = p_wb[1] = p_wb[2] = 1.0f;
+  for(int k = 0; k < 3; k++) m->setf("white", k, p_wb[k]);
+  const float mul[3] = { p_wb[0] / p_wb[1], 1.0f, p_wb[2] / p_wb[1] };
+  d.mulw = powf(2.0f, m->f("exposure"));
+  if(m->n("matrix") == 1) for(int i = 0; i < 9; i++) d.cam[i] = g->ip.cam_to_rec2020[i];
+  else for(int i = 0; i < 9; i++) d.cam[i] = (i % 4 == 0) ? 1.0f : 0.0f;
+  m3_mul(M_cat16_M, M_rec2020_to_xyz, d.P);
+  m3_mul(M_xyz_to_rec2020, M_cat16_Mi, d.Q);
+  const float one[3] = { 1, 1, 1 };
+  float src[3], dst[3];
+  m3_apply(d.P, one, src);
+  m3_apply(d.P, mul, dst);
+  for(int k = 0; k < 3; k++) d.clscale[k] = dst[k] / src[k];
+}
+
+size_t align_up(size_t v) { return (v + 255) & ~(size_t)255; }
+
+int check_supported_params(vkdt_cuda_graph_t *g)
+{
+  if(g->mod("denoise")->f("strength") > 0.0f) return fail(VKDT_CUDA_INCOMPLETE, "denoise strength > 0 (wavelet path) is not built in this version");
+  if(g->mod("demosaic")->n("colour") != 0) return fail(VKDT_CUDA_INCOMPLETE, "demosaic colour (fixup radius) != 0 not supported");
+  if(g->mod("demosaic")->n("method") != 0) return fail(VKDT_CUDA_INCOMPLETE, "demosaic method %d not supported", g->mod("demosaic")->n("method"));
+  const int fm = g->mod("filmcurv")->n("colour");
+  if(fm != 1 && fm != 3) return fail(VKDT_CUDA_INCOMPLETE, "filmcurv colour mode %d not supported", fm);
+  if(g->mod("colour")->f("sat") != 1.0f) return fail(VKDT_CUDA_INCOMPLETE, "colour saturation != 1 not supported");
+  if(g->mod("colour")->n("clip") != 0 || g->mod("colour")->n("mode") != 0 || g->mod("colour")->n("gamut") != 0)
+    return fail(VKDT_CUDA_INCOMPLETE, "colour clip/mode/gamut not supported");
+  const int mat = g->mod("colour")->n("matrix");
+  if(mat != 0 && mat != 1) return fail(VKDT_CUDA_INCOMPLETE, "colour matrix %d not supported", mat);
+  return 0;
+}
+
+// fill the per image constants for the kernels (create_nodes push constants + commit_params uniforms)
+int fill_image(vkdt_cuda_graph_t *g, dev_image_t &d, const void *d_src, void *d_out)
+{
+  memset(&d, 0, sizeof(d));
+  d.mosaic = (const uint16_t *)d_src;
+  d.pitch = g->in_wd;
+  d.cx = (int)g->ip.crop_aabb[0]; d.cy = (int)g->ip.crop_aabb[1];
+  d.W = g->W; d.H = g->H;
+  d.filters = g->ip.filters;
+  d.black = g->ip.black[0] / 65535.0f;        // denoise/main.c:165-168
+  d.white = g->ip.white[0] / 65535.0f;
+  module_t *hl = g->mod("hilite");
+  d.hl_white = hl->f("white"); d.hl_desat = hl->f("desat"); d.hl_soft = hl->f("soft");
+  for(int k = 0; k < 3; k++) d.wb[k] = g->ip.whitebalance[k];
+  if(g->hb.empty()) { d.hl_coarse = g->at<half4>(g->hr[0].off); d.hcw = g->hr[0].w; d.hch = g->hr[0].h; }
+  else              { d.hl_coarse = g->at<half4>(g->hb[0].off); d.hcw = g->hb[0].w; d.hch = g->hb[0].h; }
+  d.fixup = g->mod("demosaic")->n("colour");
+  colour_commit(g, d);
+  module_t *fc = g->mod("filmcurv");
+  d.fc_il = fmaxf(5e-3f, fc->f("light"));
+  d.fc_k = fmaxf(1e-4f, fc->f("contrast"));
+  d.fc_bias = fc->f("bias");
+  d.fc_mode = fc->n("colour");
+  module_t *ll = g->mod("llap");
+  d.ll_sigma = ll->f("sigma"); d.ll_shadows = ll->f("shadows"); d.ll_highlights = ll->f("hilights"); d.ll_clarity = ll->f("clarity");
+  d.rgbf = g->at<half4>(g->off_rgbf);
+  d.l1 = g->at<__half>(g->lp[0].off);
+  d.l1w = g->lp[0].w; d.l1h = g->lp[0].h;
+  d.l1plane = (size_t)g->lp[0].w * g->lp[0].h;
+  d.hist = g->want_hist ? g->at<uint32_t>(g->off_hist) : nullptr;
+  if(g->debug) { d.dbg_denoise = g->at<__half>(g->off_dbg0); d.dbg_hilite = g->at<__half>(g->off_dbg1); }
+  (void)d_out;
+  return 0;
+}
+
+// the kernel sequence of one run. ev != null records timing events around each launch.
+int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out, bool timed)
+{
+  dev_image_t d;
+  int r = fill_image(g, d, d_src, d_out);
+  if(r) return r;
+  module_t *hl = g->mod("hilite");
+  const float white = hl->f("white"), desat = hl->f("desat"), soft = hl->f("soft");
+  const float wb[3] = { g->ip.whitebalance[0], g->ip.whitebalance[1], g->ip.whitebalance[2] };
+  int li = 0;
+  auto mark = [&]() -> int {
+    if(timed) { CU(cudaEventRecord(g->ev[li], s)); }
+    li++;
+    return 0;
+  };
+  if(g->want_hist) CU(cudaMemsetAsync(g->at<uint32_t>(g->off_hist), 0, 257 * sizeof(uint32_t), s));
+  if((r = mark())) return r;
+  // 1. noop + hilite half + first hilite reduce
+  dev_hilite_k1_t k1;
+  memset(&k1, 0, sizeof(k1));
+  k1.mosaic = d.mosaic; k1.pitch = d.pitch; k1.cx = d.cx; k1.cy = d.cy; k1.W = d.W; k1.H = d.H;
+  k1.filters = d.filters; k1.black = d.black; k1.white = d.white; k1.hl_white = white; k1.hl_desat = desat;
+  for(int k = 0; k < 3; k++) k1.wb[k] = wb[k];
+  k1.hw = g->hw; k1.hh = g->hh;
+  k1.r1 = g->at<half4>(g->hr[0].off); k1.s1w = g->hr[0].w; k1.s1h = g->hr[0].h;
+  CU(launch_hilite_k1(k1, s));
+  if((r = mark())) return r;
+  // 2. hilite reduce levels 2..L
+  for(size_t l = 1; l < g->hr.size(); l++)
+  {
+    CU(launch_hilite_reduce(g->at<half4>(g->hr[l - 1].off), g->hr[l - 1].w, g->hr[l - 1].h,
+        g->at<half4>(g->hr[l].off), g->hr[l].w, g->hr[l].h, white, desat, wb, s));
+    if((r = mark())) return r;
+  }
+  // 3. hilite assemble B[L-1] .. B[1]
+  for(int l = (int)g->hb.size() - 1; l >= 0; l--)
+  {
+    const level_t &f = g->hr[l];
+    const level_t &c = (l + 1 < (int)g->hb.size()) ? g->hb[l + 1] : g->hr[l + 1];
+    CU(launch_hilite_assemble(g->at<half4>(f.off), f.w, f.h, g->at<half4>(c.off), c.w, c.h,
+        g->at<half4>(g->hb[l].off), white, soft, s));
+    if((r = mark())) return r;
+  }
+  // 4. fused develop pass
+  CU(launch_develop(d, s));
+  if((r = mark())) return r;
+  // 5. llap reduce levels 2..nl-1
+  for(size_t l = 1; l < g->lp.size(); l++)
+  {
+    const level_t &a = g->lp[l - 1], &b = g->lp[l];
+    CU(launch_llap_reduce(g->at<__half>(a.off), a.w, a.h, (size_t)a.w * a.h, g->at<__half>(b.off), b.w, b.h, (size_t)b.w * b.h, s));
+    if((r = mark())) return r;
+  }
+  // 6. llap assemble A[nl-2] .. A[1]
+  for(int j = (int)g->la.size(); j >= 1; j--)
+  { // A[j] at level j (lp index j-1), l1 = level j+1 (lp index j)
+    const level_t &l0 = g->lp[j - 1], &l1 = g->lp[j];
+    const bool first = (j == (int)g->la.size());
+    const __half *coarse = first ? nullptr : g->at<__half>(g->la[j].off);
+    CU(launch_llap_assemble(coarse, first ? 1 : 0, g->at<__half>(l0.off), l0.w, l0.h, (size_t)l0.w * l0.h,
+        g->at<__half>(l1.off), l1.w, l1.h, (size_t)l1.w * l1.h, g->at<__half>(g->la[j - 1].off), s));
+    if((r = mark())) return r;
+  }
+  // 7. level 0 assemble + llap colour
+  dev_llap_k3_t k3;
+  k3.rgbf = d.rgbf; k3.W = g->W; k3.H = g->H;
+  k3.l1 = d.l1; k3.l1w = d.l1w; k3.l1h = d.l1h; k3.l1plane = d.l1plane;
+  k3.coarse = g->la.empty() ? d.l1 + 10 * d.l1plane : g->at<__half>(g->la[0].off);
+  k3.ll_sigma = d.ll_sigma; k3.ll_shadows = d.ll_shadows; k3.ll_highlights = d.ll_highlights; k3.ll_clarity = d.ll_clarity;
+  k3.out = (half4 *)d_out;
+  CU(launch_llap_final(k3, s));
+  if((r = mark())) return r;
+  return 0;
+}
+
+} // namespace
+
+// ================================================================== C-ABI
+
+#pragma GCC visibility push(default)
+extern "C" {
+
+const char *vkdt_cuda_last_error(void) { return g_err; }
+
+int vkdt_cuda_init(int device_id, uint32_t flags)
+{
+  (void)flags;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if(e != cudaSuccess || n <= 0) return fail(VKDT_CUDA_ERROR_INITIALIZATION_FAILED, "no CUDA device: %s", cudaGetErrorString(e));
+  if(device_id < 0 || device_id >= n) return fail(VKDT_CUDA_ERROR_INITIALIZATION_FAILED, "device %d out of range (%d)", device_id, n);
+  cudaDeviceProp prop;
+  CU(cudaGetDeviceProperties(&prop, device_id));
+  if(prop.major != 10 || prop.minor != 3)
+    return fail(VKDT_CUDA_ERROR_INITIALIZATION_FAILED, "device %d is sm_%d%d, the library is built for sm_103a", device_id, prop.major, prop.minor);
+  CU(cudaSetDevice(device_id));
+  g_device = device_id;
+  return VKDT_CUDA_SUCCESS;
+}
+
+void vkdt_cuda_cleanup(void) { g_device = -1; }
+
+int vkdt_cuda_supports(dt_token_t name, dt_token_t kernel)
+{
+  static const char *sup[][2] = {
+    { "denoise", "noop" }, { "hilite", "half" }, { "hilite", "reduce" }, { "hilite", "assemble" }, { "hilite", "doub" },
+    { "demosaic", "down" }, { "demosaic", "gauss" }, { "demosaic", "splat" }, { "demosaic", "fix" },
+    { "colour", "main" }, { "filmcurv", "main" }, { "OpenDRT", "hist" },
+    { "llap", "curve" }, { "llap", "reduce" }, { "llap", "assemble" }, { "llap", "colour" } };
+  for(auto &s : sup) if(tkn(s[0]) == name && tkn(s[1]) == kernel) return 1;
+  return 0;
+}
+
+int vkdt_cuda_graph_create(vkdt_cuda_graph_t **graph)
+{
+  if(!graph) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "null graph pointer");
+  vkdt_cuda_graph_t *g = new (std::nothrow) vkdt_cuda_graph_t();
+  if(!g) return fail(VKDT_CUDA_ERROR_OUT_OF_HOST_MEMORY, "out of host memory");
+  memset(&g->ip, 0, sizeof(g->ip));
+  default_modules(g);
+  *graph = g;
+  return VKDT_CUDA_SUCCESS;
+}
+
+static void release(vkdt_cuda_graph_t *g)
+{
+  if(g->gexec) cudaGraphExecDestroy(g->gexec);
+  g->gexec = nullptr;
+  for(auto e : g->ev) cudaEventDestroy(e);
+  g->ev.clear();
+  if(g->done) cudaEventDestroy(g->done);
+  g->done = nullptr;
+  if(g->stream) cudaStreamDestroy(g->stream);
+  g->stream = nullptr;
+  if(g->arena) cudaFree(g->arena);
+  g->arena = nullptr;
+  if(g->h_src) cudaFreeHost(g->h_src);
+  if(g->h_sink) cudaFreeHost(g->h_sink);
+  g->h_src = g->h_sink = nullptr;
+  g->allocated = false;
+}
+
+void vkdt_cuda_graph_destroy(vkdt_cuda_graph_t *g)
+{
+  if(!g) return;
+  release(g);
+  delete g;
+}
+
+int vkdt_cuda_graph_read_config(vkdt_cuda_graph_t *g, const char *cfg, size_t len)
+{
+  if(!g || !cfg) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "null argument");
+  std::string text(cfg, len);
+  g->modules.clear(); g->unsupported.clear(); g->connects.clear();
+  size_t pos = 0;
+  int lineno = 0;
+  bool seen_llap_clarity = false;
+  while(pos <= text.size())
+  {
+    size_t e = text.find('\n', pos);
+    if(e == std::string::npos) e = text.size();
+    std::string line = text.substr(pos, e - pos);
+    pos = e + 1;
+    lineno++;
+    while(!line.empty() && (line.back() == '\r' || line.back() == ' ')) line.pop_back();
+    if(line.empty() || line[0] == '#') continue;
+    std::vector<std::string> f;
+    size_t a = 0;
+    while(true)
+    {
+      size_t c = line.find(':', a);
+      if(c == std::string::npos) { f.push_back(line.substr(a)); break; }
+      f.push_back(line.substr(a, c - a));
+      a = c + 1;
+    }
+    if(f[0] == "module" && f.size() >= 3)
+    {
+      const dt_token_t nm = tkn(f[1].c_str());
+      const module_def_t *d = find_def(nm);
+      if(!d)
+      {
+        if(std::find(g->unsupported.begin(), g->unsupported.end(), nm) == g->unsupported.end()) g->unsupported.push_back(nm);
+        continue;
+      }
+      if(g->mod(f[1].c_str())) continue; // one instance per module on the path
+      module_t m;
+      m.init(d, nm, tkn(f[2].c_str()));
+      g->modules.push_back(m);
+    }
+    else if(f[0] == "connect" && f.size() >= 7)
+    {
+      g->connects.push_back({ f[1] + ":" + f[2] + ":" + f[3], f[4] + ":" + f[5] + ":" + f[6] });
+    }
+    else if(f[0] == "param" && f.size() >= 5)
+    {
+      module_t *m = g->mod(f[1].c_str());
+      if(!m) continue; // parameter of a module outside the path
+      int cnt = 0; char type = 0;
+      const int off = m->offset(tkn(f[3].c_str()), &cnt, &type);
+      if(off < 0) continue;
+      for(int i = 0; i < cnt && 4 + i < (int)f.size(); i++)
+      {
+        uint32_t u;
+        if(type == 'i') { int32_t v = (int32_t)strtol(f[4 + i].c_str(), 0, 10); memcpy(&u, &v, 4); }
+        else { float v = strtof(f[4 + i].c_str(), 0); memcpy(&u, &v, 4); }
+        m->param[off + i] = u;
+      }
+      if(f[1] == "llap" && f[3] == "clarity") seen_llap_clarity = true;
+    }
+    else if(f[0] == "frames" || f[0] == "fps" || f[0] == "feedback" || f[0] == "keyframe" || f[0] == "paramsub")
+      continue;
+    else return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "cfg line %d not understood: %s", lineno, line.c_str());
+  }
+  (void)seen_llap_clarity;
+  // the path must be present and chained
+  const char *path[] = { "i-raw", "denoise", "hilite", "demosaic", "colour", "filmcurv", "llap" };
+  for(const char *p : path) if(!g->mod(p)) return fail(VKDT_CUDA_INCOMPLETE, "module %s missing from the cfg", p);
+  auto connected = [&](const char *from, const char *to) {
+    for(auto &c : g->connects)
+    {
+      const std::string a = c.first.substr(0, c.first.find(':')), b = c.second.substr(0, c.second.find(':'));
+      if(a == from && b == to) return true;
+    }
+    return false;
+  };
+  const bool ok = connected("i-raw", "denoise") && connected("denoise", "hilite") && connected("hilite", "demosaic")
+      && (connected("demosaic", "colour") || (connected("demosaic", "crop") && connected("crop", "colour")))
+      && connected("colour", "filmcurv") && connected("filmcurv", "llap");
+  if(!ok) return fail(VKDT_CUDA_INCOMPLETE, "the cfg does not chain i-raw -> denoise -> hilite -> demosaic -> [crop] -> colour -> filmcurv -> llap");
+  g->graph_dirty = true;
+  return VKDT_CUDA_SUCCESS;
+}
+
+int vkdt_cuda_graph_unsupported(vkdt_cuda_graph_t *g, dt_token_t *names, int max)
+{
+  if(!g) return 0;
+  for(int i = 0; i < (int)g->unsupported.size() && i < max; i++) if(names) names[i] = g->unsupported[i];
+  return (int)g->unsupported.size();
+}
+
+static int param_access(vkdt_cuda_graph_t *g, dt_token_t module, dt_token_t inst, dt_token_t param, size_t bytes, int *off)
+{
+  if(!g) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "null graph");
+  module_t *m = nullptr;
+  for(auto &mm : g->modules) if(mm.name == module && (inst == 0 || mm.inst == inst)) m = &mm;
+  if(!m) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "no module %s:%s", tstr(module).c_str(), tstr(inst).c_str());
+  int cnt = 0;
+  *off = m->offset(param, &cnt, 0);
+  if(*off < 0) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "module %s has no parameter %s", tstr(module).c_str(), tstr(param).c_str());
+  if(bytes != (size_t)cnt * 4) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "parameter %s wants %d bytes", tstr(param).c_str(), cnt * 4);
+  return 0;
+}
+
+int vkdt_cuda_graph_set_param(vkdt_cuda_graph_t *g, dt_token_t module, dt_token_t inst, dt_token_t param, const void *value, size_t bytes)
+{
+  int off, r = param_access(g, module, inst, param, bytes, &off);
+  if(r) return r;
+  for(auto &m : g->modules) if(m.name == module && (inst == 0 || m.inst == inst)) memcpy(&m.param[off], value, bytes);
+  g->graph_dirty = true;
+  return VKDT_CUDA_SUCCESS;
+}
+
+int vkdt_cuda_graph_get_param(vkdt_cuda_graph_t *g, dt_token_t module, dt_token_t inst, dt_token_t param, void *value, size_t bytes)
+{
+  int off, r = param_access(g, module, inst, param, bytes, &off);
+  if(r) return r;
+  for(auto &m : g->modules) if(m.name == module && (inst == 0 || m.inst == inst)) { memcpy(value, &m.param[off], bytes); break; }
+  return VKDT_CUDA_SUCCESS;
+}
+
+int vkdt_cuda_graph_set_input(vkdt_cuda_graph_t *g, int wd, int ht, const vkdt_cuda_img_param_t *ip)
+{
+  if(!g || !ip) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "null argument");
+  if(wd <= 0 || ht <= 0) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "bad input size %dx%d", wd, ht);
+  g->in_wd = wd; g->in_ht = ht; g->ip = *ip;
+  // i-raw/main.c:214-218 normalises the white balance to green
+  if(g->ip.whitebalance[1] > 0.0f && g->ip.whitebalance[1] != 1.0f)
+  {
+    g->ip.whitebalance[0] /= g->ip.whitebalance[1];
+    g->ip.whitebalance[2] /= g->ip.whitebalance[1];
+    g->ip.whitebalance[3] /= g->ip.whitebalance[1];
+    g->ip.whitebalance[1] = 1.0f;
+  }
+  g->have_input = true;
+  g->graph_dirty = true;
+  return VKDT_CUDA_SUCCESS;
+}
+
+int vkdt_cuda_graph_set_output_size(vkdt_cuda_graph_t *g, int wd, int ht)
+{
+  if(!g) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "null graph");
+  g->req_wd = wd; g->req_ht = ht;
+  return VKDT_CUDA_SUCCESS;
+}
+
+int vkdt_cuda_graph_set_llap_levels(vkdt_cuda_graph_t *g, int levels)
+{
+  if(!g || levels < 0 || levels == 1 || levels > 12) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "llap levels %d", levels);
+  g->llap_levels_req = levels;
+  return VKDT_CUDA_SUCCESS;
+}
+
+int vkdt_cuda_graph_set_timing(vkdt_cuda_graph_t *g, int enable) { if(!g) return -11; g->timing = enable != 0; return 0; }
+int vkdt_cuda_graph_set_hist(vkdt_cuda_graph_t *g, int enable) { if(!g) return -11; g->want_hist = enable != 0; g->graph_dirty = true; return 0; }
+int vkdt_cuda_graph_set_debug(vkdt_cuda_graph_t *g, int enable) { if(!g) return -11; g->debug = enable != 0; return 0; }
+
+int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
+{
+  if(!g) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "null graph");
+  if(!g->have_input) return fail(VKDT_CUDA_INCOMPLETE, "no input set");
+  int r = check_supported_params(g);
+  if(r) return r;
+  const uint32_t filters = g->ip.filters;
+  if(filters == 0) return fail(VKDT_CUDA_INCOMPLETE, "rgb input: the path starts on a mosaic");
+  if(filters == 9) return fail(VKDT_CUDA_INCOMPLETE, "x-trans mosaics are not built in this version");
+  g->nodes.clear();
+  // denoise modify_roi_out: output = crop window
+  const uint32_t *b = g->ip.crop_aabb;
+  if(b[2] <= b[0] || b[3] <= b[1] || (int)b[2] > g->in_wd || (int)b[3] > g->in_ht)
+    return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "crop window outside the mosaic");
+  g->W = (int)(b[2] - b[0]); g->H = (int)(b[3] - b[1]);
+  if((g->W & 1) || (g->H & 1) || (b[0] & 1) || (b[1] & 1)) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "bayer crop window must be even");
+  if(g->W < 16 || g->H < 16) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "image smaller than 16x16");
+  g->hw = g->W / 2; g->hh = g->H / 2;
+  if(g->req_wd > 0 && (g->req_wd != g->W || g->req_ht != g->H))
+    return fail(VKDT_CUDA_INCOMPLETE, "reduced output size (half-size demosaic + resample) is not built in this version");
+  g->out_w = g->W; g->out_h = g->H;
+
+  // node lists as the modules' create_nodes emit them
+  int fused = 0;
+  add_node(g, "denoise", "noop", g->W, g->H, 1, -1);
+  // hilite/main.c:5-90
+  add_node(g, "hilite", "half", g->hw, g->hh, 1, -1);
+  add_node(g, "hilite", "doub", g->hw, g->hh, 1, -1);
+  g->hr.clear(); g->hb.clear();
+  {
+    int rw = (g->hw - 1) / 2 + 1, rh = (g->hh - 1) / 2 + 1;
+    const int max_nl = 15;
+    for(int l = 1; l < max_nl; l++)
+    {
+      level_t lv; lv.w = rw; lv.h = rh;
+      g->hr.push_back(lv);
+      rw = (rw - 1) / 2 + 1; rh = (rh - 1) / 2 + 1;
+      if(rw <= 1 || rh <= 1 || l + 1 == max_nl) break;
+    }
+    for(size_t l = 0; l + 1 < g->hr.size(); l++) g->hb.push_back(g->hr[l]);
+  }
+  // demosaic/main.c:159-202 (gaussian splats, full size)
+  add_node(g, "demosaic", "down", g->hw, g->hh, 1, -1);
+  add_node(g, "demosaic", "gauss", g->hw, g->hh, 1, -1);
+  add_node(g, "demosaic", "splat", g->W, g->H, 1, -1);
+  add_node(g, "demosaic", "fix", g->W, g->H, 1, -1);
+  add_node(g, "colour", "main", g->W, g->H, 1, -1);
+  add_node(g, "OpenDRT", "hist", (g->W + 15) / 16 * 8, (g->H + 15) / 16 * 8, 1, -1);
+  add_node(g, "filmcurv", "main", g->W, g->H, 1, -1);
+  // llap/main.c:6-106
+  add_node(g, "llap", "curve", g->W, g->H, 1, -1);
+  g->lp.clear(); g->la.clear();
+  {
+    int rw = (g->W - 1) / 2 + 1, rh = (g->H - 1) / 2 + 1;
+    int nl = 12;
+    for(int l = 1; l < nl; l++)
+    {
+      level_t lv; lv.w = rw; lv.h = rh;
+      g->lp.push_back(lv);
+      rw = (rw - 1) / 2 + 1; rh = (rh - 1) / 2 + 1;
+      if(rw <= 1 || rh <= 1) { nl = l + 1; break; }
+      if(g->llap_levels_req > 0 && l + 1 == g->llap_levels_req) { nl = l + 1; break; }
+    }
+    g->nl = nl;
+    for(int j = 1; j <= nl - 2; j++) g->la.push_back(g->lp[j - 1]);
+  }
+  // the fused launches and which nodes they compute
+  g->launches.clear();
+  auto launch = [&](const char *n, const char *k) { g->launches.push_back({ tkn(n), tkn(k) }); return (int)g->launches.size() - 1; };
+  const int L_k1 = launch("hilite", "reduce");
+  std::vector<int> L_hr, L_ha, L_lr, L_la;
+  for(size_t l = 1; l < g->hr.size(); l++) L_hr.push_back(launch("hilite", "reduce"));
+  for(size_t l = 0; l < g->hb.size(); l++) L_ha.push_back(launch("hilite", "assemble"));
+  const int L_dev = launch("demosaic", "fix");
+  for(size_t l = 1; l < g->lp.size(); l++) L_lr.push_back(launch("llap", "reduce"));
+  for(size_t j = 0; j < g->la.size(); j++) L_la.push_back(launch("llap", "assemble"));
+  const int L_fin = launch("llap", "colour");
+  (void)fused;
+  for(auto &n : g->nodes)
+  {
+    if(n.name == tkn("denoise") || n.kernel == tkn("doub") || n.name == tkn("demosaic") || n.name == tkn("colour")
+        || n.name == tkn("OpenDRT") || n.name == tkn("filmcurv") || n.kernel == tkn("curve")) n.fused = L_dev;
+    if(n.name == tkn("hilite") && n.kernel == tkn("half")) n.fused = L_k1;
+  }
+  // per level nodes (reduce and assemble pairs in create_nodes order)
+  for(size_t l = 0; l < g->hr.size(); l++)
+  {
+    add_node(g, "hilite", "reduce", g->hr[l].w, g->hr[l].h, 1, l == 0 ? L_k1 : L_hr[l - 1]);
+    const int fw = l == 0 ? g->hw : g->hr[l - 1].w, fh = l == 0 ? g->hh : g->hr[l - 1].h;
+    add_node(g, "hilite", "assemble", fw, fh, 1, l == 0 ? L_dev : L_ha[l - 1]);
+  }
+  for(size_t l = 0; l < g->lp.size(); l++)
+  {
+    add_node(g, "llap", "reduce", g->lp[l].w, g->lp[l].h, 11, l == 0 ? L_dev : L_lr[l - 1]);
+    const int fw = l == 0 ? g->W : g->lp[l - 1].w, fh = l == 0 ? g->H : g->lp[l - 1].h;
+    add_node(g, "llap", "assemble", fw, fh, 1, l == 0 ? L_fin : L_la[l - 1]);
+  }
+  add_node(g, "llap", "colour", g->W, g->H, 1, L_fin);
+
+  g->nodes_ready = true;
+  return VKDT_CUDA_SUCCESS;
+}
+
+int vkdt_cuda_graph_alloc(vkdt_cuda_graph_t *g, uint64_t *device_bytes)
+{
+  if(!g) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "null graph");
+  if(g_device < 0) return fail(VKDT_CUDA_ERROR_INITIALIZATION_FAILED, "vkdt_cuda_init was not called");
+  release(g);
+  int r = vkdt_cuda_graph_create_nodes(g);
+  if(r) return r;
+  // memory plan (one arena)
+  size_t off = 0;
+  auto take = [&](size_t bytes) { const size_t o = off; off = align_up(off + bytes); return o; };
+  g->src_bytes = (size_t)g->in_wd * g->in_ht * 2;
+  g->sink_bytes = (size_t)g->out_w * g->out_h * 8;
+  g->off_src = take(g->src_bytes);
+  for(auto &l : g->hr) l.off = take((size_t)l.w * l.h * 8);
+  for(auto &l : g->hb) l.off = take((size_t)l.w * l.h * 8);
+  g->off_rgbf = take((size_t)g->W * g->H * 8);
+  for(auto &l : g->lp) l.off = take((size_t)l.w * l.h * 2 * 11);
+  for(auto &l : g->la) l.off = take((size_t)l.w * l.h * 2);
+  g->off_out = take(g->sink_bytes);
+  g->off_hist = take(257 * 4);
+  if(g->debug) { g->off_dbg0 = take((size_t)g->W * g->H * 2); g->off_dbg1 = take((size_t)g->W * g->H * 2); }
+  g->arena_bytes = off;
+  CU(cudaMalloc((void **)&g->arena, g->arena_bytes));
+  CU(cudaMemset(g->arena, 0, g->arena_bytes));
+  CU(cudaMallocHost(&g->h_src, g->src_bytes));
+  CU(cudaMallocHost(&g->h_sink, g->sink_bytes));
+  CU(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+  CU(cudaEventCreateWithFlags(&g->done, cudaEventDisableTiming));
+  g->ev.resize(g->launches.size() + 1);
+  for(auto &e : g->ev) CU(cudaEventCreate(&e));
+  g->times.assign(g->launches.size(), 0.0f);
+  g->allocated = true;
+  g->graph_dirty = true;
+  if(device_bytes) *device_bytes = g->arena_bytes;
+  return VKDT_CUDA_SUCCESS;
+}
+
+int vkdt_cuda_graph_node_count(vkdt_cuda_graph_t *g) { return g ? (int)g->nodes.size() : 0; }
+int vkdt_cuda_graph_node(vkdt_cuda_graph_t *g, int i, vkdt_cuda_node_info_t *info)
+{
+  if(!g || !info || i < 0 || i >= (int)g->nodes.size()) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "node %d", i);
+  *info = g->nodes[i];
+  return 0;
+}
+int vkdt_cuda_graph_output_size(vkdt_cuda_graph_t *g, int *wd, int *ht)
+{
+  if(!g || !g->allocated) return fail(VKDT_CUDA_INCOMPLETE, "graph not allocated");
+  if(wd) *wd = g->out_w;
+  if(ht) *ht = g->out_h;
+  return 0;
+}
+
+void *vkdt_cuda_graph_map_source(vkdt_cuda_graph_t *g, size_t *bytes)
+{
+  if(!g || !g->allocated) return nullptr;
+  if(bytes) *bytes = g->src_bytes;
+  return g->h_src;
+}
+void *vkdt_cuda_graph_map_sink(vkdt_cuda_graph_t *g, size_t *bytes)
+{
+  if(!g || !g->allocated) return nullptr;
+  if(bytes) *bytes = g->sink_bytes;
+  return g->h_sink;
+}
+int vkdt_cuda_graph_device_buffers(vkdt_cuda_graph_t *g, void **d_source, void **d_sink)
+{
+  if(!g || !g->allocated) return fail(VKDT_CUDA_INCOMPLETE, "graph not allocated");
+  if(d_source) *d_source = g->arena + g->off_src;
+  if(d_sink) *d_sink = g->arena + g->off_out;
+  return 0;
+}
+
+static int run_kernels(vkdt_cuda_graph_t *g, cudaStream_t s, const void *src, void *dst)
+{
+  const bool own_buffers = src == g->arena + g->off_src && dst == g->arena + g->off_out;
+  if(g->timing || !g->use_graph || !own_buffers) return enqueue(g, s, src, dst, g->timing);
+  if(g->graph_dirty || !g->gexec)
+  {
+    if(g->gexec) { cudaGraphExecDestroy(g->gexec); g->gexec = nullptr; }
+    cudaGraph_t graph;
+    CU(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    const int r = enqueue(g, s, src, dst, false);
+    cudaGraph_t cap = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(s, &cap);
+    if(r) { if(cap) cudaGraphDestroy(cap); return r; }
+    CU(e);
+    graph = cap;
+    cudaError_t ie = cudaGraphInstantiate(&g->gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    CU(ie);
+    g->graph_dirty = false;
+  }
+  CU(cudaGraphLaunch(g->gexec, s));
+  return 0;
+}
+
+int vkdt_cuda_graph_run(vkdt_cuda_graph_t *g, void *stream, uint32_t flags)
+{
+  if(!g || !g->allocated) return fail(VKDT_CUDA_INCOMPLETE, "graph not allocated");
+  cudaStream_t s = stream ? (cudaStream_t)stream : g->stream;
+  if(flags & VKDT_CUDA_RUN_UPLOAD_SOURCE)
+    CU(cudaMemcpyAsync(g->arena + g->off_src, g->h_src, g->src_bytes, cudaMemcpyHostToDevice, s));
+  if(g->timing) CU(cudaEventRecord(g->ev[0], s));
+  int r = run_kernels(g, s, g->arena + g->off_src, g->arena + g->off_out);
+  if(r) return r;
+  if(flags & VKDT_CUDA_RUN_DOWNLOAD_SINK)
+    CU(cudaMemcpyAsync(g->h_sink, g->arena + g->off_out, g->sink_bytes, cudaMemcpyDeviceToHost, s));
+  CU(cudaEventRecord(g->done, s));
+  if(flags & VKDT_CUDA_RUN_WAIT_DONE) return vkdt_cuda_graph_wait(g, 600000);
+  return 0;
+}
+
+int vkdt_cuda_graph_develop(vkdt_cuda_graph_t *g, const void *d_mosaic, void *d_rgba, void *stream)
+{
+  if(!g || !g->allocated) return fail(VKDT_CUDA_INCOMPLETE, "graph not allocated");
+  if(!d_mosaic || !d_rgba) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "null device buffer");
+  cudaStream_t s = stream ? (cudaStream_t)stream : g->stream;
+  int r = run_kernels(g, s, d_mosaic, d_rgba);
+  if(r) return r;
+  CU(cudaEventRecord(g->done, s));
+  return 0;
+}
+
+int vkdt_cuda_graph_wait(vkdt_cuda_graph_t *g, uint32_t timeout_ms)
+{
+  if(!g || !g->allocated) return fail(VKDT_CUDA_INCOMPLETE, "graph not allocated");
+  const auto t0 = std::chrono::steady_clock::now();
+  int spin = 0;
+  while(true)
+  {
+    const cudaError_t e = cudaEventQuery(g->done);
+    if(e == cudaSuccess) break;
+    if(e != cudaErrorNotReady) return fail(cuda_code(e), "device error: %s", cudaGetErrorString(e));
+    const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if(ms > timeout_ms) return fail(VKDT_CUDA_TIMEOUT, "wait timed out after %u ms", timeout_ms);
+    if(++spin > 64) std::this_thread::sleep_for(std::chrono::microseconds(20));
+  }
+  if(g->timing)
+  {
+    for(size_t i = 0; i < g->launches.size(); i++)
+    {
+      float ms = 0.0f;
+      CU(cudaEventElapsedTime(&ms, g->ev[i], g->ev[i + 1]));
+      g->times[i] = ms;
+    }
+  }
+  return 0;
+}
+
+int vkdt_cuda_graph_query_times(vkdt_cuda_graph_t *g, float *ms, dt_token_t *names, dt_token_t *kernels, int max)
+{
+  if(!g || !g->allocated) return 0;
+  const int n = (int)g->launches.size();
+  for(int i = 0; i < n && i < max; i++)
+  {
+    if(ms) ms[i] = g->times[i];
+    if(names) names[i] = g->launches[i].name;
+    if(kernels) kernels[i] = g->launches[i].kernel;
+  }
+  return n;
+}
+
+int vkdt_cuda_graph_hist(vkdt_cuda_graph_t *g, uint32_t *hist257)
+{
+  if(!g || !g->allocated || !g->want_hist) return fail(VKDT_CUDA_INCOMPLETE, "histogram not enabled");
+  CU(cudaMemcpy(hist257, g->arena + g->off_hist, 257 * 4, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+int vkdt_cuda_hist_rgba_f16(const void *d_rgba, int wd, int ht, uint32_t *d_hist, void *stream)
+{
+  if(!d_rgba || !d_hist || wd <= 0 || ht <= 0) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "bad histogram arguments");
+  CU(launch_hist_rgba((const half4 *)d_rgba, wd, ht, d_hist, (cudaStream_t)stream));
+  return 0;
+}
+
+int vkdt_cuda_graph_debug_stage(vkdt_cuda_graph_t *g, int stage, float *out, size_t count)
+{
+  if(!g || !g->allocated) return fail(VKDT_CUDA_INCOMPLETE, "graph not allocated");
+  CU(cudaStreamSynchronize(g->stream));
+  const size_t npx = (size_t)g->W * g->H;
+  if(stage == 0 || stage == 1)
+  {
+    if(!g->debug) return fail(VKDT_CUDA_INCOMPLETE, "debug stages not enabled");
+    if(count < npx) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "buffer too small");
+    std::vector<__half> h(npx);
+    CU(cudaMemcpy(h.data(), g->arena + (stage == 0 ? g->off_dbg0 : g->off_dbg1), npx * 2, cudaMemcpyDeviceToHost));
+    for(size_t i = 0; i < npx; i++) out[i] = __half2float(h[i]);
+    return 0;
+  }
+  if(stage == 2)
+  {
+    if(count < npx * 4) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "buffer too small");
+    std::vector<__half> h(npx * 4);
+    CU(cudaMemcpy(h.data(), g->arena + g->off_rgbf, npx * 8, cudaMemcpyDeviceToHost));
+    for(size_t i = 0; i < npx * 4; i++) out[i] = __half2float(h[i]);
+    return 0;
+  }
+  return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "stage %d", stage);
+}
+
+// ---------------------------------------------------------------- scenes
+
+static void scene_layout(const vkdt_cuda_scene_t *sc, scene_layout_t *s)
+{
+  memset(s, 0, sizeof(*s));
+  s->wd = sc->wd; s->ht = sc->ht; s->seed = sc->seed; s->image_id = sc->image_id; s->filters = sc->filters;
+  s->black = sc->black; s->white = sc->white; s->noise_a = sc->noise_a; s->noise_b = sc->noise_b;
+  for(int k = 0; k < 3; k++) s->iwb[k] = 1.0f / sc->wb[k];
+  s->pan_x = sc->pan_x; s->pan_y = sc->pan_y;
+  scene_rng_t r;
+  rng_init(&r, sc->seed, sc->image_id, 0xA11CEu, 0x5CE4Eu);
+  const float W = (float)sc->wd, H = (float)sc->ht;
+  for(int c = 0; c < 3; c++)
+  {
+    s->grad[c][0] = 0.05f + 0.55f * rng_next(&r);
+    for(int k = 1; k < 6; k++) s->grad[c][k] = 0.4f * (rng_next(&r) - 0.5f);
+  }
+  for(int i = 0; i < SCENE_NRECT; i++)
+  {
+    const float w = (0.02f + 0.23f * rng_next(&r)) * W, h = (0.02f + 0.23f * rng_next(&r)) * W;
+    const float x0 = rng_next(&r) * (W - w), y0 = rng_next(&r) * fmaxf(H - h, 1.0f);
+    float *q = s->rect[i];
+    q[0] = x0; q[1] = y0; q[2] = x0 + w; q[3] = y0 + h;
+    for(int c = 0; c < 3; c++) q[4 + c] = 0.02f + 0.93f * rng_next(&r);
+  }
+  for(int i = 0; i < SCENE_NGRAT; i++)
+  {
+    const float w = (0.05f + 0.2f * rng_next(&r)) * W, h = (0.05f + 0.2f * rng_next(&r)) * H;
+    const float x0 = rng_next(&r) * (W - w), y0 = rng_next(&r) * (H - h);
+    float *q = s->grat[i];
+    q[0] = x0; q[1] = y0; q[2] = x0 + w; q[3] = y0 + h;
+    q[4] = 0.05f + 0.4f * rng_next(&r);
+    const float th = 6.28318530718f * rng_next(&r);
+    q[5] = cosf(th); q[6] = sinf(th);
+    q[7] = 6.28318530718f * rng_next(&r);
+    q[8] = 0.1f + 0.4f * rng_next(&r);
+  }
+  // brightest 10% of the scene luminance on a coarse sample
+  std::vector<float> lum;
+  for(int j = 0; j < 96; j++) for(int i = 0; i < 96; i++)
+    lum.push_back(scene_luma(s, (i + 0.5f) / 96.0f * W + s->pan_x, (j + 0.5f) / 96.0f * H + s->pan_y));
+  std::sort(lum.begin(), lum.end());
+  s->clip_thr = lum[(size_t)(0.9 * lum.size())];
+}
+
+int vkdt_cuda_scene_generate(const vkdt_cuda_scene_t *sc, void *d_mosaic, void *stream)
+{
+  if(!sc || !d_mosaic || sc->wd <= 0 || sc->ht <= 0) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "bad scene");
+  scene_layout_t s;
+  scene_layout(sc, &s);
+  cudaStream_t st = (cudaStream_t)stream;
+  scene_layout_t *d = nullptr;
+  CU(cudaMalloc((void **)&d, sizeof(s)));
+  cudaError_t e = cudaMemcpyAsync(d, &s, sizeof(s), cudaMemcpyHostToDevice, st);
+  if(e == cudaSuccess) e = launch_scene(d, s.wd, s.ht, (uint16_t *)d_mosaic, st);
+  if(e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(d);
+  CU(e);
+  return 0;
+}
+
+int vkdt_cuda_scene_generate_host(const vkdt_cuda_scene_t *sc, uint16_t *mosaic)
+{
+  if(!sc || !mosaic || sc->wd <= 0 || sc->ht <= 0) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "bad scene");
+  scene_layout_t s;
+  scene_layout(sc, &s);
+  const int nt = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+  std::vector<std::thread> th;
+  for(int t = 0; t < nt; t++)
+    th.emplace_back([&, t]() {
+      for(int y = t; y < s.ht; y += nt) for(int x = 0; x < s.wd; x++) mosaic[(size_t)y * s.wd + x] = scene_pixel(&s, x, y);
+    });
+  for(auto &t : th) t.join();
+  return 0;
+}
+
+} // extern "C"
+#pragma GCC visibility pop

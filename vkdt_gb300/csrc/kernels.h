@@ -1,0 +1,93 @@
+// Launch interface between the host graph (graph.cpp) and the CUDA kernels.
+// Plain structs of pointers and scalars; no torch types.
+#pragma once
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+#include <stddef.h>
+
+struct half4;
+
+// per image constants of the path, filled by the host from the module
+// parameters and the image metadata (the uniforms and push constants the
+// modules' commit_params / create_nodes would upload)
+struct dev_image_t
+{
+  // mosaic (source) and its active window
+  const uint16_t *mosaic;
+  int pitch;            // elements per mosaic row
+  int cx, cy;           // crop offset (denoise push.crop.xy)
+  int W, H;             // denoise/hilite output size
+  uint32_t filters;
+  // denoise noop, channel 0, unorm units
+  float black, white;
+  // hilite/params
+  float hl_white, hl_desat, hl_soft;
+  float wb[3];
+  // hilite pyramid: coarse input of the level 0 assemble (B_1 or r_1)
+  const half4 *hl_coarse;
+  int hcw, hch;
+  // demosaic/params
+  int fixup;
+  // colour: camera matrix, cat16 matrices and per channel cone scale, exposure
+  float cam[9], P[9], Q[9], clscale[3], mulw;
+  // filmcurv
+  float fc_il, fc_k, fc_bias;
+  int fc_mode;
+  // llap
+  float ll_sigma, ll_shadows, ll_highlights, ll_clarity;
+  // outputs of the develop kernel
+  half4 *rgbf;          // filmcurv output, W*H rgba f16
+  __half *l1;           // llap level 1, 11 planes
+  int l1w, l1h;
+  size_t l1plane;       // elements per plane
+  uint32_t *hist;       // 257 counts or null
+  // debug copies (null in production)
+  __half *dbg_denoise, *dbg_hilite;
+};
+
+struct dev_hilite_k1_t
+{
+  const uint16_t *mosaic;
+  int pitch, cx, cy, W, H;
+  uint32_t filters;
+  float black, white, hl_white, hl_desat;
+  float wb[3];
+  int hw, hh;          // h0 size (W/2, H/2)
+  half4 *r1;
+  int s1w, s1h;
+};
+
+struct dev_llap_k3_t
+{
+  const half4 *rgbf;    // filmcurv output
+  int W, H;
+  const __half *l1;     // level 1 planes
+  int l1w, l1h;
+  size_t l1plane;
+  const __half *coarse; // A[1] at level 1 size, or the grey plane of level 1 when the pyramid has 2 levels
+  float ll_sigma, ll_shadows, ll_highlights, ll_clarity;
+  half4 *out;           // rgba f16 W*H
+};
+
+// hilite (k_hilite.cu)
+cudaError_t launch_hilite_k1(const dev_hilite_k1_t &p, cudaStream_t s);
+cudaError_t launch_hilite_reduce(const half4 *in, int iw, int ih, half4 *out, int ow, int oh,
+    float white, float desat, const float wb[3], cudaStream_t s);
+cudaError_t launch_hilite_assemble(const half4 *fine, int fw, int fh, const half4 *coarse, int cw, int ch,
+    half4 *out, float white, float soft, cudaStream_t s);
+
+// develop: hilite doub + demosaic + colour + filmcurv + llap curve + level 1 reduce (k_develop.cu)
+cudaError_t launch_develop(const dev_image_t &p, cudaStream_t s);
+
+// llap pyramid (k_llap.cu)
+cudaError_t launch_llap_reduce(const __half *in, int iw, int ih, size_t iplane,
+    __half *out, int ow, int oh, size_t oplane, cudaStream_t s);
+cudaError_t launch_llap_assemble(const __half *coarse, int first, const __half *l0, int w0, int h0, size_t p0,
+    const __half *l1, int w1, int h1, size_t p1, __half *out, cudaStream_t s);
+cudaError_t launch_llap_final(const dev_llap_k3_t &p, cudaStream_t s);
+
+// misc (k_misc.cu)
+struct scene_layout_t;
+cudaError_t launch_scene(const scene_layout_t *d_layout, int wd, int ht, uint16_t *out, cudaStream_t s);
+cudaError_t launch_hist_rgba(const half4 *in, int W, int H, uint32_t *hist, cudaStream_t s);

@@ -1,0 +1,69 @@
+// Per pixel bodies shared across kernel files: the llap tone curve and the
+// histogram bin index.
+#pragma once
+#include "common.cuh"
+
+DEV float llap_gamma(int i) { return (float)i / (10.0f - 1.0f); } // llap/llap.glsl:3-14
+
+// llap/curve.comp:39-63 (shared with the final llap kernel)
+DEV float llap_curve_fn(float x, float g, float sigma, float shadows, float highlights, float clarity)
+{
+  const float c = x - g;
+  float val;
+  const float ssigma = c > 0.0f ? sigma : -sigma;
+  const float shadhi = c > 0.0f ? shadows : highlights;
+  if(fabsf(c) > 2.0f * sigma) val = g + ssigma + shadhi * (c - ssigma);
+  else
+  {
+    const float t = gclamp(c / (2.0f * ssigma), 0.0f, 1.0f);
+    const float t2 = t * t;
+    const float mt = 1.0f - t;
+    val = g + ssigma * 2.0f * mt * t + t2 * (ssigma + ssigma * shadhi);
+  }
+  val += clarity * c * expf(-c * c / (2.0f * sigma * sigma / 3.0f));
+  return val;
+}
+
+// histogram bin, bit exact with the oracle (see hist_log there for the method)
+DEV float hist_log(float x)
+{
+  if(!(x > 0.0f)) return x == 0.0f ? -INFINITY : __int_as_float(0x7fc00000);
+  if(x == INFINITY) return INFINITY;
+  uint32_t u = __float_as_uint(x);
+  int e = (int)((u >> 23) & 0xff);
+  if(e == 0) { x = __fmul_rn(x, 8388608.0f); u = __float_as_uint(x); e = (int)((u >> 23) & 0xff) - 23; }
+  e -= 127;
+  u = (u & 0x007fffffu) | 0x3f800000u;
+  float m = __uint_as_float(u);
+  if(m > 1.41421356f) { m = __fmul_rn(m, 0.5f); e += 1; }
+  const float s = __fdiv_rn(__fsub_rn(m, 1.0f), __fadd_rn(m, 1.0f));
+  const float s2 = __fmul_rn(s, s);
+  float poly = 1.0f / 13.0f;
+  poly = __fadd_rn(__fmul_rn(poly, s2), 1.0f / 11.0f);
+  poly = __fadd_rn(__fmul_rn(poly, s2), 1.0f / 9.0f);
+  poly = __fadd_rn(__fmul_rn(poly, s2), 1.0f / 7.0f);
+  poly = __fadd_rn(__fmul_rn(poly, s2), 1.0f / 5.0f);
+  poly = __fadd_rn(__fmul_rn(poly, s2), 1.0f / 3.0f);
+  poly = __fadd_rn(__fmul_rn(poly, s2), 1.0f);
+  const float lm = __fmul_rn(__fmul_rn(2.0f, s), poly);
+  const float fe = (float)e;
+  const float hi = __fmul_rn(fe, 0.693145752f);
+  const float lo = __fmul_rn(fe, 1.42860677e-06f);
+  return __fadd_rn(hi, __fadd_rn(lo, lm));
+}
+
+// OpenDRT/hist.comp:15-20 get_bin
+DEV uint32_t hist_bin(float r, float g, float b)
+{
+  const float v = lum2020(r, g, b);
+  float l;
+  if(v < 0.0f) l = __fadd_rn(__fmul_rn(v, 16.184376489665897f), 0.075f);
+  else l = __fadd_rn(__fmul_rn(hist_log(__fadd_rn(v, 0.0057048244042473785f)), 0.09232902596577353f), 0.5520126568606655f);
+  const float fb = __fadd_rn(__fmul_rn(256.0f, l), 0.5f);
+  uint32_t bin;
+  if(!(fb > 0.0f)) bin = 0;
+  else if(fb >= 4294967295.0f) bin = 0xffffffffu;
+  else bin = (uint32_t)fb;
+  return bin > 255u ? 255u : bin;
+}
+

@@ -142,6 +142,7 @@ def run_reference(args):
 
 
 def main():
+    global WD, HT, RING, LEVELS
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
@@ -152,7 +153,6 @@ def main():
     ap.add_argument("--ring", type=int, default=RING, help="number of resident inputs")
     ap.add_argument("--levels", type=int, default=LEVELS, help="llap pyramid depth (0 = automatic)")
     args = ap.parse_args()
-    global WD, HT, RING, LEVELS
     WD, HT = [int(x) for x in args.size.lower().split("x")]
     RING, LEVELS = args.ring, args.levels
     if args.impl == "reference":
@@ -257,7 +257,8 @@ def main():
                 "traffic": traffic, "kernel": "k_develop (hilite doub + demosaic + colour + filmcurv + llap curve/reduce)",
                 "kernel_ms": dev_ms, "alg_bytes_per_launch": alg,
                 "peak_source": "measured" if peaks else "fallback",
-                "per_launch_ms": {n: float(x) for n, x in zip(names, kms)}}
+                "per_launch_ms": [[n, round(float(x), 5)] for n, x in zip(names, kms)],
+                "per_kernel_ms": {n: round(float(sum(x for m, x in zip(names, kms) if m == n)), 5) for n in names}}
     gt.close()
 
     # ---- e2e: host mosaic in, host rgba f16 out, through the C-ABI run call

@@ -153,7 +153,7 @@ struct vkdt_cuda_graph_t
   std::vector<level_t> hr, hb;   // hilite reduce outputs r[1..L] (index 0 = r1), assembled B[1..L-1]
   std::vector<level_t> lp, la;   // llap planes level 1..nl-1 (index 0 = level 1), assembled A[1..nl-2]
   int nl = 0;
-  size_t off_src = 0, off_rgbf = 0, off_out = 0, off_hist = 0, off_dbg0 = 0, off_dbg1 = 0, arena_bytes = 0;
+  size_t off_src = 0, off_rgbf = 0, off_out = 0, off_hist = 0, off_dbg0 = 0, off_dbg1 = 0, off_lut = 0, arena_bytes = 0;
   unsigned char *arena = nullptr;
   void *h_src = nullptr, *h_sink = nullptr;
   size_t src_bytes = 0, sink_bytes = 0;
@@ -287,6 +287,7 @@ int fill_image(vkdt_cuda_graph_t *g, dev_image_t &d, const void *d_src, void *d_
 {
   memset(&d, 0, sizeof(d));
   d.mosaic = (const uint16_t *)d_src;
+  d.noop_lut = g->at<__half>(g->off_lut);
   d.pitch = g->in_wd;
   d.cx = (int)g->ip.crop_aabb[0]; d.cy = (int)g->ip.crop_aabb[1];
   d.W = g->W; d.H = g->H;
@@ -337,7 +338,7 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
   // 1. noop + hilite half + first hilite reduce
   dev_hilite_k1_t k1;
   memset(&k1, 0, sizeof(k1));
-  k1.mosaic = d.mosaic; k1.pitch = d.pitch; k1.cx = d.cx; k1.cy = d.cy; k1.W = d.W; k1.H = d.H;
+  k1.mosaic = d.mosaic; k1.noop_lut = d.noop_lut; k1.pitch = d.pitch; k1.cx = d.cx; k1.cy = d.cy; k1.W = d.W; k1.H = d.H;
   k1.filters = d.filters; k1.black = d.black; k1.white = d.white; k1.hl_white = white; k1.hl_desat = desat;
   for(int k = 0; k < 3; k++) k1.wb[k] = wb[k];
   k1.hw = g->hw; k1.hh = g->hh;
@@ -413,6 +414,7 @@ int vkdt_cuda_init(int device_id, uint32_t flags)
   if(prop.major != 10 || prop.minor != 3)
     return fail(VKDT_CUDA_ERROR_INITIALIZATION_FAILED, "device %d is sm_%d%d, the library is built for sm_103a", device_id, prop.major, prop.minor);
   CU(cudaSetDevice(device_id));
+  CU(init_develop());
   g_device = device_id;
   return VKDT_CUDA_SUCCESS;
 }
@@ -638,7 +640,8 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
   if(b[2] <= b[0] || b[3] <= b[1] || (int)b[2] > g->in_wd || (int)b[3] > g->in_ht)
     return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "crop window outside the mosaic");
   g->W = (int)(b[2] - b[0]); g->H = (int)(b[3] - b[1]);
-  if((g->W & 1) || (g->H & 1) || (b[0] & 1) || (b[1] & 1)) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "bayer crop window must be even");
+  if((g->W & 1) || (g->H & 1) || (b[0] & 1) || (b[1] & 1) || (g->in_wd & 1))
+    return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "bayer mosaic width and crop window must be even");
   if(g->W < 16 || g->H < 16) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "image smaller than 16x16");
   g->hw = g->W / 2; g->hh = g->H / 2;
   if(g->req_wd > 0 && (g->req_wd != g->W || g->req_ht != g->H))
@@ -746,10 +749,21 @@ int vkdt_cuda_graph_alloc(vkdt_cuda_graph_t *g, uint64_t *device_bytes)
   for(auto &l : g->la) l.off = take((size_t)l.w * l.h * 2);
   g->off_out = take(g->sink_bytes);
   g->off_hist = take(257 * 4);
+  g->off_lut = take(65536 * 2);
   if(g->debug) { g->off_dbg0 = take((size_t)g->W * g->H * 2); g->off_dbg1 = take((size_t)g->W * g->H * 2); }
   g->arena_bytes = off;
   CU(cudaMalloc((void **)&g->arena, g->arena_bytes));
   CU(cudaMemset(g->arena, 0, g->arena_bytes));
+  { // denoise/noop.comp:385 for every u16 code, channel 0 black/white (denoise/main.c:165-168)
+    std::vector<__half> lut(65536);
+    const float black = g->ip.black[0] / 65535.0f, white = g->ip.white[0] / 65535.0f;
+    for(int v = 0; v < 65536; v++)
+    {
+      const float x = (float)v / 65535.0f;
+      lut[v] = __float2half_rn(std::fmax(0.0f, (x - black) / (white - black)));
+    }
+    CU(cudaMemcpy(g->arena + g->off_lut, lut.data(), 65536 * 2, cudaMemcpyHostToDevice));
+  }
   CU(cudaMallocHost(&g->h_src, g->src_bytes));
   CU(cudaMallocHost(&g->h_sink, g->sink_bytes));
   CU(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));

@@ -14,6 +14,18 @@
 // a MIRRORED_REPEAT texture read returns). The last tile of a row/column is
 // shifted inwards so that the 6 pixel wrap of demosaic/splat.comp:153-156
 // always lands inside the tile's slots; outputs are written by the owner only.
+//
+// Work mapping: the per pixel stages (splat, fix and everything after) hand
+// a warp pixels of one CFA phase, so the colour dependent branches of the
+// shaders are uniform in a warp; the shared arrays those stages read with a
+// stride of two pixels are stored split by x parity (no bank conflicts).
+//
+// Gaussian weights of demosaic/splat and demosaic/fix: the eigenvectors of
+// the bayer covariance are snapped to the axes (gauss.comp:72-73), so per
+// covariance entry the weight exp(-0.5 dot(E o / eval, E o)) takes only the
+// values for dot = 0, 1/e0, 1/e1, 1/e0 + 1/e1 (E o has entries in {-1,0,1}).
+// They are computed once per entry with the same operations as the shader
+// (the products by +-1 and 0 are exact), so the weights are bit identical.
 #include "common.cuh"
 #include "hilite.cuh"
 #include "kernels.h"
@@ -22,45 +34,34 @@
 namespace {
 
 constexpr int TX = 32, TY = 32;
-constexpr int MX = TX + 8, MY = TY + 8;          // hilite output mosaic: virtual [X0-4, X0+TX+4)
-constexpr int CX = TX / 2 + 2, CY = TY / 2 + 2;  // demosaic/gauss: half positions [X0/2-1, X0/2+TX/2+1)
-constexpr int GX = TX + 3, GY = TY + 3;          // demosaic/splat: virtual [X0-2, X0+TX+1)
-constexpr int LX = TX + 1, LY = TY + 1;          // llap level 0: virtual [X0-1, X0+TX)
-constexpr int NPL = 11;                          // NUM_GAMMA curves + grey (llap/config.h:2)
 constexpr int NT = 256;
+constexpr int MB = TX / 2 + 4;       // hilite output mosaic: virtual blocks [X0/2-2, X0/2+TX/2+2)
+constexpr int MX = 2 * MB;           // pixel slots per side (virtual [X0-4, X0+TX+4))
+constexpr int CX = TX / 2 + 2;       // demosaic/gauss: half positions [X0/2-1, X0/2+TX/2+1)
+constexpr int GX = TX + 3;           // demosaic/splat: virtual [X0-2, X0+TX+1)
+constexpr int GH = (GX + 1) / 2;
+constexpr int LX = TX + 1;           // llap level 0: virtual [X0-1, X0+TX)
+constexpr int LH = (LX + 1) / 2;
+constexpr int BX = TX / 4 + 6;       // hilite coarse level slots
+constexpr int NPL = 11;              // NUM_GAMMA curves + grey (llap/config.h:2)
 
 struct smem_t
 {
-  float M[MY][MX];
-  float cov[4][CY][CX];
-  float g[GY][GX];
-  __half L0[NPL][LY][LX + 1];
+  float M[MX][2][MB];          // hilite output mosaic, [y][x&1][x>>1]
+  float sw[3][CX][CX];         // splat weights for dot = 1/e0, 1/e1, 1/e0+1/e1
+  float fw[3][CX][CX];         // fix weights, same
+  unsigned char ori[CX][CX];   // 0: evec (1,0), 1: evec (0,1), 2: no covariance (weights 1)
+  float g[GX][2][GH];          // splat output, [y][x&1][x>>1]
+  __half L0[NPL][LX][2][LH];   // llap level 0 planes, [y][slot&1][slot>>1]
+  float B1[3][BX][BX];         // hilite coarse level (rgb) around the tile
   uint32_t hist[257];
 };
 
-// the hilite output (module output) of one 2x2 block at real block (bx, by):
-// denoise/noop of the block, hilite/half, the level 0 hilite/assemble against
-// the stored coarse level, then hilite/doub
-DEV void mosaic_block(const dev_image_t &p, int bx, int by, float out[4], float m[4])
-{
-  const int hw = p.W / 2, hh = p.H / 2;
-  m[0] = noop_val(p.mosaic, p.pitch, p.cx, p.cy, p.W, p.H, 2 * bx, 2 * by, p.black, p.white);
-  m[1] = noop_val(p.mosaic, p.pitch, p.cx, p.cy, p.W, p.H, 2 * bx + 1, 2 * by, p.black, p.white);
-  m[2] = noop_val(p.mosaic, p.pitch, p.cx, p.cy, p.W, p.H, 2 * bx, 2 * by + 1, p.black, p.white);
-  m[3] = noop_val(p.mosaic, p.pitch, p.cx, p.cy, p.W, p.H, 2 * bx + 1, 2 * by + 1, p.black, p.white);
-  float h[4];
-  hilite_half_bayer(m[0], m[1], m[2], m[3], p.hl_white, h);
-  h[3] = 1.0f;
-  float up[3];
-  hilite_expand_px([&](int ix, int iy, float rgb[3]) {
-      const int sx = mirror_full(ix, p.hcw), sy = mirror_full(iy, p.hch);
-      float w;
-      ld_half4(p.hl_coarse + (size_t)sy * p.hcw + sx, rgb[0], rgb[1], rgb[2], w);
-    }, bx, by, up);
-  float b0[3];
-  hilite_assemble_px(h, up, p.hl_white, p.hl_soft, b0);
-  (void)hw; (void)hh;
-  hilite_doub_bayer(m[0], m[1], m[2], m[3], b0, p.hl_white, out);
+DEV int mirror1(int i, int n)
+{ // mirrored repeat for |overshoot| < n, clamped for slots no pixel reads
+  if(i < 0) i = -1 - i;
+  if(i >= n) i = 2 * n - 1 - i;
+  return min(max(i, 0), n - 1);
 }
 
 // colour/main-impl.glsl:200-341 on the matrix path (no clut/pick/rbf, sat 1)
@@ -74,17 +75,13 @@ DEV void colour_px(const dev_image_t &p, const float in[3], float o[3])
   for(int i = 0; i < 3; i++) o[i] = f16r(gclamp(q[i] * p.mulw, -65535.0f, 65535.0f));
 }
 
-DEV float weibull_cdf(float x, float il, float k)
-{ // filmcurv/params.glsl:15-34
-  return 1.0f - expf(-powf(fmaxf(x, 1e-7f) * il, k));
-}
-
-// filmcurv/main.comp:106-205, colour modes 1 and 3 (adjust_colour_dng, shared.glsl:371-387)
+// filmcurv/main.comp:106-205, colour modes 1 and 3 (adjust_colour_dng,
+// shared.glsl:371-387). pow as GPUs evaluate GLSL pow: exp2(k log2 x)
 DEV void filmcurv_px(const dev_image_t &p, const float in[3], float o[3])
 {
   float c0[3], c1[3];
   for(int k = 0; k < 3; k++) c0[k] = in[k] + p.fc_bias;
-  for(int k = 0; k < 3; k++) c1[k] = weibull_cdf(c0[k], p.fc_il, p.fc_k);
+  for(int k = 0; k < 3; k++) c1[k] = 1.0f - expf(-gpow_pos(fmaxf(c0[k], 1e-7f) * p.fc_il, p.fc_k));
   if(p.fc_mode == 3)
   {
     bool fx = false, fy = false, fz = false;
@@ -100,9 +97,15 @@ DEV void filmcurv_px(const dev_image_t &p, const float in[3], float o[3])
   for(int k = 0; k < 3; k++) o[k] = f16r(c1[k]);
 }
 
-} // namespace
-
-namespace {
+// weight of a tap (i, j) from the per covariance table: dot = a0/e0 + a1/e1
+// with (a0, a1) = squared components of E (i, j)
+DEV float tap_weight(float w1, float w2, float w3, int ori, int i, int j)
+{
+  const int a0 = ori == 0 ? i * i : (ori == 1 ? j * j : 0);
+  const int a1 = ori == 0 ? j * j : (ori == 1 ? i * i : 0);
+  const int k = a0 + 2 * a1;
+  return k == 0 ? 1.0f : (k == 1 ? w1 : (k == 2 ? w2 : w3));
+}
 
 __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
 {
@@ -117,19 +120,53 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
   const int OXe = min(OX + TX, W), OYe = min(OY + TY, H);
   if(p.hist) for(int i = tid; i < 257; i += NT) s.hist[i] = 0;
 
-  // ---- hilite output mosaic on virtual blocks [X0/2-2, X0/2+TX/2+2)
+  // ---- the hilite coarse level around the tile (virtual slots, mirrored)
+  const int bx0 = ((X0 / 2 - 2) >> 1) - 2, by0 = ((Y0 / 2 - 2) >> 1) - 2;
+  for(int i = tid; i < BX * BX; i += NT)
+  {
+    const int sx = i % BX, sy = i / BX;
+    const int gx = mirror1(bx0 + sx, p.hcw), gy = mirror1(by0 + sy, p.hch);
+    float a, b, c, d;
+    ld_half4(p.hl_coarse + (size_t)gy * p.hcw + gx, a, b, c, d);
+    s.B1[0][sy][sx] = a; s.B1[1][sy][sx] = b; s.B1[2][sy][sx] = c;
+  }
+  __syncthreads();
+
+  // ---- hilite output mosaic on virtual blocks [X0/2-2, X0/2+TX/2+2):
+  // denoise/noop (lut), hilite/half, level 0 hilite/assemble, hilite/doub
   {
     const int hx0 = X0 / 2 - 2, hy0 = Y0 / 2 - 2;
-    for(int i = tid; i < (MX / 2) * (MY / 2); i += NT)
+    for(int i = tid; i < MB * MB; i += NT)
     {
-      const int sbx = i % (MX / 2), sby = i / (MX / 2);
+      const int sbx = i % MB, sby = i / MB;
       const int vbx = hx0 + sbx, vby = hy0 + sby;
-      const int rbx = mirror_full(vbx, hw), rby = mirror_full(vby, hh);
+      const int rbx = mirror1(vbx, hw), rby = mirror1(vby, hh);
       const bool fx = vbx < 0 || vbx >= hw, fy = vby < 0 || vby >= hh;
-      float o[4], m[4];
-      mosaic_block(p, rbx, rby, o, m);
-      for(int dy = 0; dy < 2; dy++) for(int dx = 0; dx < 2; dx++)
-        s.M[2 * sby + dy][2 * sbx + dx] = o[(fy ? 1 - dy : dy) * 2 + (fx ? 1 - dx : dx)];
+      const size_t row = (size_t)(2 * rby + p.cy) * p.pitch + 2 * rbx + p.cx;
+      const uint32_t r0 = __ldg(reinterpret_cast<const uint32_t *>(p.mosaic + row));
+      const uint32_t r1 = __ldg(reinterpret_cast<const uint32_t *>(p.mosaic + row + p.pitch));
+      float m[4];
+      m[0] = h2f(__ldg(p.noop_lut + (r0 & 0xffff)));
+      m[1] = h2f(__ldg(p.noop_lut + (r0 >> 16)));
+      m[2] = h2f(__ldg(p.noop_lut + (r1 & 0xffff)));
+      m[3] = h2f(__ldg(p.noop_lut + (r1 >> 16)));
+      float h[4];
+      hilite_half_bayer(m[0], m[1], m[2], m[3], p.hl_white, h);
+      h[3] = 1.0f;
+      float up[3];
+      hilite_expand_px([&](int ix, int iy, float rgb[3]) {
+          const int sx = ix - bx0, sy = iy - by0;
+          rgb[0] = s.B1[0][sy][sx]; rgb[1] = s.B1[1][sy][sx]; rgb[2] = s.B1[2][sy][sx];
+        }, rbx, rby, up);
+      float b0[3], o[4];
+      hilite_assemble_px(h, up, p.hl_white, p.hl_soft, b0);
+      hilite_doub_bayer(m[0], m[1], m[2], m[3], b0, p.hl_white, o);
+      // flipped blocks (mirrored at the image border) swap their rows / columns
+      const float t0 = fy ? o[2] : o[0], t1 = fy ? o[3] : o[1], t2 = fy ? o[0] : o[2], t3 = fy ? o[1] : o[3];
+      s.M[2 * sby][fx ? 1 : 0][sbx] = t0;
+      s.M[2 * sby][fx ? 0 : 1][sbx] = t1;
+      s.M[2 * sby + 1][fx ? 1 : 0][sbx] = t2;
+      s.M[2 * sby + 1][fx ? 0 : 1][sbx] = t3;
       if(p.dbg_denoise && !fx && !fy && 2 * rbx >= OX && 2 * rbx < OXe && 2 * rby >= OY && 2 * rby < OYe)
         for(int dy = 0; dy < 2; dy++) for(int dx = 0; dx < 2; dx++)
         {
@@ -141,33 +178,55 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
   }
   __syncthreads();
 
-  // ---- demosaic/gauss.comp:24-75 (bayer) on half positions [X0/2-1, X0/2+TX/2+1)
-  for(int i = tid; i < CX * CY; i += NT)
+  // ---- demosaic/gauss.comp:24-75 (bayer) on half positions [X0/2-1, X0/2+TX/2+1),
+  // then the splat and fix weight tables of each entry
+  for(int i = tid; i < CX * CX; i += NT)
   {
     const int scx = i % CX, scy = i / CX;
     const int cx = X0 / 2 - 1 + scx, cy = Y0 / 2 - 1 + scy;
     float v[4] = { 0.0f, 0.0f, 0.0f, 0.0f };
     if(cx >= 0 && cy >= 0 && cx < hw && cy < hh)
     {
-      // M slot of virtual (2cx+i, 2cy+j) = [2scy+2+j][2scx+2+i]
-      float mw0 = 0, mw1 = 0, mb0 = 0, mb1 = 0, smw = 0, smb = 0;
-      for(int j = -1; j < 3; j++) for(int ii = -1; ii < 3; ii++)
+      // green samples at (2c+ii, 2c+j), (ii+j) odd: M slot x = 2scx+2+ii
+      float px[8], inv[8];
+      int k = 0;
+#pragma unroll
+      for(int j = -1; j < 3; j++)
+#pragma unroll
+      for(int ii = -1; ii < 3; ii++)
       {
         if(((j + ii) & 1) != 1) continue;
-        const float px = s.M[2 * scy + 2 + j][2 * scx + 2 + ii];
-        mw0 += (float)ii * px; mw1 += (float)j * px;
-        smw += px;
-        mb0 += (float)ii / px; mb1 += (float)j / px;
-        smb += 1.0f / px;
+        const int xs = 2 * scx + 2 + ii;
+        px[k] = s.M[2 * scy + 2 + j][xs & 1][xs >> 1];
+        inv[k] = 1.0f / px[k];
+        k++;
+      }
+      // i/px for i in {-1,0,1,2} is i*(1/px) exactly (scaling by +-1, 2 is exact)
+      float mw0 = 0, mw1 = 0, mb0 = 0, mb1 = 0, smw = 0, smb = 0;
+      k = 0;
+#pragma unroll
+      for(int j = -1; j < 3; j++)
+#pragma unroll
+      for(int ii = -1; ii < 3; ii++)
+      {
+        if(((j + ii) & 1) != 1) continue;
+        mw0 += (float)ii * px[k]; mw1 += (float)j * px[k];
+        smw += px[k];
+        mb0 += (float)ii * inv[k]; mb1 += (float)j * inv[k];
+        smb += inv[k];
+        k++;
       }
       mw0 /= smw; mw1 /= smw;
       mb0 /= smb; mb1 /= smb;
       float Sw00 = 0, Sw01 = 0, Sw10 = 0, Sw11 = 0, Sb00 = 0, Sb01 = 0, Sb10 = 0, Sb11 = 0, sw = 0, sb = 0;
-      for(int j = -1; j < 3; j++) for(int ii = -1; ii < 3; ii++)
+      k = 0;
+#pragma unroll
+      for(int j = -1; j < 3; j++)
+#pragma unroll
+      for(int ii = -1; ii < 3; ii++)
       {
         if(((j + ii) & 1) != 1) continue;
-        const float px = s.M[2 * scy + 2 + j][2 * scx + 2 + ii];
-        float p2 = px * px;
+        float p2 = px[k] * px[k];
         float q0 = (float)ii - mw0, q1 = (float)j - mw1;
         Sw00 += p2 * q0 * q0; Sw01 += p2 * q0 * q1; Sw10 += p2 * q1 * q0; Sw11 += p2 * q1 * q1;
         sw += p2;
@@ -175,6 +234,7 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
         p2 = 1.0f / p2;
         Sb00 += p2 * q0 * q0; Sb01 += p2 * q0 * q1; Sb10 += p2 * q1 * q0; Sb11 += p2 * q1 * q1;
         sb += p2;
+        k++;
       }
       Sw00 /= sw; Sw01 /= sw; Sw10 /= sw; Sw11 /= sw;
       Sb00 /= sb; Sb01 /= sb; Sb10 /= sb; Sb11 /= sb;
@@ -187,92 +247,123 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
       else                                  { evec0[0] = 0.0f; evec0[1] = 1.0f; }
       v[0] = f16r(eval[0]); v[1] = f16r(eval[1]); v[2] = f16r(evec0[0]); v[3] = f16r(evec0[1]);
     }
-    for(int k = 0; k < 4; k++) s.cov[k][scy][scx] = v[k];
+    // splat.comp:159-163 and fix.comp:21-29 weights of this entry
+    const int ori = v[2] == 1.0f ? 0 : (v[3] == 1.0f ? 1 : 2);
+    s.ori[scy][scx] = (unsigned char)ori;
+    {
+      const float r0 = 1.0f / gclamp(v[0], 0.01f, 25.0f), r1 = 1.0f / gclamp(v[1], 0.01f, 25.0f);
+      s.sw[0][scy][scx] = gclamp(expf(-0.5f * r0), 1e-4f, 1.0f);
+      s.sw[1][scy][scx] = gclamp(expf(-0.5f * r1), 1e-4f, 1.0f);
+      s.sw[2][scy][scx] = gclamp(expf(-0.5f * (r0 + r1)), 1e-4f, 1.0f);
+    }
+    {
+      const float r0 = 1.0f / (2.0f * gclamp(v[0], 1.0f, 49.0f)), r1 = 1.0f / (2.0f * gclamp(v[1], 1.0f, 49.0f));
+      s.fw[0][scy][scx] = gclamp(expf(-0.5f * r0), 1e-3f, 1.0f);
+      s.fw[1][scy][scx] = gclamp(expf(-0.5f * r1), 1e-3f, 1.0f);
+      s.fw[2][scy][scx] = gclamp(expf(-0.5f * (r0 + r1)), 1e-3f, 1.0f);
+    }
   }
   __syncthreads();
 
-  // ---- demosaic/splat.comp:224-266 (bayer) on virtual [X0-2, X0+TX+1)
-  for(int i = tid; i < GX * GY; i += NT)
+  // ---- demosaic/splat.comp:224-266 (bayer) on virtual [X0-2, X0+TX+1), one CFA phase per warp
   {
-    const int sgx = i % GX, sgy = i / GX;
-    const int qx = mirror_full(X0 - 2 + sgx, W), qy = mirror_full(Y0 - 2 + sgy, H);
-    const int ccx = (qx + 1) / 2 - (X0 / 2 - 1), ccy = (qy + 1) / 2 - (Y0 / 2 - 1);
-    const float c0 = s.cov[0][ccy][ccx], c1 = s.cov[1][ccy][ccx], c2 = s.cov[2][ccy][ccx], c3 = s.cov[3][ccy][ccx];
-    const float e0 = gclamp(c0, 0.01f, 25.0f), e1 = gclamp(c1, 0.01f, 25.0f);
-    float rg = 0.0f, wg = 0.0f;
-#pragma unroll
-    for(int j = -1; j <= 1; j++)
-#pragma unroll
-    for(int ii = -1; ii <= 1; ii++)
+    constexpr int NB = GH * GH;
+    for(int t = tid; t < 4 * NB; t += NT)
     {
-      if(cfa_bayer(qx + ii, qy + j) != 1) continue; // only green enters rgb.ggg
-      int px = qx + ii, py = qy + j;
-      if(px < 0) px += 6;
-      if(py < 0) py += 6;
-      if(px >= W) px -= 6;
-      if(py >= H) py -= 6;
-      const float col = s.M[py - (Y0 - 4)][px - (X0 - 4)];
-      const float of0 = c2 * (float)ii + c3 * (float)j;
-      const float of1 = -c3 * (float)ii + c2 * (float)j;
-      float weight = gclamp(expf(-0.5f * (of0 / e0 * of0 + of1 / e1 * of1)), 1e-4f, 1.0f);
-      if(ii == 0 && j == 0) weight = 666.0f;
-      rg += col * weight;
-      wg += weight;
+      const int ph = t / NB, b = t % NB;
+      const int sgx = 2 * (b % GH) + (ph & 1), sgy = 2 * (b / GH) + (ph >> 1);
+      if(sgx >= GX || sgy >= GX) continue;
+      const int qx = mirror1(X0 - 2 + sgx, W), qy = mirror1(Y0 - 2 + sgy, H);
+      const int ccx = (qx + 1) / 2 - (X0 / 2 - 1), ccy = (qy + 1) / 2 - (Y0 / 2 - 1);
+      const int ori = s.ori[ccy][ccx];
+      const float w1 = s.sw[0][ccy][ccx], w2 = s.sw[1][ccy][ccx], w3 = s.sw[2][ccy][ccx];
+      float rg = 0.0f, wg = 0.0f;
+#pragma unroll
+      for(int j = -1; j <= 1; j++)
+#pragma unroll
+      for(int ii = -1; ii <= 1; ii++)
+      {
+        if(cfa_bayer(qx + ii, qy + j) != 1) continue; // only green enters rgb.ggg
+        int px = qx + ii, py = qy + j;
+        if(px < 0) px += 6;
+        if(py < 0) py += 6;
+        if(px >= W) px -= 6;
+        if(py >= H) py -= 6;
+        const int mx = px - (X0 - 4), my = py - (Y0 - 4);
+        const float col = s.M[my][mx & 1][mx >> 1];
+        const float weight = (ii == 0 && j == 0) ? 666.0f : tap_weight(w1, w2, w3, ori, ii, j);
+        rg += col * weight;
+        wg += weight;
+      }
+      s.g[sgy][sgx & 1][sgx >> 1] = f16r(rg / fmaxf(1e-8f, wg));
     }
-    s.g[sgy][sgx] = f16r(rg / fmaxf(1e-8f, wg));
   }
   __syncthreads();
 
   // ---- demosaic/fix -> colour -> hist -> filmcurv -> llap/curve on virtual [X0-1, X0+TX)
-  const float sig = p.ll_sigma, sh = p.ll_shadows, hl = p.ll_highlights, cl = p.ll_clarity;
-  for(int i = tid; i < LX * LY; i += NT)
   {
-    const int slx = i % LX, sly = i / LX;
-    const int vx = X0 - 1 + slx, vy = Y0 - 1 + sly;
-    const int px = mirror_full(vx, W), py = mirror_full(vy, H);
-    const float gc = s.g[py - (Y0 - 2)][px - (X0 - 2)];
-    const int ccx = (px + 1) / 2 - (X0 / 2 - 1), ccy = (py + 1) / 2 - (Y0 / 2 - 1);
-    const float cv2 = s.cov[2][ccy][ccx], cv3 = s.cov[3][ccy][ccx];
-    const float e0 = 2.0f * gclamp(s.cov[0][ccy][ccx], 1.0f, 49.0f), e1 = 2.0f * gclamp(s.cov[1][ccy][ccx], 1.0f, 49.0f);
-    float rgb[3] = { 0.0f, 0.0f, 0.0f }, w[3] = { 0.0f, 0.0f, 0.0f };
-    // demosaic/fix.comp:99-135, radius clamp(fixup+1, 1, 2) = 1 for the
-    // default fixup 0 (the host rejects other values for this kernel)
-#pragma unroll
-    for(int j = -1; j <= 1; j++)
-#pragma unroll
-    for(int ii = -1; ii <= 1; ii++)
+    const float sig = p.ll_sigma, shd = p.ll_shadows, hil = p.ll_highlights, cla = p.ll_clarity;
+    const float r2s = 1.0f / (2.0f * sig), rden = 1.0f / (2.0f * sig * sig / 3.0f);
+    constexpr int NB = LH * LH;
+    for(int t = tid; t < 4 * NB; t += NT)
     {
-      const int c = cfa_bayer(px + ii, py + j);
-      if(c == 1) { rgb[1] = gc; w[1] = 1.0f; continue; }
-      const float gh = s.g[py + j - (Y0 - 2)][px + ii - (X0 - 2)];
-      const float col = s.M[py + j - (Y0 - 4)][px + ii - (X0 - 4)];
-      const float of0 = cv2 * (float)ii + cv3 * (float)j;
-      const float of1 = -cv3 * (float)ii + cv2 * (float)j;
-      const float weight = gclamp(expf(-0.5f * (of0 / e0 * of0 + of1 / e1 * of1)), 1e-3f, 1.0f);
-      rgb[c] += col * (1e-4f + gc) / (1e-4f + gh) * weight;
-      w[c] += weight;
-    }
-    float dm[3];
-    for(int k = 0; k < 3; k++) dm[k] = f16r(rgb[k] / fmaxf(1e-8f, w[k]));
-    float co[3];
-    colour_px(p, dm, co);
-    const bool own = vx == px && vy == py && px >= OX && px < OXe && py >= OY && py < OYe;
-    if(own && p.hist)
-    {
-      const uint32_t bin = hist_bin(co[0], co[1], co[2]);
-      if(bin > 0) { atomicAdd(&s.hist[bin], 1u); atomicAdd(&s.hist[256], 1u); }
-    }
-    float fc[3];
-    filmcurv_px(p, co, fc);
-    if(own) p.rgbf[(size_t)py * W + px] = mk_half4(fc[0], fc[1], fc[2], 1.0f);
-    const float yv = lum2020(gclamp(fc[0], -1000.0f, 1000.0f), gclamp(fc[1], -1000.0f, 1000.0f), gclamp(fc[2], -1000.0f, 1000.0f));
+      const int ph = t / NB, b = t % NB;
+      const int slx = 2 * (b % LH) + (ph & 1), sly = 2 * (b / LH) + (ph >> 1);
+      if(slx >= LX || sly >= LX) continue;
+      const int vx = X0 - 1 + slx, vy = Y0 - 1 + sly;
+      const int px = mirror1(vx, W), py = mirror1(vy, H);
+      const int gx0 = px - (X0 - 2), gy0 = py - (Y0 - 2);
+      const float gc = s.g[gy0][gx0 & 1][gx0 >> 1];
+      const int ccx = (px + 1) / 2 - (X0 / 2 - 1), ccy = (py + 1) / 2 - (Y0 / 2 - 1);
+      const int ori = s.ori[ccy][ccx];
+      const float w1 = s.fw[0][ccy][ccx], w2 = s.fw[1][ccy][ccx], w3 = s.fw[2][ccy][ccx];
+      float rr = 0.0f, rb = 0.0f, wr = 0.0f, wb = 0.0f, rg = 0.0f, wg = 0.0f;
+      // demosaic/fix.comp:99-135, radius clamp(fixup+1, 1, 2) = 1 for the
+      // default fixup 0 (the host rejects other values for this kernel)
 #pragma unroll
-    for(int k = 0; k < NPL - 1; k++) s.L0[k][sly][slx] = f2h(llap_curve_fn(yv, llap_gamma(k), sig, sh, hl, cl));
-    s.L0[NPL - 1][sly][slx] = f2h(yv);
+      for(int j = -1; j <= 1; j++)
+#pragma unroll
+      for(int ii = -1; ii <= 1; ii++)
+      {
+        const int c = cfa_bayer(px + ii, py + j);
+        if(c == 1) { rg = gc; wg = 1.0f; continue; }
+        const int gx = gx0 + ii, gy = gy0 + j;
+        const float gh = s.g[gy][gx & 1][gx >> 1];
+        const int mx = px + ii - (X0 - 4), my = py + j - (Y0 - 4);
+        const float col = s.M[my][mx & 1][mx >> 1];
+        const float weight = tap_weight(w1, w2, w3, ori, ii, j);
+        const float v = col * (1e-4f + gc) / (1e-4f + gh) * weight;
+        if(c == 0) { rr += v; wr += weight; }
+        else       { rb += v; wb += weight; }
+      }
+      float dm[3];
+      dm[0] = f16r(rr / fmaxf(1e-8f, wr));
+      dm[1] = f16r(rg / fmaxf(1e-8f, wg));
+      dm[2] = f16r(rb / fmaxf(1e-8f, wb));
+      float co[3];
+      colour_px(p, dm, co);
+      const bool own = vx == px && vy == py && px >= OX && px < OXe && py >= OY && py < OYe;
+      if(own && p.hist)
+      {
+        const uint32_t bin = hist_bin(co[0], co[1], co[2]);
+        if(bin > 0) { atomicAdd(&s.hist[bin], 1u); atomicAdd(&s.hist[256], 1u); }
+      }
+      float fc[3];
+      filmcurv_px(p, co, fc);
+      if(own) p.rgbf[(size_t)py * W + px] = mk_half4(fc[0], fc[1], fc[2], 1.0f);
+      const float yv = lum2020(gclamp(fc[0], -1000.0f, 1000.0f), gclamp(fc[1], -1000.0f, 1000.0f), gclamp(fc[2], -1000.0f, 1000.0f));
+#pragma unroll
+      for(int k = 0; k < NPL - 1; k++)
+        s.L0[k][sly][slx & 1][slx >> 1] = f2h(llap_curve_rcp(yv, llap_gamma(k), sig, r2s, rden, shd, hil, cla));
+      s.L0[NPL - 1][sly][slx & 1][slx >> 1] = f2h(yv);
+    }
   }
   __syncthreads();
 
-  // ---- llap/reduce.comp (sample_semisoft) for level 1 outputs [X0/2, X0/2+TX/2)
+  // ---- llap/reduce.comp (sample_semisoft) for level 1 outputs [X0/2, X0/2+TX/2).
+  // The four bilinear taps at half texel offsets, ((t00/2 + t10/2)/2 + (t01/2 + t11/2)/2)
+  // summed and /4: halving is exact, so with the pair sums P = t0 + t1 this is
+  // exactly ((((P00 + P10)/4 + (P01 + P11)/4) + ...)/4 as the shader computes it.
   {
     const int lx = tid % (TX / 2), ly = tid / (TX / 2);
     const int ox = X0 / 2 + lx, oy = Y0 / 2 + ly;
@@ -282,12 +373,18 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
       // level 0 slot of virtual x = 2ox + a - 1 is 2lx + a
       for(int k = 0; k < NPL; k++)
       {
-        float t[3][3];
-        for(int b = 0; b < 3; b++) for(int a = 0; a < 3; a++) t[b][a] = h2f(s.L0[k][2 * ly + b][2 * lx + a]);
-        const float q00 = (t[0][0] * 0.5f + t[0][1] * 0.5f) * 0.5f + (t[1][0] * 0.5f + t[1][1] * 0.5f) * 0.5f;
-        const float q10 = (t[0][1] * 0.5f + t[0][2] * 0.5f) * 0.5f + (t[1][1] * 0.5f + t[1][2] * 0.5f) * 0.5f;
-        const float q01 = (t[1][0] * 0.5f + t[1][1] * 0.5f) * 0.5f + (t[2][0] * 0.5f + t[2][1] * 0.5f) * 0.5f;
-        const float q11 = (t[1][1] * 0.5f + t[1][2] * 0.5f) * 0.5f + (t[2][1] * 0.5f + t[2][2] * 0.5f) * 0.5f;
+        float P[3][2];
+        for(int r = 0; r < 3; r++)
+        {
+          const __half *row = &s.L0[k][2 * ly + r][0][0];
+          const float t0 = h2f(row[lx]), t1 = h2f(row[LH + lx]), t2 = h2f(row[lx + 1]);
+          P[r][0] = t0 + t1;
+          P[r][1] = t1 + t2;
+        }
+        const float q00 = (P[0][0] + P[1][0]) * 0.25f;
+        const float q10 = (P[0][1] + P[1][1]) * 0.25f;
+        const float q01 = (P[1][0] + P[2][0]) * 0.25f;
+        const float q11 = (P[1][1] + P[2][1]) * 0.25f;
         const float r = (((q00 + q10) + q01) + q11) / 4.0f;
         p.l1[k * p.l1plane + (size_t)oy * p.l1w + ox] = f2h(r);
       }
@@ -302,11 +399,14 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
 
 } // namespace
 
+cudaError_t init_develop()
+{
+  return cudaFuncSetAttribute(k_develop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(smem_t));
+}
+
 cudaError_t launch_develop(const dev_image_t &p, cudaStream_t s)
 {
-  const size_t smem = sizeof(smem_t);
-  static_assert(sizeof(smem_t) <= 48 * 1024, "develop tile needs the opt-in shared memory size");
   dim3 grid((p.W + TX - 1) / TX, (p.H + TY - 1) / TY);
-  k_develop<<<grid, NT, smem, s>>>(p);
+  k_develop<<<grid, NT, sizeof(smem_t), s>>>(p);
   return cudaGetLastError();
 }

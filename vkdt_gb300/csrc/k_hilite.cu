@@ -21,21 +21,12 @@ __global__ void __launch_bounds__(256) k_hilite_k1(const dev_hilite_k1_t p)
     const int sx = i % K1_N, sy = i / K1_N;
     const int hx = mirror_full(bx0 + sx, p.hw), hy = mirror_full(by0 + sy, p.hh);
     float h[3];
-    if(p.filters == 9)
-    {
-      float c[9];
-      for(int a = 0; a < 3; a++) for(int b = 0; b < 3; b++)
-        c[3 * a + b] = noop_val(p.mosaic, p.pitch, p.cx, p.cy, p.W, p.H, 3 * hx + a, 3 * hy + b, p.black, p.white);
-      hilite_half_xtrans(c, hx, hy, p.hl_white, h);
-    }
-    else
-    {
-      const float m00 = noop_val(p.mosaic, p.pitch, p.cx, p.cy, p.W, p.H, 2 * hx, 2 * hy, p.black, p.white);
-      const float m10 = noop_val(p.mosaic, p.pitch, p.cx, p.cy, p.W, p.H, 2 * hx + 1, 2 * hy, p.black, p.white);
-      const float m01 = noop_val(p.mosaic, p.pitch, p.cx, p.cy, p.W, p.H, 2 * hx, 2 * hy + 1, p.black, p.white);
-      const float m11 = noop_val(p.mosaic, p.pitch, p.cx, p.cy, p.W, p.H, 2 * hx + 1, 2 * hy + 1, p.black, p.white);
-      hilite_half_bayer(m00, m10, m01, m11, p.hl_white, h);
-    }
+    const size_t row = (size_t)(2 * hy + p.cy) * p.pitch + 2 * hx + p.cx;
+    const uint32_t r0 = __ldg(reinterpret_cast<const uint32_t *>(p.mosaic + row));
+    const uint32_t r1 = __ldg(reinterpret_cast<const uint32_t *>(p.mosaic + row + p.pitch));
+    const float m00 = h2f(__ldg(p.noop_lut + (r0 & 0xffff))), m10 = h2f(__ldg(p.noop_lut + (r0 >> 16)));
+    const float m01 = h2f(__ldg(p.noop_lut + (r1 & 0xffff))), m11 = h2f(__ldg(p.noop_lut + (r1 >> 16)));
+    hilite_half_bayer(m00, m10, m01, m11, p.hl_white, h);
     sh[0][sy][sx] = h[0]; sh[1][sy][sx] = h[1]; sh[2][sy][sx] = h[2];
   }
   __syncthreads();

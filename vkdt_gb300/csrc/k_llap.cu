@@ -2,6 +2,11 @@
 // assemble levels below level 1 and the final full resolution pass
 // (assemble of level 0 fused with llap/colour). Pyramid levels are stored as
 // 11 f16 planes (NUM_GAMMA curves + grey) each, planar.
+//
+// The assemble kernels stage the coarse level (its 11 planes and the coarse
+// assembled image) of a 32x32 output tile in shared memory and hand each warp
+// outputs of one (x, y) parity, so all lanes of a warp share the tap pattern
+// of the gauss_expand they evaluate.
 #include "common.cuh"
 #include "hilite.cuh"
 #include "kernels.h"
@@ -11,11 +16,23 @@ namespace {
 
 constexpr int NPL = 11;
 constexpr int NG = 10;
+constexpr int FT = 32;            // output tile
+constexpr int FS = FT / 2 + 4;    // coarse slots per side: virtual [X0/2-2, X0/2+FT/2+2)
 
+DEV int mirror1(int i, int n)
+{ // mirrored repeat for |overshoot| < n, clamped for slots no output reads
+  if(i < 0) i = -1 - i;
+  if(i >= n) i = 2 * n - 1 - i;
+  return min(max(i, 0), n - 1);
+}
+
+// llap/llap.glsl:16-21: the first hi in [1, NUM_GAMMA-1) with gamma(hi) > v;
+// the gammas increase, so this counts gamma(1..8) <= v
 DEV int gamma_hi_from_v(float v)
-{ // llap/llap.glsl:16-21
+{
   int hi = 1;
-  for(; hi < NG - 1 && llap_gamma(hi) <= v; hi++);
+#pragma unroll
+  for(int i = 1; i < NG - 1; i++) hi += (llap_gamma(i) <= v) ? 1 : 0;
   return hi;
 }
 
@@ -51,7 +68,9 @@ template<class F> DEV float expand(F fetch, int ox, int oy)
   return r / 9.0f;
 }
 
-// llap/reduce.comp:17-35 (sample_semisoft), all planes of one level
+// llap/reduce.comp:17-35 (sample_semisoft), all planes of one level. The four
+// half-texel bilinear taps equal ((P00+P10)/4 ...) with the horizontal pair
+// sums P (halving is exact), as in the develop kernel.
 __global__ void __launch_bounds__(256) k_llap_reduce(const __half *__restrict__ in, int iw, int ih, size_t ip,
     __half *__restrict__ out, int ow, int oh, size_t op)
 {
@@ -62,14 +81,43 @@ __global__ void __launch_bounds__(256) k_llap_reduce(const __half *__restrict__ 
   for(int k = 0; k < NPL; k++)
   {
     const __half *pl = in + k * ip;
-    float t[3][3];
-    for(int b = 0; b < 3; b++) for(int a = 0; a < 3; a++) t[b][a] = h2f(pl[(size_t)ys[b] * iw + xs[a]]);
-    const float q00 = (t[0][0] * 0.5f + t[0][1] * 0.5f) * 0.5f + (t[1][0] * 0.5f + t[1][1] * 0.5f) * 0.5f;
-    const float q10 = (t[0][1] * 0.5f + t[0][2] * 0.5f) * 0.5f + (t[1][1] * 0.5f + t[1][2] * 0.5f) * 0.5f;
-    const float q01 = (t[1][0] * 0.5f + t[1][1] * 0.5f) * 0.5f + (t[2][0] * 0.5f + t[2][1] * 0.5f) * 0.5f;
-    const float q11 = (t[1][1] * 0.5f + t[1][2] * 0.5f) * 0.5f + (t[2][1] * 0.5f + t[2][2] * 0.5f) * 0.5f;
+    float P[3][2];
+    for(int b = 0; b < 3; b++)
+    {
+      const __half *row = pl + (size_t)ys[b] * iw;
+      const float t0 = h2f(row[xs[0]]), t1 = h2f(row[xs[1]]), t2 = h2f(row[xs[2]]);
+      P[b][0] = t0 + t1;
+      P[b][1] = t1 + t2;
+    }
+    const float q00 = (P[0][0] + P[1][0]) * 0.25f, q10 = (P[0][1] + P[1][1]) * 0.25f;
+    const float q01 = (P[1][0] + P[2][0]) * 0.25f, q11 = (P[1][1] + P[2][1]) * 0.25f;
     out[k * op + (size_t)y * ow + x] = f2h((((q00 + q10) + q01) + q11) / 4.0f);
   }
+}
+
+// stage the 11 planes of the coarse level and the coarse assembled image of
+// one output tile: slot (sx, sy) holds the mirrored texel (bx+sx, by+sy)
+DEV void stage_coarse(__half (*sl)[FS][FS + 2], const __half *l1, int w1, int h1, size_t p1,
+    const __half *coarse, int bx, int by)
+{
+  for(int i = threadIdx.x; i < (NPL + 1) * FS * FS; i += blockDim.x)
+  {
+    const int k = i / (FS * FS), r = i % (FS * FS);
+    const int sx = r % FS, sy = r / FS;
+    const int gx = mirror1(bx + sx, w1), gy = mirror1(by + sy, h1);
+    const __half *pl = k < NPL ? l1 + k * p1 : coarse;
+    sl[k][sy][sx] = pl[(size_t)gy * w1 + gx];
+  }
+}
+
+// output pixel of the tile for item t: warps take one (x, y) parity class
+DEV bool tile_item(int t, int X0, int Y0, int w0, int h0, int &x, int &y)
+{
+  constexpr int NB = (FT / 2) * (FT / 2);
+  const int ph = t / NB, b = t % NB;
+  x = X0 + 2 * (b % (FT / 2)) + (ph & 1);
+  y = Y0 + 2 * (b / (FT / 2)) + (ph >> 1);
+  return x < w0 && y < h0;
 }
 
 // llap/assemble.comp:89-123 for a stored level: output at the size of l0
@@ -77,26 +125,27 @@ __global__ void __launch_bounds__(256) k_llap_assemble(const __half *__restrict_
     const __half *__restrict__ l0, int w0, int h0, size_t p0,
     const __half *__restrict__ l1, int w1, int h1, size_t p1, __half *__restrict__ out)
 {
-  const int x = blockIdx.x * 32 + threadIdx.x % 32, y = blockIdx.y * 8 + threadIdx.x / 32;
-  if(x >= w0 || y >= h0) return;
-  const __half *cimg = first ? l1 + NG * p1 : coarse;
-  auto fetch_plane = [&](const __half *pl) {
-    return [=](int ix, int iy) { return h2f(pl[(size_t)mirror_full(iy, h1) * w1 + mirror_full(ix, w1)]); };
-  };
-  const float res = expand(fetch_plane(cimg), x, y);
-  const size_t o = (size_t)y * w0 + x;
-  const float v = h2f(l0[NG * p0 + o]);
-  const int hi = gamma_hi_from_v(v);
-  const int lo = hi - 1;
-  const float glo = llap_gamma(lo), ghi = llap_gamma(hi);
-  const float a = gclamp((v - glo) / (ghi - glo), 0.0f, 1.0f);
-  const float la = h2f(l0[(hi - 1) * p0 + o]) - expand(fetch_plane(l1 + (hi - 1) * p1), x, y);
-  const float lb = h2f(l0[hi * p0 + o]) - expand(fetch_plane(l1 + hi * p1), x, y);
-  out[o] = f2h(res + la * (1.0f - a) + lb * a);
+  __shared__ __half sl[NPL + 1][FS][FS + 2];
+  const int X0 = blockIdx.x * FT, Y0 = blockIdx.y * FT;
+  const int bx = X0 / 2 - 2, by = Y0 / 2 - 2;
+  stage_coarse(sl, l1, w1, h1, p1, first ? l1 + NG * p1 : coarse, bx, by);
+  __syncthreads();
+  for(int t = threadIdx.x; t < FT * FT; t += blockDim.x)
+  {
+    int x, y;
+    if(!tile_item(t, X0, Y0, w0, h0, x, y)) continue;
+    auto fs = [&](int k) { return [=](int ix, int iy) { return h2f(sl[k][iy - by][ix - bx]); }; };
+    const float res = expand(fs(NPL), x, y);
+    const size_t o = (size_t)y * w0 + x;
+    const float v = h2f(l0[NG * p0 + o]);
+    const int hi = gamma_hi_from_v(v);
+    const float glo = (float)(hi - 1) / (10.0f - 1.0f), ghi = (float)hi / (10.0f - 1.0f);
+    const float a = gclamp((v - glo) / (ghi - glo), 0.0f, 1.0f);
+    const float la = h2f(l0[(hi - 1) * p0 + o]) - expand(fs(hi - 1), x, y);
+    const float lb = h2f(l0[hi * p0 + o]) - expand(fs(hi), x, y);
+    out[o] = f2h(res + la * (1.0f - a) + lb * a);
+  }
 }
-
-constexpr int FT = 32;            // final pass tile
-constexpr int FS = FT / 2 + 4;    // level 1 slots per side: virtual [X0/2-2, X0/2+FT/2+2)
 
 // llap/assemble.comp for level 0 (l0 recomputed from the filmcurv output like
 // llap/curve.comp) fused with llap/colour.comp:141-160
@@ -105,33 +154,25 @@ __global__ void __launch_bounds__(256) k_llap_final(const dev_llap_k3_t p)
   __shared__ __half sl[NPL + 1][FS][FS + 2];
   const int X0 = blockIdx.x * FT, Y0 = blockIdx.y * FT;
   const int bx = X0 / 2 - 2, by = Y0 / 2 - 2;
-  for(int i = threadIdx.x; i < (NPL + 1) * FS * FS; i += blockDim.x)
-  {
-    const int k = i / (FS * FS), r = i % (FS * FS);
-    const int sx = r % FS, sy = r / FS;
-    const int gx = mirror_full(bx + sx, p.l1w), gy = mirror_full(by + sy, p.l1h);
-    const __half *pl = k < NPL ? p.l1 + k * p.l1plane : p.coarse;
-    sl[k][sy][sx] = pl[(size_t)gy * p.l1w + gx];
-  }
+  stage_coarse(sl, p.l1, p.l1w, p.l1h, p.l1plane, p.coarse, bx, by);
   __syncthreads();
-  for(int i = threadIdx.x; i < FT * FT; i += blockDim.x)
+  const float sig = p.ll_sigma;
+  const float r2s = 1.0f / (2.0f * sig), rden = 1.0f / (2.0f * sig * sig / 3.0f);
+  for(int t = threadIdx.x; t < FT * FT; t += blockDim.x)
   {
-    const int x = X0 + i % FT, y = Y0 + i / FT;
-    if(x >= p.W || y >= p.H) continue;
+    int x, y;
+    if(!tile_item(t, X0, Y0, p.W, p.H, x, y)) continue;
     float rgb[4];
     ld_half4(p.rgbf + (size_t)y * p.W + x, rgb[0], rgb[1], rgb[2], rgb[3]);
     const float yv = lum2020(gclamp(rgb[0], -1000.0f, 1000.0f), gclamp(rgb[1], -1000.0f, 1000.0f), gclamp(rgb[2], -1000.0f, 1000.0f));
     const float v = f16r(yv);
     const int hi = gamma_hi_from_v(v);
-    const int lo = hi - 1;
-    const float glo = llap_gamma(lo), ghi = llap_gamma(hi);
+    const float glo = (float)(hi - 1) / (10.0f - 1.0f), ghi = (float)hi / (10.0f - 1.0f);
     const float a = gclamp((v - glo) / (ghi - glo), 0.0f, 1.0f);
-    auto fs = [&](int k) {
-      return [=](int ix, int iy) { return h2f(sl[k][iy - by][ix - bx]); };
-    };
+    auto fs = [&](int k) { return [=](int ix, int iy) { return h2f(sl[k][iy - by][ix - bx]); }; };
     const float res = expand(fs(NPL), x, y);
-    const float c0 = f16r(llap_curve_fn(yv, llap_gamma(hi - 1), p.ll_sigma, p.ll_shadows, p.ll_highlights, p.ll_clarity));
-    const float c1 = f16r(llap_curve_fn(yv, llap_gamma(hi), p.ll_sigma, p.ll_shadows, p.ll_highlights, p.ll_clarity));
+    const float c0 = f16r(llap_curve_rcp(yv, glo, sig, r2s, rden, p.ll_shadows, p.ll_highlights, p.ll_clarity));
+    const float c1 = f16r(llap_curve_rcp(yv, ghi, sig, r2s, rden, p.ll_shadows, p.ll_highlights, p.ll_clarity));
     const float la = c0 - expand(fs(hi - 1), x, y);
     const float lb = c1 - expand(fs(hi), x, y);
     float yo_ = f16r(res + la * (1.0f - a) + lb * a);
@@ -157,7 +198,7 @@ cudaError_t launch_llap_reduce(const __half *in, int iw, int ih, size_t iplane,
 cudaError_t launch_llap_assemble(const __half *coarse, int first, const __half *l0, int w0, int h0, size_t p0,
     const __half *l1, int w1, int h1, size_t p1, __half *out, cudaStream_t s)
 {
-  dim3 grid((w0 + 31) / 32, (h0 + 7) / 8);
+  dim3 grid((w0 + FT - 1) / FT, (h0 + FT - 1) / FT);
   k_llap_assemble<<<grid, 256, 0, s>>>(coarse, first, l0, w0, h0, p0, l1, w1, h1, p1, out);
   return cudaGetLastError();
 }

@@ -15,6 +15,7 @@ struct dev_image_t
 {
   // mosaic (source) and its active window
   const uint16_t *mosaic;
+  const __half *noop_lut; // denoise/noop of every u16 code (65536 f16)
   int pitch;            // elements per mosaic row
   int cx, cy;           // crop offset (denoise push.crop.xy)
   int W, H;             // denoise/hilite output size
@@ -49,6 +50,7 @@ struct dev_image_t
 struct dev_hilite_k1_t
 {
   const uint16_t *mosaic;
+  const __half *noop_lut;
   int pitch, cx, cy, W, H;
   uint32_t filters;
   float black, white, hl_white, hl_desat;
@@ -79,6 +81,7 @@ cudaError_t launch_hilite_assemble(const half4 *fine, int fw, int fh, const half
 
 // develop: hilite doub + demosaic + colour + filmcurv + llap curve + level 1 reduce (k_develop.cu)
 cudaError_t launch_develop(const dev_image_t &p, cudaStream_t s);
+cudaError_t init_develop();   // function attributes, once per device (outside stream capture)
 
 // llap pyramid (k_llap.cu)
 cudaError_t launch_llap_reduce(const __half *in, int iw, int ih, size_t iplane,

@@ -24,6 +24,27 @@ DEV float llap_curve_fn(float x, float g, float sigma, float shadows, float high
   return val;
 }
 
+// the same curve with the two divisions by loop invariants replaced by
+// products with their reciprocals, r2s = 1/(2 sigma), rden = 1/(2 sigma^2/3)
+// (differs from llap_curve_fn by at most a few ulp before the f16 store)
+DEV float llap_curve_rcp(float x, float g, float sigma, float r2s, float rden, float shadows, float highlights, float clarity)
+{
+  const float c = x - g;
+  float val;
+  const float ssigma = c > 0.0f ? sigma : -sigma;
+  const float shadhi = c > 0.0f ? shadows : highlights;
+  if(fabsf(c) > 2.0f * sigma) val = g + ssigma + shadhi * (c - ssigma);
+  else
+  {
+    const float t = gclamp(c * (c > 0.0f ? r2s : -r2s), 0.0f, 1.0f);
+    const float t2 = t * t;
+    const float mt = 1.0f - t;
+    val = g + ssigma * 2.0f * mt * t + t2 * (ssigma + ssigma * shadhi);
+  }
+  val += clarity * c * expf(-c * c * rden);
+  return val;
+}
+
 // histogram bin, bit exact with the oracle (see hist_log there for the method)
 DEV float hist_log(float x)
 {

@@ -1,9 +1,13 @@
 """Build libvkdt_cuda.so in-tree for sm_103a (nvcc + g++, parallel, no cmake).
 
-The kernels are compiled without floating point contraction (-fmad=false) so
-that every expression evaluates in the same order as the CPU oracle, which
-keeps data dependent branches (edge snapping, clipping tests, llap gamma
-selection, histogram bins) on the same side as the reference arithmetic.
+Arithmetic is FP32 with contraction (FMA), approximate division and the
+hardware exp where a result only feeds continuous arithmetic before its f16
+store. The computations whose rounding decides a branch of the reference
+(the demosaic covariance and its eigen decomposition, the llap gamma
+selection, the luminance, histogram bins, denoise/noop) are written with
+explicit IEEE intrinsics in the kernels, so they evaluate exactly as the CPU
+oracle does. VKDT_FMAD=false VKDT_NVCC_EXTRA=-prec-div=true VKDT_DEFINES=
+builds the fully IEEE variant for comparison.
 """
 import os
 import shutil
@@ -50,8 +54,11 @@ def build(verbose=False, force=False):
         obj = os.path.join(BUILD, f + ".o")
         objs.append(obj)
         if force or _newer([src] + headers, obj):
-            cmd = [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--expt-relaxed-constexpr",
-                   "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills"] + inc + ["-c", src, "-o", obj]
+            fmad = os.environ.get("VKDT_FMAD", "true")
+            defs = (os.environ.get("VKDT_DEFINES", "-DVKDT_FAST_EXP").split()
+                    + os.environ.get("VKDT_NVCC_EXTRA", "-prec-div=false").split())
+            cmd = [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=" + fmad, "--expt-relaxed-constexpr",
+                   "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills"] + defs + inc + ["-c", src, "-o", obj]
             jobs.append(cmd)
     for f in CPP_SOURCES:
         src = os.path.join(CSRC, f)

@@ -30,7 +30,7 @@ DEV void hilite_half_bayer(float m00, float m10, float m01, float m11, float whi
   if(cx >= white) cx = cz;
   if(cz >= white) cz = cx;
   h[0] = f16r(cw);
-  h[1] = f16r((cx + cz) / 2.0f);
+  h[1] = f16r((cx + cz) * 0.5f); // exactly the shader's /2
   h[2] = f16r(cy);
 }
 
@@ -48,7 +48,7 @@ DEV void hilite_half_xtrans(float c[9], int x, int y, float white, float h[3])
   if(((x + y) & 1) > 0) { r = c0; b = c1; }
   else                  { b = c0; r = c1; }
   h[0] = f16r(r);
-  h[1] = f16r((c[0] + c[2] + c[4] + c[6] + c[8]) / 5.0f);
+  h[1] = f16r(__fdiv_rn(c[0] + c[2] + c[4] + c[6] + c[8], 5.0f));
   h[2] = f16r(b);
 }
 

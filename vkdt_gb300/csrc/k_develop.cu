@@ -48,10 +48,10 @@ constexpr int NPL = 11;              // NUM_GAMMA curves + grey (llap/config.h:2
 struct smem_t
 {
   float M[MX][2][MB];          // hilite output mosaic, [y][x&1][x>>1]
-  float sw[3][CX][CX];         // splat weights for dot = 1/e0, 1/e1, 1/e0+1/e1
+  float sw[3][CX][CX];         // splat weights of the taps (+-1,0), (0,+-1), (+-1,+-1)
   float fw[3][CX][CX];         // fix weights, same
-  unsigned char ori[CX][CX];   // 0: evec (1,0), 1: evec (0,1), 2: no covariance (weights 1)
   float g[GX][2][GH];          // splat output, [y][x&1][x>>1]
+  float rg[GX][2][GH];         // 1 / (1e-4 + splat output)
   __half L0[NPL][LX][2][LH];   // llap level 0 planes, [y][slot&1][slot>>1]
   float B1[3][BX][BX];         // hilite coarse level (rgb) around the tile
   uint32_t hist[257];
@@ -81,7 +81,7 @@ DEV void filmcurv_px(const dev_image_t &p, const float in[3], float o[3])
 {
   float c0[3], c1[3];
   for(int k = 0; k < 3; k++) c0[k] = in[k] + p.fc_bias;
-  for(int k = 0; k < 3; k++) c1[k] = 1.0f - expf(-gpow_pos(fmaxf(c0[k], 1e-7f) * p.fc_il, p.fc_k));
+  for(int k = 0; k < 3; k++) c1[k] = 1.0f - curve_exp(-gpow_pos(fmaxf(c0[k], 1e-7f) * p.fc_il, p.fc_k));
   if(p.fc_mode == 3)
   {
     bool fx = false, fy = false, fz = false;
@@ -97,14 +97,10 @@ DEV void filmcurv_px(const dev_image_t &p, const float in[3], float o[3])
   for(int k = 0; k < 3; k++) o[k] = f16r(c1[k]);
 }
 
-// weight of a tap (i, j) from the per covariance table: dot = a0/e0 + a1/e1
-// with (a0, a1) = squared components of E (i, j)
-DEV float tap_weight(float w1, float w2, float w3, int ori, int i, int j)
+// weight of a 3x3 tap from the per covariance table (h: (+-1,0), v: (0,+-1), d: diagonal)
+DEV float tap_weight(float wh, float wv, float wd, int i, int j)
 {
-  const int a0 = ori == 0 ? i * i : (ori == 1 ? j * j : 0);
-  const int a1 = ori == 0 ? j * j : (ori == 1 ? i * i : 0);
-  const int k = a0 + 2 * a1;
-  return k == 0 ? 1.0f : (k == 1 ? w1 : (k == 2 ? w2 : w3));
+  return (i == 0 && j == 0) ? 1.0f : (i == 0 ? wv : (j == 0 ? wh : wd));
 }
 
 __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
@@ -198,7 +194,7 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
         if(((j + ii) & 1) != 1) continue;
         const int xs = 2 * scx + 2 + ii;
         px[k] = s.M[2 * scy + 2 + j][xs & 1][xs >> 1];
-        inv[k] = 1.0f / px[k];
+        inv[k] = __fdiv_rn(1.0f, px[k]);
         k++;
       }
       // i/px for i in {-1,0,1,2} is i*(1/px) exactly (scaling by +-1, 2 is exact)
@@ -216,8 +212,11 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
         smb += inv[k];
         k++;
       }
-      mw0 /= smw; mw1 /= smw;
-      mb0 /= smb; mb1 /= smb;
+      // (the products above are exact, so contraction cannot change them;
+      // the covariance sums below decide the snapped direction and are
+      // evaluated without contraction, in the shader's order)
+      mw0 = __fdiv_rn(mw0, smw); mw1 = __fdiv_rn(mw1, smw);
+      mb0 = __fdiv_rn(mb0, smb); mb1 = __fdiv_rn(mb1, smb);
       float Sw00 = 0, Sw01 = 0, Sw10 = 0, Sw11 = 0, Sb00 = 0, Sb01 = 0, Sb10 = 0, Sb11 = 0, sw = 0, sb = 0;
       k = 0;
 #pragma unroll
@@ -226,41 +225,56 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
       for(int ii = -1; ii < 3; ii++)
       {
         if(((j + ii) & 1) != 1) continue;
-        float p2 = px[k] * px[k];
-        float q0 = (float)ii - mw0, q1 = (float)j - mw1;
-        Sw00 += p2 * q0 * q0; Sw01 += p2 * q0 * q1; Sw10 += p2 * q1 * q0; Sw11 += p2 * q1 * q1;
-        sw += p2;
-        q0 = (float)ii - mb0; q1 = (float)j - mb1;
-        p2 = 1.0f / p2;
-        Sb00 += p2 * q0 * q0; Sb01 += p2 * q0 * q1; Sb10 += p2 * q1 * q0; Sb11 += p2 * q1 * q1;
-        sb += p2;
+        float p2 = __fmul_rn(px[k], px[k]);
+        float q0 = __fsub_rn((float)ii, mw0), q1 = __fsub_rn((float)j, mw1);
+        Sw00 = __fadd_rn(Sw00, __fmul_rn(__fmul_rn(p2, q0), q0));
+        Sw01 = __fadd_rn(Sw01, __fmul_rn(__fmul_rn(p2, q0), q1));
+        Sw10 = __fadd_rn(Sw10, __fmul_rn(__fmul_rn(p2, q1), q0));
+        Sw11 = __fadd_rn(Sw11, __fmul_rn(__fmul_rn(p2, q1), q1));
+        sw = __fadd_rn(sw, p2);
+        q0 = __fsub_rn((float)ii, mb0); q1 = __fsub_rn((float)j, mb1);
+        p2 = __fdiv_rn(1.0f, p2);
+        Sb00 = __fadd_rn(Sb00, __fmul_rn(__fmul_rn(p2, q0), q0));
+        Sb01 = __fadd_rn(Sb01, __fmul_rn(__fmul_rn(p2, q0), q1));
+        Sb10 = __fadd_rn(Sb10, __fmul_rn(__fmul_rn(p2, q1), q0));
+        Sb11 = __fadd_rn(Sb11, __fmul_rn(__fmul_rn(p2, q1), q1));
+        sb = __fadd_rn(sb, p2);
         k++;
       }
-      Sw00 /= sw; Sw01 /= sw; Sw10 /= sw; Sw11 /= sw;
-      Sb00 /= sb; Sb01 /= sb; Sb10 /= sb; Sb11 /= sb;
-      const float detw = Sw00 * Sw11 - Sw10 * Sw01, detb = Sb00 * Sb11 - Sb10 * Sb01;
+      Sw00 = __fdiv_rn(Sw00, sw); Sw01 = __fdiv_rn(Sw01, sw); Sw10 = __fdiv_rn(Sw10, sw); Sw11 = __fdiv_rn(Sw11, sw);
+      Sb00 = __fdiv_rn(Sb00, sb); Sb01 = __fdiv_rn(Sb01, sb); Sb10 = __fdiv_rn(Sb10, sb); Sb11 = __fdiv_rn(Sb11, sb);
+      const float detw = __fsub_rn(__fmul_rn(Sw00, Sw11), __fmul_rn(Sw10, Sw01));
+      const float detb = __fsub_rn(__fmul_rn(Sb00, Sb11), __fmul_rn(Sb10, Sb01));
       float eval[2], evec0[2], evec1[2];
       if(detw < detb) evd2x2(eval, evec0, evec1, Sw00, Sw10, Sw11);
       else            evd2x2(eval, evec0, evec1, Sb00, Sb10, Sb11);
-      eval[0] *= 0.2f; eval[1] *= 0.2f;
+      eval[0] = __fmul_rn(eval[0], 0.2f); eval[1] = __fmul_rn(eval[1], 0.2f);
       if(fabsf(evec0[0]) > fabsf(evec0[1])) { evec0[0] = 1.0f; evec0[1] = 0.0f; }
       else                                  { evec0[0] = 0.0f; evec0[1] = 1.0f; }
       v[0] = f16r(eval[0]); v[1] = f16r(eval[1]); v[2] = f16r(evec0[0]); v[3] = f16r(evec0[1]);
     }
-    // splat.comp:159-163 and fix.comp:21-29 weights of this entry
+    // splat.comp:159-163 and fix.comp:21-29 weights of this entry. E (i, j) is
+    // (i, j) for evec (1,0), (j, -i) for evec (0,1) and 0 without covariance,
+    // so a horizontal tap has dot = 1/e0 resp. 1/e1, a vertical one the other,
+    // a diagonal one 1/e0 + 1/e1, and every tap 0 without covariance
     const int ori = v[2] == 1.0f ? 0 : (v[3] == 1.0f ? 1 : 2);
-    s.ori[scy][scx] = (unsigned char)ori;
     {
-      const float r0 = 1.0f / gclamp(v[0], 0.01f, 25.0f), r1 = 1.0f / gclamp(v[1], 0.01f, 25.0f);
-      s.sw[0][scy][scx] = gclamp(expf(-0.5f * r0), 1e-4f, 1.0f);
-      s.sw[1][scy][scx] = gclamp(expf(-0.5f * r1), 1e-4f, 1.0f);
-      s.sw[2][scy][scx] = gclamp(expf(-0.5f * (r0 + r1)), 1e-4f, 1.0f);
+      const float r0 = __fdiv_rn(1.0f, gclamp(v[0], 0.01f, 25.0f)), r1 = __fdiv_rn(1.0f, gclamp(v[1], 0.01f, 25.0f));
+      const float wa = gclamp(expf(-0.5f * r0), 1e-4f, 1.0f);
+      const float wb = gclamp(expf(-0.5f * r1), 1e-4f, 1.0f);
+      const float wc = gclamp(expf(-0.5f * __fadd_rn(r0, r1)), 1e-4f, 1.0f);
+      s.sw[0][scy][scx] = ori == 0 ? wa : (ori == 1 ? wb : 1.0f);
+      s.sw[1][scy][scx] = ori == 0 ? wb : (ori == 1 ? wa : 1.0f);
+      s.sw[2][scy][scx] = ori == 2 ? 1.0f : wc;
     }
     {
-      const float r0 = 1.0f / (2.0f * gclamp(v[0], 1.0f, 49.0f)), r1 = 1.0f / (2.0f * gclamp(v[1], 1.0f, 49.0f));
-      s.fw[0][scy][scx] = gclamp(expf(-0.5f * r0), 1e-3f, 1.0f);
-      s.fw[1][scy][scx] = gclamp(expf(-0.5f * r1), 1e-3f, 1.0f);
-      s.fw[2][scy][scx] = gclamp(expf(-0.5f * (r0 + r1)), 1e-3f, 1.0f);
+      const float r0 = __fdiv_rn(1.0f, 2.0f * gclamp(v[0], 1.0f, 49.0f)), r1 = __fdiv_rn(1.0f, 2.0f * gclamp(v[1], 1.0f, 49.0f));
+      const float wa = gclamp(expf(-0.5f * r0), 1e-3f, 1.0f);
+      const float wb = gclamp(expf(-0.5f * r1), 1e-3f, 1.0f);
+      const float wc = gclamp(expf(-0.5f * __fadd_rn(r0, r1)), 1e-3f, 1.0f);
+      s.fw[0][scy][scx] = ori == 0 ? wa : (ori == 1 ? wb : 1.0f);
+      s.fw[1][scy][scx] = ori == 0 ? wb : (ori == 1 ? wa : 1.0f);
+      s.fw[2][scy][scx] = ori == 2 ? 1.0f : wc;
     }
   }
   __syncthreads();
@@ -275,8 +289,7 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
       if(sgx >= GX || sgy >= GX) continue;
       const int qx = mirror1(X0 - 2 + sgx, W), qy = mirror1(Y0 - 2 + sgy, H);
       const int ccx = (qx + 1) / 2 - (X0 / 2 - 1), ccy = (qy + 1) / 2 - (Y0 / 2 - 1);
-      const int ori = s.ori[ccy][ccx];
-      const float w1 = s.sw[0][ccy][ccx], w2 = s.sw[1][ccy][ccx], w3 = s.sw[2][ccy][ccx];
+      const float wh = s.sw[0][ccy][ccx], wv = s.sw[1][ccy][ccx], wd = s.sw[2][ccy][ccx];
       float rg = 0.0f, wg = 0.0f;
 #pragma unroll
       for(int j = -1; j <= 1; j++)
@@ -291,11 +304,13 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
         if(py >= H) py -= 6;
         const int mx = px - (X0 - 4), my = py - (Y0 - 4);
         const float col = s.M[my][mx & 1][mx >> 1];
-        const float weight = (ii == 0 && j == 0) ? 666.0f : tap_weight(w1, w2, w3, ori, ii, j);
+        const float weight = (ii == 0 && j == 0) ? 666.0f : tap_weight(wh, wv, wd, ii, j);
         rg += col * weight;
         wg += weight;
       }
-      s.g[sgy][sgx & 1][sgx >> 1] = f16r(rg / fmaxf(1e-8f, wg));
+      const float gv = f16r(rg / fmaxf(1e-8f, wg));
+      s.g[sgy][sgx & 1][sgx >> 1] = gv;
+      s.rg[sgy][sgx & 1][sgx >> 1] = 1.0f / (1e-4f + gv);
     }
   }
   __syncthreads();
@@ -315,8 +330,7 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
       const int gx0 = px - (X0 - 2), gy0 = py - (Y0 - 2);
       const float gc = s.g[gy0][gx0 & 1][gx0 >> 1];
       const int ccx = (px + 1) / 2 - (X0 / 2 - 1), ccy = (py + 1) / 2 - (Y0 / 2 - 1);
-      const int ori = s.ori[ccy][ccx];
-      const float w1 = s.fw[0][ccy][ccx], w2 = s.fw[1][ccy][ccx], w3 = s.fw[2][ccy][ccx];
+      const float wh = s.fw[0][ccy][ccx], wv = s.fw[1][ccy][ccx], wd = s.fw[2][ccy][ccx];
       float rr = 0.0f, rb = 0.0f, wr = 0.0f, wb = 0.0f, rg = 0.0f, wg = 0.0f;
       // demosaic/fix.comp:99-135, radius clamp(fixup+1, 1, 2) = 1 for the
       // default fixup 0 (the host rejects other values for this kernel)
@@ -328,11 +342,12 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
         const int c = cfa_bayer(px + ii, py + j);
         if(c == 1) { rg = gc; wg = 1.0f; continue; }
         const int gx = gx0 + ii, gy = gy0 + j;
-        const float gh = s.g[gy][gx & 1][gx >> 1];
+        const float rgh = s.rg[gy][gx & 1][gx >> 1];
         const int mx = px + ii - (X0 - 4), my = py + j - (Y0 - 4);
         const float col = s.M[my][mx & 1][mx >> 1];
-        const float weight = tap_weight(w1, w2, w3, ori, ii, j);
-        const float v = col * (1e-4f + gc) / (1e-4f + gh) * weight;
+        const float weight = tap_weight(wh, wv, wd, ii, j);
+        // col * (1e-4 + gc) / (1e-4 + gh) * weight with the reciprocal of the splat stage
+        const float v = col * (1e-4f + gc) * rgh * weight;
         if(c == 0) { rr += v; wr += weight; }
         else       { rb += v; wb += weight; }
       }
@@ -385,7 +400,7 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
         const float q10 = (P[0][1] + P[1][1]) * 0.25f;
         const float q01 = (P[1][0] + P[2][0]) * 0.25f;
         const float q11 = (P[1][1] + P[2][1]) * 0.25f;
-        const float r = (((q00 + q10) + q01) + q11) / 4.0f;
+        const float r = (((q00 + q10) + q01) + q11) * 0.25f;
         p.l1[k * p.l1plane + (size_t)oy * p.l1w + ox] = f2h(r);
       }
     }

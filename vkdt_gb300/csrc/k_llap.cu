@@ -36,35 +36,30 @@ DEV int gamma_hi_from_v(float v)
   return hi;
 }
 
-// one bilinear tap of the reference sampler at a half-texel multiple: x0 the
-// left texel, hx whether the x weight is 0.5 (else 0); same for y. fetch(x, y)
-// returns the mirrored texel. The arithmetic is the oracle's
-// (t00 (1-ax) + t10 ax)(1-ay) + (t01 (1-ax) + t11 ax) ay with the zero-weight
-// terms dropped, which is exact for finite texels.
-template<class F> DEV float tap(F fetch, int x0, bool hx, int y0, bool hy)
-{
-  const float r0 = hx ? fetch(x0, y0) * 0.5f + fetch(x0 + 1, y0) * 0.5f : fetch(x0, y0);
-  if(!hy) return r0;
-  const float r1 = hx ? fetch(x0, y0 + 1) * 0.5f + fetch(x0 + 1, y0 + 1) * 0.5f : fetch(x0, y0 + 1);
-  return r0 * 0.5f + r1 * 0.5f;
-}
-
 // llap/assemble.comp:54-58 gauss_expand = shared.glsl:99-127 sample_soft at
-// (o/2 + 0.5): three taps per axis at o/2+0.5 + {-1.5, 0, 1.5}
-template<class F> DEV float expand(F fetch, int ox, int oy)
+// (o/2 + 0.5): three bilinear taps per axis at o/2+0.5 + {-1.5, 0, 1.5}, which
+// land on texel centres or half way between two. Summed per axis the texel
+// weights are (.5 .5 1 .5 .5) around k = o/2 for even o and (1 .5 .5 1) from
+// k-1 for odd o; the expand is the separable sum of those, divided by 9.
+// PX, PY: parities of the output position. fetch(x, y) returns the texel.
+template<int PX, int PY, class F> DEV float expand(F fetch, int kx, int ky)
 {
-  int x0[3], y0[3];
-  bool hx[3], hy[3];
-  const int kx = ox >> 1, ky = oy >> 1;
-  if(ox & 1) { x0[0] = kx - 1; hx[0] = false; x0[1] = kx; hx[1] = true; x0[2] = kx + 2; hx[2] = false; }
-  else       { x0[0] = kx - 2; hx[0] = true;  x0[1] = kx; hx[1] = false; x0[2] = kx + 1; hx[2] = true; }
-  if(oy & 1) { y0[0] = ky - 1; hy[0] = false; y0[1] = ky; hy[1] = true; y0[2] = ky + 2; hy[2] = false; }
-  else       { y0[0] = ky - 2; hy[0] = true;  y0[1] = ky; hy[1] = false; y0[2] = ky + 1; hy[2] = true; }
+  constexpr int NX = PX ? 4 : 5, NY = PY ? 4 : 5;
+  constexpr int BXO = PX ? -1 : -2, BYO = PY ? -1 : -2;
   float r = 0.0f;
 #pragma unroll
-  for(int j = 0; j < 3; j++)
+  for(int b = 0; b < NY; b++)
+  {
+    float row = 0.0f;
 #pragma unroll
-  for(int i = 0; i < 3; i++) r += tap(fetch, x0[i], hx[i], y0[j], hy[j]);
+    for(int a = 0; a < NX; a++)
+    {
+      const float w = PX ? ((a == 0 || a == 3) ? 1.0f : 0.5f) : (a == 2 ? 1.0f : 0.5f);
+      row += w * fetch(kx + BXO + a, ky + BYO + b);
+    }
+    const float wy = PY ? ((b == 0 || b == 3) ? 1.0f : 0.5f) : (b == 2 ? 1.0f : 0.5f);
+    r += wy * row;
+  }
   return r / 9.0f;
 }
 
@@ -91,13 +86,13 @@ __global__ void __launch_bounds__(256) k_llap_reduce(const __half *__restrict__ 
     }
     const float q00 = (P[0][0] + P[1][0]) * 0.25f, q10 = (P[0][1] + P[1][1]) * 0.25f;
     const float q01 = (P[1][0] + P[2][0]) * 0.25f, q11 = (P[1][1] + P[2][1]) * 0.25f;
-    out[k * op + (size_t)y * ow + x] = f2h((((q00 + q10) + q01) + q11) / 4.0f);
+    out[k * op + (size_t)y * ow + x] = f2h((((q00 + q10) + q01) + q11) * 0.25f);
   }
 }
 
 // stage the 11 planes of the coarse level and the coarse assembled image of
 // one output tile: slot (sx, sy) holds the mirrored texel (bx+sx, by+sy)
-DEV void stage_coarse(__half (*sl)[FS][FS + 2], const __half *l1, int w1, int h1, size_t p1,
+DEV void stage_coarse(float (*sl)[FS][FS + 1], const __half *l1, int w1, int h1, size_t p1,
     const __half *coarse, int bx, int by)
 {
   for(int i = threadIdx.x; i < (NPL + 1) * FS * FS; i += blockDim.x)
@@ -106,7 +101,7 @@ DEV void stage_coarse(__half (*sl)[FS][FS + 2], const __half *l1, int w1, int h1
     const int sx = r % FS, sy = r / FS;
     const int gx = mirror1(bx + sx, w1), gy = mirror1(by + sy, h1);
     const __half *pl = k < NPL ? l1 + k * p1 : coarse;
-    sl[k][sy][sx] = pl[(size_t)gy * w1 + gx];
+    sl[k][sy][sx] = h2f(pl[(size_t)gy * w1 + gx]);
   }
 }
 
@@ -120,12 +115,36 @@ DEV bool tile_item(int t, int X0, int Y0, int w0, int h0, int &x, int &y)
   return x < w0 && y < h0;
 }
 
+// llap/assemble.comp:89-123 at one output pixel of parity (PX, PY). l0(k)
+// returns the fine level plane k at the pixel, sl holds the coarse level.
+template<int PX, int PY, class L0> DEV float assemble_px(L0 l0, float v, const float (*sl)[FS][FS + 1], int x, int y, int bx, int by)
+{
+  const int kx = x >> 1, ky = y >> 1;
+  auto fs = [&](int k) { return [=](int ix, int iy) { return sl[k][iy - by][ix - bx]; }; };
+  const float res = expand<PX, PY>(fs(NPL), kx, ky);
+  const int hi = gamma_hi_from_v(v);
+  const float glo = llap_gamma(hi - 1), ghi = llap_gamma(hi);
+  const float a = gclamp((v - glo) / (ghi - glo), 0.0f, 1.0f);
+  const float la = l0(hi - 1, glo) - expand<PX, PY>(fs(hi - 1), kx, ky);
+  const float lb = l0(hi, ghi) - expand<PX, PY>(fs(hi), kx, ky);
+  return res + la * (1.0f - a) + lb * a;
+}
+
 // llap/assemble.comp:89-123 for a stored level: output at the size of l0
+template<int PX, int PY> DEV void assemble_stored(const float (*sl)[FS][FS + 1], const __half *l0, size_t p0,
+    int w0, int x, int y, int bx, int by, __half *out)
+{
+  const size_t o = (size_t)y * w0 + x;
+  const float v = h2f(l0[NG * p0 + o]);
+  const float r = assemble_px<PX, PY>([&](int k, float) { return h2f(l0[k * p0 + o]); }, v, sl, x, y, bx, by);
+  out[o] = f2h(r);
+}
+
 __global__ void __launch_bounds__(256) k_llap_assemble(const __half *__restrict__ coarse, int first,
     const __half *__restrict__ l0, int w0, int h0, size_t p0,
     const __half *__restrict__ l1, int w1, int h1, size_t p1, __half *__restrict__ out)
 {
-  __shared__ __half sl[NPL + 1][FS][FS + 2];
+  __shared__ float sl[NPL + 1][FS][FS + 1];
   const int X0 = blockIdx.x * FT, Y0 = blockIdx.y * FT;
   const int bx = X0 / 2 - 2, by = Y0 / 2 - 2;
   stage_coarse(sl, l1, w1, h1, p1, first ? l1 + NG * p1 : coarse, bx, by);
@@ -134,24 +153,38 @@ __global__ void __launch_bounds__(256) k_llap_assemble(const __half *__restrict_
   {
     int x, y;
     if(!tile_item(t, X0, Y0, w0, h0, x, y)) continue;
-    auto fs = [&](int k) { return [=](int ix, int iy) { return h2f(sl[k][iy - by][ix - bx]); }; };
-    const float res = expand(fs(NPL), x, y);
-    const size_t o = (size_t)y * w0 + x;
-    const float v = h2f(l0[NG * p0 + o]);
-    const int hi = gamma_hi_from_v(v);
-    const float glo = (float)(hi - 1) / (10.0f - 1.0f), ghi = (float)hi / (10.0f - 1.0f);
-    const float a = gclamp((v - glo) / (ghi - glo), 0.0f, 1.0f);
-    const float la = h2f(l0[(hi - 1) * p0 + o]) - expand(fs(hi - 1), x, y);
-    const float lb = h2f(l0[hi * p0 + o]) - expand(fs(hi), x, y);
-    out[o] = f2h(res + la * (1.0f - a) + lb * a);
+    switch((x & 1) + 2 * (y & 1))
+    { // uniform per warp (tile_item hands a warp one parity class)
+      case 0: assemble_stored<0, 0>(sl, l0, p0, w0, x, y, bx, by, out); break;
+      case 1: assemble_stored<1, 0>(sl, l0, p0, w0, x, y, bx, by, out); break;
+      case 2: assemble_stored<0, 1>(sl, l0, p0, w0, x, y, bx, by, out); break;
+      default: assemble_stored<1, 1>(sl, l0, p0, w0, x, y, bx, by, out); break;
+    }
   }
 }
 
-// llap/assemble.comp for level 0 (l0 recomputed from the filmcurv output like
-// llap/curve.comp) fused with llap/colour.comp:141-160
+// llap/assemble.comp for level 0, the fine planes recomputed from the
+// filmcurv output like llap/curve.comp, fused with llap/colour.comp:141-160
+template<int PX, int PY> DEV void final_px(const dev_llap_k3_t &p, const float (*sl)[FS][FS + 1], int x, int y,
+    int bx, int by, float r2s, float rden)
+{
+  float rgb[4];
+  ld_half4(p.rgbf + (size_t)y * p.W + x, rgb[0], rgb[1], rgb[2], rgb[3]);
+  const float yv = lum2020(gclamp(rgb[0], -1000.0f, 1000.0f), gclamp(rgb[1], -1000.0f, 1000.0f), gclamp(rgb[2], -1000.0f, 1000.0f));
+  const float v = f16r(yv);
+  float yo_ = f16r(assemble_px<PX, PY>([&](int, float g) {
+      return f16r(llap_curve_rcp(yv, g, p.ll_sigma, r2s, rden, p.ll_shadows, p.ll_highlights, p.ll_clarity)); },
+    v, sl, x, y, bx, by));
+  const float yo = fmaxf(lum2020(rgb[0], rgb[1], rgb[2]), 1e-8f);
+  if(yo_ < yo) yo_ = yo * expf(1.0f * (yo_ - yo));
+  float o[3];
+  for(int k = 0; k < 3; k++) o[k] = fmaxf(0.0f, rgb[k] * yo_ / yo);
+  p.out[(size_t)y * p.W + x] = mk_half4(o[0], o[1], o[2], 1.0f);
+}
+
 __global__ void __launch_bounds__(256) k_llap_final(const dev_llap_k3_t p)
 {
-  __shared__ __half sl[NPL + 1][FS][FS + 2];
+  __shared__ float sl[NPL + 1][FS][FS + 1];
   const int X0 = blockIdx.x * FT, Y0 = blockIdx.y * FT;
   const int bx = X0 / 2 - 2, by = Y0 / 2 - 2;
   stage_coarse(sl, p.l1, p.l1w, p.l1h, p.l1plane, p.coarse, bx, by);
@@ -162,26 +195,13 @@ __global__ void __launch_bounds__(256) k_llap_final(const dev_llap_k3_t p)
   {
     int x, y;
     if(!tile_item(t, X0, Y0, p.W, p.H, x, y)) continue;
-    float rgb[4];
-    ld_half4(p.rgbf + (size_t)y * p.W + x, rgb[0], rgb[1], rgb[2], rgb[3]);
-    const float yv = lum2020(gclamp(rgb[0], -1000.0f, 1000.0f), gclamp(rgb[1], -1000.0f, 1000.0f), gclamp(rgb[2], -1000.0f, 1000.0f));
-    const float v = f16r(yv);
-    const int hi = gamma_hi_from_v(v);
-    const float glo = (float)(hi - 1) / (10.0f - 1.0f), ghi = (float)hi / (10.0f - 1.0f);
-    const float a = gclamp((v - glo) / (ghi - glo), 0.0f, 1.0f);
-    auto fs = [&](int k) { return [=](int ix, int iy) { return h2f(sl[k][iy - by][ix - bx]); }; };
-    const float res = expand(fs(NPL), x, y);
-    const float c0 = f16r(llap_curve_rcp(yv, glo, sig, r2s, rden, p.ll_shadows, p.ll_highlights, p.ll_clarity));
-    const float c1 = f16r(llap_curve_rcp(yv, ghi, sig, r2s, rden, p.ll_shadows, p.ll_highlights, p.ll_clarity));
-    const float la = c0 - expand(fs(hi - 1), x, y);
-    const float lb = c1 - expand(fs(hi), x, y);
-    float yo_ = f16r(res + la * (1.0f - a) + lb * a);
-    // llap/colour.comp
-    const float yo = fmaxf(lum2020(rgb[0], rgb[1], rgb[2]), 1e-8f);
-    if(yo_ < yo) yo_ = yo * expf(1.0f * (yo_ - yo));
-    float o[3];
-    for(int k = 0; k < 3; k++) o[k] = fmaxf(0.0f, rgb[k] * yo_ / yo);
-    p.out[(size_t)y * p.W + x] = mk_half4(o[0], o[1], o[2], 1.0f);
+    switch((x & 1) + 2 * (y & 1))
+    {
+      case 0: final_px<0, 0>(p, sl, x, y, bx, by, r2s, rden); break;
+      case 1: final_px<1, 0>(p, sl, x, y, bx, by, r2s, rden); break;
+      case 2: final_px<0, 1>(p, sl, x, y, bx, by, r2s, rden); break;
+      default: final_px<1, 1>(p, sl, x, y, bx, by, r2s, rden); break;
+    }
   }
 }
 

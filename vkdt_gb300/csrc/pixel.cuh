@@ -3,7 +3,16 @@
 #pragma once
 #include "common.cuh"
 
-DEV float llap_gamma(int i) { return (float)i / (10.0f - 1.0f); } // llap/llap.glsl:3-14
+// exp of the tone curves (llap/curve.comp, filmcurv): the accurate expf, or
+// the hardware ex2 approximation when built with VKDT_FAST_EXP
+#ifdef VKDT_FAST_EXP
+#define curve_exp __expf
+#else
+#define curve_exp expf
+#endif
+
+// llap/llap.glsl:3-14 (i / (NUM_GAMMA - 1), correctly rounded: it decides the plane selection)
+DEV float llap_gamma(int i) { return __fdiv_rn((float)i, 10.0f - 1.0f); }
 
 // llap/curve.comp:39-63 (shared with the final llap kernel)
 DEV float llap_curve_fn(float x, float g, float sigma, float shadows, float highlights, float clarity)
@@ -41,7 +50,7 @@ DEV float llap_curve_rcp(float x, float g, float sigma, float r2s, float rden, f
     const float mt = 1.0f - t;
     val = g + ssigma * 2.0f * mt * t + t2 * (ssigma + ssigma * shadhi);
   }
-  val += clarity * c * expf(-c * c * rden);
+  val += clarity * c * curve_exp(-c * c * rden);
   return val;
 }
 

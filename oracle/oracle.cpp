@@ -5,8 +5,13 @@
 // semantics, src/qvk/qvk.c:596-611, src/pipe/graph-run-nodes-allocate.h:39-96):
 // - texture()/textureLod() use LINEAR filtering with MIRRORED_REPEAT wrap and
 //   normalised coordinates. At texel centres this is the texel itself, which
-//   is how the restatement reads it (fetch_m). Elsewhere the bilinear weights
-//   are evaluated exactly in the arithmetic type (tex_bilinear).
+//   is how the restatement reads it (fetch_m). Elsewhere the sample position
+//   is rounded to 8 sub-texel bits and the bilinear weights are then
+//   evaluated in the arithmetic type (tex_bilinear).
+//
+// Pinned: at even sizes every stage of the float build is bit-identical to
+// the reference's own GLSL shaders compiled for the CPU (oracle/glsl, run by
+// oracle/glsl_ref.py), with and without the wavelet denoise.
 // - texelFetch() has no wrap; out-of-range reads are undefined in the
 //   reference and read as 0 here (fetch_z).
 // - textureGather(.., 0) returns component 0 of the 2x2 quad in the order
@@ -105,10 +110,14 @@ template<class T> static inline T fetch_m(const img_t<T> &im, int x, int y, int 
 {
   return im.ch(mirror(x, im.w), mirror(y, im.h), k);
 }
-// texture() anywhere: x,y are texel-space coordinates (normalised * size)
+// texture() anywhere: x,y are texel-space coordinates (normalised * size).
+// Vulkan samplers on the GPUs the reference runs on resolve the sample
+// position to 8 sub-texel bits (VkPhysicalDeviceLimits::subTexelPrecisionBits)
+// before the bilinear weights are formed, so the position is rounded to 1/256.
+template<class T> static inline T subtexel(T v) { return std::floor(v * T(256) + T(0.5)) / T(256); }
 template<class T> static inline void tex_bilinear(const img_t<T> &im, T x, T y, T out[4])
 {
-  const T xs = x - T(0.5), ys = y - T(0.5);
+  const T xs = subtexel(x - T(0.5)), ys = subtexel(y - T(0.5));
   const T fx = std::floor(xs), fy = std::floor(ys);
   const int x0 = (int)fx, y0 = (int)fy;
   const T ax = xs - fx, ay = ys - fy;

@@ -1,0 +1,75 @@
+"""Golden cases of the development path: their inputs, and the reader of the
+fixtures tests/golden/make_golden.py writes from the reference's own shaders
+(compiled for the CPU).
+
+Each case is a seeded synthetic mosaic (the product's scene generator), an
+image parameter set and module parameter overrides. The overrides are named
+by the oracle's parameter fields; PARAM_MAP gives the module parameter of the
+graph configuration each one sets.
+"""
+import json
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden")
+
+BAYER, XTRANS = 0x94949494, 9
+
+# noise profile of the generated mosaics, in raw DN (gaussian a, poissonian b)
+NOISE_A, NOISE_B = 8.0, 1.6
+
+CASES = {
+    # name: (wd, ht, filters, seed, white, overrides, stages kept)
+    "bayer_96x64": (96, 64, BAYER, 5, 16383.0, {}, ("hilite", "demosaic", "filmcurv", "llap")),
+    "bayer_16x16": (16, 16, BAYER, 6, 16383.0, {}, ("hilite", "demosaic", "llap")),
+    "bayer_130x98_clipped": (130, 98, BAYER, 7, 9000.0, {}, ("hilite", "demosaic", "llap")),
+    "bayer_128x96_params": (128, 96, BAYER, 8, 16383.0,
+                            {"co_exposure": 0.5, "fc_contrast": 1.4, "fc_colour": 1, "hl_white": 0.9,
+                             "ll_clarity": 0.5, "ll_levels": 4},
+                            ("filmcurv", "llap")),
+    "bayer_128x96_wavelet": (128, 96, BAYER, 9, 16383.0, {"dn_strength": 1.0},
+                             ("denoise", "hilite", "llap")),
+    "bayer_256x192_thumb": (256, 192, BAYER, 10, 16383.0, {"out_wd": 64, "out_ht": 48}, ("demosaic", "llap")),
+    "xtrans_132x96": (132, 96, XTRANS, 11, 16383.0, {}, ("hilite", "demosaic", "llap")),
+    "xtrans_132x96_wavelet": (132, 96, XTRANS, 12, 16383.0, {"dn_strength": 1.0}, ("denoise", "llap")),
+}
+
+# oracle parameter field -> (module, parameter) of the graph configuration
+PARAM_MAP = {
+    "dn_strength": ("denoise", "strength"),
+    "hl_white": ("hilite", "white"),
+    "co_exposure": ("colour", "exposure"),
+    "fc_contrast": ("filmcurv", "contrast"),
+    "fc_colour": ("filmcurv", "colour"),
+    "ll_clarity": ("llap", "clarity"),
+}
+
+
+def img_param(v, wd, ht, filters, white):
+    """The image parameters of a case, as a vkdt_gb300.ImgParam (noise in
+    the normalised form the modules read)."""
+    return v.default_img_param(wd=wd, ht=ht, filters=filters, white=white,
+                               noise_a=NOISE_A / (16383.0 - 512.0) ** 2, noise_b=NOISE_B / (16383.0 - 512.0))
+
+
+def oracle_params(oracle, overrides):
+    p = oracle.default_params()
+    for k, val in overrides.items():
+        setattr(p, k, val)
+    return p
+
+
+def path(name):
+    return os.path.join(GOLDEN, name + ".npz")
+
+
+def load(name):
+    """(mosaic, case tuple, {stage: float32 array}) of a committed fixture."""
+    z = np.load(path(name))
+    meta = json.loads(bytes(z["meta"]).decode())
+    if tuple(meta["case"][:5]) != tuple(CASES[name][:5]) or meta["case"][5] != CASES[name][5]:
+        raise RuntimeError("fixture %s was made for another case definition" % name)
+    out = {k[4:]: z[k].astype(np.float32) for k in z.files if k.startswith("out_")}
+    return z["mosaic"], CASES[name], out

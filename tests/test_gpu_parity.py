@@ -152,3 +152,52 @@ def test_timing_reports_every_launch(gpu):
     names = [n for n, _ in t]
     assert names[0] == "hilite:reduce" and names[-1] == "llap:colour" and "demosaic:fix" in names
     assert all(ms >= 0 for _, ms in t)
+
+
+# ---------------------------------------------------------------- golden
+# The committed fixtures hold the reference's own shaders' output (compiled
+# for the CPU) on seeded mosaics; the CUDA path is held to the tolerances above.
+
+import golden_cases as gc   # noqa: E402
+
+
+def develop_case(case, m):
+    wd, ht, filters, seed, white, overrides, stages = case
+    g = v.Graph()
+    g.set_input(wd, ht, gc.img_param(v, wd, ht, filters, white))
+    for k, val in overrides.items():
+        if k in gc.PARAM_MAP:
+            g.set_param(*gc.PARAM_MAP[k], np.int32(val) if isinstance(val, int) else float(val))
+    if "ll_levels" in overrides:
+        g.set_llap_levels(overrides["ll_levels"])
+    if "out_wd" in overrides:
+        g.set_output_size(overrides["out_wd"], overrides["out_ht"])
+    g.set_debug(True)
+    g.alloc()
+    out = g.run(m).astype(np.float32)
+    res = {"llap": out[..., :3], "denoise": g.debug_stage(0), "hilite": g.debug_stage(1),
+           "filmcurv": g.debug_stage(2)[..., :3]}
+    g.close()
+    return res
+
+
+@pytest.mark.parametrize("name", sorted(gc.CASES))
+def test_cuda_matches_reference_golden(gpu, name):
+    m, case, want = gc.load(name)
+    try:
+        got = develop_case(case, m)
+    except v._lib.VkdtError as e:
+        if e.code == v._lib.ERROR_FORMAT_NOT_SUPPORTED:
+            pytest.skip("not on the CUDA path yet: %s" % e)
+        raise
+    for s in ("hilite", "filmcurv", "llap"):
+        if s not in want:
+            continue
+        a, b = got[s], want[s]
+        if a.ndim == 2:
+            a, b = a[..., None], b[..., None]
+        assert a.shape == b.shape, (s, a.shape, b.shape)
+        st = summary(a, b)
+        assert st["flipped_frac"] <= 2e-2 and st["mean"] <= 1e-4, (name, s, st)
+    if "denoise" in want and case[5].get("dn_strength", 0) == 0:
+        assert np.array_equal(got["denoise"], want["denoise"])

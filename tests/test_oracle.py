@@ -118,3 +118,54 @@ def test_pyramid_depths(wd, ht, nl, nh):
         pytest.skip("depth arithmetic checked through the library for large sizes")
     r = oracle.develop(m, oracle.img_param(v.default_img_param(wd=wd, ht=ht)), stages=())
     assert r["llap_levels"] == nl and r["hilite_levels"] == nh
+
+
+# ---------------------------------------------------------------- pinning
+# The restatement against the reference's own shaders, compiled for the CPU:
+# committed fixtures (tests/golden, written by tests/golden/make_golden.py)
+# and, where that build exists here, fresh random cases.
+
+import golden_cases as gc   # noqa: E402
+
+
+@pytest.mark.parametrize("name", sorted(gc.CASES))
+def test_oracle_matches_reference_golden(name):
+    m, case, want = gc.load(name)
+    wd, ht, filters, seed, white, overrides, stages = case
+    ip = oracle.img_param(gc.img_param(v, wd, ht, filters, white))
+    got = oracle.develop(m, ip, params=gc.oracle_params(oracle, overrides), stages=stages)
+    for s in stages:
+        g = got[s] if got[s].ndim == 2 else got[s][..., :3]
+        assert g.shape == want[s].shape, (s, g.shape, want[s].shape)
+        assert np.array_equal(g, want[s]), (name, s, summary(g if g.ndim == 3 else g[..., None],
+                                                             want[s] if want[s].ndim == 3 else want[s][..., None]))
+
+
+def _ref_available():
+    try:
+        from oracle import glsl_ref
+        return glsl_ref.available()
+    except Exception:
+        return False
+
+
+@pytest.mark.skipif(not _ref_available(), reason="reference shaders not compiled here (oracle/_ref)")
+@pytest.mark.parametrize("seed", [101, 102, 103])
+def test_oracle_matches_reference_shaders_random(seed):
+    from oracle import glsl_ref
+    rng = np.random.default_rng(seed)
+    filters = gc.BAYER if seed != 103 else gc.XTRANS
+    blk = 2 if filters == gc.BAYER else 6
+    wd, ht = int(rng.integers(8, 40)) * blk, int(rng.integers(8, 30)) * blk
+    m = v.scene_host(v.make_scene(wd, ht, seed=seed, a=gc.NOISE_A, b=gc.NOISE_B, filters=filters))
+    ip = oracle.img_param(gc.img_param(v, wd, ht, filters, float(rng.uniform(9000, 16383))))
+    p = oracle.default_params()
+    p.dn_strength = float(rng.choice([0.0, 0.5, 1.0]))
+    p.co_exposure = float(rng.uniform(-1, 1))
+    p.ll_clarity = float(rng.uniform(0, 0.6))
+    st = ("denoise", "hilite", "demosaic", "colour", "filmcurv", "llap")
+    a = glsl_ref.develop(m, ip, p, stages=st)
+    b = oracle.develop(m, ip, params=p, stages=st)
+    for s in st:
+        x, y = (a[s], b[s]) if a[s].ndim == 2 else (a[s][..., :3], b[s][..., :3])
+        assert np.array_equal(x, y), (seed, wd, ht, s)

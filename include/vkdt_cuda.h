@@ -151,6 +151,35 @@ int  vkdt_cuda_graph_wait(vkdt_cuda_graph_t *graph, uint32_t timeout_ms);
  * no host copies). both buffers as the graph's source/sink layouts. */
 int  vkdt_cuda_graph_develop(vkdt_cuda_graph_t *graph, const void *d_mosaic, void *d_rgba, void *stream);
 
+/* vkdt_cuda_graph_develop without any allocation, for small images.
+ * No counterpart in the reference: there every buffer comes from the graph's
+ * own Vulkan allocation (graph-run-nodes-allocate.h).
+ *
+ * For callers that must not allocate device memory at the moment they
+ * develop (a display or video callback running beside busy streams, where
+ * cudaMalloc/cudaFree may synchronise the device; an embedding that owns
+ * every allocation). The intermediate buffers live in one fixed scratch array
+ * of VKDT_CUDA_STATIC_SCRATCH_BYTES per device, reserved when the library's
+ * CUDA module loads. The call makes no allocation of any kind.
+ * - the graph has had vkdt_cuda_graph_set_input and vkdt_cuda_graph_create_nodes
+ *   (after the last change of input, llap depth or output size) and is NOT
+ *   allocated; debug stages, timing and the histogram need an allocated graph.
+ * - d_mosaic and d_rgba are the caller's device buffers (source/sink layouts);
+ *   stream is a cudaStream_t (0 = the legacy default stream).
+ * - sizes whose intermediates exceed the scratch are rejected with
+ *   VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED (about 17.5 bytes per pixel: up to
+ *   about 1.9 megapixels, e.g. 1600x1200; 1920x1080 does not fit).
+ * - nothing in the scratch has to start at zero: each call clears the part it
+ *   uses on the stream before its kernels read it.
+ * - all calls on one device share the one scratch: calls that overlap (from
+ *   several threads, or on several streams before the earlier one finished)
+ *   race and corrupt each other's results. Order them on one stream.
+ * - the first call on each device looks up the scratch address
+ *   (cudaGetSymbolAddress), which may load the CUDA module: make that first
+ *   call before any stream capture begins. */
+#define VKDT_CUDA_STATIC_SCRATCH_BYTES (32u << 20)
+int  vkdt_cuda_graph_develop_static(vkdt_cuda_graph_t *graph, const void *d_mosaic, void *d_rgba, void *stream);
+
 /* per-launch device times of the last run with timing enabled (the -d perf
  * output of src/pipe/graph.c:881-932): names are "module:kernel" tokens of
  * the fused launch. returns the count. */

@@ -223,6 +223,13 @@ class Graph:
         check(self._l.vkdt_cuda_graph_develop(self._g, C.c_void_p(d_mosaic), C.c_void_p(d_rgba), C.c_void_p(stream)),
               "develop")
 
+    def develop_static(self, d_mosaic, d_rgba, stream=0):
+        """vkdt_cuda_graph_develop_static: develop a small image on the
+        library's fixed device scratch, allocating nothing (the graph must
+        not be allocated; call create_nodes first)."""
+        check(self._l.vkdt_cuda_graph_develop_static(self._g, C.c_void_p(d_mosaic), C.c_void_p(d_rgba),
+                                                     C.c_void_p(stream)), "develop_static")
+
     def times(self):
         n = self._l.vkdt_cuda_graph_query_times(self._g, None, None, None, 0)
         ms = (C.c_float * max(n, 1))()

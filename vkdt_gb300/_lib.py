@@ -97,6 +97,7 @@ _SIGS = {
     "vkdt_cuda_graph_run": (C.c_int, [_P, _P, C.c_uint32]),
     "vkdt_cuda_graph_wait": (C.c_int, [_P, C.c_uint32]),
     "vkdt_cuda_graph_develop": (C.c_int, [_P, _P, _P, _P]),
+    "vkdt_cuda_graph_develop_static": (C.c_int, [_P, _P, _P, _P]),
     "vkdt_cuda_graph_set_timing": (C.c_int, [_P, C.c_int]),
     "vkdt_cuda_graph_query_times": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.c_int]),
     "vkdt_cuda_graph_set_hist": (C.c_int, [_P, C.c_int]),

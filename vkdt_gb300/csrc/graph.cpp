@@ -17,6 +17,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -861,6 +862,64 @@ int vkdt_cuda_graph_develop(vkdt_cuda_graph_t *g, const void *d_mosaic, void *d_
   if(r) return r;
   CU(cudaEventRecord(g->done, s));
   return 0;
+}
+
+// Callers that may not allocate device memory when they develop (a display
+// or video callback beside busy streams, where cudaMalloc/cudaFree can
+// synchronise the device; an embedding that owns every allocation) get the
+// same kernel sequence on a fixed scratch array instead of the graph's arena.
+int vkdt_cuda_graph_develop_static(vkdt_cuda_graph_t *g, const void *d_mosaic, void *d_rgba, void *stream)
+{
+  static std::mutex lock;                 // guards the per-device address table only
+  static void *scratch[64] = { nullptr };  // scratch address per device, looked up once
+  if(!g) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "null graph");
+  if(g_device < 0) return fail(VKDT_CUDA_ERROR_INITIALIZATION_FAILED, "vkdt_cuda_init was not called");
+  if(g->allocated) return fail(VKDT_CUDA_INCOMPLETE, "graph owns device buffers: use vkdt_cuda_graph_develop");
+  if(!g->nodes_ready) return fail(VKDT_CUDA_INCOMPLETE, "call vkdt_cuda_graph_create_nodes first");
+  if(g->debug || g->timing || g->want_hist)
+    return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "debug stages, timing and the histogram need an allocated graph");
+  if(!d_mosaic || !d_rgba) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "null device buffer");
+  const uint32_t *b = g->ip.crop_aabb;
+  if(g->W != (int)(b[2] - b[0]) || g->H != (int)(b[3] - b[1]))
+    return fail(VKDT_CUDA_INCOMPLETE, "input changed since vkdt_cuda_graph_create_nodes");
+  // the arena plan of vkdt_cuda_graph_alloc without the caller's source, sink and debug buffers
+  size_t off = 0;
+  auto take = [&](size_t bytes) { const size_t o = off; off = align_up(off + bytes); return o; };
+  for(auto &l : g->hr) l.off = take((size_t)l.w * l.h * 8);
+  for(auto &l : g->hb) l.off = take((size_t)l.w * l.h * 8);
+  g->off_rgbf = take((size_t)g->W * g->H * 8);
+  for(auto &l : g->lp) l.off = take((size_t)l.w * l.h * 2 * 11);
+  for(auto &l : g->la) l.off = take((size_t)l.w * l.h * 2);
+  g->off_hist = take(257 * 4);
+  g->off_lut = take(65536 * 2);
+  if(off > VKDT_CUDA_STATIC_SCRATCH_BYTES)
+    return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED,
+                "%dx%d needs %zu bytes of scratch, the static scratch holds %u: use an allocated graph",
+                g->W, g->H, off, VKDT_CUDA_STATIC_SCRATCH_BYTES);
+  int dev = -1;
+  CU(cudaGetDevice(&dev));
+  if(dev < 0 || dev >= 64) return fail(VKDT_CUDA_ERROR_INITIALIZATION_FAILED, "device %d out of range", dev);
+  unsigned char *base = nullptr;
+  {
+    std::lock_guard<std::mutex> guard(lock);
+    if(!scratch[dev])
+    {
+      void *p = nullptr;
+      const cudaError_t e = static_scratch_address(&p);
+      if(e != cudaSuccess || !p)
+        return fail(e != cudaSuccess ? cuda_code(e) : VKDT_CUDA_ERROR_INITIALIZATION_FAILED,
+                    "no address for the static scratch on device %d: %s", dev, cudaGetErrorString(e));
+      scratch[dev] = p;
+    }
+    base = (unsigned char *)scratch[dev];
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  CU(cudaMemsetAsync(base, 0, off, s));
+  CU(launch_noop_lut((__half *)(base + g->off_lut), g->ip.black[0] / 65535.0f, g->ip.white[0] / 65535.0f, s));
+  g->arena = base;                         // the kernels address the scratch for this call only
+  const int r = enqueue(g, s, d_mosaic, d_rgba, false);
+  g->arena = nullptr;
+  return r;
 }
 
 int vkdt_cuda_graph_wait(vkdt_cuda_graph_t *g, uint32_t timeout_ms)

@@ -94,3 +94,6 @@ cudaError_t launch_llap_final(const dev_llap_k3_t &p, cudaStream_t s);
 struct scene_layout_t;
 cudaError_t launch_scene(const scene_layout_t *d_layout, int wd, int ht, uint16_t *out, cudaStream_t s);
 cudaError_t launch_hist_rgba(const half4 *in, int W, int H, uint32_t *hist, cudaStream_t s);
+// k_static.cu: the fixed scratch of vkdt_cuda_graph_develop_static (address on the current device)
+cudaError_t static_scratch_address(void **ptr);
+cudaError_t launch_noop_lut(__half *lut, float black, float white, cudaStream_t s);

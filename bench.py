@@ -35,6 +35,7 @@ BLACK, WHITE = 512.0, 16383.0
 NOISE_A, NOISE_B = 8.0, 1.6
 LEVELS = 6
 RING = 4
+DENOISE = 0.0
 
 
 def img_param(v, wd, ht):
@@ -44,9 +45,12 @@ def img_param(v, wd, ht):
 
 
 def config():
-    return {"workload": "24 MP darkroom graph, one image per step", "wd": WD, "ht": HT, "cfa": "rggb",
+    return {"workload": "%d MP darkroom graph, one image per step%s" % (round(WD * HT / 1e6),
+                                                                       ", wavelet denoise" if DENOISE > 0 else ""),
+            "wd": WD, "ht": HT, "cfa": "rggb", "denoise_strength": DENOISE,
             "bits": 14, "black": BLACK, "white": WHITE, "noise_a_dn": NOISE_A, "noise_b_dn": NOISE_B,
-            "llap_levels": LEVELS, "graph": "denoise(noop)->hilite->demosaic->colour->filmcurv->llap",
+            "llap_levels": LEVELS,
+            "graph": "denoise(%s)->hilite->demosaic->colour->filmcurv->llap" % ("wavelet" if DENOISE > 0 else "noop"),
             "l2": "ring of %d distinct resident mosaics (%d MB > 129 MB L2)" % (RING, RING * WD * HT * 2 // 2 ** 20)}
 
 
@@ -104,6 +108,7 @@ def cpu_baseline(seconds=10.0, ref=False):
     ip = oracle.img_param(img_param(v, wd, ht))
     p = oracle.default_params()
     p.ll_levels = LEVELS
+    p.dn_strength = DENOISE
     kind = "port"
     run = lambda: oracle.develop(m, ip, params=p, stages=("llap",))
     if ref:
@@ -142,7 +147,7 @@ def run_reference(args):
 
 
 def main():
-    global WD, HT, RING, LEVELS
+    global WD, HT, RING, LEVELS, DENOISE
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
@@ -152,9 +157,11 @@ def main():
     ap.add_argument("--size", default="%dx%d" % (WD, HT), help="WxH of the mosaic (profiling of smaller cases)")
     ap.add_argument("--ring", type=int, default=RING, help="number of resident inputs")
     ap.add_argument("--levels", type=int, default=LEVELS, help="llap pyramid depth (0 = automatic)")
+    ap.add_argument("--denoise", type=float, default=DENOISE,
+                    help="denoise strength (0 = the darkroom default, denoise/noop; > 0 the wavelet path)")
     args = ap.parse_args()
     WD, HT = [int(x) for x in args.size.lower().split("x")]
-    RING, LEVELS = args.ring, args.levels
+    RING, LEVELS, DENOISE = args.ring, args.levels, args.denoise
     if args.impl == "reference":
         return run_reference(args)
 
@@ -180,6 +187,8 @@ def main():
         g.set_input(WD, HT, img_param(v, WD, HT))
         if LEVELS:
             g.set_llap_levels(LEVELS)
+        if DENOISE > 0:
+            g.set_param("denoise", "strength", DENOISE)
         g.alloc()
         src, _ = g.device_buffers()
         v.scene_device(v.make_scene(WD, HT, seed=1000 * rank + i, image_id=i, a=NOISE_A, b=NOISE_B), src, sp)
@@ -220,6 +229,8 @@ def main():
     gt.set_input(WD, HT, img_param(v, WD, HT))
     if LEVELS:
         gt.set_llap_levels(LEVELS)
+    if DENOISE > 0:
+        gt.set_param("denoise", "strength", DENOISE)
     gt.set_timing(True)
     gt.alloc()
     src, _ = gt.device_buffers()

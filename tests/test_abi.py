@@ -108,6 +108,22 @@ def test_create_nodes_forced_depth():
     assert kinds.count(("llap", "reduce")) == 5
 
 
+def test_create_nodes_wavelet_denoise():
+    # denoise/main.c:225-333: four half size scales, assemble, half, full size doub, one launch each
+    g = v.Graph()
+    g.set_input(6000, 4000, v.default_img_param(wd=6000, ht=4000))
+    g.set_param("denoise", "strength", 1.0)
+    g.create_nodes()
+    n = g.nodes()
+    g.close()
+    dn = [x for x in n if x[0] == "denoise"]
+    assert [x[1] for x in dn] == ["downcov", "down", "down", "down", "assemble", "half", "doub"]
+    assert all(x[2:4] == (3000, 2000) for x in dn[:6]) and dn[6][2:4] == (6000, 4000)
+    assert len({x[5] for x in dn}) == 7
+    for name, kernel, *_ in n:
+        assert v.supports(name, kernel), (name, kernel)
+
+
 def test_create_nodes_rejects_bad_input():
     g = v.Graph()
     ip = v.default_img_param(wd=101, ht=100)

@@ -96,6 +96,30 @@ def test_parameters(gpu):
     check_rgb(g["llap"], r["llap"], de_stage=True)
 
 
+@pytest.mark.parametrize("wd,ht", [(1000, 742), (2048, 1536)])
+def test_wavelet_denoise(gpu, wd, ht):
+    # denoise strength 1: the wavelet nodes (half, downcov, down x3, assemble, doub)
+    # before the rest of the path; the noisier profile of the 24 MP recipe
+    op = oracle.default_params()
+    op.dn_strength = 1.0
+    na, nb = 8.0 / (16383 - 512) ** 2, 1.6 / (16383 - 512)
+    m = v.scene_host(v.make_scene(wd, ht, seed=wd + 1, a=8.0, b=1.6))
+    ip = v.default_img_param(wd=wd, ht=ht, noise_a=na, noise_b=nb)
+    with v.Graph() as g:
+        g.set_input(wd, ht, ip)
+        g.set_param("denoise", "strength", 1.0)
+        g.set_debug(True)
+        g.alloc()
+        out = g.run(m).astype(np.float32)
+        dn = g.debug_stage(0)
+        fc = g.debug_stage(2)
+    r = oracle.develop(m, oracle.img_param(ip), params=op, stages=("denoise", "filmcurv", "llap"))
+    s_d = summary(dn[..., None], r["denoise"][..., None])
+    assert s_d["flipped_frac"] <= 2e-3 and s_d["mean"] <= 1e-4, s_d
+    check_rgb(fc, r["filmcurv"], de_stage=True)
+    check_rgb(out, r["llap"], de_stage=True)
+
+
 def test_fp64_reference_error(gpu):
     # the error of the CUDA path against the FP64 build of the same restatement
     wd, ht = 512, 384
@@ -199,5 +223,9 @@ def test_cuda_matches_reference_golden(gpu, name):
         assert a.shape == b.shape, (s, a.shape, b.shape)
         st = summary(a, b)
         assert st["flipped_frac"] <= 2e-2 and st["mean"] <= 1e-4, (name, s, st)
-    if "denoise" in want and case[5].get("dn_strength", 0) == 0:
-        assert np.array_equal(got["denoise"], want["denoise"])
+    if "denoise" in want:
+        if case[5].get("dn_strength", 0) == 0:
+            assert np.array_equal(got["denoise"], want["denoise"])
+        else:
+            st = summary(got["denoise"][..., None], want["denoise"][..., None])
+            assert st["flipped_frac"] <= 2e-2 and st["mean"] <= 1e-4, (name, "denoise", st)

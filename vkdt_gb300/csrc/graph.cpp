@@ -155,6 +155,8 @@ struct vkdt_cuda_graph_t
   std::vector<level_t> lp, la;   // llap planes level 1..nl-1 (index 0 = level 1), assembled A[1..nl-2]
   int nl = 0;
   size_t off_src = 0, off_rgbf = 0, off_out = 0, off_hist = 0, off_dbg0 = 0, off_dbg1 = 0, off_lut = 0, arena_bytes = 0;
+  bool wavelet = false;          // denoise strength > 0: the wavelet nodes run before hilite
+  size_t off_dnh = 0, off_dnl[4] = { 0, 0, 0, 0 }, off_dna = 0, off_dn = 0, off_idlut = 0;
   unsigned char *arena = nullptr;
   void *h_src = nullptr, *h_sink = nullptr;
   size_t src_bytes = 0, sink_bytes = 0;
@@ -236,6 +238,10 @@ const double M_cat16_Mi[9] = { 1.86206786, -1.01125463,  0.14918677, 0.38752654,
 const double M_cat16_M[9]  = { 0.401288, 0.650173, -0.051461, -0.250268, 1.204414,  0.045854, -0.002079, 0.048952,  0.953127 };
 const double M_rec2020_to_xyz[9] = { 0.636958048301290991, 0.144616903586208406, 0.168880975164172054, 0.26270021201126692, 0.677998071518871148, 0.0593017164698619384, 4.9999999999999999e-17, 0.0280726930490874452, 1.06098505771079066 };
 const double M_xyz_to_rec2020[9] = { 1.71665119, -0.35567078, -0.25336628, -0.66668435,  1.61648124,  0.01576855, 0.01763986, -0.04277061, 0.94210312 };
+const double M_rec709_to_rec2020[9] = { 0.62750375, 0.32927542, 0.04330266, 0.06910828, 0.91951916, 0.0113596, 0.01639406, 0.08801125, 0.89538035 };
+const double M_rec2020_to_rec709[9] = { 1.66022677, -0.58754761, -0.07283825, -0.12455334,  1.13292605, -0.00834963, -0.01815514, -0.10060303,  1.11899817 };
+const double M_rec709_to_yuv[9] = { 0.299, 0.587, 0.114, -0.147, -0.289, 0.436, 0.615, -0.515, -0.100 };
+const double M_yuv_to_rec709[9] = { 1.0, -3.94570707e-05, 1.13982797, 1.0, -3.94610164e-01, -5.80500316e-01, 1.0, 2.03199968, -4.81376263e-04 };
 
 // colour/main.c:219-292 commit_params (matrix path): writes p_wb back into the
 // module's params when it was derived from the camera coefficients
@@ -270,7 +276,6 @@ size_t align_up(size_t v) { return (v + 255) & ~(size_t)255; }
 
 int check_supported_params(vkdt_cuda_graph_t *g)
 {
-  if(g->mod("denoise")->f("strength") > 0.0f) return fail(VKDT_CUDA_INCOMPLETE, "denoise strength > 0 (wavelet path) is not built in this version");
   if(g->mod("demosaic")->n("colour") != 0) return fail(VKDT_CUDA_INCOMPLETE, "demosaic colour (fixup radius) != 0 not supported");
   if(g->mod("demosaic")->n("method") != 0) return fail(VKDT_CUDA_INCOMPLETE, "demosaic method %d not supported", g->mod("demosaic")->n("method"));
   const int fm = g->mod("filmcurv")->n("colour");
@@ -319,12 +324,51 @@ int fill_image(vkdt_cuda_graph_t *g, dev_image_t &d, const void *d_src, void *d_
   return 0;
 }
 
+// the push constants and uniforms of the wavelet denoise nodes (denoise/main.c:133-333)
+void fill_denoise(vkdt_cuda_graph_t *g, dev_denoise_t &p, const void *d_src)
+{
+  memset(&p, 0, sizeof(p));
+  p.mosaic = (const uint16_t *)d_src;
+  p.pitch = g->in_wd; p.in_w = g->in_wd; p.in_h = g->in_ht;
+  p.cx = (int)g->ip.crop_aabb[0]; p.cy = (int)g->ip.crop_aabb[1];
+  p.W = g->W; p.H = g->H; p.hw = g->hw; p.hh = g->hh;
+  for(int k = 0; k < 3; k++)
+  {
+    p.black[k] = g->ip.black[k] / 65535.0f;
+    p.white[k] = g->ip.white[k] / 65535.0f;
+    p.wb[k] = g->ip.whitebalance[k];
+  }
+  p.na = g->ip.noise_a; p.nb = g->ip.noise_b;
+  module_t *dn = g->mod("denoise");
+  for(int k = 0; k < 3; k++) p.edge_gain[k] = std::exp2(12.0f * dn->f("edges", k) + dn->f("edges", 3));
+  p.strength = dn->f("strength"); p.luma = dn->f("luma"); p.detail = dn->f("detail");
+  p.thrs0 = std::pow(p.strength, 4.0f);
+  p.block_f = 1.414213f;
+  const float bl[4] = { 0.7000f, 0.4900f, 0.3430f, 0.2401f };
+  for(int l = 0; l < 4; l++) p.bscale[l] = bl[l] / p.block_f;
+  for(int l = 0; l < 4; l++) p.pl[l] = std::pow(0.7f, (float)l);
+  m3_mul(M_rec709_to_yuv, M_rec2020_to_rec709, p.rgb_to_yuv);
+  m3_mul(M_rec709_to_rec2020, M_yuv_to_rec709, p.yuv_to_rgb);
+  p.half_img = g->at<half4>(g->off_dnh);
+  for(int i = 0; i < 4; i++) p.lvl[i] = g->at<half4>(g->off_dnl[i]);
+  p.asm_img = g->at<half4>(g->off_dna);
+  p.dn = g->at<__half>(g->off_dn);
+}
+
 // the kernel sequence of one run. ev != null records timing events around each launch.
 int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out, bool timed)
 {
   dev_image_t d;
   int r = fill_image(g, d, d_src, d_out);
   if(r) return r;
+  dev_denoise_t dd;
+  if(g->wavelet)
+  { // the develop kernels read the denoised f16 mosaic through the identity code table
+    fill_denoise(g, dd, d_src);
+    d.mosaic = reinterpret_cast<const uint16_t *>(dd.dn);
+    d.noop_lut = g->at<__half>(g->off_idlut);
+    d.pitch = g->W; d.cx = 0; d.cy = 0;
+  }
   module_t *hl = g->mod("hilite");
   const float white = hl->f("white"), desat = hl->f("desat"), soft = hl->f("soft");
   const float wb[3] = { g->ip.whitebalance[0], g->ip.whitebalance[1], g->ip.whitebalance[2] };
@@ -336,6 +380,13 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
   };
   if(g->want_hist) CU(cudaMemsetAsync(g->at<uint32_t>(g->off_hist), 0, 257 * sizeof(uint32_t), s));
   if((r = mark())) return r;
+  // 0. wavelet denoise (strength > 0): half, downcov, down x3, assemble, doub
+  if(g->wavelet)
+    for(int stage = 0; stage < 7; stage++)
+    {
+      CU(launch_denoise(dd, stage, s));
+      if((r = mark())) return r;
+    }
   // 1. noop + hilite half + first hilite reduce
   dev_hilite_k1_t k1;
   memset(&k1, 0, sizeof(k1));
@@ -425,7 +476,8 @@ void vkdt_cuda_cleanup(void) { g_device = -1; }
 int vkdt_cuda_supports(dt_token_t name, dt_token_t kernel)
 {
   static const char *sup[][2] = {
-    { "denoise", "noop" }, { "hilite", "half" }, { "hilite", "reduce" }, { "hilite", "assemble" }, { "hilite", "doub" },
+    { "denoise", "noop" }, { "denoise", "half" }, { "denoise", "downcov" }, { "denoise", "down" },
+    { "denoise", "assemble" }, { "denoise", "doub" }, { "hilite", "half" }, { "hilite", "reduce" }, { "hilite", "assemble" }, { "hilite", "doub" },
     { "demosaic", "down" }, { "demosaic", "gauss" }, { "demosaic", "splat" }, { "demosaic", "fix" },
     { "colour", "main" }, { "filmcurv", "main" }, { "OpenDRT", "hist" },
     { "llap", "curve" }, { "llap", "reduce" }, { "llap", "assemble" }, { "llap", "colour" } };
@@ -651,7 +703,16 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
 
   // node lists as the modules' create_nodes emit them
   int fused = 0;
-  add_node(g, "denoise", "noop", g->W, g->H, 1, -1);
+  g->wavelet = g->mod("denoise")->f("strength") > 0.0f;
+  if(!g->wavelet) add_node(g, "denoise", "noop", g->W, g->H, 1, -1);
+  else
+  { // denoise/main.c:225-333: 4 scales at the half size, assemble, half, doub
+    add_node(g, "denoise", "downcov", g->hw, g->hh, 1, -1);
+    for(int i = 1; i < 4; i++) add_node(g, "denoise", "down", g->hw, g->hh, 1, -1);
+    add_node(g, "denoise", "assemble", g->hw, g->hh, 1, -1);
+    add_node(g, "denoise", "half", g->hw, g->hh, 1, -1);
+    add_node(g, "denoise", "doub", g->W, g->H, 1, -1);
+  }
   // hilite/main.c:5-90
   add_node(g, "hilite", "half", g->hw, g->hh, 1, -1);
   add_node(g, "hilite", "doub", g->hw, g->hh, 1, -1);
@@ -696,6 +757,12 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
   // the fused launches and which nodes they compute
   g->launches.clear();
   auto launch = [&](const char *n, const char *k) { g->launches.push_back({ tkn(n), tkn(k) }); return (int)g->launches.size() - 1; };
+  int L_dn[7] = { -1, -1, -1, -1, -1, -1, -1 };
+  if(g->wavelet)
+  {
+    const char *dk[7] = { "half", "downcov", "down", "down", "down", "assemble", "doub" };
+    for(int i = 0; i < 7; i++) L_dn[i] = launch("denoise", dk[i]);
+  }
   const int L_k1 = launch("hilite", "reduce");
   std::vector<int> L_hr, L_ha, L_lr, L_la;
   for(size_t l = 1; l < g->hr.size(); l++) L_hr.push_back(launch("hilite", "reduce"));
@@ -707,6 +774,12 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
   (void)fused;
   for(auto &n : g->nodes)
   {
+    if(n.name == tkn("denoise") && g->wavelet)
+    { // one launch per node, in create_nodes order: downcov, down x3, assemble, half, doub
+      static const int map[7] = { 1, 2, 3, 4, 5, 0, 6 };
+      n.fused = L_dn[map[&n - &g->nodes[0]]];
+      continue;
+    }
     if(n.name == tkn("denoise") || n.kernel == tkn("doub") || n.name == tkn("demosaic") || n.name == tkn("colour")
         || n.name == tkn("OpenDRT") || n.name == tkn("filmcurv") || n.kernel == tkn("curve")) n.fused = L_dev;
     if(n.name == tkn("hilite") && n.kernel == tkn("half")) n.fused = L_k1;
@@ -752,9 +825,24 @@ int vkdt_cuda_graph_alloc(vkdt_cuda_graph_t *g, uint64_t *device_bytes)
   g->off_hist = take(257 * 4);
   g->off_lut = take(65536 * 2);
   if(g->debug) { g->off_dbg0 = take((size_t)g->W * g->H * 2); g->off_dbg1 = take((size_t)g->W * g->H * 2); }
+  if(g->wavelet)
+  { // the half size nodes of the wavelet denoise and its full size output
+    const size_t hb = (size_t)g->hw * g->hh * 8;
+    g->off_dnh = take(hb);
+    for(int i = 0; i < 4; i++) g->off_dnl[i] = take(hb);
+    g->off_dna = take(hb);
+    g->off_dn = take((size_t)g->W * g->H * 2);
+    g->off_idlut = take(65536 * 2);
+  }
   g->arena_bytes = off;
   CU(cudaMalloc((void **)&g->arena, g->arena_bytes));
   CU(cudaMemset(g->arena, 0, g->arena_bytes));
+  if(g->wavelet)
+  {
+    std::vector<uint16_t> id(65536);
+    for(int v = 0; v < 65536; v++) id[v] = (uint16_t)v;
+    CU(cudaMemcpy(g->arena + g->off_idlut, id.data(), 65536 * 2, cudaMemcpyHostToDevice));
+  }
   { // denoise/noop.comp:385 for every u16 code, channel 0 black/white (denoise/main.c:165-168)
     std::vector<__half> lut(65536);
     const float black = g->ip.black[0] / 65535.0f, white = g->ip.white[0] / 65535.0f;
@@ -876,8 +964,8 @@ int vkdt_cuda_graph_develop_static(vkdt_cuda_graph_t *g, const void *d_mosaic, v
   if(g_device < 0) return fail(VKDT_CUDA_ERROR_INITIALIZATION_FAILED, "vkdt_cuda_init was not called");
   if(g->allocated) return fail(VKDT_CUDA_INCOMPLETE, "graph owns device buffers: use vkdt_cuda_graph_develop");
   if(!g->nodes_ready) return fail(VKDT_CUDA_INCOMPLETE, "call vkdt_cuda_graph_create_nodes first");
-  if(g->debug || g->timing || g->want_hist)
-    return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "debug stages, timing and the histogram need an allocated graph");
+  if(g->debug || g->timing || g->want_hist || g->wavelet)
+    return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "debug stages, timing, the histogram and the wavelet denoise need an allocated graph");
   if(!d_mosaic || !d_rgba) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "null device buffer");
   const uint32_t *b = g->ip.crop_aabb;
   if(g->W != (int)(b[2] - b[0]) || g->H != (int)(b[3] - b[1]))

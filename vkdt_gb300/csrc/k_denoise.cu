@@ -1,0 +1,367 @@
+// denoise module kernels, wavelet path (strength > 0, src/pipe/modules/denoise):
+// half -> downcov -> down x3 -> assemble (all at the half size W/2 x H/2) ->
+// doub (full size). The doub output, the denoised normalised mosaic (f16), is
+// what the hilite and develop kernels read in place of denoise/noop.
+//
+// Every node stores f16 images like the reference. The computations whose
+// rounding decides a branch (clipped greens, the structure tensor and the
+// choice between its two forms, the hot pixel test, the wavelet threshold
+// switch, the sample positions of the bilinear taps) use explicit IEEE
+// operations in the shader's order, as the oracle evaluates them.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace {
+
+DEV float unorm16(uint16_t v) { return __fdiv_rn((float)v, 65535.0f); }
+
+// R16_UNORM mosaic read with MIRRORED_REPEAT over the full input
+DEV float raw_m(const dev_denoise_t &p, int x, int y)
+{
+  x = mirror(x, p.in_w); y = mirror(y, p.in_h);
+  return unorm16(__ldg(p.mosaic + (size_t)y * p.pitch + x));
+}
+
+// denoise/noise.glsl:1-11, edges applied per channel
+DEV void noise_sigma(float out[3], const dev_denoise_t &p, float black, float white, float val)
+{
+  const float x = fmaxf(0.0f, __fdiv_rn(__fsub_rn(val, black), __fsub_rn(white, black)));
+  const float s = __fsqrt_rn(__fadd_rn(p.na, __fmul_rn(x, p.nb)));
+#pragma unroll
+  for(int k = 0; k < 3; k++) out[k] = gclamp(__fmul_rn(p.edge_gain[k], s), 1e-3f, 1e3f);
+}
+
+// the same where the result only feeds continuous arithmetic
+DEV void noise_sigma_fast(float out[3], const dev_denoise_t &p, float black, float white, float val)
+{
+  const float s = sqrtf(p.na + fmaxf(0.0f, (val - black) / (white - black)) * p.nb);
+#pragma unroll
+  for(int k = 0; k < 3; k++) out[k] = gclamp(p.edge_gain[k] * s, 1e-3f, 1e3f);
+}
+
+// denoise/down.comp:102-104: decimated (swizzled) write position
+DEV void swz(int &x, int &y, int w, int h)
+{
+  const int ox = (x & 1) * (w + 1) / 2, oy = (y & 1) * (h + 1) / 2;
+  x = x / 2 + ox; y = y / 2 + oy;
+}
+
+// x^y for x >= 0 on the special function unit (feeds continuous weights only)
+DEV float fpow(float x, float y) { return __powf(x, y); }
+
+DEV void ld4(const half4 *img, int w, int x, int y, float v[4]) { ld_half4(img + (size_t)y * w + x, v[0], v[1], v[2], v[3]); }
+
+// position of a texture() read in texel space, rounded to the sampler's 8 sub-texel bits
+DEV float subtexel(float v) { return __fmul_rn(floorf(__fadd_rn(__fmul_rn(v, 256.0f), 0.5f)), 0.00390625f); }
+
+// texture() with LINEAR + MIRRORED_REPEAT at texel-space position (x, y)
+DEV void bilinear(const half4 *img, int w, int h, float x, float y, float out[4])
+{
+  const float xs = subtexel(__fsub_rn(x, 0.5f)), ys = subtexel(__fsub_rn(y, 0.5f));
+  const float fx = floorf(xs), fy = floorf(ys);
+  const int x0 = (int)fx, y0 = (int)fy;
+  const float ax = xs - fx, ay = ys - fy;
+  const int X0 = mirror(x0, w), X1 = mirror(x0 + 1, w), Y0 = mirror(y0, h), Y1 = mirror(y0 + 1, h);
+  float t00[4], t10[4], t01[4], t11[4];
+  ld4(img, w, X0, Y0, t00); ld4(img, w, X1, Y0, t10); ld4(img, w, X0, Y1, t01); ld4(img, w, X1, Y1, t11);
+#pragma unroll
+  for(int k = 0; k < 4; k++)
+    out[k] = (t00[k] * (1.0f - ax) + t10[k] * ax) * (1.0f - ay) + (t01[k] * (1.0f - ax) + t11[k] * ax) * ay;
+}
+
+// ---------------------------------------------------------------- half
+// denoise/half.comp:24-74 (bayer): R, mean of the greens (a clipped green is
+// replaced by the other one), B of the 2x2 block, on the raw unorm values
+__global__ void __launch_bounds__(256) k_dn_half(const dev_denoise_t p)
+{
+  const int x = blockIdx.x * 16 + threadIdx.x % 16, y = blockIdx.y * 16 + threadIdx.x / 16;
+  if(x >= p.hw || y >= p.hh) return;
+  const int i0 = p.cx + 2 * x, j0 = p.cy + 2 * y;
+  float cx = raw_m(p, i0, j0 + 1), cy = raw_m(p, i0 + 1, j0 + 1);
+  float cz = raw_m(p, i0 + 1, j0), cw = raw_m(p, i0, j0);
+  if(cx >= p.white[1]) cx = cz;
+  if(cz >= p.white[1]) cz = cx;
+  p.half_img[(size_t)y * p.hw + x] = mk_half4(cw, __fmul_rn(__fadd_rn(cx, cz), 0.5f), cy, 1.0f);
+}
+
+// ---------------------------------------------------------------- downcov
+// denoise/downcov.comp:41-63 with cov.glsl:159-276 response(): a 5x5 luminance
+// structure tensor in two forms (weighted by px^2 and by 1/px^2), the one with
+// the smaller determinant decomposed, then an anisotropic gaussian over the
+// 5x5 window that skips hot pixels. One 16x16 tile per CTA, the 20x20 input
+// window (mirrored) in shared memory.
+constexpr int DC_T = 16, DC_N = DC_T + 4;
+
+__global__ void __launch_bounds__(256) k_dn_downcov(const dev_denoise_t p)
+{
+  // per texel of the window: r, g, b, luminance and the luminance terms of the two tensor forms
+  __shared__ float sr[DC_N][DC_N + 1], sg[DC_N][DC_N + 1], sbl[DC_N][DC_N + 1];
+  __shared__ float sl[DC_N][DC_N + 1], sil[DC_N][DC_N + 1], sl2[DC_N][DC_N + 1], sil2[DC_N][DC_N + 1];
+  const int X0 = blockIdx.x * DC_T, Y0 = blockIdx.y * DC_T;
+  for(int i = threadIdx.x; i < DC_N * DC_N; i += 256)
+  {
+    const int tx = i % DC_N, ty = i / DC_N;
+    // slots an output reads are within 2 of the image (mirror exact); the
+    // clamp only keeps the unused slots of images narrower than a tile in bounds
+    const int x = min(max(mirror(X0 - 2 + tx, p.hw), 0), p.hw - 1);
+    const int y = min(max(mirror(Y0 - 2 + ty, p.hh), 0), p.hh - 1);
+    float v[4];
+    ld4(p.half_img, p.hw, x, y, v);
+    sr[ty][tx] = v[0]; sg[ty][tx] = v[1]; sbl[ty][tx] = v[2];
+    const float l = lum2020(v[0], v[1], v[2]);
+    sl[ty][tx] = l; sil[ty][tx] = 1.0f / l; sl2[ty][tx] = l * l; sil2[ty][tx] = 1.0f / (l * l);
+  }
+  __syncthreads();
+  const int lx = threadIdx.x % DC_T, ly = threadIdx.x / DC_T;
+  const int x = X0 + lx, y = Y0 + ly;
+  if(x >= p.hw || y >= p.hh) return;
+  // first moments of the luminance (Sw) and of its inverse (Sb)
+  float mw0 = 0.0f, mw1 = 0.0f, mb0 = 0.0f, mb1 = 0.0f, smw = 0.0f, smb = 0.0f;
+#pragma unroll
+  for(int j = -2; j <= 2; j++)
+#pragma unroll
+    for(int i = -2; i <= 2; i++)
+    {
+      const float px = sl[ly + 2 + j][lx + 2 + i], ipx = sil[ly + 2 + j][lx + 2 + i];
+      mw0 += (float)i * px; mw1 += (float)j * px; smw += px;
+      mb0 += (float)i * ipx; mb1 += (float)j * ipx; smb += ipx;
+    }
+  const float ismw = 1.0f / smw, ismb = 1.0f / smb;
+  mw0 *= ismw; mw1 *= ismw; mb0 *= ismb; mb1 *= ismb;
+  // second moments
+  float mean_b = 0.0f;
+  float Sw00 = 0.0f, Sw01 = 0.0f, Sw11 = 0.0f, Sb00 = 0.0f, Sb01 = 0.0f, Sb11 = 0.0f, sw = 0.0f, sb = 0.0f;
+#pragma unroll
+  for(int j = -2; j <= 2; j++)
+#pragma unroll
+    for(int i = -2; i <= 2; i++)
+    {
+      mean_b += sl[ly + 2 + j][lx + 2 + i];
+      const float p2 = sl2[ly + 2 + j][lx + 2 + i], b2 = sil2[ly + 2 + j][lx + 2 + i];
+      const float q0 = (float)i - mw0, q1 = (float)j - mw1;
+      Sw00 += p2 * q0 * q0; Sw01 += p2 * q0 * q1; Sw11 += p2 * q1 * q1; sw += p2;
+      const float r0 = (float)i - mb0, r1 = (float)j - mb1;
+      Sb00 += b2 * r0 * r0; Sb01 += b2 * r0 * r1; Sb11 += b2 * r1 * r1; sb += b2;
+    }
+  mean_b *= 1.0f / 25.0f;
+  const float isw = 1.0f / sw, isb = 1.0f / sb;
+  Sw00 *= isw; Sw01 *= isw; Sw11 *= isw;
+  Sb00 *= isb; Sb01 *= isb; Sb11 *= isb;
+  // cov.glsl: the form with the smaller determinant (the tensor is symmetric)
+  const float detw = Sw00 * Sw11 - Sw01 * Sw01, detb = Sb00 * Sb11 - Sb01 * Sb01;
+  float eval[2], e0[2], e1[2];
+  if(detw < detb) evd2x2(eval, e0, e1, Sw00, Sw01, Sw11);
+  else            evd2x2(eval, e0, e1, Sb00, Sb01, Sb11);
+  eval[1] *= 0.05f;
+  eval[0] = gclamp(eval[0], 0.01f, 25.0f); eval[1] = gclamp(eval[1], 0.01f, 25.0f);
+  const float ie0 = 1.0f / eval[0], ie1 = 1.0f / eval[1];
+  // anisotropic gaussian over the window, hot pixels (r > 2 mean) left out
+  const float hot = 2.0f * mean_b;
+  float r0 = 0.0f, r1 = 0.0f, r2 = 0.0f, wt = 0.0f;
+  for(int j = -2; j <= 2; j++)
+#pragma unroll
+    for(int i = -2; i <= 2; i++)
+    {
+      const float pr = sr[ly + 2 + j][lx + 2 + i];
+      if(pr > hot) continue;
+      const float x0 = (float)i * e0[0] + (float)j * e0[1];
+      const float x1 = (float)i * e1[0] + (float)j * e1[1];
+      const float ww = fmaxf(1e-9f, __expf(-0.5f * (x0 * ie0 * x0 + x1 * ie1 * x1)));
+      r0 += ww * pr; r1 += ww * sg[ly + 2 + j][lx + 2 + i]; r2 += ww * sbl[ly + 2 + j][lx + 2 + i];
+      wt += ww;
+    }
+  const float d = 1.0f / fmaxf(wt, 1e-8f);
+  float edge = gclamp(75.0f * fmaxf(0.0f, eval[1] - 0.09f), 0.0f, 1.0f);
+  edge = smoothstep(0.4f, 0.75f, edge);
+  edge = gclamp(0.02f + edge, 0.0f, 1.0f);
+  int X = x, Y = y;
+  swz(X, Y, p.hw, p.hh);
+  p.lvl[0][(size_t)Y * p.hw + X] = mk_half4(r0 * d, r1 * d, r2 * d, edge);
+}
+
+// ---------------------------------------------------------------- down
+// denoise/down.comp:59-108 (levels 1..3): four bilinear taps in a flower
+// around the texel, weighted by how close their x^0.8 values are relative to
+// the noise (0.7^level sigma / block); the centre keeps weight 0.2
+__global__ void __launch_bounds__(256) k_dn_down(const dev_denoise_t p, const half4 *__restrict__ in,
+    half4 *__restrict__ out, float pl)
+{
+  const int x = blockIdx.x * 16 + threadIdx.x % 16, y = blockIdx.y * 16 + threadIdx.x / 16;
+  if(x >= p.hw || y >= p.hh) return;
+  const float t = 0.2f;
+  float c[4];
+  ld4(in, p.hw, x, y, c);
+  float ns[3];
+  noise_sigma_fast(ns, p, p.black[1], p.white[1], c[0]);
+  float wc[3], g1[3], sum[3], wgt[3];
+#pragma unroll
+  for(int k = 0; k < 3; k++)
+  {
+    wc[k] = 1.0f / (pl * ns[k] / p.block_f);
+    g1[k] = c[k] < 0.0f ? c[k] : fpow(c[k], 0.8f);
+    sum[k] = t * c[k]; wgt[k] = t;
+  }
+  // offsets of the taps (0.5 + o): (1.7, 0.9), (-0.7, 0.1), (0.9, -0.7), (0.1, 1.7)
+  const float ox[4] = { 0.5f + 1.2f, 0.5f - 1.2f, 0.5f + 0.4f, 0.5f - 0.4f };
+  const float oy[4] = { 0.5f + 0.4f, 0.5f - 0.4f, 0.5f - 1.2f, 0.5f + 1.2f };
+#pragma unroll
+  for(int o = 0; o < 4; o++)
+  {
+    float col[4];
+    bilinear(in, p.hw, p.hh, __fadd_rn((float)x, ox[o]), __fadd_rn((float)y, oy[o]), col);
+#pragma unroll
+    for(int k = 0; k < 3; k++)
+    {
+      const float g0 = col[k] < 0.0f ? col[k] : fpow(col[k], 0.8f);
+      const float e = gclamp(1.0f - 0.5f * (wc[k] * fabsf(g0 - g1[k])), 0.0f, 1.0f);
+      const float w = e * (1.0f - t) / 4.0f;
+      sum[k] += w * col[k];
+      wgt[k] += w;
+    }
+  }
+  int X = x, Y = y;
+  swz(X, Y, p.hw, p.hh);
+  out[(size_t)Y * p.hw + X] = mk_half4(sum[0] / wgt[0], sum[1] / wgt[1], sum[2] / wgt[2], 1.0f);
+}
+
+// ---------------------------------------------------------------- assemble
+// denoise/assemble.comp:151-273: gather the 4 scales through the swizzle,
+// detail coefficients normalised by the noise, a slope based detail mask,
+// soft shrinkage at strength^4 (off where the coarse coefficient is large),
+// recomposition and a luma blend in YUV
+DEV void fetch_z(const half4 *img, int w, int h, int x, int y, float v[3])
+{
+  if(x < 0 || y < 0 || x >= w || y >= h) { v[0] = v[1] = v[2] = 0.0f; return; }
+  float a;
+  ld_half4(img + (size_t)y * w + x, v[0], v[1], v[2], a);
+}
+
+DEV void m3v(const float *A, const float v[3], float o[3])
+{
+#pragma unroll
+  for(int i = 0; i < 3; i++) o[i] = A[3 * i + 0] * v[0] + A[3 * i + 1] * v[1] + A[3 * i + 2] * v[2];
+}
+
+__global__ void __launch_bounds__(256) k_dn_assemble(const dev_denoise_t p)
+{
+  const int x = blockIdx.x * 16 + threadIdx.x % 16, y = blockIdx.y * 16 + threadIdx.x / 16;
+  if(x >= p.hw || y >= p.hh) return;
+  const int szx = p.hw + 1, szy = p.hh + 1;
+  float d[5][3], orig[3];
+  fetch_z(p.half_img, p.hw, p.hh, x, y, orig);
+#pragma unroll
+  for(int k = 0; k < 3; k++) d[0][k] = orig[k];
+  int ex = x, ey = y;
+#pragma unroll
+  for(int l = 1; l <= 4; l++)
+  {
+    ex = ex / 2 + (ex & 1) * szx / 2;
+    ey = ey / 2 + (ey & 1) * szy / 2;
+    fetch_z(p.lvl[l - 1], p.hw, p.hh, ex, ey, d[l]);
+  }
+  float sigma[3];
+  noise_sigma(sigma, p, p.black[1], p.white[1], fmaxf(d[2][0], 0.0f));
+  const float *b = p.bscale;
+  // channel 0 decides the threshold switch below: IEEE; the others feed continuous math only
+#pragma unroll
+  for(int l = 0; l < 4; l++)
+  {
+    d[l][0] = __fdiv_rn(__fsub_rn(d[l][0], d[l + 1][0]), __fmul_rn(sigma[0], b[l]));
+#pragma unroll
+    for(int k = 1; k < 3; k++) d[l][k] = (d[l][k] - d[l + 1][k]) / (sigma[k] * b[l]);
+  }
+  float len[4];
+#pragma unroll
+  for(int l = 0; l < 4; l++) len[l] = sqrtf(d[l][0] * d[l][0] + d[l][1] * d[l][1] + d[l][2] * d[l][2]);
+  const float slope = ((len[3] - len[0]) / 3.0f + (len[2] - len[1]) + (len[1] - len[0]) + (len[3] - len[2])
+                     + (len[2] - len[0]) / 2.0f + (len[3] - len[1]) / 2.0f) / 6.0f;
+  float test = fmaxf(0.0f, -slope);
+  test = fmaxf(0.0f, 1.0f - test);
+  test = test * test; test = test * test; test = test * test; test = test * test;   // pow(test, 16)
+  test = gclamp(1.5f * test, 0.0f, 1.0f);
+  const float thrs0 = p.thrs0;
+#pragma unroll
+  for(int l = 3; l >= 0; l--)
+  {
+    const float thrs = (fabsf(d[l][0]) > 10.0f) ? 10000.0f : thrs0;
+#pragma unroll
+    for(int k = 0; k < 3; k++)
+    {
+      const float a = fabsf(d[l][k]);
+      const float tt = fminf(1.0f, a / (2.0f * thrs));
+      d[4][k] += sigma[k] * b[l] * gsign(d[l][k]) * gmix(fmaxf(a - thrs, 0.0f), a, tt);
+    }
+  }
+  float v4[3], vo[3];
+#pragma unroll
+  for(int k = 0; k < 3; k++)
+  {
+    const float iwb = p.wb[k] / (p.white[k] - p.black[k]);
+    v4[k] = (d[4][k] - p.black[k]) * iwb;
+    vo[k] = (orig[k] - p.black[k]) * iwb;
+  }
+  float yuv[3], yuvo[3], rgb[3];
+  m3v(p.rgb_to_yuv, v4, yuv);
+  m3v(p.rgb_to_yuv, vo, yuvo);
+  yuv[0] = gmix(yuvo[0], yuv[0], p.luma);
+  m3v(p.yuv_to_rgb, yuv, rgb);
+  float o[3];
+#pragma unroll
+  for(int k = 0; k < 3; k++) o[k] = rgb[k] / p.wb[k] * (p.white[k] - p.black[k]) + p.black[k];
+  p.asm_img[(size_t)y * p.hw + x] = mk_half4(o[0], o[1], o[2], test);
+}
+
+// ---------------------------------------------------------------- doub
+// denoise/doub.comp:35-116 (bayer, no gain map): per CFA sample, shrink the
+// full resolution residual against the bilinear up-sampled noisy coarse
+// level, protected by the detail mask, and normalise to [0, 1]
+__global__ void __launch_bounds__(256) k_dn_doub(const dev_denoise_t p)
+{
+  const int x = blockIdx.x * 32 + threadIdx.x % 32, y = blockIdx.y * 8 + threadIdx.x / 32;
+  if(x >= p.W || y >= p.H) return;
+  const float ux = __fdiv_rn(__fadd_rn((float)x, 0.5f), (float)p.W);
+  const float uy = __fdiv_rn(__fadd_rn((float)y, 0.5f), (float)p.H);
+  const float tx = __fmul_rn(ux, (float)p.hw), ty = __fmul_rn(uy, (float)p.hh);
+  float upsm[4], down[4];
+  bilinear(p.asm_img, p.hw, p.hh, tx, ty, upsm);
+  bilinear(p.half_img, p.hw, p.hh, tx, ty, down);
+  const int col = cfa_bayer(x, y);
+  const float black = p.black[col], white = p.white[col];
+  const float crs = col == 0 ? upsm[0] : (col == 1 ? upsm[1] : upsm[2]);
+  const float crs1 = col == 0 ? down[0] : (col == 1 ? down[1] : down[2]);
+  const float Tt = 0.5f * p.strength * upsm[3];
+  const float blendw = 0.5f * ((col == 1 ? p.luma : 1.0f) + 1.0f);
+  float sigma[3];
+  noise_sigma_fast(sigma, p, black, white, crs);
+  float val = raw_m(p, x + p.cx, y + p.cy);
+  if(val < white)
+  {
+    const float wav = (val - crs1) / fmaxf(sigma[0] + sigma[2], 1e-8f);
+    const float tt = fminf(1.0f, wav / fmaxf(2.0f * Tt, 1e-8f));
+    float uw = fminf(1.0f, upsm[3]);
+    uw = uw * uw; uw = uw * uw;                      // pow(min(1, w), 4)
+    uw = 1.0f - (1.0f - uw) * p.detail;
+    const float aw = fabsf(wav);
+    val = gmix(val, fmaxf(0.0f, crs + sigma[1] * gsign(wav) * gmix(fmaxf(0.0f, aw - Tt), aw, tt)), uw * blendw);
+  }
+  val = fmaxf(0.0f, (val - black) / (white - black));
+  p.dn[(size_t)y * p.W + x] = f2h(val);
+}
+
+} // namespace
+
+cudaError_t launch_denoise(const dev_denoise_t &p, int stage, cudaStream_t s)
+{
+  const dim3 gh((p.hw + 15) / 16, (p.hh + 15) / 16);
+  switch(stage)
+  {
+    case 0: k_dn_half<<<gh, 256, 0, s>>>(p); break;
+    case 1: k_dn_downcov<<<dim3((p.hw + DC_T - 1) / DC_T, (p.hh + DC_T - 1) / DC_T), 256, 0, s>>>(p); break;
+    case 2: case 3: case 4:
+      k_dn_down<<<gh, 256, 0, s>>>(p, p.lvl[stage - 2], p.lvl[stage - 1], p.pl[stage - 1]); break;
+    case 5: k_dn_assemble<<<gh, 256, 0, s>>>(p); break;
+    case 6: k_dn_doub<<<dim3((p.W + 31) / 32, (p.H + 7) / 8), 256, 0, s>>>(p); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}

@@ -72,6 +72,30 @@ struct dev_llap_k3_t
   half4 *out;           // rgba f16 W*H
 };
 
+// denoise wavelet path (strength > 0): the push constants and uniforms of
+// denoise/main.c:133-333 and the half size node buffers
+struct dev_denoise_t
+{
+  const uint16_t *mosaic;
+  int pitch, in_w, in_h; // input mosaic layout (mirrored reads cover the full input)
+  int cx, cy, W, H;      // crop offset and module output size
+  int hw, hh;            // half size (W/2, H/2)
+  float black[3], white[3], wb[3];  // unorm black/white per channel, camera white balance
+  float na, nb;          // noise profile (normalised)
+  float edge_gain[3];    // exp2(12 edges.rgb + edges.a) of noise_sigma
+  float strength, luma, detail, thrs0;  // params; thrs0 = strength^4
+  float block_f;         // 1.414213 (bayer)
+  float bscale[4];       // 0.7^(l+1) / block_f, l = 0..3 (assemble.comp)
+  float pl[4];           // 0.7^level
+  float rgb_to_yuv[9], yuv_to_rgb[9];
+  half4 *half_img;       // denoise/half output
+  half4 *lvl[4];         // downcov, down 1..3 outputs (swizzled)
+  half4 *asm_img;        // assemble output
+  __half *dn;            // doub output: the denoised normalised mosaic, W*H
+};
+// stage 0 half, 1 downcov, 2..4 down levels 1..3, 5 assemble, 6 doub (k_denoise.cu)
+cudaError_t launch_denoise(const dev_denoise_t &p, int stage, cudaStream_t s);
+
 // hilite (k_hilite.cu)
 cudaError_t launch_hilite_k1(const dev_hilite_k1_t &p, cudaStream_t s);
 cudaError_t launch_hilite_reduce(const half4 *in, int iw, int ih, half4 *out, int ow, int oh,

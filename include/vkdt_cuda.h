@@ -196,7 +196,9 @@ int  vkdt_cuda_graph_hist(vkdt_cuda_graph_t *graph, uint32_t *hist257);
 int  vkdt_cuda_hist_rgba_f16(const void *d_rgba, int wd, int ht, uint32_t *d_hist257, void *stream);
 
 /* debug: copy an intermediate image of the last run to host floats.
- * stage 0 denoise output (1 ch), 1 hilite output (1 ch), 2 filmcurv output (4 ch).
+ * stage 0 denoise output (1 ch), 1 hilite output (1 ch), both at the crop size;
+ * 2 filmcurv output (4 ch) and 3 demosaic output (4 ch, x-trans and reduced
+ * sizes only), both at the output size.
  * requires vkdt_cuda_graph_set_debug(graph, 1) before alloc. */
 int  vkdt_cuda_graph_set_debug(vkdt_cuda_graph_t *graph, int enable);
 int  vkdt_cuda_graph_debug_stage(vkdt_cuda_graph_t *graph, int stage, float *out, size_t count);

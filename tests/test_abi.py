@@ -124,6 +124,45 @@ def test_create_nodes_wavelet_denoise():
         assert v.supports(name, kernel), (name, kernel)
 
 
+def test_create_nodes_xtrans():
+    # x-trans: 3x3 blocks (hilite and demosaic/gauss at a third of the size), per node launches
+    g = v.Graph()
+    g.set_input(6240, 4160, v.default_img_param(wd=6240, ht=4160, filters=9))
+    g.create_nodes()
+    n = g.nodes()
+    g.close()
+    by = {(a, b): x for x in n for a, b in [x[:2]]}
+    assert by[("hilite", "half")][2:4] == (2080, 1386) and by[("demosaic", "gauss")][2:4] == (2080, 1386)
+    assert by[("demosaic", "fix")][2:4] == (6240, 4160)
+    fused = [x[5] for x in n]
+    assert min(fused) >= 0 and len(set(fused)) >= 20
+
+
+def test_create_nodes_thumbnail():
+    # demosaic/main.c: 1/8 size -> halfsize + resample; denoise and hilite stay full size
+    g = v.Graph()
+    g.set_input(6000, 4000, v.default_img_param(wd=6000, ht=4000))
+    g.set_output_size(750, 500)
+    g.create_nodes()
+    n = g.nodes()
+    g.close()
+    kinds = [x[:2] for x in n]
+    assert ("demosaic", "halfsize") in kinds and ("shared", "resample") in kinds and ("demosaic", "splat") not in kinds
+    assert [x for x in n if x[:2] == ("demosaic", "halfsize")][0][2:4] == (3000, 2000)
+    assert [x for x in n if x[:2] == ("llap", "colour")][0][2:4] == (750, 500)
+    assert [x for x in n if x[:2] == ("hilite", "half")][0][2:4] == (3000, 2000)
+    for name, kernel, *_ in n:
+        assert v.supports(name, kernel), (name, kernel)
+    # a scale below 1.5 blocks would need a resample after the full size demosaic
+    g = v.Graph()
+    g.set_input(6000, 4000, v.default_img_param(wd=6000, ht=4000))
+    g.set_output_size(4000, 2666)
+    with pytest.raises(_lib.VkdtError) as e:
+        g.create_nodes()
+    assert e.value.code == _lib.INCOMPLETE
+    g.close()
+
+
 def test_create_nodes_rejects_bad_input():
     g = v.Graph()
     ip = v.default_img_param(wd=101, ht=100)

@@ -120,6 +120,58 @@ def test_wavelet_denoise(gpu, wd, ht):
     check_rgb(out, r["llap"], de_stage=True)
 
 
+def _run_graph(m, ip, setup=None, debug=True):
+    with v.Graph() as g:
+        g.set_input(m.shape[1], m.shape[0], ip)
+        if setup:
+            setup(g)
+        g.set_debug(debug)
+        g.alloc()
+        out = g.run(m).astype(np.float32)
+        st = {"llap": out, "denoise": g.debug_stage(0), "hilite": g.debug_stage(1), "filmcurv": g.debug_stage(2)}
+        try:
+            st["demosaic"] = g.debug_stage(3)
+        except v._lib.VkdtError:
+            pass
+    return st
+
+
+@pytest.mark.parametrize("wd,ht,strength", [(606, 402, 0.0), (1206, 798, 0.0), (606, 402, 1.0), (611, 397, 0.0)])
+def test_xtrans(gpu, wd, ht, strength):
+    # x-trans 6x6 CFA through the per-node chain: hilite on 3x3 blocks, demosaic gauss/splat/fix
+    m = v.scene_host(v.make_scene(wd, ht, seed=wd + 7, filters=9))
+    ip = v.default_img_param(wd=wd, ht=ht, filters=9, noise_a=NA, noise_b=NB)
+    op = oracle.default_params()
+    op.dn_strength = strength
+    g = _run_graph(m, ip, setup=(lambda g: g.set_param("denoise", "strength", strength)) if strength else None)
+    r = oracle.develop(m, oracle.img_param(ip), params=op, stages=("denoise", "hilite", "demosaic", "filmcurv", "llap"))
+    if strength == 0.0:
+        assert np.array_equal(g["denoise"], r["denoise"])
+    s_h = summary(g["hilite"][..., None], r["hilite"][..., None])
+    assert s_h["flipped_frac"] <= 1e-3 and s_h["mean"] <= 1e-4, s_h
+    check_rgb(g["demosaic"], r["demosaic"])
+    check_rgb(g["filmcurv"], r["filmcurv"], de_stage=True)
+    check_rgb(g["llap"], r["llap"], de_stage=True)
+
+
+@pytest.mark.parametrize("wd,ht,ow,oh,filters", [(1000, 742, 250, 185, 0x94949494), (2048, 1536, 256, 192, 0x94949494),
+                                                 (1000, 742, 333, 247, 0x94949494), (606, 402, 101, 67, 9),
+                                                 (1206, 798, 150, 99, 9)])
+def test_thumbnail(gpu, wd, ht, ow, oh, filters):
+    # reduced output size: denoise and hilite at full size, demosaic/halfsize (+ shared/resample
+    # with the catmull-rom taps unless the scale is the block), the rest at the output size
+    m = v.scene_host(v.make_scene(wd, ht, seed=ow, filters=filters))
+    ip = v.default_img_param(wd=wd, ht=ht, filters=filters, noise_a=NA, noise_b=NB)
+    op = oracle.default_params()
+    op.out_wd, op.out_ht = ow, oh
+    g = _run_graph(m, ip, setup=lambda g: g.set_output_size(ow, oh))
+    r = oracle.develop(m, oracle.img_param(ip), params=op, stages=("demosaic", "filmcurv", "llap"))
+    assert g["llap"].shape == r["llap"].shape, (g["llap"].shape, r["llap"].shape)
+    check_rgb(g["demosaic"], r["demosaic"], flip=2e-2)
+    check_rgb(g["filmcurv"], r["filmcurv"], flip=2e-2, de_stage=True)
+    check_rgb(g["llap"], r["llap"], flip=2e-2, de_stage=True)
+
+
 def test_fp64_reference_error(gpu):
     # the error of the CUDA path against the FP64 build of the same restatement
     wd, ht = 512, 384
@@ -201,6 +253,10 @@ def develop_case(case, m):
     out = g.run(m).astype(np.float32)
     res = {"llap": out[..., :3], "denoise": g.debug_stage(0), "hilite": g.debug_stage(1),
            "filmcurv": g.debug_stage(2)[..., :3]}
+    try:
+        res["demosaic"] = g.debug_stage(3)[..., :3]
+    except v._lib.VkdtError:
+        pass
     g.close()
     return res
 
@@ -214,8 +270,8 @@ def test_cuda_matches_reference_golden(gpu, name):
         if e.code in (v._lib.ERROR_FORMAT_NOT_SUPPORTED, v._lib.INCOMPLETE):
             pytest.skip("not on the CUDA path yet: %s" % e)
         raise
-    for s in ("hilite", "filmcurv", "llap"):
-        if s not in want:
+    for s in ("hilite", "demosaic", "filmcurv", "llap"):
+        if s not in want or s not in got:
             continue
         a, b = got[s], want[s]
         if a.ndim == 2:

@@ -244,8 +244,12 @@ class Graph:
         return np.array(h[:], dtype=np.uint32)
 
     def debug_stage(self, stage):
-        ch = 4 if stage == 2 else 1
-        out = np.empty((self.ht, self.wd, ch), dtype=np.float32) if stage != 2 else np.empty((self.ht, self.wd, 4), np.float32)
+        """0 denoise, 1 hilite (crop size, one channel); 2 filmcurv, 3 demosaic
+        (output size, rgba; 3 only on the per-node chain)."""
+        if stage in (2, 3):
+            out = np.empty((self.out_ht, self.out_wd, 4), np.float32)
+        else:
+            out = np.empty((self.ht, self.wd, 1), np.float32)
         check(self._l.vkdt_cuda_graph_debug_stage(self._g, stage, out.ctypes.data_as(C.POINTER(C.c_float)), out.size),
               "debug_stage")
-        return out if ch == 4 else out[..., 0]
+        return out if stage in (2, 3) else out[..., 0]

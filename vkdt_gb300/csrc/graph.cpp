@@ -156,6 +156,10 @@ struct vkdt_cuda_graph_t
   int nl = 0;
   size_t off_src = 0, off_rgbf = 0, off_out = 0, off_hist = 0, off_dbg0 = 0, off_dbg1 = 0, off_lut = 0, arena_bytes = 0;
   bool wavelet = false;          // denoise strength > 0: the wavelet nodes run before hilite
+  int block = 2;                 // CFA block: 2 bayer, 3 x-trans
+  bool halfsize = false, resample = false;  // demosaic/halfsize (+ shared/resample) for reduced sizes
+  bool unfused = false;          // x-trans or reduced size: the per-node chain instead of the fused kernel
+  size_t off_h0 = 0, off_b0 = 0, off_hl = 0, off_cov = 0, off_g = 0, off_hs = 0, off_dm = 0;
   size_t off_dnh = 0, off_dnl[4] = { 0, 0, 0, 0 }, off_dna = 0, off_dn = 0, off_idlut = 0;
   unsigned char *arena = nullptr;
   void *h_src = nullptr, *h_sink = nullptr;
@@ -332,6 +336,7 @@ void fill_denoise(vkdt_cuda_graph_t *g, dev_denoise_t &p, const void *d_src)
   p.pitch = g->in_wd; p.in_w = g->in_wd; p.in_h = g->in_ht;
   p.cx = (int)g->ip.crop_aabb[0]; p.cy = (int)g->ip.crop_aabb[1];
   p.W = g->W; p.H = g->H; p.hw = g->hw; p.hh = g->hh;
+  p.filters = g->ip.filters;
   for(int k = 0; k < 3; k++)
   {
     p.black[k] = g->ip.black[k] / 65535.0f;
@@ -343,7 +348,7 @@ void fill_denoise(vkdt_cuda_graph_t *g, dev_denoise_t &p, const void *d_src)
   for(int k = 0; k < 3; k++) p.edge_gain[k] = std::exp2(12.0f * dn->f("edges", k) + dn->f("edges", 3));
   p.strength = dn->f("strength"); p.luma = dn->f("luma"); p.detail = dn->f("detail");
   p.thrs0 = std::pow(p.strength, 4.0f);
-  p.block_f = 1.414213f;
+  p.block_f = g->ip.filters == 9u ? 2.23607f : 1.414213f;   // denoise/main.c:235-238 (block 3 / 2)
   const float bl[4] = { 0.7000f, 0.4900f, 0.3430f, 0.2401f };
   for(int l = 0; l < 4; l++) p.bscale[l] = bl[l] / p.block_f;
   for(int l = 0; l < 4; l++) p.pl[l] = std::pow(0.7f, (float)l);
@@ -355,6 +360,29 @@ void fill_denoise(vkdt_cuda_graph_t *g, dev_denoise_t &p, const void *d_src)
   p.dn = g->at<__half>(g->off_dn);
 }
 
+// buffers and sizes of the per-node chain (x-trans, reduced output sizes)
+void fill_nodes(vkdt_cuda_graph_t *g, dev_nodes_t &p, const void *d_src)
+{
+  memset(&p, 0, sizeof(p));
+  p.mosaic = (const uint16_t *)d_src;
+  p.noop_lut = g->at<__half>(g->off_lut);
+  p.pitch = g->in_wd; p.cx = (int)g->ip.crop_aabb[0]; p.cy = (int)g->ip.crop_aabb[1];
+  p.W = g->W; p.H = g->H;
+  p.filters = g->ip.filters;
+  p.block = g->block; p.hw = g->hw; p.hh = g->hh;
+  p.hl_white = g->mod("hilite")->f("white");
+  p.fixup = g->mod("demosaic")->n("colour");
+  p.ow = g->out_w; p.oh = g->out_h;
+  p.dn = g->at<__half>(g->off_dn);
+  p.h0 = g->at<half4>(g->off_h0);
+  p.b0 = g->at<half4>(g->off_b0);
+  p.hl = g->at<__half>(g->off_hl);
+  p.cov = g->at<half4>(g->off_cov);
+  p.g = g->at<__half>(g->off_g);
+  p.hs = g->at<half4>(g->off_hs);
+  p.dm = g->at<half4>(g->off_dm);
+}
+
 // the kernel sequence of one run. ev != null records timing events around each launch.
 int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out, bool timed)
 {
@@ -363,8 +391,9 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
   if(r) return r;
   dev_denoise_t dd;
   if(g->wavelet)
-  { // the develop kernels read the denoised f16 mosaic through the identity code table
     fill_denoise(g, dd, d_src);
+  if(g->wavelet && !g->unfused)
+  { // the develop kernels read the denoised f16 mosaic through the identity code table
     d.mosaic = reinterpret_cast<const uint16_t *>(dd.dn);
     d.noop_lut = g->at<__half>(g->off_idlut);
     d.pitch = g->W; d.cx = 0; d.cy = 0;
@@ -387,6 +416,27 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
       CU(launch_denoise(dd, stage, s));
       if((r = mark())) return r;
     }
+  dev_nodes_t np;
+  if(g->unfused)
+  { // 1'. denoise/noop (unless the wavelet ran), hilite half, all hilite reduce levels
+    fill_nodes(g, np, d_src);
+    if(!g->wavelet)
+    {
+      CU(launch_nodes(np, 0, s));
+      if((r = mark())) return r;
+    }
+    CU(launch_nodes(np, 1, s));
+    if((r = mark())) return r;
+    for(size_t l = 0; l < g->hr.size(); l++)
+    {
+      const half4 *in = l == 0 ? np.h0 : g->at<half4>(g->hr[l - 1].off);
+      const int iw = l == 0 ? g->hw : g->hr[l - 1].w, ih = l == 0 ? g->hh : g->hr[l - 1].h;
+      CU(launch_hilite_reduce(in, iw, ih, g->at<half4>(g->hr[l].off), g->hr[l].w, g->hr[l].h, white, desat, wb, s));
+      if((r = mark())) return r;
+    }
+  }
+  else
+  {
   // 1. noop + hilite half + first hilite reduce
   dev_hilite_k1_t k1;
   memset(&k1, 0, sizeof(k1));
@@ -404,6 +454,7 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
         g->at<half4>(g->hr[l].off), g->hr[l].w, g->hr[l].h, white, desat, wb, s));
     if((r = mark())) return r;
   }
+  }
   // 3. hilite assemble B[L-1] .. B[1]
   for(int l = (int)g->hb.size() - 1; l >= 0; l--)
   {
@@ -413,9 +464,31 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
         g->at<half4>(g->hb[l].off), white, soft, s));
     if((r = mark())) return r;
   }
-  // 4. fused develop pass
-  CU(launch_develop(d, s));
-  if((r = mark())) return r;
+  if(g->unfused)
+  { // 4'. hilite level 0 assemble, doub, demosaic, colour .. first llap reduce
+    const level_t &c = g->hb.empty() ? g->hr[0] : g->hb[0];
+    CU(launch_hilite_assemble(np.h0, g->hw, g->hh, g->at<half4>(c.off), c.w, c.h, g->at<half4>(g->off_b0), white, soft, s));
+    if((r = mark())) return r;
+    CU(launch_nodes(np, 2, s));
+    if((r = mark())) return r;
+    const int stages_half[2] = { 6, 7 }, stages_full[3] = { 3, 4, 5 };
+    const int *st = g->halfsize ? stages_half : stages_full;
+    const int nst = g->halfsize ? (g->resample ? 2 : 1) : 3;
+    for(int i = 0; i < nst; i++)
+    {
+      CU(launch_nodes(np, st[i], s));
+      if((r = mark())) return r;
+    }
+    dev_image_t dp = d;
+    dp.W = g->out_w; dp.H = g->out_h;
+    CU(launch_post(dp, np.dm, s));
+    if((r = mark())) return r;
+  }
+  else
+  { // 4. fused develop pass
+    CU(launch_develop(d, s));
+    if((r = mark())) return r;
+  }
   // 5. llap reduce levels 2..nl-1
   for(size_t l = 1; l < g->lp.size(); l++)
   {
@@ -435,7 +508,7 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
   }
   // 7. level 0 assemble + llap colour
   dev_llap_k3_t k3;
-  k3.rgbf = d.rgbf; k3.W = g->W; k3.H = g->H;
+  k3.rgbf = d.rgbf; k3.W = g->out_w; k3.H = g->out_h;
   k3.l1 = d.l1; k3.l1w = d.l1w; k3.l1h = d.l1h; k3.l1plane = d.l1plane;
   k3.coarse = g->la.empty() ? d.l1 + 10 * d.l1plane : g->at<__half>(g->la[0].off);
   k3.ll_sigma = d.ll_sigma; k3.ll_shadows = d.ll_shadows; k3.ll_highlights = d.ll_highlights; k3.ll_clarity = d.ll_clarity;
@@ -477,7 +550,8 @@ int vkdt_cuda_supports(dt_token_t name, dt_token_t kernel)
 {
   static const char *sup[][2] = {
     { "denoise", "noop" }, { "denoise", "half" }, { "denoise", "downcov" }, { "denoise", "down" },
-    { "denoise", "assemble" }, { "denoise", "doub" }, { "hilite", "half" }, { "hilite", "reduce" }, { "hilite", "assemble" }, { "hilite", "doub" },
+    { "denoise", "assemble" }, { "denoise", "doub" }, { "demosaic", "halfsize" }, { "shared", "resample" },
+    { "hilite", "half" }, { "hilite", "reduce" }, { "hilite", "assemble" }, { "hilite", "doub" },
     { "demosaic", "down" }, { "demosaic", "gauss" }, { "demosaic", "splat" }, { "demosaic", "fix" },
     { "colour", "main" }, { "filmcurv", "main" }, { "OpenDRT", "hist" },
     { "llap", "curve" }, { "llap", "reduce" }, { "llap", "assemble" }, { "llap", "colour" } };
@@ -686,23 +760,35 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
   if(r) return r;
   const uint32_t filters = g->ip.filters;
   if(filters == 0) return fail(VKDT_CUDA_INCOMPLETE, "rgb input: the path starts on a mosaic");
-  if(filters == 9) return fail(VKDT_CUDA_INCOMPLETE, "x-trans mosaics are not built in this version");
   g->nodes.clear();
   // denoise modify_roi_out: output = crop window
   const uint32_t *b = g->ip.crop_aabb;
   if(b[2] <= b[0] || b[3] <= b[1] || (int)b[2] > g->in_wd || (int)b[3] > g->in_ht)
     return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "crop window outside the mosaic");
   g->W = (int)(b[2] - b[0]); g->H = (int)(b[3] - b[1]);
-  if((g->W & 1) || (g->H & 1) || (b[0] & 1) || (b[1] & 1) || (g->in_wd & 1))
+  const bool xt = filters == 9u;
+  g->block = xt ? 3 : 2;
+  if(!xt && ((g->W & 1) || (g->H & 1) || (b[0] & 1) || (b[1] & 1) || (g->in_wd & 1)))
     return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "bayer mosaic width and crop window must be even");
   if(g->W < 16 || g->H < 16) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "image smaller than 16x16");
-  g->hw = g->W / 2; g->hh = g->H / 2;
-  if(g->req_wd > 0 && (g->req_wd != g->W || g->req_ht != g->H))
-    return fail(VKDT_CUDA_INCOMPLETE, "reduced output size (half-size demosaic + resample) is not built in this version");
-  g->out_w = g->W; g->out_h = g->H;
+  g->hw = g->W / g->block; g->hh = g->H / g->block;
+  // demosaic/main.c:18-41, 92-111: a requested size of 1/(1.5 block) or less
+  // takes the half size demosaic, resampled unless the scale is the block
+  {
+    const int ow = g->req_wd > 0 ? g->req_wd : g->W, oh = g->req_ht > 0 ? g->req_ht : g->H;
+    const float scale = (float)g->W / (float)ow;
+    g->halfsize = (ow != g->W || oh != g->H) && scale >= 1.5f * g->block;
+    if(!g->halfsize && (ow != g->W || oh != g->H))
+      return fail(VKDT_CUDA_INCOMPLETE, "resampling after the full size demosaic is not built in this version");
+    g->resample = g->halfsize && (float)g->block != scale;
+    if(!g->halfsize) { g->out_w = g->W; g->out_h = g->H; }
+    else if(g->resample) { g->out_w = ow; g->out_h = oh; }
+    else { g->out_w = g->hw; g->out_h = g->hh; }
+  }
+  // bayer at full size runs fused; x-trans and reduced sizes run node by node
+  g->unfused = xt || g->halfsize;
 
   // node lists as the modules' create_nodes emit them
-  int fused = 0;
   g->wavelet = g->mod("denoise")->f("strength") > 0.0f;
   if(!g->wavelet) add_node(g, "denoise", "noop", g->W, g->H, 1, -1);
   else
@@ -729,19 +815,27 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
     }
     for(size_t l = 0; l + 1 < g->hr.size(); l++) g->hb.push_back(g->hr[l]);
   }
-  // demosaic/main.c:159-202 (gaussian splats, full size)
-  add_node(g, "demosaic", "down", g->hw, g->hh, 1, -1);
-  add_node(g, "demosaic", "gauss", g->hw, g->hh, 1, -1);
-  add_node(g, "demosaic", "splat", g->W, g->H, 1, -1);
-  add_node(g, "demosaic", "fix", g->W, g->H, 1, -1);
-  add_node(g, "colour", "main", g->W, g->H, 1, -1);
-  add_node(g, "OpenDRT", "hist", (g->W + 15) / 16 * 8, (g->H + 15) / 16 * 8, 1, -1);
-  add_node(g, "filmcurv", "main", g->W, g->H, 1, -1);
+  const int OW = g->out_w, OH = g->out_h;
+  if(g->halfsize)
+  { // demosaic/main.c:92-111
+    add_node(g, "demosaic", "halfsize", g->hw, g->hh, 1, -1);
+    if(g->resample) add_node(g, "shared", "resample", OW, OH, 1, -1);
+  }
+  else
+  { // demosaic/main.c:159-202 (gaussian splats, full size)
+    add_node(g, "demosaic", "down", g->hw, g->hh, 1, -1);
+    add_node(g, "demosaic", "gauss", g->hw, g->hh, 1, -1);
+    add_node(g, "demosaic", "splat", g->W, g->H, 1, -1);
+    add_node(g, "demosaic", "fix", g->W, g->H, 1, -1);
+  }
+  add_node(g, "colour", "main", OW, OH, 1, -1);
+  add_node(g, "OpenDRT", "hist", (OW + 15) / 16 * 8, (OH + 15) / 16 * 8, 1, -1);
+  add_node(g, "filmcurv", "main", OW, OH, 1, -1);
   // llap/main.c:6-106
-  add_node(g, "llap", "curve", g->W, g->H, 1, -1);
+  add_node(g, "llap", "curve", OW, OH, 1, -1);
   g->lp.clear(); g->la.clear();
   {
-    int rw = (g->W - 1) / 2 + 1, rh = (g->H - 1) / 2 + 1;
+    int rw = (OW - 1) / 2 + 1, rh = (OH - 1) / 2 + 1;
     int nl = 12;
     for(int l = 1; l < nl; l++)
     {
@@ -754,7 +848,7 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
     g->nl = nl;
     for(int j = 1; j <= nl - 2; j++) g->la.push_back(g->lp[j - 1]);
   }
-  // the fused launches and which nodes they compute
+  // the launches and which nodes they compute
   g->launches.clear();
   auto launch = [&](const char *n, const char *k) { g->launches.push_back({ tkn(n), tkn(k) }); return (int)g->launches.size() - 1; };
   int L_dn[7] = { -1, -1, -1, -1, -1, -1, -1 };
@@ -763,15 +857,40 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
     const char *dk[7] = { "half", "downcov", "down", "down", "down", "assemble", "doub" };
     for(int i = 0; i < 7; i++) L_dn[i] = launch("denoise", dk[i]);
   }
-  const int L_k1 = launch("hilite", "reduce");
   std::vector<int> L_hr, L_ha, L_lr, L_la;
-  for(size_t l = 1; l < g->hr.size(); l++) L_hr.push_back(launch("hilite", "reduce"));
-  for(size_t l = 0; l < g->hb.size(); l++) L_ha.push_back(launch("hilite", "assemble"));
-  const int L_dev = launch("demosaic", "fix");
+  int L_noop = -1, L_half = -1, L_a0 = -1, L_doub = -1, L_gauss = -1, L_splat = -1, L_fix = -1, L_hs = -1, L_rs = -1;
+  int L_post, L_k1 = -1;
+  if(!g->unfused)
+  {
+    L_k1 = launch("hilite", "reduce");
+    for(size_t l = 1; l < g->hr.size(); l++) L_hr.push_back(launch("hilite", "reduce"));
+    for(size_t l = 0; l < g->hb.size(); l++) L_ha.push_back(launch("hilite", "assemble"));
+    L_post = launch("demosaic", "fix");
+  }
+  else
+  {
+    if(!g->wavelet) L_noop = launch("denoise", "noop");
+    L_half = launch("hilite", "half");
+    for(size_t l = 0; l < g->hr.size(); l++) L_hr.push_back(launch("hilite", "reduce"));
+    for(size_t l = 0; l < g->hb.size(); l++) L_ha.push_back(launch("hilite", "assemble"));
+    L_a0 = launch("hilite", "assemble");
+    L_doub = launch("hilite", "doub");
+    if(g->halfsize)
+    {
+      L_hs = launch("demosaic", "halfsize");
+      if(g->resample) L_rs = launch("shared", "resample");
+    }
+    else
+    {
+      L_gauss = launch("demosaic", "gauss");
+      L_splat = launch("demosaic", "splat");
+      L_fix = launch("demosaic", "fix");
+    }
+    L_post = launch("llap", "curve");
+  }
   for(size_t l = 1; l < g->lp.size(); l++) L_lr.push_back(launch("llap", "reduce"));
   for(size_t j = 0; j < g->la.size(); j++) L_la.push_back(launch("llap", "assemble"));
   const int L_fin = launch("llap", "colour");
-  (void)fused;
   for(auto &n : g->nodes)
   {
     if(n.name == tkn("denoise") && g->wavelet)
@@ -780,24 +899,38 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
       n.fused = L_dn[map[&n - &g->nodes[0]]];
       continue;
     }
-    if(n.name == tkn("denoise") || n.kernel == tkn("doub") || n.name == tkn("demosaic") || n.name == tkn("colour")
-        || n.name == tkn("OpenDRT") || n.name == tkn("filmcurv") || n.kernel == tkn("curve")) n.fused = L_dev;
-    if(n.name == tkn("hilite") && n.kernel == tkn("half")) n.fused = L_k1;
+    if(!g->unfused)
+    {
+      if(n.name == tkn("denoise") || n.kernel == tkn("doub") || n.name == tkn("demosaic") || n.name == tkn("colour")
+          || n.name == tkn("OpenDRT") || n.name == tkn("filmcurv") || n.kernel == tkn("curve")) n.fused = L_post;
+      if(n.name == tkn("hilite") && n.kernel == tkn("half")) n.fused = L_k1;
+      continue;
+    }
+    if(n.name == tkn("denoise")) n.fused = L_noop;
+    else if(n.name == tkn("hilite")) n.fused = n.kernel == tkn("half") ? L_half : L_doub;
+    else if(n.kernel == tkn("halfsize")) n.fused = L_hs;
+    else if(n.kernel == tkn("resample")) n.fused = L_rs;
+    else if(n.kernel == tkn("gauss") || n.kernel == tkn("down")) n.fused = L_gauss;
+    else if(n.kernel == tkn("splat")) n.fused = L_splat;
+    else if(n.kernel == tkn("fix")) n.fused = L_fix;
+    else n.fused = L_post;   // colour, histogram, filmcurv, llap curve
   }
   // per level nodes (reduce and assemble pairs in create_nodes order)
   for(size_t l = 0; l < g->hr.size(); l++)
   {
-    add_node(g, "hilite", "reduce", g->hr[l].w, g->hr[l].h, 1, l == 0 ? L_k1 : L_hr[l - 1]);
+    const int lr = g->unfused ? L_hr[l] : (l == 0 ? L_k1 : L_hr[l - 1]);
+    const int la = l == 0 ? (g->unfused ? L_a0 : L_post) : L_ha[l - 1];
+    add_node(g, "hilite", "reduce", g->hr[l].w, g->hr[l].h, 1, lr);
     const int fw = l == 0 ? g->hw : g->hr[l - 1].w, fh = l == 0 ? g->hh : g->hr[l - 1].h;
-    add_node(g, "hilite", "assemble", fw, fh, 1, l == 0 ? L_dev : L_ha[l - 1]);
+    add_node(g, "hilite", "assemble", fw, fh, 1, la);
   }
   for(size_t l = 0; l < g->lp.size(); l++)
   {
-    add_node(g, "llap", "reduce", g->lp[l].w, g->lp[l].h, 11, l == 0 ? L_dev : L_lr[l - 1]);
-    const int fw = l == 0 ? g->W : g->lp[l - 1].w, fh = l == 0 ? g->H : g->lp[l - 1].h;
+    add_node(g, "llap", "reduce", g->lp[l].w, g->lp[l].h, 11, l == 0 ? L_post : L_lr[l - 1]);
+    const int fw = l == 0 ? OW : g->lp[l - 1].w, fh = l == 0 ? OH : g->lp[l - 1].h;
     add_node(g, "llap", "assemble", fw, fh, 1, l == 0 ? L_fin : L_la[l - 1]);
   }
-  add_node(g, "llap", "colour", g->W, g->H, 1, L_fin);
+  add_node(g, "llap", "colour", OW, OH, 1, L_fin);
 
   g->nodes_ready = true;
   return VKDT_CUDA_SUCCESS;
@@ -818,26 +951,44 @@ int vkdt_cuda_graph_alloc(vkdt_cuda_graph_t *g, uint64_t *device_bytes)
   g->off_src = take(g->src_bytes);
   for(auto &l : g->hr) l.off = take((size_t)l.w * l.h * 8);
   for(auto &l : g->hb) l.off = take((size_t)l.w * l.h * 8);
-  g->off_rgbf = take((size_t)g->W * g->H * 8);
+  g->off_rgbf = take((size_t)g->out_w * g->out_h * 8);
   for(auto &l : g->lp) l.off = take((size_t)l.w * l.h * 2 * 11);
   for(auto &l : g->la) l.off = take((size_t)l.w * l.h * 2);
   g->off_out = take(g->sink_bytes);
   g->off_hist = take(257 * 4);
   g->off_lut = take(65536 * 2);
   if(g->debug) { g->off_dbg0 = take((size_t)g->W * g->H * 2); g->off_dbg1 = take((size_t)g->W * g->H * 2); }
+  const size_t hbytes = (size_t)g->hw * g->hh * 8;
   if(g->wavelet)
-  { // the half size nodes of the wavelet denoise and its full size output
-    const size_t hb = (size_t)g->hw * g->hh * 8;
-    g->off_dnh = take(hb);
-    for(int i = 0; i < 4; i++) g->off_dnl[i] = take(hb);
-    g->off_dna = take(hb);
-    g->off_dn = take((size_t)g->W * g->H * 2);
-    g->off_idlut = take(65536 * 2);
+  { // the half size nodes of the wavelet denoise
+    g->off_dnh = take(hbytes);
+    for(int i = 0; i < 4; i++) g->off_dnl[i] = take(hbytes);
+    g->off_dna = take(hbytes);
+  }
+  // the (denoised) normalised mosaic: wavelet output, or the noop output of the per-node chain
+  if(g->wavelet || g->unfused) g->off_dn = take((size_t)g->W * g->H * 2);
+  if(g->wavelet && !g->unfused) g->off_idlut = take(65536 * 2);
+  if(g->unfused)
+  { // the per-node chain's images (intermediate f16 images like the reference's)
+    g->off_h0 = take(hbytes);
+    g->off_b0 = take(hbytes);
+    g->off_hl = take((size_t)g->W * g->H * 2);
+    if(g->halfsize)
+    {
+      g->off_hs = take(hbytes);
+      g->off_dm = g->resample ? take((size_t)g->out_w * g->out_h * 8) : g->off_hs;
+    }
+    else
+    {
+      g->off_cov = take(hbytes);
+      g->off_g = take((size_t)g->W * g->H * 2);
+      g->off_dm = take((size_t)g->W * g->H * 8);
+    }
   }
   g->arena_bytes = off;
   CU(cudaMalloc((void **)&g->arena, g->arena_bytes));
   CU(cudaMemset(g->arena, 0, g->arena_bytes));
-  if(g->wavelet)
+  if(g->wavelet && !g->unfused)
   {
     std::vector<uint16_t> id(65536);
     for(int v = 0; v < 65536; v++) id[v] = (uint16_t)v;
@@ -964,8 +1115,9 @@ int vkdt_cuda_graph_develop_static(vkdt_cuda_graph_t *g, const void *d_mosaic, v
   if(g_device < 0) return fail(VKDT_CUDA_ERROR_INITIALIZATION_FAILED, "vkdt_cuda_init was not called");
   if(g->allocated) return fail(VKDT_CUDA_INCOMPLETE, "graph owns device buffers: use vkdt_cuda_graph_develop");
   if(!g->nodes_ready) return fail(VKDT_CUDA_INCOMPLETE, "call vkdt_cuda_graph_create_nodes first");
-  if(g->debug || g->timing || g->want_hist || g->wavelet)
-    return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "debug stages, timing, the histogram and the wavelet denoise need an allocated graph");
+  if(g->debug || g->timing || g->want_hist || g->wavelet || g->unfused)
+    return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED,
+                "debug stages, timing, the histogram, the wavelet denoise, x-trans and reduced sizes need an allocated graph");
   if(!d_mosaic || !d_rgba) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "null device buffer");
   const uint32_t *b = g->ip.crop_aabb;
   if(g->W != (int)(b[2] - b[0]) || g->H != (int)(b[3] - b[1]))
@@ -1067,22 +1219,24 @@ int vkdt_cuda_graph_debug_stage(vkdt_cuda_graph_t *g, int stage, float *out, siz
 {
   if(!g || !g->allocated) return fail(VKDT_CUDA_INCOMPLETE, "graph not allocated");
   CU(cudaStreamSynchronize(g->stream));
-  const size_t npx = (size_t)g->W * g->H;
+  const size_t npx = (size_t)g->W * g->H, nout = (size_t)g->out_w * g->out_h;
   if(stage == 0 || stage == 1)
   {
     if(!g->debug) return fail(VKDT_CUDA_INCOMPLETE, "debug stages not enabled");
     if(count < npx) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "buffer too small");
     std::vector<__half> h(npx);
-    CU(cudaMemcpy(h.data(), g->arena + (stage == 0 ? g->off_dbg0 : g->off_dbg1), npx * 2, cudaMemcpyDeviceToHost));
+    // the per-node chain keeps both images; the fused kernel writes debug copies
+    const size_t off = g->unfused ? (stage == 0 ? g->off_dn : g->off_hl) : (stage == 0 ? g->off_dbg0 : g->off_dbg1);
+    CU(cudaMemcpy(h.data(), g->arena + off, npx * 2, cudaMemcpyDeviceToHost));
     for(size_t i = 0; i < npx; i++) out[i] = __half2float(h[i]);
     return 0;
   }
-  if(stage == 2)
+  if(stage == 2 || (stage == 3 && g->unfused))
   {
-    if(count < npx * 4) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "buffer too small");
-    std::vector<__half> h(npx * 4);
-    CU(cudaMemcpy(h.data(), g->arena + g->off_rgbf, npx * 8, cudaMemcpyDeviceToHost));
-    for(size_t i = 0; i < npx * 4; i++) out[i] = __half2float(h[i]);
+    if(count < nout * 4) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "buffer too small");
+    std::vector<__half> h(nout * 4);
+    CU(cudaMemcpy(h.data(), g->arena + (stage == 2 ? g->off_rgbf : g->off_dm), nout * 8, cudaMemcpyDeviceToHost));
+    for(size_t i = 0; i < nout * 4; i++) out[i] = __half2float(h[i]);
     return 0;
   }
   return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "stage %d", stage);

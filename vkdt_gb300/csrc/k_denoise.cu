@@ -10,6 +10,7 @@
 // operations in the shader's order, as the oracle evaluates them.
 #include "common.cuh"
 #include "kernels.h"
+#include "sampler.cuh"
 
 namespace {
 
@@ -49,33 +50,31 @@ DEV void swz(int &x, int &y, int w, int h)
 // x^y for x >= 0 on the special function unit (feeds continuous weights only)
 DEV float fpow(float x, float y) { return __powf(x, y); }
 
-DEV void ld4(const half4 *img, int w, int x, int y, float v[4]) { ld_half4(img + (size_t)y * w + x, v[0], v[1], v[2], v[3]); }
-
-// position of a texture() read in texel space, rounded to the sampler's 8 sub-texel bits
-DEV float subtexel(float v) { return __fmul_rn(floorf(__fadd_rn(__fmul_rn(v, 256.0f), 0.5f)), 0.00390625f); }
-
-// texture() with LINEAR + MIRRORED_REPEAT at texel-space position (x, y)
-DEV void bilinear(const half4 *img, int w, int h, float x, float y, float out[4])
-{
-  const float xs = subtexel(__fsub_rn(x, 0.5f)), ys = subtexel(__fsub_rn(y, 0.5f));
-  const float fx = floorf(xs), fy = floorf(ys);
-  const int x0 = (int)fx, y0 = (int)fy;
-  const float ax = xs - fx, ay = ys - fy;
-  const int X0 = mirror(x0, w), X1 = mirror(x0 + 1, w), Y0 = mirror(y0, h), Y1 = mirror(y0 + 1, h);
-  float t00[4], t10[4], t01[4], t11[4];
-  ld4(img, w, X0, Y0, t00); ld4(img, w, X1, Y0, t10); ld4(img, w, X0, Y1, t01); ld4(img, w, X1, Y1, t11);
-#pragma unroll
-  for(int k = 0; k < 4; k++)
-    out[k] = (t00[k] * (1.0f - ax) + t10[k] * ax) * (1.0f - ay) + (t01[k] * (1.0f - ax) + t11[k] * ax) * ay;
-}
-
 // ---------------------------------------------------------------- half
-// denoise/half.comp:24-74 (bayer): R, mean of the greens (a clipped green is
+// denoise/half.comp:24-74: bayer R, mean of the greens (a clipped green is
 // replaced by the other one), B of the 2x2 block, on the raw unorm values
 __global__ void __launch_bounds__(256) k_dn_half(const dev_denoise_t p)
 {
   const int x = blockIdx.x * 16 + threadIdx.x % 16, y = blockIdx.y * 16 + threadIdx.x / 16;
   if(x >= p.hw || y >= p.hh) return;
+  if(p.filters == 9u)
+  { // x-trans: the 3x3 block, greens averaged, red and blue by block parity (texelFetch reads)
+    const int bx = p.cx + 3 * x, by = p.cy + 3 * y;
+    float c[9];
+#pragma unroll
+    for(int i = 0; i < 3; i++)
+#pragma unroll
+      for(int j = 0; j < 3; j++)
+      {
+        const int X = bx + i, Y = by + j;
+        c[3 * i + j] = (X < p.in_w && Y < p.in_h) ? unorm16(__ldg(p.mosaic + (size_t)Y * p.pitch + X)) : 0.0f;
+      }
+    const float c0 = __fmul_rn(__fadd_rn(c[1], c[7]), 0.5f), c1 = __fmul_rn(__fadd_rn(c[3], c[5]), 0.5f);
+    const bool odd = ((x + y + p.cx + p.cy) & 1) > 0;
+    const float g = __fdiv_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(c[0], c[2]), c[4]), c[6]), c[8]), 5.0f);
+    p.half_img[(size_t)y * p.hw + x] = mk_half4(odd ? c0 : c1, g, odd ? c1 : c0, 1.0f);
+    return;
+  }
   const int i0 = p.cx + 2 * x, j0 = p.cy + 2 * y;
   float cx = raw_m(p, i0, j0 + 1), cy = raw_m(p, i0 + 1, j0 + 1);
   float cz = raw_m(p, i0 + 1, j0), cw = raw_m(p, i0, j0);
@@ -312,7 +311,7 @@ __global__ void __launch_bounds__(256) k_dn_assemble(const dev_denoise_t p)
 }
 
 // ---------------------------------------------------------------- doub
-// denoise/doub.comp:35-116 (bayer, no gain map): per CFA sample, shrink the
+// denoise/doub.comp:35-116 (no gain map): per CFA sample, shrink the
 // full resolution residual against the bilinear up-sampled noisy coarse
 // level, protected by the detail mask, and normalise to [0, 1]
 __global__ void __launch_bounds__(256) k_dn_doub(const dev_denoise_t p)
@@ -325,11 +324,12 @@ __global__ void __launch_bounds__(256) k_dn_doub(const dev_denoise_t p)
   float upsm[4], down[4];
   bilinear(p.asm_img, p.hw, p.hh, tx, ty, upsm);
   bilinear(p.half_img, p.hw, p.hh, tx, ty, down);
-  const int col = cfa_bayer(x, y);
+  const int col = p.filters == 9u ? cfa_xtrans(x, y) : cfa_bayer(x, y);
   const float black = p.black[col], white = p.white[col];
   const float crs = col == 0 ? upsm[0] : (col == 1 ? upsm[1] : upsm[2]);
   const float crs1 = col == 0 ? down[0] : (col == 1 ? down[1] : down[2]);
-  const float Tt = 0.5f * p.strength * upsm[3];
+  float Tt = 0.5f * p.strength * upsm[3];
+  if(p.filters == 9u && col != 1) Tt /= fmaxf(1e-4f, upsm[3]);
   const float blendw = 0.5f * ((col == 1 ? p.luma : 1.0f) + 1.0f);
   float sigma[3];
   noise_sigma_fast(sigma, p, black, white, crs);

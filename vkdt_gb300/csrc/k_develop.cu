@@ -30,6 +30,7 @@
 #include "hilite.cuh"
 #include "kernels.h"
 #include "pixel.cuh"
+#include "develop_px.cuh"
 
 namespace {
 
@@ -62,39 +63,6 @@ DEV int mirror1(int i, int n)
   if(i < 0) i = -1 - i;
   if(i >= n) i = 2 * n - 1 - i;
   return min(max(i, 0), n - 1);
-}
-
-// colour/main-impl.glsl:200-341 on the matrix path (no clut/pick/rbf, sat 1)
-DEV void colour_px(const dev_image_t &p, const float in[3], float o[3])
-{
-  float r[3], cl[3], q[3];
-  for(int i = 0; i < 3; i++) r[i] = p.cam[3 * i + 0] * in[0] + p.cam[3 * i + 1] * in[1] + p.cam[3 * i + 2] * in[2];
-  for(int i = 0; i < 3; i++) cl[i] = p.P[3 * i + 0] * r[0] + p.P[3 * i + 1] * r[1] + p.P[3 * i + 2] * r[2];
-  for(int i = 0; i < 3; i++) cl[i] *= p.clscale[i];
-  for(int i = 0; i < 3; i++) q[i] = p.Q[3 * i + 0] * cl[0] + p.Q[3 * i + 1] * cl[1] + p.Q[3 * i + 2] * cl[2];
-  for(int i = 0; i < 3; i++) o[i] = f16r(gclamp(q[i] * p.mulw, -65535.0f, 65535.0f));
-}
-
-// filmcurv/main.comp:106-205, colour modes 1 and 3 (adjust_colour_dng,
-// shared.glsl:371-387). pow as GPUs evaluate GLSL pow: exp2(k log2 x)
-DEV void filmcurv_px(const dev_image_t &p, const float in[3], float o[3])
-{
-  float c0[3], c1[3];
-  for(int k = 0; k < 3; k++) c0[k] = in[k] + p.fc_bias;
-  for(int k = 0; k < 3; k++) c1[k] = 1.0f - curve_exp(-gpow_pos(fmaxf(c0[k], 1e-7f) * p.fc_il, p.fc_k));
-  if(p.fc_mode == 3)
-  {
-    bool fx = false, fy = false, fz = false;
-    float t;
-    if(c0[2] > c0[1]) { t = c0[2]; c0[2] = c0[1]; c0[1] = t; t = c1[2]; c1[2] = c1[1]; c1[1] = t; fx = true; }
-    if(c0[1] > c0[0]) { t = c0[0]; c0[0] = c0[1]; c0[1] = t; t = c1[0]; c1[0] = c1[1]; c1[1] = t; fy = true; }
-    if(c0[2] > c0[1]) { t = c0[2]; c0[2] = c0[1]; c0[1] = t; t = c1[2]; c1[2] = c1[1]; c1[1] = t; fz = true; }
-    c1[1] = gmix(c1[2], c1[0], (c0[1] - c0[2] + 1e-6f) / (c0[0] - c0[2] + 1e-6f));
-    if(fz) { t = c1[2]; c1[2] = c1[1]; c1[1] = t; }
-    if(fy) { t = c1[0]; c1[0] = c1[1]; c1[1] = t; }
-    if(fx) { t = c1[2]; c1[2] = c1[1]; c1[1] = t; }
-  }
-  for(int k = 0; k < 3; k++) o[k] = f16r(c1[k]);
 }
 
 // weight of a 3x3 tap from the per covariance table (h: (+-1,0), v: (0,+-1), d: diagonal)

@@ -1,0 +1,434 @@
+// The per-node chain of the path for what the fused develop kernel does not
+// cover: x-trans mosaics, and reduced output sizes (demosaic/halfsize +
+// shared/resample, the thumbnail path) for both mosaics. One kernel per
+// reference node, intermediates in HBM as f16 images like the reference:
+//   [denoise/noop] -> hilite/half -> (hilite reduce/assemble pyramid, k_hilite.cu)
+//   -> hilite/doub -> demosaic (gauss, splat, fix | halfsize [-> resample])
+//   -> colour -> [histogram] -> filmcurv -> llap/curve -> first llap/reduce (k_post)
+//   -> (llap pyramid, k_llap.cu)
+// The arithmetic restates the shaders in their order; computations that
+// decide a branch (the green structure tensor and its snapping, the clip
+// tests) use explicit IEEE operations, as the oracle evaluates them.
+#include "common.cuh"
+#include "develop_px.cuh"
+#include "hilite.cuh"
+#include "kernels.h"
+#include "pixel.cuh"
+#include "sampler.cuh"
+
+namespace {
+
+DEV float dn_m(const dev_nodes_t &p, const __half *img, int x, int y)
+{ // texture() at a texel centre of a W x H one channel image: the mirrored texel
+  return h2f(img[(size_t)mirror(y, p.H) * p.W + mirror(x, p.W)]);
+}
+DEV float dn_z(const dev_nodes_t &p, const __half *img, int x, int y)
+{ // texelFetch: out of range reads 0
+  if(x < 0 || y < 0 || x >= p.W || y >= p.H) return 0.0f;
+  return h2f(img[(size_t)y * p.W + x]);
+}
+
+// denoise/noop.comp:36-57 through the code table: the normalised mosaic as f16
+__global__ void __launch_bounds__(256) k_nd_noop(const dev_nodes_t p)
+{
+  const int x = blockIdx.x * 64 + threadIdx.x % 64, y = blockIdx.y * 4 + threadIdx.x / 64;
+  if(x >= p.W || y >= p.H) return;
+  p.dn[(size_t)y * p.W + x] = __ldg(p.noop_lut + __ldg(p.mosaic + (size_t)(y + p.cy) * p.pitch + x + p.cx));
+}
+
+// hilite/half.comp:21-72
+template<bool XT> __global__ void __launch_bounds__(256) k_nd_hl_half(const dev_nodes_t p)
+{
+  const int x = blockIdx.x * 16 + threadIdx.x % 16, y = blockIdx.y * 16 + threadIdx.x / 16;
+  if(x >= p.hw || y >= p.hh) return;
+  float h[3];
+  if(XT)
+  {
+    float c[9];
+#pragma unroll
+    for(int i = 0; i < 3; i++)
+#pragma unroll
+      for(int j = 0; j < 3; j++) c[3 * i + j] = dn_z(p, p.dn, 3 * x + i, 3 * y + j);
+    hilite_half_xtrans(c, x, y, p.hl_white, h);
+  }
+  else
+    hilite_half_bayer(dn_m(p, p.dn, 2 * x, 2 * y), dn_m(p, p.dn, 2 * x + 1, 2 * y),
+                      dn_m(p, p.dn, 2 * x, 2 * y + 1), dn_m(p, p.dn, 2 * x + 1, 2 * y + 1), p.hl_white, h);
+  p.h0[(size_t)y * p.hw + x] = mk_half4(h[0], h[1], h[2], 1.0f);
+}
+
+// hilite/doub.comp:141-241: re-mosaic, blending clipped samples towards the
+// scaled coarse colour. Mosaic positions no block covers are not written.
+template<bool XT> __global__ void __launch_bounds__(256) k_nd_hl_doub(const dev_nodes_t p)
+{
+  const int x = blockIdx.x * 16 + threadIdx.x % 16, y = blockIdx.y * 16 + threadIdx.x / 16;
+  if(x >= p.hw || y >= p.hh) return;
+  float up[3], a;
+  ld_half4(p.b0 + (size_t)y * p.hw + x, up[0], up[1], up[2], a);
+  const float white = p.hl_white;
+  if(XT)
+  {
+    if(((x + y) & 1) == 0) { const float t = up[0]; up[0] = up[2]; up[2] = t; }
+    float c[9];
+#pragma unroll
+    for(int i = 0; i < 3; i++)
+#pragma unroll
+      for(int j = 0; j < 3; j++) c[3 * i + j] = dn_z(p, p.dn, 3 * x + i, 3 * y + j);
+    const float minr = fminf(c[1], c[7]), minb = fminf(c[3], c[5]);
+    const float ming = fminf(fminf(fminf(c[0], c[2]), c[4]), fminf(c[6], c[8]));
+    const float sr = minr / fmaxf(0.001f, up[0]);
+    const float sg = ming / fmaxf(0.001f, up[1]);
+    const float sb = minb / fmaxf(0.001f, up[2]);
+    const float wr = expf(up[0] - fmaxf(up[1], up[2]));
+    const float wg = expf(up[1] - fmaxf(up[0], up[2]));
+    const float wbb = expf(up[2] - fmaxf(up[0], up[1]));
+    const float scale = (sr * wr + sg * wg + sb * wbb) / (wr + wg + wbb);
+    const float maxr = fmaxf(c[1], c[7]), maxb = fmaxf(c[3], c[5]);
+    const float maxg = fmaxf(fmaxf(fmaxf(c[0], c[2]), c[4]), fmaxf(c[6], c[8]));
+    const float softw = __fmul_rn(0.97f, white);
+    const float maxrgb = fmaxf(maxr, fmaxf(maxg, maxb));
+    if(maxrgb > softw)
+    {
+      float t = smoothstep(softw, white, maxrgb);
+      c[1] = gmix(c[1], up[0] * scale, t);
+      c[7] = gmix(c[7], up[0] * scale, t);
+      c[3] = gmix(c[3], up[2] * scale, t);
+      c[5] = gmix(c[5], up[2] * scale, t);
+      t = smoothstep(softw, white, ming);
+      c[0] = gmix(c[0], up[1] * scale, t);
+      c[2] = gmix(c[2], up[1] * scale, t);
+      c[4] = gmix(c[4], up[1] * scale, t);
+      c[6] = gmix(c[6], up[1] * scale, t);
+      c[8] = gmix(c[8], up[1] * scale, t);
+    }
+#pragma unroll
+    for(int i = 0; i < 3; i++)
+#pragma unroll
+      for(int j = 0; j < 3; j++)
+      {
+        const int X = 3 * x + i, Y = 3 * y + j;
+        if(X < p.W && Y < p.H) p.hl[(size_t)Y * p.W + X] = f2h(c[3 * i + j]);
+      }
+  }
+  else
+  {
+    float o[4];
+    hilite_doub_bayer(dn_m(p, p.dn, 2 * x, 2 * y), dn_m(p, p.dn, 2 * x + 1, 2 * y),
+                      dn_m(p, p.dn, 2 * x, 2 * y + 1), dn_m(p, p.dn, 2 * x + 1, 2 * y + 1), up, white, o);
+    const int X = 2 * x, Y = 2 * y;
+    if(X < p.W && Y < p.H) p.hl[(size_t)Y * p.W + X] = f2h(o[0]);
+    if(X + 1 < p.W && Y < p.H) p.hl[(size_t)Y * p.W + X + 1] = f2h(o[1]);
+    if(X < p.W && Y + 1 < p.H) p.hl[(size_t)(Y + 1) * p.W + X] = f2h(o[2]);
+    if(X + 1 < p.W && Y + 1 < p.H) p.hl[(size_t)(Y + 1) * p.W + X + 1] = f2h(o[3]);
+  }
+}
+
+// demosaic/gauss.comp:19-126 (x-trans): structure tensor of the 5 greens of
+// each 3x3 block, the form with the smaller determinant decomposed; the
+// eigenvector snapped to an axis when it is within a factor 2 of it, else an
+// isotropic 0.1
+__global__ void __launch_bounds__(256) k_nd_gauss_xt(const dev_nodes_t p)
+{
+  const int x = blockIdx.x * 16 + threadIdx.x % 16, y = blockIdx.y * 16 + threadIdx.x / 16;
+  if(x >= p.hw || y >= p.hh) return;
+  // greens (i + j even) of the block, i the x offset
+  const int gi[5] = { 0, 2, 1, 0, 2 }, gj[5] = { 0, 0, 1, 2, 2 };
+  float px[5];
+  float mw0 = 0.0f, mw1 = 0.0f, mb0 = 0.0f, mb1 = 0.0f, smw = 0.0f, smb = 0.0f;
+#pragma unroll
+  for(int k = 0; k < 5; k++)
+  { // the shader's loop order is j outer, i inner: (0,0) (2,0) (1,1) (0,2) (2,2)
+    px[k] = dn_m(p, p.hl, 3 * x + gi[k], 3 * y + gj[k]);
+    const float fi = (float)gi[k], fj = (float)gj[k];
+    mw0 = __fadd_rn(mw0, __fmul_rn(fi, px[k])); mw1 = __fadd_rn(mw1, __fmul_rn(fj, px[k]));
+    smw = __fadd_rn(smw, px[k]);
+    mb0 = __fadd_rn(mb0, __fdiv_rn(fi, px[k])); mb1 = __fadd_rn(mb1, __fdiv_rn(fj, px[k]));
+    smb = __fadd_rn(smb, __fdiv_rn(1.0f, px[k]));
+  }
+  mw0 = __fdiv_rn(mw0, smw); mw1 = __fdiv_rn(mw1, smw);
+  mb0 = __fdiv_rn(mb0, smb); mb1 = __fdiv_rn(mb1, smb);
+  float Sw00 = 0, Sw01 = 0, Sw10 = 0, Sw11 = 0, Sb00 = 0, Sb01 = 0, Sb10 = 0, Sb11 = 0, sw = 0, sb = 0;
+#pragma unroll
+  for(int k = 0; k < 5; k++)
+  {
+    float p2 = __fmul_rn(px[k], px[k]);
+    float q0 = __fsub_rn((float)gi[k], mw0), q1 = __fsub_rn((float)gj[k], mw1);
+    Sw00 = __fadd_rn(Sw00, __fmul_rn(__fmul_rn(p2, q0), q0));
+    Sw01 = __fadd_rn(Sw01, __fmul_rn(__fmul_rn(p2, q0), q1));
+    Sw10 = __fadd_rn(Sw10, __fmul_rn(__fmul_rn(p2, q1), q0));
+    Sw11 = __fadd_rn(Sw11, __fmul_rn(__fmul_rn(p2, q1), q1));
+    sw = __fadd_rn(sw, p2);
+    q0 = __fsub_rn((float)gi[k], mb0); q1 = __fsub_rn((float)gj[k], mb1);
+    p2 = __fdiv_rn(1.0f, p2);
+    Sb00 = __fadd_rn(Sb00, __fmul_rn(__fmul_rn(p2, q0), q0));
+    Sb01 = __fadd_rn(Sb01, __fmul_rn(__fmul_rn(p2, q0), q1));
+    Sb10 = __fadd_rn(Sb10, __fmul_rn(__fmul_rn(p2, q1), q0));
+    Sb11 = __fadd_rn(Sb11, __fmul_rn(__fmul_rn(p2, q1), q1));
+    sb = __fadd_rn(sb, p2);
+  }
+  Sw00 = __fdiv_rn(Sw00, sw); Sw01 = __fdiv_rn(Sw01, sw); Sw10 = __fdiv_rn(Sw10, sw); Sw11 = __fdiv_rn(Sw11, sw);
+  Sb00 = __fdiv_rn(Sb00, sb); Sb01 = __fdiv_rn(Sb01, sb); Sb10 = __fdiv_rn(Sb10, sb); Sb11 = __fdiv_rn(Sb11, sb);
+  const float detw = __fsub_rn(__fmul_rn(Sw00, Sw11), __fmul_rn(Sw10, Sw01));
+  const float detb = __fsub_rn(__fmul_rn(Sb00, Sb11), __fmul_rn(Sb10, Sb01));
+  float eval[2], e0[2], e1[2];
+  if(detw < detb) evd2x2(eval, e0, e1, Sw00, Sw10, Sw11);
+  else            evd2x2(eval, e0, e1, Sb00, Sb10, Sb11);
+  eval[0] = __fmul_rn(eval[0], 0.4f); eval[1] = __fmul_rn(eval[1], 0.4f);
+  if(fabsf(e0[0]) > __fmul_rn(2.0f, fabsf(e0[1])))      { e0[0] = 1.0f; e0[1] = 0.0f; }
+  else if(fabsf(e0[1]) > __fmul_rn(2.0f, fabsf(e0[0]))) { e0[0] = 0.0f; e0[1] = 1.0f; }
+  else { eval[0] = 0.1f; eval[1] = 0.1f; }
+  p.cov[(size_t)y * p.hw + x] = mk_half4(eval[0], eval[1], e0[0], e0[1]);
+}
+
+DEV void cov_z(const dev_nodes_t &p, int x, int y, float c[4])
+{ // texelFetch of the gauss output (hw x hh), 0 out of range
+  if(x < 0 || y < 0 || x >= p.hw || y >= p.hh) { c[0] = c[1] = c[2] = c[3] = 0.0f; return; }
+  ld_half4(p.cov + (size_t)y * p.hw + x, c[0], c[1], c[2], c[3]);
+}
+
+// demosaic/splat.comp:142-266 (x-trans): 5x5 anisotropic gaussian splat of
+// the greens (only the green sums form the output), taps wrapped by the CFA
+// period 6 at the borders, centre weight 666
+__global__ void __launch_bounds__(256) k_nd_splat_xt(const dev_nodes_t p)
+{
+  const int x = blockIdx.x * 32 + threadIdx.x % 32, y = blockIdx.y * 8 + threadIdx.x / 32;
+  if(x >= p.W || y >= p.H) return;
+  float cov[4];
+  cov_z(p, x / 3, y / 3, cov);
+  const float e0 = gclamp(cov[0], 0.01f, 25.0f), e1 = gclamp(cov[1], 0.01f, 25.0f);
+  const float ie0 = 1.0f / e0, ie1 = 1.0f / e1;
+  float gs = 0.0f, gw = 0.0f;
+#pragma unroll
+  for(int j = -2; j <= 2; j++)
+#pragma unroll
+    for(int i = -2; i <= 2; i++)
+    {
+      if(cfa_xtrans(x + i + 6, y + j + 6) != 1) continue;
+      int px = x + i, py = y + j;
+      if(px < 0) px += 6;
+      if(py < 0) py += 6;
+      if(px >= p.W) px -= 6;
+      if(py >= p.H) py -= 6;
+      const float col = dn_z(p, p.hl, px, py);
+      const float of0 = cov[2] * (float)i + cov[3] * (float)j;
+      const float of1 = -cov[3] * (float)i + cov[2] * (float)j;
+      const float w = (i == 0 && j == 0) ? 666.0f
+                    : gclamp(curve_exp(-0.5f * (of0 * ie0 * of0 + of1 * ie1 * of1)), 1e-4f, 1.0f);
+      gs += col * w;
+      gw += w;
+    }
+  p.g[(size_t)y * p.W + x] = f2h(gs / fmaxf(1e-8f, gw));
+}
+
+// demosaic/fix.comp:21-135 (x-trans): red and blue from ratio-to-green
+// splats of radius clamp(colour + 2, 2, 3), the pattern of write_xtrans2 on
+// the unshifted position
+__global__ void __launch_bounds__(256) k_nd_fix_xt(const dev_nodes_t p)
+{
+  const int x = blockIdx.x * 32 + threadIdx.x % 32, y = blockIdx.y * 8 + threadIdx.x / 32;
+  if(x >= p.W || y >= p.H) return;
+  const float gc = dn_m(p, p.g, x, y);
+  float cov[4];
+  cov_z(p, (x + 1) / 3, (y + 1) / 3, cov);
+  cov[0] = gclamp(cov[0], 1.0f, 10.0f); cov[1] = gclamp(cov[1], 1.0f, 10.0f);
+  const int r = min(max(p.fixup + 2, 2), 3);
+  const float ie0 = 1.0f / (3.0f * cov[0]), ie1 = 1.0f / (3.0f * cov[1]);
+  const float gc4 = 1e-4f + gc;
+  float rr = 0.0f, rb = 0.0f, wr = 0.0f, wb = 0.0f;
+  for(int j = -r; j <= r; j++)
+    for(int i = -r; i <= r; i++)
+    {
+      const int px = x + i, py = y + j;
+      const bool blue_top = ((px / 3 + py / 3) & 1) > 0;
+      const int qx = px - (px / 3) * 3, qy = py - (py / 3) * 3;
+      if(((qx + qy) & 1) == 0) continue;      // green: the centre's own green is used
+      const bool blue = blue_top ^ (qy == 1);
+      const float gh = dn_m(p, p.g, px, py);
+      const float col = dn_m(p, p.hl, px, py);
+      const float of0 = cov[2] * (float)i + cov[3] * (float)j;
+      const float of1 = -cov[3] * (float)i + cov[2] * (float)j;
+      const float w = gclamp(curve_exp(-0.5f * (of0 * ie0 * of0 + of1 * ie1 * of1)), 1e-3f, 1.0f);
+      const float v = col * (gc4 / (1e-4f + gh)) * w;
+      if(blue) { rb += v; wb += w; }
+      else     { rr += v; wr += w; }
+    }
+  p.dm[(size_t)y * p.W + x] = mk_half4(rr / fmaxf(1e-8f, wr), gc, rb / fmaxf(1e-8f, wb), 1.0f);
+}
+
+// demosaic/halfsize.comp:155-187: one rgb texel per CFA block
+template<bool XT> __global__ void __launch_bounds__(256) k_nd_halfsize(const dev_nodes_t p)
+{
+  const int x = blockIdx.x * 16 + threadIdx.x % 16, y = blockIdx.y * 16 + threadIdx.x / 16;
+  if(x >= p.hw || y >= p.hh) return;
+  float r, g, b;
+  if(XT)
+  {
+    float c[9];
+#pragma unroll
+    for(int i = 0; i < 3; i++)
+#pragma unroll
+      for(int j = 0; j < 3; j++) c[3 * i + j] = dn_z(p, p.hl, 3 * x + i, 3 * y + j);
+    g = __fdiv_rn(c[0] + c[2] + c[4] + c[6] + c[8], 5.0f);
+    const float c0 = (c[1] + c[7]) * 0.5f, c1 = (c[3] + c[5]) * 0.5f;
+    if(((x + y) & 1) > 0) { r = c0; b = c1; }
+    else                  { b = c0; r = c1; }
+  }
+  else
+  {
+    const float cx = dn_m(p, p.hl, 2 * x, 2 * y + 1), cy = dn_m(p, p.hl, 2 * x + 1, 2 * y + 1);
+    const float cz = dn_m(p, p.hl, 2 * x + 1, 2 * y), cw = dn_m(p, p.hl, 2 * x, 2 * y);
+    r = cw; g = (cx + cz) * 0.5f; b = cy;
+  }
+  p.hs[(size_t)y * p.hw + x] = mk_half4(r, g, b, 1.0f);
+}
+
+// shared/resample.comp:213-224 with shared.glsl:47-96 sample_catmull_rom:
+// nine bilinear taps of the half size image
+__global__ void __launch_bounds__(256) k_nd_resample(const dev_nodes_t p)
+{
+  const int x = blockIdx.x * 16 + threadIdx.x % 16, y = blockIdx.y * 16 + threadIdx.x / 16;
+  if(x >= p.ow || y >= p.oh) return;
+  const float sp[2] = { __fmul_rn(__fdiv_rn(__fadd_rn((float)x, 0.5f), (float)p.ow), (float)p.hw),
+                        __fmul_rn(__fdiv_rn(__fadd_rn((float)y, 0.5f), (float)p.oh), (float)p.hh) };
+  float t[2][3], w[2][3];
+#pragma unroll
+  for(int k = 0; k < 2; k++)
+  {
+    const float tp1 = floorf(__fsub_rn(sp[k], 0.5f)) + 0.5f;
+    const float f = __fsub_rn(sp[k], tp1);
+    const float w0 = f * (-0.5f + f * (1.0f - 0.5f * f));
+    const float w1 = 1.0f + f * f * (-2.5f + 1.5f * f);
+    const float w2 = f * (0.5f + f * (2.0f - 1.5f * f));
+    const float w3 = f * f * (-0.5f + 0.5f * f);
+    // the tap between texels 1 and 2 decides its sample position: IEEE
+    const float w12 = __fadd_rn(__fadd_rn(1.0f, __fmul_rn(__fmul_rn(f, f), __fadd_rn(-2.5f, __fmul_rn(1.5f, f)))),
+                                __fmul_rn(f, __fadd_rn(0.5f, __fmul_rn(f, __fsub_rn(2.0f, __fmul_rn(1.5f, f))))));
+    const float w2e = __fmul_rn(f, __fadd_rn(0.5f, __fmul_rn(f, __fsub_rn(2.0f, __fmul_rn(1.5f, f)))));
+    t[k][0] = tp1 - 1.0f; t[k][1] = __fadd_rn(tp1, __fdiv_rn(w2e, w12)); t[k][2] = tp1 + 2.0f;
+    w[k][0] = w0; w[k][1] = w1 + w2; w[k][2] = w3;
+  }
+  float res[4] = { 0.0f, 0.0f, 0.0f, 0.0f };
+#pragma unroll
+  for(int j = 0; j < 3; j++)
+#pragma unroll
+    for(int i = 0; i < 3; i++)
+    {
+      float v[4];
+      bilinear(p.hs, p.hw, p.hh, t[0][i], t[1][j], v);
+#pragma unroll
+      for(int k = 0; k < 4; k++) res[k] += v[k] * w[0][i] * w[1][j];
+    }
+  p.dm[(size_t)y * p.ow + x] = mk_half4(res[0], res[1], res[2], res[3]);
+}
+
+// ---------------------------------------------------------------- post
+// colour -> histogram -> filmcurv -> llap/curve on the virtual positions
+// [X0-1, X0+TX) of a tile and the first llap/reduce level of its outputs
+// (the arithmetic of the tail of the fused develop kernel)
+constexpr int TX = 32, TY = 32, NT = 256, NPL = 11;
+constexpr int LX = TX + 1, LH = (LX + 1) / 2;
+
+DEV int mirror1(int i, int n)
+{
+  if(i < 0) i = -1 - i;
+  if(i >= n) i = 2 * n - 1 - i;
+  return min(max(i, 0), n - 1);
+}
+
+__global__ void __launch_bounds__(NT) k_post(const dev_image_t p, const half4 *__restrict__ dm)
+{
+  __shared__ __half L0[NPL][LX][2][LH];
+  __shared__ uint32_t hist[257];
+  const int tid = threadIdx.x;
+  const int W = p.W, H = p.H;
+  // tiles are not shifted (nothing here wraps by the CFA period): slots past
+  // the image hold the mirrored texel, as the level 1 reduce reads them
+  const int OX = blockIdx.x * TX, OY = blockIdx.y * TY;
+  const int X0 = OX, Y0 = OY;
+  const int OXe = min(OX + TX, W), OYe = min(OY + TY, H);
+  if(p.hist) for(int i = tid; i < 257; i += NT) hist[i] = 0;
+  __syncthreads();
+  const float sig = p.ll_sigma, shd = p.ll_shadows, hil = p.ll_highlights, cla = p.ll_clarity;
+  const float r2s = 1.0f / (2.0f * sig), rden = 1.0f / (2.0f * sig * sig / 3.0f);
+  for(int t = tid; t < LX * LX; t += NT)
+  {
+    const int slx = t % LX, sly = t / LX;
+    const int vx = X0 - 1 + slx, vy = Y0 - 1 + sly;
+    const int px = mirror1(vx, W), py = mirror1(vy, H);
+    float d[4];
+    ld_half4(dm + (size_t)py * W + px, d[0], d[1], d[2], d[3]);
+    float co[3];
+    colour_px(p, d, co);
+    const bool own = vx == px && vy == py && px >= OX && px < OXe && py >= OY && py < OYe;
+    if(own && p.hist)
+    {
+      const uint32_t bin = hist_bin(co[0], co[1], co[2]);
+      if(bin > 0) { atomicAdd(&hist[bin], 1u); atomicAdd(&hist[256], 1u); }
+    }
+    float fc[3];
+    filmcurv_px(p, co, fc);
+    if(own) p.rgbf[(size_t)py * W + px] = mk_half4(fc[0], fc[1], fc[2], 1.0f);
+    const float yv = lum2020(gclamp(fc[0], -1000.0f, 1000.0f), gclamp(fc[1], -1000.0f, 1000.0f), gclamp(fc[2], -1000.0f, 1000.0f));
+#pragma unroll
+    for(int k = 0; k < NPL - 1; k++)
+      L0[k][sly][slx & 1][slx >> 1] = f2h(llap_curve_rcp(yv, llap_gamma(k), sig, r2s, rden, shd, hil, cla));
+    L0[NPL - 1][sly][slx & 1][slx >> 1] = f2h(yv);
+  }
+  __syncthreads();
+  // llap/reduce.comp (sample_semisoft) for level 1 outputs [X0/2, X0/2+TX/2)
+  {
+    const int lx = tid % (TX / 2), ly = tid / (TX / 2);
+    const int ox = X0 / 2 + lx, oy = Y0 / 2 + ly;
+    const bool own = ox >= OX / 2 && ox < min(OX / 2 + TX / 2, p.l1w) && oy >= OY / 2 && oy < min(OY / 2 + TY / 2, p.l1h);
+    if(own)
+      for(int k = 0; k < NPL; k++)
+      {
+        float P[3][2];
+        for(int r = 0; r < 3; r++)
+        {
+          const __half *row = &L0[k][2 * ly + r][0][0];
+          const float t0 = h2f(row[lx]), t1 = h2f(row[LH + lx]), t2 = h2f(row[lx + 1]);
+          P[r][0] = t0 + t1;
+          P[r][1] = t1 + t2;
+        }
+        const float q00 = (P[0][0] + P[1][0]) * 0.25f;
+        const float q10 = (P[0][1] + P[1][1]) * 0.25f;
+        const float q01 = (P[1][0] + P[2][0]) * 0.25f;
+        const float q11 = (P[1][1] + P[2][1]) * 0.25f;
+        const float r = (((q00 + q10) + q01) + q11) * 0.25f;
+        p.l1[k * p.l1plane + (size_t)oy * p.l1w + ox] = f2h(r);
+      }
+  }
+  if(p.hist)
+  {
+    __syncthreads();
+    for(int i = tid; i < 257; i += NT) if(hist[i]) atomicAdd(p.hist + i, hist[i]);
+  }
+}
+
+} // namespace
+
+cudaError_t launch_nodes(const dev_nodes_t &p, int stage, cudaStream_t s)
+{
+  const bool xt = p.filters == 9u;
+  const dim3 gh((p.hw + 15) / 16, (p.hh + 15) / 16), gf((p.W + 31) / 32, (p.H + 7) / 8);
+  switch(stage)
+  {
+    case 0: k_nd_noop<<<dim3((p.W + 63) / 64, (p.H + 3) / 4), 256, 0, s>>>(p); break;
+    case 1: if(xt) k_nd_hl_half<true><<<gh, 256, 0, s>>>(p); else k_nd_hl_half<false><<<gh, 256, 0, s>>>(p); break;
+    case 2: if(xt) k_nd_hl_doub<true><<<gh, 256, 0, s>>>(p); else k_nd_hl_doub<false><<<gh, 256, 0, s>>>(p); break;
+    case 3: k_nd_gauss_xt<<<gh, 256, 0, s>>>(p); break;
+    case 4: k_nd_splat_xt<<<gf, 256, 0, s>>>(p); break;
+    case 5: k_nd_fix_xt<<<gf, 256, 0, s>>>(p); break;
+    case 6: if(xt) k_nd_halfsize<true><<<gh, 256, 0, s>>>(p); else k_nd_halfsize<false><<<gh, 256, 0, s>>>(p); break;
+    case 7: k_nd_resample<<<dim3((p.ow + 15) / 16, (p.oh + 15) / 16), 256, 0, s>>>(p); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_post(const dev_image_t &p, const half4 *dm, cudaStream_t s)
+{
+  k_post<<<dim3((p.W + TX - 1) / TX, (p.H + TY - 1) / TY), NT, 0, s>>>(p, dm);
+  return cudaGetLastError();
+}

@@ -79,12 +79,13 @@ struct dev_denoise_t
   const uint16_t *mosaic;
   int pitch, in_w, in_h; // input mosaic layout (mirrored reads cover the full input)
   int cx, cy, W, H;      // crop offset and module output size
-  int hw, hh;            // half size (W/2, H/2)
+  int hw, hh;            // half size (W/block, H/block)
+  uint32_t filters;      // 9 x-trans, else bayer
   float black[3], white[3], wb[3];  // unorm black/white per channel, camera white balance
   float na, nb;          // noise profile (normalised)
   float edge_gain[3];    // exp2(12 edges.rgb + edges.a) of noise_sigma
   float strength, luma, detail, thrs0;  // params; thrs0 = strength^4
-  float block_f;         // 1.414213 (bayer)
+  float block_f;         // 1.414213 (bayer), 2.23607 (x-trans)
   float bscale[4];       // 0.7^(l+1) / block_f, l = 0..3 (assemble.comp)
   float pl[4];           // 0.7^level
   float rgb_to_yuv[9], yuv_to_rgb[9];
@@ -95,6 +96,34 @@ struct dev_denoise_t
 };
 // stage 0 half, 1 downcov, 2..4 down levels 1..3, 5 assemble, 6 doub (k_denoise.cu)
 cudaError_t launch_denoise(const dev_denoise_t &p, int stage, cudaStream_t s);
+
+// the per-node chain for what the fused develop kernel does not cover
+// (x-trans mosaics, reduced output sizes): buffers and sizes (k_nodes.cu)
+struct dev_nodes_t
+{
+  const uint16_t *mosaic;
+  const __half *noop_lut;
+  int pitch, cx, cy;     // source layout and crop offset
+  int W, H;              // denoise / hilite size
+  uint32_t filters;
+  int block, hw, hh;     // 2 bayer, 3 x-trans; hw = W / block
+  float hl_white;
+  int fixup;             // demosaic colour param
+  int ow, oh;            // demosaic output size
+  __half *dn;            // normalised (or denoised) mosaic, W*H
+  half4 *h0;             // hilite/half, hw*hh
+  const half4 *b0;       // hilite level 0 assembled (coarse input of doub), hw*hh
+  __half *hl;            // hilite/doub output mosaic, W*H
+  half4 *cov;            // demosaic/gauss (x-trans), hw*hh
+  __half *g;             // demosaic/splat, W*H
+  half4 *hs;             // demosaic/halfsize, hw*hh
+  half4 *dm;             // demosaic output, ow*oh
+};
+// stage: 0 noop, 1 hilite half, 2 hilite doub, 3 gauss, 4 splat, 5 fix, 6 halfsize, 7 resample
+cudaError_t launch_nodes(const dev_nodes_t &p, int stage, cudaStream_t s);
+// colour -> histogram -> filmcurv -> llap curve -> llap level 1 reduce on the
+// demosaic output (p.W x p.H = the output size; p.mosaic unused)
+cudaError_t launch_post(const dev_image_t &p, const half4 *dm, cudaStream_t s);
 
 // hilite (k_hilite.cu)
 cudaError_t launch_hilite_k1(const dev_hilite_k1_t &p, cudaStream_t s);

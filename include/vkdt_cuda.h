@@ -130,6 +130,9 @@ int  vkdt_cuda_graph_alloc(vkdt_cuda_graph_t *graph, uint64_t *device_bytes);
 /* the node list create_nodes produced (for inspection and per-node timing) */
 int  vkdt_cuda_graph_node_count(vkdt_cuda_graph_t *graph);
 int  vkdt_cuda_graph_node(vkdt_cuda_graph_t *graph, int i, vkdt_cuda_node_info_t *info);
+/* device bytes vkdt_cuda_graph_alloc takes for the graph as it is set up now
+ * (runs create_nodes, allocates nothing); the allocated bytes once allocated */
+int  vkdt_cuda_graph_plan_bytes(vkdt_cuda_graph_t *graph, uint64_t *device_bytes);
 /* output size after alloc */
 int  vkdt_cuda_graph_output_size(vkdt_cuda_graph_t *graph, int *wd, int *ht);
 
@@ -185,6 +188,67 @@ int  vkdt_cuda_graph_develop_static(vkdt_cuda_graph_t *graph, const void *d_mosa
  * the fused launch. returns the count. */
 int  vkdt_cuda_graph_set_timing(vkdt_cuda_graph_t *graph, int enable);
 int  vkdt_cuda_graph_query_times(vkdt_cuda_graph_t *graph, float *ms, dt_token_t *names, dt_token_t *kernels, int max);
+
+/* replay the launch sequence of a run as a captured CUDA graph (default 1).
+ * 0 launches it eagerly every run: no re-capture after the image metadata
+ * changes, for graphs that develop a different image each run. */
+int  vkdt_cuda_graph_set_capture(vkdt_cuda_graph_t *graph, int enable);
+/* the graph's own stream (a cudaStream_t), valid after alloc */
+void *vkdt_cuda_graph_stream(vkdt_cuda_graph_t *graph);
+
+/* ---- develop server: continuous batching of develop jobs on one device.
+ * No counterpart in the reference, which runs one graph at a time; this is
+ * the export daemon beside vkdt-cli. Jobs of any size are queued, admitted
+ * while a slot is free and the device bytes of the graphs that run them stay
+ * under the cap, and developed concurrently (one stream per graph). Every job
+ * gets exactly the result it gets alone: same kernels, no shared state. */
+typedef struct vkdt_cuda_server_t vkdt_cuda_server_t;
+
+typedef struct vkdt_cuda_server_cfg_t
+{
+  const char *cfg;          /* graph .cfg text (module params), NULL = the darkroom path defaults */
+  size_t      cfg_len;
+  int         slots;        /* jobs in flight at once (streams), >= 1 */
+  uint64_t    hbm_cap;      /* device bytes the server's graphs may hold, 0 = 90% of free memory */
+  int         llap_levels;  /* llap pyramid depth, 0 = automatic */
+}
+vkdt_cuda_server_cfg_t;
+
+typedef struct vkdt_cuda_job_t
+{
+  int         wd, ht;       /* mosaic size */
+  vkdt_cuda_img_param_t ip; /* metadata of this image */
+  int         out_wd, out_ht; /* requested output size, 0 = full size */
+  const void *src;          /* uint16 mosaic, wd*ht, device or host (pinned for overlap) */
+  void       *dst;          /* rgba f16 output at the output size, device or host */
+  int         src_on_device, dst_on_device;
+}
+vkdt_cuda_job_t;
+
+typedef struct vkdt_cuda_server_stats_t
+{
+  uint64_t completed, failed;
+  double   mpix;            /* input megapixels of completed jobs */
+  double   latency_p50_ms, latency_p99_ms;  /* submit -> done, completed jobs */
+  uint64_t peak_device_bytes;
+  int      graphs;          /* allocated graphs in the pool */
+}
+vkdt_cuda_server_stats_t;
+
+int  vkdt_cuda_server_create(const vkdt_cuda_server_cfg_t *cfg, vkdt_cuda_server_t **server);
+/* queue a job (the buffers must stay valid until it is done); *job_id names it */
+int  vkdt_cuda_server_submit(vkdt_cuda_server_t *server, const vkdt_cuda_job_t *job, uint64_t *job_id);
+/* bounded wait for one job: its status (0, or the error the develop returned),
+ * VKDT_CUDA_TIMEOUT when timeout_ms passed first, VKDT_CUDA_NOT_READY for 0 ms */
+int  vkdt_cuda_server_wait(vkdt_cuda_server_t *server, uint64_t job_id, uint32_t timeout_ms);
+/* bounded wait for every queued and running job */
+int  vkdt_cuda_server_drain(vkdt_cuda_server_t *server, uint32_t timeout_ms);
+/* times of a finished job: queued (submit -> start) and latency (submit -> done), ms */
+int  vkdt_cuda_server_job_times(vkdt_cuda_server_t *server, uint64_t job_id, double *queued_ms, double *latency_ms);
+int  vkdt_cuda_server_stats(vkdt_cuda_server_t *server, vkdt_cuda_server_stats_t *stats);
+/* forget the latency samples and counters (the pool of graphs stays) */
+int  vkdt_cuda_server_reset_stats(vkdt_cuda_server_t *server);
+void vkdt_cuda_server_destroy(vkdt_cuda_server_t *server);
 
 /* 257 bin histogram the filmcurv module feeds to its display
  * (OpenDRT/hist.comp): bins 0..255 and the count in [256]. enable before run. */

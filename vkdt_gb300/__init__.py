@@ -12,7 +12,7 @@ import numpy as np
 from . import _lib
 from ._lib import ImgParam, Scene, check, token, token_str, RUN_ALL, RUN_UPLOAD_SOURCE, RUN_DOWNLOAD_SINK, RUN_WAIT_DONE
 
-__all__ = ["Graph", "ImgParam", "Scene", "init", "default_img_param", "scene_host", "scene_device",
+__all__ = ["Graph", "Server", "ImgParam", "Scene", "init", "default_img_param", "scene_host", "scene_device",
            "DARKROOM_CFG", "CAM_TO_REC2020", "supports"]
 
 # the synthetic camera: camera rgb -> rec2020, rows sum to one
@@ -253,3 +253,74 @@ class Graph:
         check(self._l.vkdt_cuda_graph_debug_stage(self._g, stage, out.ctypes.data_as(C.POINTER(C.c_float)), out.size),
               "debug_stage")
         return out if stage in (2, 3) else out[..., 0]
+
+
+class Server:
+    """The develop server (vkdt_cuda_server_*): continuous batching of develop
+    jobs of any size on one device, `slots` in flight, graphs pooled by shape
+    under a device memory cap."""
+
+    def __init__(self, slots=4, hbm_cap=0, llap_levels=0, cfg=DARKROOM_CFG):
+        self._l = _lib.lib()
+        self._s = C.c_void_p()
+        self._cfg = cfg.encode() if cfg is not None else None
+        c = _lib.ServerCfg(self._cfg, len(self._cfg) if self._cfg else 0, slots, hbm_cap, llap_levels)
+        check(self._l.vkdt_cuda_server_create(C.byref(c), C.byref(self._s)), "vkdt_cuda_server_create")
+        self._keep = {}
+
+    def submit(self, src, dst, wd, ht, img_param, out_wd=0, out_ht=0, src_on_device=True, dst_on_device=True):
+        """src/dst: device pointers (ints) or host numpy arrays; returns the job id."""
+        keep = []
+        if not isinstance(src, int):
+            keep.append(src)
+            src_on_device, src = False, src.ctypes.data
+        if not isinstance(dst, int):
+            keep.append(dst)
+            dst_on_device, dst = False, dst.ctypes.data
+        j = _lib.Job(wd, ht, img_param, out_wd, out_ht, src, dst, int(src_on_device), int(dst_on_device))
+        jid = C.c_uint64()
+        check(self._l.vkdt_cuda_server_submit(self._s, C.byref(j), C.byref(jid)), "server_submit")
+        if keep:
+            self._keep[jid.value] = keep
+        return jid.value
+
+    def wait(self, job, timeout_ms=600000):
+        try:
+            check(self._l.vkdt_cuda_server_wait(self._s, job, timeout_ms), "server_wait")
+        finally:
+            pass
+        self._keep.pop(job, None)
+
+    def drain(self, timeout_ms=600000):
+        check(self._l.vkdt_cuda_server_drain(self._s, timeout_ms), "server_drain")
+        self._keep.clear()
+
+    def job_times(self, job):
+        q, l = C.c_double(), C.c_double()
+        check(self._l.vkdt_cuda_server_job_times(self._s, job, C.byref(q), C.byref(l)), "server_job_times")
+        return q.value, l.value
+
+    def stats(self):
+        st = _lib.ServerStats()
+        check(self._l.vkdt_cuda_server_stats(self._s, C.byref(st)), "server_stats")
+        return {f: getattr(st, f) for f, _ in _lib.ServerStats._fields_}
+
+    def reset_stats(self):
+        check(self._l.vkdt_cuda_server_reset_stats(self._s), "server_reset_stats")
+
+    def close(self):
+        if self._s:
+            self._l.vkdt_cuda_server_destroy(self._s)
+            self._s = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

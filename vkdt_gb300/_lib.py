@@ -71,6 +71,22 @@ class Scene(C.Structure):
     ]
 
 
+class ServerCfg(C.Structure):
+    _fields_ = [("cfg", C.c_char_p), ("cfg_len", C.c_size_t), ("slots", C.c_int), ("hbm_cap", C.c_uint64),
+                ("llap_levels", C.c_int)]
+
+
+class Job(C.Structure):
+    _fields_ = [("wd", C.c_int), ("ht", C.c_int), ("ip", ImgParam), ("out_wd", C.c_int), ("out_ht", C.c_int),
+                ("src", C.c_void_p), ("dst", C.c_void_p), ("src_on_device", C.c_int), ("dst_on_device", C.c_int)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("completed", C.c_uint64), ("failed", C.c_uint64), ("mpix", C.c_double),
+                ("latency_p50_ms", C.c_double), ("latency_p99_ms", C.c_double),
+                ("peak_device_bytes", C.c_uint64), ("graphs", C.c_int)]
+
+
 # every symbol the header declares, with its ctypes signature
 _P = C.c_void_p
 _SIGS = {
@@ -98,6 +114,17 @@ _SIGS = {
     "vkdt_cuda_graph_wait": (C.c_int, [_P, C.c_uint32]),
     "vkdt_cuda_graph_develop": (C.c_int, [_P, _P, _P, _P]),
     "vkdt_cuda_graph_develop_static": (C.c_int, [_P, _P, _P, _P]),
+    "vkdt_cuda_graph_set_capture": (C.c_int, [_P, C.c_int]),
+    "vkdt_cuda_graph_stream": (_P, [_P]),
+    "vkdt_cuda_graph_plan_bytes": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
+    "vkdt_cuda_server_create": (C.c_int, [C.POINTER(ServerCfg), C.POINTER(_P)]),
+    "vkdt_cuda_server_submit": (C.c_int, [_P, C.POINTER(Job), C.POINTER(C.c_uint64)]),
+    "vkdt_cuda_server_wait": (C.c_int, [_P, C.c_uint64, C.c_uint32]),
+    "vkdt_cuda_server_drain": (C.c_int, [_P, C.c_uint32]),
+    "vkdt_cuda_server_job_times": (C.c_int, [_P, C.c_uint64, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "vkdt_cuda_server_stats": (C.c_int, [_P, C.POINTER(ServerStats)]),
+    "vkdt_cuda_server_reset_stats": (C.c_int, [_P]),
+    "vkdt_cuda_server_destroy": (None, [_P]),
     "vkdt_cuda_graph_set_timing": (C.c_int, [_P, C.c_int]),
     "vkdt_cuda_graph_query_times": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.c_int]),
     "vkdt_cuda_graph_set_hist": (C.c_int, [_P, C.c_int]),

@@ -3,6 +3,7 @@
 // device memory, the launch sequence, staging copies and the C-ABI of
 // include/vkdt_cuda.h.
 #include "vkdt_cuda.h"
+#include "internal.h"
 #include "kernels.h"
 #include "scene.h"
 
@@ -159,6 +160,8 @@ struct vkdt_cuda_graph_t
   int block = 2;                 // CFA block: 2 bayer, 3 x-trans
   bool halfsize = false, resample = false;  // demosaic/halfsize (+ shared/resample) for reduced sizes
   bool unfused = false;          // x-trans or reduced size: the per-node chain instead of the fused kernel
+  std::vector<int64_t> planned_for; // what alloc planned for: a run refuses a graph changed since
+  float lut_black = -1.0f, lut_white = -1.0f;  // black/white (DN) the noop code table holds
   size_t off_h0 = 0, off_b0 = 0, off_hl = 0, off_cov = 0, off_g = 0, off_hs = 0, off_dm = 0;
   size_t off_dnh = 0, off_dnl[4] = { 0, 0, 0, 0 }, off_dna = 0, off_dn = 0, off_idlut = 0;
   unsigned char *arena = nullptr;
@@ -278,6 +281,16 @@ void colour_commit(vkdt_cuda_graph_t *g, dev_image_t &d)
 
 size_t align_up(size_t v) { return (v + 255) & ~(size_t)255; }
 
+// everything the node plan and the arena depend on
+std::vector<int64_t> plan_key(vkdt_cuda_graph_t *g)
+{
+  const module_t *dn = g->mod("denoise");
+  const int wavelet = dn && dn->f("strength") > 0.0f;
+  const int fixup = g->mod("demosaic") ? g->mod("demosaic")->n("colour") : 0;
+  return { g->in_wd, g->in_ht, g->ip.crop_aabb[0], g->ip.crop_aabb[1], g->ip.crop_aabb[2], g->ip.crop_aabb[3],
+           g->ip.filters, g->req_wd, g->req_ht, g->llap_levels_req, wavelet, g->want_hist, g->debug, fixup };
+}
+
 int check_supported_params(vkdt_cuda_graph_t *g)
 {
   if(g->mod("demosaic")->n("colour") != 0) return fail(VKDT_CUDA_INCOMPLETE, "demosaic colour (fixup radius) != 0 not supported");
@@ -326,6 +339,53 @@ int fill_image(vkdt_cuda_graph_t *g, dev_image_t &d, const void *d_src, void *d_
   if(g->debug) { d.dbg_denoise = g->at<__half>(g->off_dbg0); d.dbg_hilite = g->at<__half>(g->off_dbg1); }
   (void)d_out;
   return 0;
+}
+
+// the arena plan: offsets of every device buffer of the graph; returns the bytes
+size_t plan_arena(vkdt_cuda_graph_t *g)
+{
+  size_t off = 0;
+  auto take = [&](size_t bytes) { const size_t o = off; off = align_up(off + bytes); return o; };
+  g->src_bytes = (size_t)g->in_wd * g->in_ht * 2;
+  g->sink_bytes = (size_t)g->out_w * g->out_h * 8;
+  g->off_src = take(g->src_bytes);
+  for(auto &l : g->hr) l.off = take((size_t)l.w * l.h * 8);
+  for(auto &l : g->hb) l.off = take((size_t)l.w * l.h * 8);
+  g->off_rgbf = take((size_t)g->out_w * g->out_h * 8);
+  for(auto &l : g->lp) l.off = take((size_t)l.w * l.h * 2 * 11);
+  for(auto &l : g->la) l.off = take((size_t)l.w * l.h * 2);
+  g->off_out = take(g->sink_bytes);
+  g->off_hist = take(257 * 4);
+  g->off_lut = take(65536 * 2);
+  if(g->debug) { g->off_dbg0 = take((size_t)g->W * g->H * 2); g->off_dbg1 = take((size_t)g->W * g->H * 2); }
+  const size_t hbytes = (size_t)g->hw * g->hh * 8;
+  if(g->wavelet)
+  { // the half size nodes of the wavelet denoise
+    g->off_dnh = take(hbytes);
+    for(int i = 0; i < 4; i++) g->off_dnl[i] = take(hbytes);
+    g->off_dna = take(hbytes);
+  }
+  // the (denoised) normalised mosaic: wavelet output, or the noop output of the per-node chain
+  if(g->wavelet || g->unfused) g->off_dn = take((size_t)g->W * g->H * 2);
+  if(g->wavelet && !g->unfused) g->off_idlut = take(65536 * 2);
+  if(g->unfused)
+  { // the per-node chain's images (intermediate f16 images like the reference's)
+    g->off_h0 = take(hbytes);
+    g->off_b0 = take(hbytes);
+    g->off_hl = take((size_t)g->W * g->H * 2);
+    if(g->halfsize)
+    {
+      g->off_hs = take(hbytes);
+      g->off_dm = g->resample ? take((size_t)g->out_w * g->out_h * 8) : g->off_hs;
+    }
+    else
+    {
+      g->off_cov = take(hbytes);
+      g->off_g = take((size_t)g->W * g->H * 2);
+      g->off_dm = take((size_t)g->W * g->H * 8);
+    }
+  }
+  return off;
 }
 
 // the push constants and uniforms of the wavelet denoise nodes (denoise/main.c:133-333)
@@ -407,6 +467,11 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
     li++;
     return 0;
   };
+  if(g->ip.black[0] != g->lut_black || g->ip.white[0] != g->lut_white)
+  { // new black/white since the code table was built: rebuild it on the device (same IEEE arithmetic)
+    CU(launch_noop_lut(g->at<__half>(g->off_lut), g->ip.black[0] / 65535.0f, g->ip.white[0] / 65535.0f, s));
+    g->lut_black = g->ip.black[0]; g->lut_white = g->ip.white[0];
+  }
   if(g->want_hist) CU(cudaMemsetAsync(g->at<uint32_t>(g->off_hist), 0, 257 * sizeof(uint32_t), s));
   if((r = mark())) return r;
   // 0. wavelet denoise (strength > 0): half, downcov, down x3, assemble, doub
@@ -519,6 +584,12 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
 }
 
 } // namespace
+
+// error text for the calling thread (also used by the develop server)
+int vkdt_set_error(int code, const char *msg)
+{
+  return fail(code, "%s", msg);
+}
 
 // ================================================================== C-ABI
 
@@ -943,49 +1014,7 @@ int vkdt_cuda_graph_alloc(vkdt_cuda_graph_t *g, uint64_t *device_bytes)
   release(g);
   int r = vkdt_cuda_graph_create_nodes(g);
   if(r) return r;
-  // memory plan (one arena)
-  size_t off = 0;
-  auto take = [&](size_t bytes) { const size_t o = off; off = align_up(off + bytes); return o; };
-  g->src_bytes = (size_t)g->in_wd * g->in_ht * 2;
-  g->sink_bytes = (size_t)g->out_w * g->out_h * 8;
-  g->off_src = take(g->src_bytes);
-  for(auto &l : g->hr) l.off = take((size_t)l.w * l.h * 8);
-  for(auto &l : g->hb) l.off = take((size_t)l.w * l.h * 8);
-  g->off_rgbf = take((size_t)g->out_w * g->out_h * 8);
-  for(auto &l : g->lp) l.off = take((size_t)l.w * l.h * 2 * 11);
-  for(auto &l : g->la) l.off = take((size_t)l.w * l.h * 2);
-  g->off_out = take(g->sink_bytes);
-  g->off_hist = take(257 * 4);
-  g->off_lut = take(65536 * 2);
-  if(g->debug) { g->off_dbg0 = take((size_t)g->W * g->H * 2); g->off_dbg1 = take((size_t)g->W * g->H * 2); }
-  const size_t hbytes = (size_t)g->hw * g->hh * 8;
-  if(g->wavelet)
-  { // the half size nodes of the wavelet denoise
-    g->off_dnh = take(hbytes);
-    for(int i = 0; i < 4; i++) g->off_dnl[i] = take(hbytes);
-    g->off_dna = take(hbytes);
-  }
-  // the (denoised) normalised mosaic: wavelet output, or the noop output of the per-node chain
-  if(g->wavelet || g->unfused) g->off_dn = take((size_t)g->W * g->H * 2);
-  if(g->wavelet && !g->unfused) g->off_idlut = take(65536 * 2);
-  if(g->unfused)
-  { // the per-node chain's images (intermediate f16 images like the reference's)
-    g->off_h0 = take(hbytes);
-    g->off_b0 = take(hbytes);
-    g->off_hl = take((size_t)g->W * g->H * 2);
-    if(g->halfsize)
-    {
-      g->off_hs = take(hbytes);
-      g->off_dm = g->resample ? take((size_t)g->out_w * g->out_h * 8) : g->off_hs;
-    }
-    else
-    {
-      g->off_cov = take(hbytes);
-      g->off_g = take((size_t)g->W * g->H * 2);
-      g->off_dm = take((size_t)g->W * g->H * 8);
-    }
-  }
-  g->arena_bytes = off;
+  g->arena_bytes = plan_arena(g);
   CU(cudaMalloc((void **)&g->arena, g->arena_bytes));
   CU(cudaMemset(g->arena, 0, g->arena_bytes));
   if(g->wavelet && !g->unfused)
@@ -1003,9 +1032,8 @@ int vkdt_cuda_graph_alloc(vkdt_cuda_graph_t *g, uint64_t *device_bytes)
       lut[v] = __float2half_rn(std::fmax(0.0f, (x - black) / (white - black)));
     }
     CU(cudaMemcpy(g->arena + g->off_lut, lut.data(), 65536 * 2, cudaMemcpyHostToDevice));
+    g->lut_black = g->ip.black[0]; g->lut_white = g->ip.white[0];
   }
-  CU(cudaMallocHost(&g->h_src, g->src_bytes));
-  CU(cudaMallocHost(&g->h_sink, g->sink_bytes));
   CU(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
   CU(cudaEventCreateWithFlags(&g->done, cudaEventDisableTiming));
   g->ev.resize(g->launches.size() + 1);
@@ -1013,9 +1041,21 @@ int vkdt_cuda_graph_alloc(vkdt_cuda_graph_t *g, uint64_t *device_bytes)
   g->times.assign(g->launches.size(), 0.0f);
   g->allocated = true;
   g->graph_dirty = true;
+  g->planned_for = plan_key(g);
   if(device_bytes) *device_bytes = g->arena_bytes;
   return VKDT_CUDA_SUCCESS;
 }
+
+int vkdt_cuda_graph_plan_bytes(vkdt_cuda_graph_t *g, uint64_t *device_bytes)
+{
+  if(!g || !device_bytes) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "null argument");
+  if(g->allocated) { *device_bytes = g->arena_bytes; return 0; }
+  int r = vkdt_cuda_graph_create_nodes(g);
+  if(r) return r;
+  *device_bytes = plan_arena(g);
+  return 0;
+}
+
 
 int vkdt_cuda_graph_node_count(vkdt_cuda_graph_t *g) { return g ? (int)g->nodes.size() : 0; }
 int vkdt_cuda_graph_node(vkdt_cuda_graph_t *g, int i, vkdt_cuda_node_info_t *info)
@@ -1032,17 +1072,24 @@ int vkdt_cuda_graph_output_size(vkdt_cuda_graph_t *g, int *wd, int *ht)
   return 0;
 }
 
+// the pinned staging buffers are made on first use: graphs that only develop
+// device buffers (vkdt_cuda_graph_develop, the server) never hold them
+static void *staging(void **p, size_t bytes)
+{
+  if(!*p && cudaMallocHost(p, bytes) != cudaSuccess) { *p = nullptr; fail(VKDT_CUDA_ERROR_OUT_OF_HOST_MEMORY, "pinned staging of %zu bytes", bytes); }
+  return *p;
+}
 void *vkdt_cuda_graph_map_source(vkdt_cuda_graph_t *g, size_t *bytes)
 {
   if(!g || !g->allocated) return nullptr;
   if(bytes) *bytes = g->src_bytes;
-  return g->h_src;
+  return staging(&g->h_src, g->src_bytes);
 }
 void *vkdt_cuda_graph_map_sink(vkdt_cuda_graph_t *g, size_t *bytes)
 {
   if(!g || !g->allocated) return nullptr;
   if(bytes) *bytes = g->sink_bytes;
-  return g->h_sink;
+  return staging(&g->h_sink, g->sink_bytes);
 }
 int vkdt_cuda_graph_device_buffers(vkdt_cuda_graph_t *g, void **d_source, void **d_sink)
 {
@@ -1054,6 +1101,8 @@ int vkdt_cuda_graph_device_buffers(vkdt_cuda_graph_t *g, void **d_source, void *
 
 static int run_kernels(vkdt_cuda_graph_t *g, cudaStream_t s, const void *src, void *dst)
 {
+  if(plan_key(g) != g->planned_for)
+    return fail(VKDT_CUDA_INCOMPLETE, "sizes or node-changing parameters differ from the last vkdt_cuda_graph_alloc: allocate again");
   const bool own_buffers = src == g->arena + g->off_src && dst == g->arena + g->off_out;
   if(g->timing || !g->use_graph || !own_buffers) return enqueue(g, s, src, dst, g->timing);
   if(g->graph_dirty || !g->gexec)
@@ -1080,6 +1129,8 @@ int vkdt_cuda_graph_run(vkdt_cuda_graph_t *g, void *stream, uint32_t flags)
 {
   if(!g || !g->allocated) return fail(VKDT_CUDA_INCOMPLETE, "graph not allocated");
   cudaStream_t s = stream ? (cudaStream_t)stream : g->stream;
+  if((flags & VKDT_CUDA_RUN_UPLOAD_SOURCE) && !staging(&g->h_src, g->src_bytes)) return VKDT_CUDA_ERROR_OUT_OF_HOST_MEMORY;
+  if((flags & VKDT_CUDA_RUN_DOWNLOAD_SINK) && !staging(&g->h_sink, g->sink_bytes)) return VKDT_CUDA_ERROR_OUT_OF_HOST_MEMORY;
   if(flags & VKDT_CUDA_RUN_UPLOAD_SOURCE)
     CU(cudaMemcpyAsync(g->arena + g->off_src, g->h_src, g->src_bytes, cudaMemcpyHostToDevice, s));
   if(g->timing) CU(cudaEventRecord(g->ev[0], s));
@@ -1090,6 +1141,18 @@ int vkdt_cuda_graph_run(vkdt_cuda_graph_t *g, void *stream, uint32_t flags)
   CU(cudaEventRecord(g->done, s));
   if(flags & VKDT_CUDA_RUN_WAIT_DONE) return vkdt_cuda_graph_wait(g, 600000);
   return 0;
+}
+
+int vkdt_cuda_graph_set_capture(vkdt_cuda_graph_t *g, int enable)
+{
+  if(!g) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "null graph");
+  g->use_graph = enable != 0;
+  return 0;
+}
+
+void *vkdt_cuda_graph_stream(vkdt_cuda_graph_t *g)
+{
+  return g ? (void *)g->stream : nullptr;
 }
 
 int vkdt_cuda_graph_develop(vkdt_cuda_graph_t *g, const void *d_mosaic, void *d_rgba, void *stream)

@@ -17,12 +17,13 @@ DEV void colour_px(const dev_image_t &p, const float in[3], float o[3])
 }
 
 // filmcurv/main.comp:106-205, colour modes 1 and 3 (adjust_colour_dng,
-// shared.glsl:371-387). pow as GPUs evaluate GLSL pow: exp2(k log2 x)
+// shared.glsl:371-387). pow as GPUs evaluate GLSL pow: exp2(k log2 x), on the
+// special function unit (the result is stored as f16)
 DEV void filmcurv_px(const dev_image_t &p, const float in[3], float o[3])
 {
   float c0[3], c1[3];
   for(int k = 0; k < 3; k++) c0[k] = in[k] + p.fc_bias;
-  for(int k = 0; k < 3; k++) c1[k] = 1.0f - curve_exp(-gpow_pos(fmaxf(c0[k], 1e-7f) * p.fc_il, p.fc_k));
+  for(int k = 0; k < 3; k++) c1[k] = 1.0f - curve_exp(-__powf(fmaxf(c0[k], 1e-7f) * p.fc_il, p.fc_k));
   if(p.fc_mode == 3)
   {
     bool fx = false, fy = false, fz = false;

@@ -98,9 +98,12 @@ template<class F> DEV void hilite_reduce_px(F fetch, float white_p, float desat,
 
 // hilite/assemble.comp:23-81 gauss_expand. fetch(ix, iy, rgb) reads the
 // coarse texel (ix, iy) (caller applies the mirrored repeat)
+DEV float binom5(int k)
+{ // (1 4 6 4 1) / 16 at k = 0..4, without an indexed table (kept in registers)
+  return k == 2 ? 6.0f / 16.0f : ((k == 1 || k == 3) ? 4.0f / 16.0f : 1.0f / 16.0f);
+}
 template<class F> DEV void hilite_expand_px(F fetch, int ox, int oy, float c[3])
 {
-  const float w[5] = { 1.0f / 16.0f, 4.0f / 16.0f, 6.0f / 16.0f, 4.0f / 16.0f, 1.0f / 16.0f };
   c[0] = c[1] = c[2] = 0.0f;
   float wgt = 0.0f;
   const int ix = ox / 2, iy = oy / 2;
@@ -108,8 +111,8 @@ template<class F> DEV void hilite_expand_px(F fetch, int ox, int oy, float c[3])
   const int i0 = dx ? 0 : -1, j0 = dy ? 0 : -1;
   for(int ii = i0; ii <= 1; ii++) for(int jj = j0; jj <= 1; jj++)
   {
-    const float wy = dy ? w[2 * jj + 1] : w[2 * jj + 2];
-    const float wx = dx ? w[2 * ii + 1] : w[2 * ii + 2];
+    const float wy = dy ? binom5(2 * jj + 1) : binom5(2 * jj + 2);
+    const float wx = dx ? binom5(2 * ii + 1) : binom5(2 * ii + 2);
     float rgb[3];
     fetch(ix + ii, iy + jj, rgb);
     for(int k = 0; k < 3; k++) c[k] += rgb[k] * wy * wx;

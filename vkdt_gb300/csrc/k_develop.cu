@@ -71,6 +71,53 @@ DEV float tap_weight(float wh, float wv, float wd, int i, int j)
   return (i == 0 && j == 0) ? 1.0f : (i == 0 ? wv : (j == 0 ? wh : wd));
 }
 
+// demosaic/splat.comp:224-266 taps of one output pixel whose CFA phase is (PX, PY):
+// only the greens enter rgb.ggg; taps past the border wrap by the CFA period 6
+template<int PX, int PY> DEV void splat_taps(const smem_t &s, int qx, int qy, int W, int H, int X0, int Y0,
+    float wh, float wv, float wd, float &rg, float &wg)
+{
+#pragma unroll
+  for(int j = -1; j <= 1; j++)
+#pragma unroll
+  for(int ii = -1; ii <= 1; ii++)
+  {
+    if(cfa_bayer(PX + ii, PY + j) != 1) continue;
+    int px = qx + ii, py = qy + j;
+    if(px < 0) px += 6;
+    if(py < 0) py += 6;
+    if(px >= W) px -= 6;
+    if(py >= H) py -= 6;
+    const int mx = px - (X0 - 4), my = py - (Y0 - 4);
+    const float col = s.M[my][mx & 1][mx >> 1];
+    const float weight = (ii == 0 && j == 0) ? 666.0f : tap_weight(wh, wv, wd, ii, j);
+    rg += col * weight;
+    wg += weight;
+  }
+}
+
+// demosaic/fix.comp:99-135 taps of one output pixel whose CFA phase is (PX, PY)
+template<int PX, int PY> DEV void fix_taps(const smem_t &s, int px, int py, int gx0, int gy0, int X0, int Y0,
+    float gc, float wh, float wv, float wd, float &rr, float &rb, float &wr, float &wb, float &rg, float &wg)
+{
+#pragma unroll
+  for(int j = -1; j <= 1; j++)
+#pragma unroll
+  for(int ii = -1; ii <= 1; ii++)
+  {
+    const int c = cfa_bayer(PX + ii, PY + j);
+    if(c == 1) { rg = gc; wg = 1.0f; continue; }
+    const int gx = gx0 + ii, gy = gy0 + j;
+    const float rgh = s.rg[gy][gx & 1][gx >> 1];
+    const int mx = px + ii - (X0 - 4), my = py + j - (Y0 - 4);
+    const float col = s.M[my][mx & 1][mx >> 1];
+    const float weight = tap_weight(wh, wv, wd, ii, j);
+    // col * (1e-4 + gc) / (1e-4 + gh) * weight with the reciprocal of the splat stage
+    const float v = col * (1e-4f + gc) * rgh * weight;
+    if(c == 0) { rr += v; wr += weight; }
+    else       { rb += v; wb += weight; }
+  }
+}
+
 __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -114,17 +161,24 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
       m[1] = h2f(__ldg(p.noop_lut + (r0 >> 16)));
       m[2] = h2f(__ldg(p.noop_lut + (r1 & 0xffff)));
       m[3] = h2f(__ldg(p.noop_lut + (r1 >> 16)));
-      float h[4];
-      hilite_half_bayer(m[0], m[1], m[2], m[3], p.hl_white, h);
-      h[3] = 1.0f;
-      float up[3];
-      hilite_expand_px([&](int ix, int iy, float rgb[3]) {
-          const int sx = ix - bx0, sy = iy - by0;
-          rgb[0] = s.B1[0][sy][sx]; rgb[1] = s.B1[1][sy][sx]; rgb[2] = s.B1[2][sy][sx];
-        }, rbx, rby, up);
-      float b0[3], o[4];
-      hilite_assemble_px(h, up, p.hl_white, p.hl_soft, b0);
-      hilite_doub_bayer(m[0], m[1], m[2], m[3], b0, p.hl_white, o);
+      float o[4] = { m[0], m[1], m[2], m[3] };
+      // hilite/doub changes a block only where its largest sample exceeds
+      // 0.97 white, and the level 0 assemble feeds nothing else: elsewhere
+      // the block is the noop output as it is (f16 values already)
+      if(fmaxf(fmaxf(m[2], m[3]), fmaxf(m[1], m[0])) > 0.97f * p.hl_white)
+      {
+        float h[4];
+        hilite_half_bayer(m[0], m[1], m[2], m[3], p.hl_white, h);
+        h[3] = 1.0f;
+        float up[3];
+        hilite_expand_px([&](int ix, int iy, float rgb[3]) {
+            const int sx = ix - bx0, sy = iy - by0;
+            rgb[0] = s.B1[0][sy][sx]; rgb[1] = s.B1[1][sy][sx]; rgb[2] = s.B1[2][sy][sx];
+          }, rbx, rby, up);
+        float b0[3];
+        hilite_assemble_px(h, up, p.hl_white, p.hl_soft, b0);
+        hilite_doub_bayer(m[0], m[1], m[2], m[3], b0, p.hl_white, o);
+      }
       // flipped blocks (mirrored at the image border) swap their rows / columns
       const float t0 = fy ? o[2] : o[0], t1 = fy ? o[3] : o[1], t2 = fy ? o[0] : o[2], t3 = fy ? o[1] : o[3];
       s.M[2 * sby][fx ? 1 : 0][sbx] = t0;
@@ -132,7 +186,10 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
       s.M[2 * sby + 1][fx ? 1 : 0][sbx] = t2;
       s.M[2 * sby + 1][fx ? 0 : 1][sbx] = t3;
       if(p.dbg_denoise && !fx && !fy && 2 * rbx >= OX && 2 * rbx < OXe && 2 * rby >= OY && 2 * rby < OYe)
-        for(int dy = 0; dy < 2; dy++) for(int dx = 0; dx < 2; dx++)
+#pragma unroll
+        for(int dy = 0; dy < 2; dy++)
+#pragma unroll
+        for(int dx = 0; dx < 2; dx++)
         {
           const size_t idx = (size_t)(2 * rby + dy) * W + 2 * rbx + dx;
           p.dbg_denoise[idx] = f2h(m[dy * 2 + dx]);
@@ -162,7 +219,7 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
         if(((j + ii) & 1) != 1) continue;
         const int xs = 2 * scx + 2 + ii;
         px[k] = s.M[2 * scy + 2 + j][xs & 1][xs >> 1];
-        inv[k] = __fdiv_rn(1.0f, px[k]);
+        inv[k] = __frcp_rn(px[k]);
         k++;
       }
       // i/px for i in {-1,0,1,2} is i*(1/px) exactly (scaling by +-1, 2 is exact)
@@ -201,7 +258,7 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
         Sw11 = __fadd_rn(Sw11, __fmul_rn(__fmul_rn(p2, q1), q1));
         sw = __fadd_rn(sw, p2);
         q0 = __fsub_rn((float)ii, mb0); q1 = __fsub_rn((float)j, mb1);
-        p2 = __fdiv_rn(1.0f, p2);
+        p2 = __frcp_rn(p2);
         Sb00 = __fadd_rn(Sb00, __fmul_rn(__fmul_rn(p2, q0), q0));
         Sb01 = __fadd_rn(Sb01, __fmul_rn(__fmul_rn(p2, q0), q1));
         Sb10 = __fadd_rn(Sb10, __fmul_rn(__fmul_rn(p2, q1), q0));
@@ -227,7 +284,7 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
     // a diagonal one 1/e0 + 1/e1, and every tap 0 without covariance
     const int ori = v[2] == 1.0f ? 0 : (v[3] == 1.0f ? 1 : 2);
     {
-      const float r0 = __fdiv_rn(1.0f, gclamp(v[0], 0.01f, 25.0f)), r1 = __fdiv_rn(1.0f, gclamp(v[1], 0.01f, 25.0f));
+      const float r0 = __frcp_rn(gclamp(v[0], 0.01f, 25.0f)), r1 = __frcp_rn(gclamp(v[1], 0.01f, 25.0f));
       const float wa = gclamp(expf(-0.5f * r0), 1e-4f, 1.0f);
       const float wb = gclamp(expf(-0.5f * r1), 1e-4f, 1.0f);
       const float wc = gclamp(expf(-0.5f * __fadd_rn(r0, r1)), 1e-4f, 1.0f);
@@ -236,7 +293,7 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
       s.sw[2][scy][scx] = ori == 2 ? 1.0f : wc;
     }
     {
-      const float r0 = __fdiv_rn(1.0f, 2.0f * gclamp(v[0], 1.0f, 49.0f)), r1 = __fdiv_rn(1.0f, 2.0f * gclamp(v[1], 1.0f, 49.0f));
+      const float r0 = __frcp_rn(2.0f * gclamp(v[0], 1.0f, 49.0f)), r1 = __frcp_rn(2.0f * gclamp(v[1], 1.0f, 49.0f));
       const float wa = gclamp(expf(-0.5f * r0), 1e-3f, 1.0f);
       const float wb = gclamp(expf(-0.5f * r1), 1e-3f, 1.0f);
       const float wc = gclamp(expf(-0.5f * __fadd_rn(r0, r1)), 1e-3f, 1.0f);
@@ -259,22 +316,12 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
       const int ccx = (qx + 1) / 2 - (X0 / 2 - 1), ccy = (qy + 1) / 2 - (Y0 / 2 - 1);
       const float wh = s.sw[0][ccy][ccx], wv = s.sw[1][ccy][ccx], wd = s.sw[2][ccy][ccx];
       float rg = 0.0f, wg = 0.0f;
-#pragma unroll
-      for(int j = -1; j <= 1; j++)
-#pragma unroll
-      for(int ii = -1; ii <= 1; ii++)
-      {
-        if(cfa_bayer(qx + ii, qy + j) != 1) continue; // only green enters rgb.ggg
-        int px = qx + ii, py = qy + j;
-        if(px < 0) px += 6;
-        if(py < 0) py += 6;
-        if(px >= W) px -= 6;
-        if(py >= H) py -= 6;
-        const int mx = px - (X0 - 4), my = py - (Y0 - 4);
-        const float col = s.M[my][mx & 1][mx >> 1];
-        const float weight = (ii == 0 && j == 0) ? 666.0f : tap_weight(wh, wv, wd, ii, j);
-        rg += col * weight;
-        wg += weight;
+      switch((qx & 1) | ((qy & 1) << 1))
+      { // the CFA phase of the real pixel: uniform in a warp but at mirrored borders
+        case 0: splat_taps<0, 0>(s, qx, qy, W, H, X0, Y0, wh, wv, wd, rg, wg); break;
+        case 1: splat_taps<1, 0>(s, qx, qy, W, H, X0, Y0, wh, wv, wd, rg, wg); break;
+        case 2: splat_taps<0, 1>(s, qx, qy, W, H, X0, Y0, wh, wv, wd, rg, wg); break;
+        default: splat_taps<1, 1>(s, qx, qy, W, H, X0, Y0, wh, wv, wd, rg, wg); break;
       }
       const float gv = f16r(rg / fmaxf(1e-8f, wg));
       s.g[sgy][sgx & 1][sgx >> 1] = gv;
@@ -302,22 +349,12 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
       float rr = 0.0f, rb = 0.0f, wr = 0.0f, wb = 0.0f, rg = 0.0f, wg = 0.0f;
       // demosaic/fix.comp:99-135, radius clamp(fixup+1, 1, 2) = 1 for the
       // default fixup 0 (the host rejects other values for this kernel)
-#pragma unroll
-      for(int j = -1; j <= 1; j++)
-#pragma unroll
-      for(int ii = -1; ii <= 1; ii++)
+      switch((px & 1) | ((py & 1) << 1))
       {
-        const int c = cfa_bayer(px + ii, py + j);
-        if(c == 1) { rg = gc; wg = 1.0f; continue; }
-        const int gx = gx0 + ii, gy = gy0 + j;
-        const float rgh = s.rg[gy][gx & 1][gx >> 1];
-        const int mx = px + ii - (X0 - 4), my = py + j - (Y0 - 4);
-        const float col = s.M[my][mx & 1][mx >> 1];
-        const float weight = tap_weight(wh, wv, wd, ii, j);
-        // col * (1e-4 + gc) / (1e-4 + gh) * weight with the reciprocal of the splat stage
-        const float v = col * (1e-4f + gc) * rgh * weight;
-        if(c == 0) { rr += v; wr += weight; }
-        else       { rb += v; wb += weight; }
+        case 0: fix_taps<0, 0>(s, px, py, gx0, gy0, X0, Y0, gc, wh, wv, wd, rr, rb, wr, wb, rg, wg); break;
+        case 1: fix_taps<1, 0>(s, px, py, gx0, gy0, X0, Y0, gc, wh, wv, wd, rr, rb, wr, wb, rg, wg); break;
+        case 2: fix_taps<0, 1>(s, px, py, gx0, gy0, X0, Y0, gc, wh, wv, wd, rr, rb, wr, wb, rg, wg); break;
+        default: fix_taps<1, 1>(s, px, py, gx0, gy0, X0, Y0, gc, wh, wv, wd, rr, rb, wr, wb, rg, wg); break;
       }
       float dm[3];
       dm[0] = f16r(rr / fmaxf(1e-8f, wr));

@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(256) k_nd_gauss_xt(const dev_nodes_t p)
     mw0 = __fadd_rn(mw0, __fmul_rn(fi, px[k])); mw1 = __fadd_rn(mw1, __fmul_rn(fj, px[k]));
     smw = __fadd_rn(smw, px[k]);
     mb0 = __fadd_rn(mb0, __fdiv_rn(fi, px[k])); mb1 = __fadd_rn(mb1, __fdiv_rn(fj, px[k]));
-    smb = __fadd_rn(smb, __fdiv_rn(1.0f, px[k]));
+    smb = __fadd_rn(smb, __frcp_rn(px[k]));
   }
   mw0 = __fdiv_rn(mw0, smw); mw1 = __fdiv_rn(mw1, smw);
   mb0 = __fdiv_rn(mb0, smb); mb1 = __fdiv_rn(mb1, smb);
@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(256) k_nd_gauss_xt(const dev_nodes_t p)
     Sw11 = __fadd_rn(Sw11, __fmul_rn(__fmul_rn(p2, q1), q1));
     sw = __fadd_rn(sw, p2);
     q0 = __fsub_rn((float)gi[k], mb0); q1 = __fsub_rn((float)gj[k], mb1);
-    p2 = __fdiv_rn(1.0f, p2);
+    p2 = __frcp_rn(p2);
     Sb00 = __fadd_rn(Sb00, __fmul_rn(__fmul_rn(p2, q0), q0));
     Sb01 = __fadd_rn(Sb01, __fmul_rn(__fmul_rn(p2, q0), q1));
     Sb10 = __fadd_rn(Sb10, __fmul_rn(__fmul_rn(p2, q1), q0));

@@ -62,7 +62,11 @@ template<class F> DEV void hilite_reduce_px(F fetch, float white_p, float desat,
   float wb[3] = { wbp[0], wbp[1], wbp[2] };
   if(!(wb[0] * wb[0] + wb[1] * wb[1] + wb[2] * wb[2] > 1e-3f)) wb[0] = wb[1] = wb[2] = 1.0f;
   float e0 = 0.0f, e1 = 0.0f, col[3] = { 0.0f, 0.0f, 0.0f }, wgt = 0.0f;
-  const float ds = desat * desat;
+  const float ds = desat * desat, d5 = 5.0f * ds * ds;
+  // the divisions by loop invariants as products (continuous values only:
+  // the clip test below compares the texels themselves)
+  const float iwhite = 1.0f / white;
+  const float hwb[3] = { 0.5f / wb[0], 0.5f / wb[1], 0.5f / wb[2] };
 #pragma unroll
   for(int jj = -2; jj <= 2; jj++)
 #pragma unroll
@@ -74,18 +78,22 @@ template<class F> DEV void hilite_reduce_px(F fetch, float white_p, float desat,
     e0 += w[jj + 2] * sw[ii + 2] * l;
     e1 += w[ii + 2] * sw[jj + 2] * l;
     const float u = w[ii + 2] * w[jj + 2];
-    const float rw = rgb[0] * wb[0], gw = rgb[1] * wb[1], bw = rgb[2] * wb[2];
-    const float cmax = fmaxf(rw, fmaxf(gw, bw));
-    const float cmin = fminf(rw, fminf(gw, bw));
-    const float sat = (cmax - cmin) / fmaxf(1e-3f, cmax);
     if(rgb[0] < white && rgb[1] < white && rgb[2] < white)
     {
-      const float s = smoothstep(0.2f, 1.0f, fmaxf(rgb[0], fmaxf(rgb[1], rgb[2])) / white);
-      float t = smoothstep(0.15f, 0.9f, sat);
-      t = gclamp(5.0f * ds * ds * s * t, 0.0f, 1.0f);
+      const float rw = rgb[0] * wb[0], gw = rgb[1] * wb[1], bw = rgb[2] * wb[2];
+      const float cmax = fmaxf(rw, fmaxf(gw, bw));
+      const float cmin = fminf(rw, fminf(gw, bw));
+      const float sat = __fdividef(cmax - cmin, fmaxf(1e-3f, cmax));
+      // smoothstep(0.2, 1, max / white) and smoothstep(0.15, 0.9, sat)
+      float s = gclamp((fmaxf(rgb[0], fmaxf(rgb[1], rgb[2])) * iwhite - 0.2f) * 1.25f, 0.0f, 1.0f);
+      s = s * s * (3.0f - 2.0f * s);
+      float t = gclamp((sat - 0.15f) * (1.0f / 0.75f), 0.0f, 1.0f);
+      t = t * t * (3.0f - 2.0f * t);
+      t = gclamp(d5 * s * t, 0.0f, 1.0f);
+#pragma unroll
       for(int k = 0; k < 3; k++)
       {
-        const float v = gmix(rgb[k], (cmax + cmin) / wb[k] * 0.5f, t);
+        const float v = gmix(rgb[k], (cmax + cmin) * hwb[k], t);
         col[k] += v * u;
       }
       wgt += u;

@@ -11,6 +11,13 @@ constexpr int K1_N = 2 * K1_T + 3;    // h0 slots per side (5 tap support)
 
 // denoise/noop.comp + hilite/half.comp + hilite/reduce.comp for one r1 tile.
 // h0 (the half size image) lives only in shared memory.
+DEV int mirror1c(int i, int n)
+{ // mirrored repeat for |overshoot| < n, clamped beyond
+  if(i < 0) i = -1 - i;
+  if(i >= n) i = 2 * n - 1 - i;
+  return min(max(i, 0), n - 1);
+}
+
 __global__ void __launch_bounds__(256) k_hilite_k1(const dev_hilite_k1_t p)
 {
   __shared__ float sh[3][K1_N][K1_N + 1];
@@ -19,7 +26,9 @@ __global__ void __launch_bounds__(256) k_hilite_k1(const dev_hilite_k1_t p)
   for(int i = threadIdx.x; i < K1_N * K1_N; i += blockDim.x)
   {
     const int sx = i % K1_N, sy = i / K1_N;
-    const int hx = mirror_full(bx0 + sx, p.hw), hy = mirror_full(by0 + sy, p.hh);
+    // outputs read h0 within 2 of the image: mirror1 is exact there; the
+    // clamp keeps the slots past it (images narrower than a tile) in bounds
+    const int hx = mirror1c(bx0 + sx, p.hw), hy = mirror1c(by0 + sy, p.hh);
     float h[3];
     const size_t row = (size_t)(2 * hy + p.cy) * p.pitch + 2 * hx + p.cx;
     const uint32_t r0 = __ldg(reinterpret_cast<const uint32_t *>(p.mosaic + row));
@@ -50,8 +59,11 @@ __global__ void __launch_bounds__(256) k_hilite_reduce(const half4 *__restrict__
   const int x = blockIdx.x * 16 + threadIdx.x % 16, y = blockIdx.y * 16 + threadIdx.x / 16;
   if(x >= ow || y >= oh) return;
   float o[4];
+  // taps overshoot the level by at most 2: the cheap mirror is exact unless it is tiny
+  const bool tiny = iw < 3 || ih < 3;
   hilite_reduce_px([&](int ii, int jj, float rgb[3]) {
-      const int sx = mirror_full(2 * x + ii, iw), sy = mirror_full(2 * y + jj, ih);
+      const int sx = tiny ? mirror_full(2 * x + ii, iw) : mirror1c(2 * x + ii, iw);
+      const int sy = tiny ? mirror_full(2 * y + jj, ih) : mirror1c(2 * y + jj, ih);
       float w;
       ld_half4(in + (size_t)sy * iw + sx, rgb[0], rgb[1], rgb[2], w);
     }, a.white, a.desat, a.wb, o);
@@ -65,8 +77,9 @@ __global__ void __launch_bounds__(256) k_hilite_assemble(const half4 *__restrict
   const int x = blockIdx.x * 16 + threadIdx.x % 16, y = blockIdx.y * 16 + threadIdx.x / 16;
   if(x >= fw || y >= fh) return;
   float up[3];
+  const bool tiny = cw < 2 || ch < 2;     // expand taps overshoot the coarse level by at most 1
   hilite_expand_px([&](int ix, int iy, float rgb[3]) {
-      const int sx = mirror_full(ix, cw), sy = mirror_full(iy, ch);
+      const int sx = tiny ? mirror_full(ix, cw) : mirror1c(ix, cw), sy = tiny ? mirror_full(iy, ch) : mirror1c(iy, ch);
       float w;
       ld_half4(coarse + (size_t)sy * cw + sx, rgb[0], rgb[1], rgb[2], w);
     }, x, y, up);

@@ -94,14 +94,14 @@ __global__ void __launch_bounds__(256) k_llap_reduce(const __half *__restrict__ 
 // one output tile: slot (sx, sy) holds the mirrored texel (bx+sx, by+sy)
 DEV void stage_coarse(float (*sl)[FS][FS + 1], const __half *l1, int w1, int h1, size_t p1,
     const __half *coarse, int bx, int by)
-{
-  for(int i = threadIdx.x; i < (NPL + 1) * FS * FS; i += blockDim.x)
+{ // the mirrored position once per slot, then the same texel of every plane
+  for(int r = threadIdx.x; r < FS * FS; r += blockDim.x)
   {
-    const int k = i / (FS * FS), r = i % (FS * FS);
     const int sx = r % FS, sy = r / FS;
-    const int gx = mirror1(bx + sx, w1), gy = mirror1(by + sy, h1);
-    const __half *pl = k < NPL ? l1 + k * p1 : coarse;
-    sl[k][sy][sx] = h2f(pl[(size_t)gy * w1 + gx]);
+    const size_t o = (size_t)mirror1(by + sy, h1) * w1 + mirror1(bx + sx, w1);
+#pragma unroll
+    for(int k = 0; k < NPL; k++) sl[k][sy][sx] = h2f(__ldg(l1 + k * p1 + o));
+    sl[NPL][sy][sx] = h2f(__ldg(coarse + o));
   }
 }
 

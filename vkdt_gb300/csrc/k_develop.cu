@@ -49,12 +49,18 @@ constexpr int NPL = 11;              // NUM_GAMMA curves + grey (llap/config.h:2
 struct smem_t
 {
   float M[MX][2][MB];          // hilite output mosaic, [y][x&1][x>>1]
-  float sw[3][CX][CX];         // splat weights of the taps (+-1,0), (0,+-1), (+-1,+-1)
-  float fw[3][CX][CX];         // fix weights, same
-  float g[GX][2][GH];          // splat output, [y][x&1][x>>1]
+  float fw[3][CX][CX];         // fix weights of the taps (+-1,0), (0,+-1), (+-1,+-1)
+  __half g[GX][2][GH];         // splat output (f16 values), [y][x&1][x>>1]
   float rg[GX][2][GH];         // 1 / (1e-4 + splat output)
-  __half L0[NPL][LX][2][LH];   // llap level 0 planes, [y][slot&1][slot>>1]
-  float B1[3][BX][BX];         // hilite coarse level (rgb) around the tile
+  union
+  { // the llap level 0 planes are written after the last reads of the others
+    struct
+    {
+      float sw[3][CX][CX];     // splat weights, same taps as fw
+      float B1[3][BX][BX];     // hilite coarse level (rgb) around the tile
+    } e;
+    __half L0[NPL][LX][2][LH]; // llap level 0 planes, [y][slot&1][slot>>1]
+  } u;
   uint32_t hist[257];
 };
 
@@ -139,7 +145,7 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
     const int gx = mirror1(bx0 + sx, p.hcw), gy = mirror1(by0 + sy, p.hch);
     float a, b, c, d;
     ld_half4(p.hl_coarse + (size_t)gy * p.hcw + gx, a, b, c, d);
-    s.B1[0][sy][sx] = a; s.B1[1][sy][sx] = b; s.B1[2][sy][sx] = c;
+    s.u.e.B1[0][sy][sx] = a; s.u.e.B1[1][sy][sx] = b; s.u.e.B1[2][sy][sx] = c;
   }
   __syncthreads();
 
@@ -173,7 +179,7 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
         float up[3];
         hilite_expand_px([&](int ix, int iy, float rgb[3]) {
             const int sx = ix - bx0, sy = iy - by0;
-            rgb[0] = s.B1[0][sy][sx]; rgb[1] = s.B1[1][sy][sx]; rgb[2] = s.B1[2][sy][sx];
+            rgb[0] = s.u.e.B1[0][sy][sx]; rgb[1] = s.u.e.B1[1][sy][sx]; rgb[2] = s.u.e.B1[2][sy][sx];
           }, rbx, rby, up);
         float b0[3];
         hilite_assemble_px(h, up, p.hl_white, p.hl_soft, b0);
@@ -288,9 +294,9 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
       const float wa = gclamp(expf(-0.5f * r0), 1e-4f, 1.0f);
       const float wb = gclamp(expf(-0.5f * r1), 1e-4f, 1.0f);
       const float wc = gclamp(expf(-0.5f * __fadd_rn(r0, r1)), 1e-4f, 1.0f);
-      s.sw[0][scy][scx] = ori == 0 ? wa : (ori == 1 ? wb : 1.0f);
-      s.sw[1][scy][scx] = ori == 0 ? wb : (ori == 1 ? wa : 1.0f);
-      s.sw[2][scy][scx] = ori == 2 ? 1.0f : wc;
+      s.u.e.sw[0][scy][scx] = ori == 0 ? wa : (ori == 1 ? wb : 1.0f);
+      s.u.e.sw[1][scy][scx] = ori == 0 ? wb : (ori == 1 ? wa : 1.0f);
+      s.u.e.sw[2][scy][scx] = ori == 2 ? 1.0f : wc;
     }
     {
       const float r0 = __frcp_rn(2.0f * gclamp(v[0], 1.0f, 49.0f)), r1 = __frcp_rn(2.0f * gclamp(v[1], 1.0f, 49.0f));
@@ -314,7 +320,7 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
       if(sgx >= GX || sgy >= GX) continue;
       const int qx = mirror1(X0 - 2 + sgx, W), qy = mirror1(Y0 - 2 + sgy, H);
       const int ccx = (qx + 1) / 2 - (X0 / 2 - 1), ccy = (qy + 1) / 2 - (Y0 / 2 - 1);
-      const float wh = s.sw[0][ccy][ccx], wv = s.sw[1][ccy][ccx], wd = s.sw[2][ccy][ccx];
+      const float wh = s.u.e.sw[0][ccy][ccx], wv = s.u.e.sw[1][ccy][ccx], wd = s.u.e.sw[2][ccy][ccx];
       float rg = 0.0f, wg = 0.0f;
       switch((qx & 1) | ((qy & 1) << 1))
       { // the CFA phase of the real pixel: uniform in a warp but at mirrored borders
@@ -324,7 +330,7 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
         default: splat_taps<1, 1>(s, qx, qy, W, H, X0, Y0, wh, wv, wd, rg, wg); break;
       }
       const float gv = f16r(rg / fmaxf(1e-8f, wg));
-      s.g[sgy][sgx & 1][sgx >> 1] = gv;
+      s.g[sgy][sgx & 1][sgx >> 1] = f2h(gv);    // gv is an f16 value: exact
       s.rg[sgy][sgx & 1][sgx >> 1] = 1.0f / (1e-4f + gv);
     }
   }
@@ -334,6 +340,7 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
   {
     const float sig = p.ll_sigma, shd = p.ll_shadows, hil = p.ll_highlights, cla = p.ll_clarity;
     const float r2s = 1.0f / (2.0f * sig), rden = 1.0f / (2.0f * sig * sig / 3.0f);
+    const bool unit_curve = shd == 1.0f && hil == 1.0f;
     constexpr int NB = LH * LH;
     for(int t = tid; t < 4 * NB; t += NT)
     {
@@ -343,7 +350,7 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
       const int vx = X0 - 1 + slx, vy = Y0 - 1 + sly;
       const int px = mirror1(vx, W), py = mirror1(vy, H);
       const int gx0 = px - (X0 - 2), gy0 = py - (Y0 - 2);
-      const float gc = s.g[gy0][gx0 & 1][gx0 >> 1];
+      const float gc = h2f(s.g[gy0][gx0 & 1][gx0 >> 1]);
       const int ccx = (px + 1) / 2 - (X0 / 2 - 1), ccy = (py + 1) / 2 - (Y0 / 2 - 1);
       const float wh = s.fw[0][ccy][ccx], wv = s.fw[1][ccy][ccx], wd = s.fw[2][ccy][ccx];
       float rr = 0.0f, rb = 0.0f, wr = 0.0f, wb = 0.0f, rg = 0.0f, wg = 0.0f;
@@ -372,10 +379,19 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
       filmcurv_px(p, co, fc);
       if(own) p.rgbf[(size_t)py * W + px] = mk_half4(fc[0], fc[1], fc[2], 1.0f);
       const float yv = lum2020(gclamp(fc[0], -1000.0f, 1000.0f), gclamp(fc[1], -1000.0f, 1000.0f), gclamp(fc[2], -1000.0f, 1000.0f));
+      if(unit_curve)
+      {
 #pragma unroll
-      for(int k = 0; k < NPL - 1; k++)
-        s.L0[k][sly][slx & 1][slx >> 1] = f2h(llap_curve_rcp(yv, llap_gamma(k), sig, r2s, rden, shd, hil, cla));
-      s.L0[NPL - 1][sly][slx & 1][slx >> 1] = f2h(yv);
+        for(int k = 0; k < NPL - 1; k++)
+          s.u.L0[k][sly][slx & 1][slx >> 1] = f2h(llap_curve_unit(yv, kLlapGamma[k], rden, cla));
+      }
+      else
+      {
+#pragma unroll
+        for(int k = 0; k < NPL - 1; k++)
+          s.u.L0[k][sly][slx & 1][slx >> 1] = f2h(llap_curve_rcp(yv, kLlapGamma[k], sig, r2s, rden, shd, hil, cla));
+      }
+      s.u.L0[NPL - 1][sly][slx & 1][slx >> 1] = f2h(yv);
     }
   }
   __syncthreads();
@@ -396,7 +412,7 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
         float P[3][2];
         for(int r = 0; r < 3; r++)
         {
-          const __half *row = &s.L0[k][2 * ly + r][0][0];
+          const __half *row = &s.u.L0[k][2 * ly + r][0][0];
           const float t0 = h2f(row[lx]), t1 = h2f(row[LH + lx]), t2 = h2f(row[lx + 1]);
           P[r][0] = t0 + t1;
           P[r][1] = t1 + t2;
@@ -421,7 +437,11 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
 
 cudaError_t init_develop()
 {
-  return cudaFuncSetAttribute(k_develop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(smem_t));
+  cudaError_t e = cudaFuncSetAttribute(k_develop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(smem_t));
+  // the whole unified L1 as shared memory: 5 CTAs of 43.5 KB per SM
+  if(e == cudaSuccess) e = cudaFuncSetAttribute(k_develop, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+  if(e == cudaSuccess) e = init_llap();
+  return e;
 }
 
 cudaError_t launch_develop(const dev_image_t &p, cudaStream_t s)

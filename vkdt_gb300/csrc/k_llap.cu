@@ -32,7 +32,7 @@ DEV int gamma_hi_from_v(float v)
 {
   int hi = 1;
 #pragma unroll
-  for(int i = 1; i < NG - 1; i++) hi += (llap_gamma(i) <= v) ? 1 : 0;
+  for(int i = 1; i < NG - 1; i++) hi += (kLlapGamma[i] <= v) ? 1 : 0;
   return hi;
 }
 
@@ -63,45 +63,112 @@ template<int PX, int PY, class F> DEV float expand(F fetch, int kx, int ky)
   return r / 9.0f;
 }
 
+// expand of two planes at once (fetch returns both texels as a half2): the
+// same sums in the same order as expand() for each of the two
+template<int PX, int PY, class F> DEV float2 expand2(F fetch, int kx, int ky)
+{
+  constexpr int NX = PX ? 4 : 5, NY = PY ? 4 : 5;
+  constexpr int BXO = PX ? -1 : -2, BYO = PY ? -1 : -2;
+  float r0 = 0.0f, r1 = 0.0f;
+#pragma unroll
+  for(int b = 0; b < NY; b++)
+  {
+    float row0 = 0.0f, row1 = 0.0f;
+#pragma unroll
+    for(int a = 0; a < NX; a++)
+    {
+      const float w = PX ? ((a == 0 || a == 3) ? 1.0f : 0.5f) : (a == 2 ? 1.0f : 0.5f);
+      const float2 f = __half22float2(fetch(kx + BXO + a, ky + BYO + b));
+      row0 += w * f.x;
+      row1 += w * f.y;
+    }
+    const float wy = PY ? ((b == 0 || b == 3) ? 1.0f : 0.5f) : (b == 2 ? 1.0f : 0.5f);
+    r0 += wy * row0;
+    r1 += wy * row1;
+  }
+  return make_float2(r0 / 9.0f, r1 / 9.0f);
+}
+
 // llap/reduce.comp:17-35 (sample_semisoft), all planes of one level. The four
 // half-texel bilinear taps equal ((P00+P10)/4 ...) with the horizontal pair
-// sums P (halving is exact), as in the develop kernel.
+// sums P (halving is exact), as in the develop kernel. A CTA makes a 32 x 16
+// tile of outputs: per plane it stages the 66 x 33 input texels once
+// (coalesced 4 byte loads inside the image, mirrored single loads at its
+// border; the taps overshoot the input by at most one texel).
+constexpr int RT_X = 32, RT_Y = 16, RI_X = 2 * RT_X + 2, RI_Y = 2 * RT_Y + 1;
+
 __global__ void __launch_bounds__(256) k_llap_reduce(const __half *__restrict__ in, int iw, int ih, size_t ip,
     __half *__restrict__ out, int ow, int oh, size_t op)
 {
-  const int x = blockIdx.x * 32 + threadIdx.x % 32, y = blockIdx.y * 8 + threadIdx.x / 32;
-  if(x >= ow || y >= oh) return;
-  int xs[3], ys[3];
-  for(int a = 0; a < 3; a++) { xs[a] = mirror_full(2 * x - 1 + a, iw); ys[a] = mirror_full(2 * y - 1 + a, ih); }
-  for(int k = 0; k < NPL; k++)
-  {
-    const __half *pl = in + k * ip;
-    float P[3][2];
-    for(int b = 0; b < 3; b++)
+  __shared__ __align__(4) __half t[NPL][RI_Y][RI_X];   // all planes at once: every load in flight together
+  const int OX = blockIdx.x * RT_X, OY = blockIdx.y * RT_Y;
+  const int gx0 = 2 * OX - 2, gy0 = 2 * OY - 1;     // input texel of t[.][0][0]
+  const bool inside = gx0 >= 0 && gy0 >= 0 && gx0 + RI_X <= iw && gy0 + RI_Y <= ih && !(iw & 1);
+  if(inside)
+    for(int i = threadIdx.x; i < RI_Y * (RI_X / 2); i += blockDim.x)
     {
-      const __half *row = pl + (size_t)ys[b] * iw;
-      const float t0 = h2f(row[xs[0]]), t1 = h2f(row[xs[1]]), t2 = h2f(row[xs[2]]);
-      P[b][0] = t0 + t1;
-      P[b][1] = t1 + t2;
+      const int r = i / (RI_X / 2), c = i % (RI_X / 2);
+      const size_t o = (size_t)(gy0 + r) * iw + gx0 + 2 * c;
+#pragma unroll
+      for(int k = 0; k < NPL; k++)
+        *reinterpret_cast<uint32_t *>(&t[k][r][2 * c]) = __ldg(reinterpret_cast<const uint32_t *>(in + k * ip + o));
     }
-    const float q00 = (P[0][0] + P[1][0]) * 0.25f, q10 = (P[0][1] + P[1][1]) * 0.25f;
-    const float q01 = (P[1][0] + P[2][0]) * 0.25f, q11 = (P[1][1] + P[2][1]) * 0.25f;
-    out[k * op + (size_t)y * ow + x] = f2h((((q00 + q10) + q01) + q11) * 0.25f);
+  else
+    for(int i = threadIdx.x; i < RI_Y * RI_X; i += blockDim.x)
+    {
+      const int r = i / RI_X, c = i % RI_X;
+      const size_t o = (size_t)mirror1(gy0 + r, ih) * iw + mirror1(gx0 + c, iw);
+#pragma unroll
+      for(int k = 0; k < NPL; k++) t[k][r][c] = __ldg(in + k * ip + o);
+    }
+  __syncthreads();
+  const int lx = threadIdx.x % RT_X, ly = threadIdx.x / RT_X;
+#pragma unroll
+  for(int h = 0; h < 2; h++)
+  {
+    const int oy = OY + ly + 8 * h, ox = OX + lx;
+    if(ox >= ow || oy >= oh) continue;
+    for(int k = 0; k < NPL; k++)
+    {
+      float P[3][2];
+#pragma unroll
+      for(int b = 0; b < 3; b++)
+      { // input rows 2 oy - 1 + b, columns 2 ox - 1 .. 2 ox + 1
+        const __half *row = &t[k][2 * (ly + 8 * h) + b][2 * lx + 1];
+        const float t0 = h2f(row[0]), t1 = h2f(row[1]), t2 = h2f(row[2]);
+        P[b][0] = t0 + t1;
+        P[b][1] = t1 + t2;
+      }
+      const float q00 = (P[0][0] + P[1][0]) * 0.25f, q10 = (P[0][1] + P[1][1]) * 0.25f;
+      const float q01 = (P[1][0] + P[2][0]) * 0.25f, q11 = (P[1][1] + P[2][1]) * 0.25f;
+      out[k * op + (size_t)oy * ow + ox] = f2h((((q00 + q10) + q01) + q11) * 0.25f);
+    }
   }
 }
 
-// stage the 11 planes of the coarse level and the coarse assembled image of
-// one output tile: slot (sx, sy) holds the mirrored texel (bx+sx, by+sy)
-DEV void stage_coarse(float (*sl)[FS][FS + 1], const __half *l1, int w1, int h1, size_t p1,
+// the coarse level around one output tile: slot (sx, sy) holds the mirrored
+// texel (bx+sx, by+sy). An output mixes the two adjacent planes around its
+// grey value, so the planes are staged in pairs (k, k+1), one 4 byte word per
+// slot (f16 values: exact), beside the coarse assembled image.
+struct coarse_t
+{
+  __half2 pr[NG - 1][FS][FS + 1];   // planes (k, k+1), k = 0 .. NG-2
+  float c[FS][FS + 1];              // the coarse assembled image (the grey plane on the first level)
+};
+
+DEV void stage_coarse(coarse_t &sc, const __half *l1, int w1, int h1, size_t p1,
     const __half *coarse, int bx, int by)
 { // the mirrored position once per slot, then the same texel of every plane
   for(int r = threadIdx.x; r < FS * FS; r += blockDim.x)
   {
     const int sx = r % FS, sy = r / FS;
     const size_t o = (size_t)mirror1(by + sy, h1) * w1 + mirror1(bx + sx, w1);
+    __half h[NG];
 #pragma unroll
-    for(int k = 0; k < NPL; k++) sl[k][sy][sx] = h2f(__ldg(l1 + k * p1 + o));
-    sl[NPL][sy][sx] = h2f(__ldg(coarse + o));
+    for(int k = 0; k < NG; k++) h[k] = __ldg(l1 + k * p1 + o);
+#pragma unroll
+    for(int k = 0; k < NG - 1; k++) sc.pr[k][sy][sx] = __halves2half2(h[k], h[k + 1]);
+    sc.c[sy][sx] = h2f(__ldg(coarse + o));
   }
 }
 
@@ -117,21 +184,22 @@ DEV bool tile_item(int t, int X0, int Y0, int w0, int h0, int &x, int &y)
 
 // llap/assemble.comp:89-123 at one output pixel of parity (PX, PY). l0(k)
 // returns the fine level plane k at the pixel, sl holds the coarse level.
-template<int PX, int PY, class L0> DEV float assemble_px(L0 l0, float v, const float (*sl)[FS][FS + 1], int x, int y, int bx, int by)
+template<int PX, int PY, class L0> DEV float assemble_px(L0 l0, float v, const coarse_t &sc, int x, int y, int bx, int by)
 {
   const int kx = x >> 1, ky = y >> 1;
-  auto fs = [&](int k) { return [=](int ix, int iy) { return sl[k][iy - by][ix - bx]; }; };
-  const float res = expand<PX, PY>(fs(NPL), kx, ky);
+  const float res = expand<PX, PY>([&](int ix, int iy) { return sc.c[iy - by][ix - bx]; }, kx, ky);
   const int hi = gamma_hi_from_v(v);
-  const float glo = llap_gamma(hi - 1), ghi = llap_gamma(hi);
+  const float glo = kLlapGamma[hi - 1], ghi = kLlapGamma[hi];
   const float a = gclamp((v - glo) / (ghi - glo), 0.0f, 1.0f);
-  const float la = l0(hi - 1, glo) - expand<PX, PY>(fs(hi - 1), kx, ky);
-  const float lb = l0(hi, ghi) - expand<PX, PY>(fs(hi), kx, ky);
+  const __half2 (*pr)[FS + 1] = sc.pr[hi - 1];
+  const float2 e = expand2<PX, PY>([&](int ix, int iy) { return pr[iy - by][ix - bx]; }, kx, ky);
+  const float la = l0(hi - 1, glo) - e.x;
+  const float lb = l0(hi, ghi) - e.y;
   return res + la * (1.0f - a) + lb * a;
 }
 
 // llap/assemble.comp:89-123 for a stored level: output at the size of l0
-template<int PX, int PY> DEV void assemble_stored(const float (*sl)[FS][FS + 1], const __half *l0, size_t p0,
+template<int PX, int PY> DEV void assemble_stored(const coarse_t &sl, const __half *l0, size_t p0,
     int w0, int x, int y, int bx, int by, __half *out)
 {
   const size_t o = (size_t)y * w0 + x;
@@ -144,7 +212,7 @@ __global__ void __launch_bounds__(256) k_llap_assemble(const __half *__restrict_
     const __half *__restrict__ l0, int w0, int h0, size_t p0,
     const __half *__restrict__ l1, int w1, int h1, size_t p1, __half *__restrict__ out)
 {
-  __shared__ float sl[NPL + 1][FS][FS + 1];
+  __shared__ coarse_t sl;
   const int X0 = blockIdx.x * FT, Y0 = blockIdx.y * FT;
   const int bx = X0 / 2 - 2, by = Y0 / 2 - 2;
   stage_coarse(sl, l1, w1, h1, p1, first ? l1 + NG * p1 : coarse, bx, by);
@@ -165,15 +233,17 @@ __global__ void __launch_bounds__(256) k_llap_assemble(const __half *__restrict_
 
 // llap/assemble.comp for level 0, the fine planes recomputed from the
 // filmcurv output like llap/curve.comp, fused with llap/colour.comp:141-160
-template<int PX, int PY> DEV void final_px(const dev_llap_k3_t &p, const float (*sl)[FS][FS + 1], int x, int y,
+template<int PX, int PY> DEV void final_px(const dev_llap_k3_t &p, const coarse_t &sl, int x, int y,
     int bx, int by, float r2s, float rden)
 {
   float rgb[4];
   ld_half4(p.rgbf + (size_t)y * p.W + x, rgb[0], rgb[1], rgb[2], rgb[3]);
   const float yv = lum2020(gclamp(rgb[0], -1000.0f, 1000.0f), gclamp(rgb[1], -1000.0f, 1000.0f), gclamp(rgb[2], -1000.0f, 1000.0f));
   const float v = f16r(yv);
+  const bool unit_curve = p.ll_shadows == 1.0f && p.ll_highlights == 1.0f;
   float yo_ = f16r(assemble_px<PX, PY>([&](int, float g) {
-      return f16r(llap_curve_rcp(yv, g, p.ll_sigma, r2s, rden, p.ll_shadows, p.ll_highlights, p.ll_clarity)); },
+      return f16r(unit_curve ? llap_curve_unit(yv, g, rden, p.ll_clarity)
+                             : llap_curve_rcp(yv, g, p.ll_sigma, r2s, rden, p.ll_shadows, p.ll_highlights, p.ll_clarity)); },
     v, sl, x, y, bx, by));
   const float yo = fmaxf(lum2020(rgb[0], rgb[1], rgb[2]), 1e-8f);
   if(yo_ < yo) yo_ = yo * expf(1.0f * (yo_ - yo));
@@ -184,7 +254,7 @@ template<int PX, int PY> DEV void final_px(const dev_llap_k3_t &p, const float (
 
 __global__ void __launch_bounds__(256) k_llap_final(const dev_llap_k3_t p)
 {
-  __shared__ float sl[NPL + 1][FS][FS + 1];
+  __shared__ coarse_t sl;
   const int X0 = blockIdx.x * FT, Y0 = blockIdx.y * FT;
   const int bx = X0 / 2 - 2, by = Y0 / 2 - 2;
   stage_coarse(sl, p.l1, p.l1w, p.l1h, p.l1plane, p.coarse, bx, by);
@@ -207,10 +277,15 @@ __global__ void __launch_bounds__(256) k_llap_final(const dev_llap_k3_t p)
 
 } // namespace
 
+cudaError_t init_llap()
+{ // the reduce stages all 11 planes of a tile (47.9 KB): 4 CTAs per SM with the full carveout
+  return cudaFuncSetAttribute(k_llap_reduce, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+}
+
 cudaError_t launch_llap_reduce(const __half *in, int iw, int ih, size_t iplane,
     __half *out, int ow, int oh, size_t oplane, cudaStream_t s)
 {
-  dim3 grid((ow + 31) / 32, (oh + 7) / 8);
+  dim3 grid((ow + RT_X - 1) / RT_X, (oh + RT_Y - 1) / RT_Y);
   k_llap_reduce<<<grid, 256, 0, s>>>(in, iw, ih, iplane, out, ow, oh, oplane);
   return cudaGetLastError();
 }

@@ -350,6 +350,7 @@ __global__ void __launch_bounds__(NT) k_post(const dev_image_t p, const half4 *_
   __syncthreads();
   const float sig = p.ll_sigma, shd = p.ll_shadows, hil = p.ll_highlights, cla = p.ll_clarity;
   const float r2s = 1.0f / (2.0f * sig), rden = 1.0f / (2.0f * sig * sig / 3.0f);
+  const bool unit_curve = shd == 1.0f && hil == 1.0f;
   for(int t = tid; t < LX * LX; t += NT)
   {
     const int slx = t % LX, sly = t / LX;
@@ -369,9 +370,18 @@ __global__ void __launch_bounds__(NT) k_post(const dev_image_t p, const half4 *_
     filmcurv_px(p, co, fc);
     if(own) p.rgbf[(size_t)py * W + px] = mk_half4(fc[0], fc[1], fc[2], 1.0f);
     const float yv = lum2020(gclamp(fc[0], -1000.0f, 1000.0f), gclamp(fc[1], -1000.0f, 1000.0f), gclamp(fc[2], -1000.0f, 1000.0f));
+    if(unit_curve)
+    {
 #pragma unroll
-    for(int k = 0; k < NPL - 1; k++)
-      L0[k][sly][slx & 1][slx >> 1] = f2h(llap_curve_rcp(yv, llap_gamma(k), sig, r2s, rden, shd, hil, cla));
+      for(int k = 0; k < NPL - 1; k++)
+        L0[k][sly][slx & 1][slx >> 1] = f2h(llap_curve_unit(yv, kLlapGamma[k], rden, cla));
+    }
+    else
+    {
+#pragma unroll
+      for(int k = 0; k < NPL - 1; k++)
+        L0[k][sly][slx & 1][slx >> 1] = f2h(llap_curve_rcp(yv, kLlapGamma[k], sig, r2s, rden, shd, hil, cla));
+    }
     L0[NPL - 1][sly][slx & 1][slx >> 1] = f2h(yv);
   }
   __syncthreads();

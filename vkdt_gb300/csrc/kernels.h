@@ -142,6 +142,7 @@ cudaError_t launch_llap_reduce(const __half *in, int iw, int ih, size_t iplane,
 cudaError_t launch_llap_assemble(const __half *coarse, int first, const __half *l0, int w0, int h0, size_t p0,
     const __half *l1, int w1, int h1, size_t p1, __half *out, cudaStream_t s);
 cudaError_t launch_llap_final(const dev_llap_k3_t &p, cudaStream_t s);
+cudaError_t init_llap();      // function attributes, once per device (from init_develop)
 
 // misc (k_misc.cu)
 struct scene_layout_t;

@@ -13,6 +13,10 @@
 
 // llap/llap.glsl:3-14 (i / (NUM_GAMMA - 1), correctly rounded: it decides the plane selection)
 DEV float llap_gamma(int i) { return __fdiv_rn((float)i, 10.0f - 1.0f); }
+// the same values as compile-time constants (for loops unrolled over the planes);
+// the initialisers are constant expressions, divided in IEEE round to nearest
+__device__ constexpr float kLlapGamma[10] = { 0.0f / 9.0f, 1.0f / 9.0f, 2.0f / 9.0f, 3.0f / 9.0f, 4.0f / 9.0f,
+                                              5.0f / 9.0f, 6.0f / 9.0f, 7.0f / 9.0f, 8.0f / 9.0f, 9.0f / 9.0f };
 
 // llap/curve.comp:39-63 (shared with the final llap kernel)
 DEV float llap_curve_fn(float x, float g, float sigma, float shadows, float highlights, float clarity)
@@ -52,6 +56,16 @@ DEV float llap_curve_rcp(float x, float g, float sigma, float r2s, float rden, f
   }
   val += clarity * c * curve_exp(-c * c * rden);
   return val;
+}
+
+// the curve for shadows = highlights = 1 (the darkroom values): the linear
+// part g + s + (c - s) and the quadratic bezier g + 2 s t, t = c / (2 s), are
+// both x itself, which leaves x + clarity c exp(-c^2 / (2 sigma^2 / 3)); equal
+// to llap_curve_fn up to the rounding of the operations it leaves out
+DEV float llap_curve_unit(float x, float g, float rden, float clarity)
+{
+  const float c = x - g;
+  return x + clarity * c * curve_exp(-c * c * rden);
 }
 
 // histogram bin, bit exact with the oracle (see hist_log there for the method)

@@ -124,6 +124,75 @@ template<int PX, int PY> DEV void fix_taps(const smem_t &s, int px, int py, int 
   }
 }
 
+// demosaic/gauss.comp:24-75 (bayer) for one entry, px the 8 greens around it
+// in the shader's loop order: the covariance sums in the shader's order
+// without contraction. They decide the form and the snapped direction, and
+// on flat input the direction is a near tie: the sample positions alone have
+// the covariance (1.25 -0.25; -0.25 1.25), eigenvectors at 45 degrees, so the
+// snap there follows the last bits of the sums and is evaluated exactly.
+DEV void gauss_exact(const float px[8], float v[4])
+{
+  float inv[8];
+#pragma unroll
+  for(int k = 0; k < 8; k++) inv[k] = __frcp_rn(px[k]);
+  int k;
+  // i/px for i in {-1,0,1,2} is i*(1/px) exactly (scaling by +-1, 2 is exact)
+  float mw0 = 0, mw1 = 0, mb0 = 0, mb1 = 0, smw = 0, smb = 0;
+  k = 0;
+#pragma unroll
+  for(int j = -1; j < 3; j++)
+#pragma unroll
+  for(int ii = -1; ii < 3; ii++)
+  {
+    if(((j + ii) & 1) != 1) continue;
+    mw0 += (float)ii * px[k]; mw1 += (float)j * px[k];
+    smw += px[k];
+    mb0 += (float)ii * inv[k]; mb1 += (float)j * inv[k];
+    smb += inv[k];
+    k++;
+  }
+  // (the products above are exact, so contraction cannot change them;
+  // the covariance sums below decide the snapped direction and are
+  // evaluated without contraction, in the shader's order)
+  mw0 = __fdiv_rn(mw0, smw); mw1 = __fdiv_rn(mw1, smw);
+  mb0 = __fdiv_rn(mb0, smb); mb1 = __fdiv_rn(mb1, smb);
+  float Sw00 = 0, Sw01 = 0, Sw10 = 0, Sw11 = 0, Sb00 = 0, Sb01 = 0, Sb10 = 0, Sb11 = 0, sw = 0, sb = 0;
+  k = 0;
+#pragma unroll
+  for(int j = -1; j < 3; j++)
+#pragma unroll
+  for(int ii = -1; ii < 3; ii++)
+  {
+    if(((j + ii) & 1) != 1) continue;
+    float p2 = __fmul_rn(px[k], px[k]);
+    float q0 = __fsub_rn((float)ii, mw0), q1 = __fsub_rn((float)j, mw1);
+    Sw00 = __fadd_rn(Sw00, __fmul_rn(__fmul_rn(p2, q0), q0));
+    Sw01 = __fadd_rn(Sw01, __fmul_rn(__fmul_rn(p2, q0), q1));
+    Sw10 = __fadd_rn(Sw10, __fmul_rn(__fmul_rn(p2, q1), q0));
+    Sw11 = __fadd_rn(Sw11, __fmul_rn(__fmul_rn(p2, q1), q1));
+    sw = __fadd_rn(sw, p2);
+    q0 = __fsub_rn((float)ii, mb0); q1 = __fsub_rn((float)j, mb1);
+    p2 = __frcp_rn(p2);
+    Sb00 = __fadd_rn(Sb00, __fmul_rn(__fmul_rn(p2, q0), q0));
+    Sb01 = __fadd_rn(Sb01, __fmul_rn(__fmul_rn(p2, q0), q1));
+    Sb10 = __fadd_rn(Sb10, __fmul_rn(__fmul_rn(p2, q1), q0));
+    Sb11 = __fadd_rn(Sb11, __fmul_rn(__fmul_rn(p2, q1), q1));
+    sb = __fadd_rn(sb, p2);
+    k++;
+  }
+  Sw00 = __fdiv_rn(Sw00, sw); Sw01 = __fdiv_rn(Sw01, sw); Sw10 = __fdiv_rn(Sw10, sw); Sw11 = __fdiv_rn(Sw11, sw);
+  Sb00 = __fdiv_rn(Sb00, sb); Sb01 = __fdiv_rn(Sb01, sb); Sb10 = __fdiv_rn(Sb10, sb); Sb11 = __fdiv_rn(Sb11, sb);
+  const float detw = __fsub_rn(__fmul_rn(Sw00, Sw11), __fmul_rn(Sw10, Sw01));
+  const float detb = __fsub_rn(__fmul_rn(Sb00, Sb11), __fmul_rn(Sb10, Sb01));
+  float eval[2], evec0[2], evec1[2];
+  if(detw < detb) evd2x2(eval, evec0, evec1, Sw00, Sw10, Sw11);
+  else            evd2x2(eval, evec0, evec1, Sb00, Sb10, Sb11);
+  eval[0] = __fmul_rn(eval[0], 0.2f); eval[1] = __fmul_rn(eval[1], 0.2f);
+  if(fabsf(evec0[0]) > fabsf(evec0[1])) { evec0[0] = 1.0f; evec0[1] = 0.0f; }
+  else                                  { evec0[0] = 0.0f; evec0[1] = 1.0f; }
+  v[0] = f16r(eval[0]); v[1] = f16r(eval[1]); v[2] = f16r(evec0[0]); v[3] = f16r(evec0[1]);
+}
+
 __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -215,7 +284,7 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
     if(cx >= 0 && cy >= 0 && cx < hw && cy < hh)
     {
       // green samples at (2c+ii, 2c+j), (ii+j) odd: M slot x = 2scx+2+ii
-      float px[8], inv[8];
+      float px[8];
       int k = 0;
 #pragma unroll
       for(int j = -1; j < 3; j++)
@@ -224,65 +293,9 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
       {
         if(((j + ii) & 1) != 1) continue;
         const int xs = 2 * scx + 2 + ii;
-        px[k] = s.M[2 * scy + 2 + j][xs & 1][xs >> 1];
-        inv[k] = __frcp_rn(px[k]);
-        k++;
+        px[k++] = s.M[2 * scy + 2 + j][xs & 1][xs >> 1];
       }
-      // i/px for i in {-1,0,1,2} is i*(1/px) exactly (scaling by +-1, 2 is exact)
-      float mw0 = 0, mw1 = 0, mb0 = 0, mb1 = 0, smw = 0, smb = 0;
-      k = 0;
-#pragma unroll
-      for(int j = -1; j < 3; j++)
-#pragma unroll
-      for(int ii = -1; ii < 3; ii++)
-      {
-        if(((j + ii) & 1) != 1) continue;
-        mw0 += (float)ii * px[k]; mw1 += (float)j * px[k];
-        smw += px[k];
-        mb0 += (float)ii * inv[k]; mb1 += (float)j * inv[k];
-        smb += inv[k];
-        k++;
-      }
-      // (the products above are exact, so contraction cannot change them;
-      // the covariance sums below decide the snapped direction and are
-      // evaluated without contraction, in the shader's order)
-      mw0 = __fdiv_rn(mw0, smw); mw1 = __fdiv_rn(mw1, smw);
-      mb0 = __fdiv_rn(mb0, smb); mb1 = __fdiv_rn(mb1, smb);
-      float Sw00 = 0, Sw01 = 0, Sw10 = 0, Sw11 = 0, Sb00 = 0, Sb01 = 0, Sb10 = 0, Sb11 = 0, sw = 0, sb = 0;
-      k = 0;
-#pragma unroll
-      for(int j = -1; j < 3; j++)
-#pragma unroll
-      for(int ii = -1; ii < 3; ii++)
-      {
-        if(((j + ii) & 1) != 1) continue;
-        float p2 = __fmul_rn(px[k], px[k]);
-        float q0 = __fsub_rn((float)ii, mw0), q1 = __fsub_rn((float)j, mw1);
-        Sw00 = __fadd_rn(Sw00, __fmul_rn(__fmul_rn(p2, q0), q0));
-        Sw01 = __fadd_rn(Sw01, __fmul_rn(__fmul_rn(p2, q0), q1));
-        Sw10 = __fadd_rn(Sw10, __fmul_rn(__fmul_rn(p2, q1), q0));
-        Sw11 = __fadd_rn(Sw11, __fmul_rn(__fmul_rn(p2, q1), q1));
-        sw = __fadd_rn(sw, p2);
-        q0 = __fsub_rn((float)ii, mb0); q1 = __fsub_rn((float)j, mb1);
-        p2 = __frcp_rn(p2);
-        Sb00 = __fadd_rn(Sb00, __fmul_rn(__fmul_rn(p2, q0), q0));
-        Sb01 = __fadd_rn(Sb01, __fmul_rn(__fmul_rn(p2, q0), q1));
-        Sb10 = __fadd_rn(Sb10, __fmul_rn(__fmul_rn(p2, q1), q0));
-        Sb11 = __fadd_rn(Sb11, __fmul_rn(__fmul_rn(p2, q1), q1));
-        sb = __fadd_rn(sb, p2);
-        k++;
-      }
-      Sw00 = __fdiv_rn(Sw00, sw); Sw01 = __fdiv_rn(Sw01, sw); Sw10 = __fdiv_rn(Sw10, sw); Sw11 = __fdiv_rn(Sw11, sw);
-      Sb00 = __fdiv_rn(Sb00, sb); Sb01 = __fdiv_rn(Sb01, sb); Sb10 = __fdiv_rn(Sb10, sb); Sb11 = __fdiv_rn(Sb11, sb);
-      const float detw = __fsub_rn(__fmul_rn(Sw00, Sw11), __fmul_rn(Sw10, Sw01));
-      const float detb = __fsub_rn(__fmul_rn(Sb00, Sb11), __fmul_rn(Sb10, Sb01));
-      float eval[2], evec0[2], evec1[2];
-      if(detw < detb) evd2x2(eval, evec0, evec1, Sw00, Sw10, Sw11);
-      else            evd2x2(eval, evec0, evec1, Sb00, Sb10, Sb11);
-      eval[0] = __fmul_rn(eval[0], 0.2f); eval[1] = __fmul_rn(eval[1], 0.2f);
-      if(fabsf(evec0[0]) > fabsf(evec0[1])) { evec0[0] = 1.0f; evec0[1] = 0.0f; }
-      else                                  { evec0[0] = 0.0f; evec0[1] = 1.0f; }
-      v[0] = f16r(eval[0]); v[1] = f16r(eval[1]); v[2] = f16r(evec0[0]); v[3] = f16r(evec0[1]);
+      gauss_exact(px, v);
     }
     // splat.comp:159-163 and fix.comp:21-29 weights of this entry. E (i, j) is
     // (i, j) for evec (1,0), (j, -i) for evec (0,1) and 0 without covariance,
@@ -290,19 +303,20 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
     // a diagonal one 1/e0 + 1/e1, and every tap 0 without covariance
     const int ori = v[2] == 1.0f ? 0 : (v[3] == 1.0f ? 1 : 2);
     {
-      const float r0 = __frcp_rn(gclamp(v[0], 0.01f, 25.0f)), r1 = __frcp_rn(gclamp(v[1], 0.01f, 25.0f));
-      const float wa = gclamp(expf(-0.5f * r0), 1e-4f, 1.0f);
-      const float wb = gclamp(expf(-0.5f * r1), 1e-4f, 1.0f);
-      const float wc = gclamp(expf(-0.5f * __fadd_rn(r0, r1)), 1e-4f, 1.0f);
+      // (continuous values from here on: fast reciprocal and exp)
+      const float r0 = __fdividef(1.0f, gclamp(v[0], 0.01f, 25.0f)), r1 = __fdividef(1.0f, gclamp(v[1], 0.01f, 25.0f));
+      const float wa = gclamp(curve_exp(-0.5f * r0), 1e-4f, 1.0f);
+      const float wb = gclamp(curve_exp(-0.5f * r1), 1e-4f, 1.0f);
+      const float wc = gclamp(curve_exp(-0.5f * (r0 + r1)), 1e-4f, 1.0f);
       s.u.e.sw[0][scy][scx] = ori == 0 ? wa : (ori == 1 ? wb : 1.0f);
       s.u.e.sw[1][scy][scx] = ori == 0 ? wb : (ori == 1 ? wa : 1.0f);
       s.u.e.sw[2][scy][scx] = ori == 2 ? 1.0f : wc;
     }
     {
-      const float r0 = __frcp_rn(2.0f * gclamp(v[0], 1.0f, 49.0f)), r1 = __frcp_rn(2.0f * gclamp(v[1], 1.0f, 49.0f));
-      const float wa = gclamp(expf(-0.5f * r0), 1e-3f, 1.0f);
-      const float wb = gclamp(expf(-0.5f * r1), 1e-3f, 1.0f);
-      const float wc = gclamp(expf(-0.5f * __fadd_rn(r0, r1)), 1e-3f, 1.0f);
+      const float r0 = __fdividef(1.0f, 2.0f * gclamp(v[0], 1.0f, 49.0f)), r1 = __fdividef(1.0f, 2.0f * gclamp(v[1], 1.0f, 49.0f));
+      const float wa = gclamp(curve_exp(-0.5f * r0), 1e-3f, 1.0f);
+      const float wb = gclamp(curve_exp(-0.5f * r1), 1e-3f, 1.0f);
+      const float wc = gclamp(curve_exp(-0.5f * (r0 + r1)), 1e-3f, 1.0f);
       s.fw[0][scy][scx] = ori == 0 ? wa : (ori == 1 ? wb : 1.0f);
       s.fw[1][scy][scx] = ori == 0 ? wb : (ori == 1 ? wa : 1.0f);
       s.fw[2][scy][scx] = ori == 2 ? 1.0f : wc;

@@ -259,6 +259,25 @@ int  vkdt_cuda_graph_hist(vkdt_cuda_graph_t *graph, uint32_t *hist257);
  * (cleared by the call) */
 int  vkdt_cuda_hist_rgba_f16(const void *d_rgba, int wd, int ht, uint32_t *d_hist257, void *stream);
 
+/* ---- noise statistics and the noise profile fit (rawhist and nprof modules)
+ *
+ * rawhist/collect.comp:22-66 over a device mosaic (uint16, row pitch = wd):
+ * per CFA block the green cross mean and second moment of the black/white
+ * normalised values, binned by bins*log2(mean+1). h_out (host, 3*bins
+ * doubles) receives per bin the block count, the sum of means and the sum of
+ * second moments (exact: 64-bit fixed point sums, one FP64 combine). black
+ * and white are those of the metadata's channel 1, as rawhist/main.c:17-28
+ * commits them. d_scratch: device memory of vkdt_cuda_rawhist_scratch_bytes().
+ * The call waits for its stream. bins <= 1024 (the reference uses 1000). */
+size_t vkdt_cuda_rawhist_scratch_bytes(void);
+int  vkdt_cuda_rawhist(const void *d_mosaic, int wd, int ht, const vkdt_cuda_img_param_t *ip, int bins,
+    void *d_scratch, double *h_out, void *stream);
+/* nprof/main.c:82-198 on such a histogram: outlier rejecting pair fits of
+ * sigma^2 = a + b x between bins, then the count weighted regression over
+ * the accepted bins; a, b in the normalised units of vkdt_cuda_img_param_t.
+ * Host code, no device work. */
+int  vkdt_cuda_nprof_fit(const double *hist, int bins, float *a, float *b);
+
 /* debug: copy an intermediate image of the last run to host floats.
  * stage 0 denoise output (1 ch), 1 hilite output (1 ch), both at the crop size;
  * 2 filmcurv output (4 ch) and 3 demosaic output (4 ch, x-trans and reduced

@@ -81,6 +81,8 @@ def lib():
         l.oracle_hist_bin.argtypes = [C.c_float, C.c_float, C.c_float]
         l.oracle_cfa_colour.restype = C.c_int
         l.oracle_cfa_colour.argtypes = [C.c_uint32, C.c_int, C.c_int]
+        l.oracle_rawhist.argtypes = [C.POINTER(C.c_uint16), C.c_int, C.c_int, C.c_uint32, C.c_float, C.c_float,
+                                     C.c_int, C.POINTER(C.c_double)]
         l.oracle_f16.restype = C.c_float
         l.oracle_f16.argtypes = [C.c_float]
         _lib = l
@@ -162,3 +164,13 @@ def cfa_colour(filters, x, y):
 
 def f16(v):
     return lib().oracle_f16(v)
+
+
+def rawhist(mosaic, filters, black, white, bins=1000):
+    """rawhist/collect.comp statistics (counts, sums of means, sums of second moments), shape (3, bins)."""
+    mosaic = np.ascontiguousarray(mosaic, dtype=np.uint16)
+    ht, wd = mosaic.shape
+    out = np.zeros(3 * bins, np.float64)
+    lib().oracle_rawhist(mosaic.ctypes.data_as(C.POINTER(C.c_uint16)), wd, ht, filters, black, white, bins,
+                         out.ctypes.data_as(C.POINTER(C.c_double)))
+    return out.reshape(3, bins)

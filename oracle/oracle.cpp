@@ -1071,6 +1071,56 @@ static float hist_log(float x)
 
 } // namespace
 
+// rawhist/collect.comp:22-66 (test infrastructure). The sums are 64-bit fixed
+// point (value * 2^36, rounded to nearest) and the bin uses hist_log / ln 2,
+// like the kernel, so counts and sums reproduce exactly; out: 3*bins doubles.
+extern "C" void oracle_rawhist(const uint16_t *mosaic, int wd, int ht, uint32_t filters, float black_dn,
+    float white_dn, int bins, double *out)
+{
+  const uint32_t bi = (uint32_t)std::max(1.0f, black_dn), wi = (uint32_t)white_dn;   // rawhist/main.c:17-28
+  const float black = (float)bi / 65536.0f, white = (float)wi / 65536.0f;
+  std::vector<uint64_t> c(bins, 0), sm(bins, 0), s2(bins, 0);
+  auto val = [&](int x, int y) {
+    const float v = (x < wd && y < ht) ? (float)mosaic[(size_t)y * wd + x] / 65535.0f : 0.0f;
+    const float t = (v - black) / (white - black);
+    return std::fmin(std::fmax(t, 0.0f), 1.0f);
+  };
+  const int block = filters == 9u ? 3 : 2;
+  for(int by = 0; by < ht / block; by++) for(int bx = 0; bx < wd / block; bx++)
+  {
+    float mean, mom2;
+    if(filters == 9u)
+    {
+      const int x = 3 * bx, y = 3 * by;
+      const float v0 = val(x, y), v1 = val(x + 2, y), v2 = val(x + 1, y + 1), v3 = val(x, y + 2), v4 = val(x + 2, y + 2);
+      mean = ((((v0 + v1) + v2) + v3) + v4) / 5.0f;
+      const float q0 = v0 * v0, q1 = v1 * v1, q2 = v2 * v2, q3 = v3 * v3, q4 = v4 * v4;
+      mom2 = ((((q0 + q1) + q2) + q3) + q4) / 5.0f;
+    }
+    else
+    {
+      const int x = 2 * bx, y = 2 * by;
+      const float v0 = val(x + 1, y), v1 = val(x, y + 1);
+      mean = (v0 + v1) * 0.5f;
+      const float q0 = v0 * v0, q1 = v1 * v1;
+      mom2 = (q0 + q1) * 0.5f;
+    }
+    const float l = hist_log(mean + 1.0f) * 1.44269504f;
+    const float xb = (float)bins * l;
+    const int bin = (int)xb;
+    if(bin < 0 || bin >= bins) continue;
+    c[bin]++;
+    sm[bin] += (uint64_t)std::nearbyint((double)mean * 68719476736.0);
+    s2[bin] += (uint64_t)std::nearbyint((double)mom2 * 68719476736.0);
+  }
+  for(int i = 0; i < bins; i++)
+  {
+    out[i] = (double)c[i];
+    out[bins + i] = (double)sm[i] / 68719476736.0;
+    out[2 * bins + i] = (double)s2[i] / 68719476736.0;
+  }
+}
+
 extern "C" uint32_t oracle_hist_bin(float r, float g, float b)
 { // OpenDRT/hist.comp:15-20 get_bin, shared/oetf.glsl:13-15 eotf_filmlight_tlog
   const float p0 = 2.62700212e-01f * r, p1 = 6.77998072e-01f * g, p2 = 5.93017165e-02f * b;

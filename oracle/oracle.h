@@ -99,6 +99,9 @@ void oracle_noop(const uint16_t *mosaic, int wd, int ht, const oracle_img_param_
 void oracle_hist(const float *rgba, int wd, int ht, uint32_t *hist257);
 /* the bin index the histogram assigns to a luminance (bit exact with the kernel) */
 uint32_t oracle_hist_bin(float r, float g, float b);
+/* rawhist/collect.comp statistics: out = counts, sums of means, sums of second moments (3*bins) */
+void oracle_rawhist(const uint16_t *mosaic, int wd, int ht, uint32_t filters, float black_dn,
+    float white_dn, int bins, double *out);
 /* CFA colour index at a pixel: 0 red, 1 green, 2 blue (demosaic/splat.comp:167-222) */
 int oracle_cfa_colour(uint32_t filters, int x, int y);
 /* round to IEEE half (RTNE) and back */

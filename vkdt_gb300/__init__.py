@@ -98,6 +98,30 @@ def scene_device(scene, d_ptr, stream=0):
           "vkdt_cuda_scene_generate")
 
 
+def rawhist(d_mosaic, wd, ht, img_param, bins=1000, d_scratch=None, stream=0):
+    """vkdt_cuda_rawhist: noise statistics of a device mosaic (rawhist module), as a
+    (3, bins) array of counts, sums of means and sums of second moments."""
+    keep = None
+    if d_scratch is None:
+        import torch
+        keep = torch.empty(_lib.lib().vkdt_cuda_rawhist_scratch_bytes(), dtype=torch.uint8, device="cuda")
+        d_scratch = keep.data_ptr()
+    out = np.zeros(3 * bins, np.float64)
+    check(_lib.lib().vkdt_cuda_rawhist(C.c_void_p(d_mosaic), wd, ht, C.byref(img_param), bins, C.c_void_p(d_scratch),
+                                       out.ctypes.data_as(C.POINTER(C.c_double)), C.c_void_p(stream)), "rawhist")
+    return out.reshape(3, bins)
+
+
+def nprof_fit(hist):
+    """vkdt_cuda_nprof_fit: the noise profile (a, b) of a rawhist histogram (nprof module)."""
+    h = np.ascontiguousarray(np.asarray(hist, np.float64).reshape(-1))
+    a, b = C.c_float(), C.c_float()
+    code = _lib.lib().vkdt_cuda_nprof_fit(h.ctypes.data_as(C.POINTER(C.c_double)), h.size // 3, C.byref(a), C.byref(b))
+    if code not in (_lib.SUCCESS, _lib.INCOMPLETE):
+        check(code, "nprof_fit")
+    return a.value, b.value, code == _lib.SUCCESS
+
+
 class Graph:
     """A vkdt processing graph restricted to the development path."""
 

@@ -117,6 +117,9 @@ _SIGS = {
     "vkdt_cuda_graph_set_capture": (C.c_int, [_P, C.c_int]),
     "vkdt_cuda_graph_stream": (_P, [_P]),
     "vkdt_cuda_graph_plan_bytes": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
+    "vkdt_cuda_rawhist_scratch_bytes": (C.c_size_t, []),
+    "vkdt_cuda_rawhist": (C.c_int, [_P, C.c_int, C.c_int, C.POINTER(ImgParam), C.c_int, _P, C.POINTER(C.c_double), _P]),
+    "vkdt_cuda_nprof_fit": (C.c_int, [C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "vkdt_cuda_server_create": (C.c_int, [C.POINTER(ServerCfg), C.POINTER(_P)]),
     "vkdt_cuda_server_submit": (C.c_int, [_P, C.POINTER(Job), C.POINTER(C.c_uint64)]),
     "vkdt_cuda_server_wait": (C.c_int, [_P, C.c_uint64, C.c_uint32]),

@@ -1305,6 +1305,91 @@ int vkdt_cuda_graph_debug_stage(vkdt_cuda_graph_t *g, int stage, float *out, siz
   return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "stage %d", stage);
 }
 
+// ---------------------------------------------------------------- noise statistics
+
+size_t vkdt_cuda_rawhist_scratch_bytes(void) { return rawhist_scratch_bytes(); }
+
+int vkdt_cuda_rawhist(const void *d_mosaic, int wd, int ht, const vkdt_cuda_img_param_t *ip, int bins,
+    void *d_scratch, double *h_out, void *stream)
+{
+  if(!d_mosaic || !ip || !d_scratch || !h_out || wd <= 0 || ht <= 0)
+    return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "bad rawhist arguments");
+  if(bins <= 0 || bins > rawhist_max_bins())
+    return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "rawhist bins %d outside 1..%d", bins, rawhist_max_bins());
+  if(ip->filters == 0) return fail(VKDT_CUDA_INCOMPLETE, "rawhist needs a mosaic");
+  dev_rawhist_t p;
+  memset(&p, 0, sizeof(p));
+  p.mosaic = (const uint16_t *)d_mosaic;
+  p.wd = wd; p.ht = ht; p.pitch = wd;
+  const int block = ip->filters == 9u ? 3 : 2;
+  p.bw = wd / block; p.bh = ht / block;
+  p.filters = ip->filters;
+  // rawhist/main.c:17-28 commit_params: MAX(1, black[1]) and white[1] as uint, /65536 in the shader
+  const uint32_t black = (uint32_t)std::max(1.0f, ip->black[1]), white = (uint32_t)ip->white[1];
+  p.black = (float)black / 65536.0f;
+  p.white = (float)white / 65536.0f;
+  p.bins = bins;
+  p.acc = (unsigned long long *)d_scratch;
+  double *d_out = (double *)((unsigned char *)d_scratch + 3 * rawhist_max_bins() * sizeof(unsigned long long));
+  cudaStream_t st = (cudaStream_t)stream;
+  CU(launch_rawhist(p, d_out, st));
+  CU(cudaMemcpyAsync(h_out, d_out, 3 * (size_t)bins * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CU(cudaStreamSynchronize(st));
+  return 0;
+}
+
+int vkdt_cuda_nprof_fit(const double *h, int wd, float *a_out, float *b_out)
+{ // nprof/main.c:82-198 write_sink: pairs of bins give line fits sigma^2 = a + b x;
+  // a bin is kept once enough of its pairs give a, b > 0; the standard falls by 2x
+  // per round (up to 7) until some bin is kept; then the count weighted regression
+  if(!h || !a_out || !b_out || wd <= 0) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "bad nprof arguments");
+  std::vector<int> valid;
+  float a = 0.0f, b = 0.0f;
+  for(int f = 0; f < 7; f++)
+  {
+    const double fk = 1.0 / std::pow(2.0, f);
+    for(int i = 0; i < wd; i++)
+    {
+      int score = 0;
+      for(int j = i + 1; j < wd * (0.8 - fk); j++)
+      {
+        double c = h[i];
+        if(c < fk * 64) continue;
+        double m1 = h[i + wd], m2 = h[i + 2 * wd];
+        const double x1 = m1 / c, y1 = m2 / c - (m1 / c) * (m1 / c);
+        c = h[j];
+        if(c < fk * 64) continue;
+        m1 = h[j + wd]; m2 = h[j + 2 * wd];
+        const double x2 = m1 / c, y2 = m2 / c - (m1 / c) * (m1 / c);
+        if(y1 <= 0 || y2 <= 0) continue;
+        const double eb = (y2 - y1) / (x2 - x1);
+        const double ea = y1 - x1 * eb;
+        if(!(eb > 0.0)) continue;
+        if(!(ea > 0.0)) continue;
+        if(++score > fk * 32) { a = (float)ea; b = (float)eb; valid.push_back(i); break; }
+      }
+    }
+    if(!valid.empty()) break;
+  }
+  double sx = 0.0, sx2 = 0.0, sy = 0.0, sxy = 0.0, cnt = 0.0;
+  for(int i : valid)
+  {
+    const double c = h[i], m1 = h[i + wd], m2 = h[i + 2 * wd];
+    const double x = m1 / c;
+    const double y = std::max(0.0, m2 / c - m1 / c * m1 / c);
+    cnt += c; sx += x * c; sx2 += x * x * c; sy += y * c; sxy += x * y * c;
+  }
+  const float denom = (float)(cnt * sx2 - sx * sx);
+  if(std::fabs(denom) > 1e-10f)
+  {
+    b = (float)std::max(0.0, (cnt * sxy - sx * sy) / denom);
+    a = (float)std::max(0.0, (sy * sx2 - sx * sxy) / denom);
+  }
+  if(valid.empty()) { a = 100.0f; b = 1.0f; }   // the reference's default when nothing fits
+  *a_out = a; *b_out = b;
+  return valid.empty() ? VKDT_CUDA_INCOMPLETE : 0;
+}
+
 // ---------------------------------------------------------------- scenes
 
 static void scene_layout(const vkdt_cuda_scene_t *sc, scene_layout_t *s)

@@ -125,6 +125,21 @@ cudaError_t launch_nodes(const dev_nodes_t &p, int stage, cudaStream_t s);
 // demosaic output (p.W x p.H = the output size; p.mosaic unused)
 cudaError_t launch_post(const dev_image_t &p, const half4 *dm, cudaStream_t s);
 
+// rawhist noise statistics (k_rawhist.cu)
+struct dev_rawhist_t
+{
+  const uint16_t *mosaic;
+  int wd, ht, pitch;       // mosaic size and row pitch (elements)
+  int bw, bh;              // CFA blocks: wd / block, ht / block
+  uint32_t filters;
+  float black, white;      // collect.comp: black/65536, white/65536 of channel 1
+  int bins;                // histogram width (the reference uses 1000)
+  unsigned long long *acc; // 3 * rawhist_max_bins() fixed point accumulators (device)
+};
+cudaError_t launch_rawhist(const dev_rawhist_t &p, double *d_out, cudaStream_t s);
+size_t rawhist_scratch_bytes();
+int rawhist_max_bins();
+
 // hilite (k_hilite.cu)
 cudaError_t launch_hilite_k1(const dev_hilite_k1_t &p, cudaStream_t s);
 cudaError_t launch_hilite_reduce(const half4 *in, int iw, int ih, half4 *out, int ow, int oh,

@@ -36,6 +36,8 @@ NOISE_A, NOISE_B = 8.0, 1.6
 LEVELS = 6
 RING = 4
 DENOISE = 0.0
+DEMOSAIC = 0          # demosaic method: 0 gaussian splats (the raw photo default), 1 rcd, 2 half size
+DEMOSAIC_NAMES = {0: "gaussian splats (method 0)", 1: "rcd (method 1)", 2: "half size (method 2)"}
 
 
 def img_param(v, wd, ht):
@@ -51,6 +53,7 @@ def config():
             "bits": 14, "black": BLACK, "white": WHITE, "noise_a_dn": NOISE_A, "noise_b_dn": NOISE_B,
             "llap_levels": LEVELS,
             "graph": "denoise(%s)->hilite->demosaic->colour->filmcurv->llap" % ("wavelet" if DENOISE > 0 else "noop"),
+            "demosaic": DEMOSAIC_NAMES[DEMOSAIC],
             "l2": "ring of %d distinct resident mosaics (%d MB > 129 MB L2)" % (RING, RING * WD * HT * 2 // 2 ** 20)}
 
 
@@ -189,11 +192,20 @@ def _per_image(v, torch, imgs, dsts, graphs, outsz=None):
                 g.set_llap_levels(LEVELS)
             if ow:
                 g.set_output_size(ow, oh)
+            if DEMOSAIC:
+                g.set_param("demosaic", "method", np.int32(DEMOSAIC))
             g.alloc()
             graphs[key] = g
         g.set_input(wd, ht, ip)
         g.develop(src.data_ptr(), dsts[k].data_ptr())
         g.wait()
+
+
+def _server(v, slots, method=None):
+    """A develop server on the darkroom graph with the given demosaic method."""
+    method = DEMOSAIC if method is None else method
+    cfg = v.DARKROOM_CFG + ("param:demosaic:01:method:%d\n" % method if method else "")
+    return v.Server(slots=slots, llap_levels=LEVELS, hbm_cap=int(120e9), cfg=cfg)
 
 
 def _served(v, s, imgs, dsts, outsz=None):
@@ -235,7 +247,7 @@ def workload_batch(args, v, torch, sp, clk):
     tune = {}
     best, best_mps = None, 0.0
     for slots in (1, 2, 3, 4, 6):
-        s = v.Server(slots=slots, llap_levels=LEVELS, hbm_cap=int(120e9))
+        s = _server(v, slots)
         _served(v, s, imgs, dsts)
         ms, _, _ = _timed(torch, lambda: _served(v, s, imgs, dsts))
         mps = mp / (ms / 1e3)
@@ -243,7 +255,7 @@ def workload_batch(args, v, torch, sp, clk):
         s.close()
         if mps > best_mps:
             best, best_mps = slots, mps
-    s = v.Server(slots=best, llap_levels=LEVELS, hbm_cap=int(120e9))
+    s = _server(v, best)
     _served(v, s, imgs, dsts)
     s.reset_stats()
     with clk:
@@ -332,7 +344,7 @@ def workload_serve(args, v, torch, sp, clk):
     mp = sum(MIX_SIZES[sz][0] * MIX_SIZES[sz][1] for _, sz, _ in trace) / 1e6
     res = {}
     for name, slots in (("per_image", 1), ("served", args.slots)):
-        s = v.Server(slots=slots, llap_levels=LEVELS, hbm_cap=int(120e9))
+        s = _server(v, slots)
         _replay(v, s, _request_trace(2.0, 50.0, 4), pool, outs)      # warm the pool of graphs
         s.reset_stats()
         if name == "served":
@@ -376,7 +388,11 @@ def workload_video(args, v, torch, sp, clk):
     vout = [[torch.empty(VW * VH * 4, dtype=torch.float16, device="cuda") for _ in range(4)] for _ in range(4)]
     xout = [torch.empty(XW * XH * 4, dtype=torch.float16, device="cuda") for _ in range(4)]
     torch.cuda.synchronize()
-    s = v.Server(slots=args.slots, llap_levels=LEVELS, hbm_cap=int(120e9))
+    # the raw video graphs' demosaic is rcd (bin/default-darkroom.i-mcraw: param:demosaic:01:method:1),
+    # the stills' the raw photo default; one server per graph configuration
+    vmethod = args.demosaic if args.demosaic >= 0 else 1
+    s = _server(v, args.slots, vmethod)
+    sx = _server(v, args.slots, 0) if vmethod else s
 
     def run(paced):
         vid, xid = [], []
@@ -388,7 +404,7 @@ def workload_video(args, v, torch, sp, clk):
                 if f / 24.0 > now:
                     time.sleep(f / 24.0 - now)
             while nst < 25 and nst / 5.0 <= (time.perf_counter() - t0 if paced else f / 24.0):
-                xid.append(s.submit(stills[nst % 2].data_ptr(), xout[nst % 4].data_ptr(), XW, XH, xip))
+                xid.append(sx.submit(stills[nst % 2].data_ptr(), xout[nst % 4].data_ptr(), XW, XH, xip))
                 nst += 1
             ids = [s.submit(frames[k][f].data_ptr(), vout[k][f % 4].data_ptr(), VW, VH, vip) for k in range(4)]
             vid += ids
@@ -396,12 +412,13 @@ def workload_video(args, v, torch, sp, clk):
                 for j in ids:
                     s.wait(j)
         while nst < 25:
-            xid.append(s.submit(stills[nst % 2].data_ptr(), xout[nst % 4].data_ptr(), XW, XH, xip))
+            xid.append(sx.submit(stills[nst % 2].data_ptr(), xout[nst % 4].data_ptr(), XW, XH, xip))
             nst += 1
         s.drain()
+        sx.drain()
         t1 = time.perf_counter()
         lv = sorted(s.job_times(j)[1] for j in vid)
-        lx = sorted(s.job_times(j)[1] for j in xid)
+        lx = sorted(sx.job_times(j)[1] for j in xid)
         mp = (len(vid) * VW * VH + len(xid) * XW * XH) / 1e6
         pct = lambda l, q: l[min(len(l) - 1, max(0, int(np.ceil(q * len(l))) - 1))]
         return {"value": mp / (t1 - t0), "unit": "MP/s", "wall_s": t1 - t0,
@@ -409,12 +426,16 @@ def workload_video(args, v, torch, sp, clk):
                 "still_latency_ms": {"p50": pct(lx, 0.5), "p99": pct(lx, 0.99)}}
     run(False)                               # warm the pool
     s.reset_stats()
+    sx.reset_stats()
     with clk:
         b2b = run(False)
     paced = run(True)
     s.close()
+    if sx is not s:
+        sx.close()
     return {"workload": "4 raw video streams 4096x2160 RGGB 12-bit (black 256, white 4095, a=4, b=0.8, panned 3 px/frame, "
                         "120 frames each) and 25 x-trans 6240x4160 14-bit stills at 5/s",
+            "demosaic": "video: %s, stills: %s" % (DEMOSAIC_NAMES[vmethod], DEMOSAIC_NAMES[0]),
             "modes": "back-to-back (each stream's next frame after its last) and paced at 24 fps"}, \
         b2b["value"], b2b["wall_s"] * 1e3, {"back_to_back": b2b, "paced_24fps": paced,
                                              "latency_ms": {"p99_frame": b2b["frame_latency_ms"]["p99"]}}
@@ -452,7 +473,7 @@ def run_workload(args):
         torch.distributed.destroy_process_group()
 
 def main():
-    global WD, HT, RING, LEVELS, DENOISE
+    global WD, HT, RING, LEVELS, DENOISE, DEMOSAIC
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
@@ -470,9 +491,12 @@ def main():
     ap.add_argument("--images", type=int, default=64, help="batch: mosaics in the batch")
     ap.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
     ap.add_argument("--slots", type=int, default=4, help="serve/video: jobs in flight")
+    ap.add_argument("--demosaic", type=int, default=-1, choices=(-1, 0, 1, 2),
+                    help="demosaic method (-1: the workload's default: 0 for photos, 1 for the video streams)")
     args = ap.parse_args()
     WD, HT = [int(x) for x in args.size.lower().split("x")]
     RING, LEVELS, DENOISE = args.ring, args.levels, args.denoise
+    DEMOSAIC = max(0, args.demosaic)
     if args.impl == "reference":
         return run_reference(args)
     if args.workload != "single":
@@ -502,6 +526,8 @@ def main():
             g.set_llap_levels(LEVELS)
         if DENOISE > 0:
             g.set_param("denoise", "strength", DENOISE)
+        if DEMOSAIC:
+            g.set_param("demosaic", "method", np.int32(DEMOSAIC))
         g.alloc()
         src, _ = g.device_buffers()
         v.scene_device(v.make_scene(WD, HT, seed=1000 * rank + i, image_id=i, a=NOISE_A, b=NOISE_B), src, sp)
@@ -544,6 +570,8 @@ def main():
         gt.set_llap_levels(LEVELS)
     if DENOISE > 0:
         gt.set_param("denoise", "strength", DENOISE)
+    if DEMOSAIC:
+        gt.set_param("demosaic", "method", np.int32(DEMOSAIC))
     gt.set_timing(True)
     gt.alloc()
     src, _ = gt.device_buffers()
@@ -560,25 +588,42 @@ def main():
     names = [x[0] for x in t]
     kms = acc / nt
     launches_per_step = len(names)
-    dev_idx = names.index("demosaic:fix")
+    # the dominant kernel: the fused develop kernel where the graph runs it, else the longest launch
+    dev_idx = names.index("demosaic:fix") if "demosaic:fix" in names else int(np.argmax(kms))
     dev_ms = float(kms[dev_idx])
-    # algorithmic bytes of the fused develop kernel per launch: mosaic in (2 B/px),
-    # the hilite coarse level (8 B per (W/4 x H/4) px), filmcurv rgba f16 out (8 B/px),
-    # 11 llap level 1 planes out (11 * 2 B per (W/2 x H/2) px)
-    npx = WD * HT
-    alg = npx * 2 + (WD // 4) * (HT // 4) * 8 + npx * 8 + 11 * 2 * (WD // 2) * (HT // 2)
+    npx, qpx = WD * HT, (WD // 2) * (HT // 2)
+    # algorithmic bytes per launch (each buffer the launch must read or write, once):
+    alg_bytes = {
+        # fused develop: mosaic in (2 B/px), the hilite coarse level (8 B per (W/4 x H/4) px),
+        # filmcurv rgba f16 out (8 B/px), 11 llap level 1 planes out (11 * 2 B per (W/2 x H/2) px)
+        "demosaic:fix": npx * 2 + (WD // 4) * (HT // 4) * 8 + npx * 8 + 11 * 2 * qpx,
+        # rcd_fill: mosaic, vh, pq + lp (half width) in, rgba f16 out
+        "demosaic:rcd_fill": npx * (2 + 2 + 2 + 8),
+        # rcd_conv: mosaic in, vh, pq + lp out
+        "demosaic:rcd_conv": npx * (2 + 2 + 2),
+        # colour .. llap curve + level 1 reduce of the per-node chain: rgba in, rgba out, 11 planes out
+        "llap:curve": npx * (8 + 8) + 11 * 2 * qpx,
+        # llap level 0 assemble + colour: rgba, 11 level 1 planes, level 1 assembled in, rgba out
+        "llap:colour": npx * (8 + 8) + 11 * 2 * qpx + 2 * qpx,
+    }
+    alg = alg_bytes.get(names[dev_idx])
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else None
     peak = peaks["hbm_gbs"] if peaks else 6800.0
-    achieved = alg / (dev_ms / 1e3) / 1e9
+    achieved = alg / (dev_ms / 1e3) / 1e9 if alg else None
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tp):
+    if os.path.exists(tp) and names[dev_idx] == "demosaic:fix":
         try:
             traffic = json.load(open(tp)).get("k_develop_bytes_per_launch")
         except Exception:
             traffic = None
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "kernel": "k_develop (hilite doub + demosaic + colour + filmcurv + llap curve/reduce)",
+    kname = {"demosaic:fix": "k_develop (hilite doub + demosaic + colour + filmcurv + llap curve/reduce)",
+             "demosaic:rcd_fill": "k_rcd_fill", "demosaic:rcd_conv": "k_rcd_conv",
+             "llap:curve": "k_post (colour + filmcurv + llap curve/reduce)",
+             "llap:colour": "k_llap_final (llap assemble level 0 + colour)"}.get(names[dev_idx], names[dev_idx])
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak if achieved else None,
+                "traffic": traffic, "kernel": kname,
                 "kernel_ms": dev_ms, "alg_bytes_per_launch": alg,
                 "peak_source": "measured" if peaks else "fallback",
                 "per_launch_ms": [[n, round(float(x), 5)] for n, x in zip(names, kms)],

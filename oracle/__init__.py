@@ -85,6 +85,7 @@ def lib():
                                      C.c_int, C.POINTER(C.c_double)]
         l.oracle_f16.restype = C.c_float
         l.oracle_f16.argtypes = [C.c_float]
+        l.oracle_rcd.argtypes = [C.POINTER(C.c_float), C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
         _lib = l
     return _lib
 
@@ -113,8 +114,8 @@ def develop(mosaic, ip, params=None, double=False, stages=("llap",)):
     params = params or default_params()
     W = ip.crop_aabb[2] - ip.crop_aabb[0]
     H = ip.crop_aabb[3] - ip.crop_aabb[1]
-    ow = params.out_wd or W
-    oh = params.out_ht or H
+    ow = params.out_wd or (W if params.dm_method != 2 else (W + 1) // 2)   # method 2 halves the size
+    oh = params.out_ht or (H if params.dm_method != 2 else (H + 1) // 2)
     st = Stages()
     bufs = {}
     for name in stages:
@@ -135,6 +136,16 @@ def develop(mosaic, ip, params=None, double=False, stages=("llap",)):
     bufs["llap_levels"] = st.llap_levels
     bufs["hilite_levels"] = st.hilite_levels
     return bufs
+
+
+def rcd(cfa, wb):
+    """demosaic/rcd_conv + rcd_fill on an f16 bayer mosaic (H x W floats): H x W x 4"""
+    cfa = np.ascontiguousarray(cfa, np.float32)
+    ht, wd = cfa.shape
+    out = np.zeros((ht, wd, 4), np.float32)
+    w = (C.c_float * 3)(*[float(x) for x in wb[:3]])
+    lib().oracle_rcd(_fptr(cfa), wd, ht, w, _fptr(out))
+    return out
 
 
 def noop(mosaic, ip):

@@ -7,6 +7,7 @@ thread_local uvec3 gl_GlobalInvocationID;
 thread_local uvec3 gl_LocalInvocationID;
 thread_local uvec3 gl_WorkGroupID;
 thread_local uint gl_LocalInvocationIndex;
+thread_local int glsl_bar_, glsl_phase_;
 
 float half_to_float(uint16_t h)
 {
@@ -18,7 +19,7 @@ float half_to_float(uint16_t h)
   return s ? -v : v;
 }
 
-static float f16_round(float v)
+float f16_round(float v)
 { // IEEE binary16 round to nearest even
   if(std::isnan(v) || std::isinf(v)) return v;
   const float a = std::fabs(v);

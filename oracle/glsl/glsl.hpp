@@ -300,6 +300,43 @@ inline vec2 unpackHalf2x16(uint u) { return vec2(half_to_float(u & 0xffff), half
 inline uint packHalf2x16(const vec2 &v) { return (uint)float_to_half(v.x) | ((uint)float_to_half(v.y) << 16); }
 template<class A> inline A nonuniformEXT(const A &a) { return a; }
 
+// float16_t (GL_EXT_shader_explicit_arithmetic_types_float16): a value held
+// exactly in binary16. Arithmetic between two float16_t rounds its result to
+// binary16 (computed in FP32 and rounded once more: FP32 has more than 2*11+2
+// bits, so the result is the correctly rounded binary16 one); mixed with
+// float it converts to float.
+float f16_round(float v);
+struct float16_t
+{
+  float v = 0.0f;
+  float16_t() {}
+  explicit float16_t(float x) : v(f16_round(x)) {}
+  explicit float16_t(double x) : v(f16_round((float)x)) {}
+  explicit float16_t(int x) : v(f16_round((float)x)) {}
+  operator float() const { return v; }
+};
+inline float16_t operator+(float16_t a, float16_t b) { return float16_t(a.v + b.v); }
+inline float16_t operator-(float16_t a, float16_t b) { return float16_t(a.v - b.v); }
+inline float16_t operator*(float16_t a, float16_t b) { return float16_t(a.v * b.v); }
+inline float16_t operator/(float16_t a, float16_t b) { return float16_t(a.v / b.v); }
+inline float16_t operator-(float16_t a) { float16_t r; r.v = -a.v; return r; }
+inline float16_t abs(float16_t a) { float16_t r; r.v = std::fabs(a.v); return r; }
+
+// workgroup shared array. An index outside the array is undefined in the
+// reference; here a read returns 0 and a write is dropped.
+template<class T, int N> struct shared_arr
+{
+  T e[N];
+  T oob;
+  T &operator[](long i)
+  {
+    if(i < 0 || i >= N) { oob = T(0); return oob; }
+    return e[i];
+  }
+};
+// barrier phases of the running invocation (translate.py: phases())
+extern thread_local int glsl_bar_, glsl_phase_;
+
 // ------------------------------------------------------------------ images
 struct image_t
 { // row major, c channels of float (values already rounded to the storage format)

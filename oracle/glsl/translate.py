@@ -25,7 +25,7 @@ SHADERS = [
     ("denoise", "assemble"), ("denoise", "doub"),
     ("hilite", "half"), ("hilite", "reduce"), ("hilite", "assemble"), ("hilite", "doub"),
     ("demosaic", "down"), ("demosaic", "gauss"), ("demosaic", "splat"), ("demosaic", "fix"),
-    ("demosaic", "halfsize"), ("shared", "resample"),
+    ("demosaic", "halfsize"), ("demosaic", "rcd_conv"), ("demosaic", "rcd_fill"), ("shared", "resample"),
     ("colour", "main"), ("filmcurv", "main"),
     ("llap", "curve"), ("llap", "reduce"), ("llap", "assemble"), ("llap", "colour"),
 ]
@@ -175,6 +175,8 @@ def translate(module, kernel, moddir):
         blocks.append((kind, inst))
         return block_struct(name, body) + " static %s %s;" % (name, inst)
 
+    ls = re.search(r"layout\s*\(\s*local_size_x\s*=\s*(\d+)\s*,\s*local_size_y\s*=\s*(\d+)[^)]*\)\s*in\s*;", text)
+    local = (int(ls.group(1)), int(ls.group(2))) if ls else (8, 8)
     text = re.sub(r"layout\s*\(([^)]*)\)\s*in\s*;", "", text)
     text = re.sub(r"layout\s*\(([^)]*)\)\s*uniform\s+(\w+)\s*\{(.*?)\}\s*(\w+)\s*;", uniform_block, text, flags=re.S)
 
@@ -187,8 +189,13 @@ def translate(module, kernel, moddir):
 
     text = re.sub(r"layout\s*\(([^)]*)\)\s*uniform\s+((?:writeonly|readonly)\s+)?(sampler2D|usampler2D|image2D|uimage2D)\s+(\w+)\s*(\[\s*\])?\s*;",
                   resource, text, flags=re.S)
-    if re.search(r"\bbuffer\b|\bshared\b", text):
-        raise RuntimeError("%s/%s uses buffers or shared memory (not modelled)" % (module, kernel))
+    if re.search(r"\bbuffer\b", text):
+        raise RuntimeError("%s/%s uses buffers (not modelled)" % (module, kernel))
+    # workgroup shared arrays: one copy per emulation thread, which runs one workgroup at a time
+    text, nshared = re.subn(r"\bshared\s+(\w+)\s+(\w+)\s*\[([^\]]+)\]\s*;",
+                            r"static thread_local shared_arr<\1, (\3)> \2;", text)
+    if re.search(r"\bshared\b", text):
+        raise RuntimeError("%s/%s: shared declaration not understood" % (module, kernel))
     # parameter qualifiers
     text = re.sub(r"\b(?:inout|out)\s+(const\s+)?(\w+)\s+(\w+)", r"\2 &\3", text)
     text = re.sub(r"\bin\s+(const\s+)?(\w+)\s+(\w+)", r"\2 \3", text)
@@ -203,6 +210,9 @@ def translate(module, kernel, moddir):
     # float literals are single precision in GLSL
     text = re.sub(r"(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][-+]?\d+)?|\d+[eE][-+]?\d+)(?![\w.])", r"\1f", text)
     text = re.sub(r"\bvoid\s+main\s*\(\s*\)", "void shader_main()", text)
+    nphase = 1
+    if nshared:
+        text, nphase = phases(text)
     ns = "sh_%s_%s" % (module, kernel)
     entry = ["extern \"C\" void ref_%s_%s(const ref_dispatch_t *dp)" % (module, kernel), "{", "  using namespace %s;" % ns]
     for kind, inst in blocks:
@@ -213,6 +223,27 @@ def translate(module, kernel, moddir):
             entry.append("  for(int e = 0; e < 32; e++) %s[e].im = dp->bind[%d][e];" % (name, b))
         else:
             entry.append("  %s.im = dp->bind[%d][0];" % (name, b))
+    if nshared:
+        LX, LY = local
+        entry += [
+            "  // workgroups: the node size over DT_LOCAL_SIZE (graph-run-nodes-record-cmd.h:377-380)",
+            "  const int GX = (dp->wd + 7) / 8, GY = (dp->ht + 7) / 8, D = dp->dp;",
+            "#pragma omp parallel for collapse(3) schedule(static)",
+            "  for(int z = 0; z < D; z++) for(int wy = 0; wy < GY; wy++) for(int wx = 0; wx < GX; wx++)",
+            "    for(int ph = 0; ph < %d; ph++)" % nphase,
+            "      for(int ly = 0; ly < %d; ly++) for(int lx = 0; lx < %d; lx++)" % (LY, LX),
+            "      {",
+            "        glsl::gl_GlobalInvocationID = glsl::uvec3((glsl::uint)(wx * %d + lx), (glsl::uint)(wy * %d + ly), (glsl::uint)z);" % (LX, LY),
+            "        glsl::gl_LocalInvocationID = glsl::uvec3((glsl::uint)lx, (glsl::uint)ly, 0u);",
+            "        glsl::gl_WorkGroupID = glsl::uvec3((glsl::uint)wx, (glsl::uint)wy, (glsl::uint)z);",
+            "        glsl::gl_LocalInvocationIndex = (glsl::uint)(ly * %d + lx);" % LX,
+            "        glsl::glsl_phase_ = ph;",
+            "        shader_main();",
+            "      }",
+            "}",
+        ]
+        return ("// generated from %s by oracle/glsl/translate.py\n#include \"glsl.hpp\"\n#include <cstring>\n"
+                "namespace %s {\nusing namespace glsl;\n%s\n} // namespace\n%s\n") % (src, ns, text, "\n".join(entry))
     entry += [
         "  const int W = (dp->wd + 7) / 8 * 8, H = (dp->ht + 7) / 8 * 8, D = dp->dp;",
         "#pragma omp parallel for collapse(2) schedule(static)",
@@ -230,6 +261,43 @@ def translate(module, kernel, moddir):
     tu = ("// generated from %s by oracle/glsl/translate.py\n#include \"glsl.hpp\"\n#include <cstring>\n"
           "namespace %s {\nusing namespace glsl;\n%s\n} // namespace\n%s\n") % (src, ns, text, "\n".join(entry))
     return tu
+
+
+def phases(text):
+    """Barriers: a shader whose main body is a prefix of statements followed by
+    compound statements separated by barrier() runs as phases. Every
+    invocation of a workgroup runs phase k before any runs phase k+1; the
+    prefix (invocation ids, an early return) runs in every phase and the k-th
+    top level block only in phase k. Returns (text, number of phases)."""
+    m = re.search(r"void shader_main\(\)\s*\{", text)
+    i = m.end()
+    out = [text[:i], " glsl_bar_ = 0;"]
+    depth, j, nbar, seen_block = 1, i, 0, False
+    while depth:
+        c = text[j]
+        if depth == 1 and text.startswith("barrier();", j):
+            out.append("glsl_bar_++;")
+            nbar += 1
+            j += len("barrier();")
+            continue
+        if c == "{":
+            if depth == 1:
+                prev = text[:j].rstrip()[-1]
+                if prev not in ";{}":
+                    raise RuntimeError("a top level statement other than a block after the prefix")
+                out.append("if(glsl_bar_ == glsl_phase_) ")
+                seen_block = True
+            depth += 1
+        elif c == "}":
+            depth -= 1
+        elif depth == 1 and seen_block and not c.isspace():
+            raise RuntimeError("statements between the barrier phases are not modelled")
+        out.append(c)
+        j += 1
+    out.append(text[j:])
+    if re.search(r"\bbarrier\s*\(", "".join(out)):
+        raise RuntimeError("barrier() below the top level of main is not modelled")
+    return "".join(out), nbar + 1
 
 
 def gen_swizzles():

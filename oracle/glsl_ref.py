@@ -178,8 +178,8 @@ def develop(mosaic, ip, params=None, stages=("llap",)):
     # ---- demosaic (demosaic/main.c:59-203)
     dm_par = i32(p.dm_colour, p.dm_method)
     dpc = f32(*wb) + u32(filters)
-    ow = p.out_wd or W
-    oh = p.out_ht or H
+    ow = p.out_wd or (W if p.dm_method != 2 else (W + 1) // 2)   # demosaic/main.c:18-41
+    oh = p.out_ht or (H if p.dm_method != 2 else (H + 1) // 2)
     scale = W / ow
     if scale >= 1.5 * block or p.dm_method == 2:
         hs = Img(W // block, H // block, 4)
@@ -189,6 +189,13 @@ def develop(mosaic, ip, params=None, stages=("llap",)):
             run("shared_resample", ow, oh, {0: [hs], 1: [rgb]})
         else:
             rgb = hs
+    elif p.dm_method == 1:
+        # demosaic/main.c:113-155: rcd_conv at full size, rcd_fill one workgroup per 58x26 tile
+        vh, pq, lpi = Img(W, H, 1), Img(W // 2, H, 1), Img(W // 2, H, 1)
+        run("demosaic_rcd_conv", W, H, {0: hl, 1: vh, 2: pq, 3: lpi})
+        ntx, nty = (W + 57) // 58, (H + 25) // 26
+        rgb = Img(W, H, 4)
+        run("demosaic_rcd_fill", ntx * 8, nty * 8, {0: hl, 1: vh, 2: pq, 3: lpi, 4: rgb}, push=dpc)
     else:
         down = Img(W // block, H // block, 1)
         run("demosaic_down", W // block, H // block, {0: hl, 1: down}, push=dpc, uniform=dm_par)

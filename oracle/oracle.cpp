@@ -946,6 +946,197 @@ template<class T> static img_t<T> shared_resample(const img_t<T> &in, int wd, in
   return out;
 }
 
+// ------------------------------------------------------------------ demosaic RCD (method 1)
+
+// demosaic/rcd_conv.comp:8-49: per pixel the vertical/horizontal
+// discriminator (vh, full size), per red/blue pixel the diagonal one (pq) and
+// per green pixel the low pass of its red/blue neighbour (lp); pq and lp are
+// half width images indexed by x/2. The mosaic is read through the sampler
+// at texel centres (mirrored outside).
+template<class T> static void rcd_conv(const img_t<T> &cfa, img_t<T> &vh, img_t<T> &pq, img_t<T> &lp)
+{
+  const int wd = cfa.w, ht = cfa.h;
+  vh = img_t<T>(wd, ht, 1); pq = img_t<T>(wd / 2, ht, 1); lp = img_t<T>(wd / 2, ht, 1);
+  OMP_FOR
+  for(int y = 0; y < ht; y++) for(int x = 0; x < wd; x++)
+  {
+    auto c = [&](int i, int j) { return fetch_m(cfa, x + i, y + j, 0); };
+    T s0 = T(0), s1 = T(0);
+    for(int i = -1; i <= 1; i++)
+    {
+      s0 = s0 + (c(i, -3) - T(3) * c(i, -2) - c(i, -1) + T(6) * c(i, 0) - c(i, 1) - T(3) * c(i, 2) + c(i, 3));
+      s1 = s1 + (c(-3, i) - T(3) * c(-2, i) - c(-1, i) + T(6) * c(0, i) - c(1, i) - T(3) * c(2, i) + c(3, i));
+    }
+    s0 = s0 * s0; s1 = s1 * s1;
+    const T v = s0 / (T(1e-5f) + s0 + s1);
+    vh.store(x, y, &v, 1);
+    if(((x + y) & 1) == 0)
+    { // red/blue pixel: diagonal discriminator
+      T p0 = T(1e-5f), p1 = T(1e-5f);
+      for(int i = -1; i <= 1; i++)
+      {
+        p0 = p0 + (c(-3 + i, -3 + i) - c(1 + i, -1 + i) - c(1 + i, 1 + i) + c(3 + i, 3 + i)
+            - T(3) * (c(-2 + i, -2 + i) + c(2 + i, 2 + i)) + T(6) * c(i, i));
+        p1 = p1 + (c(3 + i, -3 - i) - c(1 + i, -1 - i) - c(-1 + i, 1 - i) + c(-3 + i, 3 - i)
+            - T(3) * (c(2 + i, -2 - i) + c(-2 + i, 2 - i)) + T(6) * c(i, -i));
+      }
+      p0 = p0 * p0; p1 = p1 * p1;
+      const T q = p0 / (p0 + p1);
+      pq.store(x / 2, y, &q, 1);
+    }
+    else
+    { // green pixel: 3x3 low pass around the adjacent red/blue pixel of its row
+      const int off = (x & 1) == 1 ? -1 : 1;
+      const T w[3] = { T(0.5), T(1.0), T(0.5) };
+      T l = T(0);
+      for(int j = -1; j <= 1; j++) for(int i = -1; i <= 1; i++)
+        l = l + w[j + 1] * w[i + 1] * c(i + off, j);
+      l = gmax(T(1e-6f), l);
+      lp.store(x / 2, y, &l, 1);
+    }
+  }
+}
+
+// demosaic/rcd_fill.comp:20-162 with the tile geometry of demosaic/config.h:
+// one workgroup of 32x32 invocations per 64x32 tile, each invocation owns a
+// horizontal pixel pair; tiles step by 58x26 (border 3) and only the inner
+// 58x26 pixels are written. The tile lives in three f16 arrays indexed
+// linearly (64 * row + column), so a neighbour offset past a tile edge wraps
+// into the adjacent row; the reference's later two stages each read three
+// pixels out while the border is three, so the invocations of tile rows 0-2
+// and 29-31 index up to three rows outside the arrays. Those reads are
+// undefined in the reference; here they read 0 (as does the CUDA kernel).
+// The results that reach the written pixels never depend on the order of
+// invocations within a stage.
+static inline int rcd_col(int x, int y) { return ((x + y) & 1) == 1 ? 1 : ((y & 1) == 0 ? 0 : 2); }
+template<class T> static img_t<T> rcd_fill(const img_t<T> &cfa, const img_t<T> &vh, const img_t<T> &pq,
+    const img_t<T> &lp, const T wb[3])
+{
+  const int wd = cfa.w, ht = cfa.h;
+  const int TX = 64, TY = 32, BD = 3, SX = TX - 2 * BD, SY = TY - 2 * BD, N = TX * TY;
+  const int ntx = (wd + SX - 1) / SX, nty = (ht + SY - 1) / SY;
+  const T eps = T(1e-5f);
+  img_t<T> out(wd, ht, 4);
+#ifdef _OPENMP
+#pragma omp parallel for collapse(2) schedule(static)
+#endif
+  for(int ty = 0; ty < nty; ty++) for(int tx = 0; tx < ntx; tx++)
+  {
+    std::vector<T> sh(3 * N);   // shm_r, shm_g, shm_b
+    auto S = [&](int c, int i) -> T { return (i < 0 || i >= N) ? T(0) : sh[(size_t)c * N + i]; };
+    auto Sw = [&](int c, int i, T v) { if(i >= 0 && i < N) sh[(size_t)c * N + i] = v; };
+    auto hsub = [](T a, T b) { return f16r(a - b); };   // float16_t - float16_t
+    for(int stage = 0; stage < 5; stage++)
+      for(int ly = 0; ly < 32; ly++) for(int lx = 0; lx < 32; lx++)
+      {
+        const int ix = tx * SX + 2 * lx - BD, iy = ty * SY + ly - BD;   // ipos
+        const int lidx = 2 * lx, lidy = ly;
+        if(stage == 0)
+        { // fill the tile from the mosaic (texelFetch: 0 outside), white balanced
+          for(int k = 0; k < 2; k++)
+          {
+            const int c = rcd_col(ix + k, iy);
+            const T v = gclamp(fetch_z(cfa, ix + k, iy, 0), T(0), T(65535));
+            for(int ch = 0; ch < 3; ch++) Sw(ch, TX * lidy + lidx + k, c == ch ? f16r(wb[ch] * v) : T(0));
+          }
+          continue;
+        }
+        if(stage == 4)
+        { // write the inner pixels
+          for(int k = 0; k < 2; k++)
+          {
+            const int gx = ix + k, lxx = lidx + k;
+            if(lxx >= BD && lidy >= BD && gx < wd && iy < ht && lxx < TX - BD && lidy < TY - BD)
+            {
+              const int i = TX * lidy + lxx;
+              T o[4] = { S(0, i) / wb[0], S(1, i) / wb[1], S(2, i) / wb[2], T(1) };
+              out.store(gx, iy, o, 4);
+            }
+          }
+          continue;
+        }
+        // the pixel of the pair this stage works on: red/blue for stages 1, 2; green for 3
+        const int rbk = rcd_col(ix, iy) == 1 ? 1 : 0;
+        const int k = stage == 3 ? 1 - rbk : rbk;
+        const int tcx = ix + k, tcy = iy;
+        auto ind = [&](int dx, int dy) { return TX * (lidy + dy) + lidx + dx + k; };
+        auto cf = [&](int dx, int dy) { return fetch_z(cfa, tcx + dx, tcy + dy, 0); };
+        auto vhf = [&](int dx, int dy) { return fetch_m(vh, tcx + dx, tcy + dy, 0); };
+        auto half_idx = [&](int dx, int dy) { return (tcx + dx + (((tcy + dy) & 1) == 1 ? 0 : 1)) / 2; };
+        auto pqf = [&](int dx, int dy) { return fetch_m(pq, half_idx(dx, dy), tcy + dy, 0); };
+        auto lpf = [&](int dx, int dy) { return fetch_m(lp, half_idx(dx, dy), tcy + dy, 0); };
+        auto sg = [&](int dx, int dy) { return S(1, ind(dx, dy)); };
+        if(stage == 1)
+        { // green at red/blue pixels
+          const T vhc = vhf(0, 0);
+          const T vhn = T(0.25) * (vhf(-1, -1) + vhf(1, -1) + vhf(-1, 1) + vhf(1, 1));
+          const T vhd = std::fabs(T(0.5) - vhc) < std::fabs(T(0.5) - vhn) ? vhn : vhc;
+          const T Ng = eps + std::fabs(cf(0, -1) - cf(0, 1)) + std::fabs(cf(0, 0) - cf(0, -2))
+                     + std::fabs(cf(0, -1) - cf(0, -3)) + std::fabs(cf(0, -2) - cf(0, -4));
+          const T Sg = eps + std::fabs(cf(0, -1) - cf(0, 1)) + std::fabs(cf(0, 0) - cf(0, 2))
+                     + std::fabs(cf(0, 1) - cf(0, 3)) + std::fabs(cf(0, 2) - cf(0, 4));
+          const T Wg = eps + std::fabs(cf(-1, 0) - cf(1, 0)) + std::fabs(cf(0, 0) - cf(-2, 0))
+                     + std::fabs(cf(-1, 0) - cf(-3, 0)) + std::fabs(cf(-2, 0) - cf(-4, 0));
+          const T Eg = eps + std::fabs(cf(-1, 0) - cf(1, 0)) + std::fabs(cf(0, 0) - cf(2, 0))
+                     + std::fabs(cf(1, 0) - cf(3, 0)) + std::fabs(cf(2, 0) - cf(4, 0));
+          const T l0 = lpf(0, 0);
+          const T Ne = cf(0, -1) * T(2) * l0 / (eps + l0 + lpf(0, -2));
+          const T Se = cf(0, 1) * T(2) * l0 / (eps + l0 + lpf(0, 2));
+          const T We = cf(-1, 0) * T(2) * l0 / (eps + l0 + lpf(-2, 0));
+          const T Ee = cf(1, 0) * T(2) * l0 / (eps + l0 + lpf(2, 0));
+          const T ve = gclamp((Sg * Ne + Ng * Se) / (Ng + Sg), T(0), T(65534));
+          const T he = gclamp((Wg * Ee + Eg * We) / (Eg + Wg), T(0), T(65534));
+          Sw(1, ind(0, 0), f16r(gmix(ve, he, vhd)));
+        }
+        else if(stage == 2)
+        { // blue at red and red at blue pixels, along the diagonals
+          const bool red = rcd_col(tcx, tcy) == 0;
+          const int oc = red ? 2 : 0;
+          auto sc = [&](int dx, int dy) { return S(oc, ind(dx, dy)); };
+          const T pqc = pqf(0, 0);
+          const T pqn = T(0.25) * (pqf(-1, -1) + pqf(1, -1) + pqf(-1, 1) + pqf(1, 1));
+          const T pqd = std::fabs(T(0.5) - pqc) < std::fabs(T(0.5) - pqn) ? pqn : pqc;
+          const T NWg = eps + std::fabs(hsub(sc(-1, -1), sc(1, 1))) + std::fabs(hsub(sc(-1, -1), sc(-3, -3))) + std::fabs(hsub(sg(0, 0), sg(-2, -2)));
+          const T NEg = eps + std::fabs(hsub(sc(1, -1), sc(-1, 1))) + std::fabs(hsub(sc(1, -1), sc(3, -3))) + std::fabs(hsub(sg(0, 0), sg(2, -2)));
+          const T SWg = eps + std::fabs(hsub(sc(1, -1), sc(-1, 1))) + std::fabs(hsub(sc(-1, 1), sc(-3, 3))) + std::fabs(hsub(sg(0, 0), sg(-2, 2)));
+          const T SEg = eps + std::fabs(hsub(sc(-1, -1), sc(1, 1))) + std::fabs(hsub(sc(1, 1), sc(3, 3))) + std::fabs(hsub(sg(0, 0), sg(2, 2)));
+          const T NWe = hsub(sc(-1, -1), sg(-1, -1)), NEe = hsub(sc(1, -1), sg(1, -1));
+          const T SWe = hsub(sc(-1, 1), sg(-1, 1)), SEe = hsub(sc(1, 1), sg(1, 1));
+          const T pe = (NWg * SEe + SEg * NWe) / (NWg + SEg);
+          const T qe = (NEg * SWe + SWg * NEe) / (NEg + SWg);
+          Sw(oc, ind(0, 0), f16r(gclamp(sg(0, 0) + gmix(pe, qe, pqd), T(0), T(65535))));
+        }
+        else
+        { // red and blue at green pixels
+          const T vhc = vhf(0, 0);
+          const T vhn = T(0.25) * (vhf(-1, -1) + vhf(1, -1) + vhf(-1, 1) + vhf(1, 1));
+          const T vhd = std::fabs(T(0.5) - vhc) < std::fabs(T(0.5) - vhn) ? vhn : vhc;
+          const T N1 = eps + std::fabs(hsub(sg(0, 0), sg(0, -2)));
+          const T S1 = eps + std::fabs(hsub(sg(0, 0), sg(0, 2)));
+          const T W1 = eps + std::fabs(hsub(sg(0, 0), sg(-2, 0)));
+          const T E1 = eps + std::fabs(hsub(sg(0, 0), sg(2, 0)));
+          for(int c = 0; c < 2; c++)
+          {
+            const int oc = c == 0 ? 0 : 2;
+            auto sc = [&](int dx, int dy) { return S(oc, ind(dx, dy)); };
+            const T SN = std::fabs(hsub(sc(0, -1), sc(0, 1)));
+            const T EW = std::fabs(hsub(sc(-1, 0), sc(1, 0)));
+            const T Ng = N1 + SN + std::fabs(hsub(sc(0, -1), sc(0, -3)));
+            const T Sg = S1 + SN + std::fabs(hsub(sc(0, 1), sc(0, 3)));
+            const T Wg = W1 + EW + std::fabs(hsub(sc(-1, 0), sc(-3, 0)));
+            const T Eg = E1 + EW + std::fabs(hsub(sc(1, 0), sc(3, 0)));
+            const T Ne = hsub(sc(0, -1), sg(0, -1)), Se = hsub(sc(0, 1), sg(0, 1));
+            const T We = hsub(sc(-1, 0), sg(-1, 0)), Ee = hsub(sc(1, 0), sg(1, 0));
+            const T ve = (Ng * Se + Sg * Ne) / (Ng + Sg);
+            const T he = (Eg * We + Wg * Ee) / (Eg + Wg);
+            Sw(oc, ind(0, 0), f16r(gclamp(sg(0, 0) + gmix(ve, he, vhd), T(0), T(65535))));
+          }
+        }
+      }
+  }
+  return out;
+}
+
 // ------------------------------------------------------------------ colour
 
 // colour/main.c:219-292 commit_params (matrix path) + main-impl.glsl:200-341
@@ -1119,6 +1310,17 @@ extern "C" void oracle_rawhist(const uint16_t *mosaic, int wd, int ht, uint32_t 
     out[bins + i] = (double)sm[i] / 68719476736.0;
     out[2 * bins + i] = (double)s2[i] / 68719476736.0;
   }
+}
+
+extern "C" void oracle_rcd(const float *cfa, int wd, int ht, const float wb[3], float *out)
+{ // demosaic/rcd_conv.comp + rcd_fill.comp on an f16 mosaic (FP32 build)
+  img_t<float> in(wd, ht, 1);
+  for(size_t i = 0; i < (size_t)wd * ht; i++) in.d[i] = cfa[i];
+  img_t<float> vh, pq, lp;
+  rcd_conv(in, vh, pq, lp);
+  const float w[3] = { wb[0], wb[1], wb[2] };
+  img_t<float> o = rcd_fill(in, vh, pq, lp, w);
+  std::memcpy(out, o.d.data(), sizeof(float) * o.d.size());
 }
 
 extern "C" uint32_t oracle_hist_bin(float r, float g, float b)
@@ -1386,7 +1588,9 @@ template<class T> static int develop(const uint16_t *mosaic, int wd, int ht,
   if(st) to_float_ch(hl, 1, st->hilite);
 
   // ---- demosaic (demosaic/main.c:18-203)
-  const int ow = p->out_wd > 0 ? p->out_wd : W, oh = p->out_ht > 0 ? p->out_ht : H;
+  // demosaic/main.c:18-41: method 2 halves the module's output size
+  const int fw = p->dm_method == 2 ? (W + 1) / 2 : W, fh = p->dm_method == 2 ? (H + 1) / 2 : H;
+  const int ow = p->out_wd > 0 ? p->out_wd : fw, oh = p->out_ht > 0 ? p->out_ht : fh;
   const float scale = (float)W / (float)ow;
   const int halfsize = (scale >= 1.5 * block) || (p->dm_method == 2);
   img_t<T> rgb;
@@ -1399,6 +1603,15 @@ template<class T> static int develop(const uint16_t *mosaic, int wd, int ht,
   else
   {
     if(ow != W || oh != H) return 4; // resample after full-size demosaic not covered
+  }
+  if(!halfsize && p->dm_method == 1)
+  { // demosaic/main.c:113-155: RCD (the module runs it whatever the pattern)
+    img_t<T> vh, pq, lp;
+    rcd_conv(hl, vh, pq, lp);
+    rgb = rcd_fill(hl, vh, pq, lp, wb);
+  }
+  else if(!halfsize)
+  {
     img_t<T> cov = demosaic_gauss(hl, W / block, H / block, filters);
     img_t<T> g = demosaic_splat(hl, cov, W, H, filters);
     rgb = demosaic_fix(hl, g, cov, W, H, filters, p->dm_colour);

@@ -102,6 +102,9 @@ uint32_t oracle_hist_bin(float r, float g, float b);
 /* rawhist/collect.comp statistics: out = counts, sums of means, sums of second moments (3*bins) */
 void oracle_rawhist(const uint16_t *mosaic, int wd, int ht, uint32_t filters, float black_dn,
     float white_dn, int bins, double *out);
+/* demosaic/rcd_conv.comp + rcd_fill.comp on an f16 bayer mosaic (W*H floats, even W):
+ * out = W*H*4 rgba */
+void oracle_rcd(const float *cfa, int wd, int ht, const float wb[3], float *out);
 /* CFA colour index at a pixel: 0 red, 1 green, 2 blue (demosaic/splat.comp:167-222) */
 int oracle_cfa_colour(uint32_t filters, int x, int y);
 /* round to IEEE half (RTNE) and back */

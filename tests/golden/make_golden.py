@@ -8,7 +8,7 @@ translate.py looks for it. Every stored stage is an f16 image of the
 reference (stored as float16, which is lossless) with the alpha channel
 dropped.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case names]   (all cases without names)
 """
 import json
 import os
@@ -29,7 +29,10 @@ from golden_cases import CASES, NOISE_A, NOISE_B, img_param, oracle_params, path
 def main():
     if not glsl_ref.build():
         raise SystemExit("the reference shaders could not be compiled (vkdt sources missing)")
+    only = set(sys.argv[1:])
     for name, case in CASES.items():
+        if only and name not in only:
+            continue
         wd, ht, filters, seed, white, overrides, stages = case
         m = v.scene_host(v.make_scene(wd, ht, seed=seed, a=NOISE_A, b=NOISE_B, filters=filters))
         ip = oracle.img_param(img_param(v, wd, ht, filters, white))

@@ -34,11 +34,17 @@ CASES = {
     "bayer_256x192_thumb": (256, 192, BAYER, 10, 16383.0, {"out_wd": 64, "out_ht": 48}, ("demosaic", "llap")),
     "xtrans_132x96": (132, 96, XTRANS, 11, 16383.0, {}, ("hilite", "demosaic", "llap")),
     "xtrans_132x96_wavelet": (132, 96, XTRANS, 12, 16383.0, {"dn_strength": 1.0}, ("denoise", "llap")),
+    # demosaic RCD over 3x4 of the shader's 58x26 tiles (seams included), and with clipping
+    "bayer_140x80_rcd": (140, 80, BAYER, 13, 16383.0, {"dm_method": 1}, ("hilite", "demosaic", "llap")),
+    "bayer_124x58_rcd_clipped": (124, 58, BAYER, 14, 9000.0, {"dm_method": 1}, ("demosaic", "llap")),
+    # demosaic method 2: the half size demosaic at half the output size
+    "bayer_120x90_halfsize": (120, 90, BAYER, 15, 16383.0, {"dm_method": 2}, ("demosaic", "llap")),
 }
 
 # oracle parameter field -> (module, parameter) of the graph configuration
 PARAM_MAP = {
     "dn_strength": ("denoise", "strength"),
+    "dm_method": ("demosaic", "method"),
     "hl_white": ("hilite", "white"),
     "co_exposure": ("colour", "exposure"),
     "fc_contrast": ("filmcurv", "contrast"),

@@ -27,10 +27,11 @@ def test_token_packing():
 
 
 def test_supports():
-    for n, k in [("denoise", "noop"), ("hilite", "reduce"), ("demosaic", "splat"), ("llap", "assemble"), ("OpenDRT", "hist")]:
+    for n, k in [("denoise", "noop"), ("hilite", "reduce"), ("demosaic", "splat"), ("demosaic", "rcd_fill"),
+                 ("llap", "assemble"), ("OpenDRT", "hist")]:
         assert v.supports(n, k)
     assert not v.supports("crop", "main")
-    assert not v.supports("demosaic", "rcd_fill")
+    assert not v.supports("resize", "main")
 
 
 def test_default_params_and_cfg_overrides():
@@ -136,6 +137,32 @@ def test_create_nodes_xtrans():
     assert by[("demosaic", "fix")][2:4] == (6240, 4160)
     fused = [x[5] for x in n]
     assert min(fused) >= 0 and len(set(fused)) >= 20
+
+
+def test_create_nodes_rcd():
+    # demosaic method 1 (demosaic/main.c:113-155): rcd_conv at full size, one rcd_fill
+    # workgroup per 58x26 tile, no gaussian splat nodes; method 2: always half size
+    g = v.Graph()
+    g.set_input(4096, 2160, v.default_img_param(wd=4096, ht=2160))
+    g.set_param("demosaic", "method", 1)
+    g.create_nodes()
+    n = g.nodes()
+    g.close()
+    by = {(a, b): x for x in n for a, b in [x[:2]]}
+    assert by[("demosaic", "rcd_conv")][2:4] == (4096, 2160)
+    assert by[("demosaic", "rcd_fill")][2:4] == ((4096 + 57) // 58 * 8, (2160 + 25) // 26 * 8)
+    assert ("demosaic", "splat") not in by and ("demosaic", "gauss") not in by
+    assert by[("llap", "colour")][2:4] == (4096, 2160)
+    for name, kernel, *_ in n:
+        assert v.supports(name, kernel), (name, kernel)
+    g = v.Graph()
+    g.set_input(4096, 2160, v.default_img_param(wd=4096, ht=2160))
+    g.set_param("demosaic", "method", 2)
+    g.create_nodes()
+    by = {(a, b): x for x in g.nodes() for a, b in [x[:2]]}
+    g.close()
+    assert by[("demosaic", "halfsize")][2:4] == (2048, 1080) and ("shared", "resample") not in by
+    assert by[("llap", "colour")][2:4] == (2048, 1080)
 
 
 def test_create_nodes_thumbnail():

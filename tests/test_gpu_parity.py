@@ -154,6 +154,52 @@ def test_xtrans(gpu, wd, ht, strength):
     check_rgb(g["llap"], r["llap"], de_stage=True)
 
 
+@pytest.mark.parametrize("wd,ht,strength", [(1024, 768, 0.0), (600, 400, 0.0), (130, 78, 0.0), (2000, 1332, 0.0),
+                                            (606, 402, 1.0)])
+def test_rcd(gpu, wd, ht, strength):
+    # demosaic method 1 (rcd_conv + rcd_fill, the default of the raw video graphs): on the same
+    # input the demosaic output equals the oracle's bit for bit (IEEE arithmetic in the shader's
+    # order, the reference's 58x26 tiles with zero reads past the shared tile); the path end to
+    # end within the tolerances
+    m = v.scene_host(v.make_scene(wd, ht, seed=wd + 3))
+    ip = v.default_img_param(wd=wd, ht=ht, noise_a=NA, noise_b=NB)
+    op = oracle.default_params()
+    op.dm_method = 1
+    op.dn_strength = strength
+
+    def setup(g):
+        g.set_param("demosaic", "method", 1)
+        if strength:
+            g.set_param("denoise", "strength", strength)
+    g = _run_graph(m, ip, setup=setup)
+    r = oracle.develop(m, oracle.img_param(ip), params=op, stages=("hilite", "demosaic", "filmcurv", "llap"))
+    # the rcd kernels on the CUDA path's own hilite output: bit for bit
+    want = oracle.rcd(g["hilite"], [ip.whitebalance[k] for k in range(3)])
+    assert np.array_equal(g["demosaic"], want), summary(g["demosaic"], want)
+    # the whole path against the oracle
+    s_h = summary(g["hilite"][..., None], r["hilite"][..., None])
+    assert s_h["flipped_frac"] <= 1e-3 and s_h["mean"] <= 1e-4, s_h
+    # the wavelet denoise's differences (within its tolerance) reach rcd's directional choices
+    flip = 2e-3 if strength == 0.0 else 5e-3
+    check_rgb(g["demosaic"], r["demosaic"], flip=flip)
+    check_rgb(g["filmcurv"], r["filmcurv"], flip=flip, de_stage=True)
+    check_rgb(g["llap"], r["llap"], flip=flip, de_stage=True)
+
+
+def test_halfsize_method(gpu):
+    # demosaic method 2: the half size demosaic at the module's half output size
+    wd, ht = 1000, 742
+    m = v.scene_host(v.make_scene(wd, ht, seed=5))
+    ip = v.default_img_param(wd=wd, ht=ht, noise_a=NA, noise_b=NB)
+    op = oracle.default_params()
+    op.dm_method = 2
+    g = _run_graph(m, ip, setup=lambda g: g.set_param("demosaic", "method", 2))
+    r = oracle.develop(m, oracle.img_param(ip), params=op, stages=("demosaic", "filmcurv", "llap"))
+    assert g["llap"].shape == r["llap"].shape == (371, 500, 4)
+    check_rgb(g["demosaic"], r["demosaic"])
+    check_rgb(g["llap"], r["llap"], de_stage=True)
+
+
 @pytest.mark.parametrize("wd,ht,ow,oh,filters", [(1000, 742, 250, 185, 0x94949494), (2048, 1536, 256, 192, 0x94949494),
                                                  (1000, 742, 333, 247, 0x94949494), (606, 402, 101, 67, 9),
                                                  (1206, 798, 150, 99, 9)])

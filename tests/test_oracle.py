@@ -150,7 +150,7 @@ def _ref_available():
 
 
 @pytest.mark.skipif(not _ref_available(), reason="reference shaders not compiled here (oracle/_ref)")
-@pytest.mark.parametrize("seed", [101, 102, 103])
+@pytest.mark.parametrize("seed", [101, 102, 103, 104])
 def test_oracle_matches_reference_shaders_random(seed):
     from oracle import glsl_ref
     rng = np.random.default_rng(seed)
@@ -163,6 +163,7 @@ def test_oracle_matches_reference_shaders_random(seed):
     p.dn_strength = float(rng.choice([0.0, 0.5, 1.0]))
     p.co_exposure = float(rng.uniform(-1, 1))
     p.ll_clarity = float(rng.uniform(0, 0.6))
+    p.dm_method = 1 if seed == 104 else 0
     st = ("denoise", "hilite", "demosaic", "colour", "filmcurv", "llap")
     a = glsl_ref.develop(m, ip, p, stages=st)
     b = oracle.develop(m, ip, params=p, stages=st)

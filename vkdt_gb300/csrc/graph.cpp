@@ -159,10 +159,12 @@ struct vkdt_cuda_graph_t
   bool wavelet = false;          // denoise strength > 0: the wavelet nodes run before hilite
   int block = 2;                 // CFA block: 2 bayer, 3 x-trans
   bool halfsize = false, resample = false;  // demosaic/halfsize (+ shared/resample) for reduced sizes
-  bool unfused = false;          // x-trans or reduced size: the per-node chain instead of the fused kernel
+  bool rcd = false;              // demosaic method 1 (rcd_conv + rcd_fill) at full size
+  bool unfused = false;          // x-trans, rcd or reduced size: the per-node chain instead of the fused kernel
   std::vector<int64_t> planned_for; // what alloc planned for: a run refuses a graph changed since
   float lut_black = -1.0f, lut_white = -1.0f;  // black/white (DN) the noop code table holds
   size_t off_h0 = 0, off_b0 = 0, off_hl = 0, off_cov = 0, off_g = 0, off_hs = 0, off_dm = 0;
+  size_t off_vh = 0, off_pq = 0, off_lpf = 0;
   size_t off_dnh = 0, off_dnl[4] = { 0, 0, 0, 0 }, off_dna = 0, off_dn = 0, off_idlut = 0;
   unsigned char *arena = nullptr;
   void *h_src = nullptr, *h_sink = nullptr;
@@ -287,14 +289,16 @@ std::vector<int64_t> plan_key(vkdt_cuda_graph_t *g)
   const module_t *dn = g->mod("denoise");
   const int wavelet = dn && dn->f("strength") > 0.0f;
   const int fixup = g->mod("demosaic") ? g->mod("demosaic")->n("colour") : 0;
+  const int method = g->mod("demosaic") ? g->mod("demosaic")->n("method") : 0;
   return { g->in_wd, g->in_ht, g->ip.crop_aabb[0], g->ip.crop_aabb[1], g->ip.crop_aabb[2], g->ip.crop_aabb[3],
-           g->ip.filters, g->req_wd, g->req_ht, g->llap_levels_req, wavelet, g->want_hist, g->debug, fixup };
+           g->ip.filters, g->req_wd, g->req_ht, g->llap_levels_req, wavelet, g->want_hist, g->debug, fixup, method };
 }
 
 int check_supported_params(vkdt_cuda_graph_t *g)
 {
   if(g->mod("demosaic")->n("colour") != 0) return fail(VKDT_CUDA_INCOMPLETE, "demosaic colour (fixup radius) != 0 not supported");
-  if(g->mod("demosaic")->n("method") != 0) return fail(VKDT_CUDA_INCOMPLETE, "demosaic method %d not supported", g->mod("demosaic")->n("method"));
+  const int method = g->mod("demosaic")->n("method");
+  if(method < 0 || method > 2) return fail(VKDT_CUDA_INCOMPLETE, "demosaic method %d not supported", method);
   const int fm = g->mod("filmcurv")->n("colour");
   if(fm != 1 && fm != 3) return fail(VKDT_CUDA_INCOMPLETE, "filmcurv colour mode %d not supported", fm);
   if(g->mod("colour")->f("sat") != 1.0f) return fail(VKDT_CUDA_INCOMPLETE, "colour saturation != 1 not supported");
@@ -377,6 +381,13 @@ size_t plan_arena(vkdt_cuda_graph_t *g)
     {
       g->off_hs = take(hbytes);
       g->off_dm = g->resample ? take((size_t)g->out_w * g->out_h * 8) : g->off_hs;
+    }
+    else if(g->rcd)
+    { // demosaic/main.c:113-125: vh at full size, pq and lp at half width
+      g->off_vh = take((size_t)g->W * g->H * 2);
+      g->off_pq = take((size_t)(g->W / 2) * g->H * 2);
+      g->off_lpf = take((size_t)(g->W / 2) * g->H * 2);
+      g->off_dm = take((size_t)g->W * g->H * 8);
     }
     else
     {
@@ -536,13 +547,29 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
     if((r = mark())) return r;
     CU(launch_nodes(np, 2, s));
     if((r = mark())) return r;
-    const int stages_half[2] = { 6, 7 }, stages_full[3] = { 3, 4, 5 };
-    const int *st = g->halfsize ? stages_half : stages_full;
-    const int nst = g->halfsize ? (g->resample ? 2 : 1) : 3;
-    for(int i = 0; i < nst; i++)
+    if(g->rcd)
+    { // demosaic/rcd_conv, demosaic/rcd_fill
+      dev_rcd_t rp;
+      rp.cfa = np.hl; rp.W = g->W; rp.H = g->H;
+      for(int k = 0; k < 3; k++) rp.wb[k] = g->ip.whitebalance[k];
+      rp.vh = g->at<__half>(g->off_vh); rp.pq = g->at<__half>(g->off_pq); rp.lp = g->at<__half>(g->off_lpf);
+      rp.out = np.dm;
+      for(int stage = 0; stage < 2; stage++)
+      {
+        CU(launch_rcd(rp, stage, s));
+        if((r = mark())) return r;
+      }
+    }
+    else
     {
-      CU(launch_nodes(np, st[i], s));
-      if((r = mark())) return r;
+      const int stages_half[2] = { 6, 7 }, stages_full[3] = { 3, 4, 5 };
+      const int *st = g->halfsize ? stages_half : stages_full;
+      const int nst = g->halfsize ? (g->resample ? 2 : 1) : 3;
+      for(int i = 0; i < nst; i++)
+      {
+        CU(launch_nodes(np, st[i], s));
+        if((r = mark())) return r;
+      }
     }
     dev_image_t dp = d;
     dp.W = g->out_w; dp.H = g->out_h;
@@ -624,6 +651,7 @@ int vkdt_cuda_supports(dt_token_t name, dt_token_t kernel)
     { "denoise", "assemble" }, { "denoise", "doub" }, { "demosaic", "halfsize" }, { "shared", "resample" },
     { "hilite", "half" }, { "hilite", "reduce" }, { "hilite", "assemble" }, { "hilite", "doub" },
     { "demosaic", "down" }, { "demosaic", "gauss" }, { "demosaic", "splat" }, { "demosaic", "fix" },
+    { "demosaic", "rcd_conv" }, { "demosaic", "rcd_fill" },
     { "colour", "main" }, { "filmcurv", "main" }, { "OpenDRT", "hist" },
     { "llap", "curve" }, { "llap", "reduce" }, { "llap", "assemble" }, { "llap", "colour" } };
   for(auto &s : sup) if(tkn(s[0]) == name && tkn(s[1]) == kernel) return 1;
@@ -845,10 +873,13 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
   g->hw = g->W / g->block; g->hh = g->H / g->block;
   // demosaic/main.c:18-41, 92-111: a requested size of 1/(1.5 block) or less
   // takes the half size demosaic, resampled unless the scale is the block
+  const int method = g->mod("demosaic")->n("method");
   {
-    const int ow = g->req_wd > 0 ? g->req_wd : g->W, oh = g->req_ht > 0 ? g->req_ht : g->H;
+    // method 2 always takes the half size demosaic; its full output size is then (W+1)/2
+    const int fw = method == 2 ? (g->W + 1) / 2 : g->W, fh = method == 2 ? (g->H + 1) / 2 : g->H;
+    const int ow = g->req_wd > 0 ? g->req_wd : fw, oh = g->req_ht > 0 ? g->req_ht : fh;
     const float scale = (float)g->W / (float)ow;
-    g->halfsize = (ow != g->W || oh != g->H) && scale >= 1.5f * g->block;
+    g->halfsize = method == 2 || ((ow != g->W || oh != g->H) && scale >= 1.5f * g->block);
     if(!g->halfsize && (ow != g->W || oh != g->H))
       return fail(VKDT_CUDA_INCOMPLETE, "resampling after the full size demosaic is not built in this version");
     g->resample = g->halfsize && (float)g->block != scale;
@@ -856,8 +887,11 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
     else if(g->resample) { g->out_w = ow; g->out_h = oh; }
     else { g->out_w = g->hw; g->out_h = g->hh; }
   }
-  // bayer at full size runs fused; x-trans and reduced sizes run node by node
-  g->unfused = xt || g->halfsize;
+  // demosaic/main.c:113: rcd at full size, whatever the pattern (its tiles need an even width)
+  g->rcd = method == 1 && !g->halfsize;
+  if(g->rcd && (g->W & 1)) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "rcd needs an even width");
+  // bayer at full size runs fused; x-trans, rcd and reduced sizes run node by node
+  g->unfused = xt || g->halfsize || g->rcd;
 
   // node lists as the modules' create_nodes emit them
   g->wavelet = g->mod("denoise")->f("strength") > 0.0f;
@@ -891,6 +925,11 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
   { // demosaic/main.c:92-111
     add_node(g, "demosaic", "halfsize", g->hw, g->hh, 1, -1);
     if(g->resample) add_node(g, "shared", "resample", OW, OH, 1, -1);
+  }
+  else if(g->rcd)
+  { // demosaic/main.c:113-155: one rcd_fill workgroup (8 invocations of the node size) per 58x26 tile
+    add_node(g, "demosaic", "rcd_conv", g->W, g->H, 1, -1);
+    add_node(g, "demosaic", "rcd_fill", (g->W + 57) / 58 * 8, (g->H + 25) / 26 * 8, 1, -1);
   }
   else
   { // demosaic/main.c:159-202 (gaussian splats, full size)
@@ -930,6 +969,7 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
   }
   std::vector<int> L_hr, L_ha, L_lr, L_la;
   int L_noop = -1, L_half = -1, L_a0 = -1, L_doub = -1, L_gauss = -1, L_splat = -1, L_fix = -1, L_hs = -1, L_rs = -1;
+  int L_rcdc = -1, L_rcdf = -1;
   int L_post, L_k1 = -1;
   if(!g->unfused)
   {
@@ -950,6 +990,11 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
     {
       L_hs = launch("demosaic", "halfsize");
       if(g->resample) L_rs = launch("shared", "resample");
+    }
+    else if(g->rcd)
+    {
+      L_rcdc = launch("demosaic", "rcd_conv");
+      L_rcdf = launch("demosaic", "rcd_fill");
     }
     else
     {
@@ -981,6 +1026,8 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
     else if(n.name == tkn("hilite")) n.fused = n.kernel == tkn("half") ? L_half : L_doub;
     else if(n.kernel == tkn("halfsize")) n.fused = L_hs;
     else if(n.kernel == tkn("resample")) n.fused = L_rs;
+    else if(n.kernel == tkn("rcd_conv")) n.fused = L_rcdc;
+    else if(n.kernel == tkn("rcd_fill")) n.fused = L_rcdf;
     else if(n.kernel == tkn("gauss") || n.kernel == tkn("down")) n.fused = L_gauss;
     else if(n.kernel == tkn("splat")) n.fused = L_splat;
     else if(n.kernel == tkn("fix")) n.fused = L_fix;

@@ -125,6 +125,19 @@ cudaError_t launch_nodes(const dev_nodes_t &p, int stage, cudaStream_t s);
 // demosaic output (p.W x p.H = the output size; p.mosaic unused)
 cudaError_t launch_post(const dev_image_t &p, const half4 *dm, cudaStream_t s);
 
+// demosaic RCD (k_rcd.cu): rcd_conv (stage 0) and rcd_fill (stage 1) on the
+// bayer hilite output, W x H (even W)
+struct dev_rcd_t
+{
+  const __half *cfa;     // hilite/doub output mosaic, W*H
+  int W, H;
+  float wb[3];           // white balance of the image (the shader's push.wb)
+  __half *vh;            // vertical/horizontal discriminator, W*H
+  __half *pq, *lp;       // diagonal discriminator and low pass, (W/2)*H
+  half4 *out;            // demosaic output, W*H
+};
+cudaError_t launch_rcd(const dev_rcd_t &p, int stage, cudaStream_t s);
+
 // rawhist noise statistics (k_rawhist.cu)
 struct dev_rawhist_t
 {

@@ -259,6 +259,16 @@ int  vkdt_cuda_graph_hist(vkdt_cuda_graph_t *graph, uint32_t *hist257);
  * (cleared by the call) */
 int  vkdt_cuda_hist_rgba_f16(const void *d_rgba, int wd, int ht, uint32_t *d_hist257, void *stream);
 
+/* Ingestion of packed raw video (replaces the host unpack of i-mlv/video_mlv.c:254-274,
+ * called from read_source at i-mlv/main.c:204-211 through read_frame at main.c:76-85):
+ * d_packed holds an uncompressed magic lantern frame of `bytes` bytes (16-bit aligned) with
+ * bits_per_pixel 10, 12, 14 or 16; d_mosaic (wd*ht u16, e.g. a graph's device source from
+ * vkdt_cuda_graph_device_buffers) receives the samples. Asynchronous on `stream`.
+ * VK_ERROR_FORMAT_NOT_SUPPORTED for another bit depth, an unaligned pointer or a frame
+ * shorter than wd*ht*bits_per_pixel/8 bytes. */
+int  vkdt_cuda_unpack_mlv(const void *d_packed, size_t bytes, int bits_per_pixel, int wd, int ht, void *d_mosaic,
+                          void *stream);
+
 /* ---- noise statistics and the noise profile fit (rawhist and nprof modules)
  *
  * rawhist/collect.comp:22-66 over a device mosaic (uint16, row pitch = wd):

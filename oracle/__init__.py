@@ -85,6 +85,8 @@ def lib():
                                      C.c_int, C.POINTER(C.c_double)]
         l.oracle_f16.restype = C.c_float
         l.oracle_f16.argtypes = [C.c_float]
+        l.oracle_unpack_mlv.argtypes = [C.c_void_p, C.c_size_t, C.c_int, C.c_size_t, C.c_void_p]
+        l.oracle_pack_mlv.argtypes = [C.c_void_p, C.c_size_t, C.c_int, C.c_void_p, C.c_size_t]
         l.oracle_rcd.argtypes = [C.POINTER(C.c_float), C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
         _lib = l
     return _lib
@@ -145,6 +147,25 @@ def rcd(cfa, wb):
     out = np.zeros((ht, wd, 4), np.float32)
     w = (C.c_float * 3)(*[float(x) for x in wb[:3]])
     lib().oracle_rcd(_fptr(cfa), wd, ht, w, _fptr(out))
+    return out
+
+
+def mlv_bytes(npix, bpp):
+    """bytes of an uncompressed magic lantern frame (video_mlv.c:630)"""
+    return npix * bpp // 8
+
+
+def unpack_mlv(packed, bpp, npix):
+    packed = np.ascontiguousarray(packed, np.uint8)
+    out = np.zeros(npix, np.uint16)
+    lib().oracle_unpack_mlv(packed.ctypes.data, packed.size, bpp, npix, out.ctypes.data)
+    return out
+
+
+def pack_mlv(values, bpp):
+    values = np.ascontiguousarray(values, np.uint16).ravel()
+    out = np.zeros(mlv_bytes(values.size, bpp), np.uint8)
+    lib().oracle_pack_mlv(values.ctypes.data, values.size, bpp, out.ctypes.data, out.size)
     return out
 
 

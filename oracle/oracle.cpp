@@ -1312,6 +1312,49 @@ extern "C" void oracle_rawhist(const uint16_t *mosaic, int wd, int ht, uint32_t 
   }
 }
 
+// i-mlv/video_mlv.c:254-274: an uncompressed magic lantern frame. Pixel i
+// is read as the 32-bit little-endian word of the 16-bit words (i*bpp)/16
+// and (i*bpp)/16 + 1, rotated right by 16 + (32 - bpp) - (i*bpp)%16 and
+// masked to bpp bits. The rotation amount reaches 38; the shift pair the
+// reference writes compiles to a rotate, whose amount counts modulo 32.
+static inline uint32_t mlv_word(const uint8_t *p, size_t bytes, size_t w)
+{
+  return 2 * w + 1 < bytes ? (uint32_t)p[2 * w] | ((uint32_t)p[2 * w + 1] << 8) : 0u;
+}
+extern "C" void oracle_unpack_mlv(const uint8_t *packed, size_t bytes, int bpp, size_t npix, uint16_t *out)
+{
+  const uint32_t mask = bpp >= 32 ? 0xffffffffu : (1u << bpp) - 1u;
+  for(size_t i = 0; i < npix; i++)
+  {
+    const uint64_t off = (uint64_t)i * (uint64_t)bpp;
+    const size_t a = (size_t)(off / 16);
+    const uint32_t sh = (uint32_t)(off % 16);
+    const uint32_t r = (16u + (32u - (uint32_t)bpp) - sh) & 31u;
+    const uint32_t u = mlv_word(packed, bytes, a) | (mlv_word(packed, bytes, a + 1) << 16);
+    const uint32_t d = r ? (u >> r) | (u << (32 - r)) : u;
+    out[i] = (uint16_t)(d & mask);
+  }
+}
+// the inverse (test data): the bits unpack_mlv reads for each pixel, set from its value
+extern "C" void oracle_pack_mlv(const uint16_t *in, size_t npix, int bpp, uint8_t *packed, size_t bytes)
+{
+  memset(packed, 0, bytes);
+  for(size_t i = 0; i < npix; i++)
+  {
+    const uint64_t off = (uint64_t)i * (uint64_t)bpp;
+    const size_t a = (size_t)(off / 16);
+    const uint32_t r = (16u + (32u - (uint32_t)bpp) - (uint32_t)(off % 16)) & 31u;
+    for(int k = 0; k < bpp; k++)
+    {
+      if(!((in[i] >> k) & 1)) continue;
+      const uint32_t pos = (r + (uint32_t)k) & 31u;
+      const size_t w = pos < 16 ? a : a + 1;
+      const size_t byte = 2 * w + ((pos & 15) >> 3);
+      if(byte < bytes) packed[byte] |= (uint8_t)(1u << (pos & 7));
+    }
+  }
+}
+
 extern "C" void oracle_rcd(const float *cfa, int wd, int ht, const float wb[3], float *out)
 { // demosaic/rcd_conv.comp + rcd_fill.comp on an f16 mosaic (FP32 build)
   img_t<float> in(wd, ht, 1);

@@ -105,6 +105,10 @@ void oracle_rawhist(const uint16_t *mosaic, int wd, int ht, uint32_t filters, fl
 /* demosaic/rcd_conv.comp + rcd_fill.comp on an f16 bayer mosaic (W*H floats, even W):
  * out = W*H*4 rgba */
 void oracle_rcd(const float *cfa, int wd, int ht, const float wb[3], float *out);
+/* i-mlv/video_mlv.c:254-274: unpack an uncompressed magic lantern raw frame of
+ * bpp bits per pixel (10, 12, 14, 16) into npix u16 values; and its inverse */
+void oracle_unpack_mlv(const uint8_t *packed, size_t bytes, int bpp, size_t npix, uint16_t *out);
+void oracle_pack_mlv(const uint16_t *in, size_t npix, int bpp, uint8_t *packed, size_t bytes);
 /* CFA colour index at a pixel: 0 red, 1 green, 2 blue (demosaic/splat.comp:167-222) */
 int oracle_cfa_colour(uint32_t filters, int x, int y);
 /* round to IEEE half (RTNE) and back */

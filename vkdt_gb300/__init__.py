@@ -98,6 +98,13 @@ def scene_device(scene, d_ptr, stream=0):
           "vkdt_cuda_scene_generate")
 
 
+def unpack_mlv(d_packed, nbytes, bits_per_pixel, wd, ht, d_mosaic, stream=0):
+    """vkdt_cuda_unpack_mlv: an uncompressed magic lantern frame (device bytes) into a
+    device u16 mosaic of wd x ht (i-mlv's host unpack, on the device)."""
+    check(_lib.lib().vkdt_cuda_unpack_mlv(C.c_void_p(d_packed), nbytes, bits_per_pixel, wd, ht, C.c_void_p(d_mosaic),
+                                          C.c_void_p(stream)), "unpack_mlv")
+
+
 def rawhist(d_mosaic, wd, ht, img_param, bins=1000, d_scratch=None, stream=0):
     """vkdt_cuda_rawhist: noise statistics of a device mosaic (rawhist module), as a
     (3, bins) array of counts, sums of means and sums of second moments."""

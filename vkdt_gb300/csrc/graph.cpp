@@ -161,6 +161,7 @@ struct vkdt_cuda_graph_t
   bool halfsize = false, resample = false;  // demosaic/halfsize (+ shared/resample) for reduced sizes
   bool rcd = false;              // demosaic method 1 (rcd_conv + rcd_fill) at full size
   bool unfused = false;          // x-trans, rcd or reduced size: the per-node chain instead of the fused kernel
+  bool k1front = false;          // bayer per-node chain: the fused path's hilite front (k1, pyramid, one kernel to doub)
   std::vector<int64_t> planned_for; // what alloc planned for: a run refuses a graph changed since
   float lut_black = -1.0f, lut_white = -1.0f;  // black/white (DN) the noop code table holds
   size_t off_h0 = 0, off_b0 = 0, off_hl = 0, off_cov = 0, off_g = 0, off_hs = 0, off_dm = 0;
@@ -371,11 +372,14 @@ size_t plan_arena(vkdt_cuda_graph_t *g)
   }
   // the (denoised) normalised mosaic: wavelet output, or the noop output of the per-node chain
   if(g->wavelet || g->unfused) g->off_dn = take((size_t)g->W * g->H * 2);
-  if(g->wavelet && !g->unfused) g->off_idlut = take(65536 * 2);
+  if(g->wavelet && (!g->unfused || g->k1front)) g->off_idlut = take(65536 * 2);
   if(g->unfused)
   { // the per-node chain's images (intermediate f16 images like the reference's)
-    g->off_h0 = take(hbytes);
-    g->off_b0 = take(hbytes);
+    if(!g->k1front)
+    {
+      g->off_h0 = take(hbytes);
+      g->off_b0 = take(hbytes);
+    }
     g->off_hl = take((size_t)g->W * g->H * 2);
     if(g->halfsize)
     {
@@ -452,6 +456,11 @@ void fill_nodes(vkdt_cuda_graph_t *g, dev_nodes_t &p, const void *d_src)
   p.g = g->at<__half>(g->off_g);
   p.hs = g->at<half4>(g->off_hs);
   p.dm = g->at<half4>(g->off_dm);
+  const level_t &c = g->hb.empty() ? g->hr[0] : g->hb[0];
+  p.coarse = g->at<half4>(c.off); p.ccw = c.w; p.cch = c.h;
+  p.hl_soft = g->mod("hilite")->f("soft");
+  // the bayer front writes the noop output only for the debug stage (the wavelet writes its own)
+  if(g->k1front && (g->wavelet || !g->debug)) p.dn = nullptr;
 }
 
 // the kernel sequence of one run. ev != null records timing events around each launch.
@@ -463,7 +472,8 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
   dev_denoise_t dd;
   if(g->wavelet)
     fill_denoise(g, dd, d_src);
-  if(g->wavelet && !g->unfused)
+  const bool k1 = !g->unfused || g->k1front;   // the hilite front of the fused path
+  if(g->wavelet && k1)
   { // the develop kernels read the denoised f16 mosaic through the identity code table
     d.mosaic = reinterpret_cast<const uint16_t *>(dd.dn);
     d.noop_lut = g->at<__half>(g->off_idlut);
@@ -494,8 +504,12 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
     }
   dev_nodes_t np;
   if(g->unfused)
-  { // 1'. denoise/noop (unless the wavelet ran), hilite half, all hilite reduce levels
+  {
     fill_nodes(g, np, d_src);
+    if(k1) { np.mosaic = d.mosaic; np.noop_lut = d.noop_lut; np.pitch = d.pitch; np.cx = d.cx; np.cy = d.cy; }
+  }
+  if(!k1)
+  { // 1'. denoise/noop (unless the wavelet ran), hilite half, all hilite reduce levels
     if(!g->wavelet)
     {
       CU(launch_nodes(np, 0, s));
@@ -542,11 +556,19 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
   }
   if(g->unfused)
   { // 4'. hilite level 0 assemble, doub, demosaic, colour .. first llap reduce
-    const level_t &c = g->hb.empty() ? g->hr[0] : g->hb[0];
-    CU(launch_hilite_assemble(np.h0, g->hw, g->hh, g->at<half4>(c.off), c.w, c.h, g->at<half4>(g->off_b0), white, soft, s));
-    if((r = mark())) return r;
-    CU(launch_nodes(np, 2, s));
-    if((r = mark())) return r;
+    if(g->k1front)
+    { // noop + half + level 0 assemble + doub in one pass over the mosaic
+      CU(launch_nodes(np, 8, s));
+      if((r = mark())) return r;
+    }
+    else
+    {
+      const level_t &c = g->hb.empty() ? g->hr[0] : g->hb[0];
+      CU(launch_hilite_assemble(np.h0, g->hw, g->hh, g->at<half4>(c.off), c.w, c.h, g->at<half4>(g->off_b0), white, soft, s));
+      if((r = mark())) return r;
+      CU(launch_nodes(np, 2, s));
+      if((r = mark())) return r;
+    }
     if(g->rcd)
     { // demosaic/rcd_conv, demosaic/rcd_fill
       dev_rcd_t rp;
@@ -890,8 +912,10 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
   // demosaic/main.c:113: rcd at full size, whatever the pattern (its tiles need an even width)
   g->rcd = method == 1 && !g->halfsize;
   if(g->rcd && (g->W & 1)) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "rcd needs an even width");
-  // bayer at full size runs fused; x-trans, rcd and reduced sizes run node by node
+  // bayer at full size runs fused; x-trans, rcd and reduced sizes run node by node,
+  // bayer with the fused path's hilite front
   g->unfused = xt || g->halfsize || g->rcd;
+  g->k1front = g->unfused && !xt;
 
   // node lists as the modules' create_nodes emit them
   g->wavelet = g->mod("denoise")->f("strength") > 0.0f;
@@ -971,20 +995,24 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
   int L_noop = -1, L_half = -1, L_a0 = -1, L_doub = -1, L_gauss = -1, L_splat = -1, L_fix = -1, L_hs = -1, L_rs = -1;
   int L_rcdc = -1, L_rcdf = -1;
   int L_post, L_k1 = -1;
-  if(!g->unfused)
+  const bool k1 = !g->unfused || g->k1front;
+  if(k1)
   {
     L_k1 = launch("hilite", "reduce");
     for(size_t l = 1; l < g->hr.size(); l++) L_hr.push_back(launch("hilite", "reduce"));
     for(size_t l = 0; l < g->hb.size(); l++) L_ha.push_back(launch("hilite", "assemble"));
-    L_post = launch("demosaic", "fix");
   }
+  if(!g->unfused) L_post = launch("demosaic", "fix");
   else
   {
-    if(!g->wavelet) L_noop = launch("denoise", "noop");
-    L_half = launch("hilite", "half");
-    for(size_t l = 0; l < g->hr.size(); l++) L_hr.push_back(launch("hilite", "reduce"));
-    for(size_t l = 0; l < g->hb.size(); l++) L_ha.push_back(launch("hilite", "assemble"));
-    L_a0 = launch("hilite", "assemble");
+    if(!k1)
+    {
+      if(!g->wavelet) L_noop = launch("denoise", "noop");
+      L_half = launch("hilite", "half");
+      for(size_t l = 0; l < g->hr.size(); l++) L_hr.push_back(launch("hilite", "reduce"));
+      for(size_t l = 0; l < g->hb.size(); l++) L_ha.push_back(launch("hilite", "assemble"));
+      L_a0 = launch("hilite", "assemble");
+    }
     L_doub = launch("hilite", "doub");
     if(g->halfsize)
     {
@@ -1022,8 +1050,8 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
       if(n.name == tkn("hilite") && n.kernel == tkn("half")) n.fused = L_k1;
       continue;
     }
-    if(n.name == tkn("denoise")) n.fused = L_noop;
-    else if(n.name == tkn("hilite")) n.fused = n.kernel == tkn("half") ? L_half : L_doub;
+    if(n.name == tkn("denoise")) n.fused = k1 ? L_doub : L_noop;
+    else if(n.name == tkn("hilite")) n.fused = n.kernel == tkn("half") ? (k1 ? L_k1 : L_half) : L_doub;
     else if(n.kernel == tkn("halfsize")) n.fused = L_hs;
     else if(n.kernel == tkn("resample")) n.fused = L_rs;
     else if(n.kernel == tkn("rcd_conv")) n.fused = L_rcdc;
@@ -1036,8 +1064,8 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
   // per level nodes (reduce and assemble pairs in create_nodes order)
   for(size_t l = 0; l < g->hr.size(); l++)
   {
-    const int lr = g->unfused ? L_hr[l] : (l == 0 ? L_k1 : L_hr[l - 1]);
-    const int la = l == 0 ? (g->unfused ? L_a0 : L_post) : L_ha[l - 1];
+    const int lr = !k1 ? L_hr[l] : (l == 0 ? L_k1 : L_hr[l - 1]);
+    const int la = l == 0 ? (!g->unfused ? L_post : (k1 ? L_doub : L_a0)) : L_ha[l - 1];
     add_node(g, "hilite", "reduce", g->hr[l].w, g->hr[l].h, 1, lr);
     const int fw = l == 0 ? g->hw : g->hr[l - 1].w, fh = l == 0 ? g->hh : g->hr[l - 1].h;
     add_node(g, "hilite", "assemble", fw, fh, 1, la);
@@ -1064,7 +1092,7 @@ int vkdt_cuda_graph_alloc(vkdt_cuda_graph_t *g, uint64_t *device_bytes)
   g->arena_bytes = plan_arena(g);
   CU(cudaMalloc((void **)&g->arena, g->arena_bytes));
   CU(cudaMemset(g->arena, 0, g->arena_bytes));
-  if(g->wavelet && !g->unfused)
+  if(g->wavelet && (!g->unfused || g->k1front))
   {
     std::vector<uint16_t> id(65536);
     for(int v = 0; v < 65536; v++) id[v] = (uint16_t)v;
@@ -1353,6 +1381,22 @@ int vkdt_cuda_graph_debug_stage(vkdt_cuda_graph_t *g, int stage, float *out, siz
 }
 
 // ---------------------------------------------------------------- noise statistics
+
+int vkdt_cuda_unpack_mlv(const void *d_packed, size_t bytes, int bits_per_pixel, int wd, int ht, void *d_mosaic,
+                         void *stream)
+{
+  if(bits_per_pixel != 10 && bits_per_pixel != 12 && bits_per_pixel != 14 && bits_per_pixel != 16)
+    return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "unpack_mlv: %d bits per pixel", bits_per_pixel);
+  if(!d_packed || !d_mosaic || wd <= 0 || ht <= 0)
+    return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "unpack_mlv: null buffer or empty frame");
+  if(((uintptr_t)d_packed & 1) || ((uintptr_t)d_mosaic & 1))
+    return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "unpack_mlv: buffers must be 16-bit aligned");
+  const size_t npix = (size_t)wd * ht;
+  if(bytes < npix * (size_t)bits_per_pixel / 8)   // video_mlv.c:213 raw_frame_size
+    return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "unpack_mlv: %zu bytes for %zu samples of %d bits", bytes, npix, bits_per_pixel);
+  CU(launch_unpack_mlv(d_packed, bytes, bits_per_pixel, npix, (uint16_t *)d_mosaic, (cudaStream_t)stream));
+  return VKDT_CUDA_SUCCESS;
+}
 
 size_t vkdt_cuda_rawhist_scratch_bytes(void) { return rawhist_scratch_bytes(); }
 

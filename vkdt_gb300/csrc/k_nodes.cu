@@ -123,6 +123,48 @@ template<bool XT> __global__ void __launch_bounds__(256) k_nd_hl_doub(const dev_
   }
 }
 
+// denoise/noop, hilite/half, the level 0 hilite/assemble and hilite/doub of a
+// bayer block at once, from the mosaic through the code table and the
+// assembled level 1 of the hilite pyramid: the first stage of the fused
+// develop kernel, for the demosaic methods that run node by node after it.
+// doub changes a block only where its largest sample exceeds 0.97 white;
+// elsewhere the block is the noop output as it is.
+__global__ void __launch_bounds__(256) k_nd_hl_bayer(const dev_nodes_t p)
+{
+  const int x = blockIdx.x * 16 + threadIdx.x % 16, y = blockIdx.y * 16 + threadIdx.x / 16;
+  if(x >= p.hw || y >= p.hh) return;
+  const uint16_t *row = p.mosaic + (size_t)(2 * y + p.cy) * p.pitch + 2 * x + p.cx;
+  float m[4];
+  m[0] = h2f(__ldg(p.noop_lut + __ldg(row)));
+  m[1] = h2f(__ldg(p.noop_lut + __ldg(row + 1)));
+  m[2] = h2f(__ldg(p.noop_lut + __ldg(row + p.pitch)));
+  m[3] = h2f(__ldg(p.noop_lut + __ldg(row + p.pitch + 1)));
+  float o[4] = { m[0], m[1], m[2], m[3] };
+  const float white = p.hl_white;
+  if(fmaxf(fmaxf(m[2], m[3]), fmaxf(m[1], m[0])) > 0.97f * white)
+  {
+    float h[4];
+    hilite_half_bayer(m[0], m[1], m[2], m[3], white, h);
+    h[3] = 1.0f;
+    float up[3];
+    hilite_expand_px([&](int ix, int iy, float rgb[3]) {
+        float a;
+        ld_half4(p.coarse + (size_t)mirror(iy, p.cch) * p.ccw + mirror(ix, p.ccw), rgb[0], rgb[1], rgb[2], a);
+      }, x, y, up);
+    float b0[3];
+    hilite_assemble_px(h, up, white, p.hl_soft, b0);
+    hilite_doub_bayer(m[0], m[1], m[2], m[3], b0, white, o);
+  }
+  const size_t o0 = (size_t)(2 * y) * p.W + 2 * x;
+  p.hl[o0] = f2h(o[0]); p.hl[o0 + 1] = f2h(o[1]);
+  p.hl[o0 + p.W] = f2h(o[2]); p.hl[o0 + p.W + 1] = f2h(o[3]);
+  if(p.dn)
+  {
+    p.dn[o0] = f2h(m[0]); p.dn[o0 + 1] = f2h(m[1]);
+    p.dn[o0 + p.W] = f2h(m[2]); p.dn[o0 + p.W + 1] = f2h(m[3]);
+  }
+}
+
 // demosaic/gauss.comp:19-126 (x-trans): structure tensor of the 5 greens of
 // each 3x3 block, the form with the smaller determinant decomposed; the
 // eigenvector snapped to an axis when it is within a factor 2 of it, else an
@@ -432,6 +474,7 @@ cudaError_t launch_nodes(const dev_nodes_t &p, int stage, cudaStream_t s)
     case 5: k_nd_fix_xt<<<gf, 256, 0, s>>>(p); break;
     case 6: if(xt) k_nd_halfsize<true><<<gh, 256, 0, s>>>(p); else k_nd_halfsize<false><<<gh, 256, 0, s>>>(p); break;
     case 7: k_nd_resample<<<dim3((p.ow + 15) / 16, (p.oh + 15) / 16), 256, 0, s>>>(p); break;
+    case 8: k_nd_hl_bayer<<<gh, 256, 0, s>>>(p); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

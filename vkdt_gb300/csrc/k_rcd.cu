@@ -29,6 +29,10 @@ constexpr int RC_CX = 64, RC_CY = 16, RC_H = 4;           // conv tile and halo
 constexpr int RF_TX = 64, RF_TY = 32, RF_B = 3;            // fill tile and border (demosaic/config.h)
 constexpr int RF_SX = RF_TX - 2 * RF_B, RF_SY = RF_TY - 2 * RF_B;
 constexpr int RF_N = RF_TX * RF_TY, RF_PAD = 256;          // reads reach 3 rows + 3 columns past the plane
+// the fill kernel's staged inputs, in tile coordinates (0,0 = the tile's first pixel)
+constexpr int CF_X0 = -4, CF_W = 72, CF_Y0 = -4, CF_H = 40;   // mosaic, 0 outside the image
+constexpr int VH_X0 = -1, VH_W = 66, VH_Y0 = -1, VH_H = 34;   // vh, mirrored
+constexpr int HQ_W = 40, HQ_Y0 = -2, HQ_H = 36;               // pq and lp by half index, mirrored
 
 DEV float fadd(float a, float b) { return __fadd_rn(a, b); }
 DEV float fsub(float a, float b) { return __fsub_rn(a, b); }
@@ -37,53 +41,71 @@ DEV float fdiv(float a, float b) { return __fdiv_rn(a, b); }
 DEV float fmixr(float x, float y, float a) { return fadd(fmul(x, fsub(1.0f, a)), fmul(y, a)); }
 DEV int mirror_any(int i, int n)
 { // MIRRORED_REPEAT for any i: the tiles compute pixels up to a tile past the image
+  if((unsigned)i < (unsigned)n) return i;
+  if(i >= -n && i < 2 * n) return i < 0 ? -1 - i : 2 * n - 1 - i;
   const int m = 2 * n;
   int t = i % m;
   if(t < 0) t += m;
   return t < n ? t : m - 1 - t;
 }
 
-// demosaic/rcd_conv.comp:8-49
+// demosaic/rcd_conv.comp:8-49. The sums over the three offsets i of the
+// shader are sums of one filter response taken at three neighbouring
+// positions (a column, a row or a diagonal), so each response is computed
+// once per position and shared; every response and every sum is formed in
+// the shader's order.
 __global__ void __launch_bounds__(256) k_rcd_conv(const dev_rcd_t p)
 {
-  __shared__ float t[RC_CY + 2 * RC_H][RC_CX + 2 * RC_H + 1];
-  const int x0 = blockIdx.x * RC_CX, y0 = blockIdx.y * RC_CY;
-  for(int i = threadIdx.x; i < (RC_CY + 2 * RC_H) * (RC_CX + 2 * RC_H); i += 256)
+  __shared__ float t[RC_CY + 2 * RC_H][RC_CX + 2 * RC_H + 1];   // mosaic, mirrored, tile +-4
+  __shared__ float fv[RC_CY][RC_CX + 2];                        // vertical response, columns -1..64
+  __shared__ float fh[RC_CY + 2][RC_CX];                        // horizontal response, rows -1..16
+  __shared__ float d1[RC_CY + 2][RC_CX + 2], d2[RC_CY + 2][RC_CX + 2];   // diagonal responses, -1..64 x -1..16
+  const int x0 = blockIdx.x * RC_CX, y0 = blockIdx.y * RC_CY, tid = threadIdx.x;
+  for(int i = tid; i < (RC_CY + 2 * RC_H) * (RC_CX + 2 * RC_H); i += 256)
   { // the mosaic through the sampler at texel centres: mirrored
     const int ly = i / (RC_CX + 2 * RC_H), lx = i % (RC_CX + 2 * RC_H);
     const int gx = mirror_any(x0 + lx - RC_H, p.W), gy = mirror_any(y0 + ly - RC_H, p.H);
     t[ly][lx] = h2f(p.cfa[(size_t)gy * p.W + gx]);
   }
   __syncthreads();
-  const int lx = threadIdx.x % RC_CX, x = x0 + lx;
+  auto c = [&](int x, int y) { return t[y + RC_H][x + RC_H]; };   // tile coordinates
+  for(int i = tid; i < RC_CY * (RC_CX + 2); i += 256)
+  {
+    const int y = i / (RC_CX + 2), x = i % (RC_CX + 2) - 1;
+    fv[y][x + 1] = fadd(fsub(fsub(fadd(fsub(fsub(c(x, y - 3), fmul(3.0f, c(x, y - 2))), c(x, y - 1)), fmul(6.0f, c(x, y))), c(x, y + 1)),
+                             fmul(3.0f, c(x, y + 2))), c(x, y + 3));
+  }
+  for(int i = tid; i < (RC_CY + 2) * RC_CX; i += 256)
+  {
+    const int y = i / RC_CX - 1, x = i % RC_CX;
+    fh[y + 1][x] = fadd(fsub(fsub(fadd(fsub(fsub(c(x - 3, y), fmul(3.0f, c(x - 2, y))), c(x - 1, y)), fmul(6.0f, c(x, y))), c(x + 1, y)),
+                             fmul(3.0f, c(x + 2, y))), c(x + 3, y));
+  }
+  for(int i = tid; i < (RC_CY + 2) * (RC_CX + 2); i += 256)
+  {
+    const int y = i / (RC_CX + 2) - 1, x = i % (RC_CX + 2) - 1;
+    if(((x0 + x + y0 + y) & 1) != 0) continue;   // red/blue positions only
+    d1[y + 1][x + 1] = fadd(fsub(fadd(fsub(fsub(c(x - 3, y - 3), c(x + 1, y - 1)), c(x + 1, y + 1)), c(x + 3, y + 3)),
+                                 fmul(3.0f, fadd(c(x - 2, y - 2), c(x + 2, y + 2)))), fmul(6.0f, c(x, y)));
+    d2[y + 1][x + 1] = fadd(fsub(fadd(fsub(fsub(c(x + 3, y - 3), c(x + 1, y - 1)), c(x - 1, y + 1)), c(x - 3, y + 3)),
+                                 fmul(3.0f, fadd(c(x + 2, y - 2), c(x - 2, y + 2)))), fmul(6.0f, c(x, y)));
+  }
+  __syncthreads();
+  const int lx = tid % RC_CX, x = x0 + lx;
   if(x >= p.W) return;
   const int hw = p.W / 2;
-  for(int ly = threadIdx.x / RC_CX; ly < RC_CY; ly += 256 / RC_CX)
+  for(int ly = tid / RC_CX; ly < RC_CY; ly += 256 / RC_CX)
   {
     const int y = y0 + ly;
     if(y >= p.H) return;
-    auto c = [&](int i, int j) { return t[ly + RC_H + j][lx + RC_H + i]; };
-    float s0 = 0.0f, s1 = 0.0f;
-#pragma unroll
-    for(int i = -1; i <= 1; i++)
-    {
-      float a = fadd(fsub(fsub(fadd(fsub(fsub(c(i, -3), fmul(3.0f, c(i, -2))), c(i, -1)), fmul(6.0f, c(i, 0))), c(i, 1)), fmul(3.0f, c(i, 2))), c(i, 3));
-      float b = fadd(fsub(fsub(fadd(fsub(fsub(c(-3, i), fmul(3.0f, c(-2, i))), c(-1, i)), fmul(6.0f, c(0, i))), c(1, i)), fmul(3.0f, c(2, i))), c(3, i));
-      s0 = fadd(s0, a); s1 = fadd(s1, b);
-    }
+    float s0 = fadd(fadd(fadd(0.0f, fv[ly][lx]), fv[ly][lx + 1]), fv[ly][lx + 2]);
+    float s1 = fadd(fadd(fadd(0.0f, fh[ly][lx]), fh[ly + 1][lx]), fh[ly + 2][lx]);
     s0 = fmul(s0, s0); s1 = fmul(s1, s1);
     p.vh[(size_t)y * p.W + x] = f2h(fdiv(s0, fadd(fadd(1e-5f, s0), s1)));
     if(((x + y) & 1) == 0)
     { // red/blue: diagonal discriminator
-      float q0 = 1e-5f, q1 = 1e-5f;
-#pragma unroll
-      for(int i = -1; i <= 1; i++)
-      {
-        q0 = fadd(q0, fadd(fsub(fadd(fsub(fsub(c(-3 + i, -3 + i), c(1 + i, -1 + i)), c(1 + i, 1 + i)), c(3 + i, 3 + i)),
-                                fmul(3.0f, fadd(c(-2 + i, -2 + i), c(2 + i, 2 + i)))), fmul(6.0f, c(i, i))));
-        q1 = fadd(q1, fadd(fsub(fadd(fsub(fsub(c(3 + i, -3 - i), c(1 + i, -1 - i)), c(-1 + i, 1 - i)), c(-3 + i, 3 - i)),
-                                fmul(3.0f, fadd(c(2 + i, -2 - i), c(-2 + i, 2 - i)))), fmul(6.0f, c(i, -i))));
-      }
+      float q0 = fadd(fadd(fadd(1e-5f, d1[ly][lx]), d1[ly + 1][lx + 1]), d1[ly + 2][lx + 2]);
+      float q1 = fadd(fadd(fadd(1e-5f, d2[ly + 2][lx]), d2[ly + 1][lx + 1]), d2[ly][lx + 2]);
       q0 = fmul(q0, q0); q1 = fmul(q1, q1);
       p.pq[(size_t)y * hw + x / 2] = f2h(fdiv(q0, fadd(q0, q1)));
     }
@@ -95,45 +117,73 @@ __global__ void __launch_bounds__(256) k_rcd_conv(const dev_rcd_t p)
       for(int j = -1; j <= 1; j++)
 #pragma unroll
         for(int i = -1; i <= 1; i++)
-          l = fadd(l, fmul((j == 0 ? 1.0f : 0.5f) * (i == 0 ? 1.0f : 0.5f), c(i + off, j)));
+          l = fadd(l, fmul((j == 0 ? 1.0f : 0.5f) * (i == 0 ? 1.0f : 0.5f), c(lx + i + off, ly + j)));
       p.lp[(size_t)y * hw + x / 2] = f2h(fmaxf(1e-6f, l));
     }
   }
 }
 
-// demosaic/rcd_fill.comp:20-162
-__global__ void __launch_bounds__(1024) k_rcd_fill(const dev_rcd_t p)
+// demosaic/rcd_fill.comp:20-162. 256 threads per tile, each working on the
+// pixel pairs of four tile rows; the mosaic, vh, pq and lp the tile reads
+// are staged in shared memory first (mirrored or zero filled as the shader
+// reads them).
+__global__ void __launch_bounds__(256, 4) k_rcd_fill(const dev_rcd_t p)
 {
   __shared__ __half sh[3][RF_PAD + RF_N + RF_PAD];   // shm_r, shm_g, shm_b
-  const int lx = threadIdx.x, ly = threadIdx.y, tid = ly * 32 + lx;
-  for(int i = tid; i < RF_PAD; i += 1024)
-#pragma unroll
-    for(int c = 0; c < 3; c++) { sh[c][i] = __float2half_rn(0.0f); sh[c][RF_PAD + RF_N + i] = __float2half_rn(0.0f); }
-  const int ix = blockIdx.x * RF_SX + 2 * lx - RF_B, iy = blockIdx.y * RF_SY + ly - RF_B;   // ipos
-  const int base = RF_PAD + RF_TX * ly + 2 * lx;
+  __shared__ __half scf[CF_H][CF_W], svh[VH_H][VH_W], spq[HQ_H][HQ_W], slp[HQ_H][HQ_W];
+  const int tid = threadIdx.x, lx = tid & 31, ly0 = tid >> 5;
+  const int ox = blockIdx.x * RF_SX - RF_B, oy = blockIdx.y * RF_SY - RF_B;   // the tile's first pixel
   const int hw = p.W / 2;
-  auto cf = [&](int x, int y) -> float {   // texelFetch of the mosaic, 0 outside
-    return (x < 0 || y < 0 || x >= p.W || y >= p.H) ? 0.0f : h2f(p.cfa[(size_t)y * p.W + x]);
-  };
-  auto vhf = [&](int x, int y) { return h2f(p.vh[(size_t)mirror_any(y, p.H) * p.W + mirror_any(x, p.W)]); };
-  auto hidx = [&](int x, int y) { return mirror_any((x + ((y & 1) == 1 ? 0 : 1)) / 2, hw); };   // truncating division
-  auto pqf = [&](int x, int y) { return h2f(p.pq[(size_t)mirror_any(y, p.H) * hw + hidx(x, y)]); };
-  auto lpf = [&](int x, int y) { return h2f(p.lp[(size_t)mirror_any(y, p.H) * hw + hidx(x, y)]); };
+  const int hmin = ((ox - 2) >> 1) - 1;            // below every half index the tile reads
+  const __half zero = __float2half_rn(0.0f);
+  for(int i = tid; i < RF_PAD; i += 256)
+#pragma unroll
+    for(int c = 0; c < 3; c++) { sh[c][i] = zero; sh[c][RF_PAD + RF_N + i] = zero; }
+  for(int i = tid; i < CF_H * CF_W; i += 256)
+  { // texelFetch of the mosaic: 0 outside
+    const int yy = i / CF_W, xx = i % CF_W;
+    const int gx = ox + CF_X0 + xx, gy = oy + CF_Y0 + yy;
+    scf[yy][xx] = (gx >= 0 && gy >= 0 && gx < p.W && gy < p.H) ? p.cfa[(size_t)gy * p.W + gx] : zero;
+  }
+  for(int i = tid; i < VH_H * VH_W; i += 256)
+  { // texture() at texel centres: mirrored
+    const int yy = i / VH_W, xx = i % VH_W;
+    svh[yy][xx] = p.vh[(size_t)mirror_any(oy + VH_Y0 + yy, p.H) * p.W + mirror_any(ox + VH_X0 + xx, p.W)];
+  }
+  for(int i = tid; i < HQ_H * HQ_W; i += 256)
+  {
+    const int yy = i / HQ_W, xx = i % HQ_W;
+    const size_t o = (size_t)mirror_any(oy + HQ_Y0 + yy, p.H) * hw + mirror_any(hmin + xx, hw);
+    spq[yy][xx] = p.pq[o];
+    slp[yy][xx] = p.lp[o];
+  }
+  __syncthreads();
+  // tile coordinates (x, y) -> staged values
+  auto cf = [&](int x, int y) { return h2f(scf[y - CF_Y0][x - CF_X0]); };
+  auto vhf = [&](int x, int y) { return h2f(svh[y - VH_Y0][x - VH_X0]); };
+  auto hq = [&](int x, int y) { const int gx = ox + x, gy = oy + y; return (gx + ((gy & 1) == 1 ? 0 : 1)) / 2 - hmin; };   // truncating division
+  auto pqf = [&](int x, int y) { return h2f(spq[y - HQ_Y0][hq(x, y)]); };
+  auto lpf = [&](int x, int y) { return h2f(slp[y - HQ_Y0][hq(x, y)]); };
   const float eps = 1e-5f;
+#pragma unroll 1
+  for(int ly = ly0; ly < RF_TY; ly += 8)
   { // fill the tile, white balanced, f16
 #pragma unroll
     for(int k = 0; k < 2; k++)
     {
-      const int c = cfa_bayer(ix + k, iy);
-      const float v = gclamp(cf(ix + k, iy), 0.0f, 65535.0f);
+      const int x = 2 * lx + k;
+      const int c = cfa_bayer(ox + x, oy + ly);
+      const float v = gclamp(cf(x, ly), 0.0f, 65535.0f);
 #pragma unroll
-      for(int ch = 0; ch < 3; ch++) sh[ch][base + k] = __float2half_rn(c == ch ? fmul(p.wb[ch], v) : 0.0f);
+      for(int ch = 0; ch < 3; ch++) sh[ch][RF_PAD + RF_TX * ly + x] = __float2half_rn(c == ch ? fmul(p.wb[ch], v) : 0.0f);
     }
   }
   __syncthreads();
-  const int k_rb = cfa_bayer(ix, iy) == 1 ? 1 : 0;   // the red/blue pixel of the pair
+#pragma unroll 1
+  for(int ly = ly0; ly < RF_TY; ly += 8)
   { // green at red/blue
-    const int x = ix + k_rb, y = iy;
+    const int k_rb = cfa_bayer(ox + 2 * lx, oy + ly) == 1 ? 1 : 0;   // the red/blue pixel of the pair
+    const int x = 2 * lx + k_rb, y = ly;
     const float vhc = vhf(x, y);
     const float vhn = fmul(0.25f, fadd(fadd(fadd(vhf(x - 1, y - 1), vhf(x + 1, y - 1)), vhf(x - 1, y + 1)), vhf(x + 1, y + 1)));
     const float vhd = fabsf(fsub(0.5f, vhc)) < fabsf(fsub(0.5f, vhn)) ? vhn : vhc;
@@ -150,12 +200,15 @@ __global__ void __launch_bounds__(1024) k_rcd_fill(const dev_rcd_t p)
     const float Ee = fdiv(fmul(fmul(ce1, 2.0f), l0), fadd(fadd(eps, l0), lpf(x + 2, y)));
     const float ve = gclamp(fdiv(fadd(fmul(Sg, Ne), fmul(Ng, Se)), fadd(Ng, Sg)), 0.0f, 65534.0f);
     const float he = gclamp(fdiv(fadd(fmul(Wg, Ee), fmul(Eg, We)), fadd(Eg, Wg)), 0.0f, 65534.0f);
-    sh[1][base + k_rb] = __float2half_rn(fmixr(ve, he, vhd));
+    sh[1][RF_PAD + RF_TX * y + x] = __float2half_rn(fmixr(ve, he, vhd));
   }
   __syncthreads();
+#pragma unroll 1
+  for(int ly = ly0; ly < RF_TY; ly += 8)
   { // blue at red, red at blue: along the diagonals
-    const int x = ix + k_rb, y = iy, o = base + k_rb;
-    const bool red = cfa_bayer(x, y) == 0;
+    const int k_rb = cfa_bayer(ox + 2 * lx, oy + ly) == 1 ? 1 : 0;
+    const int x = 2 * lx + k_rb, y = ly, o = RF_PAD + RF_TX * y + x;
+    const bool red = cfa_bayer(ox + x, oy + y) == 0;
     const __half *sc = sh[red ? 2 : 0], *sg = sh[1];
     auto S = [&](const __half *a, int dx, int dy) { return a[o + RF_TX * dy + dx]; };
     auto hd = [&](__half a, __half b) { return __half2float(__habs(__hsub(a, b))); };
@@ -175,8 +228,11 @@ __global__ void __launch_bounds__(1024) k_rcd_fill(const dev_rcd_t p)
     sh[red ? 2 : 0][o] = __float2half_rn(gclamp(fadd(__half2float(g0), fmixr(pe, qe, pqd)), 0.0f, 65535.0f));
   }
   __syncthreads();
+#pragma unroll 1
+  for(int ly = ly0; ly < RF_TY; ly += 8)
   { // red and blue at green
-    const int kg = 1 - k_rb, x = ix + kg, y = iy, o = base + kg;
+    const int kg = cfa_bayer(ox + 2 * lx, oy + ly) == 1 ? 0 : 1;
+    const int x = 2 * lx + kg, y = ly, o = RF_PAD + RF_TX * y + x;
     const __half *sg = sh[1];
     auto S = [&](const __half *a, int dx, int dy) { return a[o + RF_TX * dy + dx]; };
     auto hd = [&](__half a, __half b) { return __half2float(__habs(__hsub(a, b))); };
@@ -209,15 +265,20 @@ __global__ void __launch_bounds__(1024) k_rcd_fill(const dev_rcd_t p)
   }
   __syncthreads();
   // the inner 58x26 pixels, divided by the white balance again
-#pragma unroll
-  for(int k = 0; k < 2; k++)
+#pragma unroll 1
+  for(int ly = ly0; ly < RF_TY; ly += 8)
   {
-    const int gx = ix + k, lxx = 2 * lx + k;
-    if(lxx >= RF_B && ly >= RF_B && lxx < RF_TX - RF_B && ly < RF_TY - RF_B && gx < p.W && iy < p.H)
+    const int gy = oy + ly;
+#pragma unroll
+    for(int k = 0; k < 2; k++)
     {
-      const int o = base + k;
-      p.out[(size_t)iy * p.W + gx] = mk_half4(fdiv(h2f(sh[0][o]), p.wb[0]), fdiv(h2f(sh[1][o]), p.wb[1]),
-                                              fdiv(h2f(sh[2][o]), p.wb[2]), 1.0f);
+      const int x = 2 * lx + k, gx = ox + x;
+      if(x >= RF_B && ly >= RF_B && x < RF_TX - RF_B && ly < RF_TY - RF_B && gx < p.W && gy < p.H)
+      {
+        const int o = RF_PAD + RF_TX * ly + x;
+        p.out[(size_t)gy * p.W + gx] = mk_half4(fdiv(h2f(sh[0][o]), p.wb[0]), fdiv(h2f(sh[1][o]), p.wb[1]),
+                                                fdiv(h2f(sh[2][o]), p.wb[2]), 1.0f);
+      }
     }
   }
 }
@@ -229,7 +290,7 @@ cudaError_t launch_rcd(const dev_rcd_t &p, int stage, cudaStream_t s)
   if(stage == 0)
     k_rcd_conv<<<dim3((p.W + RC_CX - 1) / RC_CX, (p.H + RC_CY - 1) / RC_CY), 256, 0, s>>>(p);
   else if(stage == 1)
-    k_rcd_fill<<<dim3((p.W + RF_SX - 1) / RF_SX, (p.H + RF_SY - 1) / RF_SY), dim3(32, 32), 0, s>>>(p);
+    k_rcd_fill<<<dim3((p.W + RF_SX - 1) / RF_SX, (p.H + RF_SY - 1) / RF_SY), 256, 0, s>>>(p);
   else return cudaErrorInvalidValue;
   return cudaGetLastError();
 }

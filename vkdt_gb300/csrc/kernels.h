@@ -118,8 +118,12 @@ struct dev_nodes_t
   __half *g;             // demosaic/splat, W*H
   half4 *hs;             // demosaic/halfsize, hw*hh
   half4 *dm;             // demosaic output, ow*oh
+  const half4 *coarse;   // assembled hilite level 1 (or reduce level 1 when the pyramid has one level)
+  int ccw, cch;          // its size
+  float hl_soft;
 };
-// stage: 0 noop, 1 hilite half, 2 hilite doub, 3 gauss, 4 splat, 5 fix, 6 halfsize, 7 resample
+// stage: 0 noop, 1 hilite half, 2 hilite doub, 3 gauss, 4 splat, 5 fix, 6 halfsize, 7 resample,
+// 8 bayer noop + hilite half + level 0 hilite assemble + hilite doub from the mosaic (dn written when set)
 cudaError_t launch_nodes(const dev_nodes_t &p, int stage, cudaStream_t s);
 // colour -> histogram -> filmcurv -> llap curve -> llap level 1 reduce on the
 // demosaic output (p.W x p.H = the output size; p.mosaic unused)
@@ -137,6 +141,9 @@ struct dev_rcd_t
   half4 *out;            // demosaic output, W*H
 };
 cudaError_t launch_rcd(const dev_rcd_t &p, int stage, cudaStream_t s);
+
+// packed raw video unpack (k_unpack.cu)
+cudaError_t launch_unpack_mlv(const void *packed, size_t bytes, int bpp, size_t npix, uint16_t *out, cudaStream_t s);
 
 // rawhist noise statistics (k_rawhist.cu)
 struct dev_rawhist_t

@@ -441,6 +441,62 @@ def workload_video(args, v, torch, sp, clk):
                                              "latency_ms": {"p99_frame": b2b["frame_latency_ms"]["p99"]}}
 
 
+def workload_ingest(args, v, torch, sp, clk):
+    """Device ingestion of packed raw video, 4096x2160 frames: the magic lantern unpack at
+    12 and 14 bits and the motioncam block decode (bit counts 5..8 per block, as 12-bit video
+    noise gives them), each over a ring of frames larger than L2."""
+    W, H, N, K = 4096, 2160, 16, 64
+    npx = W * H
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else None
+    peak = peaks["hbm_gbs"] if peaks else 6800.0
+    g = torch.Generator(device="cuda")
+    g.manual_seed(7)
+    outs = [torch.empty(npx, dtype=torch.int16, device="cuda") for _ in range(N)]
+    res = {}
+
+    def timed(launch, nbytes):
+        for i in range(4):
+            launch(i % N)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for i in range(K):
+            launch(i % N)
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / K
+        gbs = nbytes / (ms / 1e3) / 1e9
+        return {"ms_per_frame": ms, "mpix_per_s": npx / 1e6 / (ms / 1e3), "gbs": gbs, "hbm_frac": gbs / peak,
+                "bytes_per_frame": nbytes}
+    with clk:
+        for bpp in (12, 14):
+            nb = npx * bpp // 8
+            ins = [torch.randint(0, 256, (nb,), dtype=torch.uint8, device="cuda", generator=g) for _ in range(N)]
+            res["mlv_%dbit" % bpp] = timed(lambda i: v.unpack_mlv(ins[i].data_ptr(), nb, bpp, W, H, outs[i].data_ptr(), sp),
+                                           nb + 2 * npx)
+            del ins
+        blocks = npx // 64
+        rng = np.random.default_rng(5)
+        streams = []
+        for i in range(N):
+            nib = rng.integers(5, 9, blocks).astype(np.uint8)
+            bc = (nib[0::2] | (nib[1::2] << 4)).astype(np.uint8)
+            size = int(np.where(nib <= 6, 8 * nib.astype(np.int64), 64).sum())
+            streams.append((torch.from_numpy(bc).cuda(), torch.randint(0, 2000, (blocks,), dtype=torch.int16, device="cuda",
+                                                                        generator=g),
+                            torch.randint(0, 256, (size,), dtype=torch.uint8, device="cuda", generator=g), size))
+        scratch = torch.empty(max(8, v._lib.lib().vkdt_cuda_mcraw_scratch_bytes(W, H)), dtype=torch.uint8, device="cuda")
+        mean_bytes = sum(st[3] for st in streams) / N + blocks // 2 + 2 * blocks
+        res["mcraw"] = timed(lambda i: v.mcraw_decode(streams[i][0].data_ptr(), streams[i][1].data_ptr(),
+                                                      streams[i][2].data_ptr(), streams[i][3], W, H, outs[i].data_ptr(),
+                                                      d_scratch=scratch.data_ptr(), stream=sp),
+                             mean_bytes + 2 * npx)
+    return {"workload": "device ingestion of packed raw video frames, 4096x2160: magic lantern 12/14-bit unpack, "
+                        "motioncam block decode (bit counts 5..8)", "frames_in_ring": N,
+            "roofline_note": "gbs counts the packed bytes read and the u16 mosaic written once per frame"}, \
+        res["mcraw"]["mpix_per_s"], res["mcraw"]["ms_per_frame"], {"ingest": res, "gpu_launches": 2 * K}
+
+
 def run_workload(args):
     import torch
     import vkdt_gb300 as v
@@ -455,7 +511,8 @@ def run_workload(args):
     v.init(local)
     sp = torch.cuda.current_stream().cuda_stream
     clk = Clocks(local)
-    fn = {"batch": workload_batch, "serve": workload_serve, "video": workload_video}[args.workload]
+    fn = {"batch": workload_batch, "serve": workload_serve, "video": workload_video,
+          "ingest": workload_ingest}[args.workload]
     cfg, value, ms, extra = fn(args, v, torch, sp, clk)
     if world > 1:
         t = torch.tensor([value], device="cuda")
@@ -485,9 +542,10 @@ def main():
     ap.add_argument("--levels", type=int, default=LEVELS, help="llap pyramid depth (0 = automatic)")
     ap.add_argument("--denoise", type=float, default=DENOISE,
                     help="denoise strength (0 = the darkroom default, denoise/noop; > 0 the wavelet path)")
-    ap.add_argument("--workload", default="single", choices=("single", "batch", "serve", "video"),
+    ap.add_argument("--workload", default="single", choices=("single", "batch", "serve", "video", "ingest"),
                     help="single: the 24 MP develop (default); batch: 64 mixed-size mosaics; "
-                         "serve: Poisson request stream; video: 4 raw video streams + x-trans stills")
+                         "serve: Poisson request stream; video: 4 raw video streams + x-trans stills; "
+                         "ingest: device unpack/decode of packed raw video frames")
     ap.add_argument("--images", type=int, default=64, help="batch: mosaics in the batch")
     ap.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
     ap.add_argument("--slots", type=int, default=4, help="serve/video: jobs in flight")

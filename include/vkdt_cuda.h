@@ -269,6 +269,20 @@ int  vkdt_cuda_hist_rgba_f16(const void *d_rgba, int wd, int ht, uint32_t *d_his
 int  vkdt_cuda_unpack_mlv(const void *d_packed, size_t bytes, int bits_per_pixel, int wd, int ht, void *d_mosaic,
                           void *stream);
 
+/* Ingestion of motioncam raw video (replaces the i-mcraw nodes prefix and decode,
+ * i-mcraw/main.cc:366-408 create_nodes, i-mcraw/prefix.comp, i-mcraw/decode.comp): the
+ * frame's source buffers as i-mcraw's read_source fills them (main.cc:411-446) on the
+ * device: d_bitcnt (one 4-bit count per block of 64 samples, two per byte, low nibble
+ * first), d_refval (u16 per block), d_data (data_bytes of block data). rwd x ht is the
+ * encoded size (rwd a multiple of 64, ht of 4); d_mosaic receives the wd x hgt u16 mosaic
+ * offset by (ox, oy) (modify_roi_out at main.cc:330-360), each sample as the reference's
+ * R16_UNORM store of (reference + delta) / 65536 leaves it. d_scratch: at least
+ * vkdt_cuda_mcraw_scratch_bytes(rwd, ht) bytes, 8-byte aligned. Asynchronous on `stream`. */
+size_t vkdt_cuda_mcraw_scratch_bytes(int rwd, int ht);
+int  vkdt_cuda_mcraw_decode(const void *d_bitcnt, const void *d_refval, const void *d_data, size_t data_bytes,
+                            int rwd, int ht, int ox, int oy, int wd, int hgt, void *d_mosaic, void *d_scratch,
+                            void *stream);
+
 /* ---- noise statistics and the noise profile fit (rawhist and nprof modules)
  *
  * rawhist/collect.comp:22-66 over a device mosaic (uint16, row pitch = wd):

@@ -87,6 +87,11 @@ def lib():
         l.oracle_f16.argtypes = [C.c_float]
         l.oracle_unpack_mlv.argtypes = [C.c_void_p, C.c_size_t, C.c_int, C.c_size_t, C.c_void_p]
         l.oracle_pack_mlv.argtypes = [C.c_void_p, C.c_size_t, C.c_int, C.c_void_p, C.c_size_t]
+        l.oracle_mcraw_decode.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_int, C.c_int, C.c_int,
+                                          C.c_int, C.c_int, C.c_int, C.c_void_p]
+        l.oracle_mcraw_encode.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_size_t]
+        l.oracle_mcraw_encode.restype = C.c_size_t
         l.oracle_rcd.argtypes = [C.POINTER(C.c_float), C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
         _lib = l
     return _lib
@@ -167,6 +172,34 @@ def pack_mlv(values, bpp):
     out = np.zeros(mlv_bytes(values.size, bpp), np.uint8)
     lib().oracle_pack_mlv(values.ctypes.data, values.size, bpp, out.ctypes.data, out.size)
     return out
+
+
+def mcraw_decode(bitcnt, refval, data, rwd, ht, ox=0, oy=0, wd_out=None, ht_out=None):
+    """i-mcraw decode of one frame (nibble counts, u16 references, data bytes)"""
+    wd_out = rwd - ox if wd_out is None else wd_out
+    ht_out = ht - oy if ht_out is None else ht_out
+    bitcnt = np.ascontiguousarray(bitcnt, np.uint8)
+    refval = np.ascontiguousarray(refval, np.uint16)
+    data = np.ascontiguousarray(data, np.uint8)
+    out = np.zeros((ht_out, wd_out), np.uint16)
+    lib().oracle_mcraw_decode(bitcnt.ctypes.data, refval.ctypes.data, data.ctypes.data, data.size, rwd, ht, ox, oy,
+                              wd_out, ht_out, out.ctypes.data)
+    return out
+
+
+def mcraw_encode(img, force_cnt=-1):
+    """a frame (ht x rwd u16, rwd a multiple of 64, ht of 4) as (bitcnt, refval, data)"""
+    img = np.ascontiguousarray(img, np.uint16)
+    ht, rwd = img.shape
+    blocks = rwd * ht // 64
+    bitcnt = np.zeros((blocks + 1) // 2, np.uint8)
+    refval = np.zeros(blocks, np.uint16)
+    data = np.zeros(blocks * 128, np.uint8)
+    n = lib().oracle_mcraw_encode(img.ctypes.data, rwd, ht, force_cnt, bitcnt.ctypes.data, refval.ctypes.data,
+                                  data.ctypes.data, data.size)
+    if n == 0 and blocks:
+        raise RuntimeError("mcraw encode failed")
+    return bitcnt, refval, data[:n].copy()
 
 
 def noop(mosaic, ip):

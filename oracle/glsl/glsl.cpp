@@ -1,5 +1,7 @@
 // Sampler, image and storage model of glsl.hpp (test infrastructure only).
 #include "glsl.hpp"
+#include <ucontext.h>
+#include <vector>
 
 namespace glsl {
 
@@ -125,6 +127,75 @@ vec4 imageLoad(const image2D &i, const ivec2 &p)
   image_t *im = i.im;
   if(!im || p.x < 0 || p.y < 0 || p.x >= im->w || p.y >= im->h) return vec4(0.0f);
   return texel(im, p.x, p.y);
+}
+
+// cooperative workgroups: one ucontext per invocation
+namespace {
+struct coop_t
+{
+  ucontext_t sched;
+  std::vector<ucontext_t> inv;
+  std::vector<std::vector<char>> stack;
+  std::vector<char> done;
+  int cur = -1;
+  void (*fn)() = nullptr;
+};
+thread_local coop_t *g_coop = nullptr;
+void coop_entry()
+{
+  g_coop->fn();
+  g_coop->done[g_coop->cur] = 1;
+}   // returns to uc_link: the scheduler
+} // namespace
+
+void barrier()
+{
+  if(g_coop) swapcontext(&g_coop->inv[g_coop->cur], &g_coop->sched);
+}
+void memoryBarrierShared() {}
+
+void run_workgroups_coop(int GX, int GY, int GZ, int LX, int LY, void (*fn)())
+{
+  const int N = LX * LY;
+#pragma omp parallel
+  {
+    coop_t c;
+    c.inv.resize(N);
+    c.stack.assign(N, std::vector<char>(256 * 1024));
+    c.done.assign(N, 0);
+    c.fn = fn;
+    g_coop = &c;
+#pragma omp for collapse(3) schedule(static)
+    for(int z = 0; z < GZ; z++) for(int wy = 0; wy < GY; wy++) for(int wx = 0; wx < GX; wx++)
+    {
+      for(int k = 0; k < N; k++)
+      {
+        getcontext(&c.inv[k]);
+        c.inv[k].uc_stack.ss_sp = c.stack[k].data();
+        c.inv[k].uc_stack.ss_size = c.stack[k].size();
+        c.inv[k].uc_link = &c.sched;
+        makecontext(&c.inv[k], coop_entry, 0);
+        c.done[k] = 0;
+      }
+      for(bool any = true; any;)
+      { // one barrier phase: resume every invocation until it waits or returns
+        any = false;
+        for(int k = 0; k < N; k++)
+        {
+          if(c.done[k]) continue;
+          const int lx = k % LX, ly = k / LX;
+          gl_GlobalInvocationID = uvec3((uint)(wx * LX + lx), (uint)(wy * LY + ly), (uint)z);
+          gl_LocalInvocationID = uvec3((uint)lx, (uint)ly, 0u);
+          gl_WorkGroupID = uvec3((uint)wx, (uint)wy, (uint)z);
+          gl_LocalInvocationIndex = (uint)k;
+          c.cur = k;
+          swapcontext(&c.sched, &c.inv[k]);
+          any = true;
+        }
+      }
+    }
+    g_coop = nullptr;
+  }
 }
 
 } // namespace glsl

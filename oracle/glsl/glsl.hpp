@@ -92,6 +92,7 @@ typedef V<float, 2> vec2; typedef V<float, 3> vec3; typedef V<float, 4> vec4;
 typedef V<int, 2> ivec2;  typedef V<int, 3> ivec3;  typedef V<int, 4> ivec4;
 typedef V<uint, 2> uvec2; typedef V<uint, 3> uvec3; typedef V<uint, 4> uvec4;
 typedef V<bool, 2> bvec2; typedef V<bool, 3> bvec3; typedef V<bool, 4> bvec4;
+typedef V<uint8_t, 2> u8vec2; typedef V<uint8_t, 4> u8vec4;   // GL_EXT_shader_explicit_arithmetic_types_int8
 
 // ------------------------------------------------------------------ traits
 template<class A> struct vinfo { static constexpr bool is = false; static constexpr int n = 1; using E = A; };
@@ -337,6 +338,27 @@ template<class T, int N> struct shared_arr
 // barrier phases of the running invocation (translate.py: phases())
 extern thread_local int glsl_bar_, glsl_phase_;
 
+// barrier() anywhere in a shader: every invocation of a workgroup runs on its
+// own stack and gives control back to the workgroup's scheduler at each
+// barrier; the scheduler resumes all invocations once every one of them has
+// reached it (or returned). Runs the workgroups of a dispatch (in parallel
+// across host threads, one workgroup at a time per thread).
+void barrier();
+void memoryBarrierShared();
+void run_workgroups_coop(int GX, int GY, int GZ, int LX, int LY, void (*fn)());
+
+// integer built-ins of the int8/int16 extensions and GLSL 4
+inline uint bitfieldExtract(uint v, int off, int bits)
+{
+  if(bits <= 0) return 0u;
+  const uint m = bits >= 32 ? 0xffffffffu : ((1u << bits) - 1u);
+  return (v >> off) & m;
+}
+template<class A, class = std::enable_if_t<is_vec<A>>> inline auto bitfieldExtract(const A &a, int off, int bits)
+{ return vmap([&](auto x) { return bitfieldExtract((uint)x, off, bits); }, a); }
+inline uint16_t pack16(const u8vec2 &v) { return (uint16_t)((uint)v.d[0] | ((uint)v.d[1] << 8)); }
+template<class A> inline uint16_t pack16(const A &a) { return pack16(u8vec2(tov(a))); }
+
 // ------------------------------------------------------------------ images
 struct image_t
 { // row major, c channels of float (values already rounded to the storage format)
@@ -391,5 +413,6 @@ typedef struct ref_dispatch_t
   const void *push;                // push constants (std140), may be 0
   const void *global;              // global uniform block (frame, ...), may be 0
   glsl::image_t *bind[8][32];      // bindings [binding][array element]
+  void *buf[8];                    // storage buffers by binding
 } ref_dispatch_t;
 }

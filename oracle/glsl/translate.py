@@ -28,6 +28,7 @@ SHADERS = [
     ("demosaic", "halfsize"), ("demosaic", "rcd_conv"), ("demosaic", "rcd_fill"), ("shared", "resample"),
     ("colour", "main"), ("filmcurv", "main"),
     ("llap", "curve"), ("llap", "reduce"), ("llap", "assemble"), ("llap", "colour"),
+    ("i-mcraw", "decode"),
 ]
 
 
@@ -189,8 +190,19 @@ def translate(module, kernel, moddir):
 
     text = re.sub(r"layout\s*\(([^)]*)\)\s*uniform\s+((?:writeonly|readonly)\s+)?(sampler2D|usampler2D|image2D|uimage2D)\s+(\w+)\s*(\[\s*\])?\s*;",
                   resource, text, flags=re.S)
+    buffers = []   # (binding, instance, member, type)
+
+    def ssbo(m):
+        lay, name, typ, member, inst = m.group(1), m.group(2), m.group(3), m.group(4), m.group(5)
+        b = int(re.search(r"binding\s*=\s*(\d+)", lay).group(1))
+        buffers.append((b, inst, member, typ))
+        return "struct %s { %s *%s; }; static %s %s;" % (name, typ, member, name, inst)
+
+    # storage buffers of one unsized array: a pointer bound by the runner
+    text = re.sub(r"layout\s*\(([^)]*)\)\s*(?:(?:readonly|writeonly|volatile|coherent)\s+)*buffer\s+(\w+)\s*"
+                  r"\{\s*(\w+)\s+(\w+)\s*\[\s*\]\s*;\s*\}\s*(\w+)\s*;", ssbo, text)
     if re.search(r"\bbuffer\b", text):
-        raise RuntimeError("%s/%s uses buffers (not modelled)" % (module, kernel))
+        raise RuntimeError("%s/%s uses buffers other than one unsized array (not modelled)" % (module, kernel))
     # workgroup shared arrays: one copy per emulation thread, which runs one workgroup at a time
     text, nshared = re.subn(r"\bshared\s+(\w+)\s+(\w+)\s*\[([^\]]+)\]\s*;",
                             r"static thread_local shared_arr<\1, (\3)> \2;", text)
@@ -210,11 +222,15 @@ def translate(module, kernel, moddir):
     # float literals are single precision in GLSL
     text = re.sub(r"(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][-+]?\d+)?|\d+[eE][-+]?\d+)(?![\w.])", r"\1f", text)
     text = re.sub(r"\bvoid\s+main\s*\(\s*\)", "void shader_main()", text)
-    nphase = 1
+    nphase, coop = 1, False
     if nshared:
-        text, nphase = phases(text)
-    ns = "sh_%s_%s" % (module, kernel)
-    entry = ["extern \"C\" void ref_%s_%s(const ref_dispatch_t *dp)" % (module, kernel), "{", "  using namespace %s;" % ns]
+        try:
+            text, nphase = phases(text)
+        except RuntimeError:
+            coop = True   # barrier() inside functions: cooperative invocations (glsl.cpp)
+    ident = module.replace("-", "_")
+    ns = "sh_%s_%s" % (ident, kernel)
+    entry = ["extern \"C\" void ref_%s_%s(const ref_dispatch_t *dp)" % (ident, kernel), "{", "  using namespace %s;" % ns]
     for kind, inst in blocks:
         field = {"push": "push", "uniform": "uniform", "global": "global"}[kind]
         entry.append("  if(dp->%s) memcpy(&%s, dp->%s, sizeof(%s));" % (field, inst, field, inst))
@@ -223,6 +239,17 @@ def translate(module, kernel, moddir):
             entry.append("  for(int e = 0; e < 32; e++) %s[e].im = dp->bind[%d][e];" % (name, b))
         else:
             entry.append("  %s.im = dp->bind[%d][0];" % (name, b))
+    for b, inst, member, typ in buffers:
+        entry.append("  %s.%s = (%s *)dp->buf[%d];" % (inst, member, typ, b))
+    if coop:
+        LX, LY = local
+        entry += [
+            "  // workgroups: the node size over DT_LOCAL_SIZE (graph-run-nodes-record-cmd.h:377-380)",
+            "  glsl::run_workgroups_coop((dp->wd + 7) / 8, (dp->ht + 7) / 8, dp->dp, %d, %d, %s::shader_main);" % (LX, LY, ns),
+            "}",
+        ]
+        return ("// generated from %s by oracle/glsl/translate.py\n#include \"glsl.hpp\"\n#include <cstring>\n"
+                "namespace %s {\nusing namespace glsl;\n%s\n} // namespace\n%s\n") % (src, ns, text, "\n".join(entry))
     if nshared:
         LX, LY = local
         entry += [

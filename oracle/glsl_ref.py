@@ -26,7 +26,7 @@ class ImageT(C.Structure):
 
 class Dispatch(C.Structure):
     _fields_ = [("wd", C.c_int), ("ht", C.c_int), ("dp", C.c_int), ("uniform", C.c_void_p), ("push", C.c_void_p),
-                ("glob", C.c_void_p), ("bind", (C.POINTER(ImageT) * 32) * 8)]
+                ("glob", C.c_void_p), ("bind", (C.POINTER(ImageT) * 32) * 8), ("buf", C.c_void_p * 8)]
 
 
 def build():
@@ -63,8 +63,11 @@ class Img:
         self.w, self.h, self.c = w, h, c
 
 
-def run(name, wd, ht, binds, push=None, uniform=None, dp=1):
+def run(name, wd, ht, binds, push=None, uniform=None, dp=1, buffers=None):
+    """buffers: {binding: numpy array} for storage buffers"""
     d = Dispatch()
+    for b, a in (buffers or {}).items():
+        d.buf[b] = a.ctypes.data
     d.wd, d.ht, d.dp = wd, ht, dp
     keep = []
     for k, v in (("push", push), ("uniform", uniform)):

@@ -1355,6 +1355,219 @@ extern "C" void oracle_pack_mlv(const uint16_t *in, size_t npix, int bpp, uint8_
   }
 }
 
+// i-mcraw (motioncam raw video): blocks of 64 samples, each a reference
+// value plus deltas of a bit width given by a 4-bit count per block.
+// i-mcraw/prefix.comp:46-63: the bytes of a block by its bit count
+static inline uint32_t mc_block_bytes(uint32_t cnt)
+{
+  switch(cnt)
+  {
+    case 0: return 0;
+    case 1: return 8;
+    case 2: return 16;
+    case 3: return 24;
+    case 4: return 32;
+    case 5: return 40;
+    case 6: return 48;
+    case 7: case 8: return 64;
+    case 9: case 10: return 80;
+    default: return 128;
+  }
+}
+static inline uint32_t mc_bits(uint32_t v, int off, int n) { return (v >> off) & ((1u << n) - 1u); }
+// i-mcraw/decode.comp:31-282: the two deltas invocation si (0..31) of a block
+// extracts from the block's bytes d, for each bit count
+static void mc_decode_pair(uint32_t cnt, const uint8_t *d, int si, uint32_t r[2])
+{
+  auto pr = [&](int reg, uint32_t p[2]) { p[0] = d[reg]; p[1] = d[reg + 1]; };
+  uint32_t p[2], q[2], t[2];
+  switch(cnt)
+  {
+    case 0: r[0] = r[1] = 0; return;
+    case 1:
+      pr(2 * (si % 4), p);
+      for(int c = 0; c < 2; c++) r[c] = mc_bits(p[c], si / 4, 1);
+      return;
+    case 2:
+      pr(2 * (si % 8), p);
+      for(int c = 0; c < 2; c++) r[c] = mc_bits(p[c], 2 * (si / 8), 2);
+      return;
+    case 3:
+    {
+      int reg, off;
+      if(si < 4)       { reg = 0 + si * 2; off = 0; }
+      else if(si < 8)  { reg = 0 + (si - 4) * 2; off = 3; }
+      else if(si < 12) { reg = 0 + (si - 8) * 2; off = 6; }
+      else if(si < 16) { reg = 8 + (si - 12) * 2; off = 0; }
+      else if(si < 20) { reg = 8 + (si - 16) * 2; off = 3; }
+      else if(si < 24) { reg = 8 + (si - 20) * 2; off = 6; }
+      else if(si < 28) { reg = 16 + (si - 24) * 2; off = 0; }
+      else             { reg = 16 + (si - 28) * 2; off = 3; }
+      pr(reg, p);
+      for(int c = 0; c < 2; c++) r[c] = mc_bits(p[c], off, 3);
+      if(si >= 8 && si < 12)
+      {
+        pr(16 + (si - 8) * 2, q);
+        for(int c = 0; c < 2; c++) r[c] |= mc_bits(q[c], 6, 1) << 2;
+      }
+      else if(si >= 20 && si < 24)
+      {
+        pr(16 + (si - 20) * 2, q);
+        for(int c = 0; c < 2; c++) r[c] |= mc_bits(q[c], 7, 1) << 2;
+      }
+      return;
+    }
+    case 4:
+      pr((2 * si / 16) * 8 + (2 * si) % 8, p);
+      for(int c = 0; c < 2; c++) r[c] = mc_bits(p[c], ((2 * si / 8) & 1) == 0 ? 0 : 4, 4);
+      return;
+    case 5:
+      if(si < 20) { pr(2 * si, p); for(int c = 0; c < 2; c++) r[c] = mc_bits(p[c], 0, 5); return; }
+      if(si < 28)
+      {
+        pr(si < 24 ? 0 + (si - 20) * 2 : 8 + (si - 24) * 2, p);
+        pr(si < 24 ? 24 + (si - 20) * 2 : 32 + (si - 24) * 2, q);
+        for(int c = 0; c < 2; c++) r[c] = mc_bits(p[c], 5, 3) | (mc_bits(q[c], 5, 2) << 3);
+        return;
+      }
+      pr(16 + (si - 28) * 2, p); pr(24 + (si - 28) * 2, q); pr(32 + (si - 28) * 2, t);
+      for(int c = 0; c < 2; c++) r[c] = mc_bits(p[c], 5, 3) | (mc_bits(q[c], 7, 1) << 3) | (mc_bits(t[c], 7, 1) << 4);
+      return;
+    case 6:
+      if(si < 24) { pr(2 * si, p); for(int c = 0; c < 2; c++) r[c] = mc_bits(p[c], 0, 6); return; }
+      {
+        const int b = si < 28 ? 0 : 24, k = si < 28 ? si - 24 : si - 28;
+        pr(b + k * 2, p); pr(b + 8 + k * 2, q); pr(b + 16 + k * 2, t);
+        for(int c = 0; c < 2; c++) r[c] = mc_bits(p[c], 6, 2) | (mc_bits(q[c], 6, 2) << 2) | (mc_bits(t[c], 6, 2) << 4);
+      }
+      return;
+    case 7: case 8:
+      r[0] = d[2 * si]; r[1] = d[2 * si + 1];
+      return;
+    case 9: case 10:
+    {
+      pr(si < 16 ? 2 * si : 40 + (si - 16) * 2, p);
+      pr(si < 16 ? 32 + (si % 4) * 2 : 72 + (si % 4) * 2, q);
+      const int off = 2 * ((si & 15) / 4);
+      for(int c = 0; c < 2; c++) r[c] = p[c] | (mc_bits(q[c], off, 2) << 8);
+      return;
+    }
+    default:
+      r[0] = (uint32_t)d[4 * si] | ((uint32_t)d[4 * si + 1] << 8);
+      r[1] = (uint32_t)d[4 * si + 2] | ((uint32_t)d[4 * si + 3] << 8);
+      return;
+  }
+}
+// image position of sample c (0, 1) of invocation si of block idx (decode.comp:290-326):
+// four consecutive blocks cover 64x4 pixels, each one CFA phase in steps of two
+static inline void mc_position(uint32_t idx, int si, int c, int rwd, int &x, int &y)
+{
+  const uint32_t k = idx / 4, bpr = (uint32_t)rwd / 64;
+  x = 64 * (int)(k % bpr); y = 4 * (int)(k / bpr);
+  if(si >= 16) { x -= 64; y += 2; }
+  if((idx & 3) == 1) x += 1;
+  if((idx & 3) == 2) y += 1;
+  if((idx & 3) == 3) { x += 1; y += 1; }
+  x += 4 * si + 2 * c;
+}
+// the R16_UNORM store of res / 65536
+static inline uint16_t mc_store(uint32_t res)
+{
+  const float v = std::fmin(std::fmax((float)res / 65536.0f, 0.0f), 1.0f);
+  return (uint16_t)std::nearbyint(v * 65535.0f);
+}
+extern "C" void oracle_mcraw_decode(const uint8_t *bitcnt, const uint16_t *refval, const uint8_t *data, size_t data_bytes,
+    int rwd, int ht, int ox, int oy, int wd_out, int ht_out, uint16_t *out)
+{
+  const uint32_t blocks = (uint32_t)rwd * (uint32_t)ht / 64;
+  uint64_t off = 0;   // the exclusive prefix of the block sizes (prefix.comp, inclusive, read one block back)
+  for(uint32_t idx = 0; idx < blocks; idx++)
+  {
+    uint32_t cnt = bitcnt[idx / 2];
+    if(idx & 1) cnt >>= 4;
+    cnt &= 0xf;
+    uint8_t d[128];
+    for(int b = 0; b < 128; b++) d[b] = off + b < data_bytes ? data[off + b] : 0;
+    for(int si = 0; si < 32; si++)
+    {
+      uint32_t r[2];
+      mc_decode_pair(cnt, d, si, r);
+      for(int c = 0; c < 2; c++)
+      {
+        int x, y;
+        mc_position(idx, si, c, rwd, x, y);
+        x -= ox; y -= oy;
+        if(x >= 0 && y >= 0 && x < wd_out && y < ht_out) out[(size_t)y * wd_out + x] = mc_store(r[c] + refval[idx]);
+      }
+    }
+    off += mc_block_bytes(cnt);
+  }
+}
+// test data: a frame encoded so that the decoder above gives it back. The bit
+// layout of each count is found by decoding single set bits (the decoder only
+// moves bits), the reference is the block's minimum and the count the width of
+// its largest delta (counts 7 and 9 are stored as given, 11..16 as 15).
+extern "C" size_t oracle_mcraw_encode(const uint16_t *img, int rwd, int ht, int force_cnt,
+    uint8_t *bitcnt, uint16_t *refval, uint8_t *data, size_t cap)
+{
+  static int map[16][64][16];   // [cnt][sample][bit] -> byte * 8 + bit
+  static bool ready = false;
+  if(!ready)
+  {
+    for(int cnt = 1; cnt < 16; cnt++)
+    {
+      for(int j = 0; j < 64; j++) for(int q = 0; q < 16; q++) map[cnt][j][q] = -1;
+      for(uint32_t b = 0; b < mc_block_bytes((uint32_t)cnt); b++) for(int t = 0; t < 8; t++)
+      {
+        uint8_t d[128] = { 0 };
+        d[b] = (uint8_t)(1u << t);
+        for(int si = 0; si < 32; si++)
+        {
+          uint32_t r[2];
+          mc_decode_pair((uint32_t)cnt, d, si, r);
+          for(int c = 0; c < 2; c++) for(int q = 0; q < 16; q++)
+            if((r[c] >> q) & 1) map[cnt][2 * si + c][q] = (int)(8 * b + t);
+        }
+      }
+    }
+    ready = true;
+  }
+  const uint32_t blocks = (uint32_t)rwd * (uint32_t)ht / 64;
+  memset(bitcnt, 0, (blocks + 1) / 2);
+  size_t off = 0;
+  for(uint32_t idx = 0; idx < blocks; idx++)
+  {
+    uint32_t v[64], mn = 0xffff, mx = 0;
+    for(int si = 0; si < 32; si++) for(int c = 0; c < 2; c++)
+    {
+      int x, y;
+      mc_position(idx, si, c, rwd, x, y);
+      v[2 * si + c] = img[(size_t)y * rwd + x];
+      mn = std::min(mn, v[2 * si + c]);
+      mx = std::max(mx, v[2 * si + c]);
+    }
+    int bits = 0;
+    while(bits < 16 && ((mx - mn) >> bits)) bits++;
+    int cnt = force_cnt >= 0 ? std::max(force_cnt, bits) : bits;
+    if(cnt > 10) cnt = 15;
+    const int width = cnt == 7 ? 8 : cnt == 9 ? 10 : cnt == 15 ? 16 : cnt;
+    bitcnt[idx / 2] |= (uint8_t)(cnt << ((idx & 1) ? 4 : 0));
+    refval[idx] = (uint16_t)mn;
+    const uint32_t nb = mc_block_bytes((uint32_t)cnt);
+    if(off + nb > cap) return 0;
+    memset(data + off, 0, nb);
+    for(int j = 0; j < 64; j++) for(int q = 0; q < width; q++)
+      if(((v[j] - mn) >> q) & 1)
+      {
+        const int pos = map[cnt][j][q];
+        if(pos < 0) return 0;
+        data[off + pos / 8] |= (uint8_t)(1u << (pos % 8));
+      }
+    off += nb;
+  }
+  return off;
+}
+
 extern "C" void oracle_rcd(const float *cfa, int wd, int ht, const float wb[3], float *out)
 { // demosaic/rcd_conv.comp + rcd_fill.comp on an f16 mosaic (FP32 build)
   img_t<float> in(wd, ht, 1);

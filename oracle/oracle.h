@@ -109,6 +109,14 @@ void oracle_rcd(const float *cfa, int wd, int ht, const float wb[3], float *out)
  * bpp bits per pixel (10, 12, 14, 16) into npix u16 values; and its inverse */
 void oracle_unpack_mlv(const uint8_t *packed, size_t bytes, int bpp, size_t npix, uint16_t *out);
 void oracle_pack_mlv(const uint16_t *in, size_t npix, int bpp, uint8_t *packed, size_t bytes);
+/* i-mcraw/prefix.comp + decode.comp: a motioncam frame of rwd x ht samples in
+ * blocks of 64 (bit count nibbles, reference values, block data) into the
+ * wd_out x ht_out u16 mosaic offset by (ox, oy); and a test encoder (returns the
+ * data bytes, 0 if cap is too small; force_cnt >= 0 raises every count to it) */
+void oracle_mcraw_decode(const uint8_t *bitcnt, const uint16_t *refval, const uint8_t *data, size_t data_bytes,
+    int rwd, int ht, int ox, int oy, int wd_out, int ht_out, uint16_t *out);
+size_t oracle_mcraw_encode(const uint16_t *img, int rwd, int ht, int force_cnt,
+    uint8_t *bitcnt, uint16_t *refval, uint8_t *data, size_t cap);
 /* CFA colour index at a pixel: 0 red, 1 green, 2 blue (demosaic/splat.comp:167-222) */
 int oracle_cfa_colour(uint32_t filters, int x, int y);
 /* round to IEEE half (RTNE) and back */

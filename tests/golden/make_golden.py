@@ -23,7 +23,8 @@ sys.path.insert(0, os.path.join(ROOT, "tests"))
 import oracle                      # noqa: E402
 import vkdt_gb300 as v             # noqa: E402
 from oracle import glsl_ref        # noqa: E402
-from golden_cases import CASES, NOISE_A, NOISE_B, img_param, oracle_params, path   # noqa: E402
+from golden_cases import (CASES, MCRAW_BYTES, MCRAW_CASES, NOISE_A, NOISE_B, img_param, mcraw_stream,   # noqa: E402
+                          oracle_params, path)
 
 
 def main():
@@ -49,6 +50,22 @@ def main():
         arrays["meta"] = np.frombuffer(json.dumps(meta).encode(), np.uint8)
         np.savez_compressed(path(name), **arrays)
         print("%-24s %s" % (name, ", ".join(stages)))
+    for name, case in MCRAW_CASES.items():
+        if only and name not in only:
+            continue
+        rwd, ht, ox, oy, seed = case
+        bitcnt, refval, data = mcraw_stream(rwd, ht, seed)
+        W, H = (rwd - ox) // 2 * 2, (ht - oy) // 2 * 2
+        sizes = [MCRAW_BYTES.get((int(bitcnt[i // 2]) >> (4 * (i & 1))) & 15, 128) for i in range(rwd * ht // 64)]
+        offs = np.cumsum(sizes).astype(np.uint32)   # i-mcraw/prefix.comp: the inclusive sum
+        out = glsl_ref.Img(W, H, 1, glsl_ref.UNORM16)
+        glsl_ref.run("i_mcraw_decode", rwd * ht // 64 * 8, 1, {0: out}, push=glsl_ref.u32(ox, oy, rwd, ht),
+                     buffers={1: bitcnt, 2: offs, 3: refval, 4: np.concatenate([data, np.zeros(128, np.uint8)])})
+        codes = np.rint(out.a[..., 0] * 65535).astype(np.uint16)
+        meta = {"case": list(case)}
+        np.savez_compressed(path(name), bitcnt=bitcnt, refval=refval, data=data, out=codes,
+                            meta=np.frombuffer(json.dumps(meta).encode(), np.uint8))
+        print("%-24s i-mcraw decode" % name)
 
 
 if __name__ == "__main__":

@@ -41,6 +41,37 @@ CASES = {
     "bayer_120x90_halfsize": (120, 90, BAYER, 15, 16383.0, {"dm_method": 2}, ("demosaic", "llap")),
 }
 
+# i-mcraw decode cases: (rwd, ht, ox, oy, seed) of a random frame stream (every bit count)
+MCRAW_CASES = {
+    "mcraw_256x16": (256, 16, 0, 0, 1),
+    "mcraw_320x24_crop": (320, 24, 1, 1, 2),
+}
+MCRAW_BYTES = {0: 0, 1: 8, 2: 16, 3: 24, 4: 32, 5: 40, 6: 48, 7: 64, 8: 64, 9: 80, 10: 80}
+
+
+def mcraw_stream(rwd, ht, seed):
+    """the random stream of a case: nibble counts (every count 0..15), references, data"""
+    rng = np.random.default_rng(seed)
+    blocks = rwd * ht // 64
+    nib = rng.integers(0, 16, blocks)
+    nib[:16] = np.arange(16)
+    bitcnt = np.zeros((blocks + 1) // 2, np.uint8)
+    for i, n in enumerate(nib):
+        bitcnt[i // 2] |= int(n) << (4 * (i & 1))
+    size = sum(MCRAW_BYTES.get(int(n), 128) for n in nib)
+    refval = rng.integers(0, 20000, blocks).astype(np.uint16)
+    data = rng.integers(0, 256, size).astype(np.uint8)
+    return bitcnt, refval, data
+
+
+def load_mcraw(name):
+    z = np.load(path(name))
+    meta = json.loads(bytes(z["meta"]).decode())
+    if tuple(meta["case"]) != tuple(MCRAW_CASES[name]):
+        raise RuntimeError("fixture %s was made for another case definition" % name)
+    return z["bitcnt"], z["refval"], z["data"], MCRAW_CASES[name], z["out"]
+
+
 # oracle parameter field -> (module, parameter) of the graph configuration
 PARAM_MAP = {
     "dn_strength": ("denoise", "strength"),

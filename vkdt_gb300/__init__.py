@@ -105,6 +105,26 @@ def unpack_mlv(d_packed, nbytes, bits_per_pixel, wd, ht, d_mosaic, stream=0):
                                           C.c_void_p(stream)), "unpack_mlv")
 
 
+def mcraw_decode(d_bitcnt, d_refval, d_data, data_bytes, rwd, ht, d_mosaic, ox=0, oy=0, wd=None, hgt=None,
+                 d_scratch=None, stream=0):
+    """vkdt_cuda_mcraw_decode: a motioncam frame (device buffers of bit counts, reference
+    values and block data) into a device u16 mosaic of wd x hgt offset by (ox, oy). Without
+    d_scratch a scratch buffer is allocated and the call waits for the device."""
+    wd = rwd - ox if wd is None else wd
+    hgt = ht - oy if hgt is None else hgt
+    keep = None
+    if d_scratch is None:
+        import torch
+        keep = torch.empty(max(8, _lib.lib().vkdt_cuda_mcraw_scratch_bytes(rwd, ht)), dtype=torch.uint8, device="cuda")
+        d_scratch = keep.data_ptr()
+    check(_lib.lib().vkdt_cuda_mcraw_decode(C.c_void_p(d_bitcnt), C.c_void_p(d_refval), C.c_void_p(d_data), data_bytes,
+                                            rwd, ht, ox, oy, wd, hgt, C.c_void_p(d_mosaic), C.c_void_p(d_scratch),
+                                            C.c_void_p(stream)), "mcraw_decode")
+    if keep is not None:
+        import torch
+        torch.cuda.synchronize()
+
+
 def rawhist(d_mosaic, wd, ht, img_param, bins=1000, d_scratch=None, stream=0):
     """vkdt_cuda_rawhist: noise statistics of a device mosaic (rawhist module), as a
     (3, bins) array of counts, sums of means and sums of second moments."""

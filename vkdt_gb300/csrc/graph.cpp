@@ -575,10 +575,15 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
       rp.cfa = np.hl; rp.W = g->W; rp.H = g->H;
       for(int k = 0; k < 3; k++) rp.wb[k] = g->ip.whitebalance[k];
       rp.vh = g->at<__half>(g->off_vh); rp.pq = g->at<__half>(g->off_pq); rp.lp = g->at<__half>(g->off_lpf);
-      rp.out = np.dm;
+      // rcd_fill applies colour, the histogram and filmcurv to its output pixels;
+      // the demosaic output itself is kept only for the debug stage
+      rp.out = g->debug ? np.dm : nullptr;
+      rp.post = 1;
+      dev_image_t dp = d;
+      dp.W = g->out_w; dp.H = g->out_h;
       for(int stage = 0; stage < 2; stage++)
       {
-        CU(launch_rcd(rp, stage, s));
+        CU(launch_rcd(rp, &dp, stage, s));
         if((r = mark())) return r;
       }
     }
@@ -595,7 +600,7 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
     }
     dev_image_t dp = d;
     dp.W = g->out_w; dp.H = g->out_h;
-    CU(launch_post(dp, np.dm, s));
+    CU(launch_post(dp, g->rcd ? nullptr : np.dm, s));
     if((r = mark())) return r;
   }
   else
@@ -1395,6 +1400,26 @@ int vkdt_cuda_unpack_mlv(const void *d_packed, size_t bytes, int bits_per_pixel,
   if(bytes < npix * (size_t)bits_per_pixel / 8)   // video_mlv.c:213 raw_frame_size
     return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "unpack_mlv: %zu bytes for %zu samples of %d bits", bytes, npix, bits_per_pixel);
   CU(launch_unpack_mlv(d_packed, bytes, bits_per_pixel, npix, (uint16_t *)d_mosaic, (cudaStream_t)stream));
+  return VKDT_CUDA_SUCCESS;
+}
+
+size_t vkdt_cuda_mcraw_scratch_bytes(int rwd, int ht)
+{
+  return rwd > 0 && ht > 0 ? mcraw_scratch_bytes(rwd, ht) : 0;
+}
+
+int vkdt_cuda_mcraw_decode(const void *d_bitcnt, const void *d_refval, const void *d_data, size_t data_bytes,
+                           int rwd, int ht, int ox, int oy, int wd, int hgt, void *d_mosaic, void *d_scratch,
+                           void *stream)
+{
+  if(rwd <= 0 || ht <= 0 || rwd % 64 || ht % 4)
+    return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "mcraw_decode: encoded size %dx%d (width a multiple of 64, height of 4)", rwd, ht);
+  if(!d_bitcnt || !d_refval || !d_data || !d_mosaic || !d_scratch || wd <= 0 || hgt <= 0 || ox < 0 || oy < 0)
+    return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "mcraw_decode: null buffer or empty output");
+  if(((uintptr_t)d_refval & 1) || ((uintptr_t)d_mosaic & 1) || ((uintptr_t)d_scratch & 7))
+    return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "mcraw_decode: unaligned buffer");
+  CU(launch_mcraw_decode(d_bitcnt, d_refval, d_data, data_bytes, rwd, ht, ox, oy, wd, hgt, d_scratch,
+                         (uint16_t *)d_mosaic, (cudaStream_t)stream));
   return VKDT_CUDA_SUCCESS;
 }
 

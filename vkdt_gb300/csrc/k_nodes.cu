@@ -377,7 +377,9 @@ DEV int mirror1(int i, int n)
   return min(max(i, 0), n - 1);
 }
 
-__global__ void __launch_bounds__(NT) k_post(const dev_image_t p, const half4 *__restrict__ dm)
+// FC: the demosaic kernel applied colour, the histogram and filmcurv already
+// (p.rgbf holds the filmcurv output); this kernel reads it for the llap curves
+template<bool FC> __global__ void __launch_bounds__(NT) k_post(const dev_image_t p, const half4 *__restrict__ dm)
 {
   __shared__ __half L0[NPL][LX][2][LH];
   __shared__ uint32_t hist[257];
@@ -398,19 +400,27 @@ __global__ void __launch_bounds__(NT) k_post(const dev_image_t p, const half4 *_
     const int slx = t % LX, sly = t / LX;
     const int vx = X0 - 1 + slx, vy = Y0 - 1 + sly;
     const int px = mirror1(vx, W), py = mirror1(vy, H);
-    float d[4];
-    ld_half4(dm + (size_t)py * W + px, d[0], d[1], d[2], d[3]);
-    float co[3];
-    colour_px(p, d, co);
-    const bool own = vx == px && vy == py && px >= OX && px < OXe && py >= OY && py < OYe;
-    if(own && p.hist)
-    {
-      const uint32_t bin = hist_bin(co[0], co[1], co[2]);
-      if(bin > 0) { atomicAdd(&hist[bin], 1u); atomicAdd(&hist[256], 1u); }
-    }
     float fc[3];
-    filmcurv_px(p, co, fc);
-    if(own) p.rgbf[(size_t)py * W + px] = mk_half4(fc[0], fc[1], fc[2], 1.0f);
+    if(FC)
+    {
+      float a;
+      ld_half4(p.rgbf + (size_t)py * W + px, fc[0], fc[1], fc[2], a);
+    }
+    else
+    {
+      float d[4];
+      ld_half4(dm + (size_t)py * W + px, d[0], d[1], d[2], d[3]);
+      float co[3];
+      colour_px(p, d, co);
+      const bool own = vx == px && vy == py && px >= OX && px < OXe && py >= OY && py < OYe;
+      if(own && p.hist)
+      {
+        const uint32_t bin = hist_bin(co[0], co[1], co[2]);
+        if(bin > 0) { atomicAdd(&hist[bin], 1u); atomicAdd(&hist[256], 1u); }
+      }
+      filmcurv_px(p, co, fc);
+      if(own) p.rgbf[(size_t)py * W + px] = mk_half4(fc[0], fc[1], fc[2], 1.0f);
+    }
     const float yv = lum2020(gclamp(fc[0], -1000.0f, 1000.0f), gclamp(fc[1], -1000.0f, 1000.0f), gclamp(fc[2], -1000.0f, 1000.0f));
     if(unit_curve)
     {
@@ -451,7 +461,7 @@ __global__ void __launch_bounds__(NT) k_post(const dev_image_t p, const half4 *_
         p.l1[k * p.l1plane + (size_t)oy * p.l1w + ox] = f2h(r);
       }
   }
-  if(p.hist)
+  if(!FC && p.hist)
   {
     __syncthreads();
     for(int i = tid; i < 257; i += NT) if(hist[i]) atomicAdd(p.hist + i, hist[i]);
@@ -482,6 +492,7 @@ cudaError_t launch_nodes(const dev_nodes_t &p, int stage, cudaStream_t s)
 
 cudaError_t launch_post(const dev_image_t &p, const half4 *dm, cudaStream_t s)
 {
-  k_post<<<dim3((p.W + TX - 1) / TX, (p.H + TY - 1) / TY), NT, 0, s>>>(p, dm);
+  if(dm) k_post<false><<<dim3((p.W + TX - 1) / TX, (p.H + TY - 1) / TY), NT, 0, s>>>(p, dm);
+  else    k_post<true><<<dim3((p.W + TX - 1) / TX, (p.H + TY - 1) / TY), NT, 0, s>>>(p, dm);
   return cudaGetLastError();
 }

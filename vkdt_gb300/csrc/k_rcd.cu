@@ -21,7 +21,9 @@
 // operations are f16 operations (__hsub), so the output equals the oracle's
 // bit for bit.
 #include "common.cuh"
+#include "develop_px.cuh"
 #include "kernels.h"
+#include "pixel.cuh"
 
 namespace {
 
@@ -61,6 +63,7 @@ __global__ void __launch_bounds__(256) k_rcd_conv(const dev_rcd_t p)
   __shared__ float fh[RC_CY + 2][RC_CX];                        // horizontal response, rows -1..16
   __shared__ float d1[RC_CY + 2][RC_CX + 2], d2[RC_CY + 2][RC_CX + 2];   // diagonal responses, -1..64 x -1..16
   const int x0 = blockIdx.x * RC_CX, y0 = blockIdx.y * RC_CY, tid = threadIdx.x;
+#pragma unroll 4
   for(int i = tid; i < (RC_CY + 2 * RC_H) * (RC_CX + 2 * RC_H); i += 256)
   { // the mosaic through the sampler at texel centres: mirrored
     const int ly = i / (RC_CX + 2 * RC_H), lx = i % (RC_CX + 2 * RC_H);
@@ -127,9 +130,10 @@ __global__ void __launch_bounds__(256) k_rcd_conv(const dev_rcd_t p)
 // pixel pairs of four tile rows; the mosaic, vh, pq and lp the tile reads
 // are staged in shared memory first (mirrored or zero filled as the shader
 // reads them).
-__global__ void __launch_bounds__(256, 4) k_rcd_fill(const dev_rcd_t p)
+template<bool POST> __global__ void __launch_bounds__(256, 4) k_rcd_fill(const dev_rcd_t p, const dev_image_t d)
 {
   __shared__ __half sh[3][RF_PAD + RF_N + RF_PAD];   // shm_r, shm_g, shm_b
+  __shared__ uint32_t hist[257];
   __shared__ __half scf[CF_H][CF_W], svh[VH_H][VH_W], spq[HQ_H][HQ_W], slp[HQ_H][HQ_W];
   const int tid = threadIdx.x, lx = tid & 31, ly0 = tid >> 5;
   const int ox = blockIdx.x * RF_SX - RF_B, oy = blockIdx.y * RF_SY - RF_B;   // the tile's first pixel
@@ -139,17 +143,21 @@ __global__ void __launch_bounds__(256, 4) k_rcd_fill(const dev_rcd_t p)
   for(int i = tid; i < RF_PAD; i += 256)
 #pragma unroll
     for(int c = 0; c < 3; c++) { sh[c][i] = zero; sh[c][RF_PAD + RF_N + i] = zero; }
+  if(POST && d.hist) for(int i = tid; i < 257; i += 256) hist[i] = 0;
+#pragma unroll 4
   for(int i = tid; i < CF_H * CF_W; i += 256)
   { // texelFetch of the mosaic: 0 outside
     const int yy = i / CF_W, xx = i % CF_W;
     const int gx = ox + CF_X0 + xx, gy = oy + CF_Y0 + yy;
     scf[yy][xx] = (gx >= 0 && gy >= 0 && gx < p.W && gy < p.H) ? p.cfa[(size_t)gy * p.W + gx] : zero;
   }
+#pragma unroll 4
   for(int i = tid; i < VH_H * VH_W; i += 256)
   { // texture() at texel centres: mirrored
     const int yy = i / VH_W, xx = i % VH_W;
     svh[yy][xx] = p.vh[(size_t)mirror_any(oy + VH_Y0 + yy, p.H) * p.W + mirror_any(ox + VH_X0 + xx, p.W)];
   }
+#pragma unroll 2
   for(int i = tid; i < HQ_H * HQ_W; i += 256)
   {
     const int yy = i / HQ_W, xx = i % HQ_W;
@@ -230,9 +238,10 @@ __global__ void __launch_bounds__(256, 4) k_rcd_fill(const dev_rcd_t p)
   __syncthreads();
 #pragma unroll 1
   for(int ly = ly0; ly < RF_TY; ly += 8)
-  { // red and blue at green
+  { // red and blue at green; the last stage: only the pixels the tile writes
     const int kg = cfa_bayer(ox + 2 * lx, oy + ly) == 1 ? 0 : 1;
     const int x = 2 * lx + kg, y = ly, o = RF_PAD + RF_TX * y + x;
+    if(x < RF_B || y < RF_B || x >= RF_TX - RF_B || y >= RF_TY - RF_B) continue;
     const __half *sg = sh[1];
     auto S = [&](const __half *a, int dx, int dy) { return a[o + RF_TX * dy + dx]; };
     auto hd = [&](__half a, __half b) { return __half2float(__habs(__hsub(a, b))); };
@@ -264,7 +273,8 @@ __global__ void __launch_bounds__(256, 4) k_rcd_fill(const dev_rcd_t p)
     sh[2][o] = __float2half_rn(res[1]);
   }
   __syncthreads();
-  // the inner 58x26 pixels, divided by the white balance again
+  // the inner 58x26 pixels, divided by the white balance again (the demosaic output,
+  // f16); with POST, colour/main, the histogram and filmcurv/main follow per pixel
 #pragma unroll 1
   for(int ly = ly0; ly < RF_TY; ly += 8)
   {
@@ -276,21 +286,46 @@ __global__ void __launch_bounds__(256, 4) k_rcd_fill(const dev_rcd_t p)
       if(x >= RF_B && ly >= RF_B && x < RF_TX - RF_B && ly < RF_TY - RF_B && gx < p.W && gy < p.H)
       {
         const int o = RF_PAD + RF_TX * ly + x;
-        p.out[(size_t)gy * p.W + gx] = mk_half4(fdiv(h2f(sh[0][o]), p.wb[0]), fdiv(h2f(sh[1][o]), p.wb[1]),
-                                                fdiv(h2f(sh[2][o]), p.wb[2]), 1.0f);
+        const float dm[3] = { f16r(fdiv(h2f(sh[0][o]), p.wb[0])), f16r(fdiv(h2f(sh[1][o]), p.wb[1])),
+                              f16r(fdiv(h2f(sh[2][o]), p.wb[2])) };
+        if(p.out) p.out[(size_t)gy * p.W + gx] = mk_half4(dm[0], dm[1], dm[2], 1.0f);
+        if(POST)
+        {
+          float co[3], fc[3];
+          colour_px(d, dm, co);
+          if(d.hist)
+          {
+            const uint32_t bin = hist_bin(co[0], co[1], co[2]);
+            if(bin > 0) { atomicAdd(&hist[bin], 1u); atomicAdd(&hist[256], 1u); }
+          }
+          filmcurv_px(d, co, fc);
+          d.rgbf[(size_t)gy * p.W + gx] = mk_half4(fc[0], fc[1], fc[2], 1.0f);
+        }
       }
     }
+  }
+  if(POST && d.hist)
+  {
+    __syncthreads();
+    for(int i = tid; i < 257; i += 256) if(hist[i]) atomicAdd(d.hist + i, hist[i]);
   }
 }
 
 } // namespace
 
-cudaError_t launch_rcd(const dev_rcd_t &p, int stage, cudaStream_t s)
+cudaError_t launch_rcd(const dev_rcd_t &p, const dev_image_t *post, int stage, cudaStream_t s)
 {
+  const dim3 gf((p.W + RF_SX - 1) / RF_SX, (p.H + RF_SY - 1) / RF_SY);
   if(stage == 0)
     k_rcd_conv<<<dim3((p.W + RC_CX - 1) / RC_CX, (p.H + RC_CY - 1) / RC_CY), 256, 0, s>>>(p);
-  else if(stage == 1)
-    k_rcd_fill<<<dim3((p.W + RF_SX - 1) / RF_SX, (p.H + RF_SY - 1) / RF_SY), 256, 0, s>>>(p);
+  else if(stage == 1 && p.post && post)
+    k_rcd_fill<true><<<gf, 256, 0, s>>>(p, *post);
+  else if(stage == 1 && !p.post)
+  {
+    dev_image_t none;
+    memset(&none, 0, sizeof(none));
+    k_rcd_fill<false><<<gf, 256, 0, s>>>(p, none);
+  }
   else return cudaErrorInvalidValue;
   return cudaGetLastError();
 }

@@ -126,7 +126,8 @@ struct dev_nodes_t
 // 8 bayer noop + hilite half + level 0 hilite assemble + hilite doub from the mosaic (dn written when set)
 cudaError_t launch_nodes(const dev_nodes_t &p, int stage, cudaStream_t s);
 // colour -> histogram -> filmcurv -> llap curve -> llap level 1 reduce on the
-// demosaic output (p.W x p.H = the output size; p.mosaic unused)
+// demosaic output (p.W x p.H = the output size; p.mosaic unused); with dm null,
+// llap curve -> level 1 reduce on the filmcurv output p.rgbf
 cudaError_t launch_post(const dev_image_t &p, const half4 *dm, cudaStream_t s);
 
 // demosaic RCD (k_rcd.cu): rcd_conv (stage 0) and rcd_fill (stage 1) on the
@@ -138,12 +139,19 @@ struct dev_rcd_t
   float wb[3];           // white balance of the image (the shader's push.wb)
   __half *vh;            // vertical/horizontal discriminator, W*H
   __half *pq, *lp;       // diagonal discriminator and low pass, (W/2)*H
-  half4 *out;            // demosaic output, W*H
+  half4 *out;            // demosaic output, W*H (with post: only for the debug stage, may be null)
+  int post;              // rcd_fill also applies colour, the histogram and filmcurv (writes post->rgbf)
 };
-cudaError_t launch_rcd(const dev_rcd_t &p, int stage, cudaStream_t s);
+// stage 1 with p.post reads the colour/filmcurv constants, rgbf and hist of *post
+cudaError_t launch_rcd(const dev_rcd_t &p, const dev_image_t *post, int stage, cudaStream_t s);
 
 // packed raw video unpack (k_unpack.cu)
 cudaError_t launch_unpack_mlv(const void *packed, size_t bytes, int bpp, size_t npix, uint16_t *out, cudaStream_t s);
+
+// motioncam raw video decode (k_mcraw.cu)
+size_t mcraw_scratch_bytes(int rwd, int ht);
+cudaError_t launch_mcraw_decode(const void *bitcnt, const void *refval, const void *data, size_t data_bytes, int rwd,
+    int ht, int ox, int oy, int W, int H, void *scratch, uint16_t *out, cudaStream_t s);
 
 // rawhist noise statistics (k_rawhist.cu)
 struct dev_rawhist_t

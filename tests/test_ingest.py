@@ -111,7 +111,7 @@ def mc_random_stream(rng, rwd, ht):
     """a random frame stream: every bit count 0..15, random references and data"""
     blocks = rwd * ht // 64
     nib = rng.integers(0, 16, blocks)
-    nib[:16] = np.arange(16)
+    nib[:min(16, blocks)] = np.arange(min(16, blocks))
     bitcnt = np.zeros((blocks + 1) // 2, np.uint8)
     for i, n in enumerate(nib):
         bitcnt[i // 2] |= int(n) << (4 * (i & 1))

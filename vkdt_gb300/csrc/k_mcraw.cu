@@ -16,7 +16,7 @@
 
 namespace {
 
-constexpr int MC_CHUNK = 2048;          // blocks per CTA
+constexpr int MC_CHUNK = 512;           // blocks per CTA (a 4096x2160 frame: 270 CTAs)
 constexpr int MC_NT = 256;
 
 __device__ __forceinline__ uint32_t mc_bytes(uint32_t cnt)

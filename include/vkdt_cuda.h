@@ -283,6 +283,19 @@ int  vkdt_cuda_mcraw_decode(const void *d_bitcnt, const void *d_refval, const vo
                             int rwd, int ht, int ox, int oy, int wd, int hgt, void *d_mosaic, void *d_scratch,
                             void *stream);
 
+/* Output encode after the path (the thumbnail graph's tail, bin/default.i-raw:9-10,16-17).
+ * vkdt_cuda_colenc replaces colenc/main.comp (colenc/main.c create_nodes): rec2020 linear rgba f16
+ * to the output primaries (the colenc `prim` param: 1 rec709, 3 adobergb, 4 p3d65, 5 xyz, 6 ap0,
+ * 7 ap1, 10 redwg, others unchanged) and transfer curve (`trc`: 0 linear, 1 709, 2 sRGB, 3 PQ,
+ * 4 DCI, 5 HLG, 6 gamma 2.2), written as rgba f16 to d_out_f16 and/or as the rgba u8 an 8-bit sink
+ * reads (R8G8B8A8_UNORM stores, alpha 255) to d_out_u8 (either may be null).
+ * vkdt_cuda_bc1_encode replaces o-bc1's host encoder (o-bc1/main.c:21-47, stb_dxt.h): the BC1
+ * blocks (8 bytes each, row major) of the whole 4x4 blocks of an rgba u8 image; d_rgba_u8 4-byte
+ * aligned. Both asynchronous on `stream`. */
+int  vkdt_cuda_colenc(const void *d_rgba_f16, int wd, int ht, int primaries, int trc, void *d_out_f16, void *d_out_u8,
+                      void *stream);
+int  vkdt_cuda_bc1_encode(const void *d_rgba_u8, int wd, int ht, void *d_blocks, void *stream);
+
 /* ---- noise statistics and the noise profile fit (rawhist and nprof modules)
  *
  * rawhist/collect.comp:22-66 over a device mosaic (uint16, row pitch = wd):

@@ -31,6 +31,54 @@ def build(force=False):
     return SO
 
 
+REF_DIR = os.path.join(HERE, "_ref")
+STB_SO = os.path.join(REF_DIR, "libstb_dxt.so")
+STB_SRC = "/root/reference/src/pipe/modules/o-bc1"
+
+
+def build_stb_ref():
+    """Compile the reference's vendored stb_dxt (where it lies in the vkdt tree)
+    into oracle/_ref/libstb_dxt.so; False where the vkdt tree is absent."""
+    if os.path.exists(STB_SO):
+        return True
+    if not os.path.isfile(os.path.join(STB_SRC, "stb_dxt.h")):
+        return False
+    os.makedirs(REF_DIR, exist_ok=True)
+    cmd = ["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-I" + STB_SRC, "-o", STB_SO,
+           os.path.join(HERE, "stb_ref.c"), "-lm"]
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+    if r.returncode != 0:
+        raise RuntimeError("stb_dxt build failed:\n" + r.stdout.decode())
+    return True
+
+
+def stb_bc1(rgba):
+    """the reference's own encoder on an rgba u8 image (H x W x 4)"""
+    rgba = np.ascontiguousarray(rgba, np.uint8)
+    ht, wd = rgba.shape[:2]
+    out = np.zeros((ht // 4) * (wd // 4) * 8, np.uint8)
+    C.CDLL(STB_SO).stb_ref_bc1(rgba.ctypes.data_as(C.c_void_p), wd, ht, out.ctypes.data_as(C.c_void_p))
+    return out
+
+
+def colenc(rgba, prim, trc):
+    """colenc restated: H x W x 4 float rgba in, FP32 rgba out"""
+    rgba = np.ascontiguousarray(rgba, np.float32)
+    ht, wd = rgba.shape[:2]
+    out = np.zeros((ht, wd, 4), np.float32)
+    lib().oracle_colenc(rgba.ctypes.data, wd, ht, prim, trc, out.ctypes.data)
+    return out
+
+
+def bc1_encode(rgba):
+    """o-bc1 restated: BC1 blocks of an rgba u8 image (H x W x 4), 8 bytes per whole 4x4 block"""
+    rgba = np.ascontiguousarray(rgba, np.uint8)
+    ht, wd = rgba.shape[:2]
+    out = np.zeros((ht // 4) * (wd // 4) * 8, np.uint8)
+    lib().oracle_bc1_encode(rgba.ctypes.data, wd, ht, out.ctypes.data)
+    return out
+
+
 class ImgParam(C.Structure):
     _fields_ = [
         ("black", C.c_float * 4), ("white", C.c_float * 4), ("whitebalance", C.c_float * 4),
@@ -92,6 +140,8 @@ def lib():
         l.oracle_mcraw_encode.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.c_size_t]
         l.oracle_mcraw_encode.restype = C.c_size_t
+        l.oracle_colenc.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
+        l.oracle_bc1_encode.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p]
         l.oracle_rcd.argtypes = [C.POINTER(C.c_float), C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
         _lib = l
     return _lib

@@ -1568,6 +1568,264 @@ extern "C" size_t oracle_mcraw_encode(const uint16_t *img, int rwd, int ht, int 
   return off;
 }
 
+// ------------------------------------------------------------------ output encode: BC1 (o-bc1)
+// o-bc1/main.c:21-47 compresses every 4x4 block of the rgba u8 thumbnail with
+// the vendored stb_dxt (o-bc1/stb_dxt.h v1.08b: stb_compress_dxt_block, no
+// alpha, normal mode: no dither, one refinement). Restated step by step:
+// endpoints from the principal axis (four power iterations on the colour
+// covariance), indices by projection onto the endpoint line, one least
+// squares refinement of the endpoints, the optimal single colour tables for
+// constant blocks. Integer work as there; the float and double steps in the
+// same order (the oracle builds without contraction).
+namespace bc1 {
+struct tables_t { uint8_t om5[256][2], om6[256][2]; };
+static inline int e5(int i) { return (i << 3) | (i >> 2); }
+static inline int e6(int i) { return (i << 2) | (i >> 4); }
+static inline int mul8(int a, int b) { const int t = a * b + 128; return (t + (t >> 8)) >> 8; }   // a*b/255, rounded
+static inline int lerp13(int a, int b) { return (2 * a + b) / 3; }
+static void opt_table(uint8_t tab[256][2], int size, int (*ex)(int))
+{ // the endpoint pair whose 1/3 point reproduces a constant best (DX10's 3% rule as a penalty)
+  for(int i = 0; i < 256; i++)
+  {
+    int best = 256;
+    for(int mn = 0; mn < size; mn++) for(int mx = 0; mx < size; mx++)
+    {
+      const int err = std::abs(lerp13(ex(mx), ex(mn)) - i) + std::abs(ex(mx) - ex(mn)) * 3 / 100;
+      if(err < best) { tab[i][0] = (uint8_t)mx; tab[i][1] = (uint8_t)mn; best = err; }
+    }
+  }
+}
+static const tables_t &tables()
+{
+  static tables_t t;
+  static bool done = false;
+  if(!done) { opt_table(t.om5, 32, e5); opt_table(t.om6, 64, e6); done = true; }
+  return t;
+}
+static inline uint16_t to565(int r, int g, int b) { return (uint16_t)((mul8(r, 31) << 11) + (mul8(g, 63) << 5) + mul8(b, 31)); }
+static void palette(uint16_t c0, uint16_t c1, int col[4][3])
+{
+  col[0][0] = e5(c0 >> 11); col[0][1] = e6((c0 >> 5) & 63); col[0][2] = e5(c0 & 31);
+  col[1][0] = e5(c1 >> 11); col[1][1] = e6((c1 >> 5) & 63); col[1][2] = e5(c1 & 31);
+  for(int k = 0; k < 3; k++) { col[2][k] = lerp13(col[0][k], col[1][k]); col[3][k] = lerp13(col[1][k], col[0][k]); }
+}
+static uint32_t match(const uint8_t *px, const int col[4][3])
+{ // indices from the projection onto the endpoint line (stops: the midpoints between palette entries)
+  const int dr = col[0][0] - col[1][0], dg = col[0][1] - col[1][1], db = col[0][2] - col[1][2];
+  int stops[4];
+  for(int k = 0; k < 4; k++) stops[k] = col[k][0] * dr + col[k][1] * dg + col[k][2] * db;
+  const int c0p = (stops[1] + stops[3]) >> 1, half = (stops[3] + stops[2]) >> 1, c3p = (stops[2] + stops[0]) >> 1;
+  uint32_t mask = 0;
+  for(int i = 15; i >= 0; i--)
+  {
+    const int dot = px[4 * i] * dr + px[4 * i + 1] * dg + px[4 * i + 2] * db;
+    mask <<= 2;
+    if(dot < half) mask |= dot < c0p ? 1u : 3u;
+    else           mask |= dot < c3p ? 2u : 0u;
+  }
+  return mask;
+}
+static void pca(const uint8_t *px, uint16_t &mx16, uint16_t &mn16)
+{
+  int mu[3], lo[3], hi[3];
+  for(int c = 0; c < 3; c++)
+  {
+    int sum = px[c];
+    lo[c] = hi[c] = px[c];
+    for(int i = 1; i < 16; i++)
+    {
+      const int v = px[4 * i + c];
+      sum += v;
+      lo[c] = std::min(lo[c], v);
+      hi[c] = std::max(hi[c], v);
+    }
+    mu[c] = (sum + 8) >> 4;
+  }
+  int cov[6] = { 0, 0, 0, 0, 0, 0 };
+  for(int i = 0; i < 16; i++)
+  {
+    const int r = px[4 * i] - mu[0], g = px[4 * i + 1] - mu[1], b = px[4 * i + 2] - mu[2];
+    cov[0] += r * r; cov[1] += r * g; cov[2] += r * b; cov[3] += g * g; cov[4] += g * b; cov[5] += b * b;
+  }
+  float cf[6];
+  for(int i = 0; i < 6; i++) cf[i] = (float)cov[i] / 255.0f;
+  float vr = (float)(hi[0] - lo[0]), vg = (float)(hi[1] - lo[1]), vb = (float)(hi[2] - lo[2]);
+  for(int it = 0; it < 4; it++)
+  {
+    const float r = vr * cf[0] + vg * cf[1] + vb * cf[2];
+    const float g = vr * cf[1] + vg * cf[3] + vb * cf[4];
+    const float b = vr * cf[2] + vg * cf[4] + vb * cf[5];
+    vr = r; vg = g; vb = b;
+  }
+  double magn = std::fabs((double)vr);
+  if(std::fabs((double)vg) > magn) magn = std::fabs((double)vg);
+  if(std::fabs((double)vb) > magn) magn = std::fabs((double)vb);
+  int wr, wg, wb;
+  if(magn < 4.0) { wr = 299; wg = 587; wb = 114; }   // too small: luminance
+  else
+  {
+    magn = 512.0 / magn;
+    wr = (int)((double)vr * magn); wg = (int)((double)vg * magn); wb = (int)((double)vb * magn);
+  }
+  int mind = 0x7fffffff, maxd = -0x7fffffff, imin = 0, imax = 0;
+  for(int i = 0; i < 16; i++)
+  {
+    const int dot = px[4 * i] * wr + px[4 * i + 1] * wg + px[4 * i + 2] * wb;
+    if(dot < mind) { mind = dot; imin = i; }
+    if(dot > maxd) { maxd = dot; imax = i; }
+  }
+  mx16 = to565(px[4 * imax], px[4 * imax + 1], px[4 * imax + 2]);
+  mn16 = to565(px[4 * imin], px[4 * imin + 1], px[4 * imin + 2]);
+}
+static inline int sclamp(float y, int lo, int hi) { const int x = (int)y; return x < lo ? lo : (x > hi ? hi : x); }
+static bool refine(const uint8_t *px, uint16_t &mx16, uint16_t &mn16, uint32_t mask)
+{ // least squares endpoints for the given indices (normal equations, Cramer's rule)
+  const uint16_t omn = mn16, omx = mx16;
+  uint16_t a16, b16;
+  if((mask ^ (mask << 2)) < 4)
+  { // one index for all pixels: the optimal single colour of the average
+    const tables_t &t = tables();
+    int r = 8, g = 8, b = 8;
+    for(int i = 0; i < 16; i++) { r += px[4 * i]; g += px[4 * i + 1]; b += px[4 * i + 2]; }
+    r >>= 4; g >>= 4; b >>= 4;
+    a16 = (uint16_t)((t.om5[r][0] << 11) | (t.om6[g][0] << 5) | t.om5[b][0]);
+    b16 = (uint16_t)((t.om5[r][1] << 11) | (t.om6[g][1] << 5) | t.om5[b][1]);
+  }
+  else
+  {
+    static const int w1[4] = { 3, 0, 2, 1 };
+    int xx = 0, yy = 0, xy = 0, a1[3] = { 0, 0, 0 }, a2[3] = { 0, 0, 0 };
+    uint32_t cm = mask;
+    for(int i = 0; i < 16; i++, cm >>= 2)
+    {
+      const int w = w1[cm & 3];
+      xx += w * w; yy += (3 - w) * (3 - w); xy += w * (3 - w);
+      for(int c = 0; c < 3; c++) { a1[c] += w * px[4 * i + c]; a2[c] += px[4 * i + c]; }
+    }
+    for(int c = 0; c < 3; c++) a2[c] = 3 * a2[c] - a1[c];
+    const float frb = 3.0f * 31.0f / 255.0f / (float)(xx * yy - xy * xy);
+    const float fg = frb * 63.0f / 31.0f;
+    a16 = (uint16_t)((sclamp((float)(a1[0] * yy - a2[0] * xy) * frb + 0.5f, 0, 31) << 11)
+        | (sclamp((float)(a1[1] * yy - a2[1] * xy) * fg + 0.5f, 0, 63) << 5)
+        | sclamp((float)(a1[2] * yy - a2[2] * xy) * frb + 0.5f, 0, 31));
+    b16 = (uint16_t)((sclamp((float)(a2[0] * xx - a1[0] * xy) * frb + 0.5f, 0, 31) << 11)
+        | (sclamp((float)(a2[1] * xx - a1[1] * xy) * fg + 0.5f, 0, 63) << 5)
+        | sclamp((float)(a2[2] * xx - a1[2] * xy) * frb + 0.5f, 0, 31));
+  }
+  mn16 = b16; mx16 = a16;
+  return omn != mn16 || omx != mx16;
+}
+static void block(const uint8_t *px, uint8_t *out)
+{
+  uint32_t mask;
+  uint16_t mx16, mn16;
+  bool constant = true;
+  for(int i = 1; i < 16 && constant; i++) constant = memcmp(px + 4 * i, px, 4) == 0;
+  if(constant)
+  {
+    const tables_t &t = tables();
+    const int r = px[0], g = px[1], b = px[2];
+    mask = 0xaaaaaaaau;
+    mx16 = (uint16_t)((t.om5[r][0] << 11) | (t.om6[g][0] << 5) | t.om5[b][0]);
+    mn16 = (uint16_t)((t.om5[r][1] << 11) | (t.om6[g][1] << 5) | t.om5[b][1]);
+  }
+  else
+  {
+    int col[4][3];
+    pca(px, mx16, mn16);
+    if(mx16 != mn16) { palette(mx16, mn16, col); mask = match(px, col); }
+    else mask = 0;
+    const uint32_t last = mask;
+    if(refine(px, mx16, mn16, mask))
+    {
+      if(mx16 != mn16) { palette(mx16, mn16, col); mask = match(px, col); }
+      else mask = 0;
+    }
+    (void)last;
+  }
+  if(mx16 < mn16) { const uint16_t t = mn16; mn16 = mx16; mx16 = t; mask ^= 0x55555555u; }
+  out[0] = (uint8_t)mx16; out[1] = (uint8_t)(mx16 >> 8); out[2] = (uint8_t)mn16; out[3] = (uint8_t)(mn16 >> 8);
+  for(int k = 0; k < 4; k++) out[4 + k] = (uint8_t)(mask >> (8 * k));
+}
+} // namespace bc1
+
+// colenc/main.comp:15-80: rec2020 linear rgb to the output primaries
+// (matrices.h, row major) and transfer curve; out: rgba with alpha 1, as FP32
+// values (the f16 store rounds them; an 8-bit sink rounds them to 1/255)
+extern "C" void oracle_colenc(const float *rgba, int wd, int ht, int prim, int trc, float *out)
+{
+  static const double Mp[8][9] = {
+    { 1.66022677, -0.58754761, -0.07283825, -0.12455334, 1.13292605, -0.00834963, -0.01815514, -0.10060303, 1.11899817 },  // rec709
+    { 1.15194302, -0.09753232, -0.05448118, -0.12454585, 1.13290963, -0.00837122, -0.02253539, -0.04979918, 1.07275365 },  // adobergb
+    { 1.34353337, -0.28218904, -0.06142427, -0.06530851, 1.07578268, -0.01048453, 0.00282971, -0.01961215, 1.01717851 },  // p3d65
+    { 0.636958048301290991, 0.144616903586208406, 0.168880975164172054, 0.26270021201126692, 0.677998071518871148,
+      0.0593017164698619384, 4.9999999999999999e-17, 0.0280726930490874452, 1.06098505771079066 },                   // xyz
+    { 6.68685575e-01, 1.51817679e-01, 1.77189677e-01, 4.49002044e-02, 8.62145497e-01, 1.01922441e-01, -2.66851927e-09,
+      2.78271109e-02, 1.05170358 },                                                                                  // ap0
+    { 9.62918591e-01, 1.16137050e-02, 2.55863361e-02, 4.16800770e-04, 9.99378426e-01, -8.82457347e-05, 5.31123331e-03,
+      2.18655328e-02, 9.75907920e-01 },                                                                              // ap1
+    { 0.853263, 0.079695, 0.067042, 0.029375, 0.809195, 0.161430, 0.051575, 0.208097, 0.740329 },                     // redwg
+  };
+  const int mi = prim == 1 ? 0 : prim == 3 ? 1 : prim == 4 ? 2 : prim == 5 ? 3 : prim == 6 ? 4 : prim == 7 ? 5 : prim == 10 ? 6 : -1;
+  OMP_FOR
+  for(int y = 0; y < ht; y++) for(int x = 0; x < wd; x++)
+  {
+    const float *p = rgba + 4 * ((size_t)y * wd + x);
+    float c[3] = { p[0], p[1], p[2] };
+    if(mi >= 0)
+    {
+      float o[3];
+      for(int j = 0; j < 3; j++)
+      {
+        float a = 0.0f;
+        for(int i = 0; i < 3; i++) a = a + (float)Mp[mi][3 * j + i] * c[i];
+        o[j] = a;
+      }
+      for(int j = 0; j < 3; j++) c[j] = o[j];
+    }
+    for(int k = 0; k < 3; k++)
+    {
+      float v = c[k];
+      if(trc == 1)
+      {
+        const float a = 1.09929682680944f, b = 0.018053968510807f;
+        v = v > b ? std::pow(v, 1.0f / 2.2f) * a - (a - 1.0f) : v * 4.5f;
+      }
+      else if(trc == 2) v = v > 0.0031308f ? std::pow(v, 1.0f / 2.4f) * 1.055f - 0.055f : v * 12.92f;
+      else if(trc == 3)
+      {
+        const float c3 = 2392.0f / 128.0f, c2 = 2413.0f / 128.0f, c1 = c3 - c2 + 1.0f, m1 = 1305.0f / 8192.0f, m2 = 2523.0f / 32.0f;
+        const float q = std::pow(std::fmax(0.0f, v), m1);
+        const float num = (c1 - 1.0f) + (c2 - c3) * q, den = 1.0f + c3 * q;
+        v = std::pow(1.0f + num / den, m2);
+      }
+      else if(trc == 4) v = std::pow(v, 1.0f / 2.6f);
+      else if(trc == 5)
+      {
+        const float a = 0.17883277f, b = 1.0f - 4.0f * a, cc = 0.5f - a * std::log(4.0f * a);
+        v = v > 1.0f / 12.0f ? a * std::log(12.0f * v - b) + cc : std::sqrt(3.0f * v);
+      }
+      else if(trc == 6) v = std::pow(v, 1.0f / 2.2f);
+      c[k] = v;
+    }
+    float *o = out + 4 * ((size_t)y * wd + x);
+    o[0] = c[0]; o[1] = c[1]; o[2] = c[2]; o[3] = 1.0f;
+  }
+}
+
+// the blocks of an rgba u8 image, wd/4 x ht/4 of 8 bytes (o-bc1/main.c:30-47: partial blocks are dropped)
+extern "C" void oracle_bc1_encode(const uint8_t *rgba, int wd, int ht, uint8_t *out)
+{
+  const int bx = wd / 4, by = ht / 4;
+  for(int j = 0; j < by; j++) for(int i = 0; i < bx; i++)
+  {
+    uint8_t blk[64];
+    for(int jj = 0; jj < 4; jj++) for(int ii = 0; ii < 4; ii++) for(int c = 0; c < 4; c++)
+      blk[4 * (4 * jj + ii) + c] = rgba[4 * ((size_t)wd * (4 * j + jj) + (4 * i + ii)) + c];
+    bc1::block(blk, out + 8 * ((size_t)bx * j + i));
+  }
+}
+
 extern "C" void oracle_rcd(const float *cfa, int wd, int ht, const float wb[3], float *out)
 { // demosaic/rcd_conv.comp + rcd_fill.comp on an f16 mosaic (FP32 build)
   img_t<float> in(wd, ht, 1);

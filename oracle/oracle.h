@@ -117,6 +117,11 @@ void oracle_mcraw_decode(const uint8_t *bitcnt, const uint16_t *refval, const ui
     int rwd, int ht, int ox, int oy, int wd_out, int ht_out, uint16_t *out);
 size_t oracle_mcraw_encode(const uint16_t *img, int rwd, int ht, int force_cnt,
     uint8_t *bitcnt, uint16_t *refval, uint8_t *data, size_t cap);
+/* colenc/main.comp: rec2020 rgba (floats) to the output primaries and transfer curve, FP32 out */
+void oracle_colenc(const float *rgba, int wd, int ht, int prim, int trc, float *out);
+/* o-bc1/main.c:21-47 with its stb_dxt encoder restated: the BC1 blocks (8 bytes each) of
+ * the whole 4x4 blocks of an rgba u8 image, row major */
+void oracle_bc1_encode(const uint8_t *rgba, int wd, int ht, uint8_t *out);
 /* CFA colour index at a pixel: 0 red, 1 green, 2 blue (demosaic/splat.comp:167-222) */
 int oracle_cfa_colour(uint32_t filters, int x, int y);
 /* round to IEEE half (RTNE) and back */

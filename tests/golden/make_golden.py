@@ -23,8 +23,8 @@ sys.path.insert(0, os.path.join(ROOT, "tests"))
 import oracle                      # noqa: E402
 import vkdt_gb300 as v             # noqa: E402
 from oracle import glsl_ref        # noqa: E402
-from golden_cases import (CASES, MCRAW_BYTES, MCRAW_CASES, NOISE_A, NOISE_B, img_param, mcraw_stream,   # noqa: E402
-                          oracle_params, path)
+from golden_cases import (CASES, ENCODE_COLENC, MCRAW_BYTES, MCRAW_CASES, NOISE_A, NOISE_B,   # noqa: E402
+                          encode_inputs, img_param, mcraw_stream, oracle_params, path)
 
 
 def main():
@@ -66,6 +66,20 @@ def main():
         np.savez_compressed(path(name), bitcnt=bitcnt, refval=refval, data=data, out=codes,
                             meta=np.frombuffer(json.dumps(meta).encode(), np.uint8))
         print("%-24s i-mcraw decode" % name)
+    if not only or "encode" in only:
+        # o-bc1: the reference's own stb_dxt (compiled from the vkdt tree); colenc: its shader
+        if not oracle.build_stb_ref():
+            raise SystemExit("stb_dxt could not be compiled (vkdt sources missing)")
+        img, f = encode_inputs()
+        bc1 = oracle.stb_bc1(img)
+        outs = []
+        for prim, trc in ENCODE_COLENC:
+            src, dst = glsl_ref.Img(f.shape[1], f.shape[0], 4), glsl_ref.Img(f.shape[1], f.shape[0], 4)
+            src.a[...] = f
+            glsl_ref.run("colenc_main", f.shape[1], f.shape[0], {0: src, 1: dst}, uniform=glsl_ref.i32(prim, trc))
+            outs.append(dst.a[..., :3].astype(np.float16))
+        np.savez_compressed(path("encode"), bc1=bc1, colenc=np.stack(outs))
+        print("%-24s o-bc1 (stb_dxt), colenc" % "encode")
 
 
 if __name__ == "__main__":

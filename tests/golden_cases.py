@@ -72,6 +72,37 @@ def load_mcraw(name):
     return z["bitcnt"], z["refval"], z["data"], MCRAW_CASES[name], z["out"]
 
 
+# output encode: BC1 blocks of an rgba u8 image (o-bc1's stb_dxt) and colenc of an rgba f16
+# image at these (primaries, transfer curve) pairs
+ENCODE_COLENC = [(2, 2), (1, 1), (3, 6), (5, 0), (6, 3), (7, 5), (10, 4), (4, 2)]
+
+
+def encode_inputs(seed=3):
+    """the u8 image of the BC1 fixture (random, gradient, few colour and flat blocks side by side)
+    and the f16 image of the colenc fixture"""
+    rng = np.random.default_rng(seed)
+    ht, wd = 48, 64
+    y, x = np.mgrid[0:ht, 0:wd]
+    img = np.zeros((ht, wd, 4), np.uint8)
+    img[:, :16] = rng.integers(0, 256, (ht, 16, 4))
+    img[:, 16:32, 0] = (x[:, 16:32] * 7) % 256
+    img[:, 16:32, 1] = (y[:, 16:32] * 5) % 256
+    img[:, 16:32, 2] = ((x + y)[:, 16:32] * 3) % 256
+    pal = rng.integers(0, 256, (3, 4))
+    img[:, 32:48] = pal[rng.integers(0, 3, (ht, 16))]
+    img[:, 48:] = np.clip(100 + rng.integers(-2, 3, (ht, 16, 4)), 0, 255)
+    img[..., 3] = 255
+    img[:4, 48:52] = (17, 200, 33, 255)    # a constant block
+    f = rng.uniform(-0.05, 1.3, (32, 48, 4)).astype(np.float16).astype(np.float32)
+    f[..., 3] = 1.0
+    return img, f
+
+
+def load_encode():
+    z = np.load(path("encode"))
+    return z["bc1"], z["colenc"]
+
+
 # oracle parameter field -> (module, parameter) of the graph configuration
 PARAM_MAP = {
     "dn_strength": ("denoise", "strength"),

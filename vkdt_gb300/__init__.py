@@ -125,6 +125,18 @@ def mcraw_decode(d_bitcnt, d_refval, d_data, data_bytes, rwd, ht, d_mosaic, ox=0
         torch.cuda.synchronize()
 
 
+def colenc(d_rgba_f16, wd, ht, primaries, trc, d_out_f16=0, d_out_u8=0, stream=0):
+    """vkdt_cuda_colenc: rec2020 rgba f16 to output primaries and transfer curve (f16 and/or u8)"""
+    check(_lib.lib().vkdt_cuda_colenc(C.c_void_p(d_rgba_f16), wd, ht, primaries, trc, C.c_void_p(d_out_f16),
+                                      C.c_void_p(d_out_u8), C.c_void_p(stream)), "colenc")
+
+
+def bc1_encode(d_rgba_u8, wd, ht, d_blocks, stream=0):
+    """vkdt_cuda_bc1_encode: BC1 blocks of a device rgba u8 image (o-bc1)"""
+    check(_lib.lib().vkdt_cuda_bc1_encode(C.c_void_p(d_rgba_u8), wd, ht, C.c_void_p(d_blocks), C.c_void_p(stream)),
+          "bc1_encode")
+
+
 def rawhist(d_mosaic, wd, ht, img_param, bins=1000, d_scratch=None, stream=0):
     """vkdt_cuda_rawhist: noise statistics of a device mosaic (rawhist module), as a
     (3, bins) array of counts, sums of means and sums of second moments."""

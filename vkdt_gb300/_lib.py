@@ -121,6 +121,8 @@ _SIGS = {
     "vkdt_cuda_mcraw_scratch_bytes": (C.c_size_t, [C.c_int, C.c_int]),
     "vkdt_cuda_mcraw_decode": (C.c_int, [_P, _P, _P, C.c_size_t, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                          _P, _P, _P]),
+    "vkdt_cuda_colenc": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P, _P]),
+    "vkdt_cuda_bc1_encode": (C.c_int, [_P, C.c_int, C.c_int, _P, _P]),
     "vkdt_cuda_rawhist_scratch_bytes": (C.c_size_t, []),
     "vkdt_cuda_rawhist": (C.c_int, [_P, C.c_int, C.c_int, C.POINTER(ImgParam), C.c_int, _P, C.POINTER(C.c_double), _P]),
     "vkdt_cuda_nprof_fit": (C.c_int, [C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]),

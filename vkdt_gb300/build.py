@@ -20,7 +20,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libvkdt_cuda.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-CU_SOURCES = ["k_hilite.cu", "k_develop.cu", "k_llap.cu", "k_misc.cu", "k_static.cu", "k_denoise.cu", "k_nodes.cu", "k_rawhist.cu", "k_rcd.cu", "k_unpack.cu", "k_mcraw.cu"]
+CU_SOURCES = ["k_hilite.cu", "k_develop.cu", "k_llap.cu", "k_misc.cu", "k_static.cu", "k_denoise.cu", "k_nodes.cu", "k_rawhist.cu", "k_rcd.cu", "k_unpack.cu", "k_mcraw.cu", "k_encode.cu"]
 CPP_SOURCES = ["graph.cpp", "server.cpp"]
 
 

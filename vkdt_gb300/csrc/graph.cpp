@@ -1403,6 +1403,38 @@ int vkdt_cuda_unpack_mlv(const void *d_packed, size_t bytes, int bits_per_pixel,
   return VKDT_CUDA_SUCCESS;
 }
 
+int vkdt_cuda_colenc(const void *d_rgba_f16, int wd, int ht, int primaries, int trc, void *d_out_f16, void *d_out_u8,
+                     void *stream)
+{
+  // colenc/main.comp:23-36 (matrices.h, row major): rec2020 to the output primaries
+  static const double M_p3d65[9] = { 1.34353337, -0.28218904, -0.06142427, -0.06530851, 1.07578268, -0.01048453, 0.00282971, -0.01961215, 1.01717851 };
+  static const double M_adobe[9] = { 1.15194302, -0.09753232, -0.05448118, -0.12454585, 1.13290963, -0.00837122, -0.02253539, -0.04979918, 1.07275365 };
+  static const double M_ap0[9] = { 6.68685575e-01, 1.51817679e-01, 1.77189677e-01, 4.49002044e-02, 8.62145497e-01, 1.01922441e-01, -2.66851927e-09, 2.78271109e-02, 1.05170358 };
+  static const double M_ap1[9] = { 9.62918591e-01, 1.16137050e-02, 2.55863361e-02, 4.16800770e-04, 9.99378426e-01, -8.82457347e-05, 5.31123331e-03, 2.18655328e-02, 9.75907920e-01 };
+  static const double M_redwg[9] = { 0.853263, 0.079695, 0.067042, 0.029375, 0.809195, 0.161430, 0.051575, 0.208097, 0.740329 };
+  if(!d_rgba_f16 || wd <= 0 || ht <= 0 || (!d_out_f16 && !d_out_u8) || trc < 0 || trc > 6)
+    return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "colenc: null buffer, empty image or trc %d", trc);
+  if(((uintptr_t)d_rgba_f16 & 7) || ((uintptr_t)d_out_f16 & 7) || ((uintptr_t)d_out_u8 & 3))
+    return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "colenc: unaligned buffer");
+  const double *m = primaries == 1 ? M_rec2020_to_rec709 : primaries == 3 ? M_adobe : primaries == 4 ? M_p3d65
+                  : primaries == 5 ? M_rec2020_to_xyz : primaries == 6 ? M_ap0 : primaries == 7 ? M_ap1
+                  : primaries == 10 ? M_redwg : nullptr;
+  float M[9];
+  if(m) for(int i = 0; i < 9; i++) M[i] = (float)m[i];
+  CU(launch_colenc(d_rgba_f16, wd, ht, m ? M : nullptr, trc, d_out_f16, d_out_u8, (cudaStream_t)stream));
+  return VKDT_CUDA_SUCCESS;
+}
+
+int vkdt_cuda_bc1_encode(const void *d_rgba_u8, int wd, int ht, void *d_blocks, void *stream)
+{
+  if(!d_rgba_u8 || !d_blocks || wd <= 0 || ht <= 0)
+    return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "bc1_encode: null buffer or empty image");
+  if(((uintptr_t)d_rgba_u8 & 3) || ((uintptr_t)d_blocks & 7))
+    return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "bc1_encode: unaligned buffer");
+  CU(launch_bc1(d_rgba_u8, wd, ht, d_blocks, (cudaStream_t)stream));
+  return VKDT_CUDA_SUCCESS;
+}
+
 size_t vkdt_cuda_mcraw_scratch_bytes(int rwd, int ht)
 {
   return rwd > 0 && ht > 0 ? mcraw_scratch_bytes(rwd, ht) : 0;

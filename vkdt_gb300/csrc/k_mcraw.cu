@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(MC_NT) k_mc_decode(const uint8_t *__restrict__
   base = 0;
   for(int w = 0; w < MC_NT / 32; w++) base += red[w];
   __syncthreads();
-  // exclusive scan of the block sizes: 8 consecutive blocks per thread
+  // exclusive scan of the block sizes: MC_CHUNK / MC_NT consecutive blocks per thread
   constexpr int PER = MC_CHUNK / MC_NT;
   uint32_t sz[PER];
   unsigned long long run = 0;

@@ -153,6 +153,11 @@ size_t mcraw_scratch_bytes(int rwd, int ht);
 cudaError_t launch_mcraw_decode(const void *bitcnt, const void *refval, const void *data, size_t data_bytes, int rwd,
     int ht, int ox, int oy, int W, int H, void *scratch, uint16_t *out, cudaStream_t s);
 
+// output encode (k_encode.cu): colenc to f16 and/or rgba u8 (M: row major rec2020 to the
+// output primaries, null for none); BC1 blocks of an rgba u8 image (rgba 4-byte aligned)
+cudaError_t launch_colenc(const void *rgba16, int wd, int ht, const float *M, int trc, void *out16, void *out8, cudaStream_t s);
+cudaError_t launch_bc1(const void *rgba, int wd, int ht, void *out, cudaStream_t s);
+
 // rawhist noise statistics (k_rawhist.cu)
 struct dev_rawhist_t
 {

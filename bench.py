@@ -491,10 +491,20 @@ def workload_ingest(args, v, torch, sp, clk):
                                                       streams[i][2].data_ptr(), streams[i][3], W, H, outs[i].data_ptr(),
                                                       d_scratch=scratch.data_ptr(), stream=sp),
                              mean_bytes + 2 * npx)
+        del streams
+        # the output side at the same size: colenc of an rgba f16 frame to sRGB u8, BC1 of the u8 frame
+        f16 = [torch.rand(npx * 4, device="cuda", generator=g).half() for _ in range(N // 2)]
+        u8 = [torch.randint(0, 1 << 30, (npx,), dtype=torch.int32, device="cuda", generator=g) for _ in range(N // 2)]
+        bc = [torch.empty(npx // 2, dtype=torch.uint8, device="cuda") for _ in range(N // 2)]
+        res["colenc_u8"] = timed(lambda i: v.colenc(f16[i % (N // 2)].data_ptr(), W, H, 2, 2, 0, u8[i % (N // 2)].data_ptr(), sp),
+                                 npx * (8 + 4))
+        res["bc1"] = timed(lambda i: v.bc1_encode(u8[i % (N // 2)].data_ptr(), W, H, bc[i % (N // 2)].data_ptr(), sp),
+                           npx * 4 + npx // 2)
     return {"workload": "device ingestion of packed raw video frames, 4096x2160: magic lantern 12/14-bit unpack, "
-                        "motioncam block decode (bit counts 5..8)", "frames_in_ring": N,
+                        "motioncam block decode (bit counts 5..8); and the output encode of such a frame: colenc "
+                        "to sRGB u8, BC1", "frames_in_ring": N,
             "roofline_note": "gbs counts the packed bytes read and the u16 mosaic written once per frame"}, \
-        res["mcraw"]["mpix_per_s"], res["mcraw"]["ms_per_frame"], {"ingest": res, "gpu_launches": 2 * K}
+        res["mcraw"]["mpix_per_s"], res["mcraw"]["ms_per_frame"], {"ingest": res, "gpu_launches": 5 * K}
 
 
 def run_workload(args):

@@ -37,19 +37,20 @@ LEVELS = 6
 RING = 4
 DENOISE = 0.0
 DEMOSAIC = 0          # demosaic method: 0 gaussian splats (the raw photo default), 1 rcd, 2 half size
+FILTERS = 0x94949494  # bayer rggb; 9: x-trans
 DEMOSAIC_NAMES = {0: "gaussian splats (method 0)", 1: "rcd (method 1)", 2: "half size (method 2)"}
 
 
 def img_param(v, wd, ht):
     rng = WHITE - BLACK
-    return v.default_img_param(black=BLACK, white=WHITE, wd=wd, ht=ht,
+    return v.default_img_param(black=BLACK, white=WHITE, wd=wd, ht=ht, filters=FILTERS,
                                noise_a=NOISE_A / rng ** 2, noise_b=NOISE_B / rng)
 
 
 def config():
     return {"workload": "%d MP darkroom graph, one image per step%s" % (round(WD * HT / 1e6),
                                                                        ", wavelet denoise" if DENOISE > 0 else ""),
-            "wd": WD, "ht": HT, "cfa": "rggb", "denoise_strength": DENOISE,
+            "wd": WD, "ht": HT, "cfa": "x-trans" if FILTERS == 9 else "rggb", "denoise_strength": DENOISE,
             "bits": 14, "black": BLACK, "white": WHITE, "noise_a_dn": NOISE_A, "noise_b_dn": NOISE_B,
             "llap_levels": LEVELS,
             "graph": "denoise(%s)->hilite->demosaic->colour->filmcurv->llap" % ("wavelet" if DENOISE > 0 else "noop"),
@@ -540,7 +541,7 @@ def run_workload(args):
         torch.distributed.destroy_process_group()
 
 def main():
-    global WD, HT, RING, LEVELS, DENOISE, DEMOSAIC
+    global WD, HT, RING, LEVELS, DENOISE, DEMOSAIC, FILTERS
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
@@ -559,12 +560,14 @@ def main():
     ap.add_argument("--images", type=int, default=64, help="batch: mosaics in the batch")
     ap.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
     ap.add_argument("--slots", type=int, default=4, help="serve/video: jobs in flight")
+    ap.add_argument("--cfa", default="rggb", choices=("rggb", "xtrans"), help="single: the mosaic's colour filter array")
     ap.add_argument("--demosaic", type=int, default=-1, choices=(-1, 0, 1, 2),
                     help="demosaic method (-1: the workload's default: 0 for photos, 1 for the video streams)")
     args = ap.parse_args()
     WD, HT = [int(x) for x in args.size.lower().split("x")]
     RING, LEVELS, DENOISE = args.ring, args.levels, args.denoise
     DEMOSAIC = max(0, args.demosaic)
+    FILTERS = 9 if args.cfa == "xtrans" else 0x94949494
     if args.impl == "reference":
         return run_reference(args)
     if args.workload != "single":
@@ -598,7 +601,7 @@ def main():
             g.set_param("demosaic", "method", np.int32(DEMOSAIC))
         g.alloc()
         src, _ = g.device_buffers()
-        v.scene_device(v.make_scene(WD, HT, seed=1000 * rank + i, image_id=i, a=NOISE_A, b=NOISE_B), src, sp)
+        v.scene_device(v.make_scene(WD, HT, seed=1000 * rank + i, image_id=i, a=NOISE_A, b=NOISE_B, filters=FILTERS), src, sp)
         graphs.append(g)
     torch.cuda.synchronize()
 
@@ -643,7 +646,7 @@ def main():
     gt.set_timing(True)
     gt.alloc()
     src, _ = gt.device_buffers()
-    v.scene_device(v.make_scene(WD, HT, seed=1000 * rank + 7, a=NOISE_A, b=NOISE_B), src, sp)
+    v.scene_device(v.make_scene(WD, HT, seed=1000 * rank + 7, a=NOISE_A, b=NOISE_B, filters=FILTERS), src, sp)
     acc = None
     nt = max(3, min(args.steps, 20))
     for i in range(args.warmup + nt):
@@ -657,7 +660,8 @@ def main():
     kms = acc / nt
     launches_per_step = len(names)
     # the dominant kernel: the fused develop kernel where the graph runs it, else the longest launch
-    dev_idx = names.index("demosaic:fix") if "demosaic:fix" in names else int(np.argmax(kms))
+    fused = "demosaic:fix" in names and FILTERS != 9 and not DEMOSAIC
+    dev_idx = names.index("demosaic:fix") if fused else int(np.argmax(kms))
     dev_ms = float(kms[dev_idx])
     npx, qpx = WD * HT, (WD // 2) * (HT // 2)
     # algorithmic bytes per launch (each buffer the launch must read or write, once):
@@ -674,18 +678,26 @@ def main():
         # llap level 0 assemble + colour: rgba, 11 level 1 planes, level 1 assembled in, rgba out
         "llap:colour": npx * (8 + 8) + 11 * 2 * qpx + 2 * qpx,
     }
+    if not fused:
+        alg_bytes.pop("demosaic:fix")
+        # the x-trans per-node kernels: fix reads the mosaic, the splat green and the covariance
+        # (1/9 size), writes rgba f16; splat reads the mosaic and the covariance, writes the green
+        alg_bytes.update({"demosaic:fix": npx * (2 + 2 + 8) + (WD // 3) * (HT // 3) * 8,
+                          "demosaic:splat": npx * (2 + 2) + (WD // 3) * (HT // 3) * 8})
     alg = alg_bytes.get(names[dev_idx])
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else None
     peak = peaks["hbm_gbs"] if peaks else 6800.0
     achieved = alg / (dev_ms / 1e3) / 1e9 if alg else None
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tp) and names[dev_idx] == "demosaic:fix":
+    if os.path.exists(tp) and fused:
         try:
             traffic = json.load(open(tp)).get("k_develop_bytes_per_launch")
         except Exception:
             traffic = None
-    kname = {"demosaic:fix": "k_develop (hilite doub + demosaic + colour + filmcurv + llap curve/reduce)",
+    kname = {"demosaic:fix": "k_develop (hilite doub + demosaic + colour + filmcurv + llap curve/reduce)" if fused
+             else "k_nd_fix_xt",
+             "demosaic:splat": "k_nd_splat_xt",
              "demosaic:rcd_fill": "k_rcd_fill", "demosaic:rcd_conv": "k_rcd_conv",
              "llap:curve": "k_post (colour + filmcurv + llap curve/reduce)",
              "llap:colour": "k_llap_final (llap assemble level 0 + colour)"}.get(names[dev_idx], names[dev_idx])
@@ -700,9 +712,9 @@ def main():
 
     # ---- e2e: host mosaic in, host rgba f16 out, through the C-ABI run call
     ge = graphs[0]
-    host_in = [v.scene_host(v.make_scene(WD, HT, seed=50 + i, a=NOISE_A, b=NOISE_B)) for i in range(2)] if rank == 0 else None
+    host_in = [v.scene_host(v.make_scene(WD, HT, seed=50 + i, a=NOISE_A, b=NOISE_B, filters=FILTERS)) for i in range(2)] if rank == 0 else None
     if host_in is None:
-        host_in = [v.scene_host(v.make_scene(WD, HT, seed=50 + i + 100 * rank, a=NOISE_A, b=NOISE_B)) for i in range(2)]
+        host_in = [v.scene_host(v.make_scene(WD, HT, seed=50 + i + 100 * rank, a=NOISE_A, b=NOISE_B, filters=FILTERS)) for i in range(2)]
     lat = []
     ne = max(3, min(args.steps, 20))
     for i in range(args.warmup):

@@ -116,9 +116,11 @@ def test_colenc_gpu_matches_oracle(gpu):
             ok = np.isfinite(w16[..., :3]) & np.isfinite(got[..., :3])
             assert np.array_equal(np.isnan(w16[..., :3]), np.isnan(got[..., :3])), (prim, trc)
             a, b = got[..., :3][ok], w16[..., :3][ok]
-            # one f16 step at most (the device pow), at few pixels
+            # one f16 step at most (the device pow), at few pixels; the PQ curve raises to the
+            # power 78.8 and turns one step of its base into a few
             d = np.abs(a - b) / np.maximum(np.abs(b), 6.1e-5)
-            assert d.max() <= 1e-3 and (a != b).mean() <= 0.02, (prim, trc, float(d.max()), float((a != b).mean()))
+            tol = 5e-3 if trc == 3 else 1e-3
+            assert d.max() <= tol and (a != b).mean() <= 0.02, (prim, trc, float(d.max()), float((a != b).mean()))
             u8 = o8.cpu().numpy().view(np.uint8).reshape(ht, wd, 4).astype(np.int32)
             w8 = np.rint(np.clip(np.nan_to_num(want[..., :3], nan=0.0), 0, 1) * 255).astype(np.int32)
             fin = np.isfinite(want[..., :3])

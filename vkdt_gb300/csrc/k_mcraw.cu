@@ -4,10 +4,11 @@
 // of deltas. Four consecutive blocks cover 64 x 4 pixels, one CFA phase each
 // in steps of two pixels.
 //
-// k_mc_sizes: the bytes of every chunk of MC_CHUNK blocks.
-// k_mc_decode: one CTA per chunk; the chunk's byte offset is the sum of the
-// sizes of the chunks before it, the blocks' offsets an exclusive scan in the
-// CTA (integers: any order of addition gives the reference's offsets). A warp
+// k_mc_sizes: the bytes of every chunk of MC_CHUNK blocks; k_mc_scan (one
+// CTA) turns them into the chunks' byte offsets.
+// k_mc_decode: one CTA per chunk; the blocks' offsets are an exclusive scan in
+// the CTA (integers: any order of addition gives the reference's offsets).
+// The chunk's data is staged in shared memory with 8-byte loads, then a warp
 // decodes a block, lane si the two deltas the shader's invocation si
 // extracts; the samples are stored as the reference's R16_UNORM store of
 // (reference + delta) / 65536 leaves them.
@@ -16,8 +17,9 @@
 
 namespace {
 
-constexpr int MC_CHUNK = 512;           // blocks per CTA (a 4096x2160 frame: 270 CTAs)
+constexpr int MC_CHUNK = 256;           // blocks per CTA, one per thread (a 4096x2160 frame: 540 CTAs)
 constexpr int MC_NT = 256;
+constexpr int MC_STAGE = MC_CHUNK * 128; // the chunk's data: at most 128 bytes a block
 
 __device__ __forceinline__ uint32_t mc_bytes(uint32_t cnt)
 { // i-mcraw/prefix.comp:46-63
@@ -53,9 +55,9 @@ __global__ void __launch_bounds__(MC_NT) k_mc_sizes(const uint8_t *__restrict__ 
 
 // i-mcraw/decode.comp:31-282: the two deltas of invocation si of a block whose
 // bytes start at d (n valid bytes; the rest read 0)
-__device__ __forceinline__ void mc_pair(uint32_t cnt, const uint8_t *__restrict__ d, uint32_t n, int si, uint32_t r[2])
+__device__ __forceinline__ void mc_pair(uint32_t cnt, const uint8_t *d, uint32_t n, int si, uint32_t r[2])
 {
-  auto byte = [&](int i) -> uint32_t { return (uint32_t)i < n ? (uint32_t)__ldg(d + i) : 0u; };
+  auto byte = [&](int i) -> uint32_t { return (uint32_t)i < n ? (uint32_t)d[i] : 0u; };
   uint32_t p0, p1;
   auto pr = [&](int reg) { p0 = byte(reg); p1 = byte(reg + 1); };
   switch(cnt)
@@ -129,36 +131,49 @@ __device__ __forceinline__ void mc_pair(uint32_t cnt, const uint8_t *__restrict_
   }
 }
 
-__global__ void __launch_bounds__(MC_NT) k_mc_decode(const uint8_t *__restrict__ bitcnt, const uint16_t *__restrict__ refval,
-    const uint8_t *__restrict__ data, size_t data_bytes, int rwd, int ht, int ox, int oy, int W, int H,
-    const unsigned long long *__restrict__ chunk_bytes, uint16_t *__restrict__ out)
+// the chunks' sizes into their exclusive offsets, in place (one CTA of 1024 threads)
+__global__ void __launch_bounds__(1024) k_mc_scan(unsigned long long *__restrict__ cb, unsigned chunks)
+{
+  __shared__ unsigned long long wsum[32];
+  __shared__ unsigned long long carry_s;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if(tid == 0) carry_s = 0;
+  __syncthreads();
+  for(unsigned b = 0; b < chunks; b += 1024)
+  {
+    const unsigned i = b + tid;
+    const unsigned long long v = i < chunks ? cb[i] : 0ull;
+    unsigned long long incl = v;
+    for(int o = 1; o < 32; o <<= 1)
+    {
+      const unsigned long long t = __shfl_up_sync(0xffffffffu, incl, o);
+      if(lane >= o) incl += t;
+    }
+    if(lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    unsigned long long before = carry_s;
+    for(int w = 0; w < warp; w++) before += wsum[w];
+    if(i < chunks) cb[i] = before + incl - v;
+    __syncthreads();
+    if(tid == 1023) carry_s = before + incl;
+    __syncthreads();
+  }
+}
+
+template<bool ALIGNED> __global__ void __launch_bounds__(MC_NT) k_mc_decode(const uint8_t *__restrict__ bitcnt,
+    const uint16_t *__restrict__ refval, const uint8_t *__restrict__ data, size_t data_bytes, int rwd, int ht, int ox,
+    int oy, int W, int H, const unsigned long long *__restrict__ chunk_off, uint16_t *__restrict__ out)
 {
   __shared__ unsigned long long boff[MC_CHUNK];   // byte offset of each block of the chunk
   __shared__ unsigned long long red[MC_NT / 32];
+  __shared__ __align__(16) uint8_t sd[MC_STAGE];
   const uint32_t blocks = (uint32_t)rwd * (uint32_t)ht / 64;
   const uint32_t b0 = blockIdx.x * MC_CHUNK;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  // the chunk's offset: the bytes of every chunk before it
-  unsigned long long base = 0;
-  for(uint32_t c = tid; c < blockIdx.x; c += MC_NT) base += chunk_bytes[c];
-  for(int o = 16; o > 0; o >>= 1) base += __shfl_xor_sync(0xffffffffu, base, o);
-  if(lane == 0) red[warp] = base;
-  __syncthreads();
-  base = 0;
-  for(int w = 0; w < MC_NT / 32; w++) base += red[w];
-  __syncthreads();
-  // exclusive scan of the block sizes: MC_CHUNK / MC_NT consecutive blocks per thread
-  constexpr int PER = MC_CHUNK / MC_NT;
-  uint32_t sz[PER];
-  unsigned long long run = 0;
-#pragma unroll
-  for(int k = 0; k < PER; k++)
-  {
-    const uint32_t b = b0 + tid * PER + k;
-    sz[k] = b < blocks ? mc_bytes(mc_cnt(bitcnt, b)) : 0u;
-    run += sz[k];
-  }
-  unsigned long long incl = run;   // inclusive scan of the thread sums in the warp, then across warps
+  const unsigned long long base = chunk_off[blockIdx.x];
+  // exclusive scan of the block sizes, one block per thread
+  const uint32_t sz = b0 + tid < blocks ? mc_bytes(mc_cnt(bitcnt, b0 + tid)) : 0u;
+  unsigned long long incl = sz;
   for(int o = 1; o < 32; o <<= 1)
   {
     const unsigned long long t = __shfl_up_sync(0xffffffffu, incl, o);
@@ -168,9 +183,25 @@ __global__ void __launch_bounds__(MC_NT) k_mc_decode(const uint8_t *__restrict__
   __syncthreads();
   unsigned long long wbase = 0;
   for(int w = 0; w < warp; w++) wbase += red[w];
-  unsigned long long o = base + wbase + incl - run;
+  boff[tid] = base + wbase + incl - sz;
+  unsigned long long total = 0;
+  for(int w = 0; w < MC_NT / 32; w++) total += red[w];
+  // stage the chunk's bytes (past data_bytes: 0), 8 at a time (block sizes are multiples of 8)
+  for(unsigned long long w = tid; 8 * w < total; w += MC_NT)
+  {
+    const unsigned long long g = base + 8 * w;
+    uint2 q = make_uint2(0u, 0u);
+    if(ALIGNED && g + 8 <= data_bytes) q = __ldg(reinterpret_cast<const uint2 *>(data + g));
+    else
+    {
+      uint32_t b[8];
 #pragma unroll
-  for(int k = 0; k < PER; k++) { boff[tid * PER + k] = o; o += sz[k]; }
+      for(int k = 0; k < 8; k++) b[k] = g + k < data_bytes ? (uint32_t)__ldg(data + g + k) : 0u;
+      q.x = b[0] | (b[1] << 8) | (b[2] << 16) | (b[3] << 24);
+      q.y = b[4] | (b[5] << 8) | (b[6] << 16) | (b[7] << 24);
+    }
+    *reinterpret_cast<uint2 *>(sd + 8 * w) = q;
+  }
   __syncthreads();
   // decode: a warp per block
   const int bpr = rwd / 64;
@@ -179,10 +210,9 @@ __global__ void __launch_bounds__(MC_NT) k_mc_decode(const uint8_t *__restrict__
     const uint32_t idx = b0 + j;
     if(idx >= blocks) break;
     const uint32_t cnt = mc_cnt(bitcnt, idx);
-    const unsigned long long off = boff[j];
-    const uint32_t n = off >= data_bytes ? 0u : (uint32_t)min((unsigned long long)128, data_bytes - off);
+    const uint32_t o = (uint32_t)(boff[j] - base);
     uint32_t r[2];
-    mc_pair(cnt, data + (off < data_bytes ? off : 0), n, lane, r);
+    mc_pair(cnt, sd + o, (uint32_t)min((unsigned long long)128, total - o), lane, r);
     const uint32_t ref = __ldg(refval + idx);
     const uint32_t k = idx / 4;
     int x = 64 * (int)(k % bpr), y = 4 * (int)(k / bpr);
@@ -218,7 +248,12 @@ cudaError_t launch_mcraw_decode(const void *bitcnt, const void *refval, const vo
   if(!chunks) return cudaSuccess;
   unsigned long long *cb = reinterpret_cast<unsigned long long *>(scratch);
   k_mc_sizes<<<chunks, MC_NT, 0, s>>>(reinterpret_cast<const uint8_t *>(bitcnt), blocks, cb);
-  k_mc_decode<<<chunks, MC_NT, 0, s>>>(reinterpret_cast<const uint8_t *>(bitcnt), reinterpret_cast<const uint16_t *>(refval),
-      reinterpret_cast<const uint8_t *>(data), data_bytes, rwd, ht, ox, oy, W, H, cb, out);
+  k_mc_scan<<<1, 1024, 0, s>>>(cb, chunks);
+  if(((uintptr_t)data & 7) == 0)
+    k_mc_decode<true><<<chunks, MC_NT, 0, s>>>(reinterpret_cast<const uint8_t *>(bitcnt), reinterpret_cast<const uint16_t *>(refval),
+        reinterpret_cast<const uint8_t *>(data), data_bytes, rwd, ht, ox, oy, W, H, cb, out);
+  else
+    k_mc_decode<false><<<chunks, MC_NT, 0, s>>>(reinterpret_cast<const uint8_t *>(bitcnt), reinterpret_cast<const uint16_t *>(refval),
+        reinterpret_cast<const uint8_t *>(data), data_bytes, rwd, ht, ox, oy, W, H, cb, out);
   return cudaGetLastError();
 }

@@ -16,6 +16,12 @@ import oracle
 import vkdt_gb300 as v
 
 
+def _ordered(x):
+    """f16 values as integers in the order of the values (one f16 step apart: 1 apart)"""
+    i = np.asarray(x, np.float32).astype(np.float16).view(np.int16).astype(np.int32)
+    return np.where(i < 0, -(i & 0x7fff), i)
+
+
 def _same(a, b):
     return np.array_equal(np.nan_to_num(a, nan=-7.0), np.nan_to_num(b, nan=-7.0))
 
@@ -118,9 +124,9 @@ def test_colenc_gpu_matches_oracle(gpu):
             a, b = got[..., :3][ok], w16[..., :3][ok]
             # one f16 step at most (the device pow), at few pixels; the PQ curve raises to the
             # power 78.8 and turns one step of its base into a few
-            d = np.abs(a - b) / np.maximum(np.abs(b), 6.1e-5)
-            tol = 5e-3 if trc == 3 else 1e-3
-            assert d.max() <= tol and (a != b).mean() <= 0.02, (prim, trc, float(d.max()), float((a != b).mean()))
+            steps = np.abs(_ordered(a) - _ordered(b))
+            tol = 4 if trc == 3 else 1
+            assert steps.max() <= tol and (a != b).mean() <= 0.02, (prim, trc, int(steps.max()), float((a != b).mean()))
             u8 = o8.cpu().numpy().view(np.uint8).reshape(ht, wd, 4).astype(np.int32)
             w8 = np.rint(np.clip(np.nan_to_num(want[..., :3], nan=0.0), 0, 1) * 255).astype(np.int32)
             fin = np.isfinite(want[..., :3])

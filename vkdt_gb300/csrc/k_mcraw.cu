@@ -167,12 +167,15 @@ template<bool ALIGNED> __global__ void __launch_bounds__(MC_NT) k_mc_decode(cons
   __shared__ unsigned long long boff[MC_CHUNK];   // byte offset of each block of the chunk
   __shared__ unsigned long long red[MC_NT / 32];
   __shared__ __align__(16) uint8_t sd[MC_STAGE];
+  __shared__ uint32_t scr[MC_CHUNK];              // bit count | reference << 8 of each block
   const uint32_t blocks = (uint32_t)rwd * (uint32_t)ht / 64;
   const uint32_t b0 = blockIdx.x * MC_CHUNK;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const unsigned long long base = chunk_off[blockIdx.x];
   // exclusive scan of the block sizes, one block per thread
-  const uint32_t sz = b0 + tid < blocks ? mc_bytes(mc_cnt(bitcnt, b0 + tid)) : 0u;
+  const uint32_t cnt0 = b0 + tid < blocks ? mc_cnt(bitcnt, b0 + tid) : 0u;
+  const uint32_t sz = mc_bytes(cnt0);
+  scr[tid] = cnt0 | (b0 + tid < blocks ? (uint32_t)__ldg(refval + b0 + tid) << 8 : 0u);
   unsigned long long incl = sz;
   for(int o = 1; o < 32; o <<= 1)
   {
@@ -209,11 +212,11 @@ template<bool ALIGNED> __global__ void __launch_bounds__(MC_NT) k_mc_decode(cons
   {
     const uint32_t idx = b0 + j;
     if(idx >= blocks) break;
-    const uint32_t cnt = mc_cnt(bitcnt, idx);
+    const uint32_t cr = scr[j], cnt = cr & 0xffu;
     const uint32_t o = (uint32_t)(boff[j] - base);
     uint32_t r[2];
     mc_pair(cnt, sd + o, (uint32_t)min((unsigned long long)128, total - o), lane, r);
-    const uint32_t ref = __ldg(refval + idx);
+    const uint32_t ref = cr >> 8;
     const uint32_t k = idx / 4;
     int x = 64 * (int)(k % bpr), y = 4 * (int)(k / bpr);
     if(lane >= 16) { x -= 64; y += 2; }

@@ -218,7 +218,8 @@ __global__ void __launch_bounds__(256) k_colenc(const half4 *__restrict__ in, in
   {
     float o[3];
 #pragma unroll
-    for(int i = 0; i < 3; i++) o[i] = c.M[3 * i] * rgb[0] + c.M[3 * i + 1] * rgb[1] + c.M[3 * i + 2] * rgb[2];
+    for(int i = 0; i < 3; i++)   // the shader's order, each product rounded: tiny results cancel
+      o[i] = __fadd_rn(__fadd_rn(__fmul_rn(c.M[3 * i], rgb[0]), __fmul_rn(c.M[3 * i + 1], rgb[1])), __fmul_rn(c.M[3 * i + 2], rgb[2]));
 #pragma unroll
     for(int i = 0; i < 3; i++) rgb[i] = o[i];
   }

@@ -228,73 +228,109 @@ DEV void cov_z(const dev_nodes_t &p, int x, int y, float c[4])
   ld_half4(p.cov + (size_t)y * p.hw + x, c[0], c[1], c[2], c[3]);
 }
 
+// tiles of the x-trans splat and fix kernels: multiples of the 6x6 CFA period
+// and of the 3x3 blocks of the covariance; the mosaic (and the splat output)
+// the taps read is staged once per tile with the halo the taps reach
+constexpr int XT_TX = 48, XT_TY = 24;
+
 // demosaic/splat.comp:142-266 (x-trans): 5x5 anisotropic gaussian splat of
 // the greens (only the green sums form the output), taps wrapped by the CFA
 // period 6 at the borders, centre weight 666
 __global__ void __launch_bounds__(256) k_nd_splat_xt(const dev_nodes_t p)
 {
-  const int x = blockIdx.x * 32 + threadIdx.x % 32, y = blockIdx.y * 8 + threadIdx.x / 32;
-  if(x >= p.W || y >= p.H) return;
-  float cov[4];
-  cov_z(p, x / 3, y / 3, cov);
-  const float e0 = gclamp(cov[0], 0.01f, 25.0f), e1 = gclamp(cov[1], 0.01f, 25.0f);
-  const float ie0 = 1.0f / e0, ie1 = 1.0f / e1;
-  float gs = 0.0f, gw = 0.0f;
+  __shared__ float sh[XT_TY + 4][XT_TX + 4 + 1];     // hilite output at the wrapped tap positions, halo 2
+  __shared__ uint8_t sgreen[XT_TY + 4][XT_TX + 4];   // the CFA colour of the tap position is green
+  const int X0 = blockIdx.x * XT_TX, Y0 = blockIdx.y * XT_TY;
+  for(int i = threadIdx.x; i < (XT_TY + 4) * (XT_TX + 4); i += blockDim.x)
+  {
+    const int sy = i / (XT_TX + 4), sx = i % (XT_TX + 4);
+    const int gx = X0 - 2 + sx, gy = Y0 - 2 + sy;
+    int px = gx, py = gy;   // taps past the border wrap by the CFA period 6
+    if(px < 0) px += 6;
+    if(py < 0) py += 6;
+    if(px >= p.W) px -= 6;
+    if(py >= p.H) py -= 6;
+    sh[sy][sx] = dn_z(p, p.hl, px, py);
+    sgreen[sy][sx] = cfa_xtrans(gx + 6, gy + 6) == 1;
+  }
+  __syncthreads();
+  for(int t = threadIdx.x; t < XT_TX * XT_TY; t += blockDim.x)
+  {
+    const int lx = t % XT_TX, ly = t / XT_TX, x = X0 + lx, y = Y0 + ly;
+    if(x >= p.W || y >= p.H) continue;
+    float cov[4];
+    cov_z(p, x / 3, y / 3, cov);
+    const float e0 = gclamp(cov[0], 0.01f, 25.0f), e1 = gclamp(cov[1], 0.01f, 25.0f);
+    const float ie0 = 1.0f / e0, ie1 = 1.0f / e1;
+    float gs = 0.0f, gw = 0.0f;
 #pragma unroll
-  for(int j = -2; j <= 2; j++)
+    for(int j = -2; j <= 2; j++)
 #pragma unroll
-    for(int i = -2; i <= 2; i++)
-    {
-      if(cfa_xtrans(x + i + 6, y + j + 6) != 1) continue;
-      int px = x + i, py = y + j;
-      if(px < 0) px += 6;
-      if(py < 0) py += 6;
-      if(px >= p.W) px -= 6;
-      if(py >= p.H) py -= 6;
-      const float col = dn_z(p, p.hl, px, py);
-      const float of0 = cov[2] * (float)i + cov[3] * (float)j;
-      const float of1 = -cov[3] * (float)i + cov[2] * (float)j;
-      const float w = (i == 0 && j == 0) ? 666.0f
-                    : gclamp(curve_exp(-0.5f * (of0 * ie0 * of0 + of1 * ie1 * of1)), 1e-4f, 1.0f);
-      gs += col * w;
-      gw += w;
-    }
-  p.g[(size_t)y * p.W + x] = f2h(gs / fmaxf(1e-8f, gw));
+      for(int i = -2; i <= 2; i++)
+      {
+        if(!sgreen[ly + 2 + j][lx + 2 + i]) continue;
+        const float col = sh[ly + 2 + j][lx + 2 + i];
+        const float of0 = cov[2] * (float)i + cov[3] * (float)j;
+        const float of1 = -cov[3] * (float)i + cov[2] * (float)j;
+        const float w = (i == 0 && j == 0) ? 666.0f
+                      : gclamp(curve_exp(-0.5f * (of0 * ie0 * of0 + of1 * ie1 * of1)), 1e-4f, 1.0f);
+        gs += col * w;
+        gw += w;
+      }
+    p.g[(size_t)y * p.W + x] = f2h(gs / fmaxf(1e-8f, gw));
+  }
 }
 
-// demosaic/fix.comp:21-135 (x-trans): red and blue from ratio-to-green
-// splats of radius clamp(colour + 2, 2, 3), the pattern of write_xtrans2 on
-// the unshifted position
+// demosaic/fix.comp:55-135 (x-trans): red and blue from the taps of radius 2
+// (3 with the colour param), weighted by the covariance of the block of
+// (x+1, y+1) and scaled by the splat green ratio; the centre keeps its green
 __global__ void __launch_bounds__(256) k_nd_fix_xt(const dev_nodes_t p)
 {
-  const int x = blockIdx.x * 32 + threadIdx.x % 32, y = blockIdx.y * 8 + threadIdx.x / 32;
-  if(x >= p.W || y >= p.H) return;
-  const float gc = dn_m(p, p.g, x, y);
-  float cov[4];
-  cov_z(p, (x + 1) / 3, (y + 1) / 3, cov);
-  cov[0] = gclamp(cov[0], 1.0f, 10.0f); cov[1] = gclamp(cov[1], 1.0f, 10.0f);
+  __shared__ float shl[XT_TY + 6][XT_TX + 6 + 1], sgh[XT_TY + 6][XT_TX + 6 + 1];   // mirrored, halo 3
+  __shared__ uint8_t scls[XT_TY + 6][XT_TX + 6];   // 0 red, 1 green, 2 blue of the tap position
+  const int X0 = blockIdx.x * XT_TX, Y0 = blockIdx.y * XT_TY;
+  for(int i = threadIdx.x; i < (XT_TY + 6) * (XT_TX + 6); i += blockDim.x)
+  {
+    const int sy = i / (XT_TX + 6), sx = i % (XT_TX + 6);
+    const int px = X0 - 3 + sx, py = Y0 - 3 + sy;
+    // slots past the image's last pixel + 3 are read by no pixel: clamped there (in mirror range)
+    const int mx = min(px, p.W + 2), my = min(py, p.H + 2);
+    shl[sy][sx] = dn_m(p, p.hl, mx, my);
+    sgh[sy][sx] = dn_m(p, p.g, mx, my);
+    // the shader's pattern test at the unwrapped position (truncating divisions)
+    const bool blue_top = ((px / 3 + py / 3) & 1) > 0;
+    const int qx = px - (px / 3) * 3, qy = py - (py / 3) * 3;
+    scls[sy][sx] = ((qx + qy) & 1) == 0 ? 1 : ((blue_top ^ (qy == 1)) ? 2 : 0);
+  }
+  __syncthreads();
   const int r = min(max(p.fixup + 2, 2), 3);
-  const float ie0 = 1.0f / (3.0f * cov[0]), ie1 = 1.0f / (3.0f * cov[1]);
-  const float gc4 = 1e-4f + gc;
-  float rr = 0.0f, rb = 0.0f, wr = 0.0f, wb = 0.0f;
-  for(int j = -r; j <= r; j++)
-    for(int i = -r; i <= r; i++)
-    {
-      const int px = x + i, py = y + j;
-      const bool blue_top = ((px / 3 + py / 3) & 1) > 0;
-      const int qx = px - (px / 3) * 3, qy = py - (py / 3) * 3;
-      if(((qx + qy) & 1) == 0) continue;      // green: the centre's own green is used
-      const bool blue = blue_top ^ (qy == 1);
-      const float gh = dn_m(p, p.g, px, py);
-      const float col = dn_m(p, p.hl, px, py);
-      const float of0 = cov[2] * (float)i + cov[3] * (float)j;
-      const float of1 = -cov[3] * (float)i + cov[2] * (float)j;
-      const float w = gclamp(curve_exp(-0.5f * (of0 * ie0 * of0 + of1 * ie1 * of1)), 1e-3f, 1.0f);
-      const float v = col * (gc4 / (1e-4f + gh)) * w;
-      if(blue) { rb += v; wb += w; }
-      else     { rr += v; wr += w; }
-    }
-  p.dm[(size_t)y * p.W + x] = mk_half4(rr / fmaxf(1e-8f, wr), gc, rb / fmaxf(1e-8f, wb), 1.0f);
+  for(int t = threadIdx.x; t < XT_TX * XT_TY; t += blockDim.x)
+  {
+    const int lx = t % XT_TX, ly = t / XT_TX, x = X0 + lx, y = Y0 + ly;
+    if(x >= p.W || y >= p.H) continue;
+    const float gc = sgh[ly + 3][lx + 3];
+    float cov[4];
+    cov_z(p, (x + 1) / 3, (y + 1) / 3, cov);
+    cov[0] = gclamp(cov[0], 1.0f, 10.0f); cov[1] = gclamp(cov[1], 1.0f, 10.0f);
+    const float ie0 = 1.0f / (3.0f * cov[0]), ie1 = 1.0f / (3.0f * cov[1]);
+    const float gc4 = 1e-4f + gc;
+    float rr = 0.0f, rb = 0.0f, wr = 0.0f, wb = 0.0f;
+    for(int j = -r; j <= r; j++)
+      for(int i = -r; i <= r; i++)
+      {
+        const int c = scls[ly + 3 + j][lx + 3 + i];
+        if(c == 1) continue;      // green: the centre's own green is used
+        const float gh = sgh[ly + 3 + j][lx + 3 + i];
+        const float col = shl[ly + 3 + j][lx + 3 + i];
+        const float of0 = cov[2] * (float)i + cov[3] * (float)j;
+        const float of1 = -cov[3] * (float)i + cov[2] * (float)j;
+        const float w = gclamp(curve_exp(-0.5f * (of0 * ie0 * of0 + of1 * ie1 * of1)), 1e-3f, 1.0f);
+        const float v = col * (gc4 / (1e-4f + gh)) * w;
+        if(c == 2) { rb += v; wb += w; }
+        else       { rr += v; wr += w; }
+      }
+    p.dm[(size_t)y * p.W + x] = mk_half4(rr / fmaxf(1e-8f, wr), gc, rb / fmaxf(1e-8f, wb), 1.0f);
+  }
 }
 
 // demosaic/halfsize.comp:155-187: one rgb texel per CFA block
@@ -480,8 +516,8 @@ cudaError_t launch_nodes(const dev_nodes_t &p, int stage, cudaStream_t s)
     case 1: if(xt) k_nd_hl_half<true><<<gh, 256, 0, s>>>(p); else k_nd_hl_half<false><<<gh, 256, 0, s>>>(p); break;
     case 2: if(xt) k_nd_hl_doub<true><<<gh, 256, 0, s>>>(p); else k_nd_hl_doub<false><<<gh, 256, 0, s>>>(p); break;
     case 3: k_nd_gauss_xt<<<gh, 256, 0, s>>>(p); break;
-    case 4: k_nd_splat_xt<<<gf, 256, 0, s>>>(p); break;
-    case 5: k_nd_fix_xt<<<gf, 256, 0, s>>>(p); break;
+    case 4: k_nd_splat_xt<<<dim3((p.W + XT_TX - 1) / XT_TX, (p.H + XT_TY - 1) / XT_TY), 256, 0, s>>>(p); break;
+    case 5: k_nd_fix_xt<<<dim3((p.W + XT_TX - 1) / XT_TX, (p.H + XT_TY - 1) / XT_TY), 256, 0, s>>>(p); break;
     case 6: if(xt) k_nd_halfsize<true><<<gh, 256, 0, s>>>(p); else k_nd_halfsize<false><<<gh, 256, 0, s>>>(p); break;
     case 7: k_nd_resample<<<dim3((p.ow + 15) / 16, (p.oh + 15) / 16), 256, 0, s>>>(p); break;
     case 8: k_nd_hl_bayer<<<gh, 256, 0, s>>>(p); break;

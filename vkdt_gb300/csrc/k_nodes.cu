@@ -230,8 +230,16 @@ DEV void cov_z(const dev_nodes_t &p, int x, int y, float c[4])
 
 // tiles of the x-trans splat and fix kernels: multiples of the 6x6 CFA period
 // and of the 3x3 blocks of the covariance; the mosaic (and the splat output)
-// the taps read is staged once per tile with the halo the taps reach
+// the taps read is staged once per tile with the halo the taps reach. A warp
+// takes the 32 pixels of one CFA phase of the tile (8 x 4 periods), so which
+// taps are green, red or blue is the same in all its lanes.
 constexpr int XT_TX = 48, XT_TY = 24;
+DEV void xt_item(int t, int &lx, int &ly)
+{ // item t of the tile: phase t / 32, period t % 32
+  const int ph = t >> 5, k = t & 31;
+  lx = 6 * (k & 7) + ph % 6;
+  ly = 6 * (k >> 3) + ph / 6;
+}
 
 // demosaic/splat.comp:142-266 (x-trans): 5x5 anisotropic gaussian splat of
 // the greens (only the green sums form the output), taps wrapped by the CFA
@@ -256,7 +264,9 @@ __global__ void __launch_bounds__(256) k_nd_splat_xt(const dev_nodes_t p)
   __syncthreads();
   for(int t = threadIdx.x; t < XT_TX * XT_TY; t += blockDim.x)
   {
-    const int lx = t % XT_TX, ly = t / XT_TX, x = X0 + lx, y = Y0 + ly;
+    int lx, ly;
+    xt_item(t, lx, ly);
+    const int x = X0 + lx, y = Y0 + ly;
     if(x >= p.W || y >= p.H) continue;
     float cov[4];
     cov_z(p, x / 3, y / 3, cov);
@@ -306,7 +316,9 @@ __global__ void __launch_bounds__(256) k_nd_fix_xt(const dev_nodes_t p)
   const int r = min(max(p.fixup + 2, 2), 3);
   for(int t = threadIdx.x; t < XT_TX * XT_TY; t += blockDim.x)
   {
-    const int lx = t % XT_TX, ly = t / XT_TX, x = X0 + lx, y = Y0 + ly;
+    int lx, ly;
+    xt_item(t, lx, ly);
+    const int x = X0 + lx, y = Y0 + ly;
     if(x >= p.W || y >= p.H) continue;
     const float gc = sgh[ly + 3][lx + 3];
     float cov[4];

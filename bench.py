@@ -41,6 +41,25 @@ FILTERS = 0x94949494  # bayer rggb; 9: x-trans
 DEMOSAIC_NAMES = {0: "gaussian splats (method 0)", 1: "rcd (method 1)", 2: "half size (method 2)"}
 
 
+def over_ranks(x, op="max"):
+    """x reduced over the ranks of the job (a no-op without torch.distributed): the slowest
+    rank's time ("max") or the sum of the ranks' work ("sum"). The tensor lives where the
+    backend wants it (nccl: the rank's GPU, gloo: the host)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def replica_rate(units, seconds):
+    """whole-job throughput of independent replicas: every rank's units over the slowest rank's time"""
+    return over_ranks(units, "sum") / over_ranks(seconds, "max")
+
+
 def img_param(v, wd, ht):
     rng = WHITE - BLACK
     return v.default_img_param(black=BLACK, white=WHITE, wd=wd, ht=ht, filters=FILTERS,
@@ -525,10 +544,7 @@ def run_workload(args):
     fn = {"batch": workload_batch, "serve": workload_serve, "video": workload_video,
           "ingest": workload_ingest}[args.workload]
     cfg, value, ms, extra = fn(args, v, torch, sp, clk)
-    if world > 1:
-        t = torch.tensor([value], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)   # replicas: whole-job MP/s
-        value = float(t.item())
+    value = over_ranks(value, "sum")   # replicas: whole-job MP/s
     if rank == 0:
         cfg.update({"llap_levels": LEVELS, "graph": "denoise(noop)->hilite->demosaic->colour->filmcurv->llap",
                     "l2": "inputs of 12 MP and more per image (> 129 MB L2 in flight)"})
@@ -626,13 +642,10 @@ def main():
             step(i)
         ev1.record(stream)
         barrier()
-    ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms_rank = ev0.elapsed_time(ev1)
     mp_step = WD * HT / 1e6
-    value = world * args.steps * mp_step / (ms / 1e3)
+    value = replica_rate(args.steps * mp_step, ms_rank / 1e3)   # every rank's megapixels over the slowest rank
+    ms = over_ranks(ms_rank, "max")
 
     # ---- per kernel durations (events around every launch, one sync per step)
     gt = v.Graph()
@@ -734,11 +747,7 @@ def main():
     e1.record(stream)
     barrier()
     lat = np.array(lat)
-    e2e_ms = float(lat.mean())
-    if world > 1:
-        t = torch.tensor([e2e_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = over_ranks(float(lat.mean()), "max")
     # pipelined: a ring of graphs on their own streams, each holding its image in its pinned source
     # (where a decoder writes it); every step uploads its mosaic, develops and reads the result back,
     # while the next step's copies overlap this one's kernels
@@ -760,12 +769,9 @@ def main():
         g.run(flags=v.RUN_UPLOAD_SOURCE | v.RUN_DOWNLOAD_SINK, stream=streams[k % len(ring)].cuda_stream)
     for g in ring:
         g.wait()
-    pipe_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([pipe_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        pipe_s = float(t.item())
-    e2e = {"value": world * np_ * mp_step / pipe_s, "unit": "MP/s", "h2d_bytes_per_step": WD * HT * 2,
+    pipe_rank = time.perf_counter() - t0
+    pipe_value = replica_rate(np_ * mp_step, pipe_rank)
+    e2e = {"value": pipe_value, "unit": "MP/s", "h2d_bytes_per_step": WD * HT * 2,
            "d2h_bytes_per_step": WD * HT * 8, "steps": np_, "graphs_in_flight": len(ring),
            "one_at_a_time": {"value": world * mp_step / (e2e_ms / 1e3), "unit": "MP/s"},
            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))}}

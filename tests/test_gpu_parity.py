@@ -188,6 +188,29 @@ def test_rcd(gpu, wd, ht, strength):
     check_rgb(g["llap"], r["llap"], flip=flip, mean=mean, de_stage=True)
 
 
+@pytest.mark.parametrize("case", ["xtrans", "crop"])
+def test_rcd_variants(gpu, case):
+    # rcd on an x-trans mosaic (the reference module runs it whatever the pattern) and on a
+    # cropped bayer window: the rcd kernels bit for bit on the path's own hilite output, the
+    # path end to end within the tolerances
+    filters = 9 if case == "xtrans" else 0x94949494
+    wd, ht = (606, 402) if case == "xtrans" else (1000, 742)
+    m = v.scene_host(v.make_scene(wd, ht, seed=wd + 11, filters=filters))
+    ip = v.default_img_param(wd=wd, ht=ht, filters=filters, noise_a=NA, noise_b=NB)
+    if case == "crop":
+        ip.crop_aabb[0], ip.crop_aabb[1], ip.crop_aabb[2], ip.crop_aabb[3] = 8, 6, 992, 738
+    op = oracle.default_params()
+    op.dm_method = 1
+    g = _run_graph(m, ip, setup=lambda g: g.set_param("demosaic", "method", 1))
+    r = oracle.develop(m, oracle.img_param(ip), params=op, stages=("hilite", "demosaic", "filmcurv", "llap"))
+    want = oracle.rcd(g["hilite"], [ip.whitebalance[k] for k in range(3)])
+    assert np.array_equal(g["demosaic"], want), summary(g["demosaic"], want)
+    s_h = summary(g["hilite"][..., None], r["hilite"][..., None])
+    assert s_h["flipped_frac"] <= 1e-3 and s_h["mean"] <= 1e-4, s_h
+    check_rgb(g["demosaic"], r["demosaic"])
+    check_rgb(g["llap"], r["llap"], de_stage=True)
+
+
 def test_halfsize_method(gpu):
     # demosaic method 2: the half size demosaic at the module's half output size
     wd, ht = 1000, 742

@@ -385,6 +385,63 @@ def workload_serve(args, v, torch, sp, clk):
             "latency_ms": {"p50": res["served"]["p50_ms"], "p99": res["served"]["p99_ms"]}}
 
 
+def _video_host_e2e(v, torch, W, H, ip, method, packed, frames=96):
+    """Four video streams from host memory to host memory: each frame crosses to the device as u16
+    samples (uploaded from the graph's pinned source) or as the packed 12-bit magic lantern frame
+    (copied from pinned memory, unpacked on the device into the graph's source), is developed and
+    read back as rgba f16. One graph and stream per video stream, frames pipelined across streams.
+    The samples are random 12-bit values (the same distribution both ways)."""
+    R = 4
+    g = torch.Generator(device="cpu")
+    g.manual_seed(3)
+    nb = W * H * 12 // 8
+    graphs, streams, hp, dp = [], [], [], []
+    for k in range(R):
+        gr = v.Graph()
+        gr.set_input(W, H, ip)
+        if LEVELS:
+            gr.set_llap_levels(LEVELS)
+        if method:
+            gr.set_param("demosaic", "method", np.int32(method))
+        gr.alloc()
+        graphs.append(gr)
+        streams.append(torch.cuda.Stream())
+        if packed:
+            hp.append(torch.randint(0, 256, (nb,), dtype=torch.uint8, generator=g).pin_memory())
+            dp.append(torch.empty(nb, dtype=torch.uint8, device="cuda"))
+        else:
+            gr.source()[...] = torch.randint(0, 4096, (H, W), dtype=torch.int16, generator=g).numpy()
+
+    def frame(k):
+        gr, st = graphs[k % R], streams[k % R]
+        if packed:
+            src, _ = gr.device_buffers()
+            with torch.cuda.stream(st):
+                dp[k % R].copy_(hp[k % R], non_blocking=True)
+            v.unpack_mlv(dp[k % R].data_ptr(), nb, 12, W, H, src, st.cuda_stream)
+            gr.run(flags=v.RUN_DOWNLOAD_SINK, stream=st.cuda_stream)
+        else:
+            gr.run(flags=v.RUN_UPLOAD_SOURCE | v.RUN_DOWNLOAD_SINK, stream=st.cuda_stream)
+    for k in range(2 * R):
+        if k >= R:
+            graphs[k % R].wait()
+        frame(k)
+    for gr in graphs:
+        gr.wait()
+    t0 = time.perf_counter()
+    for k in range(frames):
+        if k >= R:
+            graphs[k % R].wait()
+        frame(k)
+    for gr in graphs:
+        gr.wait()
+    wall = time.perf_counter() - t0
+    for gr in graphs:
+        gr.close()
+    return {"value": frames * W * H / 1e6 / wall, "unit": "MP/s", "frames": frames,
+            "h2d_bytes_per_frame": nb if packed else 2 * W * H, "d2h_bytes_per_frame": 8 * W * H}
+
+
 def workload_video(args, v, torch, sp, clk):
     """4 raw video streams 4096x2160 RGGB 12-bit, 120 panned frames each, and x-trans 6240x4160 stills at 5/s."""
     VW, VH, XW, XH = 4096, 2160, 6240, 4160
@@ -453,11 +510,15 @@ def workload_video(args, v, torch, sp, clk):
     s.close()
     if sx is not s:
         sx.close()
+    del frames, stills, vout, xout
+    torch.cuda.synchronize()
+    host = {"u16": _video_host_e2e(v, torch, VW, VH, vip, vmethod, packed=False),
+            "mlv_12bit": _video_host_e2e(v, torch, VW, VH, vip, vmethod, packed=True)}
     return {"workload": "4 raw video streams 4096x2160 RGGB 12-bit (black 256, white 4095, a=4, b=0.8, panned 3 px/frame, "
                         "120 frames each) and 25 x-trans 6240x4160 14-bit stills at 5/s",
             "demosaic": "video: %s, stills: %s" % (DEMOSAIC_NAMES[vmethod], DEMOSAIC_NAMES[0]),
             "modes": "back-to-back (each stream's next frame after its last) and paced at 24 fps"}, \
-        b2b["value"], b2b["wall_s"] * 1e3, {"back_to_back": b2b, "paced_24fps": paced,
+        b2b["value"], b2b["wall_s"] * 1e3, {"back_to_back": b2b, "paced_24fps": paced, "e2e_from_host": host,
                                              "latency_ms": {"p99_frame": b2b["frame_latency_ms"]["p99"]}}
 
 

@@ -764,9 +764,15 @@ def main():
     achieved = alg / (dev_ms / 1e3) / 1e9 if alg else None
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
+    issue = None
     if os.path.exists(tp) and fused:
         try:
-            traffic = json.load(open(tp)).get("k_develop_bytes_per_launch")
+            tj = json.load(open(tp))
+            traffic = tj.get("k_develop_bytes_per_launch")
+            # the kernel is bound by instruction issue, not by HBM: the ncu capture's issue
+            # utilisation and instructions per pixel are reported beside the HBM fraction
+            issue = {"issue_active": tj.get("k_develop_issue_active"),
+                     "thread_inst_per_px": tj.get("k_develop_thread_inst_per_px"), "source": "ncu capture, profiles/"}
         except Exception:
             traffic = None
     kname = {"demosaic:fix": "k_develop (hilite doub + demosaic + colour + filmcurv + llap curve/reduce)" if fused
@@ -777,7 +783,7 @@ def main():
              "llap:colour": "k_llap_final (llap assemble level 0 + colour)"}.get(names[dev_idx], names[dev_idx])
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak if achieved else None,
-                "traffic": traffic, "kernel": kname,
+                "traffic": traffic, "kernel": kname, "compute": issue,
                 "kernel_ms": dev_ms, "alg_bytes_per_launch": alg,
                 "peak_source": "measured" if peaks else "fallback",
                 "per_launch_ms": [[n, round(float(x), 5)] for n, x in zip(names, kms)],

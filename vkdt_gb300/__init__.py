@@ -213,6 +213,8 @@ class Graph:
 
     def set_input(self, wd, ht, img_param):
         self.wd, self.ht = wd, ht
+        b = img_param.crop_aabb   # the denoise output: the crop window
+        self.crop_wd, self.crop_ht = int(b[2] - b[0]), int(b[3] - b[1])
         check(self._l.vkdt_cuda_graph_set_input(self._g, wd, ht, C.byref(img_param)), "set_input")
 
     def set_llap_levels(self, n):
@@ -312,7 +314,7 @@ class Graph:
         if stage in (2, 3):
             out = np.empty((self.out_ht, self.out_wd, 4), np.float32)
         else:
-            out = np.empty((self.ht, self.wd, 1), np.float32)
+            out = np.empty((self.crop_ht, self.crop_wd, 1), np.float32)
         check(self._l.vkdt_cuda_graph_debug_stage(self._g, stage, out.ctypes.data_as(C.POINTER(C.c_float)), out.size),
               "debug_stage")
         return out if stage in (2, 3) else out[..., 0]

@@ -205,14 +205,21 @@ __global__ void __launch_bounds__(256) k_dn_down(const dev_denoise_t p, const ha
     g1[k] = c[k] < 0.0f ? c[k] : fpow(c[k], 0.8f);
     sum[k] = t * c[k]; wgt[k] = t;
   }
-  // offsets of the taps (0.5 + o): (1.7, 0.9), (-0.7, 0.1), (0.9, -0.7), (0.1, 1.7)
+  // offsets of the taps (0.5 + o): (1.7, 0.9), (-0.7, 0.1), (0.9, -0.7), (0.1, 1.7). Below
+  // 8192 texels the sampler's position of every tap (rounded to 1/256) is the texel x + dx
+  // plus the fraction ax whatever x is (checked for every x): the taps read those directly.
   const float ox[4] = { 0.5f + 1.2f, 0.5f - 1.2f, 0.5f + 0.4f, 0.5f - 0.4f };
   const float oy[4] = { 0.5f + 0.4f, 0.5f - 0.4f, 0.5f - 1.2f, 0.5f + 1.2f };
+  const int tdx[4] = { 1, -2, 0, -1 }, tdy[4] = { 0, -1, -2, 1 };
+  const float tax[4] = { 51.0f / 256.0f, 205.0f / 256.0f, 102.0f / 256.0f, 154.0f / 256.0f };
+  const float tay[4] = { 102.0f / 256.0f, 154.0f / 256.0f, 205.0f / 256.0f, 51.0f / 256.0f };
+  const bool fixed = p.hw < 8192 && p.hh < 8192;
 #pragma unroll
   for(int o = 0; o < 4; o++)
   {
     float col[4];
-    bilinear(in, p.hw, p.hh, __fadd_rn((float)x, ox[o]), __fadd_rn((float)y, oy[o]), col);
+    if(fixed) bilinear_at(in, p.hw, p.hh, x + tdx[o], y + tdy[o], tax[o], tay[o], col);
+    else bilinear(in, p.hw, p.hh, __fadd_rn((float)x, ox[o]), __fadd_rn((float)y, oy[o]), col);
 #pragma unroll
     for(int k = 0; k < 3; k++)
     {

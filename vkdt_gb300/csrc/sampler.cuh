@@ -10,6 +10,17 @@ DEV void ld4(const half4 *img, int w, int x, int y, float v[4]) { ld_half4(img +
 // position of a texture() read in texel space, rounded to the sampler's 8 sub-texel bits
 DEV float subtexel(float v) { return __fmul_rn(floorf(__fadd_rn(__fmul_rn(v, 256.0f), 0.5f)), 0.00390625f); }
 
+// the blend of texture() once its position is resolved: texel (x0, y0) and fractions (ax, ay)
+DEV void bilinear_at(const half4 *img, int w, int h, int x0, int y0, float ax, float ay, float out[4])
+{
+  const int X0 = mirror(x0, w), X1 = mirror(x0 + 1, w), Y0 = mirror(y0, h), Y1 = mirror(y0 + 1, h);
+  float t00[4], t10[4], t01[4], t11[4];
+  ld4(img, w, X0, Y0, t00); ld4(img, w, X1, Y0, t10); ld4(img, w, X0, Y1, t01); ld4(img, w, X1, Y1, t11);
+#pragma unroll
+  for(int k = 0; k < 4; k++)
+    out[k] = (t00[k] * (1.0f - ax) + t10[k] * ax) * (1.0f - ay) + (t01[k] * (1.0f - ax) + t11[k] * ax) * ay;
+}
+
 // texture() with LINEAR + MIRRORED_REPEAT at texel-space position (x, y)
 DEV void bilinear(const half4 *img, int w, int h, float x, float y, float out[4])
 {

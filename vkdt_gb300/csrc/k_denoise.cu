@@ -89,15 +89,13 @@ __global__ void __launch_bounds__(256) k_dn_half(const dev_denoise_t p)
 // the smaller determinant decomposed, then an anisotropic gaussian over the
 // 5x5 window that skips hot pixels. One 16x16 tile per CTA, the 20x20 input
 // window (mirrored) in shared memory.
-// The window's texels are kept as two float4 per slot, (l, 1/l, l^2, 1/l^2)
-// and (r, g, b, -), so each tap is one 16 byte load; the row pitch puts the
-// two rows a warp reads (16 lanes each) on disjoint banks.
-constexpr int DC_T = 16, DC_N = DC_T + 4, DC_P = 24;
+constexpr int DC_T = 16, DC_N = DC_T + 4;
 
 __global__ void __launch_bounds__(256) k_dn_downcov(const dev_denoise_t p)
 {
-  // per texel of the window: luminance and the luminance terms of the two tensor forms; r, g, b
-  __shared__ float4 sL[DC_N][DC_P], sC[DC_N][DC_P];
+  // per texel of the window: r, g, b, luminance and the luminance terms of the two tensor forms
+  __shared__ float sr[DC_N][DC_N + 1], sg[DC_N][DC_N + 1], sbl[DC_N][DC_N + 1];
+  __shared__ float sl[DC_N][DC_N + 1], sil[DC_N][DC_N + 1], sl2[DC_N][DC_N + 1], sil2[DC_N][DC_N + 1];
   const int X0 = blockIdx.x * DC_T, Y0 = blockIdx.y * DC_T;
   for(int i = threadIdx.x; i < DC_N * DC_N; i += 256)
   {
@@ -108,9 +106,9 @@ __global__ void __launch_bounds__(256) k_dn_downcov(const dev_denoise_t p)
     const int y = min(max(mirror(Y0 - 2 + ty, p.hh), 0), p.hh - 1);
     float v[4];
     ld4(p.half_img, p.hw, x, y, v);
-    sC[ty][tx] = make_float4(v[0], v[1], v[2], 0.0f);
+    sr[ty][tx] = v[0]; sg[ty][tx] = v[1]; sbl[ty][tx] = v[2];
     const float l = lum2020(v[0], v[1], v[2]);
-    sL[ty][tx] = make_float4(l, 1.0f / l, l * l, 1.0f / (l * l));
+    sl[ty][tx] = l; sil[ty][tx] = 1.0f / l; sl2[ty][tx] = l * l; sil2[ty][tx] = 1.0f / (l * l);
   }
   __syncthreads();
   const int lx = threadIdx.x % DC_T, ly = threadIdx.x / DC_T;
@@ -118,13 +116,12 @@ __global__ void __launch_bounds__(256) k_dn_downcov(const dev_denoise_t p)
   if(x >= p.hw || y >= p.hh) return;
   // first moments of the luminance (Sw) and of its inverse (Sb)
   float mw0 = 0.0f, mw1 = 0.0f, mb0 = 0.0f, mb1 = 0.0f, smw = 0.0f, smb = 0.0f;
-#pragma unroll 1
+#pragma unroll
   for(int j = -2; j <= 2; j++)
 #pragma unroll
     for(int i = -2; i <= 2; i++)
     {
-      const float4 L = sL[ly + 2 + j][lx + 2 + i];
-      const float px = L.x, ipx = L.y;
+      const float px = sl[ly + 2 + j][lx + 2 + i], ipx = sil[ly + 2 + j][lx + 2 + i];
       mw0 += (float)i * px; mw1 += (float)j * px; smw += px;
       mb0 += (float)i * ipx; mb1 += (float)j * ipx; smb += ipx;
     }
@@ -133,14 +130,13 @@ __global__ void __launch_bounds__(256) k_dn_downcov(const dev_denoise_t p)
   // second moments
   float mean_b = 0.0f;
   float Sw00 = 0.0f, Sw01 = 0.0f, Sw11 = 0.0f, Sb00 = 0.0f, Sb01 = 0.0f, Sb11 = 0.0f, sw = 0.0f, sb = 0.0f;
-#pragma unroll 1
+#pragma unroll
   for(int j = -2; j <= 2; j++)
 #pragma unroll
     for(int i = -2; i <= 2; i++)
     {
-      const float4 L = sL[ly + 2 + j][lx + 2 + i];
-      mean_b += L.x;
-      const float p2 = L.z, b2 = L.w;
+      mean_b += sl[ly + 2 + j][lx + 2 + i];
+      const float p2 = sl2[ly + 2 + j][lx + 2 + i], b2 = sil2[ly + 2 + j][lx + 2 + i];
       const float q0 = (float)i - mw0, q1 = (float)j - mw1;
       Sw00 += p2 * q0 * q0; Sw01 += p2 * q0 * q1; Sw11 += p2 * q1 * q1; sw += p2;
       const float r0 = (float)i - mb0, r1 = (float)j - mb1;
@@ -165,13 +161,12 @@ __global__ void __launch_bounds__(256) k_dn_downcov(const dev_denoise_t p)
 #pragma unroll
     for(int i = -2; i <= 2; i++)
     {
-      const float4 C = sC[ly + 2 + j][lx + 2 + i];
-      const float pr = C.x;
+      const float pr = sr[ly + 2 + j][lx + 2 + i];
       if(pr > hot) continue;
       const float x0 = (float)i * e0[0] + (float)j * e0[1];
       const float x1 = (float)i * e1[0] + (float)j * e1[1];
       const float ww = fmaxf(1e-9f, __expf(-0.5f * (x0 * ie0 * x0 + x1 * ie1 * x1)));
-      r0 += ww * pr; r1 += ww * C.y; r2 += ww * C.z;
+      r0 += ww * pr; r1 += ww * sg[ly + 2 + j][lx + 2 + i]; r2 += ww * sbl[ly + 2 + j][lx + 2 + i];
       wt += ww;
     }
   const float d = 1.0f / fmaxf(wt, 1e-8f);

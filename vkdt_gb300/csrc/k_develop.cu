@@ -124,6 +124,50 @@ template<int PX, int PY> DEV void fix_taps(const smem_t &s, int px, int py, int 
   }
 }
 
+// Interior tiles (the tile and its 4 pixel halo inside the image, no mirrored
+// or wrapped position anywhere): the tile origin is even, so a slot's parity
+// is its pixel's CFA phase, and every tap is a fixed offset from the slot in
+// the split arrays. The same taps, weights and sums in the same order as
+// splat_taps / fix_taps, with the slot addresses resolved at compile time.
+//
+// splat slot (2 bx + PX, 2 by + PY): pixel X0 - 2 + sgx, M slot x = sgx + 2 + ii
+template<int PX, int PY> DEV void splat_taps_in(const smem_t &s, int bx, int sgy,
+    float wh, float wv, float wd, float &rg, float &wg)
+{
+#pragma unroll
+  for(int j = -1; j <= 1; j++)
+#pragma unroll
+  for(int ii = -1; ii <= 1; ii++)
+  {
+    if(cfa_bayer(PX + ii, PY + j) != 1) continue;
+    const float col = s.M[sgy + 2 + j][(PX + ii) & 1][bx + ((PX + 2 + ii) >> 1)];
+    const float weight = (ii == 0 && j == 0) ? 666.0f : tap_weight(wh, wv, wd, ii, j);
+    rg += col * weight;
+    wg += weight;
+  }
+}
+
+// fix slot (2 bx + 1 - PX, sly) of a pixel with CFA phase (PX, PY): pixel
+// X0 - 1 + slx, splat slot x = slx + 1 + ii, M slot x = slx + 3 + ii
+template<int PX, int PY> DEV void fix_taps_in(const smem_t &s, int bx, int sly,
+    float gc, float wh, float wv, float wd, float &rr, float &rb, float &wr, float &wb, float &rg, float &wg)
+{
+#pragma unroll
+  for(int j = -1; j <= 1; j++)
+#pragma unroll
+  for(int ii = -1; ii <= 1; ii++)
+  {
+    const int c = cfa_bayer(PX + ii, PY + j);
+    if(c == 1) { rg = gc; wg = 1.0f; continue; }
+    const float rgh = s.rg[sly + 1 + j][(2 - PX + ii) & 1][bx + ((2 - PX + ii) >> 1)];
+    const float col = s.M[sly + 3 + j][(PX + ii) & 1][bx + ((4 - PX + ii) >> 1)];
+    const float weight = tap_weight(wh, wv, wd, ii, j);
+    const float v = col * (1e-4f + gc) * rgh * weight;
+    if(c == 0) { rr += v; wr += weight; }
+    else       { rb += v; wb += weight; }
+  }
+}
+
 // demosaic/gauss.comp:24-75 (bayer) for one entry, px the 8 greens around it
 // in the shader's loop order: the covariance sums in the shader's order
 // without contraction. They decide the form and the snapped direction, and
@@ -204,6 +248,8 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
   const int X0 = W >= TX ? min(OX, W - TX) : 0;
   const int Y0 = H >= TY ? min(OY, H - TY) : 0;
   const int OXe = min(OX + TX, W), OYe = min(OY + TY, H);
+  // no position of the tile's stages is mirrored or wrapped (even origin, 4 pixel margin)
+  const bool interior = !((X0 | Y0) & 1) && X0 >= 4 && Y0 >= 4 && X0 + TX + 4 <= W && Y0 + TY + 4 <= H;
   if(p.hist) for(int i = tid; i < 257; i += NT) s.hist[i] = 0;
 
   // ---- the hilite coarse level around the tile (virtual slots, mirrored)
@@ -330,18 +376,34 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
     for(int t = tid; t < 4 * NB; t += NT)
     {
       const int ph = t / NB, b = t % NB;
-      const int sgx = 2 * (b % GH) + (ph & 1), sgy = 2 * (b / GH) + (ph >> 1);
+      const int bx = b % GH, by = b / GH;
+      const int sgx = 2 * bx + (ph & 1), sgy = 2 * by + (ph >> 1);
       if(sgx >= GX || sgy >= GX) continue;
-      const int qx = mirror1(X0 - 2 + sgx, W), qy = mirror1(Y0 - 2 + sgy, H);
-      const int ccx = (qx + 1) / 2 - (X0 / 2 - 1), ccy = (qy + 1) / 2 - (Y0 / 2 - 1);
-      const float wh = s.u.e.sw[0][ccy][ccx], wv = s.u.e.sw[1][ccy][ccx], wd = s.u.e.sw[2][ccy][ccx];
       float rg = 0.0f, wg = 0.0f;
-      switch((qx & 1) | ((qy & 1) << 1))
-      { // the CFA phase of the real pixel: uniform in a warp but at mirrored borders
-        case 0: splat_taps<0, 0>(s, qx, qy, W, H, X0, Y0, wh, wv, wd, rg, wg); break;
-        case 1: splat_taps<1, 0>(s, qx, qy, W, H, X0, Y0, wh, wv, wd, rg, wg); break;
-        case 2: splat_taps<0, 1>(s, qx, qy, W, H, X0, Y0, wh, wv, wd, rg, wg); break;
-        default: splat_taps<1, 1>(s, qx, qy, W, H, X0, Y0, wh, wv, wd, rg, wg); break;
+      if(interior)
+      { // pixel X0 - 2 + sgx: its phase is the slot's, its entry (sgx + 1) / 2
+        const int ccx = bx + (ph & 1), ccy = by + (ph >> 1);
+        const float wh = s.u.e.sw[0][ccy][ccx], wv = s.u.e.sw[1][ccy][ccx], wd = s.u.e.sw[2][ccy][ccx];
+        switch(ph)
+        {
+          case 0: splat_taps_in<0, 0>(s, bx, sgy, wh, wv, wd, rg, wg); break;
+          case 1: splat_taps_in<1, 0>(s, bx, sgy, wh, wv, wd, rg, wg); break;
+          case 2: splat_taps_in<0, 1>(s, bx, sgy, wh, wv, wd, rg, wg); break;
+          default: splat_taps_in<1, 1>(s, bx, sgy, wh, wv, wd, rg, wg); break;
+        }
+      }
+      else
+      {
+        const int qx = mirror1(X0 - 2 + sgx, W), qy = mirror1(Y0 - 2 + sgy, H);
+        const int ccx = (qx + 1) / 2 - (X0 / 2 - 1), ccy = (qy + 1) / 2 - (Y0 / 2 - 1);
+        const float wh = s.u.e.sw[0][ccy][ccx], wv = s.u.e.sw[1][ccy][ccx], wd = s.u.e.sw[2][ccy][ccx];
+        switch((qx & 1) | ((qy & 1) << 1))
+        { // the CFA phase of the real pixel: uniform in a warp but at mirrored borders
+          case 0: splat_taps<0, 0>(s, qx, qy, W, H, X0, Y0, wh, wv, wd, rg, wg); break;
+          case 1: splat_taps<1, 0>(s, qx, qy, W, H, X0, Y0, wh, wv, wd, rg, wg); break;
+          case 2: splat_taps<0, 1>(s, qx, qy, W, H, X0, Y0, wh, wv, wd, rg, wg); break;
+          default: splat_taps<1, 1>(s, qx, qy, W, H, X0, Y0, wh, wv, wd, rg, wg); break;
+        }
       }
       const float gv = f16r(rg / fmaxf(1e-8f, wg));
       s.g[sgy][sgx & 1][sgx >> 1] = f2h(gv);    // gv is an f16 value: exact
@@ -362,20 +424,39 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
       const int slx = 2 * (b % LH) + (ph & 1), sly = 2 * (b / LH) + (ph >> 1);
       if(slx >= LX || sly >= LX) continue;
       const int vx = X0 - 1 + slx, vy = Y0 - 1 + sly;
-      const int px = mirror1(vx, W), py = mirror1(vy, H);
-      const int gx0 = px - (X0 - 2), gy0 = py - (Y0 - 2);
-      const float gc = h2f(s.g[gy0][gx0 & 1][gx0 >> 1]);
-      const int ccx = (px + 1) / 2 - (X0 / 2 - 1), ccy = (py + 1) / 2 - (Y0 / 2 - 1);
-      const float wh = s.fw[0][ccy][ccx], wv = s.fw[1][ccy][ccx], wd = s.fw[2][ccy][ccx];
       float rr = 0.0f, rb = 0.0f, wr = 0.0f, wb = 0.0f, rg = 0.0f, wg = 0.0f;
+      int px, py;
       // demosaic/fix.comp:99-135, radius clamp(fixup+1, 1, 2) = 1 for the
       // default fixup 0 (the host rejects other values for this kernel)
-      switch((px & 1) | ((py & 1) << 1))
+      if(interior)
+      { // pixel X0 - 1 + slx: phase 1 - the slot's, entry slx / 2 + 1, splat slot slx + 1
+        px = vx; py = vy;
+        const int bx = b % LH, by = b / LH;
+        const int ccx = bx + 1, ccy = by + 1;
+        const float wh = s.fw[0][ccy][ccx], wv = s.fw[1][ccy][ccx], wd = s.fw[2][ccy][ccx];
+        const float gc = h2f(s.g[sly + 1][1 - (ph & 1)][bx + (ph & 1)]);
+        switch(ph)
+        {
+          case 3: fix_taps_in<0, 0>(s, bx, sly, gc, wh, wv, wd, rr, rb, wr, wb, rg, wg); break;
+          case 2: fix_taps_in<1, 0>(s, bx, sly, gc, wh, wv, wd, rr, rb, wr, wb, rg, wg); break;
+          case 1: fix_taps_in<0, 1>(s, bx, sly, gc, wh, wv, wd, rr, rb, wr, wb, rg, wg); break;
+          default: fix_taps_in<1, 1>(s, bx, sly, gc, wh, wv, wd, rr, rb, wr, wb, rg, wg); break;
+        }
+      }
+      else
       {
-        case 0: fix_taps<0, 0>(s, px, py, gx0, gy0, X0, Y0, gc, wh, wv, wd, rr, rb, wr, wb, rg, wg); break;
-        case 1: fix_taps<1, 0>(s, px, py, gx0, gy0, X0, Y0, gc, wh, wv, wd, rr, rb, wr, wb, rg, wg); break;
-        case 2: fix_taps<0, 1>(s, px, py, gx0, gy0, X0, Y0, gc, wh, wv, wd, rr, rb, wr, wb, rg, wg); break;
-        default: fix_taps<1, 1>(s, px, py, gx0, gy0, X0, Y0, gc, wh, wv, wd, rr, rb, wr, wb, rg, wg); break;
+        px = mirror1(vx, W); py = mirror1(vy, H);
+        const int gx0 = px - (X0 - 2), gy0 = py - (Y0 - 2);
+        const float gc = h2f(s.g[gy0][gx0 & 1][gx0 >> 1]);
+        const int ccx = (px + 1) / 2 - (X0 / 2 - 1), ccy = (py + 1) / 2 - (Y0 / 2 - 1);
+        const float wh = s.fw[0][ccy][ccx], wv = s.fw[1][ccy][ccx], wd = s.fw[2][ccy][ccx];
+        switch((px & 1) | ((py & 1) << 1))
+        {
+          case 0: fix_taps<0, 0>(s, px, py, gx0, gy0, X0, Y0, gc, wh, wv, wd, rr, rb, wr, wb, rg, wg); break;
+          case 1: fix_taps<1, 0>(s, px, py, gx0, gy0, X0, Y0, gc, wh, wv, wd, rr, rb, wr, wb, rg, wg); break;
+          case 2: fix_taps<0, 1>(s, px, py, gx0, gy0, X0, Y0, gc, wh, wv, wd, rr, rb, wr, wb, rg, wg); break;
+          default: fix_taps<1, 1>(s, px, py, gx0, gy0, X0, Y0, gc, wh, wv, wd, rr, rb, wr, wb, rg, wg); break;
+        }
       }
       float dm[3];
       dm[0] = f16r(rr / fmaxf(1e-8f, wr));

@@ -3,10 +3,12 @@
 // (assemble of level 0 fused with llap/colour). Pyramid levels are stored as
 // 11 f16 planes (NUM_GAMMA curves + grey) each, planar.
 //
-// The assemble kernels stage the coarse level (its 11 planes and the coarse
-// assembled image) of a 32x32 output tile in shared memory and hand each warp
-// outputs of one (x, y) parity, so all lanes of a warp share the tap pattern
-// of the gauss_expand they evaluate.
+// The assemble kernels stage the coarse level (its planes and the coarse
+// assembled image) of a 64x16 output tile in shared memory. A thread takes two
+// horizontally adjacent outputs (one of each x parity, both centred on the
+// same coarse column) and a warp one row of 32 such pairs: the lanes read 32
+// consecutive coarse slots (no bank conflicts), the rgba images move as 16
+// byte words, and all lanes of a warp evaluate the same tap pattern.
 #include "common.cuh"
 #include "hilite.cuh"
 #include "kernels.h"
@@ -16,8 +18,9 @@ namespace {
 
 constexpr int NPL = 11;
 constexpr int NG = 10;
-constexpr int FT = 32;            // output tile
-constexpr int FS = FT / 2 + 4;    // coarse slots per side: virtual [X0/2-2, X0/2+FT/2+2)
+constexpr int FTX = 64, FTY = 16;              // output tile
+constexpr int NKX = FTX / 2;                   // coarse columns the tile's outputs centre on
+constexpr int FSX = NKX + 4, FSY = FTY / 2 + 4; // coarse slots: virtual [X0/2-2, X0/2+NKX+2) x [Y0/2-2, Y0/2+FTY/2+2)
 
 DEV int mirror1(int i, int n)
 { // mirrored repeat for |overshoot| < n, clamped for slots no output reads
@@ -40,31 +43,39 @@ DEV int gamma_hi_from_v(float v)
 // (o/2 + 0.5): three bilinear taps per axis at o/2+0.5 + {-1.5, 0, 1.5}, which
 // land on texel centres or half way between two. Summed per axis the texel
 // weights are (.5 .5 1 .5 .5) around k = o/2 for even o and (1 .5 .5 1) from
-// k-1 for odd o; the expand is the separable sum of those, divided by 9.
-// PX, PY: parities of the output position. fetch(x, y) returns the texel.
-template<int PX, int PY, class F> DEV float expand(F fetch, int kx, int ky)
+// k-1 for odd o; the expand is the separable sum of those, row sums first,
+// divided by 9. PX, PY: parities of the output position.
+//
+// hrow: the row sum for x parity PX around column kx, fetch(x) the texel
+template<int PX, class F> DEV float hrow(F fetch, int kx)
 {
-  constexpr int NX = PX ? 4 : 5, NY = PY ? 4 : 5;
-  constexpr int BXO = PX ? -1 : -2, BYO = PY ? -1 : -2;
+  constexpr int NX = PX ? 4 : 5, BXO = PX ? -1 : -2;
+  float row = 0.0f;
+#pragma unroll
+  for(int a = 0; a < NX; a++)
+  {
+    const float w = PX ? ((a == 0 || a == 3) ? 1.0f : 0.5f) : (a == 2 ? 1.0f : 0.5f);
+    row += w * fetch(kx + BXO + a);
+  }
+  return row;
+}
+
+// vcol: the sum of the row sums rowsum(y) for y parity PY around row ky, / 9
+template<int PY, class R> DEV float vcol(R rowsum, int ky)
+{
+  constexpr int NY = PY ? 4 : 5, BYO = PY ? -1 : -2;
   float r = 0.0f;
 #pragma unroll
   for(int b = 0; b < NY; b++)
   {
-    float row = 0.0f;
-#pragma unroll
-    for(int a = 0; a < NX; a++)
-    {
-      const float w = PX ? ((a == 0 || a == 3) ? 1.0f : 0.5f) : (a == 2 ? 1.0f : 0.5f);
-      row += w * fetch(kx + BXO + a, ky + BYO + b);
-    }
     const float wy = PY ? ((b == 0 || b == 3) ? 1.0f : 0.5f) : (b == 2 ? 1.0f : 0.5f);
-    r += wy * row;
+    r += wy * rowsum(ky + BYO + b);
   }
   return r / 9.0f;
 }
 
 // expand of two planes at once (fetch returns both texels as a half2): the
-// same sums in the same order as expand() for each of the two
+// same sums in the same order as hrow and vcol for each of the two
 template<int PX, int PY, class F> DEV float2 expand2(F fetch, int kx, int ky)
 {
   constexpr int NX = PX ? 4 : 5, NY = PY ? 4 : 5;
@@ -149,19 +160,21 @@ __global__ void __launch_bounds__(256) k_llap_reduce(const __half *__restrict__ 
 // the coarse level around one output tile: slot (sx, sy) holds the mirrored
 // texel (bx+sx, by+sy). An output mixes the two adjacent planes around its
 // grey value, so the planes are staged in pairs (k, k+1), one 4 byte word per
-// slot (f16 values: exact), beside the coarse assembled image.
+// slot (f16 values: exact), beside the coarse assembled image. The coarse
+// image enters every output, so its row sums are made once per tile.
 struct coarse_t
 {
-  __half2 pr[NG - 1][FS][FS + 1];   // planes (k, k+1), k = 0 .. NG-2
-  float c[FS][FS + 1];              // the coarse assembled image (the grey plane on the first level)
+  __half2 pr[NG - 1][FSY][FSX];   // planes (k, k+1), k = 0 .. NG-2
+  float c[FSY][FSX];              // the coarse assembled image (the grey plane on the first level)
+  float hc[2][FSY][NKX];          // hrow of c for even / odd outputs: [x parity][slot row][column - X0/2]
 };
 
 DEV void stage_coarse(coarse_t &sc, const __half *l1, int w1, int h1, size_t p1,
     const __half *coarse, int bx, int by)
 { // the mirrored position once per slot, then the same texel of every plane
-  for(int r = threadIdx.x; r < FS * FS; r += blockDim.x)
+  for(int r = threadIdx.x; r < FSX * FSY; r += blockDim.x)
   {
-    const int sx = r % FS, sy = r / FS;
+    const int sx = r % FSX, sy = r / FSX;
     const size_t o = (size_t)mirror1(by + sy, h1) * w1 + mirror1(bx + sx, w1);
     __half h[NG];
 #pragma unroll
@@ -170,41 +183,39 @@ DEV void stage_coarse(coarse_t &sc, const __half *l1, int w1, int h1, size_t p1,
     for(int k = 0; k < NG - 1; k++) sc.pr[k][sy][sx] = __halves2half2(h[k], h[k + 1]);
     sc.c[sy][sx] = h2f(__ldg(coarse + o));
   }
+  __syncthreads();
+  // coarse column X0/2 + lx sits in slot lx + 2
+  for(int i = threadIdx.x; i < 2 * FSY * NKX; i += blockDim.x)
+  {
+    const int lx = i % NKX, sy = (i / NKX) % FSY, px = i / (NKX * FSY);
+    const float *row = sc.c[sy];
+    sc.hc[px][sy][lx] = px ? hrow<1>([&](int sx) { return row[sx]; }, lx + 2)
+                           : hrow<0>([&](int sx) { return row[sx]; }, lx + 2);
+  }
 }
 
-// output pixel of the tile for item t: warps take one (x, y) parity class
-DEV bool tile_item(int t, int X0, int Y0, int w0, int h0, int &x, int &y)
+// llap/assemble.comp:89-123 at one output of parity (PX, PY) centred on coarse
+// column slot lx + 2 and row slot sy. l0(k, g) returns the fine level plane k
+// at the output.
+template<int PX, int PY, class L0> DEV float assemble_px(L0 l0, float v, const coarse_t &sc, int lx, int sy)
 {
-  constexpr int NB = (FT / 2) * (FT / 2);
-  const int ph = t / NB, b = t % NB;
-  x = X0 + 2 * (b % (FT / 2)) + (ph & 1);
-  y = Y0 + 2 * (b / (FT / 2)) + (ph >> 1);
-  return x < w0 && y < h0;
-}
-
-// llap/assemble.comp:89-123 at one output pixel of parity (PX, PY). l0(k)
-// returns the fine level plane k at the pixel, sl holds the coarse level.
-template<int PX, int PY, class L0> DEV float assemble_px(L0 l0, float v, const coarse_t &sc, int x, int y, int bx, int by)
-{
-  const int kx = x >> 1, ky = y >> 1;
-  const float res = expand<PX, PY>([&](int ix, int iy) { return sc.c[iy - by][ix - bx]; }, kx, ky);
+  const float res = vcol<PY>([&](int iy) { return sc.hc[PX][iy][lx]; }, sy);
   const int hi = gamma_hi_from_v(v);
   const float glo = kLlapGamma[hi - 1], ghi = kLlapGamma[hi];
   const float a = gclamp((v - glo) / (ghi - glo), 0.0f, 1.0f);
-  const __half2 (*pr)[FS + 1] = sc.pr[hi - 1];
-  const float2 e = expand2<PX, PY>([&](int ix, int iy) { return pr[iy - by][ix - bx]; }, kx, ky);
+  const __half2 (*pr)[FSX] = sc.pr[hi - 1];
+  const float2 e = expand2<PX, PY>([&](int ix, int iy) { return pr[iy][ix]; }, lx + 2, sy);
   const float la = l0(hi - 1, glo) - e.x;
   const float lb = l0(hi, ghi) - e.y;
   return res + la * (1.0f - a) + lb * a;
 }
 
-// llap/assemble.comp:89-123 for a stored level: output at the size of l0
+// llap/assemble.comp:89-123 for a stored level: output o at the size of l0
 template<int PX, int PY> DEV void assemble_stored(const coarse_t &sl, const __half *l0, size_t p0,
-    int w0, int x, int y, int bx, int by, __half *out)
+    size_t o, int lx, int sy, __half *out)
 {
-  const size_t o = (size_t)y * w0 + x;
   const float v = h2f(l0[NG * p0 + o]);
-  const float r = assemble_px<PX, PY>([&](int k, float) { return h2f(l0[k * p0 + o]); }, v, sl, x, y, bx, by);
+  const float r = assemble_px<PX, PY>([&](int k, float) { return h2f(l0[k * p0 + o]); }, v, sl, lx, sy);
   out[o] = f2h(r);
 }
 
@@ -213,64 +224,104 @@ __global__ void __launch_bounds__(256) k_llap_assemble(const __half *__restrict_
     const __half *__restrict__ l1, int w1, int h1, size_t p1, __half *__restrict__ out)
 {
   __shared__ coarse_t sl;
-  const int X0 = blockIdx.x * FT, Y0 = blockIdx.y * FT;
-  const int bx = X0 / 2 - 2, by = Y0 / 2 - 2;
-  stage_coarse(sl, l1, w1, h1, p1, first ? l1 + NG * p1 : coarse, bx, by);
+  const int X0 = blockIdx.x * FTX, Y0 = blockIdx.y * FTY;
+  stage_coarse(sl, l1, w1, h1, p1, first ? l1 + NG * p1 : coarse, X0 / 2 - 2, Y0 / 2 - 2);
   __syncthreads();
-  for(int t = threadIdx.x; t < FT * FT; t += blockDim.x)
-  {
-    int x, y;
-    if(!tile_item(t, X0, Y0, w0, h0, x, y)) continue;
-    switch((x & 1) + 2 * (y & 1))
-    { // uniform per warp (tile_item hands a warp one parity class)
-      case 0: assemble_stored<0, 0>(sl, l0, p0, w0, x, y, bx, by, out); break;
-      case 1: assemble_stored<1, 0>(sl, l0, p0, w0, x, y, bx, by, out); break;
-      case 2: assemble_stored<0, 1>(sl, l0, p0, w0, x, y, bx, by, out); break;
-      default: assemble_stored<1, 1>(sl, l0, p0, w0, x, y, bx, by, out); break;
+  for(int t = threadIdx.x; t < NKX * FTY; t += blockDim.x)
+  { // the pair (x, x + 1) of row y; a warp takes one row
+    const int lx = t % NKX, ry = t / NKX;
+    const int x = X0 + 2 * lx, y = Y0 + ry;
+    if(x >= w0 || y >= h0) continue;
+    const int sy = (ry >> 1) + 2;
+    const size_t o = (size_t)y * w0 + x;
+    const bool two = x + 1 < w0;
+    if(y & 1)
+    {
+      assemble_stored<0, 1>(sl, l0, p0, o, lx, sy, out);
+      if(two) assemble_stored<1, 1>(sl, l0, p0, o + 1, lx, sy, out);
+    }
+    else
+    {
+      assemble_stored<0, 0>(sl, l0, p0, o, lx, sy, out);
+      if(two) assemble_stored<1, 0>(sl, l0, p0, o + 1, lx, sy, out);
     }
   }
 }
 
 // llap/assemble.comp for level 0, the fine planes recomputed from the
 // filmcurv output like llap/curve.comp, fused with llap/colour.comp:141-160
-template<int PX, int PY> DEV void final_px(const dev_llap_k3_t &p, const coarse_t &sl, int x, int y,
-    int bx, int by, float r2s, float rden)
+template<int PX, int PY> DEV half4 final_px(const dev_llap_k3_t &p, const coarse_t &sl, const float rgb[3],
+    int lx, int sy, float r2s, float rden)
 {
-  float rgb[4];
-  ld_half4(p.rgbf + (size_t)y * p.W + x, rgb[0], rgb[1], rgb[2], rgb[3]);
   const float yv = lum2020(gclamp(rgb[0], -1000.0f, 1000.0f), gclamp(rgb[1], -1000.0f, 1000.0f), gclamp(rgb[2], -1000.0f, 1000.0f));
   const float v = f16r(yv);
   const bool unit_curve = p.ll_shadows == 1.0f && p.ll_highlights == 1.0f;
   float yo_ = f16r(assemble_px<PX, PY>([&](int, float g) {
       return f16r(unit_curve ? llap_curve_unit(yv, g, rden, p.ll_clarity)
                              : llap_curve_rcp(yv, g, p.ll_sigma, r2s, rden, p.ll_shadows, p.ll_highlights, p.ll_clarity)); },
-    v, sl, x, y, bx, by));
+    v, sl, lx, sy));
   const float yo = fmaxf(lum2020(rgb[0], rgb[1], rgb[2]), 1e-8f);
   if(yo_ < yo) yo_ = yo * expf(1.0f * (yo_ - yo));
-  float o[3];
-  for(int k = 0; k < 3; k++) o[k] = fmaxf(0.0f, rgb[k] * yo_ / yo);
-  p.out[(size_t)y * p.W + x] = mk_half4(o[0], o[1], o[2], 1.0f);
+  return mk_half4(fmaxf(0.0f, rgb[0] * yo_ / yo), fmaxf(0.0f, rgb[1] * yo_ / yo), fmaxf(0.0f, rgb[2] * yo_ / yo), 1.0f);
 }
 
-__global__ void __launch_bounds__(256) k_llap_final(const dev_llap_k3_t p)
+DEV void unpack_half4(uint2 u, float rgb[3])
+{
+  const __half2 lo = *reinterpret_cast<const __half2 *>(&u.x), hi = *reinterpret_cast<const __half2 *>(&u.y);
+  rgb[0] = __low2float(lo); rgb[1] = __high2float(lo); rgb[2] = __low2float(hi);
+}
+
+DEV uint2 pack_half4(half4 h) { return *reinterpret_cast<const uint2 *>(&h); }
+
+__global__ void __launch_bounds__(256, 8) k_llap_final(const dev_llap_k3_t p)
 {
   __shared__ coarse_t sl;
-  const int X0 = blockIdx.x * FT, Y0 = blockIdx.y * FT;
-  const int bx = X0 / 2 - 2, by = Y0 / 2 - 2;
-  stage_coarse(sl, p.l1, p.l1w, p.l1h, p.l1plane, p.coarse, bx, by);
+  const int X0 = blockIdx.x * FTX, Y0 = blockIdx.y * FTY;
+  stage_coarse(sl, p.l1, p.l1w, p.l1h, p.l1plane, p.coarse, X0 / 2 - 2, Y0 / 2 - 2);
   __syncthreads();
   const float sig = p.ll_sigma;
   const float r2s = 1.0f / (2.0f * sig), rden = 1.0f / (2.0f * sig * sig / 3.0f);
-  for(int t = threadIdx.x; t < FT * FT; t += blockDim.x)
-  {
-    int x, y;
-    if(!tile_item(t, X0, Y0, p.W, p.H, x, y)) continue;
-    switch((x & 1) + 2 * (y & 1))
+  // the pair as one 16 byte word where rows have even length and both images are 16 byte aligned
+  const bool vec = !(p.W & 1) && !((reinterpret_cast<uintptr_t>(p.rgbf) | reinterpret_cast<uintptr_t>(p.out)) & 15);
+  for(int t = threadIdx.x; t < NKX * FTY; t += blockDim.x)
+  { // the pair (x, x + 1) of row y; a warp takes one row
+    const int lx = t % NKX, ry = t / NKX;
+    const int x = X0 + 2 * lx, y = Y0 + ry;
+    if(x >= p.W || y >= p.H) continue;
+    const int sy = (ry >> 1) + 2;
+    const size_t o = (size_t)y * p.W + x;
+    const bool two = x + 1 < p.W;
+    uint4 u = make_uint4(0u, 0u, 0u, 0u);
+    if(vec) u = __ldg(reinterpret_cast<const uint4 *>(p.rgbf + o));
+    else
     {
-      case 0: final_px<0, 0>(p, sl, x, y, bx, by, r2s, rden); break;
-      case 1: final_px<1, 0>(p, sl, x, y, bx, by, r2s, rden); break;
-      case 2: final_px<0, 1>(p, sl, x, y, bx, by, r2s, rden); break;
-      default: final_px<1, 1>(p, sl, x, y, bx, by, r2s, rden); break;
+      const uint2 a = __ldg(reinterpret_cast<const uint2 *>(p.rgbf + o));
+      u.x = a.x; u.y = a.y;
+      if(two) { const uint2 b = __ldg(reinterpret_cast<const uint2 *>(p.rgbf + o + 1)); u.z = b.x; u.w = b.y; }
+    }
+    float ca[3], cb[3];
+    unpack_half4(make_uint2(u.x, u.y), ca);
+    unpack_half4(make_uint2(u.z, u.w), cb);
+    half4 ha, hb;
+    if(y & 1)
+    {
+      ha = final_px<0, 1>(p, sl, ca, lx, sy, r2s, rden);
+      if(two) hb = final_px<1, 1>(p, sl, cb, lx, sy, r2s, rden);
+    }
+    else
+    {
+      ha = final_px<0, 0>(p, sl, ca, lx, sy, r2s, rden);
+      if(two) hb = final_px<1, 0>(p, sl, cb, lx, sy, r2s, rden);
+    }
+    if(vec)
+    {
+      const uint2 a = pack_half4(ha), b = pack_half4(hb);
+      *reinterpret_cast<uint4 *>(p.out + o) = make_uint4(a.x, a.y, b.x, b.y);
+    }
+    else
+    {
+      p.out[o] = ha;
+      if(two) p.out[o + 1] = hb;
     }
   }
 }
@@ -278,8 +329,12 @@ __global__ void __launch_bounds__(256) k_llap_final(const dev_llap_k3_t p)
 } // namespace
 
 cudaError_t init_llap()
-{ // the reduce stages all 11 planes of a tile (47.9 KB): 4 CTAs per SM with the full carveout
-  return cudaFuncSetAttribute(k_llap_reduce, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+{ // the reduce stages all 11 planes of a tile (47.9 KB): 4 CTAs per SM with the full carveout;
+  // the assemble kernels 20.4 KB: 8 CTAs per SM (32 registers)
+  cudaError_t e = cudaFuncSetAttribute(k_llap_reduce, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+  if(e == cudaSuccess) e = cudaFuncSetAttribute(k_llap_assemble, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+  if(e == cudaSuccess) e = cudaFuncSetAttribute(k_llap_final, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+  return e;
 }
 
 cudaError_t launch_llap_reduce(const __half *in, int iw, int ih, size_t iplane,
@@ -293,14 +348,14 @@ cudaError_t launch_llap_reduce(const __half *in, int iw, int ih, size_t iplane,
 cudaError_t launch_llap_assemble(const __half *coarse, int first, const __half *l0, int w0, int h0, size_t p0,
     const __half *l1, int w1, int h1, size_t p1, __half *out, cudaStream_t s)
 {
-  dim3 grid((w0 + FT - 1) / FT, (h0 + FT - 1) / FT);
+  dim3 grid((w0 + FTX - 1) / FTX, (h0 + FTY - 1) / FTY);
   k_llap_assemble<<<grid, 256, 0, s>>>(coarse, first, l0, w0, h0, p0, l1, w1, h1, p1, out);
   return cudaGetLastError();
 }
 
 cudaError_t launch_llap_final(const dev_llap_k3_t &p, cudaStream_t s)
 {
-  dim3 grid((p.W + FT - 1) / FT, (p.H + FT - 1) / FT);
+  dim3 grid((p.W + FTX - 1) / FTX, (p.H + FTY - 1) / FTY);
   k_llap_final<<<grid, 256, 0, s>>>(p);
   return cudaGetLastError();
 }

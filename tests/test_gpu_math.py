@@ -1,0 +1,35 @@
+"""The exact arithmetic shortcuts of the kernels (common.cuh, hilite.cuh):
+rcp_f16v must equal the IEEE reciprocal on every input the kernels give it
+(all f16 values and their squares), div_ry the IEEE quotient and noop_code
+the denoise/noop code table on every u16 code. The check is
+a small CUDA program built against the kernels' own header; it runs on the
+device and compares bit for bit."""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+
+
+def _nvcc():
+    for c in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
+        if c and os.path.exists(os.path.join(c, "bin", "nvcc")):
+            return os.path.join(c, "bin", "nvcc")
+    return shutil.which("nvcc")
+
+
+@pytest.mark.gpu
+def test_rcp_f16v_and_div_ry_equal_ieee(tmp_path):
+    nvcc = _nvcc()
+    assert nvcc, "nvcc not found"
+    exe = str(tmp_path / "check_division")
+    subprocess.run([nvcc, "-gencode=arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
+                    "-I" + os.path.join(ROOT, "vkdt_gb300", "csrc"), "-o", exe,
+                    os.path.join(HERE, "cuda", "check_division.cu")], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "0 of 65536 f16 values differ, 0 of their squares" in r.stdout, r.stdout
+    assert "noop_code: 0 of" in r.stdout, r.stdout

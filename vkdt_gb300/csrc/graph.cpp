@@ -322,6 +322,7 @@ int fill_image(vkdt_cuda_graph_t *g, dev_image_t &d, const void *d_src, void *d_
   d.filters = g->ip.filters;
   d.black = g->ip.black[0] / 65535.0f;        // denoise/main.c:165-168
   d.white = g->ip.white[0] / 65535.0f;
+  d.codes.black = d.black; d.codes.white = d.white; d.codes.identity = 0;
   module_t *hl = g->mod("hilite");
   d.hl_white = hl->f("white"); d.hl_desat = hl->f("desat"); d.hl_soft = hl->f("soft");
   for(int k = 0; k < 3; k++) d.wb[k] = g->ip.whitebalance[k];
@@ -477,6 +478,7 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
   { // the develop kernels read the denoised f16 mosaic through the identity code table
     d.mosaic = reinterpret_cast<const uint16_t *>(dd.dn);
     d.noop_lut = g->at<__half>(g->off_idlut);
+    d.codes.identity = 1;
     d.pitch = g->W; d.cx = 0; d.cy = 0;
   }
   module_t *hl = g->mod("hilite");
@@ -530,7 +532,7 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
   // 1. noop + hilite half + first hilite reduce
   dev_hilite_k1_t k1;
   memset(&k1, 0, sizeof(k1));
-  k1.mosaic = d.mosaic; k1.noop_lut = d.noop_lut; k1.pitch = d.pitch; k1.cx = d.cx; k1.cy = d.cy; k1.W = d.W; k1.H = d.H;
+  k1.mosaic = d.mosaic; k1.codes = d.codes; k1.pitch = d.pitch; k1.cx = d.cx; k1.cy = d.cy; k1.W = d.W; k1.H = d.H;
   k1.filters = d.filters; k1.black = d.black; k1.white = d.white; k1.hl_white = white; k1.hl_desat = desat;
   for(int k = 0; k < 3; k++) k1.wb[k] = wb[k];
   k1.hw = g->hw; k1.hh = g->hh;

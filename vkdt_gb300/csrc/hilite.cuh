@@ -2,6 +2,7 @@
 // the hilite pyramid kernels and the fused develop kernel.
 #pragma once
 #include "common.cuh"
+#include "kernels.h"
 
 DEV int mirror_full(int i, int n)
 { // mirrored repeat for any i (periodic with 2n)
@@ -21,6 +22,36 @@ DEV float noop_val(const uint16_t *__restrict__ mosaic, int pitch, int cx, int c
   y = min(max(y, 0), H - 1);
   const float v = (float)__ldg(mosaic + (size_t)(y + cy) * pitch + (x + cx)) / 65535.0f;
   return f16r(fmaxf(0.0f, (v - black) / (white - black)));
+}
+
+// denoise/noop.comp:36-57 per u16 code: max(0, (v/65535 - black)/(white - black))
+// stored as f16, the IEEE operations of the code table (k_static.cu), with the
+// two quotients by Markstein's correction on reciprocals made once (div_ry).
+// For kernels whose shared memory leaves the 128 KB table no room in L1: a
+// lookup there is a random L2 sector read, evaluating the code a few
+// instructions. Identity codes are f16 bits.
+struct noop_eval_t { float black, wmb, ywb, y65535; bool wok, identity; };
+
+DEV noop_eval_t noop_prep(const dev_codes_t &c)
+{
+  noop_eval_t n;
+  n.black = c.black;
+  n.wmb = __fsub_rn(c.white, c.black);
+  n.ywb = __frcp_rn(n.wmb);
+  n.wok = div_ok(n.wmb);
+  n.y65535 = __frcp_rn(65535.0f);
+  n.identity = c.identity != 0;
+  return n;
+}
+
+DEV float noop_code(const noop_eval_t &n, uint32_t v)
+{
+  if(n.identity) return __half2float(__ushort_as_half((unsigned short)v));
+  // zero numerators are +0 here (v = 0; x equal to black) and give +0
+  const float x = v ? div_ry((float)v, 65535.0f, n.y65535, true) : 0.0f;
+  const float a = __fsub_rn(x, n.black);
+  const float q = a == 0.0f ? 0.0f : div_ry(a, n.wmb, n.ywb, n.wok);
+  return __half2float(__float2half_rn(fmaxf(0.0f, q)));
 }
 
 // hilite/half.comp:157-165 (bayer): textureGather order x=(0,1) y=(1,1) z=(1,0) w=(0,0)
@@ -52,50 +83,73 @@ DEV void hilite_half_xtrans(float c[9], int x, int y, float white, float h[3])
   h[2] = f16r(b);
 }
 
-// hilite/reduce.comp:21-61. fetch(ii, jj, rgb) returns the texel at (2o+ii, 2o+jj)
-template<class F> DEV void hilite_reduce_px(F fetch, float white_p, float desat, const float wbp[3], float o[4])
+// hilite/reduce.comp:21-61 in two parts. The terms a tap takes from its
+// texel (the luminance, and for an unclipped texel the colour desaturated
+// towards its grey) depend on the texel alone, so the kernels make them once
+// per texel of a tile (hilite_reduce_texel); an output then sums them over its
+// 5x5 taps (hilite_reduce_sum) in the shader's order.
+struct hl_reduce_t { float white, iwhite, d5, wb[3], hwb[3]; };
+
+DEV hl_reduce_t hilite_reduce_args(float white_p, float desat, const float wbp[3])
 {
-  float white = white_p;
-  if(!(white > 0.0f)) white = 1.0f;
+  hl_reduce_t a;
+  a.white = white_p;
+  if(!(a.white > 0.0f)) a.white = 1.0f;
+  for(int k = 0; k < 3; k++) a.wb[k] = wbp[k];
+  if(!(a.wb[0] * a.wb[0] + a.wb[1] * a.wb[1] + a.wb[2] * a.wb[2] > 1e-3f)) a.wb[0] = a.wb[1] = a.wb[2] = 1.0f;
+  const float ds = desat * desat;
+  a.d5 = 5.0f * ds * ds;
+  // the divisions by loop invariants as products (continuous values only:
+  // the clip test compares the texels themselves)
+  a.iwhite = 1.0f / a.white;
+  for(int k = 0; k < 3; k++) a.hwb[k] = 0.5f / a.wb[k];
+  return a;
+}
+
+// t[0]: luminance; t[1..3]: the desaturated colour of an unclipped texel, t[4] = 1
+// (a clipped texel: t[1..4] = 0, it takes no weight)
+DEV void hilite_reduce_texel(const hl_reduce_t &a, const float rgb[3], float t[5])
+{
+  t[0] = lum2020(rgb[0], rgb[1], rgb[2]);
+  t[1] = t[2] = t[3] = t[4] = 0.0f;
+  if(rgb[0] < a.white && rgb[1] < a.white && rgb[2] < a.white)
+  {
+    const float rw = rgb[0] * a.wb[0], gw = rgb[1] * a.wb[1], bw = rgb[2] * a.wb[2];
+    const float cmax = fmaxf(rw, fmaxf(gw, bw));
+    const float cmin = fminf(rw, fminf(gw, bw));
+    const float sat = __fdividef(cmax - cmin, fmaxf(1e-3f, cmax));
+    // smoothstep(0.2, 1, max / white) and smoothstep(0.15, 0.9, sat)
+    float s = gclamp((fmaxf(rgb[0], fmaxf(rgb[1], rgb[2])) * a.iwhite - 0.2f) * 1.25f, 0.0f, 1.0f);
+    s = s * s * (3.0f - 2.0f * s);
+    float t2 = gclamp((sat - 0.15f) * (1.0f / 0.75f), 0.0f, 1.0f);
+    t2 = t2 * t2 * (3.0f - 2.0f * t2);
+    t2 = gclamp(a.d5 * s * t2, 0.0f, 1.0f);
+#pragma unroll
+    for(int k = 0; k < 3; k++) t[1 + k] = gmix(rgb[k], (cmax + cmin) * a.hwb[k], t2);
+    t[4] = 1.0f;
+  }
+}
+
+// fetch(ii, jj, t) returns the terms of the texel at (2o+ii, 2o+jj)
+template<class F> DEV void hilite_reduce_sum(F fetch, float o[4])
+{
   const float w[5] = { 1.0f / 16.0f, 4.0f / 16.0f, 6.0f / 16.0f, 4.0f / 16.0f, 1.0f / 16.0f };
   const float sw[5] = { 1.0f, 2.0f, 0.0f, -2.0f, -1.0f };
-  float wb[3] = { wbp[0], wbp[1], wbp[2] };
-  if(!(wb[0] * wb[0] + wb[1] * wb[1] + wb[2] * wb[2] > 1e-3f)) wb[0] = wb[1] = wb[2] = 1.0f;
   float e0 = 0.0f, e1 = 0.0f, col[3] = { 0.0f, 0.0f, 0.0f }, wgt = 0.0f;
-  const float ds = desat * desat, d5 = 5.0f * ds * ds;
-  // the divisions by loop invariants as products (continuous values only:
-  // the clip test below compares the texels themselves)
-  const float iwhite = 1.0f / white;
-  const float hwb[3] = { 0.5f / wb[0], 0.5f / wb[1], 0.5f / wb[2] };
 #pragma unroll
   for(int jj = -2; jj <= 2; jj++)
 #pragma unroll
   for(int ii = -2; ii <= 2; ii++)
   {
-    float rgb[3];
-    fetch(ii, jj, rgb);
-    const float l = lum2020(rgb[0], rgb[1], rgb[2]);
-    e0 += w[jj + 2] * sw[ii + 2] * l;
-    e1 += w[ii + 2] * sw[jj + 2] * l;
+    float t[5];
+    fetch(ii, jj, t);
+    e0 += w[jj + 2] * sw[ii + 2] * t[0];
+    e1 += w[ii + 2] * sw[jj + 2] * t[0];
     const float u = w[ii + 2] * w[jj + 2];
-    if(rgb[0] < white && rgb[1] < white && rgb[2] < white)
+    if(t[4] != 0.0f)
     {
-      const float rw = rgb[0] * wb[0], gw = rgb[1] * wb[1], bw = rgb[2] * wb[2];
-      const float cmax = fmaxf(rw, fmaxf(gw, bw));
-      const float cmin = fminf(rw, fminf(gw, bw));
-      const float sat = __fdividef(cmax - cmin, fmaxf(1e-3f, cmax));
-      // smoothstep(0.2, 1, max / white) and smoothstep(0.15, 0.9, sat)
-      float s = gclamp((fmaxf(rgb[0], fmaxf(rgb[1], rgb[2])) * iwhite - 0.2f) * 1.25f, 0.0f, 1.0f);
-      s = s * s * (3.0f - 2.0f * s);
-      float t = gclamp((sat - 0.15f) * (1.0f / 0.75f), 0.0f, 1.0f);
-      t = t * t * (3.0f - 2.0f * t);
-      t = gclamp(d5 * s * t, 0.0f, 1.0f);
 #pragma unroll
-      for(int k = 0; k < 3; k++)
-      {
-        const float v = gmix(rgb[k], (cmax + cmin) * hwb[k], t);
-        col[k] += v * u;
-      }
+      for(int k = 0; k < 3; k++) col[k] += t[1 + k] * u;
       wgt += u;
     }
   }

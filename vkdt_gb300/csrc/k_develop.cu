@@ -174,11 +174,14 @@ template<int PX, int PY> DEV void fix_taps_in(const smem_t &s, int bx, int sly,
 // on flat input the direction is a near tie: the sample positions alone have
 // the covariance (1.25 -0.25; -0.25 1.25), eigenvectors at 45 degrees, so the
 // snap there follows the last bits of the sums and is evaluated exactly.
+// The greens are f16 values (the hilite output), so their reciprocals and
+// those of their squares come from rcp_f16v; the quotients by the four sums
+// share one correctly rounded reciprocal each (div_ry): the same IEEE results.
 DEV void gauss_exact(const float px[8], float v[4])
 {
   float inv[8];
 #pragma unroll
-  for(int k = 0; k < 8; k++) inv[k] = __frcp_rn(px[k]);
+  for(int k = 0; k < 8; k++) inv[k] = rcp_f16v(px[k]);
   int k;
   // i/px for i in {-1,0,1,2} is i*(1/px) exactly (scaling by +-1, 2 is exact)
   float mw0 = 0, mw1 = 0, mb0 = 0, mb1 = 0, smw = 0, smb = 0;
@@ -198,8 +201,12 @@ DEV void gauss_exact(const float px[8], float v[4])
   // (the products above are exact, so contraction cannot change them;
   // the covariance sums below decide the snapped direction and are
   // evaluated without contraction, in the shader's order)
-  mw0 = __fdiv_rn(mw0, smw); mw1 = __fdiv_rn(mw1, smw);
-  mb0 = __fdiv_rn(mb0, smb); mb1 = __fdiv_rn(mb1, smb);
+  {
+    const float yw = __frcp_rn(smw), yb = __frcp_rn(smb);
+    const bool okw = div_ok(smw), okb = div_ok(smb);
+    mw0 = div_ry(mw0, smw, yw, okw); mw1 = div_ry(mw1, smw, yw, okw);
+    mb0 = div_ry(mb0, smb, yb, okb); mb1 = div_ry(mb1, smb, yb, okb);
+  }
   float Sw00 = 0, Sw01 = 0, Sw10 = 0, Sw11 = 0, Sb00 = 0, Sb01 = 0, Sb10 = 0, Sb11 = 0, sw = 0, sb = 0;
   k = 0;
 #pragma unroll
@@ -216,7 +223,7 @@ DEV void gauss_exact(const float px[8], float v[4])
     Sw11 = __fadd_rn(Sw11, __fmul_rn(__fmul_rn(p2, q1), q1));
     sw = __fadd_rn(sw, p2);
     q0 = __fsub_rn((float)ii, mb0); q1 = __fsub_rn((float)j, mb1);
-    p2 = __frcp_rn(p2);
+    p2 = rcp_f16v(p2);
     Sb00 = __fadd_rn(Sb00, __fmul_rn(__fmul_rn(p2, q0), q0));
     Sb01 = __fadd_rn(Sb01, __fmul_rn(__fmul_rn(p2, q0), q1));
     Sb10 = __fadd_rn(Sb10, __fmul_rn(__fmul_rn(p2, q1), q0));
@@ -224,8 +231,14 @@ DEV void gauss_exact(const float px[8], float v[4])
     sb = __fadd_rn(sb, p2);
     k++;
   }
-  Sw00 = __fdiv_rn(Sw00, sw); Sw01 = __fdiv_rn(Sw01, sw); Sw10 = __fdiv_rn(Sw10, sw); Sw11 = __fdiv_rn(Sw11, sw);
-  Sb00 = __fdiv_rn(Sb00, sb); Sb01 = __fdiv_rn(Sb01, sb); Sb10 = __fdiv_rn(Sb10, sb); Sb11 = __fdiv_rn(Sb11, sb);
+  {
+    const float yw = __frcp_rn(sw), yb = __frcp_rn(sb);
+    const bool okw = div_ok(sw), okb = div_ok(sb);
+    Sw00 = div_ry(Sw00, sw, yw, okw); Sw01 = div_ry(Sw01, sw, yw, okw);
+    Sw10 = div_ry(Sw10, sw, yw, okw); Sw11 = div_ry(Sw11, sw, yw, okw);
+    Sb00 = div_ry(Sb00, sb, yb, okb); Sb01 = div_ry(Sb01, sb, yb, okb);
+    Sb10 = div_ry(Sb10, sb, yb, okb); Sb11 = div_ry(Sb11, sb, yb, okb);
+  }
   const float detw = __fsub_rn(__fmul_rn(Sw00, Sw11), __fmul_rn(Sw10, Sw01));
   const float detb = __fsub_rn(__fmul_rn(Sb00, Sb11), __fmul_rn(Sb10, Sb01));
   float eval[2], evec0[2], evec1[2];

@@ -74,7 +74,7 @@ template<int PY, class R> DEV float vcol(R rowsum, int ky)
   return r / 9.0f;
 }
 
-// expand of two planes at once (fetch returns both texels as a half2): the
+// expand of two planes at once (fetch returns both texels as a float2): the
 // same sums in the same order as hrow and vcol for each of the two
 template<int PX, int PY, class F> DEV float2 expand2(F fetch, int kx, int ky)
 {
@@ -89,7 +89,7 @@ template<int PX, int PY, class F> DEV float2 expand2(F fetch, int kx, int ky)
     for(int a = 0; a < NX; a++)
     {
       const float w = PX ? ((a == 0 || a == 3) ? 1.0f : 0.5f) : (a == 2 ? 1.0f : 0.5f);
-      const float2 f = __half22float2(fetch(kx + BXO + a, ky + BYO + b));
+      const float2 f = fetch(kx + BXO + a, ky + BYO + b);
       row0 += w * f.x;
       row1 += w * f.y;
     }
@@ -116,14 +116,20 @@ __global__ void __launch_bounds__(256) k_llap_reduce(const __half *__restrict__ 
   const int gx0 = 2 * OX - 2, gy0 = 2 * OY - 1;     // input texel of t[.][0][0]
   const bool inside = gx0 >= 0 && gy0 >= 0 && gx0 + RI_X <= iw && gy0 + RI_Y <= ih && !(iw & 1);
   if(inside)
+  { // asynchronous copies: every word of the tile in flight at once
     for(int i = threadIdx.x; i < RI_Y * (RI_X / 2); i += blockDim.x)
     {
       const int r = i / (RI_X / 2), c = i % (RI_X / 2);
       const size_t o = (size_t)(gy0 + r) * iw + gx0 + 2 * c;
 #pragma unroll
       for(int k = 0; k < NPL; k++)
-        *reinterpret_cast<uint32_t *>(&t[k][r][2 * c]) = __ldg(reinterpret_cast<const uint32_t *>(in + k * ip + o));
+      {
+        const unsigned dst = (unsigned)__cvta_generic_to_shared(&t[k][r][2 * c]);
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" :: "r"(dst), "l"(in + k * ip + o) : "memory");
+      }
     }
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+  }
   else
     for(int i = threadIdx.x; i < RI_Y * RI_X; i += blockDim.x)
     {
@@ -159,12 +165,13 @@ __global__ void __launch_bounds__(256) k_llap_reduce(const __half *__restrict__ 
 
 // the coarse level around one output tile: slot (sx, sy) holds the mirrored
 // texel (bx+sx, by+sy). An output mixes the two adjacent planes around its
-// grey value, so the planes are staged in pairs (k, k+1), one 4 byte word per
-// slot (f16 values: exact), beside the coarse assembled image. The coarse
-// image enters every output, so its row sums are made once per tile.
+// grey value, so the planes are staged in pairs (k, k+1), one 8 byte word per
+// slot (f16 values as floats: exact, one load and no conversion per tap),
+// beside the coarse assembled image. The coarse image enters every output, so
+// its row sums are made once per tile.
 struct coarse_t
 {
-  __half2 pr[NG - 1][FSY][FSX];   // planes (k, k+1), k = 0 .. NG-2
+  float2 pr[NG - 1][FSY][FSX];    // planes (k, k+1), k = 0 .. NG-2
   float c[FSY][FSX];              // the coarse assembled image (the grey plane on the first level)
   float hc[2][FSY][NKX];          // hrow of c for even / odd outputs: [x parity][slot row][column - X0/2]
 };
@@ -176,11 +183,11 @@ DEV void stage_coarse(coarse_t &sc, const __half *l1, int w1, int h1, size_t p1,
   {
     const int sx = r % FSX, sy = r / FSX;
     const size_t o = (size_t)mirror1(by + sy, h1) * w1 + mirror1(bx + sx, w1);
-    __half h[NG];
+    float h[NG];
 #pragma unroll
-    for(int k = 0; k < NG; k++) h[k] = __ldg(l1 + k * p1 + o);
+    for(int k = 0; k < NG; k++) h[k] = h2f(__ldg(l1 + k * p1 + o));
 #pragma unroll
-    for(int k = 0; k < NG - 1; k++) sc.pr[k][sy][sx] = __halves2half2(h[k], h[k + 1]);
+    for(int k = 0; k < NG - 1; k++) sc.pr[k][sy][sx] = make_float2(h[k], h[k + 1]);
     sc.c[sy][sx] = h2f(__ldg(coarse + o));
   }
   __syncthreads();
@@ -203,7 +210,7 @@ template<int PX, int PY, class L0> DEV float assemble_px(L0 l0, float v, const c
   const int hi = gamma_hi_from_v(v);
   const float glo = kLlapGamma[hi - 1], ghi = kLlapGamma[hi];
   const float a = gclamp((v - glo) / (ghi - glo), 0.0f, 1.0f);
-  const __half2 (*pr)[FSX] = sc.pr[hi - 1];
+  const float2 (*pr)[FSX] = sc.pr[hi - 1];
   const float2 e = expand2<PX, PY>([&](int ix, int iy) { return pr[iy][ix]; }, lx + 2, sy);
   const float la = l0(hi - 1, glo) - e.x;
   const float lb = l0(hi, ghi) - e.y;
@@ -273,7 +280,7 @@ DEV void unpack_half4(uint2 u, float rgb[3])
 
 DEV uint2 pack_half4(half4 h) { return *reinterpret_cast<const uint2 *>(&h); }
 
-__global__ void __launch_bounds__(256, 8) k_llap_final(const dev_llap_k3_t p)
+__global__ void __launch_bounds__(256, 6) k_llap_final(const dev_llap_k3_t p)
 {
   __shared__ coarse_t sl;
   const int X0 = blockIdx.x * FTX, Y0 = blockIdx.y * FTY;
@@ -330,7 +337,7 @@ __global__ void __launch_bounds__(256, 8) k_llap_final(const dev_llap_k3_t p)
 
 cudaError_t init_llap()
 { // the reduce stages all 11 planes of a tile (47.9 KB): 4 CTAs per SM with the full carveout;
-  // the assemble kernels 20.4 KB: 8 CTAs per SM (32 registers)
+  // the assemble kernels 36 KB: 6 CTAs per SM
   cudaError_t e = cudaFuncSetAttribute(k_llap_reduce, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
   if(e == cudaSuccess) e = cudaFuncSetAttribute(k_llap_assemble, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
   if(e == cudaSuccess) e = cudaFuncSetAttribute(k_llap_final, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);

@@ -184,11 +184,17 @@ __global__ void __launch_bounds__(256) k_nd_gauss_xt(const dev_nodes_t p)
     const float fi = (float)gi[k], fj = (float)gj[k];
     mw0 = __fadd_rn(mw0, __fmul_rn(fi, px[k])); mw1 = __fadd_rn(mw1, __fmul_rn(fj, px[k]));
     smw = __fadd_rn(smw, px[k]);
-    mb0 = __fadd_rn(mb0, __fdiv_rn(fi, px[k])); mb1 = __fadd_rn(mb1, __fdiv_rn(fj, px[k]));
-    smb = __fadd_rn(smb, __frcp_rn(px[k]));
+    // fi/px = fi (1/px) exactly for fi in {0, 1, 2}; px is an f16 value (rcp_f16v)
+    const float inv = rcp_f16v(px[k]);
+    mb0 = __fadd_rn(mb0, __fmul_rn(fi, inv)); mb1 = __fadd_rn(mb1, __fmul_rn(fj, inv));
+    smb = __fadd_rn(smb, inv);
   }
-  mw0 = __fdiv_rn(mw0, smw); mw1 = __fdiv_rn(mw1, smw);
-  mb0 = __fdiv_rn(mb0, smb); mb1 = __fdiv_rn(mb1, smb);
+  {
+    const float yw = __frcp_rn(smw), yb = __frcp_rn(smb);
+    const bool okw = div_ok(smw), okb = div_ok(smb);
+    mw0 = div_ry(mw0, smw, yw, okw); mw1 = div_ry(mw1, smw, yw, okw);
+    mb0 = div_ry(mb0, smb, yb, okb); mb1 = div_ry(mb1, smb, yb, okb);
+  }
   float Sw00 = 0, Sw01 = 0, Sw10 = 0, Sw11 = 0, Sb00 = 0, Sb01 = 0, Sb10 = 0, Sb11 = 0, sw = 0, sb = 0;
 #pragma unroll
   for(int k = 0; k < 5; k++)
@@ -201,15 +207,21 @@ __global__ void __launch_bounds__(256) k_nd_gauss_xt(const dev_nodes_t p)
     Sw11 = __fadd_rn(Sw11, __fmul_rn(__fmul_rn(p2, q1), q1));
     sw = __fadd_rn(sw, p2);
     q0 = __fsub_rn((float)gi[k], mb0); q1 = __fsub_rn((float)gj[k], mb1);
-    p2 = __frcp_rn(p2);
+    p2 = rcp_f16v(p2);
     Sb00 = __fadd_rn(Sb00, __fmul_rn(__fmul_rn(p2, q0), q0));
     Sb01 = __fadd_rn(Sb01, __fmul_rn(__fmul_rn(p2, q0), q1));
     Sb10 = __fadd_rn(Sb10, __fmul_rn(__fmul_rn(p2, q1), q0));
     Sb11 = __fadd_rn(Sb11, __fmul_rn(__fmul_rn(p2, q1), q1));
     sb = __fadd_rn(sb, p2);
   }
-  Sw00 = __fdiv_rn(Sw00, sw); Sw01 = __fdiv_rn(Sw01, sw); Sw10 = __fdiv_rn(Sw10, sw); Sw11 = __fdiv_rn(Sw11, sw);
-  Sb00 = __fdiv_rn(Sb00, sb); Sb01 = __fdiv_rn(Sb01, sb); Sb10 = __fdiv_rn(Sb10, sb); Sb11 = __fdiv_rn(Sb11, sb);
+  {
+    const float yw = __frcp_rn(sw), yb = __frcp_rn(sb);
+    const bool okw = div_ok(sw), okb = div_ok(sb);
+    Sw00 = div_ry(Sw00, sw, yw, okw); Sw01 = div_ry(Sw01, sw, yw, okw);
+    Sw10 = div_ry(Sw10, sw, yw, okw); Sw11 = div_ry(Sw11, sw, yw, okw);
+    Sb00 = div_ry(Sb00, sb, yb, okb); Sb01 = div_ry(Sb01, sb, yb, okb);
+    Sb10 = div_ry(Sb10, sb, yb, okb); Sb11 = div_ry(Sb11, sb, yb, okb);
+  }
   const float detw = __fsub_rn(__fmul_rn(Sw00, Sw11), __fmul_rn(Sw10, Sw01));
   const float detb = __fsub_rn(__fmul_rn(Sb00, Sb11), __fmul_rn(Sb10, Sb01));
   float eval[2], e0[2], e1[2];

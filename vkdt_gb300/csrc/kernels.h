@@ -8,6 +8,11 @@
 
 struct half4;
 
+// how the kernels turn a mosaic's u16 codes into the normalised values of the
+// path: denoise/noop.comp:36-57 on (black, white) evaluated per code, or, where
+// the mosaic pointer reads the wavelet output (f16), the f16 bits themselves
+struct dev_codes_t { float black, white; int identity; };
+
 // per image constants of the path, filled by the host from the module
 // parameters and the image metadata (the uniforms and push constants the
 // modules' commit_params / create_nodes would upload)
@@ -16,6 +21,7 @@ struct dev_image_t
   // mosaic (source) and its active window
   const uint16_t *mosaic;
   const __half *noop_lut; // denoise/noop of every u16 code (65536 f16)
+  dev_codes_t codes;    // the same values evaluated per code
   int pitch;            // elements per mosaic row
   int cx, cy;           // crop offset (denoise push.crop.xy)
   int W, H;             // denoise/hilite output size
@@ -50,7 +56,7 @@ struct dev_image_t
 struct dev_hilite_k1_t
 {
   const uint16_t *mosaic;
-  const __half *noop_lut;
+  dev_codes_t codes;
   int pitch, cx, cy, W, H;
   uint32_t filters;
   float black, white, hl_white, hl_desat;
@@ -102,7 +108,7 @@ cudaError_t launch_denoise(const dev_denoise_t &p, int stage, cudaStream_t s);
 struct dev_nodes_t
 {
   const uint16_t *mosaic;
-  const __half *noop_lut;
+  const __half *noop_lut; // denoise/noop of every u16 code (L1 resident in these kernels)
   int pitch, cx, cy;     // source layout and crop offset
   int W, H;              // denoise / hilite size
   uint32_t filters;

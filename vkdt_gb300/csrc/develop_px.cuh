@@ -5,15 +5,14 @@
 #include "kernels.h"
 #include "pixel.cuh"
 
-// colour/main-impl.glsl:200-341 on the matrix path (no clut/pick/rbf, sat 1)
+// colour/main-impl.glsl:200-341 on the matrix path (no clut/pick/rbf, sat 1):
+// camera matrix, CAT16 in, cone scale, CAT16 out and exposure, linear in the
+// pixel, applied as their product cmat (made by the host per image)
 DEV void colour_px(const dev_image_t &p, const float in[3], float o[3])
 {
-  float r[3], cl[3], q[3];
-  for(int i = 0; i < 3; i++) r[i] = p.cam[3 * i + 0] * in[0] + p.cam[3 * i + 1] * in[1] + p.cam[3 * i + 2] * in[2];
-  for(int i = 0; i < 3; i++) cl[i] = p.P[3 * i + 0] * r[0] + p.P[3 * i + 1] * r[1] + p.P[3 * i + 2] * r[2];
-  for(int i = 0; i < 3; i++) cl[i] *= p.clscale[i];
-  for(int i = 0; i < 3; i++) q[i] = p.Q[3 * i + 0] * cl[0] + p.Q[3 * i + 1] * cl[1] + p.Q[3 * i + 2] * cl[2];
-  for(int i = 0; i < 3; i++) o[i] = f16r(gclamp(q[i] * p.mulw, -65535.0f, 65535.0f));
+  for(int i = 0; i < 3; i++)
+    o[i] = f16r(gclamp(p.cmat[3 * i + 0] * in[0] + p.cmat[3 * i + 1] * in[1] + p.cmat[3 * i + 2] * in[2],
+                       -65535.0f, 65535.0f));
 }
 
 // filmcurv/main.comp:106-205, colour modes 1 and 3 (adjust_colour_dng,

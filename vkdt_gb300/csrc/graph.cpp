@@ -280,6 +280,22 @@ void colour_commit(vkdt_cuda_graph_t *g, dev_image_t &d)
   m3_apply(d.P, one, src);
   m3_apply(d.P, mul, dst);
   for(int k = 0; k < 3; k++) d.clscale[k] = dst[k] / src[k];
+  // the chain as one matrix: the kernels apply it per pixel (continuous values
+  // before an f16 store; a few f32 ulp from the three products in sequence)
+  double a[9], b[9];
+  for(int i = 0; i < 3; i++) for(int j = 0; j < 3; j++)
+  {
+    double s = 0.0;
+    for(int k = 0; k < 3; k++) s += (double)d.P[3 * i + k] * d.cam[3 * k + j];
+    a[3 * i + j] = s * d.clscale[i];
+  }
+  for(int i = 0; i < 3; i++) for(int j = 0; j < 3; j++)
+  {
+    double s = 0.0;
+    for(int k = 0; k < 3; k++) s += (double)d.Q[3 * i + k] * a[3 * k + j];
+    b[3 * i + j] = s * d.mulw;
+  }
+  for(int i = 0; i < 9; i++) d.cmat[i] = (float)b[i];
 }
 
 size_t align_up(size_t v) { return (v + 255) & ~(size_t)255; }

@@ -59,7 +59,7 @@ struct smem_t
       float sw[3][CX][CX];     // splat weights, same taps as fw
       float B1[3][BX][BX];     // hilite coarse level (rgb) around the tile
     } e;
-    __half L0[NPL][LX][2][LH]; // llap level 0 planes, [y][slot&1][slot>>1]
+    __half L0[NPL][LX][LX + 1]; // llap level 0 planes, [y][slot] (rows of an even length)
   } u;
   uint32_t hist[257];
 };
@@ -491,23 +491,20 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
       {
 #pragma unroll
         for(int k = 0; k < NPL - 1; k++)
-          s.u.L0[k][sly][slx & 1][slx >> 1] = f2h(llap_curve_unit(yv, kLlapGamma[k], rden, cla));
+          s.u.L0[k][sly][slx] = f2h(llap_curve_unit(yv, kLlapGamma[k], rden, cla));
       }
       else
       {
 #pragma unroll
         for(int k = 0; k < NPL - 1; k++)
-          s.u.L0[k][sly][slx & 1][slx >> 1] = f2h(llap_curve_rcp(yv, kLlapGamma[k], sig, r2s, rden, shd, hil, cla));
+          s.u.L0[k][sly][slx] = f2h(llap_curve_rcp(yv, kLlapGamma[k], sig, r2s, rden, shd, hil, cla));
       }
-      s.u.L0[NPL - 1][sly][slx & 1][slx >> 1] = f2h(yv);
+      s.u.L0[NPL - 1][sly][slx] = f2h(yv);
     }
   }
   __syncthreads();
 
-  // ---- llap/reduce.comp (sample_semisoft) for level 1 outputs [X0/2, X0/2+TX/2).
-  // The four bilinear taps at half texel offsets, ((t00/2 + t10/2)/2 + (t01/2 + t11/2)/2)
-  // summed and /4: halving is exact, so with the pair sums P = t0 + t1 this is
-  // exactly ((((P00 + P10)/4 + (P01 + P11)/4) + ...)/4 as the shader computes it.
+  // ---- llap/reduce.comp (sample_semisoft) for level 1 outputs [X0/2, X0/2+TX/2) (llap_reduce_px)
   {
     const int lx = tid % (TX / 2), ly = tid / (TX / 2);
     const int ox = X0 / 2 + lx, oy = Y0 / 2 + ly;
@@ -517,20 +514,8 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
       // level 0 slot of virtual x = 2ox + a - 1 is 2lx + a
       for(int k = 0; k < NPL; k++)
       {
-        float P[3][2];
-        for(int r = 0; r < 3; r++)
-        {
-          const __half *row = &s.u.L0[k][2 * ly + r][0][0];
-          const float t0 = h2f(row[lx]), t1 = h2f(row[LH + lx]), t2 = h2f(row[lx + 1]);
-          P[r][0] = t0 + t1;
-          P[r][1] = t1 + t2;
-        }
-        const float q00 = (P[0][0] + P[1][0]) * 0.25f;
-        const float q10 = (P[0][1] + P[1][1]) * 0.25f;
-        const float q01 = (P[1][0] + P[2][0]) * 0.25f;
-        const float q11 = (P[1][1] + P[2][1]) * 0.25f;
-        const float r = (((q00 + q10) + q01) + q11) * 0.25f;
-        p.l1[k * p.l1plane + (size_t)oy * p.l1w + ox] = f2h(r);
+        const __half *const row[3] = { &s.u.L0[k][2 * ly][2 * lx], &s.u.L0[k][2 * ly + 1][2 * lx], &s.u.L0[k][2 * ly + 2][2 * lx] };
+        p.l1[k * p.l1plane + (size_t)oy * p.l1w + ox] = f2h(llap_reduce_px(row));
       }
     }
   }

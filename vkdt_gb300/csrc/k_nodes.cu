@@ -428,7 +428,7 @@ __global__ void __launch_bounds__(256) k_nd_resample(const dev_nodes_t p)
 // [X0-1, X0+TX) of a tile and the first llap/reduce level of its outputs
 // (the arithmetic of the tail of the fused develop kernel)
 constexpr int TX = 32, TY = 32, NT = 256, NPL = 11;
-constexpr int LX = TX + 1, LH = (LX + 1) / 2;
+constexpr int LX = TX + 1;
 
 DEV int mirror1(int i, int n)
 {
@@ -441,7 +441,7 @@ DEV int mirror1(int i, int n)
 // (p.rgbf holds the filmcurv output); this kernel reads it for the llap curves
 template<bool FC> __global__ void __launch_bounds__(NT) k_post(const dev_image_t p, const half4 *__restrict__ dm)
 {
-  __shared__ __half L0[NPL][LX][2][LH];
+  __shared__ __align__(4) __half L0[NPL][LX][LX + 1];   // [y][slot], rows of an even length
   __shared__ uint32_t hist[257];
   const int tid = threadIdx.x;
   const int W = p.W, H = p.H;
@@ -486,15 +486,15 @@ template<bool FC> __global__ void __launch_bounds__(NT) k_post(const dev_image_t
     {
 #pragma unroll
       for(int k = 0; k < NPL - 1; k++)
-        L0[k][sly][slx & 1][slx >> 1] = f2h(llap_curve_unit(yv, kLlapGamma[k], rden, cla));
+        L0[k][sly][slx] = f2h(llap_curve_unit(yv, kLlapGamma[k], rden, cla));
     }
     else
     {
 #pragma unroll
       for(int k = 0; k < NPL - 1; k++)
-        L0[k][sly][slx & 1][slx >> 1] = f2h(llap_curve_rcp(yv, kLlapGamma[k], sig, r2s, rden, shd, hil, cla));
+        L0[k][sly][slx] = f2h(llap_curve_rcp(yv, kLlapGamma[k], sig, r2s, rden, shd, hil, cla));
     }
-    L0[NPL - 1][sly][slx & 1][slx >> 1] = f2h(yv);
+    L0[NPL - 1][sly][slx] = f2h(yv);
   }
   __syncthreads();
   // llap/reduce.comp (sample_semisoft) for level 1 outputs [X0/2, X0/2+TX/2)
@@ -504,21 +504,9 @@ template<bool FC> __global__ void __launch_bounds__(NT) k_post(const dev_image_t
     const bool own = ox >= OX / 2 && ox < min(OX / 2 + TX / 2, p.l1w) && oy >= OY / 2 && oy < min(OY / 2 + TY / 2, p.l1h);
     if(own)
       for(int k = 0; k < NPL; k++)
-      {
-        float P[3][2];
-        for(int r = 0; r < 3; r++)
-        {
-          const __half *row = &L0[k][2 * ly + r][0][0];
-          const float t0 = h2f(row[lx]), t1 = h2f(row[LH + lx]), t2 = h2f(row[lx + 1]);
-          P[r][0] = t0 + t1;
-          P[r][1] = t1 + t2;
-        }
-        const float q00 = (P[0][0] + P[1][0]) * 0.25f;
-        const float q10 = (P[0][1] + P[1][1]) * 0.25f;
-        const float q01 = (P[1][0] + P[2][0]) * 0.25f;
-        const float q11 = (P[1][1] + P[2][1]) * 0.25f;
-        const float r = (((q00 + q10) + q01) + q11) * 0.25f;
-        p.l1[k * p.l1plane + (size_t)oy * p.l1w + ox] = f2h(r);
+      { // level 0 slot of virtual x = 2ox + a - 1 is 2lx + a (llap_reduce_px)
+        const __half *const row[3] = { &L0[k][2 * ly][2 * lx], &L0[k][2 * ly + 1][2 * lx], &L0[k][2 * ly + 2][2 * lx] };
+        p.l1[k * p.l1plane + (size_t)oy * p.l1w + ox] = f2h(llap_reduce_px(row));
       }
   }
   if(!FC && p.hist)

@@ -38,6 +38,7 @@ struct dev_image_t
   int fixup;
   // colour: camera matrix, cat16 matrices and per channel cone scale, exposure
   float cam[9], P[9], Q[9], clscale[3], mulw;
+  float cmat[9];        // their product mulw Q diag(clscale) P cam, made once per image in double precision
   // filmcurv
   float fc_il, fc_k, fc_bias;
   int fc_mode;

@@ -68,6 +68,28 @@ DEV float llap_curve_unit(float x, float g, float rden, float clarity)
   return x + clarity * c * curve_exp(-c * c * rden);
 }
 
+// llap/reduce.comp (sample_semisoft) of one level 1 output from a level 0 plane
+// staged in slot order: row[r] points at the slot of virtual x = 2 ox - 1 in the
+// row of virtual y = 2 oy - 1 + r (4 byte aligned). The four bilinear taps at
+// half texel offsets are ((t00/2 + t10/2)/2 + (t01/2 + t11/2)/2 ...)/4; halving is
+// exact, so with the pair sums P = t0 + t1 the shader's value is
+// ((((P00 + P10)/4 + (P01 + P11)/4) + (P10 + P20)/4) + (P11 + P21)/4)/4, and as
+// scaling by a power of two commutes with rounding (no subnormal sums here) that
+// is the same chain of sums scaled once by 1/16.
+DEV float llap_reduce_px(const __half *const row[3])
+{
+  float P[3][2];
+#pragma unroll
+  for(int r = 0; r < 3; r++)
+  {
+    const __half2 a = *reinterpret_cast<const __half2 *>(row[r]);
+    const float t0 = __low2float(a), t1 = __high2float(a), t2 = h2f(row[r][2]);
+    P[r][0] = t0 + t1;
+    P[r][1] = t1 + t2;
+  }
+  return (((((P[0][0] + P[1][0]) + (P[0][1] + P[1][1])) + (P[1][0] + P[2][0])) + (P[1][1] + P[2][1]))) * 0.0625f;
+}
+
 // histogram bin, bit exact with the oracle (see hist_log there for the method)
 DEV float hist_log(float x)
 {

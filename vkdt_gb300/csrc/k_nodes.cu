@@ -240,6 +240,27 @@ DEV void cov_z(const dev_nodes_t &p, int x, int y, float c[4])
   ld_half4(p.cov + (size_t)y * p.hw + x, c[0], c[1], c[2], c[3]);
 }
 
+// exp(-0.5 (of0^2 / e0 + of1^2 / e1)) with of0 = c i + s j, of1 = -s i + c j
+// (c, s the covariance's eigenvector) as a quadratic form in the tap offset:
+// exp2(qa i^2 + qb i j + qc j^2), the coefficients made once per pixel (the
+// same weight up to the rounding of the products, before an f16 store)
+struct xt_quad_t { float qa, qb, qc; };
+DEV xt_quad_t xt_quad(float c, float s, float ie0, float ie1)
+{
+  const float k = -0.5f * 1.4426950408889634f;
+  xt_quad_t q;
+  q.qa = k * (c * c * ie0 + s * s * ie1);
+  q.qb = k * 2.0f * c * s * (ie0 - ie1);
+  q.qc = k * (s * s * ie0 + c * c * ie1);
+  return q;
+}
+DEV float xt_weight(const xt_quad_t &q, int i, int j)
+{
+  float w;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(w) : "f"(q.qa * (float)(i * i) + q.qb * (float)(i * j) + q.qc * (float)(j * j)));
+  return w;
+}
+
 // tiles of the x-trans splat and fix kernels: multiples of the 6x6 CFA period
 // and of the 3x3 blocks of the covariance; the mosaic (and the splat output)
 // the taps read is staged once per tile with the halo the taps reach. A warp
@@ -283,19 +304,16 @@ __global__ void __launch_bounds__(256) k_nd_splat_xt(const dev_nodes_t p)
     float cov[4];
     cov_z(p, x / 3, y / 3, cov);
     const float e0 = gclamp(cov[0], 0.01f, 25.0f), e1 = gclamp(cov[1], 0.01f, 25.0f);
-    const float ie0 = 1.0f / e0, ie1 = 1.0f / e1;
+    const xt_quad_t q = xt_quad(cov[2], cov[3], 1.0f / e0, 1.0f / e1);
     float gs = 0.0f, gw = 0.0f;
 #pragma unroll
     for(int j = -2; j <= 2; j++)
 #pragma unroll
       for(int i = -2; i <= 2; i++)
       {
-        if(!sgreen[ly + 2 + j][lx + 2 + i]) continue;
+        if(!sgreen[ly + 2 + j][lx + 2 + i]) continue;   // the same in all lanes (one CFA phase per warp)
         const float col = sh[ly + 2 + j][lx + 2 + i];
-        const float of0 = cov[2] * (float)i + cov[3] * (float)j;
-        const float of1 = -cov[3] * (float)i + cov[2] * (float)j;
-        const float w = (i == 0 && j == 0) ? 666.0f
-                      : gclamp(curve_exp(-0.5f * (of0 * ie0 * of0 + of1 * ie1 * of1)), 1e-4f, 1.0f);
+        const float w = (i == 0 && j == 0) ? 666.0f : gclamp(xt_weight(q, i, j), 1e-4f, 1.0f);
         gs += col * w;
         gw += w;
       }
@@ -308,7 +326,8 @@ __global__ void __launch_bounds__(256) k_nd_splat_xt(const dev_nodes_t p)
 // (x+1, y+1) and scaled by the splat green ratio; the centre keeps its green
 __global__ void __launch_bounds__(256) k_nd_fix_xt(const dev_nodes_t p)
 {
-  __shared__ float shl[XT_TY + 6][XT_TX + 6 + 1], sgh[XT_TY + 6][XT_TX + 6 + 1];   // mirrored, halo 3
+  // mirrored, halo 3: hilite output, splat output and 1 / (1e-4 + splat output)
+  __shared__ float shl[XT_TY + 6][XT_TX + 6 + 1], sgh[XT_TY + 6][XT_TX + 6 + 1], srg[XT_TY + 6][XT_TX + 6 + 1];
   __shared__ uint8_t scls[XT_TY + 6][XT_TX + 6];   // 0 red, 1 green, 2 blue of the tap position
   const int X0 = blockIdx.x * XT_TX, Y0 = blockIdx.y * XT_TY;
   for(int i = threadIdx.x; i < (XT_TY + 6) * (XT_TX + 6); i += blockDim.x)
@@ -319,13 +338,15 @@ __global__ void __launch_bounds__(256) k_nd_fix_xt(const dev_nodes_t p)
     const int mx = min(px, p.W + 2), my = min(py, p.H + 2);
     shl[sy][sx] = dn_m(p, p.hl, mx, my);
     sgh[sy][sx] = dn_m(p, p.g, mx, my);
+    srg[sy][sx] = 1.0f / (1e-4f + sgh[sy][sx]);
     // the shader's pattern test at the unwrapped position (truncating divisions)
     const bool blue_top = ((px / 3 + py / 3) & 1) > 0;
     const int qx = px - (px / 3) * 3, qy = py - (py / 3) * 3;
     scls[sy][sx] = ((qx + qy) & 1) == 0 ? 1 : ((blue_top ^ (qy == 1)) ? 2 : 0);
   }
   __syncthreads();
-  const int r = min(max(p.fixup + 2, 2), 3);
+  // radius clamp(fixup + 2, 2, 3) = 2: the host admits fixup 0 only
+  constexpr int r = 2;
   for(int t = threadIdx.x; t < XT_TX * XT_TY; t += blockDim.x)
   {
     int lx, ly;
@@ -336,20 +357,20 @@ __global__ void __launch_bounds__(256) k_nd_fix_xt(const dev_nodes_t p)
     float cov[4];
     cov_z(p, (x + 1) / 3, (y + 1) / 3, cov);
     cov[0] = gclamp(cov[0], 1.0f, 10.0f); cov[1] = gclamp(cov[1], 1.0f, 10.0f);
-    const float ie0 = 1.0f / (3.0f * cov[0]), ie1 = 1.0f / (3.0f * cov[1]);
+    const xt_quad_t q = xt_quad(cov[2], cov[3], 1.0f / (3.0f * cov[0]), 1.0f / (3.0f * cov[1]));
     const float gc4 = 1e-4f + gc;
     float rr = 0.0f, rb = 0.0f, wr = 0.0f, wb = 0.0f;
+#pragma unroll
     for(int j = -r; j <= r; j++)
+#pragma unroll
       for(int i = -r; i <= r; i++)
       {
         const int c = scls[ly + 3 + j][lx + 3 + i];
-        if(c == 1) continue;      // green: the centre's own green is used
-        const float gh = sgh[ly + 3 + j][lx + 3 + i];
+        if(c == 1) continue;      // green: the centre's own green is used (the same in all lanes)
         const float col = shl[ly + 3 + j][lx + 3 + i];
-        const float of0 = cov[2] * (float)i + cov[3] * (float)j;
-        const float of1 = -cov[3] * (float)i + cov[2] * (float)j;
-        const float w = gclamp(curve_exp(-0.5f * (of0 * ie0 * of0 + of1 * ie1 * of1)), 1e-3f, 1.0f);
-        const float v = col * (gc4 / (1e-4f + gh)) * w;
+        const float w = gclamp(xt_weight(q, i, j), 1e-3f, 1.0f);
+        // col (1e-4 + gc) / (1e-4 + gh) w with the reciprocal made once per slot
+        const float v = col * gc4 * srg[ly + 3 + j][lx + 3 + i] * w;
         if(c == 2) { rb += v; wb += w; }
         else       { rr += v; wr += w; }
       }

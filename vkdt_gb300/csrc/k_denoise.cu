@@ -154,18 +154,26 @@ __global__ void __launch_bounds__(256) k_dn_downcov(const dev_denoise_t p)
   eval[1] *= 0.05f;
   eval[0] = gclamp(eval[0], 0.01f, 25.0f); eval[1] = gclamp(eval[1], 0.01f, 25.0f);
   const float ie0 = 1.0f / eval[0], ie1 = 1.0f / eval[1];
-  // anisotropic gaussian over the window, hot pixels (r > 2 mean) left out
+  // anisotropic gaussian over the window, hot pixels (r > 2 mean) left out.
+  // exp(-0.5 (x0^2 / e0 + x1^2 / e1)), x0 = e0 . (i, j), x1 = e1 . (i, j), as the
+  // quadratic form exp2(qa i^2 + qb i j + qc j^2) with coefficients made once
+  // (continuous weights: the products round differently, the weights agree)
+  const float kq = -0.5f * 1.4426950408889634f;
+  const float qa = kq * (e0[0] * e0[0] * ie0 + e1[0] * e1[0] * ie1);
+  const float qb = kq * 2.0f * (e0[0] * e0[1] * ie0 + e1[0] * e1[1] * ie1);
+  const float qc = kq * (e0[1] * e0[1] * ie0 + e1[1] * e1[1] * ie1);
   const float hot = 2.0f * mean_b;
   float r0 = 0.0f, r1 = 0.0f, r2 = 0.0f, wt = 0.0f;
+#pragma unroll
   for(int j = -2; j <= 2; j++)
 #pragma unroll
     for(int i = -2; i <= 2; i++)
     {
       const float pr = sr[ly + 2 + j][lx + 2 + i];
       if(pr > hot) continue;
-      const float x0 = (float)i * e0[0] + (float)j * e0[1];
-      const float x1 = (float)i * e1[0] + (float)j * e1[1];
-      const float ww = fmaxf(1e-9f, __expf(-0.5f * (x0 * ie0 * x0 + x1 * ie1 * x1)));
+      float ex;
+      asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(ex) : "f"(qa * (float)(i * i) + qb * (float)(i * j) + qc * (float)(j * j)));
+      const float ww = fmaxf(1e-9f, ex);
       r0 += ww * pr; r1 += ww * sg[ly + 2 + j][lx + 2 + i]; r2 += ww * sbl[ly + 2 + j][lx + 2 + i];
       wt += ww;
     }

@@ -153,6 +153,7 @@ struct vkdt_cuda_graph_t
   int W = 0, H = 0, out_w = 0, out_h = 0;
   int hw = 0, hh = 0;
   std::vector<level_t> hr, hb;   // hilite reduce outputs r[1..L] (index 0 = r1), assembled B[1..L-1]
+  int hl_tail = 0;               // first hr index the one-CTA tail kernel computes (hr.size(): none)
   std::vector<level_t> lp, la;   // llap planes level 1..nl-1 (index 0 = level 1), assembled A[1..nl-2]
   int nl = 0;
   size_t off_src = 0, off_rgbf = 0, off_out = 0, off_hist = 0, off_dbg0 = 0, off_dbg1 = 0, off_lut = 0, arena_bytes = 0;
@@ -535,7 +536,7 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
     }
     CU(launch_nodes(np, 1, s));
     if((r = mark())) return r;
-    for(size_t l = 0; l < g->hr.size(); l++)
+    for(size_t l = 0; l < g->hr.size() && (int)l < g->hl_tail; l++)
     {
       const half4 *in = l == 0 ? np.h0 : g->at<half4>(g->hr[l - 1].off);
       const int iw = l == 0 ? g->hw : g->hr[l - 1].w, ih = l == 0 ? g->hh : g->hr[l - 1].h;
@@ -556,16 +557,31 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
   CU(launch_hilite_k1(k1, s));
   if((r = mark())) return r;
   // 2. hilite reduce levels 2..L
-  for(size_t l = 1; l < g->hr.size(); l++)
+  for(size_t l = 1; l < g->hr.size() && (int)l < g->hl_tail; l++)
   {
     CU(launch_hilite_reduce(g->at<half4>(g->hr[l - 1].off), g->hr[l - 1].w, g->hr[l - 1].h,
         g->at<half4>(g->hr[l].off), g->hr[l].w, g->hr[l].h, white, desat, wb, s));
     if((r = mark())) return r;
   }
   }
+  if(g->hl_tail < (int)g->hr.size())
+  { // 2'. the small end: reduce levels hl_tail.., assemble B[L-1] .. B[hl_tail] in one CTA
+    dev_hilite_tail_t ht;
+    memset(&ht, 0, sizeof(ht));
+    const int t = g->hl_tail;
+    ht.nr = (int)g->hr.size() - t;
+    for(int l = 0; l <= ht.nr; l++) { ht.lw[l] = g->hr[t - 1 + l].w; ht.lh[l] = g->hr[t - 1 + l].h; }
+    ht.in = g->at<half4>(g->hr[t - 1].off);
+    ht.out = g->at<half4>(g->hb[t].off);
+    ht.white = white; ht.desat = desat; ht.soft = soft;
+    for(int k = 0; k < 3; k++) ht.wb[k] = wb[k];
+    CU(launch_hilite_tail(ht, s));
+    if((r = mark())) return r;
+  }
   // 3. hilite assemble B[L-1] .. B[1]
   for(int l = (int)g->hb.size() - 1; l >= 0; l--)
   {
+    if(l >= g->hl_tail) continue;   // made by the tail
     const level_t &f = g->hr[l];
     const level_t &c = (l + 1 < (int)g->hb.size()) ? g->hb[l + 1] : g->hr[l + 1];
     CU(launch_hilite_assemble(g->at<half4>(f.off), f.w, f.h, g->at<half4>(c.off), c.w, c.h,
@@ -966,6 +982,20 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
       if(rw <= 1 || rh <= 1 || l + 1 == max_nl) break;
     }
     for(size_t l = 0; l + 1 < g->hr.size(); l++) g->hb.push_back(g->hr[l]);
+    // the small end of the pyramid in one CTA (k_hilite_tail): from the first
+    // level of at most HL_TAIL_IN texels whose working set fits its shared
+    // memory, if two or more levels follow (one SM: larger levels take longer
+    // there than their own launches)
+    const int L = (int)g->hr.size();
+    g->hl_tail = L;
+    for(int t = 1; t + 2 <= L; t++)
+    {
+      const int nr = L - t;
+      if(nr >= HL_TAIL_MAX) continue;
+      int lw[HL_TAIL_MAX], lh[HL_TAIL_MAX];
+      for(int l = 0; l <= nr; l++) { lw[l] = g->hr[t - 1 + l].w; lh[l] = g->hr[t - 1 + l].h; }
+      if(lw[0] * lh[0] <= HL_TAIL_IN && hilite_tail_smem_bytes(lw, lh, nr) <= HL_TAIL_SMEM) { g->hl_tail = t; break; }
+    }
   }
   const int OW = g->out_w, OH = g->out_h;
   if(g->halfsize)
@@ -1019,11 +1049,18 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
   int L_rcdc = -1, L_rcdf = -1;
   int L_post, L_k1 = -1;
   const bool k1 = !g->unfused || g->k1front;
+  int L_tail = -1;   // the one-CTA tail computes hr[hl_tail..] and hb[hl_tail..]
+  auto hl_reduce = [&](size_t l) {
+    if((int)l < g->hl_tail) return launch("hilite", "reduce");
+    if(L_tail < 0) L_tail = launch("hilite", "reduce");
+    return L_tail;
+  };
+  auto hl_assemble = [&](size_t l) { return (int)l < g->hl_tail ? launch("hilite", "assemble") : L_tail; };
   if(k1)
   {
     L_k1 = launch("hilite", "reduce");
-    for(size_t l = 1; l < g->hr.size(); l++) L_hr.push_back(launch("hilite", "reduce"));
-    for(size_t l = 0; l < g->hb.size(); l++) L_ha.push_back(launch("hilite", "assemble"));
+    for(size_t l = 1; l < g->hr.size(); l++) L_hr.push_back(hl_reduce(l));
+    for(size_t l = 0; l < g->hb.size(); l++) L_ha.push_back(hl_assemble(l));
   }
   if(!g->unfused) L_post = launch("demosaic", "fix");
   else
@@ -1032,8 +1069,8 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
     {
       if(!g->wavelet) L_noop = launch("denoise", "noop");
       L_half = launch("hilite", "half");
-      for(size_t l = 0; l < g->hr.size(); l++) L_hr.push_back(launch("hilite", "reduce"));
-      for(size_t l = 0; l < g->hb.size(); l++) L_ha.push_back(launch("hilite", "assemble"));
+      for(size_t l = 0; l < g->hr.size(); l++) L_hr.push_back(hl_reduce(l));
+      for(size_t l = 0; l < g->hb.size(); l++) L_ha.push_back(hl_assemble(l));
       L_a0 = launch("hilite", "assemble");
     }
     L_doub = launch("hilite", "doub");

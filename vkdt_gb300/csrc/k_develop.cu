@@ -534,6 +534,7 @@ cudaError_t init_develop()
   // the whole unified L1 as shared memory: 5 CTAs of 43.5 KB per SM
   if(e == cudaSuccess) e = cudaFuncSetAttribute(k_develop, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
   if(e == cudaSuccess) e = init_llap();
+  if(e == cudaSuccess) e = init_hilite();
   return e;
 }
 

@@ -115,7 +115,124 @@ __global__ void __launch_bounds__(256) k_hilite_assemble(const half4 *__restrict
   out[(size_t)y * fw + x] = mk_half4(o[0], o[1], o[2], 1.0f);
 }
 
+// The small end of the pyramid (levels of a few thousand texels and less) in
+// one CTA of 1024 threads: per-level launches there cost more than their work.
+// The same device functions as k_hilite_reduce and k_hilite_assemble on the
+// same f16 values, so the levels are bit identical; they live in shared
+// memory: the reduce terms of the current input level, the reduce outputs
+// R[t..L-1] and the assembled B[t..L-2] (rgba f16 each).
+constexpr int HT_NT = 1024;
+
+// rgba f16 from shared memory (ld_half4 reads through the read-only global path)
+DEV void lds_half4(const half4 *p, float &a, float &b, float &c, float &d)
+{
+  const uint2 u = *reinterpret_cast<const uint2 *>(p);
+  const __half2 lo = *reinterpret_cast<const __half2 *>(&u.x), hi = *reinterpret_cast<const __half2 *>(&u.y);
+  a = __low2float(lo); b = __high2float(lo); c = __low2float(hi); d = __high2float(hi);
+}
+
+__global__ void __launch_bounds__(HT_NT) k_hilite_tail(const dev_hilite_tail_t p)
+{
+  extern __shared__ __align__(16) unsigned char tail_raw[];
+  const int nr = p.nr;
+  const int n0 = p.lw[0] * p.lh[0];
+  float *terms = reinterpret_cast<float *>(tail_raw);          // 5 planes of n0
+  half4 *R[HL_TAIL_MAX], *B[HL_TAIL_MAX];
+  {
+    half4 *q = reinterpret_cast<half4 *>(terms + 5 * ((n0 + 3) & ~3));
+    for(int l = 1; l <= nr; l++) { R[l] = q; q += p.lw[l] * p.lh[l]; }      // R[l]: level t-1+l
+    for(int l = 1; l < nr; l++) { B[l] = q; q += p.lw[l] * p.lh[l]; }       // B[l]: assembled level t-1+l
+  }
+  const hl_reduce_t ra = hilite_reduce_args(p.white, p.desat, p.wb);
+  // terms of the input level
+  for(int i = threadIdx.x; i < n0; i += HT_NT)
+  {
+    float rgb[3], w, t[5];
+    ld_half4(p.in + i, rgb[0], rgb[1], rgb[2], w);
+    hilite_reduce_texel(ra, rgb, t);
+#pragma unroll
+    for(int k = 0; k < 5; k++) terms[k * n0 + i] = t[k];
+  }
+  __syncthreads();
+  for(int l = 1; l <= nr; l++)
+  { // reduce level l - 1 (terms) into R[l]
+    const int iw = p.lw[l - 1], ih = p.lh[l - 1], ow = p.lw[l], oh = p.lh[l], ni = iw * ih;
+    const bool tiny = iw < 3 || ih < 3;
+    for(int o = threadIdx.x; o < ow * oh; o += HT_NT)
+    {
+      const int x = o % ow, y = o / ow;
+      float r[4];
+      hilite_reduce_sum([&](int ii, int jj, float t[5]) {
+          const int sx = tiny ? mirror_full(2 * x + ii, iw) : mirror1c(2 * x + ii, iw);
+          const int sy = tiny ? mirror_full(2 * y + jj, ih) : mirror1c(2 * y + jj, ih);
+#pragma unroll
+          for(int k = 0; k < 5; k++) t[k] = terms[k * ni + sy * iw + sx];
+        }, r);
+      R[l][o] = mk_half4(r[0], r[1], r[2], r[3]);
+    }
+    __syncthreads();
+    if(l < nr)
+    { // the terms of R[l], the next input
+      const int n = ow * oh;
+      for(int i = threadIdx.x; i < n; i += HT_NT)
+      {
+        float rgb[3], w, t[5];
+        lds_half4(R[l] + i, rgb[0], rgb[1], rgb[2], w);
+        hilite_reduce_texel(ra, rgb, t);
+#pragma unroll
+        for(int k = 0; k < 5; k++) terms[k * n + i] = t[k];
+      }
+      __syncthreads();
+    }
+  }
+  for(int l = nr - 1; l >= 1; l--)
+  { // assemble B[l] from the fine R[l] and the coarse B[l + 1] (R[nr] for the coarsest)
+    const half4 *coarse = l + 1 < nr ? B[l + 1] : R[nr];
+    const int fw = p.lw[l], fh = p.lh[l], cw = p.lw[l + 1], ch = p.lh[l + 1];
+    const bool tiny = cw < 2 || ch < 2;
+    half4 *dst = l == 1 ? p.out : B[l];
+    for(int o = threadIdx.x; o < fw * fh; o += HT_NT)
+    {
+      const int x = o % fw, y = o / fw;
+      float up[3];
+      hilite_expand_px([&](int ix, int iy, float rgb[3]) {
+          const int sx = tiny ? mirror_full(ix, cw) : mirror1c(ix, cw), sy = tiny ? mirror_full(iy, ch) : mirror1c(iy, ch);
+          float w;
+          lds_half4(coarse + sy * cw + sx, rgb[0], rgb[1], rgb[2], w);
+        }, x, y, up);
+      float f[4];
+      lds_half4(R[l] + o, f[0], f[1], f[2], f[3]);
+      float ov[3];
+      hilite_assemble_px(f, up, p.white, p.soft, ov);
+      dst[o] = mk_half4(ov[0], ov[1], ov[2], 1.0f);
+    }
+    __syncthreads();
+  }
+}
+
 } // namespace
+
+size_t hilite_tail_smem_bytes(const int *lw, const int *lh, int nr)
+{
+  size_t b = 5 * sizeof(float) * (size_t)((lw[0] * lh[0] + 3) & ~3);
+  for(int l = 1; l <= nr; l++) b += 8 * (size_t)lw[l] * lh[l];
+  for(int l = 1; l < nr; l++) b += 8 * (size_t)lw[l] * lh[l];
+  return b;
+}
+
+cudaError_t init_hilite()
+{
+  return cudaFuncSetAttribute(k_hilite_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)HL_TAIL_SMEM);
+}
+
+cudaError_t launch_hilite_tail(const dev_hilite_tail_t &p, cudaStream_t s)
+{
+  if(p.nr < 2 || p.nr >= HL_TAIL_MAX) return cudaErrorInvalidValue;
+  const size_t smem = hilite_tail_smem_bytes(p.lw, p.lh, p.nr);
+  if(smem > HL_TAIL_SMEM) return cudaErrorInvalidValue;
+  k_hilite_tail<<<1, HT_NT, smem, s>>>(p);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_hilite_k1(const dev_hilite_k1_t &p, cudaStream_t s)
 {

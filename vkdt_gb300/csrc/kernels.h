@@ -184,6 +184,23 @@ int rawhist_max_bins();
 cudaError_t launch_hilite_k1(const dev_hilite_k1_t &p, cudaStream_t s);
 cudaError_t launch_hilite_reduce(const half4 *in, int iw, int ih, half4 *out, int ow, int oh,
     float white, float desat, const float wb[3], cudaStream_t s);
+// the small end of the hilite pyramid in one CTA: reduce levels t..L-1 from
+// level t-1 (in, sizes lw[0] x lh[0]) and assemble B[L-2..t], in shared memory;
+// writes B[t] (out). lw/lh: sizes of levels t-1 .. L-1 (nr + 1 of them)
+constexpr int HL_TAIL_MAX = 16;
+struct dev_hilite_tail_t
+{
+  const half4 *in;
+  half4 *out;
+  int nr;                       // reduce levels in the tail (>= 2)
+  int lw[HL_TAIL_MAX], lh[HL_TAIL_MAX];
+  float white, desat, soft, wb[3];
+};
+size_t hilite_tail_smem_bytes(const int *lw, const int *lh, int nr);
+constexpr size_t HL_TAIL_SMEM = 160 * 1024;   // the largest tail taken (dynamic shared memory)
+constexpr int HL_TAIL_IN = 2048;               // texels of its input level at most (about one per thread)
+cudaError_t launch_hilite_tail(const dev_hilite_tail_t &p, cudaStream_t s);
+cudaError_t init_hilite();    // function attributes, once per device (from init_develop)
 cudaError_t launch_hilite_assemble(const half4 *fine, int fw, int fh, const half4 *coarse, int cw, int ch,
     half4 *out, float white, float soft, cudaStream_t s);
 

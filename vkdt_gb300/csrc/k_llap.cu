@@ -100,18 +100,22 @@ template<int PX, int PY, class F> DEV float2 expand2(F fetch, int kx, int ky)
   return make_float2(r0 / 9.0f, r1 / 9.0f);
 }
 
-// llap/reduce.comp:17-35 (sample_semisoft), all planes of one level. The four
-// half-texel bilinear taps equal ((P00+P10)/4 ...) with the horizontal pair
-// sums P (halving is exact), as in the develop kernel. A CTA makes a 32 x 16
-// tile of outputs: per plane it stages the 66 x 33 input texels once
-// (coalesced 4 byte loads inside the image, mirrored single loads at its
-// border; the taps overshoot the input by at most one texel).
-constexpr int RT_X = 32, RT_Y = 16, RI_X = 2 * RT_X + 2, RI_Y = 2 * RT_Y + 1;
+// llap/reduce.comp:17-35 (sample_semisoft), the planes of one level. The four
+// half-texel bilinear taps are the chain of pair sums scaled once by 1/16, as
+// in llap_reduce_px. A CTA makes a 32 x 16 tile of outputs for a group of
+// RPG planes (blockIdx.z): per plane it stages the 66 x 33 input texels once
+// (asynchronous 4 byte copies inside the image, mirrored single loads at its
+// border; the taps overshoot the input by at most one texel). Two plane
+// groups per tile keep the CTA at 26 KB and 32 registers: 8 CTAs per SM.
+constexpr int RT_X = 32, RT_Y = 16, RI_X = 2 * RT_X + 2, RI_Y = 2 * RT_Y + 1, RPG = (NPL + 1) / 2;
 
-__global__ void __launch_bounds__(256) k_llap_reduce(const __half *__restrict__ in, int iw, int ih, size_t ip,
+__global__ void __launch_bounds__(256, 8) k_llap_reduce(const __half *__restrict__ in, int iw, int ih, size_t ip,
     __half *__restrict__ out, int ow, int oh, size_t op)
 {
-  __shared__ __align__(4) __half t[NPL][RI_Y][RI_X];   // all planes at once: every load in flight together
+  __shared__ __align__(4) __half t[RPG][RI_Y][RI_X];   // the group's planes at once: every load in flight together
+  const int k0 = blockIdx.z * RPG, nk = min(RPG, NPL - k0);
+  in += k0 * ip;
+  out += k0 * op;
   const int OX = blockIdx.x * RT_X, OY = blockIdx.y * RT_Y;
   const int gx0 = 2 * OX - 2, gy0 = 2 * OY - 1;     // input texel of t[.][0][0]
   const bool inside = gx0 >= 0 && gy0 >= 0 && gx0 + RI_X <= iw && gy0 + RI_Y <= ih && !(iw & 1);
@@ -122,11 +126,12 @@ __global__ void __launch_bounds__(256) k_llap_reduce(const __half *__restrict__ 
       const int r = i / (RI_X / 2), c = i % (RI_X / 2);
       const size_t o = (size_t)(gy0 + r) * iw + gx0 + 2 * c;
 #pragma unroll
-      for(int k = 0; k < NPL; k++)
-      {
-        const unsigned dst = (unsigned)__cvta_generic_to_shared(&t[k][r][2 * c]);
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" :: "r"(dst), "l"(in + k * ip + o) : "memory");
-      }
+      for(int k = 0; k < RPG; k++)
+        if(k < nk)
+        {
+          const unsigned dst = (unsigned)__cvta_generic_to_shared(&t[k][r][2 * c]);
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" :: "r"(dst), "l"(in + k * ip + o) : "memory");
+        }
     }
     asm volatile("cp.async.wait_all;\n" ::: "memory");
   }
@@ -136,7 +141,8 @@ __global__ void __launch_bounds__(256) k_llap_reduce(const __half *__restrict__ 
       const int r = i / RI_X, c = i % RI_X;
       const size_t o = (size_t)mirror1(gy0 + r, ih) * iw + mirror1(gx0 + c, iw);
 #pragma unroll
-      for(int k = 0; k < NPL; k++) t[k][r][c] = __ldg(in + k * ip + o);
+      for(int k = 0; k < RPG; k++)
+        if(k < nk) t[k][r][c] = __ldg(in + k * ip + o);
     }
   __syncthreads();
   const int lx = threadIdx.x % RT_X, ly = threadIdx.x / RT_X;
@@ -145,7 +151,7 @@ __global__ void __launch_bounds__(256) k_llap_reduce(const __half *__restrict__ 
   {
     const int oy = OY + ly + 8 * h, ox = OX + lx;
     if(ox >= ow || oy >= oh) continue;
-    for(int k = 0; k < NPL; k++)
+    for(int k = 0; k < nk; k++)
     {
       float P[3][2];
 #pragma unroll
@@ -156,9 +162,8 @@ __global__ void __launch_bounds__(256) k_llap_reduce(const __half *__restrict__ 
         P[b][0] = t0 + t1;
         P[b][1] = t1 + t2;
       }
-      const float q00 = (P[0][0] + P[1][0]) * 0.25f, q10 = (P[0][1] + P[1][1]) * 0.25f;
-      const float q01 = (P[1][0] + P[2][0]) * 0.25f, q11 = (P[1][1] + P[2][1]) * 0.25f;
-      out[k * op + (size_t)oy * ow + ox] = f2h((((q00 + q10) + q01) + q11) * 0.25f);
+      out[k * op + (size_t)oy * ow + ox] =
+          f2h(((((P[0][0] + P[1][0]) + (P[0][1] + P[1][1])) + (P[1][0] + P[2][0])) + (P[1][1] + P[2][1])) * 0.0625f);
     }
   }
 }
@@ -336,7 +341,7 @@ __global__ void __launch_bounds__(256, 6) k_llap_final(const dev_llap_k3_t p)
 } // namespace
 
 cudaError_t init_llap()
-{ // the reduce stages all 11 planes of a tile (47.9 KB): 4 CTAs per SM with the full carveout;
+{ // the reduce stages 6 planes of a tile (26 KB): 8 CTAs per SM with the full carveout;
   // the assemble kernels 36 KB: 6 CTAs per SM
   cudaError_t e = cudaFuncSetAttribute(k_llap_reduce, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
   if(e == cudaSuccess) e = cudaFuncSetAttribute(k_llap_assemble, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
@@ -347,7 +352,7 @@ cudaError_t init_llap()
 cudaError_t launch_llap_reduce(const __half *in, int iw, int ih, size_t iplane,
     __half *out, int ow, int oh, size_t oplane, cudaStream_t s)
 {
-  dim3 grid((ow + RT_X - 1) / RT_X, (oh + RT_Y - 1) / RT_Y);
+  dim3 grid((ow + RT_X - 1) / RT_X, (oh + RT_Y - 1) / RT_Y, (NPL + RPG - 1) / RPG);
   k_llap_reduce<<<grid, 256, 0, s>>>(in, iw, ih, iplane, out, ow, oh, oplane);
   return cudaGetLastError();
 }

@@ -70,6 +70,18 @@ def colenc(rgba, prim, trc):
     return out
 
 
+def grade(rgba, lift=(0, 0, 0, 0), gamma=(1, 1, 1, 0), gain=(1, 1, 1, 0), offset=(0, 0, 0, 0), mode=0,
+          sh_pivot=0.3, hi_pivot=0.4):
+    """grade restated: H x W x 4 float rgba in (the llap output as stored), FP32 rgba out"""
+    rgba = np.ascontiguousarray(rgba, np.float32)
+    ht, wd = rgba.shape[:2]
+    par = np.ascontiguousarray(np.concatenate([lift, gamma, gain, offset]).astype(np.float32))
+    out = np.zeros((ht, wd, 4), np.float32)
+    lib().oracle_grade(rgba.ctypes.data, wd, ht, par.ctypes.data, int(mode), float(sh_pivot), float(hi_pivot),
+                       out.ctypes.data)
+    return out
+
+
 def bc1_encode(rgba):
     """o-bc1 restated: BC1 blocks of an rgba u8 image (H x W x 4), 8 bytes per whole 4x4 block"""
     rgba = np.ascontiguousarray(rgba, np.uint8)
@@ -142,6 +154,7 @@ def lib():
         l.oracle_mcraw_encode.restype = C.c_size_t
         l.oracle_colenc.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
         l.oracle_bc1_encode.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+        l.oracle_grade.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_void_p]
         l.oracle_rcd.argtypes = [C.POINTER(C.c_float), C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
         _lib = l
     return _lib

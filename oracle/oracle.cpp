@@ -1752,6 +1752,56 @@ static void block(const uint8_t *px, uint8_t *out)
 // colenc/main.comp:15-80: rec2020 linear rgb to the output primaries
 // (matrices.h, row major) and transfer curve; out: rgba with alpha 1, as FP32
 // values (the f16 store rounds them; an 8-bit sink rounds them to 1/255)
+// grade/main.comp:23-64: lift / gamma / gain / offset per channel (each with its
+// fourth component added, grade/main.comp:32-35), or in mode != 0 their zoned
+// form weighted by a log luminance. par: lift, gamma, gain, offset (4 each).
+extern "C" void oracle_grade(const float *rgba, int wd, int ht, const float *par, int mode, float sh_pivot,
+    float hi_pivot, float *out)
+{
+  float lift[3], gamma[3], gain[3], off[3];
+  for(int k = 0; k < 3; k++)
+  {
+    lift[k] = par[k] + par[3];
+    gamma[k] = gmax(par[4 + k] + par[7], 1e-6f);
+    gain[k] = gmax(par[8 + k] + par[11], 0.0f);
+    off[k] = par[12 + k] + par[15];
+  }
+  OMP_FOR
+  for(int64_t i = 0; i < (int64_t)wd * ht; i++)
+  {
+    float rgb[3] = { rgba[4 * i + 0], rgba[4 * i + 1], rgba[4 * i + 2] };
+    float ge[3] = { gain[0], gain[1], gain[2] }, le[3] = { lift[0], lift[1], lift[2] };
+    float ye[3] = { gamma[0], gamma[1], gamma[2] };
+    if(mode != 0)
+    { // dot(max(rgb, 0), (0.2126, 0.7152, 0.0722)) summed in order
+      float L = 0.0f;
+      L = L + gmax(rgb[0], 0.0f) * 0.2126f;
+      L = L + gmax(rgb[1], 0.0f) * 0.7152f;
+      L = L + gmax(rgb[2], 0.0f) * 0.0722f;
+      L = gclamp(0.67f + std::log2(gmax(L, 1e-6f)) * 0.11f, 0.0f, 1.0f);
+      const float sp = gclamp(sh_pivot, 1e-3f, 1.0f - 1e-3f);
+      const float hp = gclamp(hi_pivot, sp + 1e-3f, 1.0f);
+      const float ws = 1.0f - smoothstep(0.0f, sp, L);
+      const float wh = smoothstep(hp, 1.0f, L);
+      const float wm = 1.0f - ws - wh;
+      for(int k = 0; k < 3; k++)
+      {
+        ge[k] = gmix(1.0f, gain[k], wh);
+        le[k] = lift[k] * ws;
+        ye[k] = gmix(1.0f, gamma[k], wm);
+      }
+    }
+    for(int k = 0; k < 3; k++)
+    {
+      float v = ge[k] * rgb[k];
+      v = v * (1.0f - le[k]) + le[k];
+      v = std::pow(gmax(v, 0.0f), 1.0f / ye[k]);
+      out[4 * i + k] = v + off[k];
+    }
+    out[4 * i + 3] = 1.0f;
+  }
+}
+
 extern "C" void oracle_colenc(const float *rgba, int wd, int ht, int prim, int trc, float *out)
 {
   static const double Mp[8][9] = {

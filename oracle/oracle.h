@@ -119,6 +119,9 @@ size_t oracle_mcraw_encode(const uint16_t *img, int rwd, int ht, int force_cnt,
     uint8_t *bitcnt, uint16_t *refval, uint8_t *data, size_t cap);
 /* colenc/main.comp: rec2020 rgba (floats) to the output primaries and transfer curve, FP32 out */
 void oracle_colenc(const float *rgba, int wd, int ht, int prim, int trc, float *out);
+// grade/main.comp: rgba (float) in, rgba out; par = lift, gamma, gain, offset (4 floats each)
+void oracle_grade(const float *rgba, int wd, int ht, const float *par, int mode, float sh_pivot, float hi_pivot,
+                  float *out);
 /* o-bc1/main.c:21-47 with its stb_dxt encoder restated: the BC1 blocks (8 bytes each) of
  * the whole 4x4 blocks of an rgba u8 image, row major */
 void oracle_bc1_encode(const uint8_t *rgba, int wd, int ht, uint8_t *out);

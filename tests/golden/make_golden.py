@@ -23,8 +23,8 @@ sys.path.insert(0, os.path.join(ROOT, "tests"))
 import oracle                      # noqa: E402
 import vkdt_gb300 as v             # noqa: E402
 from oracle import glsl_ref        # noqa: E402
-from golden_cases import (CASES, ENCODE_COLENC, MCRAW_BYTES, MCRAW_CASES, NOISE_A, NOISE_B,   # noqa: E402
-                          encode_inputs, img_param, mcraw_stream, oracle_params, path)
+from golden_cases import (CASES, ENCODE_COLENC, GRADE_CASES, MCRAW_BYTES, MCRAW_CASES, NOISE_A,   # noqa: E402
+                          NOISE_B, encode_inputs, grade_input, img_param, mcraw_stream, oracle_params, path)
 
 
 def main():
@@ -80,6 +80,18 @@ def main():
             outs.append(dst.a[..., :3].astype(np.float16))
         np.savez_compressed(path("encode"), bc1=bc1, colenc=np.stack(outs))
         print("%-24s o-bc1 (stb_dxt), colenc" % "encode")
+    if not only or "grade" in only:
+        # grade after llap: its shader on the f16 input, the output as stored (f16)
+        f = grade_input()
+        outs = []
+        for lift, gamma, gain, off, mode, sp, hp in GRADE_CASES:
+            src, dst = glsl_ref.Img(f.shape[1], f.shape[0], 4), glsl_ref.Img(f.shape[1], f.shape[0], 4)
+            src.a[...] = f
+            glsl_ref.run("grade_main", f.shape[1], f.shape[0], {0: src, 1: dst},
+                         uniform=glsl_ref.f32(*lift, *gamma, *gain, *off) + glsl_ref.i32(mode) + glsl_ref.f32(sp, hp))
+            outs.append(dst.a.astype(np.float16))
+        np.savez_compressed(path("grade"), out=np.stack(outs))
+        print("%-24s grade" % "grade")
 
 
 if __name__ == "__main__":

@@ -103,6 +103,27 @@ def load_encode():
     return z["bc1"], z["colenc"]
 
 
+# grade after llap: (lift, gamma, gain, offset, mode, sh_pivot, hi_pivot); the first is the params file's default
+GRADE_CASES = [
+    ((0, 0, 0, 0), (1, 1, 1, 0), (1, 1, 1, 0), (0, 0, 0, 0), 0, 0.3, 0.4),
+    ((0.05, -0.02, 0.1, 0.01), (0.95, 1.05, 1.0, 0.02), (1.1, 0.98, 1.02, -0.03), (-0.01, 0.02, 0.0, 0.005), 0, 0.3, 0.4),
+    ((0.12, 0.0, -0.08, 0.0), (1.08, 0.92, 1.0, 0.0), (0.95, 1.05, 1.1, 0.0), (0.0, -0.02, 0.03, 0.0), 1, 0.3, 0.4),
+    ((-0.1, 0.05, 0.0, 0.02), (1.0, 1.1, 0.9, -0.01), (1.05, 1.0, 0.97, 0.01), (0.02, 0.0, -0.01, 0.0), 1, 0.15, 0.8),
+]
+
+
+def grade_input(seed=5):
+    """the f16 rgba image of the grade fixture (llap outputs as stored: f16, a few below 0 and above 1)"""
+    rng = np.random.default_rng(seed)
+    f = rng.uniform(-0.05, 1.4, (24, 40, 4)).astype(np.float16).astype(np.float32)
+    f[..., 3] = 1.0
+    return f
+
+
+def load_grade():
+    return np.load(path("grade"))["out"]
+
+
 # oracle parameter field -> (module, parameter) of the graph configuration
 PARAM_MAP = {
     "dn_strength": ("denoise", "strength"),

@@ -62,8 +62,9 @@ FULL_CFG = v.DARKROOM_CFG.replace(
 
 
 def test_cfg_with_modules_outside_the_path():
+    # crop (checked for the identity) and grade (applied after llap) are known; the display is not
     g = v.Graph(FULL_CFG)
-    assert sorted(g.unsupported()) == ["crop", "display", "grade"]
+    assert sorted(g.unsupported()) == ["display"]
     g.close()
 
 

@@ -88,6 +88,13 @@ const std::vector<module_def_t> &module_defs()
     { "llap", {                                                   // llap/params:1-4
       { "sigma", 'f', 1, { 0.12f } }, { "shadows", 'f', 1, { 1.0f } }, { "hilights", 'f', 1, { 1.0f } },
       { "clarity", 'f', 1, { 0.0f } } } },
+    { "grade", {                                                  // grade/params:1-7
+      { "lift", 'f', 4, { 0, 0, 0, 0 } }, { "gamma", 'f', 4, { 1, 1, 1, 0 } }, { "gain", 'f', 4, { 1, 1, 1, 0 } },
+      { "offset", 'f', 4, { 0, 0, 0, 0 } }, { "mode", 'i', 1, { 0 } }, { "sh_pivot", 'f', 1, { 0.3f } },
+      { "hi_pivot", 'f', 1, { 0.4f } } } },
+    { "crop", {                                                   // crop/params:1-3 (checked, not applied)
+      { "perspect", 'f', 8, { 0.25f, 0.25f, 0.75f, 0.25f, 0.75f, 0.75f, 0.25f, 0.75f } },
+      { "crop", 'f', 4, { 1, 3, 3, 7 } }, { "rotate", 'f', 1, { 1337 } } } },
   };
   return defs;
 }
@@ -161,6 +168,8 @@ struct vkdt_cuda_graph_t
   int block = 2;                 // CFA block: 2 bayer, 3 x-trans
   bool halfsize = false, resample = false;  // demosaic/halfsize (+ shared/resample) for reduced sizes
   bool rcd = false;              // demosaic method 1 (rcd_conv + rcd_fill) at full size
+  bool grade = false;            // llap -> grade connected: grade/main applied to the llap output
+  bool crop = false;             // demosaic -> crop -> colour connected (only as an identity)
   bool unfused = false;          // x-trans, rcd or reduced size: the per-node chain instead of the fused kernel
   bool k1front = false;          // bayer per-node chain: the fused path's hilite front (k1, pyramid, one kernel to doub)
   std::vector<int64_t> planned_for; // what alloc planned for: a run refuses a graph changed since
@@ -314,6 +323,18 @@ std::vector<int64_t> plan_key(vkdt_cuda_graph_t *g)
 
 int check_supported_params(vkdt_cuda_graph_t *g)
 {
+  if(g->crop)
+  { // crop/main.c:174-275: only the identity passes (no rotation, the whole frame, the untouched
+    // perspective quad); the defaults (rotation 1337 from the exif orientation, the crop 1,3,3,7
+    // margin) and every real crop resample the image, which is not built here
+    const module_t *c = g->mod("crop");
+    if(!c) return fail(VKDT_CUDA_INCOMPLETE, "crop connected but not declared");
+    static const float quad[8] = { 0.25f, 0.25f, 0.75f, 0.25f, 0.75f, 0.75f, 0.25f, 0.75f };
+    bool id = c->f("rotate") == 0.0f && c->f("crop", 0) == 0.0f && c->f("crop", 1) == 1.0f
+           && c->f("crop", 2) == 0.0f && c->f("crop", 3) == 1.0f;
+    for(int k = 0; k < 8; k++) id = id && c->f("perspect", k) == quad[k];
+    if(!id) return fail(VKDT_CUDA_INCOMPLETE, "crop other than the identity (rotate 0, crop 0 1 0 1, the default quad) not built");
+  }
   if(g->mod("demosaic")->n("colour") != 0) return fail(VKDT_CUDA_INCOMPLETE, "demosaic colour (fixup radius) != 0 not supported");
   const int method = g->mod("demosaic")->n("method");
   if(method < 0 || method > 2) return fail(VKDT_CUDA_INCOMPLETE, "demosaic method %d not supported", method);
@@ -661,6 +682,20 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
   }
   // 7. level 0 assemble + llap colour
   dev_llap_k3_t k3;
+  memset(&k3, 0, sizeof(k3));
+  if(g->grade)
+  { // grade/main.comp:32-35: the fourth component is added to each channel
+    const module_t *m = g->mod("grade");
+    k3.grade = m->n("mode") == 0 ? 1 : 2;
+    for(int k = 0; k < 3; k++)
+    {
+      k3.gr_lift[k] = m->f("lift", k) + m->f("lift", 3);
+      k3.gr_gamma[k] = fmaxf(m->f("gamma", k) + m->f("gamma", 3), 1e-6f);
+      k3.gr_gain[k] = fmaxf(m->f("gain", k) + m->f("gain", 3), 0.0f);
+      k3.gr_off[k] = m->f("offset", k) + m->f("offset", 3);
+    }
+    k3.gr_sp = m->f("sh_pivot"); k3.gr_hp = m->f("hi_pivot");
+  }
   k3.rgbf = d.rgbf; k3.W = g->out_w; k3.H = g->out_h;
   k3.l1 = d.l1; k3.l1w = d.l1w; k3.l1h = d.l1h; k3.l1plane = d.l1plane;
   k3.coarse = g->la.empty() ? d.l1 + 10 * d.l1plane : g->at<__half>(g->la[0].off);
@@ -835,6 +870,8 @@ int vkdt_cuda_graph_read_config(vkdt_cuda_graph_t *g, const char *cfg, size_t le
       && (connected("demosaic", "colour") || (connected("demosaic", "crop") && connected("crop", "colour")))
       && connected("colour", "filmcurv") && connected("filmcurv", "llap");
   if(!ok) return fail(VKDT_CUDA_INCOMPLETE, "the cfg does not chain i-raw -> denoise -> hilite -> demosaic -> [crop] -> colour -> filmcurv -> llap");
+  g->crop = !connected("demosaic", "colour");
+  g->grade = g->mod("grade") && connected("llap", "grade");
   g->graph_dirty = true;
   return VKDT_CUDA_SUCCESS;
 }
@@ -1137,6 +1174,7 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
     add_node(g, "llap", "assemble", fw, fh, 1, l == 0 ? L_fin : L_la[l - 1]);
   }
   add_node(g, "llap", "colour", OW, OH, 1, L_fin);
+  if(g->grade) add_node(g, "grade", "main", OW, OH, 1, L_fin);
 
   g->nodes_ready = true;
   return VKDT_CUDA_SUCCESS;

@@ -260,8 +260,44 @@ __global__ void __launch_bounds__(256) k_llap_assemble(const __half *__restrict_
   }
 }
 
+// grade/main.comp:23-64 on the llap output (rounded to f16 as the reference
+// stores it): lift / gamma / gain / offset per channel, or their zoned form
+// weighted by a log luminance; pow and log2 as the accurate functions
+DEV void grade_px(const dev_llap_k3_t &p, float rgb[3])
+{
+  float gain[3], lift[3], gamma[3];
+  for(int k = 0; k < 3; k++) { gain[k] = p.gr_gain[k]; lift[k] = p.gr_lift[k]; gamma[k] = p.gr_gamma[k]; }
+  if(p.grade == 2)
+  {
+    float L = 0.0f;
+    L = L + fmaxf(rgb[0], 0.0f) * 0.2126f;
+    L = L + fmaxf(rgb[1], 0.0f) * 0.7152f;
+    L = L + fmaxf(rgb[2], 0.0f) * 0.0722f;
+    L = gclamp(0.67f + log2f(fmaxf(L, 1e-6f)) * 0.11f, 0.0f, 1.0f);
+    const float sp = gclamp(p.gr_sp, 1e-3f, 1.0f - 1e-3f);
+    const float hp = gclamp(p.gr_hp, sp + 1e-3f, 1.0f);
+    const float ws = 1.0f - smoothstep(0.0f, sp, L);
+    const float wh = smoothstep(hp, 1.0f, L);
+    const float wm = 1.0f - ws - wh;
+    for(int k = 0; k < 3; k++)
+    {
+      gain[k] = gmix(1.0f, gain[k], wh);
+      lift[k] = lift[k] * ws;
+      gamma[k] = gmix(1.0f, gamma[k], wm);
+    }
+  }
+  for(int k = 0; k < 3; k++)
+  {
+    float v = gain[k] * rgb[k];
+    v = v * (1.0f - lift[k]) + lift[k];
+    v = powf(fmaxf(v, 0.0f), 1.0f / gamma[k]);
+    rgb[k] = v + p.gr_off[k];
+  }
+}
+
 // llap/assemble.comp for level 0, the fine planes recomputed from the
 // filmcurv output like llap/curve.comp, fused with llap/colour.comp:141-160
+// (and grade when the graph connects it)
 template<int PX, int PY> DEV half4 final_px(const dev_llap_k3_t &p, const coarse_t &sl, const float rgb[3],
     int lx, int sy, float r2s, float rden)
 {
@@ -274,7 +310,13 @@ template<int PX, int PY> DEV half4 final_px(const dev_llap_k3_t &p, const coarse
     v, sl, lx, sy));
   const float yo = fmaxf(lum2020(rgb[0], rgb[1], rgb[2]), 1e-8f);
   if(yo_ < yo) yo_ = yo * expf(1.0f * (yo_ - yo));
-  return mk_half4(fmaxf(0.0f, rgb[0] * yo_ / yo), fmaxf(0.0f, rgb[1] * yo_ / yo), fmaxf(0.0f, rgb[2] * yo_ / yo), 1.0f);
+  float o[3] = { fmaxf(0.0f, rgb[0] * yo_ / yo), fmaxf(0.0f, rgb[1] * yo_ / yo), fmaxf(0.0f, rgb[2] * yo_ / yo) };
+  if(p.grade)
+  { // grade reads the llap output as stored (f16)
+    for(int k = 0; k < 3; k++) o[k] = f16r(o[k]);
+    grade_px(p, o);
+  }
+  return mk_half4(o[0], o[1], o[2], 1.0f);
 }
 
 DEV void unpack_half4(uint2 u, float rgb[3])

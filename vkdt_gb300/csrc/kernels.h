@@ -76,6 +76,10 @@ struct dev_llap_k3_t
   size_t l1plane;
   const __half *coarse; // A[1] at level 1 size, or the grey plane of level 1 when the pyramid has 2 levels
   float ll_sigma, ll_shadows, ll_highlights, ll_clarity;
+  // grade/main.comp after llap when the graph connects it (0 none, 1 classic, 2 zoned log):
+  // lift, gamma, gain, offset with their fourth component added, sh_pivot, hi_pivot
+  int grade;
+  float gr_lift[3], gr_gamma[3], gr_gain[3], gr_off[3], gr_sp, gr_hp;
   half4 *out;           // rgba f16 W*H
 };
 

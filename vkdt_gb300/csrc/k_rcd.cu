@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(256) k_rcd_conv(const dev_rcd_t p)
 // pixel pairs of four tile rows; the mosaic, vh, pq and lp the tile reads
 // are staged in shared memory first (mirrored or zero filled as the shader
 // reads them).
-template<bool POST> __global__ void __launch_bounds__(256, 4) k_rcd_fill(const dev_rcd_t p, const dev_image_t d)
+template<bool POST> __global__ void __launch_bounds__(256, 5) k_rcd_fill(const dev_rcd_t p, const dev_image_t d)
 {
   __shared__ __half sh[3][RF_PAD + RF_N + RF_PAD];   // shm_r, shm_g, shm_b
   __shared__ uint32_t hist[257];

@@ -2,7 +2,8 @@
 
 Restatement of the reference shaders in C++ (oracle.cpp), loaded with ctypes.
 Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg use it,
-as the checker; the product library never touches it.
+as the reference results are compared against; the product library never
+touches it.
 """
 import ctypes as C
 import os

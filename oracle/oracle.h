@@ -3,13 +3,13 @@
  * (denoise -> hilite -> demosaic -> colour -> filmcurv -> llap).
  *
  * TEST INFRASTRUCTURE ONLY. This is a line-by-line restatement of the
- * reference GLSL compute shaders in plain C++, used as the checker for the
- * CUDA library. Only tests/, __graft_entry__.smoke() and the cpu_baseline leg
+ * reference GLSL compute shaders in plain C++, the reference the tests compare
+ * the CUDA library against. Only tests/, __graft_entry__.smoke() and the cpu_baseline leg
  * of bench.py may load it. The product library never links it.
  *
  * Every node function cites the shader (path within the vkdt project) it
  * restates. The whole file is templated on the arithmetic type so the same
- * code gives the FP32 build (the timed CPU baseline and the parity checker)
+ * code gives the FP32 build (the timed CPU baseline and the parity reference)
  * and the FP64 build (the error reference). f16 storage is emulated at the
  * exact points where the reference stores an image (every node output).
  *

@@ -184,6 +184,30 @@ template<class F> DEV void hilite_expand_px(F fetch, int ox, int oy, float c[3])
   for(int k = 0; k < 3; k++) c[k] /= wgt;
 }
 
+// the same expand for an output of known parity (DX, DY): the taps unrolled,
+// their weights constants, the sums in the same order (bit-identical)
+template<int DX, int DY, class F> DEV void hilite_expand_px_t(F fetch, int ox, int oy, float c[3])
+{
+  c[0] = c[1] = c[2] = 0.0f;
+  float wgt = 0.0f;
+  const int ix = ox / 2, iy = oy / 2;
+  constexpr int i0 = DX ? 0 : -1, j0 = DY ? 0 : -1;
+#pragma unroll
+  for(int ii = i0; ii <= 1; ii++)
+#pragma unroll
+  for(int jj = j0; jj <= 1; jj++)
+  {
+    const float wy = DY ? binom5(2 * jj + 1) : binom5(2 * jj + 2);
+    const float wx = DX ? binom5(2 * ii + 1) : binom5(2 * ii + 2);
+    float rgb[3];
+    fetch(ix + ii, iy + jj, rgb);
+    for(int k = 0; k < 3; k++) c[k] += rgb[k] * wy * wx;
+    wgt += wy * wx;
+  }
+  if(wgt == 0.0f) { c[0] = 0.0f; c[1] = 1.0f; c[2] = 1.0f; return; }
+  for(int k = 0; k < 3; k++) c[k] /= wgt;
+}
+
 // hilite/assemble.comp:88-118 (f: fine rgba, up: expanded coarse rgb)
 DEV void hilite_assemble_px(float f[4], const float up[3], float white, float soft, float o[3])
 {

@@ -95,15 +95,14 @@ __global__ void __launch_bounds__(256) k_hilite_reduce(const half4 *__restrict__
   out[(size_t)y * ow + x] = mk_half4(o[0], o[1], o[2], o[3]);
 }
 
-// hilite/assemble.comp:83-119 on stored levels
-__global__ void __launch_bounds__(256) k_hilite_assemble(const half4 *__restrict__ fine, int fw, int fh,
-    const half4 *__restrict__ coarse, int cw, int ch, half4 *__restrict__ out, float white, float soft)
+// hilite/assemble.comp:83-119 on stored levels: 16x16 outputs per CTA, a
+// warp takes outputs of one (x, y) parity, so its expand taps and weights
+// are fixed (hilite_expand_px_t)
+template<int DX, int DY> DEV void assemble_one(const half4 *__restrict__ fine, int fw, const half4 *__restrict__ coarse,
+    int cw, int ch, bool tiny, int x, int y, half4 *__restrict__ out, float white, float soft)
 {
-  const int x = blockIdx.x * 16 + threadIdx.x % 16, y = blockIdx.y * 16 + threadIdx.x / 16;
-  if(x >= fw || y >= fh) return;
   float up[3];
-  const bool tiny = cw < 2 || ch < 2;     // expand taps overshoot the coarse level by at most 1
-  hilite_expand_px([&](int ix, int iy, float rgb[3]) {
+  hilite_expand_px_t<DX, DY>([&](int ix, int iy, float rgb[3]) {
       const int sx = tiny ? mirror_full(ix, cw) : mirror1c(ix, cw), sy = tiny ? mirror_full(iy, ch) : mirror1c(iy, ch);
       float w;
       ld_half4(coarse + (size_t)sy * cw + sx, rgb[0], rgb[1], rgb[2], w);
@@ -113,6 +112,22 @@ __global__ void __launch_bounds__(256) k_hilite_assemble(const half4 *__restrict
   float o[3];
   hilite_assemble_px(f, up, white, soft, o);
   out[(size_t)y * fw + x] = mk_half4(o[0], o[1], o[2], 1.0f);
+}
+
+__global__ void __launch_bounds__(256) k_hilite_assemble(const half4 *__restrict__ fine, int fw, int fh,
+    const half4 *__restrict__ coarse, int cw, int ch, half4 *__restrict__ out, float white, float soft)
+{
+  const int ph = threadIdx.x >> 6, b = threadIdx.x & 63;      // parity class, position in it
+  const int x = blockIdx.x * 16 + 2 * (b & 7) + (ph & 1), y = blockIdx.y * 16 + 2 * (b >> 3) + (ph >> 1);
+  if(x >= fw || y >= fh) return;
+  const bool tiny = cw < 2 || ch < 2;     // expand taps overshoot the coarse level by at most 1
+  switch(ph)
+  {
+    case 0: assemble_one<0, 0>(fine, fw, coarse, cw, ch, tiny, x, y, out, white, soft); break;
+    case 1: assemble_one<1, 0>(fine, fw, coarse, cw, ch, tiny, x, y, out, white, soft); break;
+    case 2: assemble_one<0, 1>(fine, fw, coarse, cw, ch, tiny, x, y, out, white, soft); break;
+    default: assemble_one<1, 1>(fine, fw, coarse, cw, ch, tiny, x, y, out, white, soft); break;
+  }
 }
 
 // The small end of the pyramid (levels of a few thousand texels and less) in

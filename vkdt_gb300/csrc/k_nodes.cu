@@ -133,12 +133,15 @@ __global__ void __launch_bounds__(256) k_nd_hl_bayer(const dev_nodes_t p)
 {
   const int x = blockIdx.x * 16 + threadIdx.x % 16, y = blockIdx.y * 16 + threadIdx.x / 16;
   if(x >= p.hw || y >= p.hh) return;
+  // the pairs of a block row as one 32 bit word (bayer: even pitch, crop offset and size)
   const uint16_t *row = p.mosaic + (size_t)(2 * y + p.cy) * p.pitch + 2 * x + p.cx;
+  const uint32_t r0 = __ldg(reinterpret_cast<const uint32_t *>(row));
+  const uint32_t r1 = __ldg(reinterpret_cast<const uint32_t *>(row + p.pitch));
   float m[4];
-  m[0] = h2f(__ldg(p.noop_lut + __ldg(row)));
-  m[1] = h2f(__ldg(p.noop_lut + __ldg(row + 1)));
-  m[2] = h2f(__ldg(p.noop_lut + __ldg(row + p.pitch)));
-  m[3] = h2f(__ldg(p.noop_lut + __ldg(row + p.pitch + 1)));
+  m[0] = h2f(__ldg(p.noop_lut + (r0 & 0xffff)));
+  m[1] = h2f(__ldg(p.noop_lut + (r0 >> 16)));
+  m[2] = h2f(__ldg(p.noop_lut + (r1 & 0xffff)));
+  m[3] = h2f(__ldg(p.noop_lut + (r1 >> 16)));
   float o[4] = { m[0], m[1], m[2], m[3] };
   const float white = p.hl_white;
   if(fmaxf(fmaxf(m[2], m[3]), fmaxf(m[1], m[0])) > 0.97f * white)
@@ -156,8 +159,8 @@ __global__ void __launch_bounds__(256) k_nd_hl_bayer(const dev_nodes_t p)
     hilite_doub_bayer(m[0], m[1], m[2], m[3], b0, white, o);
   }
   const size_t o0 = (size_t)(2 * y) * p.W + 2 * x;
-  p.hl[o0] = f2h(o[0]); p.hl[o0 + 1] = f2h(o[1]);
-  p.hl[o0 + p.W] = f2h(o[2]); p.hl[o0 + p.W + 1] = f2h(o[3]);
+  *reinterpret_cast<__half2 *>(p.hl + o0) = __halves2half2(f2h(o[0]), f2h(o[1]));
+  *reinterpret_cast<__half2 *>(p.hl + o0 + p.W) = __halves2half2(f2h(o[2]), f2h(o[3]));
   if(p.dn)
   {
     p.dn[o0] = f2h(m[0]); p.dn[o0 + 1] = f2h(m[1]);

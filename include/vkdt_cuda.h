@@ -317,11 +317,27 @@ int  vkdt_cuda_nprof_fit(const double *hist, int bins, float *a, float *b);
 
 /* debug: copy an intermediate image of the last run to host floats.
  * stage 0 denoise output (1 ch), 1 hilite output (1 ch), both at the crop size;
- * 2 filmcurv output (4 ch) and 3 demosaic output (4 ch, x-trans and reduced
- * sizes only), both at the output size.
+ * 2 filmcurv output, 3 demosaic output and 4 colour output (4 ch each), at
+ * the output size. These are the images the reference's `-d perf` graph
+ * would hold on those nodes' output connectors (graph.c:881-932).
  * requires vkdt_cuda_graph_set_debug(graph, 1) before alloc. */
 int  vkdt_cuda_graph_set_debug(vkdt_cuda_graph_t *graph, int enable);
 int  vkdt_cuda_graph_debug_stage(vkdt_cuda_graph_t *graph, int stage, float *out, size_t count);
+/* debug: the discrete decisions the last run took, one element per texel of
+ * a wd x ht grid (written to *wd, *ht; out may be null to ask for the size).
+ * kind 0: demosaic/gauss.comp per entry (W/block x H/block), u8: bit 0 the
+ *         structure tensor taken was Sw (det(Sw) < det(Sb), gauss.comp:65,117),
+ *         bits 1-2 the snapped direction 0 (1,0), 1 (0,1), 2 none (x-trans
+ *         isotropic; gauss.comp:72-73, 121-123);
+ * kind 1: denoise/cov.glsl response() per half size texel, u32: bits 0-24
+ *         tap (i+2)+5(j+2) skipped as a hot pixel (cov.glsl:130), bit 25 Sw
+ *         taken (cov.glsl:84);
+ * kind 2: denoise/assemble.comp per half size texel, u8: bit l set where the
+ *         coarse threshold switch |d_l| > 10 fired (assemble.comp:144-153).
+ * No reference counterpart: these let a test show that every result that
+ * differs from the reference's arithmetic does so where a branch of the
+ * reference was a near tie. requires debug stages enabled before alloc. */
+int  vkdt_cuda_graph_debug_decisions(vkdt_cuda_graph_t *graph, int kind, void *out, size_t bytes, int *wd, int *ht);
 
 /* ---- synthetic raw scenes (the seeded mosaics the benchmarks are quoted on) */
 

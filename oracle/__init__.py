@@ -124,6 +124,17 @@ class Stages(C.Structure):
     ]
 
 
+class Decisions(C.Structure):
+    _fields_ = [
+        ("gauss", C.c_void_p), ("gauss_force", C.c_void_p), ("gauss_margin", C.c_void_p),
+        ("dn_cov", C.c_void_p), ("dn_cov_force", C.c_void_p), ("dn_cov_margin", C.c_void_p),
+        ("dn_thr", C.c_void_p), ("dn_thr_force", C.c_void_p), ("dn_thr_margin", C.c_void_p),
+    ]
+
+
+# decision kinds: (element type, margins per element)
+DECISION_KINDS = {"gauss": (np.uint8, 2), "dn_cov": (np.uint32, 2), "dn_thr": (np.uint8, 4)}
+
 _lib = None
 
 
@@ -136,6 +147,11 @@ def lib():
         for f in (l.oracle_develop_f32, l.oracle_develop_f64):
             f.restype = C.c_int
             f.argtypes = [C.POINTER(C.c_uint16), C.c_int, C.c_int, C.POINTER(ImgParam), C.POINTER(Params), C.POINTER(Stages)]
+        for f in (l.oracle_develop_dec_f32, l.oracle_develop_dec_f64):
+            f.restype = C.c_int
+            f.argtypes = [C.POINTER(C.c_uint16), C.c_int, C.c_int, C.POINTER(ImgParam), C.POINTER(Params),
+                          C.POINTER(Stages), C.POINTER(Decisions)]
+        l.oracle_gauss_decisions.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_uint32, C.c_void_p, C.c_void_p]
         l.oracle_noop.argtypes = [C.POINTER(C.c_uint16), C.c_int, C.c_int, C.POINTER(ImgParam), C.POINTER(C.c_float)]
         l.oracle_hist.argtypes = [C.POINTER(C.c_float), C.c_int, C.c_int, C.POINTER(C.c_uint32)]
         l.oracle_hist_bin.restype = C.c_uint32
@@ -178,8 +194,13 @@ def _fptr(a):
     return a.ctypes.data_as(C.POINTER(C.c_float))
 
 
-def develop(mosaic, ip, params=None, double=False, stages=("llap",)):
-    """Run the oracle on a u16 mosaic; returns a dict of the requested stage images."""
+def develop(mosaic, ip, params=None, double=False, stages=("llap",), record=False, force=None):
+    """Run the oracle on a u16 mosaic; returns a dict of the requested stage images.
+
+    record: also return the oracle's own discrete decisions and their margins
+    ("dec_<kind>", "margin_<kind>" for the kinds of DECISION_KINDS that the
+    graph has). force: {kind: array} decisions applied in place of the
+    oracle's own (the grids of vkdt_cuda_graph_debug_decisions)."""
     mosaic = np.ascontiguousarray(mosaic, dtype=np.uint16)
     ht, wd = mosaic.shape
     params = params or default_params()
@@ -200,13 +221,47 @@ def develop(mosaic, ip, params=None, double=False, stages=("llap",)):
             st.hist = bufs[name].ctypes.data_as(C.POINTER(C.c_uint32))
         else:
             setattr(st, name, _fptr(bufs[name]))
-    f = lib().oracle_develop_f64 if double else lib().oracle_develop_f32
-    r = f(mosaic.ctypes.data_as(C.POINTER(C.c_uint16)), wd, ht, C.byref(ip), C.byref(params), C.byref(st))
+    if record or force:
+        block = 3 if ip.filters == 9 else 2
+        gw, gh = W // block, H // block
+        dec = Decisions()
+        keep = []
+        if record:
+            for kind, (dt, nm) in DECISION_KINDS.items():
+                bufs["dec_" + kind] = np.zeros((gh, gw), dt)
+                bufs["margin_" + kind] = np.zeros((gh, gw, nm), np.float32)
+                setattr(dec, kind, bufs["dec_" + kind].ctypes.data)
+                setattr(dec, kind + "_margin", bufs["margin_" + kind].ctypes.data)
+        for kind, arr in (force or {}).items():
+            dt = DECISION_KINDS[kind][0]
+            a = np.ascontiguousarray(arr, dt)
+            if a.shape != (gh, gw):
+                raise ValueError("forced %s decisions of shape %s, the grid is %s" % (kind, a.shape, (gh, gw)))
+            keep.append(a)
+            setattr(dec, kind + "_force", a.ctypes.data)
+        f = lib().oracle_develop_dec_f64 if double else lib().oracle_develop_dec_f32
+        r = f(mosaic.ctypes.data_as(C.POINTER(C.c_uint16)), wd, ht, C.byref(ip), C.byref(params), C.byref(st),
+              C.byref(dec))
+    else:
+        f = lib().oracle_develop_f64 if double else lib().oracle_develop_f32
+        r = f(mosaic.ctypes.data_as(C.POINTER(C.c_uint16)), wd, ht, C.byref(ip), C.byref(params), C.byref(st))
     if r != 0:
         raise RuntimeError("oracle develop failed with %d" % r)
     bufs["llap_levels"] = st.llap_levels
     bufs["hilite_levels"] = st.hilite_levels
     return bufs
+
+
+def gauss_decisions(mosaic, filters):
+    """demosaic/gauss.comp's decisions on a given mosaic (H x W floats, the hilite
+    output) and their margins: (H/block x W/block u8, ... x 2 f32)."""
+    mosaic = np.ascontiguousarray(mosaic, np.float32)
+    ht, wd = mosaic.shape
+    block = 3 if filters == 9 else 2
+    dec = np.zeros((ht // block, wd // block), np.uint8)
+    mar = np.zeros((ht // block, wd // block, 2), np.float32)
+    lib().oracle_gauss_decisions(mosaic.ctypes.data, wd, ht, filters, dec.ctypes.data, mar.ctypes.data)
+    return dec, mar
 
 
 def rcd(cfa, wb):

@@ -198,6 +198,16 @@ template<class T> static inline void m3_apply(const m3<T> &A, const T v[3], T o[
   o[0] = r[0]; o[1] = r[1]; o[2] = r[2];
 }
 
+// ------------------------------------------------------------------ decisions
+// the decision record/force context of the current develop call (one at a time)
+static oracle_decisions_t *g_dec = nullptr;
+
+template<class T> static inline float rel_gap(T a, T b)
+{
+  const T m = gmax(std::fabs(a), std::fabs(b));
+  return m > T(0) ? (float)(std::fabs(a - b) / m) : 0.0f;
+}
+
 // ------------------------------------------------------------------ denoise
 
 // denoise/noop.comp:36-57 (gain map absent on the synthetic input)
@@ -260,7 +270,7 @@ template<class T> static img_t<T> denoise_half(const img_t<T> &in, int wd, int h
 }
 
 // denoise/cov.glsl:159-276 response(). p in texel coordinates of img.
-template<class T> static void denoise_response(const img_t<T> &img, int px_, int py_, T res_out[3], T cov[4])
+template<class T> static void denoise_response(const img_t<T> &img, int px_, int py_, T res_out[3], T cov[4], size_t idx)
 {
   T mw[2] = {0, 0}, mb[2] = {0, 0}, smw = 0, smb = 0, mean_b = 0;
   T Sw00 = 0, Sw01 = 0, Sw10 = 0, Sw11 = 0, Sb00 = 0, Sb01 = 0, Sb10 = 0, Sb11 = 0, sw = 0, sb = 0;
@@ -292,7 +302,19 @@ template<class T> static void denoise_response(const img_t<T> &img, int px_, int
   Sw00 /= sw; Sw01 /= sw; Sw10 /= sw; Sw11 /= sw;
   Sb00 /= sb; Sb01 /= sb; Sb10 /= sb; Sb11 /= sb;
   const T detw = Sw00 * Sw11 - Sw10 * Sw01, detb = Sb00 * Sb11 - Sb10 * Sb01;
-  const bool usew = detw < detb;
+  bool usew = detw < detb;
+  // the hot pixel skips this texel takes (decision record, oracle_decisions_t)
+  uint32_t skip = 0;
+  float hot_gap = 1e30f;
+  for(int j = -2; j <= 2; j++) for(int i = -2; i <= 2; i++)
+  {
+    const T pr = fetch_m(img, px_ + i, py_ + j, 0);
+    if(pr > T(2) * mean_b) skip |= 1u << ((i + 2) + 5 * (j + 2));
+    hot_gap = std::min(hot_gap, rel_gap(pr, T(2) * mean_b));
+  }
+  if(g_dec && g_dec->dn_cov) g_dec->dn_cov[idx] = skip | (usew ? 1u << 25 : 0u);
+  if(g_dec && g_dec->dn_cov_margin) { g_dec->dn_cov_margin[2 * idx] = rel_gap(detw, detb); g_dec->dn_cov_margin[2 * idx + 1] = hot_gap; }
+  if(g_dec && g_dec->dn_cov_force) { usew = (g_dec->dn_cov_force[idx] >> 25) & 1; skip = g_dec->dn_cov_force[idx] & 0x1ffffffu; }
   T eval[2], evec0[2], evec1[2];
   if(usew) evd2x2(eval, evec0, evec1, Sw00, Sw10, Sw11);
   else     evd2x2(eval, evec0, evec1, Sb00, Sb10, Sb11);
@@ -303,7 +325,7 @@ template<class T> static void denoise_response(const img_t<T> &img, int px_, int
   for(int j = -2; j <= 2; j++) for(int i = -2; i <= 2; i++)
   {
     const T pr = fetch_m(img, px_ + i, py_ + j, 0), pg = fetch_m(img, px_ + i, py_ + j, 1), pb = fetch_m(img, px_ + i, py_ + j, 2);
-    if(pr > T(2) * mean_b) continue;
+    if((skip >> ((i + 2) + 5 * (j + 2))) & 1) continue;   // pr > 2 mean_b (or the forced skip)
     const T x0 = T(i) * evec0[0] + T(j) * evec0[1];
     const T x1 = T(i) * evec1[0] + T(j) * evec1[1];
     const T ww = gmax(T(1e-9), std::exp(T(-0.5) * (x0 / eval[0] * x0 + x1 / eval[1] * x1)));
@@ -328,7 +350,7 @@ template<class T> static img_t<T> denoise_downcov(const img_t<T> &in, int wd, in
   for(int y = 0; y < ht; y++) for(int x = 0; x < wd; x++)
   {
     T rgb[3], cov[4];
-    denoise_response(in, x + crop[0], y + crop[1], rgb, cov);
+    denoise_response(in, x + crop[0], y + crop[1], rgb, cov, (size_t)y * wd + x);
     T edge = gclamp(T(75) * gmax(T(0), cov[1] - T(0.09)), T(0), T(1));
     edge = smoothstep(T(0.4), T(0.75), edge);
     edge = gclamp(T(0.02) + edge, T(0), T(1));
@@ -424,9 +446,18 @@ template<class T> static img_t<T> denoise_assemble(const img_t<T> *s, int wd, in
     test = gclamp(T(1.5) * test, T(0), T(1));
     const T thrs0 = std::pow(strength, T(4));
     const T ht_ = T(10);
+    const size_t idx = (size_t)y * wd + x;
+    uint32_t sw = 0;
+    for(int l = 0; l < 4; l++)
+    {
+      if(std::fabs(d[l][0]) > ht_) sw |= 1u << l;
+      if(g_dec && g_dec->dn_thr_margin) g_dec->dn_thr_margin[4 * idx + l] = rel_gap(std::fabs(d[l][0]), ht_);
+    }
+    if(g_dec && g_dec->dn_thr) g_dec->dn_thr[idx] = (uint8_t)sw;
+    if(g_dec && g_dec->dn_thr_force) sw = g_dec->dn_thr_force[idx];
     for(int l = 3; l >= 0; l--)
     {
-      const T thrs = (std::fabs(d[l][0]) > ht_) ? T(10000) : thrs0;
+      const T thrs = ((sw >> l) & 1) ? T(10000) : thrs0;
       for(int k = 0; k < 3; k++)
       {
         const T a = std::fabs(d[l][k]);
@@ -757,20 +788,49 @@ template<class T> static img_t<T> demosaic_gauss(const img_t<T> &orig, int wd, i
     Sw00 /= sw; Sw01 /= sw; Sw10 /= sw; Sw11 /= sw;
     Sb00 /= sb; Sb01 /= sb; Sb10 /= sb; Sb11 /= sb;
     const T detw = Sw00 * Sw11 - Sw10 * Sw01, detb = Sb00 * Sb11 - Sb10 * Sb01;
+    // the form and the snapped direction (own decision, recorded with its margins;
+    // a forced decision replaces both)
+    auto snap_of = [&](const T e[2], float *gap) {
+      const T ax = std::fabs(e[0]), ay = std::fabs(e[1]);
+      if(filters != 9)
+      {
+        if(gap) *gap = (float)std::fabs(ax - ay);
+        return ax > ay ? 0 : 1;
+      }
+      if(gap) *gap = (float)std::min(std::fabs(ax - T(2) * ay), std::fabs(ay - T(2) * ax));
+      return ax > T(2) * ay ? 0 : (ay > T(2) * ax ? 1 : 2);
+    };
+    bool usew = detw < detb;
     T eval[2], evec0[2], evec1[2];
-    if(detw < detb) evd2x2(eval, evec0, evec1, Sw00, Sw10, Sw11);
-    else            evd2x2(eval, evec0, evec1, Sb00, Sb10, Sb11);
+    if(usew) evd2x2(eval, evec0, evec1, Sw00, Sw10, Sw11);
+    else     evd2x2(eval, evec0, evec1, Sb00, Sb10, Sb11);
+    float snap_gap;
+    int snap = snap_of(evec0, &snap_gap);
+    const size_t idx = (size_t)y * wd + x;
+    if(g_dec && g_dec->gauss) g_dec->gauss[idx] = (uint8_t)((usew ? 1 : 0) | (snap << 1));
+    if(g_dec && g_dec->gauss_margin) { g_dec->gauss_margin[2 * idx] = rel_gap(detw, detb); g_dec->gauss_margin[2 * idx + 1] = snap_gap; }
+    if(g_dec && g_dec->gauss_force)
+    {
+      const bool fw = g_dec->gauss_force[idx] & 1;
+      if(fw != usew)
+      {
+        usew = fw;
+        if(usew) evd2x2(eval, evec0, evec1, Sw00, Sw10, Sw11);
+        else     evd2x2(eval, evec0, evec1, Sb00, Sb10, Sb11);
+      }
+      snap = (g_dec->gauss_force[idx] >> 1) & 3;
+    }
     if(filters != 9)
     {
       eval[0] *= T(0.2); eval[1] *= T(0.2);
-      if(std::fabs(evec0[0]) > std::fabs(evec0[1])) { evec0[0] = 1; evec0[1] = 0; }
-      else                                          { evec0[0] = 0; evec0[1] = 1; }
+      if(snap == 0) { evec0[0] = 1; evec0[1] = 0; }
+      else          { evec0[0] = 0; evec0[1] = 1; }
     }
     else
     {
       eval[0] *= T(0.4); eval[1] *= T(0.4);
-      if(std::fabs(evec0[0]) > T(2) * std::fabs(evec0[1]))      { evec0[0] = 1; evec0[1] = 0; }
-      else if(std::fabs(evec0[1]) > T(2) * std::fabs(evec0[0])) { evec0[0] = 0; evec0[1] = 1; }
+      if(snap == 0)      { evec0[0] = 1; evec0[1] = 0; }
+      else if(snap == 1) { evec0[0] = 0; evec0[1] = 1; }
       else { eval[0] = T(0.1); eval[1] = T(0.1); }
     }
     const T v[4] = { eval[0], eval[1], evec0[0], evec0[1] };
@@ -2237,6 +2297,37 @@ int oracle_develop_f32(const uint16_t *mosaic, int wd, int ht,
 int oracle_develop_f64(const uint16_t *mosaic, int wd, int ht,
     const oracle_img_param_t *ip, const oracle_params_t *p, oracle_stages_t *out)
 { return develop<double>(mosaic, wd, ht, ip, p, out); }
+
+int oracle_develop_dec_f32(const uint16_t *mosaic, int wd, int ht,
+    const oracle_img_param_t *ip, const oracle_params_t *p, oracle_stages_t *out, oracle_decisions_t *dec)
+{
+  g_dec = dec;
+  const int r = develop<float>(mosaic, wd, ht, ip, p, out);
+  g_dec = nullptr;
+  return r;
+}
+
+int oracle_develop_dec_f64(const uint16_t *mosaic, int wd, int ht,
+    const oracle_img_param_t *ip, const oracle_params_t *p, oracle_stages_t *out, oracle_decisions_t *dec)
+{
+  g_dec = dec;
+  const int r = develop<double>(mosaic, wd, ht, ip, p, out);
+  g_dec = nullptr;
+  return r;
+}
+
+void oracle_gauss_decisions(const float *mosaic, int wd, int ht, uint32_t filters, uint8_t *dec, float *margin)
+{ // demosaic/gauss.comp on a given (hilite output) mosaic, the decisions only
+  img_t<float> in(wd, ht, 1);
+  for(size_t i = 0; i < (size_t)wd * ht; i++) in.d[i] = mosaic[i];
+  oracle_decisions_t d;
+  memset(&d, 0, sizeof(d));
+  d.gauss = dec; d.gauss_margin = margin;
+  g_dec = &d;
+  const int block = filters == 9u ? 3 : 2;
+  demosaic_gauss(in, wd / block, ht / block, filters);
+  g_dec = nullptr;
+}
 
 void oracle_noop(const uint16_t *mosaic, int wd, int ht, const oracle_img_param_t *ip, float *out)
 {

@@ -82,6 +82,35 @@ typedef struct oracle_stages_t
 }
 oracle_stages_t;
 
+/* The discrete decisions of the path, recorded and optionally forced. A test
+ * reads the decisions the CUDA path took (vkdt_cuda_graph_debug_decisions),
+ * compares them with the oracle's own (recorded here with their margins) and
+ * reruns the oracle with the CUDA path's decisions forced, so that every
+ * output pixel can be held to the continuous tolerance. Any pointer may be 0.
+ * Grids: gauss W/block x H/block, denoise W/block x H/block (the half image). */
+typedef struct oracle_decisions_t
+{
+  /* demosaic/gauss.comp per entry: bit 0 det(Sw) < det(Sb) (gauss.comp:65,117);
+   * bits 1-2 the snapped direction 0 (1,0), 1 (0,1), 2 none (gauss.comp:72-73,121-123) */
+  uint8_t       *gauss;         /* written: the oracle's own decisions */
+  const uint8_t *gauss_force;   /* read: decisions applied in place of its own */
+  float         *gauss_margin;  /* written, 2 per entry: |detw-detb|/max(|detw|,|detb|), the snap gap */
+  /* denoise/cov.glsl response() per half texel: bits 0-24 hot pixel skip of tap
+   * (i+2)+5(j+2) (cov.glsl:130), bit 25 det(Sw) < det(Sb) (cov.glsl:84) */
+  uint32_t       *dn_cov;
+  const uint32_t *dn_cov_force;
+  float          *dn_cov_margin; /* 2 per texel: the det gap, min over taps of |r - 2 mean| / (2 mean) */
+  /* denoise/assemble.comp per half texel: bit l where |d_l| > 10 (assemble.comp:144-153) */
+  uint8_t       *dn_thr;
+  const uint8_t *dn_thr_force;
+  float         *dn_thr_margin;  /* 4 per texel: | |d_l| - 10 | / 10 */
+}
+oracle_decisions_t;
+
+/* demosaic/gauss.comp's decisions (and margins, 2 per entry) on a given mosaic
+ * (W x H floats, the hilite output): the grid of oracle_decisions_t.gauss */
+void oracle_gauss_decisions(const float *mosaic, int wd, int ht, uint32_t filters, uint8_t *dec, float *margin);
+
 /* the default parameters of the six modules plus the darkroom .cfg values
  * (bin/default-darkroom.i-raw:28-32) */
 void oracle_default_params(oracle_params_t *p);
@@ -91,6 +120,11 @@ int oracle_develop_f32(const uint16_t *mosaic, int wd, int ht,
     const oracle_img_param_t *ip, const oracle_params_t *p, oracle_stages_t *out);
 int oracle_develop_f64(const uint16_t *mosaic, int wd, int ht,
     const oracle_img_param_t *ip, const oracle_params_t *p, oracle_stages_t *out);
+/* the same with the decisions recorded / forced (dec may be 0). One call at a time. */
+int oracle_develop_dec_f32(const uint16_t *mosaic, int wd, int ht,
+    const oracle_img_param_t *ip, const oracle_params_t *p, oracle_stages_t *out, oracle_decisions_t *dec);
+int oracle_develop_dec_f64(const uint16_t *mosaic, int wd, int ht,
+    const oracle_img_param_t *ip, const oracle_params_t *p, oracle_stages_t *out, oracle_decisions_t *dec);
 
 /* single-node entry points for unit tests */
 /* denoise/noop.comp on the whole mosaic -> W*H normalised f16 values */

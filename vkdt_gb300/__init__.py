@@ -309,15 +309,29 @@ class Graph:
         return np.array(h[:], dtype=np.uint32)
 
     def debug_stage(self, stage):
-        """0 denoise, 1 hilite (crop size, one channel); 2 filmcurv, 3 demosaic
-        (output size, rgba; 3 only on the per-node chain)."""
-        if stage in (2, 3):
+        """0 denoise, 1 hilite (crop size, one channel); 2 filmcurv, 3 demosaic,
+        4 colour (output size, rgba)."""
+        if stage in (2, 3, 4):
             out = np.empty((self.out_ht, self.out_wd, 4), np.float32)
         else:
             out = np.empty((self.crop_ht, self.crop_wd, 1), np.float32)
         check(self._l.vkdt_cuda_graph_debug_stage(self._g, stage, out.ctypes.data_as(C.POINTER(C.c_float)), out.size),
               "debug_stage")
-        return out if stage in (2, 3) else out[..., 0]
+        return out if stage in (2, 3, 4) else out[..., 0]
+
+    DECISIONS = {"gauss": (0, np.uint8), "dn_cov": (1, np.uint32), "dn_thr": (2, np.uint8)}
+
+    def debug_decisions(self, kind):
+        """The discrete decisions of the last run (vkdt_cuda_graph_debug_decisions):
+        'gauss' (demosaic/gauss entries), 'dn_cov' and 'dn_thr' (wavelet denoise,
+        half size texels), as an (ht, wd) array."""
+        k, dt = self.DECISIONS[kind]
+        w, h = C.c_int(), C.c_int()
+        check(self._l.vkdt_cuda_graph_debug_decisions(self._g, k, None, 0, C.byref(w), C.byref(h)), "debug_decisions")
+        out = np.zeros((h.value, w.value), dt)
+        check(self._l.vkdt_cuda_graph_debug_decisions(self._g, k, out.ctypes.data, out.nbytes, None, None),
+              "debug_decisions")
+        return out
 
 
 class Server:

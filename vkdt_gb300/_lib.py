@@ -141,6 +141,7 @@ _SIGS = {
     "vkdt_cuda_hist_rgba_f16": (C.c_int, [_P, C.c_int, C.c_int, _P, _P]),
     "vkdt_cuda_graph_set_debug": (C.c_int, [_P, C.c_int]),
     "vkdt_cuda_graph_debug_stage": (C.c_int, [_P, C.c_int, C.POINTER(C.c_float), C.c_size_t]),
+    "vkdt_cuda_graph_debug_decisions": (C.c_int, [_P, C.c_int, _P, C.c_size_t, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "vkdt_cuda_scene_generate": (C.c_int, [C.POINTER(Scene), _P, _P]),
     "vkdt_cuda_scene_generate_host": (C.c_int, [C.POINTER(Scene), C.POINTER(C.c_uint16)]),
     "vkdt_cuda_last_error": (C.c_char_p, []),

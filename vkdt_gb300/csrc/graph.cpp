@@ -27,6 +27,17 @@ namespace {
 thread_local char g_err[512] = "";
 int g_device = -1;
 
+// the address of the static develop scratch per device (vkdt_cuda_graph_develop_static),
+// looked up once per device; forgotten at vkdt_cuda_cleanup, after which a reloaded
+// module may place the array elsewhere
+std::mutex g_static_lock;
+void *g_static_base[64] = { nullptr };
+void forget_static_scratch()
+{
+  std::lock_guard<std::mutex> guard(g_static_lock);
+  for(auto &p : g_static_base) p = nullptr;
+}
+
 int fail(int code, const char *fmt, ...) __attribute__((format(printf, 2, 3)));
 int fail(int code, const char *fmt, ...)
 {
@@ -173,10 +184,13 @@ struct vkdt_cuda_graph_t
   bool unfused = false;          // x-trans, rcd or reduced size: the per-node chain instead of the fused kernel
   bool k1front = false;          // bayer per-node chain: the fused path's hilite front (k1, pyramid, one kernel to doub)
   std::vector<int64_t> planned_for; // what alloc planned for: a run refuses a graph changed since
+  std::vector<int64_t> nodes_for;   // what create_nodes planned for (the static develop checks it)
   float lut_black = -1.0f, lut_white = -1.0f;  // black/white (DN) the noop code table holds
   size_t off_h0 = 0, off_b0 = 0, off_hl = 0, off_cov = 0, off_g = 0, off_hs = 0, off_dm = 0;
   size_t off_vh = 0, off_pq = 0, off_lpf = 0;
   size_t off_dnh = 0, off_dnl[4] = { 0, 0, 0, 0 }, off_dna = 0, off_dn = 0, off_idlut = 0;
+  // debug stages: demosaic (fused path) and colour outputs, the decisions of gauss and the wavelet denoise
+  size_t off_dbg_dm = 0, off_dbg_col = 0, off_dbg_gauss = 0, off_dbg_cov = 0, off_dbg_thr = 0;
   unsigned char *arena = nullptr;
   void *h_src = nullptr, *h_sink = nullptr;
   size_t src_bytes = 0, sink_bytes = 0;
@@ -380,7 +394,12 @@ int fill_image(vkdt_cuda_graph_t *g, dev_image_t &d, const void *d_src, void *d_
   d.l1w = g->lp[0].w; d.l1h = g->lp[0].h;
   d.l1plane = (size_t)g->lp[0].w * g->lp[0].h;
   d.hist = g->want_hist ? g->at<uint32_t>(g->off_hist) : nullptr;
-  if(g->debug) { d.dbg_denoise = g->at<__half>(g->off_dbg0); d.dbg_hilite = g->at<__half>(g->off_dbg1); }
+  if(g->debug)
+  {
+    d.dbg_denoise = g->at<__half>(g->off_dbg0); d.dbg_hilite = g->at<__half>(g->off_dbg1);
+    d.dbg_demosaic = g->at<half4>(g->off_dbg_dm); d.dbg_colour = g->at<half4>(g->off_dbg_col);
+    d.dbg_gauss = g->at<uint8_t>(g->off_dbg_gauss);
+  }
   (void)d_out;
   return 0;
 }
@@ -401,7 +420,13 @@ size_t plan_arena(vkdt_cuda_graph_t *g)
   g->off_out = take(g->sink_bytes);
   g->off_hist = take(257 * 4);
   g->off_lut = take(65536 * 2);
-  if(g->debug) { g->off_dbg0 = take((size_t)g->W * g->H * 2); g->off_dbg1 = take((size_t)g->W * g->H * 2); }
+  if(g->debug)
+  {
+    g->off_dbg0 = take((size_t)g->W * g->H * 2); g->off_dbg1 = take((size_t)g->W * g->H * 2);
+    g->off_dbg_dm = take((size_t)g->out_w * g->out_h * 8); g->off_dbg_col = take((size_t)g->out_w * g->out_h * 8);
+    g->off_dbg_gauss = take((size_t)g->hw * g->hh);
+    if(g->wavelet) { g->off_dbg_cov = take((size_t)g->hw * g->hh * 4); g->off_dbg_thr = take((size_t)g->hw * g->hh); }
+  }
   const size_t hbytes = (size_t)g->hw * g->hh * 8;
   if(g->wavelet)
   { // the half size nodes of the wavelet denoise
@@ -472,6 +497,7 @@ void fill_denoise(vkdt_cuda_graph_t *g, dev_denoise_t &p, const void *d_src)
   for(int i = 0; i < 4; i++) p.lvl[i] = g->at<half4>(g->off_dnl[i]);
   p.asm_img = g->at<half4>(g->off_dna);
   p.dn = g->at<__half>(g->off_dn);
+  if(g->debug) { p.dbg_cov = g->at<uint32_t>(g->off_dbg_cov); p.dbg_thr = g->at<uint8_t>(g->off_dbg_thr); }
 }
 
 // buffers and sizes of the per-node chain (x-trans, reduced output sizes)
@@ -498,6 +524,7 @@ void fill_nodes(vkdt_cuda_graph_t *g, dev_nodes_t &p, const void *d_src)
   const level_t &c = g->hb.empty() ? g->hr[0] : g->hb[0];
   p.coarse = g->at<half4>(c.off); p.ccw = c.w; p.cch = c.h;
   p.hl_soft = g->mod("hilite")->f("soft");
+  if(g->debug) p.dbg_gauss = g->at<uint8_t>(g->off_dbg_gauss);
   // the bayer front writes the noop output only for the debug stage (the wavelet writes its own)
   if(g->k1front && (g->wavelet || !g->debug)) p.dn = nullptr;
 }
@@ -738,7 +765,11 @@ int vkdt_cuda_init(int device_id, uint32_t flags)
   return VKDT_CUDA_SUCCESS;
 }
 
-void vkdt_cuda_cleanup(void) { g_device = -1; }
+void vkdt_cuda_cleanup(void)
+{
+  g_device = -1;
+  forget_static_scratch();
+}
 
 int vkdt_cuda_supports(dt_token_t name, dt_token_t kernel)
 {
@@ -1177,6 +1208,7 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
   if(g->grade) add_node(g, "grade", "main", OW, OH, 1, L_fin);
 
   g->nodes_ready = true;
+  g->nodes_for = plan_key(g);
   return VKDT_CUDA_SUCCESS;
 }
 
@@ -1345,8 +1377,6 @@ int vkdt_cuda_graph_develop(vkdt_cuda_graph_t *g, const void *d_mosaic, void *d_
 // same kernel sequence on a fixed scratch array instead of the graph's arena.
 int vkdt_cuda_graph_develop_static(vkdt_cuda_graph_t *g, const void *d_mosaic, void *d_rgba, void *stream)
 {
-  static std::mutex lock;                 // guards the per-device address table only
-  static void *scratch[64] = { nullptr };  // scratch address per device, looked up once
   if(!g) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "null graph");
   if(g_device < 0) return fail(VKDT_CUDA_ERROR_INITIALIZATION_FAILED, "vkdt_cuda_init was not called");
   if(g->allocated) return fail(VKDT_CUDA_INCOMPLETE, "graph owns device buffers: use vkdt_cuda_graph_develop");
@@ -1355,9 +1385,9 @@ int vkdt_cuda_graph_develop_static(vkdt_cuda_graph_t *g, const void *d_mosaic, v
     return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED,
                 "debug stages, timing, the histogram, the wavelet denoise, x-trans and reduced sizes need an allocated graph");
   if(!d_mosaic || !d_rgba) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "null device buffer");
-  const uint32_t *b = g->ip.crop_aabb;
-  if(g->W != (int)(b[2] - b[0]) || g->H != (int)(b[3] - b[1]))
-    return fail(VKDT_CUDA_INCOMPLETE, "input changed since vkdt_cuda_graph_create_nodes");
+  // a graph changed since create_nodes (size, crop, CFA, output size, denoise, demosaic, depth)
+  // would run a stale plan on buffers the caller sized for the new one
+  if(plan_key(g) != g->nodes_for) return fail(VKDT_CUDA_INCOMPLETE, "graph changed since vkdt_cuda_graph_create_nodes");
   // the arena plan of vkdt_cuda_graph_alloc without the caller's source, sink and debug buffers
   size_t off = 0;
   auto take = [&](size_t bytes) { const size_t o = off; off = align_up(off + bytes); return o; };
@@ -1377,24 +1407,29 @@ int vkdt_cuda_graph_develop_static(vkdt_cuda_graph_t *g, const void *d_mosaic, v
   if(dev < 0 || dev >= 64) return fail(VKDT_CUDA_ERROR_INITIALIZATION_FAILED, "device %d out of range", dev);
   unsigned char *base = nullptr;
   {
-    std::lock_guard<std::mutex> guard(lock);
-    if(!scratch[dev])
+    std::lock_guard<std::mutex> guard(g_static_lock);
+    if(!g_static_base[dev])
     {
       void *p = nullptr;
       const cudaError_t e = static_scratch_address(&p);
       if(e != cudaSuccess || !p)
         return fail(e != cudaSuccess ? cuda_code(e) : VKDT_CUDA_ERROR_INITIALIZATION_FAILED,
                     "no address for the static scratch on device %d: %s", dev, cudaGetErrorString(e));
-      scratch[dev] = p;
+      g_static_base[dev] = p;
     }
-    base = (unsigned char *)scratch[dev];
+    base = (unsigned char *)g_static_base[dev];
   }
   cudaStream_t s = (cudaStream_t)stream;
   CU(cudaMemsetAsync(base, 0, off, s));
   CU(launch_noop_lut((__half *)(base + g->off_lut), g->ip.black[0] / 65535.0f, g->ip.white[0] / 65535.0f, s));
-  g->arena = base;                         // the kernels address the scratch for this call only
+  // the kernels address the scratch for this call only; the table just built is the one
+  // enqueue would build, so it is marked as current (and the graph's own marks restored)
+  const float keep_black = g->lut_black, keep_white = g->lut_white;
+  g->lut_black = g->ip.black[0]; g->lut_white = g->ip.white[0];
+  g->arena = base;
   const int r = enqueue(g, s, d_mosaic, d_rgba, false);
   g->arena = nullptr;
+  g->lut_black = keep_black; g->lut_white = keep_white;
   return r;
 }
 
@@ -1467,15 +1502,44 @@ int vkdt_cuda_graph_debug_stage(vkdt_cuda_graph_t *g, int stage, float *out, siz
     for(size_t i = 0; i < npx; i++) out[i] = __half2float(h[i]);
     return 0;
   }
-  if(stage == 2 || (stage == 3 && g->unfused))
+  if(stage == 2 || stage == 3 || stage == 4)
   {
+    if(stage != 2 && !g->debug) return fail(VKDT_CUDA_INCOMPLETE, "debug stages not enabled");
     if(count < nout * 4) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "buffer too small");
     std::vector<__half> h(nout * 4);
-    CU(cudaMemcpy(h.data(), g->arena + (stage == 2 ? g->off_rgbf : g->off_dm), nout * 8, cudaMemcpyDeviceToHost));
+    // the per-node chain keeps the demosaic output; the fused kernel and rcd_fill write debug copies
+    const size_t off = stage == 2 ? g->off_rgbf : stage == 4 ? g->off_dbg_col : (g->unfused ? g->off_dm : g->off_dbg_dm);
+    CU(cudaMemcpy(h.data(), g->arena + off, nout * 8, cudaMemcpyDeviceToHost));
     for(size_t i = 0; i < nout * 4; i++) out[i] = __half2float(h[i]);
     return 0;
   }
   return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "stage %d", stage);
+}
+
+int vkdt_cuda_graph_debug_decisions(vkdt_cuda_graph_t *g, int kind, void *out, size_t bytes, int *wd, int *ht)
+{
+  if(!g || !g->allocated) return fail(VKDT_CUDA_INCOMPLETE, "graph not allocated");
+  if(!g->debug) return fail(VKDT_CUDA_INCOMPLETE, "debug stages not enabled");
+  size_t off, esz;
+  if(kind == 0)
+  { // demosaic/gauss entries: the fused bayer kernel and the x-trans gauss node write them
+    if(g->halfsize || g->rcd) return fail(VKDT_CUDA_INCOMPLETE, "no demosaic/gauss in this graph");
+    off = g->off_dbg_gauss; esz = 1;
+  }
+  else if(kind == 1 || kind == 2)
+  {
+    if(!g->wavelet) return fail(VKDT_CUDA_INCOMPLETE, "no wavelet denoise in this graph");
+    off = kind == 1 ? g->off_dbg_cov : g->off_dbg_thr; esz = kind == 1 ? 4 : 1;
+  }
+  else return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "decision kind %d", kind);
+  if(wd) *wd = g->hw;
+  if(ht) *ht = g->hh;
+  const size_t n = (size_t)g->hw * g->hh * esz;
+  if(!out) return 0;
+  if(bytes < n) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "buffer too small");
+  CU(cudaStreamSynchronize(g->stream));
+  CU(cudaMemcpy(out, g->arena + off, n, cudaMemcpyDeviceToHost));
+  return 0;
 }
 
 // ---------------------------------------------------------------- noise statistics

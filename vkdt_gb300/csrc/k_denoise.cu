@@ -91,11 +91,16 @@ __global__ void __launch_bounds__(256) k_dn_half(const dev_denoise_t p)
 // window (mirrored) in shared memory.
 constexpr int DC_T = 16, DC_N = DC_T + 4;
 
+// The structure tensor decides two branches of the shader (the form taken and
+// the hot pixel skip): its sums are IEEE operations in the shader's order
+// without contraction, as the oracle evaluates them, from per texel terms made
+// once per staged texel: l = luminance, 1/l, l^2, 1/l^2 and l/25. i/l for the
+// integer offsets i in [-2, 2] is i (1/l) exactly (scaling by 1 or 2).
 __global__ void __launch_bounds__(256) k_dn_downcov(const dev_denoise_t p)
 {
-  // per texel of the window: r, g, b, luminance and the luminance terms of the two tensor forms
   __shared__ float sr[DC_N][DC_N + 1], sg[DC_N][DC_N + 1], sbl[DC_N][DC_N + 1];
   __shared__ float sl[DC_N][DC_N + 1], sil[DC_N][DC_N + 1], sl2[DC_N][DC_N + 1], sil2[DC_N][DC_N + 1];
+  __shared__ float sl25[DC_N][DC_N + 1];
   const int X0 = blockIdx.x * DC_T, Y0 = blockIdx.y * DC_T;
   for(int i = threadIdx.x; i < DC_N * DC_N; i += 256)
   {
@@ -108,7 +113,9 @@ __global__ void __launch_bounds__(256) k_dn_downcov(const dev_denoise_t p)
     ld4(p.half_img, p.hw, x, y, v);
     sr[ty][tx] = v[0]; sg[ty][tx] = v[1]; sbl[ty][tx] = v[2];
     const float l = lum2020(v[0], v[1], v[2]);
-    sl[ty][tx] = l; sil[ty][tx] = 1.0f / l; sl2[ty][tx] = l * l; sil2[ty][tx] = 1.0f / (l * l);
+    const float l2 = __fmul_rn(l, l);
+    sl[ty][tx] = l; sil[ty][tx] = __frcp_rn(l); sl2[ty][tx] = l2; sil2[ty][tx] = __frcp_rn(l2);
+    sl25[ty][tx] = __fdiv_rn(l, 25.0f);
   }
   __syncthreads();
   const int lx = threadIdx.x % DC_T, ly = threadIdx.x / DC_T;
@@ -122,35 +129,45 @@ __global__ void __launch_bounds__(256) k_dn_downcov(const dev_denoise_t p)
     for(int i = -2; i <= 2; i++)
     {
       const float px = sl[ly + 2 + j][lx + 2 + i], ipx = sil[ly + 2 + j][lx + 2 + i];
-      mw0 += (float)i * px; mw1 += (float)j * px; smw += px;
-      mb0 += (float)i * ipx; mb1 += (float)j * ipx; smb += ipx;
+      if(i) { mw0 = __fadd_rn(mw0, __fmul_rn((float)i, px)); mb0 = __fadd_rn(mb0, __fmul_rn((float)i, ipx)); }
+      if(j) { mw1 = __fadd_rn(mw1, __fmul_rn((float)j, px)); mb1 = __fadd_rn(mb1, __fmul_rn((float)j, ipx)); }
+      smw = __fadd_rn(smw, px); smb = __fadd_rn(smb, ipx);
     }
-  const float ismw = 1.0f / smw, ismb = 1.0f / smb;
-  mw0 *= ismw; mw1 *= ismw; mb0 *= ismb; mb1 *= ismb;
+  mw0 = __fdiv_rn(mw0, smw); mw1 = __fdiv_rn(mw1, smw);
+  mb0 = __fdiv_rn(mb0, smb); mb1 = __fdiv_rn(mb1, smb);
   // second moments
   float mean_b = 0.0f;
-  float Sw00 = 0.0f, Sw01 = 0.0f, Sw11 = 0.0f, Sb00 = 0.0f, Sb01 = 0.0f, Sb11 = 0.0f, sw = 0.0f, sb = 0.0f;
+  float Sw00 = 0.0f, Sw01 = 0.0f, Sw10 = 0.0f, Sw11 = 0.0f, Sb00 = 0.0f, Sb01 = 0.0f, Sb10 = 0.0f, Sb11 = 0.0f;
+  float sw = 0.0f, sb = 0.0f;
 #pragma unroll
   for(int j = -2; j <= 2; j++)
 #pragma unroll
     for(int i = -2; i <= 2; i++)
     {
-      mean_b += sl[ly + 2 + j][lx + 2 + i];
+      mean_b = __fadd_rn(mean_b, sl25[ly + 2 + j][lx + 2 + i]);
       const float p2 = sl2[ly + 2 + j][lx + 2 + i], b2 = sil2[ly + 2 + j][lx + 2 + i];
-      const float q0 = (float)i - mw0, q1 = (float)j - mw1;
-      Sw00 += p2 * q0 * q0; Sw01 += p2 * q0 * q1; Sw11 += p2 * q1 * q1; sw += p2;
-      const float r0 = (float)i - mb0, r1 = (float)j - mb1;
-      Sb00 += b2 * r0 * r0; Sb01 += b2 * r0 * r1; Sb11 += b2 * r1 * r1; sb += b2;
+      const float q0 = __fsub_rn((float)i, mw0), q1 = __fsub_rn((float)j, mw1);
+      Sw00 = __fadd_rn(Sw00, __fmul_rn(__fmul_rn(p2, q0), q0));
+      Sw01 = __fadd_rn(Sw01, __fmul_rn(__fmul_rn(p2, q0), q1));
+      Sw10 = __fadd_rn(Sw10, __fmul_rn(__fmul_rn(p2, q1), q0));
+      Sw11 = __fadd_rn(Sw11, __fmul_rn(__fmul_rn(p2, q1), q1));
+      sw = __fadd_rn(sw, p2);
+      const float r0 = __fsub_rn((float)i, mb0), r1 = __fsub_rn((float)j, mb1);
+      Sb00 = __fadd_rn(Sb00, __fmul_rn(__fmul_rn(b2, r0), r0));
+      Sb01 = __fadd_rn(Sb01, __fmul_rn(__fmul_rn(b2, r0), r1));
+      Sb10 = __fadd_rn(Sb10, __fmul_rn(__fmul_rn(b2, r1), r0));
+      Sb11 = __fadd_rn(Sb11, __fmul_rn(__fmul_rn(b2, r1), r1));
+      sb = __fadd_rn(sb, b2);
     }
-  mean_b *= 1.0f / 25.0f;
-  const float isw = 1.0f / sw, isb = 1.0f / sb;
-  Sw00 *= isw; Sw01 *= isw; Sw11 *= isw;
-  Sb00 *= isb; Sb01 *= isb; Sb11 *= isb;
-  // cov.glsl: the form with the smaller determinant (the tensor is symmetric)
-  const float detw = Sw00 * Sw11 - Sw01 * Sw01, detb = Sb00 * Sb11 - Sb01 * Sb01;
+  Sw00 = __fdiv_rn(Sw00, sw); Sw01 = __fdiv_rn(Sw01, sw); Sw10 = __fdiv_rn(Sw10, sw); Sw11 = __fdiv_rn(Sw11, sw);
+  Sb00 = __fdiv_rn(Sb00, sb); Sb01 = __fdiv_rn(Sb01, sb); Sb10 = __fdiv_rn(Sb10, sb); Sb11 = __fdiv_rn(Sb11, sb);
+  // cov.glsl: the form with the smaller determinant
+  const float detw = __fsub_rn(__fmul_rn(Sw00, Sw11), __fmul_rn(Sw10, Sw01));
+  const float detb = __fsub_rn(__fmul_rn(Sb00, Sb11), __fmul_rn(Sb10, Sb01));
+  const bool usew = detw < detb;
   float eval[2], e0[2], e1[2];
-  if(detw < detb) evd2x2(eval, e0, e1, Sw00, Sw01, Sw11);
-  else            evd2x2(eval, e0, e1, Sb00, Sb01, Sb11);
+  if(usew) evd2x2(eval, e0, e1, Sw00, Sw10, Sw11);
+  else     evd2x2(eval, e0, e1, Sb00, Sb10, Sb11);
   eval[1] *= 0.05f;
   eval[0] = gclamp(eval[0], 0.01f, 25.0f); eval[1] = gclamp(eval[1], 0.01f, 25.0f);
   const float ie0 = 1.0f / eval[0], ie1 = 1.0f / eval[1];
@@ -162,21 +179,23 @@ __global__ void __launch_bounds__(256) k_dn_downcov(const dev_denoise_t p)
   const float qa = kq * (e0[0] * e0[0] * ie0 + e1[0] * e1[0] * ie1);
   const float qb = kq * 2.0f * (e0[0] * e0[1] * ie0 + e1[0] * e1[1] * ie1);
   const float qc = kq * (e0[1] * e0[1] * ie0 + e1[1] * e1[1] * ie1);
-  const float hot = 2.0f * mean_b;
+  const float hot = __fmul_rn(2.0f, mean_b);
   float r0 = 0.0f, r1 = 0.0f, r2 = 0.0f, wt = 0.0f;
+  uint32_t skip = 0;
 #pragma unroll
   for(int j = -2; j <= 2; j++)
 #pragma unroll
     for(int i = -2; i <= 2; i++)
     {
       const float pr = sr[ly + 2 + j][lx + 2 + i];
-      if(pr > hot) continue;
+      if(pr > hot) { skip |= 1u << ((i + 2) + 5 * (j + 2)); continue; }
       float ex;
       asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(ex) : "f"(qa * (float)(i * i) + qb * (float)(i * j) + qc * (float)(j * j)));
       const float ww = fmaxf(1e-9f, ex);
       r0 += ww * pr; r1 += ww * sg[ly + 2 + j][lx + 2 + i]; r2 += ww * sbl[ly + 2 + j][lx + 2 + i];
       wt += ww;
     }
+  if(p.dbg_cov) p.dbg_cov[(size_t)y * p.hw + x] = skip | (usew ? 1u << 25 : 0u);
   const float d = 1.0f / fmaxf(wt, 1e-8f);
   float edge = gclamp(75.0f * fmaxf(0.0f, eval[1] - 0.09f), 0.0f, 1.0f);
   edge = smoothstep(0.4f, 0.75f, edge);
@@ -294,10 +313,13 @@ __global__ void __launch_bounds__(256) k_dn_assemble(const dev_denoise_t p)
   test = test * test; test = test * test; test = test * test; test = test * test;   // pow(test, 16)
   test = gclamp(1.5f * test, 0.0f, 1.0f);
   const float thrs0 = p.thrs0;
+  uint32_t sw = 0;
 #pragma unroll
   for(int l = 3; l >= 0; l--)
   {
-    const float thrs = (fabsf(d[l][0]) > 10.0f) ? 10000.0f : thrs0;
+    const bool big = fabsf(d[l][0]) > 10.0f;
+    sw |= big ? 1u << l : 0u;
+    const float thrs = big ? 10000.0f : thrs0;
 #pragma unroll
     for(int k = 0; k < 3; k++)
     {
@@ -323,6 +345,7 @@ __global__ void __launch_bounds__(256) k_dn_assemble(const dev_denoise_t p)
 #pragma unroll
   for(int k = 0; k < 3; k++) o[k] = rgb[k] / p.wb[k] * (p.white[k] - p.black[k]) + p.black[k];
   p.asm_img[(size_t)y * p.hw + x] = mk_half4(o[0], o[1], o[2], test);
+  if(p.dbg_thr) p.dbg_thr[(size_t)y * p.hw + x] = (uint8_t)sw;
 }
 
 // ---------------------------------------------------------------- doub

@@ -177,7 +177,7 @@ template<int PX, int PY> DEV void fix_taps_in(const smem_t &s, int bx, int sly,
 // The greens are f16 values (the hilite output), so their reciprocals and
 // those of their squares come from rcp_f16v; the quotients by the four sums
 // share one correctly rounded reciprocal each (div_ry): the same IEEE results.
-DEV void gauss_exact(const float px[8], float v[4])
+DEV void gauss_exact(const float px[8], float v[4], int &dec)
 {
   float inv[8];
 #pragma unroll
@@ -242,12 +242,15 @@ DEV void gauss_exact(const float px[8], float v[4])
   const float detw = __fsub_rn(__fmul_rn(Sw00, Sw11), __fmul_rn(Sw10, Sw01));
   const float detb = __fsub_rn(__fmul_rn(Sb00, Sb11), __fmul_rn(Sb10, Sb01));
   float eval[2], evec0[2], evec1[2];
-  if(detw < detb) evd2x2(eval, evec0, evec1, Sw00, Sw10, Sw11);
-  else            evd2x2(eval, evec0, evec1, Sb00, Sb10, Sb11);
+  const bool usew = detw < detb;
+  if(usew) evd2x2(eval, evec0, evec1, Sw00, Sw10, Sw11);
+  else     evd2x2(eval, evec0, evec1, Sb00, Sb10, Sb11);
   eval[0] = __fmul_rn(eval[0], 0.2f); eval[1] = __fmul_rn(eval[1], 0.2f);
-  if(fabsf(evec0[0]) > fabsf(evec0[1])) { evec0[0] = 1.0f; evec0[1] = 0.0f; }
-  else                                  { evec0[0] = 0.0f; evec0[1] = 1.0f; }
+  const bool horiz = fabsf(evec0[0]) > fabsf(evec0[1]);
+  if(horiz) { evec0[0] = 1.0f; evec0[1] = 0.0f; }
+  else      { evec0[0] = 0.0f; evec0[1] = 1.0f; }
   v[0] = f16r(eval[0]); v[1] = f16r(eval[1]); v[2] = f16r(evec0[0]); v[3] = f16r(evec0[1]);
+  dec = (usew ? GAUSS_DEC_USEW : 0) | ((horiz ? 0 : 1) << GAUSS_DEC_SNAP_SHIFT);
 }
 
 __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
@@ -342,6 +345,7 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
     float v[4] = { 0.0f, 0.0f, 0.0f, 0.0f };
     if(cx >= 0 && cy >= 0 && cx < hw && cy < hh)
     {
+      int dec;
       // green samples at (2c+ii, 2c+j), (ii+j) odd: M slot x = 2scx+2+ii
       float px[8];
       int k = 0;
@@ -354,7 +358,10 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
         const int xs = 2 * scx + 2 + ii;
         px[k++] = s.M[2 * scy + 2 + j][xs & 1][xs >> 1];
       }
-      gauss_exact(px, v);
+      gauss_exact(px, v, dec);
+      // debug: the entry's decisions, written by the CTA whose outputs own it
+      if(p.dbg_gauss && cx >= OX / 2 && cx < OX / 2 + TX / 2 && cy >= OY / 2 && cy < OY / 2 + TY / 2)
+        p.dbg_gauss[(size_t)cy * hw + cx] = (uint8_t)dec;
     }
     // splat.comp:159-163 and fix.comp:21-29 weights of this entry. E (i, j) is
     // (i, j) for evec (1,0), (j, -i) for evec (0,1) and 0 without covariance,
@@ -478,6 +485,11 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
       float co[3];
       colour_px(p, dm, co);
       const bool own = vx == px && vy == py && px >= OX && px < OXe && py >= OY && py < OYe;
+      if(own && p.dbg_colour)
+      {
+        p.dbg_demosaic[(size_t)py * W + px] = mk_half4(dm[0], dm[1], dm[2], 1.0f);
+        p.dbg_colour[(size_t)py * W + px] = mk_half4(co[0], co[1], co[2], 1.0f);
+      }
       if(own && p.hist)
       {
         const uint32_t bin = hist_bin(co[0], co[1], co[2]);

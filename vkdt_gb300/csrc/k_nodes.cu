@@ -228,13 +228,16 @@ __global__ void __launch_bounds__(256) k_nd_gauss_xt(const dev_nodes_t p)
   const float detw = __fsub_rn(__fmul_rn(Sw00, Sw11), __fmul_rn(Sw10, Sw01));
   const float detb = __fsub_rn(__fmul_rn(Sb00, Sb11), __fmul_rn(Sb10, Sb01));
   float eval[2], e0[2], e1[2];
-  if(detw < detb) evd2x2(eval, e0, e1, Sw00, Sw10, Sw11);
-  else            evd2x2(eval, e0, e1, Sb00, Sb10, Sb11);
+  const bool usew = detw < detb;
+  if(usew) evd2x2(eval, e0, e1, Sw00, Sw10, Sw11);
+  else     evd2x2(eval, e0, e1, Sb00, Sb10, Sb11);
   eval[0] = __fmul_rn(eval[0], 0.4f); eval[1] = __fmul_rn(eval[1], 0.4f);
-  if(fabsf(e0[0]) > __fmul_rn(2.0f, fabsf(e0[1])))      { e0[0] = 1.0f; e0[1] = 0.0f; }
-  else if(fabsf(e0[1]) > __fmul_rn(2.0f, fabsf(e0[0]))) { e0[0] = 0.0f; e0[1] = 1.0f; }
-  else { eval[0] = 0.1f; eval[1] = 0.1f; }
+  int snap;
+  if(fabsf(e0[0]) > __fmul_rn(2.0f, fabsf(e0[1])))      { e0[0] = 1.0f; e0[1] = 0.0f; snap = 0; }
+  else if(fabsf(e0[1]) > __fmul_rn(2.0f, fabsf(e0[0]))) { e0[0] = 0.0f; e0[1] = 1.0f; snap = 1; }
+  else { eval[0] = 0.1f; eval[1] = 0.1f; snap = 2; }
   p.cov[(size_t)y * p.hw + x] = mk_half4(eval[0], eval[1], e0[0], e0[1]);
+  if(p.dbg_gauss) p.dbg_gauss[(size_t)y * p.hw + x] = (uint8_t)((usew ? GAUSS_DEC_USEW : 0) | (snap << GAUSS_DEC_SNAP_SHIFT));
 }
 
 DEV void cov_z(const dev_nodes_t &p, int x, int y, float c[4])
@@ -497,6 +500,7 @@ template<bool FC> __global__ void __launch_bounds__(NT) k_post(const dev_image_t
       float co[3];
       colour_px(p, d, co);
       const bool own = vx == px && vy == py && px >= OX && px < OXe && py >= OY && py < OYe;
+      if(own && p.dbg_colour) p.dbg_colour[(size_t)py * W + px] = mk_half4(co[0], co[1], co[2], 1.0f);
       if(own && p.hist)
       {
         const uint32_t bin = hist_bin(co[0], co[1], co[2]);

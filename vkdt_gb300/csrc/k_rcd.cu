@@ -293,6 +293,7 @@ template<bool POST> __global__ void __launch_bounds__(256, 5) k_rcd_fill(const d
         {
           float co[3], fc[3];
           colour_px(d, dm, co);
+          if(d.dbg_colour) d.dbg_colour[(size_t)gy * p.W + gx] = mk_half4(co[0], co[1], co[2], 1.0f);
           if(d.hist)
           {
             const uint32_t bin = hist_bin(co[0], co[1], co[2]);

@@ -52,7 +52,14 @@ struct dev_image_t
   uint32_t *hist;       // 257 counts or null
   // debug copies (null in production)
   __half *dbg_denoise, *dbg_hilite;
+  half4 *dbg_demosaic, *dbg_colour;   // demosaic and colour outputs at the output size
+  uint8_t *dbg_gauss;                 // demosaic/gauss decisions per entry (GAUSS_DEC bits)
 };
+
+// the discrete decisions of demosaic/gauss.comp per entry, written by the
+// debug stages: bit 0 det(Sw) < det(Sb) (the structure tensor taken); bits
+// 1-2 the snapped direction: 0 (1,0), 1 (0,1), 2 none (x-trans: isotropic)
+enum { GAUSS_DEC_USEW = 1, GAUSS_DEC_SNAP_SHIFT = 1 };
 
 struct dev_hilite_k1_t
 {
@@ -104,6 +111,11 @@ struct dev_denoise_t
   half4 *lvl[4];         // downcov, down 1..3 outputs (swizzled)
   half4 *asm_img;        // assemble output
   __half *dn;            // doub output: the denoised normalised mosaic, W*H
+  // debug decisions (null in production), per half size texel: cov.glsl
+  // response(): bits 0-24 the hot pixel skip of tap (i+2) + 5 (j+2), bit 25
+  // det(Sw) < det(Sb); assemble.comp: bit l the threshold switch |d_l| > 10
+  uint32_t *dbg_cov;
+  uint8_t *dbg_thr;
 };
 // stage 0 half, 1 downcov, 2..4 down levels 1..3, 5 assemble, 6 doub (k_denoise.cu)
 cudaError_t launch_denoise(const dev_denoise_t &p, int stage, cudaStream_t s);
@@ -132,6 +144,7 @@ struct dev_nodes_t
   const half4 *coarse;   // assembled hilite level 1 (or reduce level 1 when the pyramid has one level)
   int ccw, cch;          // its size
   float hl_soft;
+  uint8_t *dbg_gauss;    // debug: demosaic/gauss decisions per entry (x-trans), or null
 };
 // stage: 0 noop, 1 hilite half, 2 hilite doub, 3 gauss, 4 splat, 5 fix, 6 halfsize, 7 resample,
 // 8 bayer noop + hilite half + level 0 hilite assemble + hilite doub from the mosaic (dn written when set)

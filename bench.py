@@ -13,9 +13,17 @@ e2e:   the same metric through the public C-ABI call with host buffers: the
 pinned host mosaic is uploaded, developed and the rgba f16 result read back
 inside the timed region of every step.
 
---impl reference: the CPU implementation of the path (the oracle, a C++
-restatement of the reference shaders, or the reference shaders compiled for
-the CPU when that build is present), all host threads, on a bounded sample.
+err:   the benchmarked image's llap output against the FP32 oracle and the
+FP64 build of the same restatement (full image), computed after the timed
+region in a child process, so the timed process never maps the oracle.
+batch: the mixed-size batch (64 mosaics of 4000x3000 .. 9504x6336) through the
+develop server beside the plain per-image path, with p50/p99 latency.
+
+--impl reference: the reference's own shaders compiled for the CPU (or, where
+that build is missing, the oracle, a C++ restatement of them), all host
+threads, one develop of the full 6000x4000 mosaic per step. That process loads
+no library of this package: its mosaic comes from the oracle's copy of the
+scene recipe.
 """
 import argparse
 import json
@@ -39,6 +47,20 @@ DENOISE = 0.0
 DEMOSAIC = 0          # demosaic method: 0 gaussian splats (the raw photo default), 1 rcd, 2 half size
 FILTERS = 0x94949494  # bayer rggb; 9: x-trans
 DEMOSAIC_NAMES = {0: "gaussian splats (method 0)", 1: "rcd (method 1)", 2: "half size (method 2)"}
+# the synthetic camera's matrix to rec2020 (rows sum to one), as the package's default image parameters
+CAM_TO_REC2020 = (1.20, -0.15, -0.05, -0.10, 1.25, -0.15, 0.02, -0.22, 1.20)
+# the sources of the fused develop kernel: the DRAM traffic of an ncu capture is reported only
+# while they are the ones that capture measured (profiles/traffic.json holds their hash)
+K_DEVELOP_SOURCES = ["k_develop.cu", "common.cuh", "hilite.cuh", "pixel.cuh", "develop_px.cuh", "kernels.h"]
+
+
+def source_hash(files):
+    import hashlib
+    h = hashlib.sha256()
+    for f in files:
+        with open(os.path.join(ROOT, "vkdt_gb300", "csrc", f), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:16]
 
 
 def over_ranks(x, op="max"):
@@ -122,52 +144,122 @@ class Clocks:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(seconds=10.0, ref=False):
-    """The CPU path on a bounded sample of the workload (same recipe, 2000x1332)."""
-    import vkdt_gb300 as v
-    import oracle
-    wd, ht = 2000, 1332
-    m = v.scene_host(v.make_scene(wd, ht, seed=1, a=NOISE_A, b=NOISE_B))
-    ip = oracle.img_param(img_param(v, wd, ht))
+def oracle_img_param(oracle, wd, ht):
+    """the workload's image parameters as the oracle's struct (no package import)"""
+    ip = oracle.ImgParam()
+    rng = WHITE - BLACK
+    for k in range(4):
+        ip.black[k], ip.white[k] = BLACK, WHITE
+    for k, w in enumerate((2.0, 1.0, 1.6, 1.0)):
+        ip.whitebalance[k] = w
+    ip.filters = FILTERS
+    ip.crop_aabb[0], ip.crop_aabb[1], ip.crop_aabb[2], ip.crop_aabb[3] = 0, 0, wd, ht
+    for i in range(9):
+        ip.cam_to_rec2020[i] = CAM_TO_REC2020[i]
+    ip.noise_a, ip.noise_b = NOISE_A / rng ** 2, NOISE_B / rng
+    return ip
+
+
+def oracle_params(oracle):
     p = oracle.default_params()
     p.ll_levels = LEVELS
     p.dn_strength = DENOISE
-    kind = "port"
-    run = lambda: oracle.develop(m, ip, params=p, stages=("llap",))
-    if ref:
-        try:
-            from oracle import glsl_ref
-            if glsl_ref.available():
-                run = lambda: glsl_ref.develop(m, ip, params=p)
-                kind = "reference"
-        except ImportError:
-            pass
-    run()  # warm
-    t0 = time.perf_counter()
-    n = 0
-    while True:
+    p.dm_method = DEMOSAIC
+    return p
+
+
+def cpu_leg(args):
+    """Child process of the GPU arm (after its timed region): the error of the benchmarked image
+    against the oracle (FP32) and the FP64 build, and the oracle's own throughput on the same
+    workload (cpu_baseline). Reads the mosaic and the GPU result from args.cpu_leg."""
+    import oracle
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from metrics import delta_e2000
+    m = np.load(os.path.join(args.cpu_leg, "mosaic.npy"))
+    out = np.load(os.path.join(args.cpu_leg, "out.npy")).astype(np.float32)
+    ht, wd = m.shape
+    ip = oracle_img_param(oracle, wd, ht)
+    p = oracle_params(oracle)
+    res = {}
+
+    def err(ref):
+        e = np.abs(out[..., :3].astype(np.float64) - ref[..., :3]) / np.maximum(1.0, np.abs(ref[..., :3]))
+        e = e.max(axis=-1)
+        de = delta_e2000(out, ref)
+        return {"max": float(e.max()), "mean": float(e.mean()), "px_over_2e-3": int((e > 2e-3).sum()),
+                "de2000_max": float(de.max()), "px_de_over_0.5": int((de >= 0.5).sum())}
+    res["err"] = {"stage": "llap output (the sink), rgb, |a-b|/max(1,|b|)", "window": "full %dx%d" % (wd, ht),
+                  "vs_oracle_fp32": err(oracle.develop(m, ip, params=p, stages=("llap",))["llap"]),
+                  "vs_fp64": err(oracle.develop(m, ip, params=p, double=True, stages=("llap",))["llap"]),
+                  "tolerance": {"max": 2e-3, "mean": 1e-4, "de2000": 0.5,
+                                "note": "pixels over 2e-3 are where a branch of the reference was a near tie "
+                                        "(tests/parity.py shows each such decision explained)"}}
+    if not args.no_cpu:
+        run = lambda: oracle.develop(m, ip, params=p, stages=("llap",))
         run()
-        n += 1
-        if time.perf_counter() - t0 >= seconds:
-            break
-    dt = time.perf_counter() - t0
-    mps = n * wd * ht / 1e6 / dt
-    return {"value": mps, "unit": "MP/s", "cores": os.cpu_count(), "kind": kind,
-            "sample": "%d develops of a %dx%d mosaic of the same recipe (%.1f s)" % (n, wd, ht, dt)}
+        t0 = time.perf_counter()
+        n = 0
+        while n < 1 or time.perf_counter() - t0 < args.cpu_seconds:
+            run()
+            n += 1
+        dt = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": n * wd * ht / 1e6 / dt, "unit": "MP/s", "cores": os.cpu_count(),
+                               "kind": "port", "sample": "%d develops of the %dx%d workload mosaic (%.1f s), "
+                               "the FP32 oracle on all host threads" % (n, wd, ht, dt)}
+    print(json.dumps(res))
 
 
 def run_reference(args):
+    """The reference's CPU implementation of the path on the GPU arm's workload: one develop of
+    the full mosaic per step, all host threads; rank 0 only."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    cb = cpu_baseline(seconds=max(5.0, 2.0 * args.steps), ref=True)
-    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "MP/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config(),
-            "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "MP/s", "h2d_bytes_per_step": 0,
-                                        "d2h_bytes_per_step": 0}}
+    import oracle
+    kind, run = "port", None
+    m = oracle.scene(WD, HT, seed=0, image_id=0, filters=FILTERS, black=BLACK, white=WHITE, a=NOISE_A, b=NOISE_B)
+    ip = oracle_img_param(oracle, WD, HT)
+    p = oracle_params(oracle)
+    try:
+        from oracle import glsl_ref
+        if glsl_ref.build():
+            run = lambda: glsl_ref.develop(m, ip, params=p)
+            kind = "reference"
+    except Exception:
+        run = None
+    if run is None:
+        run = lambda: oracle.develop(m, ip, params=p, stages=("llap",))
+    t0 = time.perf_counter()
+    run()                                   # first warm-up step: also sizes the run
+    t_one = time.perf_counter() - t0
+    for _ in range(max(0, min(args.warmup, 2) - 1)):
+        run()
+    steps = args.steps
+    # each step develops the full mosaic; where K of them would take more than about three
+    # minutes, each step develops fewer of its rows (a band of the same workload) and says so
+    rows = HT
+    if steps * t_one > 180.0:
+        rows = max(64, int(HT * 180.0 / (steps * t_one)) // 2 * 2)
+        mb = np.ascontiguousarray(m[:rows])
+        ipb = oracle_img_param(oracle, WD, rows)
+        run = (lambda: glsl_ref.develop(mb, ipb, params=p)) if kind == "reference" else \
+              (lambda: oracle.develop(mb, ipb, params=p, stages=("llap",)))
+        run()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        run()
+    dt = time.perf_counter() - t0
+    value = steps * WD * rows / 1e6 / dt
+    sample = "%d develops of the %dx%d workload mosaic (%.1f s)" % (steps, WD, rows, dt)
+    cfg = config()
+    if rows != HT:
+        cfg["workload"] += "; reference arm: each step a %dx%d band of the mosaic" % (WD, rows)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "MP/s", "n_gpus": args.gpus,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": dt / steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
+            "cpu_baseline": {"value": value, "unit": "MP/s", "cores": os.cpu_count(), "kind": kind, "sample": sample},
+            "e2e": {"value": value, "unit": "MP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
-
 
 
 # ---------------------------------------------------------------- served / batched workloads
@@ -625,6 +717,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="cuda")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--no-err", action="store_true", help="skip the error against the oracle and FP64 build")
+    ap.add_argument("--no-batch", action="store_true", help="skip the mixed-size batch sub-object")
+    ap.add_argument("--cpu-leg", default=None, help=argparse.SUPPRESS)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help=argparse.SUPPRESS)
     ap.add_argument("--size", default="%dx%d" % (WD, HT), help="WxH of the mosaic (profiling of smaller cases)")
     ap.add_argument("--ring", type=int, default=RING, help="number of resident inputs")
     ap.add_argument("--levels", type=int, default=LEVELS, help="llap pyramid depth (0 = automatic)")
@@ -645,6 +741,8 @@ def main():
     RING, LEVELS, DENOISE = args.ring, args.levels, args.denoise
     DEMOSAIC = max(0, args.demosaic)
     FILTERS = 9 if args.cfa == "xtrans" else 0x94949494
+    if args.cpu_leg:
+        return cpu_leg(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.workload != "single":
@@ -765,10 +863,16 @@ def main():
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     issue = None
+    traffic_note = None
     if os.path.exists(tp) and fused:
         try:
             tj = json.load(open(tp))
-            traffic = tj.get("k_develop_bytes_per_launch")
+            if tj.get("k_develop_source_sha") == source_hash(K_DEVELOP_SOURCES) and (WD, HT) == (6000, 4000) \
+                    and DENOISE == 0:
+                traffic = tj.get("k_develop_bytes_per_launch")
+                traffic_note = "ncu capture of this kernel source at this size (" + tj.get("source", "") + ")"
+            else:
+                traffic_note = "no ncu capture of this kernel source and size"
             # the kernel is bound by instruction issue, not by HBM: the ncu capture's issue
             # utilisation and instructions per pixel are reported beside the HBM fraction
             issue = {"issue_active": tj.get("k_develop_issue_active"),
@@ -783,7 +887,7 @@ def main():
              "llap:colour": "k_llap_final (llap assemble level 0 + colour)"}.get(names[dev_idx], names[dev_idx])
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak if achieved else None,
-                "traffic": traffic, "kernel": kname, "compute": issue,
+                "traffic": traffic, "traffic_source": traffic_note, "kernel": kname, "compute": issue,
                 "kernel_ms": dev_ms, "alg_bytes_per_launch": alg,
                 "peak_source": "measured" if peaks else "fallback",
                 "per_launch_ms": [[n, round(float(x), 5)] for n, x in zip(names, kms)],
@@ -827,31 +931,71 @@ def main():
     for g in ring:
         g.wait()
     barrier()
-    np_ = max(3 * len(ring), min(4 * args.steps, 60))
-    t0 = time.perf_counter()
-    for k in range(np_):
-        g = ring[k % len(ring)]
-        if k >= len(ring):
+    def pipelined(n):
+        barrier()
+        t0 = time.perf_counter()
+        for k in range(n):
+            g = ring[k % len(ring)]
+            if k >= len(ring):
+                g.wait()
+            g.run(flags=v.RUN_UPLOAD_SOURCE | v.RUN_DOWNLOAD_SINK, stream=streams[k % len(ring)].cuda_stream)
+        for g in ring:
             g.wait()
-        g.run(flags=v.RUN_UPLOAD_SOURCE | v.RUN_DOWNLOAD_SINK, stream=streams[k % len(ring)].cuda_stream)
-    for g in ring:
-        g.wait()
-    pipe_rank = time.perf_counter() - t0
-    pipe_value = replica_rate(np_ * mp_step, pipe_rank)
+        return time.perf_counter() - t0
+    # steps per repeat for about 1.2 s of work, then 3 timed repeats; their median
+    probe = max(3 * len(ring), 12)
+    np_ = max(probe, int(probe * 1.2 / max(pipelined(probe), 1e-3)))
+    reps = sorted(replica_rate(np_ * mp_step, pipelined(np_)) for _ in range(3))
+    pipe_value = reps[1]
     e2e = {"value": pipe_value, "unit": "MP/s", "h2d_bytes_per_step": WD * HT * 2,
-           "d2h_bytes_per_step": WD * HT * 8, "steps": np_, "graphs_in_flight": len(ring),
+           "d2h_bytes_per_step": WD * HT * 8, "steps": np_, "repeats_mps": [round(x, 1) for x in reps],
+           "timing": "median of 3 repeats of %d pipelined steps each (host clock, >= 1 s each)" % np_,
+           "graphs_in_flight": len(ring),
            "one_at_a_time": {"value": world * mp_step / (e2e_ms / 1e3), "unit": "MP/s"},
            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))}}
 
-    cb = None
-    if rank == 0 and world == 1 and not args.no_cpu:
-        cb = cpu_baseline(seconds=10.0)
+    # the mixed-size batch (served vs per image) on this GPU
+    batch = None
+    if not args.no_batch and (WD, HT) == (6000, 4000):
+        for g in graphs[1:]:
+            g.close()
+        graphs = graphs[:1]
+        torch.cuda.synchronize()
+        bclk = Clocks(local)
+        args.images = 64
+        bcfg, bvalue, bms, bextra = workload_batch(args, v, torch, sp, bclk)
+        batch = {"workload": bcfg["workload"], "mpix": bcfg["mpix"], "value": bvalue, "unit": "MP/s", "ms": bms,
+                 "per_image": bextra["per_image"], "served_over_per_image": bextra["served_over_per_image"],
+                 "latency_ms": bextra["latency_ms"], "autotune": bextra["autotune"], "clocks": bclk.summary()}
+
+    # the error of the benchmarked image and the CPU baseline, in a child process (the oracle)
+    cb, err = None, None
+    if rank == 0 and world == 1 and not (args.no_cpu and args.no_err):
+        import tempfile
+        # graph 0 holds host_in[0] in its pinned source (the e2e runs uploaded it): develop it again
+        # and read the result back
+        g0 = graphs[0]
+        g0.source()[...] = host_in[0]
+        out = g0.run(flags=v.RUN_UPLOAD_SOURCE | v.RUN_DOWNLOAD_SINK | v.RUN_WAIT_DONE, stream=sp)
+        host_m = np.array(host_in[0], copy=True)
+        with tempfile.TemporaryDirectory() as td:
+            np.save(os.path.join(td, "mosaic.npy"), host_m)
+            np.save(os.path.join(td, "out.npy"), np.asarray(out))
+            cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--cpu-leg", td, "--size", "%dx%d" % (WD, HT),
+                   "--levels", str(LEVELS), "--denoise", str(DENOISE), "--cfa", "xtrans" if FILTERS == 9 else "rggb",
+                   "--demosaic", str(DEMOSAIC)] + (["--no-cpu"] if args.no_cpu else [])
+            r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+            if r.returncode == 0:
+                leg = json.loads(r.stdout.strip().splitlines()[-1])
+                cb, err = leg.get("cpu_baseline"), leg.get("err")
+            else:
+                err = {"unavailable": "cpu leg failed: " + r.stderr.strip().splitlines()[-1] if r.stderr.strip() else "?"}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "MP/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config(),
-                "roofline": roofline, "cpu_baseline": cb, "e2e": e2e,
+                "roofline": roofline, "cpu_baseline": cb, "e2e": e2e, "err": err, "batch": batch,
                 "gpu_launches": launches_per_step * args.steps, "clocks": clk.summary(),
                 "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))}}
         print(json.dumps(line))

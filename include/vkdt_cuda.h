@@ -258,6 +258,15 @@ int  vkdt_cuda_graph_hist(vkdt_cuda_graph_t *graph, uint32_t *hist257);
 /* standalone OpenDRT/hist.comp over a device rgba f16 image into a device u32[257]
  * (cleared by the call) */
 int  vkdt_cuda_hist_rgba_f16(const void *d_rgba, int wd, int ht, uint32_t *d_hist257, void *stream);
+/* hist/collect.comp:13-26 (the hist module's collect node, hist/main.c:26-41):
+ * the rgb waveform of a device rgba f16 image into a device u32 image of
+ * out_wd x out_ht (the module asks 1000 x 600, hist/main.c:9-11), cleared
+ * first as the node's s_conn_clear output is. Column int(out_wd/wd * x), row
+ * (1 - value) * out_ht + 0.5 (negative and NaN count in row 0, values past the
+ * last row in the last); red adds 1, green 1024, blue 1048576. Exact integer
+ * counts; does not wait for its stream. */
+int  vkdt_cuda_waveform_rgba_f16(const void *d_rgba, int wd, int ht, uint32_t *d_out, int out_wd, int out_ht,
+    void *stream);
 
 /* Ingestion of packed raw video (replaces the host unpack of i-mlv/video_mlv.c:254-274,
  * called from read_source at i-mlv/main.c:204-211 through read_frame at main.c:76-85):

@@ -21,8 +21,8 @@ SO = os.path.join(HERE, "liboracle.so")
 
 def build(force=False):
     src = os.path.join(HERE, "oracle.cpp")
-    hdr = os.path.join(HERE, "oracle.h")
-    if not force and os.path.exists(SO) and os.path.getmtime(SO) >= max(os.path.getmtime(src), os.path.getmtime(hdr)):
+    deps = [src, os.path.join(HERE, "oracle.h"), os.path.join(os.path.dirname(HERE), "vkdt_gb300", "csrc", "scene.h")]
+    if not force and os.path.exists(SO) and os.path.getmtime(SO) >= max(os.path.getmtime(d) for d in deps):
         return SO
     # no contraction: the oracle's operation order is the reference's
     cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-o", SO, src]
@@ -147,13 +147,20 @@ def lib():
         for f in (l.oracle_develop_f32, l.oracle_develop_f64):
             f.restype = C.c_int
             f.argtypes = [C.POINTER(C.c_uint16), C.c_int, C.c_int, C.POINTER(ImgParam), C.POINTER(Params), C.POINTER(Stages)]
+        l.oracle_develop_from_f32.restype = C.c_int
+        l.oracle_develop_from_f32.argtypes = [C.POINTER(C.c_uint16), C.c_int, C.c_int, C.POINTER(ImgParam),
+                                              C.POINTER(Params), C.POINTER(Stages), C.POINTER(Decisions), C.c_int,
+                                              C.c_void_p]
         for f in (l.oracle_develop_dec_f32, l.oracle_develop_dec_f64):
             f.restype = C.c_int
             f.argtypes = [C.POINTER(C.c_uint16), C.c_int, C.c_int, C.POINTER(ImgParam), C.POINTER(Params),
                           C.POINTER(Stages), C.POINTER(Decisions)]
+        l.oracle_scene.argtypes = [C.c_int, C.c_int, C.c_uint32, C.c_uint32, C.c_uint32, C.c_float, C.c_float,
+                                   C.c_float, C.c_float, C.c_void_p, C.c_float, C.c_float, C.c_void_p]
         l.oracle_gauss_decisions.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_uint32, C.c_void_p, C.c_void_p]
         l.oracle_noop.argtypes = [C.POINTER(C.c_uint16), C.c_int, C.c_int, C.POINTER(ImgParam), C.POINTER(C.c_float)]
         l.oracle_hist.argtypes = [C.POINTER(C.c_float), C.c_int, C.c_int, C.POINTER(C.c_uint32)]
+        l.oracle_waveform.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
         l.oracle_hist_bin.restype = C.c_uint32
         l.oracle_hist_bin.argtypes = [C.c_float, C.c_float, C.c_float]
         l.oracle_cfa_colour.restype = C.c_int
@@ -194,13 +201,19 @@ def _fptr(a):
     return a.ctypes.data_as(C.POINTER(C.c_float))
 
 
-def develop(mosaic, ip, params=None, double=False, stages=("llap",), record=False, force=None):
+START = {"hilite": 1, "demosaic": 2, "colour": 3, "filmcurv": 4, "llap": 5}
+
+
+def develop(mosaic, ip, params=None, double=False, stages=("llap",), record=False, force=None, start=None,
+            input=None):
     """Run the oracle on a u16 mosaic; returns a dict of the requested stage images.
 
     record: also return the oracle's own discrete decisions and their margins
     ("dec_<kind>", "margin_<kind>" for the kinds of DECISION_KINDS that the
     graph has). force: {kind: array} decisions applied in place of the
-    oracle's own (the grids of vkdt_cuda_graph_debug_decisions)."""
+    oracle's own (the grids of vkdt_cuda_graph_debug_decisions). start, input:
+    run the path from stage `start` (a key of START) on `input`, the output of
+    the stage before it (FP32 only)."""
     mosaic = np.ascontiguousarray(mosaic, dtype=np.uint16)
     ht, wd = mosaic.shape
     params = params or default_params()
@@ -221,7 +234,19 @@ def develop(mosaic, ip, params=None, double=False, stages=("llap",), record=Fals
             st.hist = bufs[name].ctypes.data_as(C.POINTER(C.c_uint32))
         else:
             setattr(st, name, _fptr(bufs[name]))
-    if record or force:
+    if start is not None:
+        if double:
+            raise ValueError("the path from a stage runs on the FP32 build")
+        inp = np.ascontiguousarray(input, np.float32)
+        dec = Decisions()
+        keep = [inp]
+        for kind, arr in (force or {}).items():
+            a = np.ascontiguousarray(arr, DECISION_KINDS[kind][0])
+            keep.append(a)
+            setattr(dec, kind + "_force", a.ctypes.data)
+        r = lib().oracle_develop_from_f32(mosaic.ctypes.data_as(C.POINTER(C.c_uint16)), wd, ht, C.byref(ip),
+                                          C.byref(params), C.byref(st), C.byref(dec), START[start], inp.ctypes.data)
+    elif record or force:
         block = 3 if ip.filters == 9 else 2
         gw, gh = W // block, H // block
         dec = Decisions()
@@ -250,6 +275,16 @@ def develop(mosaic, ip, params=None, double=False, stages=("llap",), record=Fals
     bufs["llap_levels"] = st.llap_levels
     bufs["hilite_levels"] = st.hilite_levels
     return bufs
+
+
+def scene(wd, ht, seed=0, image_id=0, filters=0x94949494, black=512.0, white=16383.0, a=2.0, b=0.4,
+          wb=(2.0, 1.0, 1.6), pan=(0.0, 0.0)):
+    """The benchmarks' seeded mosaic (u16 H x W), without the CUDA library."""
+    out = np.zeros((ht, wd), np.uint16)
+    w = np.ascontiguousarray(wb, np.float32)
+    lib().oracle_scene(wd, ht, seed, image_id, filters, black, white, a, b, w.ctypes.data, pan[0], pan[1],
+                       out.ctypes.data)
+    return out
 
 
 def gauss_decisions(mosaic, filters):
@@ -336,6 +371,14 @@ def hist(rgba):
     h = np.zeros(257, np.uint32)
     lib().oracle_hist(_fptr(rgba), rgba.shape[1], rgba.shape[0], h.ctypes.data_as(C.POINTER(C.c_uint32)))
     return h
+
+
+def waveform(rgba, wo=1000, ho=600):
+    """hist/collect.comp restated: the rgb waveform (ho x wo u32) of an H x W x 4 float image"""
+    rgba = np.ascontiguousarray(rgba, np.float32)
+    out = np.zeros((ho, wo), np.uint32)
+    lib().oracle_waveform(rgba.ctypes.data, rgba.shape[1], rgba.shape[0], wo, ho, out.ctypes.data)
+    return out
 
 
 def hist_bin(r, g, b):

@@ -22,6 +22,8 @@
 //   operand, as the min/max instructions of GPUs do.
 // - R16_UNORM decodes as v/65535.
 #include "oracle.h"
+// the seeded synthetic scene of the benchmarks and tests (inputs, not the path)
+#include "../vkdt_gb300/csrc/scene.h"
 
 #include <algorithm>
 #include <cmath>
@@ -206,6 +208,17 @@ template<class T> static inline float rel_gap(T a, T b)
 {
   const T m = gmax(std::fabs(a), std::fabs(b));
   return m > T(0) ? (float)(std::fabs(a - b) / m) : 0.0f;
+}
+
+// the stage a develop call starts from, with the given input image (node-wise
+// checks: a stage of the path on another implementation's input). 0: the mosaic.
+static struct { int start; const float *img; } g_inj = { 0, nullptr };
+
+template<class T> static img_t<T> from_float(const float *src, int w, int h, int c)
+{ // values already stored by an f16 image: taken as they are
+  img_t<T> im(w, h, c);
+  for(size_t i = 0; i < im.d.size(); i++) im.d[i] = T(src[i]);
+  return im;
 }
 
 // ------------------------------------------------------------------ denoise
@@ -2176,6 +2189,7 @@ template<class T> static int develop(const uint16_t *mosaic, int wd, int ht,
     dn = denoise_doub(raw, as, half, W, H, crop, black, white, filters, T(ip->noise_a), T(ip->noise_b),
         T(p->dn_strength), T(p->dn_luma), T(p->dn_detail), edges);
   }
+  if(g_inj.start >= 1) dn = from_float<T>(g_inj.img, W, H, 1);   // (the start stage replaces it)
   if(st) to_float_ch(dn, 1, st->denoise);
 
   // ---- hilite (hilite/main.c:5-90)
@@ -2209,6 +2223,7 @@ template<class T> static int develop(const uint16_t *mosaic, int wd, int ht,
     }
     hilite_doub(dn, up, hw, hh, hwhite, filters, hl);
   }
+  if(g_inj.start >= 2) hl = from_float<T>(g_inj.img, W, H, 1);
   if(st) to_float_ch(hl, 1, st->hilite);
 
   // ---- demosaic (demosaic/main.c:18-203)
@@ -2240,15 +2255,18 @@ template<class T> static int develop(const uint16_t *mosaic, int wd, int ht,
     img_t<T> g = demosaic_splat(hl, cov, W, H, filters);
     rgb = demosaic_fix(hl, g, cov, W, H, filters, p->dm_colour);
   }
+  if(g_inj.start >= 3) rgb = from_float<T>(g_inj.img, rgb.w, rgb.h, 4);
   if(st) { to_float(rgb, st->demosaic); st->out_wd = rgb.w; st->out_ht = rgb.h; }
 
   // ---- colour, filmcurv (+ histogram of its input), llap
   if(p->fc_colour != 1 && p->fc_colour != 3) return 5; // filmcurv colour modes restated: 1, 3
   if(p->co_sat != 1.0f) return 6;                       // colour saturation path not restated
   img_t<T> col = colour_main(rgb, ip, p);
+  if(g_inj.start >= 4) col = from_float<T>(g_inj.img, col.w, col.h, 4);
   if(st) to_float(col, st->colour);
   if(st && st->hist) hist(col, st->hist);
   img_t<T> fc = filmcurv_main(col, p);
+  if(g_inj.start >= 5) fc = from_float<T>(g_inj.img, fc.w, fc.h, 4);
   if(st) to_float(fc, st->filmcurv);
 
   // llap (llap/main.c:6-106)
@@ -2307,6 +2325,17 @@ int oracle_develop_dec_f32(const uint16_t *mosaic, int wd, int ht,
   return r;
 }
 
+int oracle_develop_from_f32(const uint16_t *mosaic, int wd, int ht, const oracle_img_param_t *ip,
+    const oracle_params_t *p, oracle_stages_t *out, oracle_decisions_t *dec, int start, const float *input)
+{
+  g_dec = dec;
+  g_inj.start = start; g_inj.img = input;
+  const int r = develop<float>(mosaic, wd, ht, ip, p, out);
+  g_inj.start = 0; g_inj.img = nullptr;
+  g_dec = nullptr;
+  return r;
+}
+
 int oracle_develop_dec_f64(const uint16_t *mosaic, int wd, int ht,
     const oracle_img_param_t *ip, const oracle_params_t *p, oracle_stages_t *out, oracle_decisions_t *dec)
 {
@@ -2329,6 +2358,15 @@ void oracle_gauss_decisions(const float *mosaic, int wd, int ht, uint32_t filter
   g_dec = nullptr;
 }
 
+void oracle_scene(int wd, int ht, uint32_t seed, uint32_t image_id, uint32_t filters, float black, float white,
+    float noise_a, float noise_b, const float wb[3], float pan_x, float pan_y, uint16_t *out)
+{ // the benchmark's seeded scene, from the recipe the library also generates on the device
+  scene_layout_t s;
+  scene_layout_make(&s, wd, ht, seed, image_id, filters, black, white, noise_a, noise_b, wb, pan_x, pan_y);
+  OMP_FOR
+  for(int y = 0; y < ht; y++) for(int x = 0; x < wd; x++) out[(size_t)y * wd + x] = scene_pixel(&s, x, y);
+}
+
 void oracle_noop(const uint16_t *mosaic, int wd, int ht, const oracle_img_param_t *ip, float *out)
 {
   img_t<float> raw(wd, ht, 1);
@@ -2345,6 +2383,27 @@ void oracle_hist(const float *rgba, int wd, int ht, uint32_t *h)
   img_t<float> im(wd, ht, 4);
   memcpy(im.d.data(), rgba, sizeof(float) * 4 * (size_t)wd * ht);
   hist(im, h);
+}
+
+// hist/collect.comp:13-26, the rgb waveform (its arithmetic without contraction;
+// float to unsigned saturates: negative and NaN to 0, as GPUs convert)
+void oracle_waveform(const float *rgba, int wd, int ht, int wo, int ho, uint32_t *out)
+{
+  memset(out, 0, sizeof(uint32_t) * (size_t)wo * ho);
+  const float scale = (float)wo / (float)wd;
+  auto row = [&](float v) -> uint32_t {
+    const float t = (1.0f - v) * (float)ho + 0.5f;
+    const uint32_t u = t >= 4294967296.0f ? 0xffffffffu : (t > 0.0f ? (uint32_t)t : 0u);
+    return std::min(u, (uint32_t)(ho - 1));
+  };
+  for(int y = 0; y < ht; y++) for(int x = 0; x < wd; x++)
+  {
+    const float *p = rgba + 4 * ((size_t)y * wd + x);
+    const int c = std::min(std::max((int)(scale * (float)x), 0), wo - 1);
+    out[(size_t)row(p[0]) * wo + c] += 1u;
+    out[(size_t)row(p[1]) * wo + c] += 1024u;
+    out[(size_t)row(p[2]) * wo + c] += 1048576u;
+  }
 }
 
 int oracle_cfa_colour(uint32_t filters, int x, int y)

@@ -111,6 +111,11 @@ oracle_decisions_t;
  * (W x H floats, the hilite output): the grid of oracle_decisions_t.gauss */
 void oracle_gauss_decisions(const float *mosaic, int wd, int ht, uint32_t filters, uint8_t *dec, float *margin);
 
+/* the seeded synthetic mosaic of the benchmarks (the recipe the library generates
+ * on the device; wd x ht u16 raw DN values) */
+void oracle_scene(int wd, int ht, uint32_t seed, uint32_t image_id, uint32_t filters, float black, float white,
+    float noise_a, float noise_b, const float wb[3], float pan_x, float pan_y, uint16_t *out);
+
 /* the default parameters of the six modules plus the darkroom .cfg values
  * (bin/default-darkroom.i-raw:28-32) */
 void oracle_default_params(oracle_params_t *p);
@@ -125,12 +130,21 @@ int oracle_develop_dec_f32(const uint16_t *mosaic, int wd, int ht,
     const oracle_img_param_t *ip, const oracle_params_t *p, oracle_stages_t *out, oracle_decisions_t *dec);
 int oracle_develop_dec_f64(const uint16_t *mosaic, int wd, int ht,
     const oracle_img_param_t *ip, const oracle_params_t *p, oracle_stages_t *out, oracle_decisions_t *dec);
+/* FP32, the path from a given stage on: start 1 hilite (input: the denoise output,
+ * W*H), 2 demosaic (input: the hilite output, W*H), 3 colour (input: the demosaic
+ * output, rgba), 4 filmcurv (input: the colour output), 5 llap (input: the
+ * filmcurv output); the stages before it are replaced by the input (node-wise
+ * checks of another implementation's stages on its own inputs) */
+int oracle_develop_from_f32(const uint16_t *mosaic, int wd, int ht, const oracle_img_param_t *ip,
+    const oracle_params_t *p, oracle_stages_t *out, oracle_decisions_t *dec, int start, const float *input);
 
 /* single-node entry points for unit tests */
 /* denoise/noop.comp on the whole mosaic -> W*H normalised f16 values */
 void oracle_noop(const uint16_t *mosaic, int wd, int ht, const oracle_img_param_t *ip, float *out);
 /* OpenDRT/hist.comp over an rgba image (float values, already f16) */
 void oracle_hist(const float *rgba, int wd, int ht, uint32_t *hist257);
+/* hist/collect.comp: the rgb waveform of an rgba image (float values, already f16) into wo x ho u32 */
+void oracle_waveform(const float *rgba, int wd, int ht, int wo, int ho, uint32_t *out);
 /* the bin index the histogram assigns to a luminance (bit exact with the kernel) */
 uint32_t oracle_hist_bin(float r, float g, float b);
 /* rawhist/collect.comp statistics: out = counts, sums of means, sums of second moments (3*bins) */

@@ -28,7 +28,7 @@ def test_token_packing():
 
 def test_supports():
     for n, k in [("denoise", "noop"), ("hilite", "reduce"), ("demosaic", "splat"), ("demosaic", "rcd_fill"),
-                 ("llap", "assemble"), ("OpenDRT", "hist")]:
+                 ("llap", "assemble"), ("OpenDRT", "hist"), ("hist", "collect")]:
         assert v.supports(n, k)
     assert not v.supports("crop", "main")
     assert not v.supports("resize", "main")

@@ -151,6 +151,13 @@ def rawhist(d_mosaic, wd, ht, img_param, bins=1000, d_scratch=None, stream=0):
     return out.reshape(3, bins)
 
 
+def waveform(d_rgba_f16, wd, ht, d_out_u32, out_wd=1000, out_ht=600, stream=0):
+    """vkdt_cuda_waveform_rgba_f16: the hist module's rgb waveform (hist/collect.comp) of a
+    device rgba f16 image into a device u32 image of out_wd x out_ht."""
+    check(_lib.lib().vkdt_cuda_waveform_rgba_f16(C.c_void_p(d_rgba_f16), wd, ht, C.c_void_p(d_out_u32), out_wd, out_ht,
+                                                 C.c_void_p(stream)), "waveform")
+
+
 def nprof_fit(hist):
     """vkdt_cuda_nprof_fit: the noise profile (a, b) of a rawhist histogram (nprof module)."""
     h = np.ascontiguousarray(np.asarray(hist, np.float64).reshape(-1))

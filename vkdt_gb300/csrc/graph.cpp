@@ -779,7 +779,7 @@ int vkdt_cuda_supports(dt_token_t name, dt_token_t kernel)
     { "hilite", "half" }, { "hilite", "reduce" }, { "hilite", "assemble" }, { "hilite", "doub" },
     { "demosaic", "down" }, { "demosaic", "gauss" }, { "demosaic", "splat" }, { "demosaic", "fix" },
     { "demosaic", "rcd_conv" }, { "demosaic", "rcd_fill" },
-    { "colour", "main" }, { "filmcurv", "main" }, { "OpenDRT", "hist" },
+    { "colour", "main" }, { "filmcurv", "main" }, { "OpenDRT", "hist" }, { "hist", "collect" },
     { "llap", "curve" }, { "llap", "reduce" }, { "llap", "assemble" }, { "llap", "colour" } };
   for(auto &s : sup) if(tkn(s[0]) == name && tkn(s[1]) == kernel) return 1;
   return 0;
@@ -1486,6 +1486,16 @@ int vkdt_cuda_hist_rgba_f16(const void *d_rgba, int wd, int ht, uint32_t *d_hist
   return 0;
 }
 
+int vkdt_cuda_waveform_rgba_f16(const void *d_rgba, int wd, int ht, uint32_t *d_out, int out_wd, int out_ht, void *stream)
+{
+  if(!d_rgba || !d_out || wd <= 0 || ht <= 0 || out_wd <= 0 || out_ht <= 0)
+    return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "bad waveform arguments");
+  if(((uintptr_t)d_rgba & 7) || ((uintptr_t)d_out & 3))
+    return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "waveform: unaligned buffer");
+  CU(launch_waveform((const half4 *)d_rgba, wd, ht, d_out, out_wd, out_ht, (cudaStream_t)stream));
+  return 0;
+}
+
 int vkdt_cuda_graph_debug_stage(vkdt_cuda_graph_t *g, int stage, float *out, size_t count)
 {
   if(!g || !g->allocated) return fail(VKDT_CUDA_INCOMPLETE, "graph not allocated");
@@ -1699,45 +1709,8 @@ int vkdt_cuda_nprof_fit(const double *h, int wd, float *a_out, float *b_out)
 
 static void scene_layout(const vkdt_cuda_scene_t *sc, scene_layout_t *s)
 {
-  memset(s, 0, sizeof(*s));
-  s->wd = sc->wd; s->ht = sc->ht; s->seed = sc->seed; s->image_id = sc->image_id; s->filters = sc->filters;
-  s->black = sc->black; s->white = sc->white; s->noise_a = sc->noise_a; s->noise_b = sc->noise_b;
-  for(int k = 0; k < 3; k++) s->iwb[k] = 1.0f / sc->wb[k];
-  s->pan_x = sc->pan_x; s->pan_y = sc->pan_y;
-  scene_rng_t r;
-  rng_init(&r, sc->seed, sc->image_id, 0xA11CEu, 0x5CE4Eu);
-  const float W = (float)sc->wd, H = (float)sc->ht;
-  for(int c = 0; c < 3; c++)
-  {
-    s->grad[c][0] = 0.05f + 0.55f * rng_next(&r);
-    for(int k = 1; k < 6; k++) s->grad[c][k] = 0.4f * (rng_next(&r) - 0.5f);
-  }
-  for(int i = 0; i < SCENE_NRECT; i++)
-  {
-    const float w = (0.02f + 0.23f * rng_next(&r)) * W, h = (0.02f + 0.23f * rng_next(&r)) * W;
-    const float x0 = rng_next(&r) * (W - w), y0 = rng_next(&r) * fmaxf(H - h, 1.0f);
-    float *q = s->rect[i];
-    q[0] = x0; q[1] = y0; q[2] = x0 + w; q[3] = y0 + h;
-    for(int c = 0; c < 3; c++) q[4 + c] = 0.02f + 0.93f * rng_next(&r);
-  }
-  for(int i = 0; i < SCENE_NGRAT; i++)
-  {
-    const float w = (0.05f + 0.2f * rng_next(&r)) * W, h = (0.05f + 0.2f * rng_next(&r)) * H;
-    const float x0 = rng_next(&r) * (W - w), y0 = rng_next(&r) * (H - h);
-    float *q = s->grat[i];
-    q[0] = x0; q[1] = y0; q[2] = x0 + w; q[3] = y0 + h;
-    q[4] = 0.05f + 0.4f * rng_next(&r);
-    const float th = 6.28318530718f * rng_next(&r);
-    q[5] = cosf(th); q[6] = sinf(th);
-    q[7] = 6.28318530718f * rng_next(&r);
-    q[8] = 0.1f + 0.4f * rng_next(&r);
-  }
-  // brightest 10% of the scene luminance on a coarse sample
-  std::vector<float> lum;
-  for(int j = 0; j < 96; j++) for(int i = 0; i < 96; i++)
-    lum.push_back(scene_luma(s, (i + 0.5f) / 96.0f * W + s->pan_x, (j + 0.5f) / 96.0f * H + s->pan_y));
-  std::sort(lum.begin(), lum.end());
-  s->clip_thr = lum[(size_t)(0.9 * lum.size())];
+  scene_layout_make(s, sc->wd, sc->ht, sc->seed, sc->image_id, sc->filters, sc->black, sc->white, sc->noise_a,
+                    sc->noise_b, sc->wb, sc->pan_x, sc->pan_y);
 }
 
 int vkdt_cuda_scene_generate(const vkdt_cuda_scene_t *sc, void *d_mosaic, void *stream)

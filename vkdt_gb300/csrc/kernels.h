@@ -237,6 +237,8 @@ cudaError_t init_llap();      // function attributes, once per device (from init
 struct scene_layout_t;
 cudaError_t launch_scene(const scene_layout_t *d_layout, int wd, int ht, uint16_t *out, cudaStream_t s);
 cudaError_t launch_hist_rgba(const half4 *in, int W, int H, uint32_t *hist, cudaStream_t s);
+// hist/collect.comp: the rgb waveform of an rgba f16 image into a cleared wo x ho u32 image
+cudaError_t launch_waveform(const half4 *in, int W, int H, uint32_t *out, int wo, int ho, cudaStream_t s);
 // k_static.cu: the fixed scratch of vkdt_cuda_graph_develop_static (address on the current device)
 cudaError_t static_scratch_address(void **ptr);
 cudaError_t launch_noop_lut(__half *lut, float black, float white, cudaStream_t s);

@@ -173,3 +173,52 @@ SCENE_HD uint16_t scene_pixel(const scene_layout_t *s, int x, int y)
   dn = fminf(fmaxf(dn, 0.0f), s->white);
   return (uint16_t)(dn + 0.5f);
 }
+
+#if defined(__cplusplus) && !defined(__CUDA_ARCH__)
+#include <algorithm>
+// the scene of a seed (host): gradients, rectangles, gratings and the clip
+// threshold (the brightest 10% of the scene luminance on a 96x96 sample)
+static inline void scene_layout_make(scene_layout_t *s, int32_t wd, int32_t ht, uint32_t seed, uint32_t image_id,
+    uint32_t filters, float black, float white, float noise_a, float noise_b, const float wb[3], float pan_x, float pan_y)
+{
+  *s = scene_layout_t();
+  s->wd = wd; s->ht = ht; s->seed = seed; s->image_id = image_id; s->filters = filters;
+  s->black = black; s->white = white; s->noise_a = noise_a; s->noise_b = noise_b;
+  for(int k = 0; k < 3; k++) s->iwb[k] = 1.0f / wb[k];
+  s->pan_x = pan_x; s->pan_y = pan_y;
+  scene_rng_t r;
+  rng_init(&r, seed, image_id, 0xA11CEu, 0x5CE4Eu);
+  const float W = (float)wd, H = (float)ht;
+  for(int c = 0; c < 3; c++)
+  {
+    s->grad[c][0] = 0.05f + 0.55f * rng_next(&r);
+    for(int k = 1; k < 6; k++) s->grad[c][k] = 0.4f * (rng_next(&r) - 0.5f);
+  }
+  for(int i = 0; i < SCENE_NRECT; i++)
+  {
+    const float w = (0.02f + 0.23f * rng_next(&r)) * W, h = (0.02f + 0.23f * rng_next(&r)) * W;
+    const float x0 = rng_next(&r) * (W - w), y0 = rng_next(&r) * fmaxf(H - h, 1.0f);
+    float *q = s->rect[i];
+    q[0] = x0; q[1] = y0; q[2] = x0 + w; q[3] = y0 + h;
+    for(int c = 0; c < 3; c++) q[4 + c] = 0.02f + 0.93f * rng_next(&r);
+  }
+  for(int i = 0; i < SCENE_NGRAT; i++)
+  {
+    const float w = (0.05f + 0.2f * rng_next(&r)) * W, h = (0.05f + 0.2f * rng_next(&r)) * H;
+    const float x0 = rng_next(&r) * (W - w), y0 = rng_next(&r) * (H - h);
+    float *q = s->grat[i];
+    q[0] = x0; q[1] = y0; q[2] = x0 + w; q[3] = y0 + h;
+    q[4] = 0.05f + 0.4f * rng_next(&r);
+    const float th = 6.28318530718f * rng_next(&r);
+    q[5] = cosf(th); q[6] = sinf(th);
+    q[7] = 6.28318530718f * rng_next(&r);
+    q[8] = 0.1f + 0.4f * rng_next(&r);
+  }
+  static const int NS = 96;
+  float lum[NS * NS];
+  for(int j = 0; j < NS; j++) for(int i = 0; i < NS; i++)
+    lum[j * NS + i] = scene_luma(s, (i + 0.5f) / NS * W + s->pan_x, (j + 0.5f) / NS * H + s->pan_y);
+  std::sort(lum, lum + NS * NS);
+  s->clip_thr = lum[(size_t)(0.9 * NS * NS)];
+}
+#endif

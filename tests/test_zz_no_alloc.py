@@ -48,7 +48,8 @@ def test_static_develop_matches_allocated_twice(gpu, wd, ht):
             if call == 1:
                 # the defining property: the call takes no device memory (the first call may
                 # load the module's kernels; the second runs the same kernels again)
-                assert torch.cuda.mem_get_info()[0] == free0 and torch.cuda.memory_allocated() == used0
+                # (torch may free a temporary of the test meanwhile: nothing grows)
+                assert torch.cuda.mem_get_info()[0] >= free0 and torch.cuda.memory_allocated() <= used0
             got = out.float().cpu().numpy()
             assert np.isfinite(got).all(), call
             assert np.array_equal(got.astype(np.float16).view(np.uint16), want.astype(np.float16).view(np.uint16)), call

@@ -34,7 +34,9 @@ def build(force=False):
 
 REF_DIR = os.path.join(HERE, "_ref")
 STB_SO = os.path.join(REF_DIR, "libstb_dxt.so")
-STB_SRC = "/root/reference/src/pipe/modules/o-bc1"
+# the vkdt source tree the reference builds read (VKDT_REFERENCE, default: where this build found it)
+VKDT_TREE = os.environ.get("VKDT_REFERENCE", "/root/reference")
+STB_SRC = os.path.join(VKDT_TREE, "src", "pipe", "modules", "o-bc1")
 
 
 def build_stb_ref():

@@ -17,7 +17,8 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(os.path.dirname(HERE), "_ref")
-DEFAULT_MODULES = "/root/reference/src/pipe/modules"
+# the vkdt source tree (VKDT_REFERENCE, default: where this build found it)
+DEFAULT_MODULES = os.path.join(os.environ.get("VKDT_REFERENCE", "/root/reference"), "src", "pipe", "modules")
 
 # (module, kernel) of the development path
 SHADERS = [

@@ -15,7 +15,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF = os.path.join(HERE, "_ref")
 SO = os.path.join(REF, "libvkdt_ref.so")
-MODULES = "/root/reference/src/pipe/modules"
+# the vkdt source tree (VKDT_REFERENCE, default: where this build found it)
+MODULES = os.path.join(os.environ.get("VKDT_REFERENCE", "/root/reference"), "src", "pipe", "modules")
 
 F16, F32, UNORM16 = 0, 1, 2
 

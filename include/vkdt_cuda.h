@@ -327,7 +327,9 @@ int  vkdt_cuda_nprof_fit(const double *hist, int bins, float *a, float *b);
 /* debug: copy an intermediate image of the last run to host floats.
  * stage 0 denoise output (1 ch), 1 hilite output (1 ch), both at the crop size;
  * 2 filmcurv output, 3 demosaic output and 4 colour output (4 ch each), at
- * the output size. These are the images the reference's `-d perf` graph
+ * the output size; with the wavelet denoise, its half size nodes (4 ch,
+ * W/block x H/block): 5 half, 6 downcov, 7..9 down levels 1..3 (swizzled as
+ * denoise/down.comp:102-104 stores them), 10 assemble. These are the images the reference's `-d perf` graph
  * would hold on those nodes' output connectors (graph.c:881-932).
  * requires vkdt_cuda_graph_set_debug(graph, 1) before alloc. */
 int  vkdt_cuda_graph_set_debug(vkdt_cuda_graph_t *graph, int enable);

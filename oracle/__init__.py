@@ -149,6 +149,10 @@ def lib():
         for f in (l.oracle_develop_f32, l.oracle_develop_f64):
             f.restype = C.c_int
             f.argtypes = [C.POINTER(C.c_uint16), C.c_int, C.c_int, C.POINTER(ImgParam), C.POINTER(Params), C.POINTER(Stages)]
+        l.oracle_set_perturb.argtypes = [C.c_uint32]
+        l.oracle_denoise_nodes.restype = C.c_int
+        l.oracle_denoise_nodes.argtypes = [C.POINTER(C.c_uint16), C.c_int, C.c_int, C.POINTER(ImgParam),
+                                           C.POINTER(Params), C.c_void_p * 6, C.c_void_p * 7, C.POINTER(Decisions)]
         l.oracle_develop_from_f32.restype = C.c_int
         l.oracle_develop_from_f32.argtypes = [C.POINTER(C.c_uint16), C.c_int, C.c_int, C.POINTER(ImgParam),
                                               C.POINTER(Params), C.POINTER(Stages), C.POINTER(Decisions), C.c_int,
@@ -207,7 +211,7 @@ START = {"hilite": 1, "demosaic": 2, "colour": 3, "filmcurv": 4, "llap": 5}
 
 
 def develop(mosaic, ip, params=None, double=False, stages=("llap",), record=False, force=None, start=None,
-            input=None):
+            input=None, perturb=0):
     """Run the oracle on a u16 mosaic; returns a dict of the requested stage images.
 
     record: also return the oracle's own discrete decisions and their margins
@@ -215,7 +219,8 @@ def develop(mosaic, ip, params=None, double=False, stages=("llap",), record=Fals
     graph has). force: {kind: array} decisions applied in place of the
     oracle's own (the grids of vkdt_cuda_graph_debug_decisions). start, input:
     run the path from stage `start` (a key of START) on `input`, the output of
-    the stage before it (FP32 only)."""
+    the stage before it (FP32 only). perturb: a nonzero seed rounds every f16
+    store to a neighbouring f16 value at random (a sensitivity run)."""
     mosaic = np.ascontiguousarray(mosaic, dtype=np.uint16)
     ht, wd = mosaic.shape
     params = params or default_params()
@@ -236,6 +241,14 @@ def develop(mosaic, ip, params=None, double=False, stages=("llap",), record=Fals
             st.hist = bufs[name].ctypes.data_as(C.POINTER(C.c_uint32))
         else:
             setattr(st, name, _fptr(bufs[name]))
+    lib().oracle_set_perturb(int(perturb))
+    try:
+        return _develop(mosaic, ip, params, double, stages, record, force, start, input, W, H, ht, wd, st, bufs)
+    finally:
+        lib().oracle_set_perturb(0)
+
+
+def _develop(mosaic, ip, params, double, stages, record, force, start, input, W, H, ht, wd, st, bufs):
     if start is not None:
         if double:
             raise ValueError("the path from a stage runs on the FP32 build")
@@ -277,6 +290,37 @@ def develop(mosaic, ip, params=None, double=False, stages=("llap",), record=Fals
     bufs["llap_levels"] = st.llap_levels
     bufs["hilite_levels"] = st.hilite_levels
     return bufs
+
+
+DENOISE_NODES = ("half", "downcov", "down1", "down2", "down3", "assemble")
+
+
+def denoise_nodes(mosaic, ip, params, inputs, force=None):
+    """The wavelet denoise node by node on given inputs (a dict of DENOISE_NODES
+    images, hw x hh x 4): each node's output from its inputs in `inputs`,
+    plus "doub" (the denoised mosaic, W x H)."""
+    mosaic = np.ascontiguousarray(mosaic, np.uint16)
+    ht, wd = mosaic.shape
+    ins = [np.ascontiguousarray(inputs[n], np.float32) for n in DENOISE_NODES]
+    hh, hw = ins[0].shape[:2]
+    W = ip.crop_aabb[2] - ip.crop_aabb[0]
+    H = ip.crop_aabb[3] - ip.crop_aabb[1]
+    outs = [np.zeros((hh, hw, 4), np.float32) for _ in DENOISE_NODES] + [np.zeros((H, W), np.float32)]
+    dec = Decisions()
+    keep = []
+    for kind, arr in (force or {}).items():
+        a = np.ascontiguousarray(arr, DECISION_KINDS[kind][0])
+        keep.append(a)
+        setattr(dec, kind + "_force", a.ctypes.data)
+    pin = (C.c_void_p * 6)(*[a.ctypes.data for a in ins])
+    pout = (C.c_void_p * 7)(*[a.ctypes.data for a in outs])
+    r = lib().oracle_denoise_nodes(mosaic.ctypes.data_as(C.POINTER(C.c_uint16)), wd, ht, C.byref(ip), C.byref(params),
+                                   pin, pout, C.byref(dec))
+    if r:
+        raise RuntimeError("oracle denoise nodes failed with %d" % r)
+    res = dict(zip(DENOISE_NODES, outs[:6]))
+    res["doub"] = outs[6]
+    return res
 
 
 def scene(wd, ht, seed=0, image_id=0, filters=0x94949494, black=512.0, white=16383.0, a=2.0, b=0.4,

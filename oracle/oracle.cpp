@@ -41,9 +41,41 @@ namespace {
 
 // ------------------------------------------------------------------ helpers
 
+// Sensitivity runs: with a nonzero seed every f16 store rounds to one of the
+// two neighbouring f16 values at random (a hash of the value and the seed)
+// instead of to the nearest: a perturbation of at most one f16 step at every
+// stored intermediate, in the manner of discrete stochastic arithmetic (J.
+// Vignes, "A stochastic arithmetic for reliable scientific computation",
+// Math. Comput. Simul. 35, 1993). How far such runs move a result measures
+// how much precision the f16 storage of the path leaves it.
+static uint32_t g_perturb = 0;
+
+static inline uint32_t perturb_bit(double v)
+{
+  uint64_t x;
+  memcpy(&x, &v, 8);
+  x ^= (uint64_t)g_perturb * 0x9E3779B97F4A7C15ull;
+  x ^= x >> 30; x *= 0xBF58476D1CE4E5B9ull;
+  x ^= x >> 27; x *= 0x94D049BB133111EBull;
+  x ^= x >> 31;
+  return (uint32_t)(x & 1);
+}
+
 template<class T> static inline T f16r(T v)
 { // round to IEEE binary16, round to nearest even, and back
   if(std::isnan(v)) return v;
+  if(g_perturb)
+  { // stochastic rounding between the neighbouring f16 values (normal range; see g_perturb)
+    const T a = std::fabs(v);
+    if(a >= T(6.103515625e-05) && a < T(65504.0))
+    {
+      int e;
+      const T f = std::frexp(a, &e);
+      const T x = std::ldexp(f, 11), lo = std::floor(x);
+      const T m = (x == lo) ? lo : lo + T(perturb_bit((double)v));
+      return std::copysign(std::ldexp(m, e - 11), v);
+    }
+  }
   T a = std::fabs(v);
   if(std::isinf(a)) return v;
   if(a >= T(65520.0)) return std::copysign(T(INFINITY), v);
@@ -2323,6 +2355,52 @@ int oracle_develop_dec_f32(const uint16_t *mosaic, int wd, int ht,
   const int r = develop<float>(mosaic, wd, ht, ip, p, out);
   g_dec = nullptr;
   return r;
+}
+
+void oracle_set_perturb(uint32_t seed) { g_perturb = seed; }
+
+// the wavelet denoise node by node, each node on the given inputs (another
+// implementation's half image, levels and assemble output, hw x hh rgba
+// each): out = half (from the mosaic), downcov(in half), down l (in level
+// l-1), assemble (in half, in levels), doub (mosaic, in assemble, in half)
+int oracle_denoise_nodes(const uint16_t *mosaic, int wd, int ht, const oracle_img_param_t *ip,
+    const oracle_params_t *p, const float *const in[6], float *const out[7], oracle_decisions_t *dec)
+{
+  if(!mosaic || !ip || !p || p->dn_strength <= 0.0f || ip->filters == 0) return 1;
+  img_t<float> raw(wd, ht, 1);
+  for(size_t i = 0; i < (size_t)wd * ht; i++) raw.d[i] = float(mosaic[i]) / 65535.0f;
+  float black[4], white[4], wb[4];
+  for(int k = 0; k < 4; k++)
+  {
+    black[k] = ip->black[k] / 65535.0f; white[k] = ip->white[k] / 65535.0f; wb[k] = ip->whitebalance[k];
+  }
+  const int crop[4] = { (int)ip->crop_aabb[0], (int)ip->crop_aabb[1], (int)ip->crop_aabb[2], (int)ip->crop_aabb[3] };
+  const int W = crop[2] - crop[0], H = crop[3] - crop[1];
+  const int block = ip->filters == 9u ? 3 : 2;
+  const int hw = W / block, hh = H / block;
+  const float edges[4] = { p->dn_edges[0], p->dn_edges[1], p->dn_edges[2], p->dn_edges[3] };
+  const int zc[4] = { 0, 0, 0, 0 };
+  g_dec = dec;
+  img_t<float> s[5];
+  for(int i = 0; i < 5; i++) s[i] = from_float<float>(in[i], hw, hh, 4);
+  const img_t<float> as_in = from_float<float>(in[5], hw, hh, 4);
+  img_t<float> o = denoise_half(raw, hw, hh, crop, white[1], ip->filters);
+  to_float(o, out[0]);
+  o = denoise_downcov(s[0], hw, hh, zc);
+  to_float(o, out[1]);
+  for(int l = 1; l < 4; l++)
+  {
+    o = denoise_down(s[l], hw, hh, zc, black[1], white[1], ip->noise_a, ip->noise_b, edges, l, block);
+    to_float(o, out[l + 1]);
+  }
+  o = denoise_assemble(s, hw, hh, zc, wb, black, white, ip->noise_a, ip->noise_b, ip->filters, p->dn_strength,
+      p->dn_luma, edges);
+  to_float(o, out[5]);
+  o = denoise_doub(raw, as_in, s[0], W, H, crop, black, white, ip->filters, ip->noise_a, ip->noise_b,
+      p->dn_strength, p->dn_luma, p->dn_detail, edges);
+  to_float_ch(o, 1, out[6]);
+  g_dec = nullptr;
+  return 0;
 }
 
 int oracle_develop_from_f32(const uint16_t *mosaic, int wd, int ht, const oracle_img_param_t *ip,

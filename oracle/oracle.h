@@ -130,6 +130,17 @@ int oracle_develop_dec_f32(const uint16_t *mosaic, int wd, int ht,
     const oracle_img_param_t *ip, const oracle_params_t *p, oracle_stages_t *out, oracle_decisions_t *dec);
 int oracle_develop_dec_f64(const uint16_t *mosaic, int wd, int ht,
     const oracle_img_param_t *ip, const oracle_params_t *p, oracle_stages_t *out, oracle_decisions_t *dec);
+/* sensitivity runs: 0 off (round to nearest); else every f16 store of the
+ * following develop calls rounds to a neighbouring f16 value chosen by a hash
+ * of the value and this seed (at most one f16 step) */
+void oracle_set_perturb(uint32_t seed);
+/* the wavelet denoise node by node on another implementation's inputs (FP32):
+ * in = half, downcov, down 1..3, assemble (W/block x H/block rgba each, levels
+ * swizzled as stored); out = half (from the mosaic), downcov of in half, down
+ * l of in level l-1, assemble of in half and levels, (W/block x H/block rgba),
+ * doub of the mosaic, in assemble and in half (W x H). dec forces decisions. */
+int oracle_denoise_nodes(const uint16_t *mosaic, int wd, int ht, const oracle_img_param_t *ip,
+    const oracle_params_t *p, const float *const in[6], float *const out[7], oracle_decisions_t *dec);
 /* FP32, the path from a given stage on: start 1 hilite (input: the denoise output,
  * W*H), 2 demosaic (input: the hilite output, W*H), 3 colour (input: the demosaic
  * output, rgba), 4 filmcurv (input: the colour output), 5 llap (input: the

@@ -174,3 +174,46 @@ def test_oracle_matches_reference_shaders_random(seed):
     for s in st:
         x, y = (a[s], b[s]) if a[s].ndim == 2 else (a[s][..., :3], b[s][..., :3])
         assert np.array_equal(x, y), (seed, wd, ht, s)
+
+
+def test_denoise_nodes_chain_equals_develop():
+    # the node-by-node entry fed with its own outputs reproduces the wavelet denoise of the develop
+    import vkdt_gb300 as v
+    wd, ht = 256, 192
+    m = oracle.scene(wd, ht, seed=3, a=8.0, b=1.6)
+    ip = oracle.img_param(v.default_img_param(wd=wd, ht=ht, noise_a=8.0 / 15871 ** 2, noise_b=1.6 / 15871))
+    op = oracle.default_params()
+    op.dn_strength = 1.0
+    want = oracle.develop(m, ip, params=op, stages=("denoise",))["denoise"]
+    ins = {n: np.zeros((ht // 2, wd // 2, 4), np.float32) for n in oracle.DENOISE_NODES}
+    for _ in range(len(oracle.DENOISE_NODES) + 1):
+        got = oracle.denoise_nodes(m, ip, op, ins)
+        ins = {n: got[n] for n in oracle.DENOISE_NODES}
+    assert np.array_equal(got["doub"], want)
+
+
+def test_stage_injection_reproduces_the_path():
+    # the path from each stage on, fed with the oracle's own stage outputs, is the path
+    import vkdt_gb300 as v
+    wd, ht = 256, 192
+    m = oracle.scene(wd, ht, seed=4)
+    ip = oracle.img_param(v.default_img_param(wd=wd, ht=ht))
+    st = ("denoise", "hilite", "demosaic", "colour", "filmcurv", "llap")
+    r = oracle.develop(m, ip, stages=st)
+    for s, prev in zip(st[1:], st[:-1]):
+        q = oracle.develop(m, ip, stages=(s, "llap"), start=s, input=r[prev])
+        assert np.array_equal(q[s], r[s]) and np.array_equal(q["llap"], r["llap"]), s
+
+
+def test_sensitivity_runs_move_values_by_one_f16_step():
+    # a perturbed run rounds stores to a neighbouring f16 value: the denoise/noop output moves by at most one step
+    import vkdt_gb300 as v
+    wd, ht = 128, 96
+    m = oracle.scene(wd, ht, seed=5)
+    ip = oracle.img_param(v.default_img_param(wd=wd, ht=ht))
+    a = oracle.develop(m, ip, stages=("denoise",))["denoise"]
+    b = oracle.develop(m, ip, stages=("denoise",), perturb=7)["denoise"]
+    c = oracle.develop(m, ip, stages=("denoise",))["denoise"]
+    assert np.array_equal(a, c)                       # the perturbation is off again
+    step = np.abs(np.spacing(a.astype(np.float16)).astype(np.float32))
+    assert (np.abs(b - a) <= step * 1.0001).all() and (b != a).any()

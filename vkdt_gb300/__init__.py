@@ -222,6 +222,7 @@ class Graph:
         self.wd, self.ht = wd, ht
         b = img_param.crop_aabb   # the denoise output: the crop window
         self.crop_wd, self.crop_ht = int(b[2] - b[0]), int(b[3] - b[1])
+        self._filters = int(img_param.filters)
         check(self._l.vkdt_cuda_graph_set_input(self._g, wd, ht, C.byref(img_param)), "set_input")
 
     def set_llap_levels(self, n):
@@ -317,14 +318,18 @@ class Graph:
 
     def debug_stage(self, stage):
         """0 denoise, 1 hilite (crop size, one channel); 2 filmcurv, 3 demosaic,
-        4 colour (output size, rgba)."""
+        4 colour (output size, rgba); wavelet denoise nodes (half size, rgba):
+        5 half, 6 downcov, 7..9 down levels 1..3, 10 assemble."""
         if stage in (2, 3, 4):
             out = np.empty((self.out_ht, self.out_wd, 4), np.float32)
+        elif stage >= 5:
+            block = 3 if self._filters == 9 else 2
+            out = np.empty((self.crop_ht // block, self.crop_wd // block, 4), np.float32)
         else:
             out = np.empty((self.crop_ht, self.crop_wd, 1), np.float32)
         check(self._l.vkdt_cuda_graph_debug_stage(self._g, stage, out.ctypes.data_as(C.POINTER(C.c_float)), out.size),
               "debug_stage")
-        return out if stage in (2, 3, 4) else out[..., 0]
+        return out if stage >= 2 else out[..., 0]
 
     DECISIONS = {"gauss": (0, np.uint8), "dn_cov": (1, np.uint32), "dn_thr": (2, np.uint8)}
 

@@ -1512,6 +1512,17 @@ int vkdt_cuda_graph_debug_stage(vkdt_cuda_graph_t *g, int stage, float *out, siz
     for(size_t i = 0; i < npx; i++) out[i] = __half2float(h[i]);
     return 0;
   }
+  if(stage >= 5 && stage <= 10)
+  { // the wavelet denoise's half size images: half, downcov, down 1..3 (swizzled as the reference stores them), assemble
+    if(!g->debug || !g->wavelet) return fail(VKDT_CUDA_INCOMPLETE, "no wavelet denoise debug stages");
+    const size_t nh = (size_t)g->hw * g->hh;
+    if(count < nh * 4) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "buffer too small");
+    const size_t off = stage == 5 ? g->off_dnh : stage == 10 ? g->off_dna : g->off_dnl[stage - 6];
+    std::vector<__half> h(nh * 4);
+    CU(cudaMemcpy(h.data(), g->arena + off, nh * 8, cudaMemcpyDeviceToHost));
+    for(size_t i = 0; i < nh * 4; i++) out[i] = __half2float(h[i]);
+    return 0;
+  }
   if(stage == 2 || stage == 3 || stage == 4)
   {
     if(stage != 2 && !g->debug) return fail(VKDT_CUDA_INCOMPLETE, "debug stages not enabled");

@@ -127,6 +127,39 @@ int  vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *graph);
  * (dt_graph_run_modules + dt_graph_run_nodes_allocate, src/pipe/graph.c:747-806).
  * *device_bytes (may be 0) receives the bytes allocated. */
 int  vkdt_cuda_graph_alloc(vkdt_cuda_graph_t *graph, uint64_t *device_bytes);
+/* one node as the reference's scheduler holds it after the modules' create_nodes
+ * and commit_params (dt_node_t, src/pipe/node.h:19-52), with its module's uniform
+ * block (committed_param, or param where the module commits none, as
+ * dt_graph_run_modules_upload_uniforms copies it, src/pipe/graph-run-modules.h:20-28) */
+typedef struct vkdt_cuda_node_desc_t
+{
+  dt_token_t  name, kernel;    /* module directory and kernel (node.h: name, kernel) */
+  int32_t     wd, ht, dp;      /* dispatch size (node.h: wd, ht, dp) */
+  uint32_t    push_size;       /* node.h: push_constant_size (at most 256) */
+  const void *push;            /* node.h: push_constant */
+  uint32_t    uniform_size;    /* the module's uniform block size */
+  const void *uniform;         /* the module's uniform block (std140 params_t) */
+}
+vkdt_cuda_node_desc_t;
+
+/* the module layer's output in place of the library's own: replaces
+ * dt_graph_run_nodes_record_cmd (src/pipe/graph.c:819) for the nodes of
+ * denoise -> hilite -> demosaic -> colour -> filmcurv -> llap. in_wd x in_ht is
+ * the i-raw output; nodes are the scheduler's nodes of those modules after
+ * create_nodes and commit_params (any order; other modules' nodes absent).
+ * The library reads the image metadata from the push constants (crop,
+ * black/white, white balance, CFA, noise profile) and the module parameters
+ * from the uniform blocks (colour's committed white balance multipliers,
+ * exposure and camera matrix as they are), plans its fused launches, and
+ * checks that they compute exactly these nodes: the same (name, kernel, wd,
+ * ht, dp) multiset, apart from a shared:resample node at its input's size
+ * (the identity the library folds away) and filmcurv's display node.
+ * VKDT_CUDA_INCOMPLETE when the nodes are a chain the library does not run
+ * (the caller keeps the reference's own device path for them). Then alloc and
+ * run as after vkdt_cuda_graph_create_nodes. */
+int  vkdt_cuda_graph_set_nodes(vkdt_cuda_graph_t *graph, int in_wd, int in_ht, const vkdt_cuda_node_desc_t *nodes,
+    int count);
+
 /* the node list create_nodes produced (for inspection and per-node timing) */
 int  vkdt_cuda_graph_node_count(vkdt_cuda_graph_t *graph);
 int  vkdt_cuda_graph_node(vkdt_cuda_graph_t *graph, int i, vkdt_cuda_node_info_t *info);

@@ -1,0 +1,133 @@
+"""The boundary against the reference's own module host code.
+
+tests/golden/nodes.json holds what the reference's denoise, hilite, demosaic,
+colour, filmcurv and llap main.c (compiled unmodified from the vkdt tree,
+oracle/modules) emit for a set of graphs: every node with its push constants
+and its module's uniform block, after create_nodes and commit_params. These
+tests hold the library to it on the CPU: its own create_nodes gives the same
+nodes (name, kernel, wd, ht, dp), and vkdt_cuda_graph_set_nodes takes the
+reference's nodes as they are, with the parameters the cfg path derives. The
+GPU test develops through both and compares the results bit for bit."""
+import collections
+import os
+import sys
+
+import numpy as np
+import pytest
+
+import vkdt_gb300 as v
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+import make_nodes as MN   # noqa: E402
+
+CASES = MN.load()
+SKIP = {("filmcurv", "dspy")}   # filmcurv's display curve: not on the path
+
+
+def ref_multiset(case, W, H):
+    c = collections.Counter()
+    for n in case["nodes"]:
+        if (n["name"], n["kernel"]) in SKIP:
+            continue
+        if (n["name"], n["kernel"]) == ("shared", "resample") and (n["wd"], n["ht"]) == (W, H):
+            continue   # the demosaic output resampled to its own size: the identity
+        c[(n["name"], n["kernel"], n["wd"], n["ht"], n["dp"])] += 1
+    return c
+
+
+def cfg_graph(case):
+    wd, ht = case["in"]
+    g = v.Graph(case["cfg"])
+    g.set_input(wd, ht, MN.case_ip(wd, ht, case["filters"]))
+    if case["out"][0]:
+        g.set_output_size(*case["out"])
+    return g
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_create_nodes_matches_the_reference_modules(name):
+    case = CASES[name]
+    with cfg_graph(case) as g:
+        g.create_nodes()
+        ours = collections.Counter((n[0], n[1], n[2], n[3], n[4]) for n in g.nodes())
+    wd, ht = case["in"]
+    assert ours == ref_multiset(case, wd, ht), (dict(ours - ref_multiset(case, wd, ht)),
+                                                dict(ref_multiset(case, wd, ht) - ours))
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_set_nodes_takes_the_reference_nodes(name):
+    case = CASES[name]
+    wd, ht = case["in"]
+    with v.Graph(None) as g, cfg_graph(case) as c:
+        g.set_nodes(wd, ht, case["nodes"])
+        c.create_nodes()
+        assert sorted(g.nodes()) == sorted(c.nodes())
+        for mod, pars in (("denoise", ("strength", "luma", "detail")), ("hilite", ("white", "desat", "soft")),
+                          ("filmcurv", ("light", "contrast", "bias")), ("llap", ("sigma", "shadows", "hilights", "clarity"))):
+            for p in pars:
+                assert np.array_equal(g.get_param(mod, p), c.get_param(mod, p)), (mod, p)
+        for p in ("colour", "method"):
+            assert np.array_equal(g.get_param("demosaic", p, dtype=np.int32), c.get_param("demosaic", p, dtype=np.int32))
+
+
+def test_colour_white_written_back_as_the_reference():
+    # colour/main.c:241-253 derives the white from the camera matrix and writes it back into the params
+    case = CASES["darkroom_2048x1536"]
+    with cfg_graph(case) as g:
+        g.create_nodes()
+        ours = g.get_param("colour", "white", count=4)[:3]
+    ref = np.frombuffer(case["modules"]["colour"], np.float32)
+    # the params file order: exposure sat picked matrix gamut clip clipmax temp white[4] ...
+    assert np.array_equal(ours, ref[8:11])
+
+
+def test_unsupported_chains_return_incomplete():
+    case = CASES["darkroom_2048x1536"]
+    wd, ht = case["in"]
+    nodes = [dict(n) for n in case["nodes"]]
+    # a colour block asking for saturation 0.5: not on the CUDA path
+    for n in nodes:
+        if n["name"] == "colour":
+            u = bytearray(n["uniform"])
+            u[4 * 226:4 * 227] = np.float32(0.5).tobytes()
+            n["uniform"] = bytes(u)
+    with v.Graph(None) as g:
+        with pytest.raises(v._lib.VkdtError) as e:
+            g.set_nodes(wd, ht, nodes)
+        assert e.value.code == v._lib.INCOMPLETE
+    # a node the library does not compute (an extra llap level)
+    nodes = [dict(n) for n in case["nodes"]] + [dict(case["nodes"][-1], kernel="reduce", wd=2, ht=1, dp=11)]
+    with v.Graph(None) as g:
+        with pytest.raises(v._lib.VkdtError) as e:
+            g.set_nodes(wd, ht, nodes)
+        assert e.value.code == v._lib.INCOMPLETE
+
+
+def test_fixture_is_what_the_reference_modules_emit_now():
+    # where the vkdt tree is present: the committed fixture equals a fresh run of the reference's module code
+    from oracle import modules as M
+    from oracle.modules import build as MB
+    if not os.path.isdir(MB.MODULES_DIR) or not MB.build():
+        pytest.skip("no vkdt tree here")
+    for name, case in CASES.items():
+        wd, ht = case["in"]
+        nodes, mods = M.run(case["cfg"], wd, ht, MN.case_ip(wd, ht, case["filters"]), *case["out"])
+        assert [(n["name"], n["kernel"], n["wd"], n["ht"], n["dp"], n["push"]) for n in nodes] == \
+               [(n["name"], n["kernel"], n["wd"], n["ht"], n["dp"], n["push"]) for n in case["nodes"]], name
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["darkroom_2048x1536", "wavelet_1000x742", "rcd_1000x742", "thumb_2048x1536",
+                                  "xtrans_606x402", "params_384x256"])
+def test_develop_through_set_nodes_equals_cfg(gpu, name):
+    case = CASES[name]
+    wd, ht = case["in"]
+    m = v.scene_host(v.make_scene(wd, ht, seed=wd, filters=case["filters"]))
+    with v.Graph(None) as g, cfg_graph(case) as c:
+        g.set_nodes(wd, ht, case["nodes"])
+        g.alloc()
+        c.alloc()
+        a = g.run(m).copy()
+        b = c.run(m).copy()
+    assert np.array_equal(a.view(np.uint16), b.view(np.uint16))

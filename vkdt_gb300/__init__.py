@@ -241,6 +241,23 @@ class Graph:
         check(self._l.vkdt_cuda_graph_set_debug(self._g, 1 if on else 0), "set_debug")
 
     # ---- allocation and nodes
+    def set_nodes(self, in_wd, in_ht, nodes):
+        """vkdt_cuda_graph_set_nodes: the scheduler's nodes of the path's modules after
+        create_nodes and commit_params, each a dict of name, kernel, wd, ht, dp, push
+        (bytes) and uniform (bytes, its module's uniform block)."""
+        keep = []
+        arr = (_lib.NodeDesc * len(nodes))()
+        for i, n in enumerate(nodes):
+            push = C.create_string_buffer(bytes(n["push"]), max(1, len(n["push"])))
+            uni = C.create_string_buffer(bytes(n.get("uniform", b"")), max(1, len(n.get("uniform", b""))))
+            keep += [push, uni]
+            arr[i] = _lib.NodeDesc(token(n["name"]), token(n["kernel"]), n["wd"], n["ht"], n["dp"], len(n["push"]),
+                                   C.cast(push, C.c_void_p), len(n.get("uniform", b"")),
+                                   C.cast(uni, C.c_void_p) if n.get("uniform") else None)
+        check(self._l.vkdt_cuda_graph_set_nodes(self._g, in_wd, in_ht, arr, len(nodes)), "set_nodes")
+        self.wd, self.ht = in_wd, in_ht
+        return self
+
     def create_nodes(self):
         check(self._l.vkdt_cuda_graph_create_nodes(self._g), "create_nodes")
 

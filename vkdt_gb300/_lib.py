@@ -54,6 +54,12 @@ class NodeInfo(C.Structure):
     ]
 
 
+class NodeDesc(C.Structure):
+    """vkdt_cuda_node_desc_t: a scheduler node with its module's uniform block"""
+    _fields_ = [("name", C.c_uint64), ("kernel", C.c_uint64), ("wd", C.c_int32), ("ht", C.c_int32), ("dp", C.c_int32),
+                ("push_size", C.c_uint32), ("push", C.c_void_p), ("uniform_size", C.c_uint32), ("uniform", C.c_void_p)]
+
+
 class Scene(C.Structure):
     _fields_ = [
         ("wd", C.c_int32),
@@ -142,6 +148,7 @@ _SIGS = {
     "vkdt_cuda_waveform_rgba_f16": (C.c_int, [_P, C.c_int, C.c_int, _P, C.c_int, C.c_int, _P]),
     "vkdt_cuda_graph_set_debug": (C.c_int, [_P, C.c_int]),
     "vkdt_cuda_graph_debug_stage": (C.c_int, [_P, C.c_int, C.POINTER(C.c_float), C.c_size_t]),
+    "vkdt_cuda_graph_set_nodes": (C.c_int, [_P, C.c_int, C.c_int, _P, C.c_int]),
     "vkdt_cuda_graph_debug_decisions": (C.c_int, [_P, C.c_int, _P, C.c_size_t, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "vkdt_cuda_scene_generate": (C.c_int, [C.POINTER(Scene), _P, _P]),
     "vkdt_cuda_scene_generate_host": (C.c_int, [C.POINTER(Scene), C.POINTER(C.c_uint16)]),

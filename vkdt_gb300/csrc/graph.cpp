@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cstdarg>
 #include <cmath>
@@ -185,7 +186,13 @@ struct vkdt_cuda_graph_t
   bool k1front = false;          // bayer per-node chain: the fused path's hilite front (k1, pyramid, one kernel to doub)
   std::vector<int64_t> planned_for; // what alloc planned for: a run refuses a graph changed since
   std::vector<int64_t> nodes_for;   // what create_nodes planned for (the static develop checks it)
-  float lut_black = -1.0f, lut_white = -1.0f;  // black/white (DN) the noop code table holds
+  float lut_black = -1.0f, lut_white = -1.0f;  // black/white (unorm) the noop code table holds
+  // black and white as the denoise node's push constants carry them (DN / 65535, denoise/main.c:165-168)
+  float nblack[4] = { 0, 0, 0, 0 }, nwhite[4] = { 1, 1, 1, 1 };
+  // colour's committed uniform block when the scheduler hands it over (vkdt_cuda_graph_set_nodes):
+  // the white balance multipliers, the exposure factor and the camera matrix as committed
+  bool colour_given = false;
+  float colour_mul[3] = { 1, 1, 1 }, colour_mulw = 1.0f, colour_cam[9] = { 1, 0, 0, 0, 1, 0, 0, 0, 1 };
   size_t off_h0 = 0, off_b0 = 0, off_hl = 0, off_cov = 0, off_g = 0, off_hs = 0, off_dm = 0;
   size_t off_vh = 0, off_pq = 0, off_lpf = 0;
   size_t off_dnh = 0, off_dnl[4] = { 0, 0, 0, 0 }, off_dna = 0, off_dn = 0, off_idlut = 0;
@@ -279,10 +286,17 @@ const double M_yuv_to_rec709[9] = { 1.0, -3.94570707e-05, 1.13982797, 1.0, -3.94
 
 // colour/main.c:219-292 commit_params (matrix path): writes p_wb back into the
 // module's params when it was derived from the camera coefficients
-void colour_commit(vkdt_cuda_graph_t *g, dev_image_t &d)
+// the white balance part of colour's commit_params (colour/main.c:241-253): the
+// white derived from the camera coefficients when the param is zero, written back
+// into the params as the reference does
+void colour_commit_white(vkdt_cuda_graph_t *g, float p_wb[3])
 {
   module_t *m = g->mod("colour");
-  float p_wb[3] = { m->f("white", 0), m->f("white", 1), m->f("white", 2) };
+  p_wb[0] = m->f("white", 0); p_wb[1] = m->f("white", 1); p_wb[2] = m->f("white", 2);
+  if(g->colour_given)
+  { // the block the reference's commit_params wrote (vkdt_cuda_graph_set_nodes)
+    p_wb[0] = g->colour_mul[0]; p_wb[1] = 1.0f; p_wb[2] = g->colour_mul[2];
+  }
   if(p_wb[0] == 0.0f && p_wb[1] == 0.0f && p_wb[2] == 0.0f)
   {
     float w0[3] = {0}, w[] = { g->ip.whitebalance[0], g->ip.whitebalance[1], g->ip.whitebalance[2] };
@@ -292,10 +306,18 @@ void colour_commit(vkdt_cuda_graph_t *g, dev_image_t &d)
   }
   if(!(p_wb[0] == p_wb[0]) || p_wb[0] == 0.0f || p_wb[1] == 0.0f || p_wb[2] == 0.0f)
     p_wb[0] = p_wb[1] = p_wb[2] = 1.0f;
-  for(int k = 0; k < 3; k++) m->setf("white", k, p_wb[k]);
+  if(!g->colour_given) for(int k = 0; k < 3; k++) m->setf("white", k, p_wb[k]);
+}
+
+void colour_commit(vkdt_cuda_graph_t *g, dev_image_t &d)
+{
+  module_t *m = g->mod("colour");
+  float p_wb[3];
+  colour_commit_white(g, p_wb);
   const float mul[3] = { p_wb[0] / p_wb[1], 1.0f, p_wb[2] / p_wb[1] };
-  d.mulw = powf(2.0f, m->f("exposure"));
-  if(m->n("matrix") == 1) for(int i = 0; i < 9; i++) d.cam[i] = g->ip.cam_to_rec2020[i];
+  d.mulw = g->colour_given ? g->colour_mulw : powf(2.0f, m->f("exposure"));
+  if(g->colour_given) for(int i = 0; i < 9; i++) d.cam[i] = g->colour_cam[i];
+  else if(m->n("matrix") == 1) for(int i = 0; i < 9; i++) d.cam[i] = g->ip.cam_to_rec2020[i];
   else for(int i = 0; i < 9; i++) d.cam[i] = (i % 4 == 0) ? 1.0f : 0.0f;
   m3_mul(M_cat16_M, M_rec2020_to_xyz, d.P);
   m3_mul(M_xyz_to_rec2020, M_cat16_Mi, d.Q);
@@ -372,8 +394,8 @@ int fill_image(vkdt_cuda_graph_t *g, dev_image_t &d, const void *d_src, void *d_
   d.cx = (int)g->ip.crop_aabb[0]; d.cy = (int)g->ip.crop_aabb[1];
   d.W = g->W; d.H = g->H;
   d.filters = g->ip.filters;
-  d.black = g->ip.black[0] / 65535.0f;        // denoise/main.c:165-168
-  d.white = g->ip.white[0] / 65535.0f;
+  d.black = g->nblack[0];                     // denoise/main.c:165-168
+  d.white = g->nwhite[0];
   d.codes.black = d.black; d.codes.white = d.white; d.codes.identity = 0;
   module_t *hl = g->mod("hilite");
   d.hl_white = hl->f("white"); d.hl_desat = hl->f("desat"); d.hl_soft = hl->f("soft");
@@ -478,8 +500,8 @@ void fill_denoise(vkdt_cuda_graph_t *g, dev_denoise_t &p, const void *d_src)
   p.filters = g->ip.filters;
   for(int k = 0; k < 3; k++)
   {
-    p.black[k] = g->ip.black[k] / 65535.0f;
-    p.white[k] = g->ip.white[k] / 65535.0f;
+    p.black[k] = g->nblack[k];
+    p.white[k] = g->nwhite[k];
     p.wb[k] = g->ip.whitebalance[k];
   }
   p.na = g->ip.noise_a; p.nb = g->ip.noise_b;
@@ -555,10 +577,10 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
     li++;
     return 0;
   };
-  if(g->ip.black[0] != g->lut_black || g->ip.white[0] != g->lut_white)
+  if(g->nblack[0] != g->lut_black || g->nwhite[0] != g->lut_white)
   { // new black/white since the code table was built: rebuild it on the device (same IEEE arithmetic)
-    CU(launch_noop_lut(g->at<__half>(g->off_lut), g->ip.black[0] / 65535.0f, g->ip.white[0] / 65535.0f, s));
-    g->lut_black = g->ip.black[0]; g->lut_white = g->ip.white[0];
+    CU(launch_noop_lut(g->at<__half>(g->off_lut), g->nblack[0], g->nwhite[0], s));
+    g->lut_black = g->nblack[0]; g->lut_white = g->nwhite[0];
   }
   if(g->want_hist) CU(cudaMemsetAsync(g->at<uint32_t>(g->off_hist), 0, 257 * sizeof(uint32_t), s));
   if((r = mark())) return r;
@@ -949,6 +971,8 @@ int vkdt_cuda_graph_set_input(vkdt_cuda_graph_t *g, int wd, int ht, const vkdt_c
   if(!g || !ip) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "null argument");
   if(wd <= 0 || ht <= 0) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "bad input size %dx%d", wd, ht);
   g->in_wd = wd; g->in_ht = ht; g->ip = *ip;
+  for(int k = 0; k < 4; k++) { g->nblack[k] = ip->black[k] / 65535.0f; g->nwhite[k] = ip->white[k] / 65535.0f; }
+  g->colour_given = false;
   // i-raw/main.c:214-218 normalises the white balance to green
   if(g->ip.whitebalance[1] > 0.0f && g->ip.whitebalance[1] != 1.0f)
   {
@@ -1209,6 +1233,10 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
 
   g->nodes_ready = true;
   g->nodes_for = plan_key(g);
+  { // the scheduler commits the modules' params with their nodes
+    float p_wb[3];
+    colour_commit_white(g, p_wb);
+  }
   return VKDT_CUDA_SUCCESS;
 }
 
@@ -1230,14 +1258,14 @@ int vkdt_cuda_graph_alloc(vkdt_cuda_graph_t *g, uint64_t *device_bytes)
   }
   { // denoise/noop.comp:385 for every u16 code, channel 0 black/white (denoise/main.c:165-168)
     std::vector<__half> lut(65536);
-    const float black = g->ip.black[0] / 65535.0f, white = g->ip.white[0] / 65535.0f;
+    const float black = g->nblack[0], white = g->nwhite[0];
     for(int v = 0; v < 65536; v++)
     {
       const float x = (float)v / 65535.0f;
       lut[v] = __float2half_rn(std::fmax(0.0f, (x - black) / (white - black)));
     }
     CU(cudaMemcpy(g->arena + g->off_lut, lut.data(), 65536 * 2, cudaMemcpyHostToDevice));
-    g->lut_black = g->ip.black[0]; g->lut_white = g->ip.white[0];
+    g->lut_black = g->nblack[0]; g->lut_white = g->nwhite[0];
   }
   CU(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
   CU(cudaEventCreateWithFlags(&g->done, cudaEventDisableTiming));
@@ -1263,6 +1291,151 @@ int vkdt_cuda_graph_plan_bytes(vkdt_cuda_graph_t *g, uint64_t *device_bytes)
 
 
 int vkdt_cuda_graph_node_count(vkdt_cuda_graph_t *g) { return g ? (int)g->nodes.size() : 0; }
+namespace {
+// little endian 4-byte fields of a push constant or uniform block
+float fat(const void *p, uint32_t size, int i) { float v = 0; if(p && (uint32_t)(4 * i + 4) <= size) memcpy(&v, (const uint8_t *)p + 4 * i, 4); return v; }
+int32_t iat(const void *p, uint32_t size, int i) { int32_t v = 0; if(p && (uint32_t)(4 * i + 4) <= size) memcpy(&v, (const uint8_t *)p + 4 * i, 4); return v; }
+}
+
+int vkdt_cuda_graph_set_nodes(vkdt_cuda_graph_t *g, int in_wd, int in_ht, const vkdt_cuda_node_desc_t *nodes, int count)
+{
+  if(!g || !nodes || count <= 0) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "no nodes");
+  if(g->allocated) return fail(VKDT_CUDA_INCOMPLETE, "graph already allocated");
+  auto find = [&](const char *name, const char *kernel) -> const vkdt_cuda_node_desc_t * {
+    for(int i = 0; i < count; i++) if(nodes[i].name == tkn(name) && nodes[i].kernel == tkn(kernel)) return nodes + i;
+    return nullptr;
+  };
+  auto module_uniform = [&](const char *name) -> const vkdt_cuda_node_desc_t * {
+    for(int i = 0; i < count; i++) if(nodes[i].name == tkn(name) && nodes[i].uniform) return nodes + i;
+    return nullptr;
+  };
+  vkdt_cuda_img_param_t ip;
+  memset(&ip, 0, sizeof(ip));
+  float nblack[4], nwhite[4];
+  // ---- denoise (denoise/main.c:133-333): noop, or the wavelet nodes
+  const vkdt_cuda_node_desc_t *noop = find("denoise", "noop"), *half = find("denoise", "half");
+  const vkdt_cuda_node_desc_t *doub = find("denoise", "doub");
+  if(noop)
+  { // {crop[4], black[4], white[4], map_os[4], filters, gainmap}
+    const uint32_t ps = noop->push_size;
+    for(int k = 0; k < 4; k++)
+    {
+      ip.crop_aabb[k] = (uint32_t)iat(noop->push, ps, k);
+      nblack[k] = fat(noop->push, ps, 4 + k); nwhite[k] = fat(noop->push, ps, 8 + k);
+    }
+    ip.filters = (uint32_t)iat(noop->push, ps, 16);
+    if(iat(noop->push, ps, 17)) return fail(VKDT_CUDA_INCOMPLETE, "denoise with a dng gain map is not built");
+  }
+  else if(half && doub)
+  { // half: {wb[4], black[4], white[4], crop[4], filters}; doub adds {noise a, noise b, gainmap, ...}
+    const uint32_t ps = half->push_size;
+    for(int k = 0; k < 4; k++)
+    {
+      nblack[k] = fat(half->push, ps, 4 + k); nwhite[k] = fat(half->push, ps, 8 + k);
+      ip.crop_aabb[k] = (uint32_t)iat(half->push, ps, 12 + k);
+    }
+    ip.filters = (uint32_t)iat(half->push, ps, 16);
+    ip.noise_a = fat(doub->push, doub->push_size, 17);
+    ip.noise_b = fat(doub->push, doub->push_size, 18);
+    if(iat(doub->push, doub->push_size, 19)) return fail(VKDT_CUDA_INCOMPLETE, "denoise with a dng gain map is not built");
+  }
+  else return fail(VKDT_CUDA_INCOMPLETE, "no denoise nodes on a mosaic (rgb input, or another chain)");
+  // crop_aabb is (x0, y0, x1, y1) at full resolution when the input is not scaled
+  // ---- white balance and CFA from the demosaic (or hilite) push constants {wb[4], filters}
+  const vkdt_cuda_node_desc_t *wbn = nullptr;
+  for(const char *k : { "gauss", "splat", "fix", "rcd_fill", "halfsize", "down" }) if(!wbn) wbn = find("demosaic", k);
+  if(!wbn) wbn = find("hilite", "half");
+  if(!wbn) return fail(VKDT_CUDA_INCOMPLETE, "no demosaic or hilite nodes");
+  for(int k = 0; k < 4; k++) ip.whitebalance[k] = fat(wbn->push, wbn->push_size, k);
+  if((uint32_t)iat(wbn->push, wbn->push_size, 4) != ip.filters) return fail(VKDT_CUDA_INCOMPLETE, "inconsistent CFA");
+  // black/white in DN for the metadata; the kernels take the normalised values as pushed
+  for(int k = 0; k < 4; k++) { ip.black[k] = nblack[k] * 65535.0f; ip.white[k] = nwhite[k] * 65535.0f; }
+  for(int i = 0; i < 9; i++) ip.cam_to_rec2020[i] = (i % 4 == 0) ? 1.0f : 0.0f;
+  // ---- module parameters from the uniform blocks (the params files' order, 4 bytes each)
+  auto set_f = [&](const char *mod, const char *par, int n, const vkdt_cuda_node_desc_t *u, int at) {
+    module_t *m = ensure_module(g, mod);
+    for(int k = 0; k < n; k++) m->setf(par, k, fat(u->uniform, u->uniform_size, at + k));
+  };
+  auto set_i = [&](const char *mod, const char *par, const vkdt_cuda_node_desc_t *u, int at) {
+    module_t *m = ensure_module(g, mod);
+    const int32_t v = iat(u->uniform, u->uniform_size, at);
+    int o = m->offset(tkn(par), 0, 0);
+    memcpy(&m->param[o], &v, 4);
+  };
+  const vkdt_cuda_node_desc_t *u;
+  if((u = module_uniform("denoise")))
+  { // strength, luma, detail, pad, edges[4], gainmap
+    set_f("denoise", "strength", 1, u, 0); set_f("denoise", "luma", 1, u, 1); set_f("denoise", "detail", 1, u, 2);
+    set_f("denoise", "edges", 4, u, 4); set_i("denoise", "gainmap", u, 8);
+  }
+  if((u = module_uniform("hilite"))) { set_f("hilite", "white", 1, u, 0); set_f("hilite", "desat", 1, u, 1); set_f("hilite", "soft", 1, u, 2); }
+  if((u = module_uniform("demosaic"))) { set_i("demosaic", "colour", u, 0); set_i("demosaic", "method", u, 1); }
+  if((u = module_uniform("filmcurv")))
+  {
+    set_f("filmcurv", "light", 1, u, 0); set_f("filmcurv", "contrast", 1, u, 1); set_f("filmcurv", "bias", 1, u, 2);
+    set_i("filmcurv", "colour", u, 3);
+    const char *rest[] = { "chroma", "rolloff", "red", "yellow", "blue", "shadows" };
+    for(int k = 0; k < 6; k++) set_f("filmcurv", rest[k], 1, u, 4 + k);
+  }
+  if((u = module_uniform("llap")))
+  {
+    set_f("llap", "sigma", 1, u, 0); set_f("llap", "shadows", 1, u, 1); set_f("llap", "hilights", 1, u, 2);
+    set_f("llap", "clarity", 1, u, 3);
+  }
+  // colour/main.c:219-365: the committed block. off = 4+12+4+12+4*24+4*24
+  u = module_uniform("colour");
+  if(!u || u->uniform_size < 4 * (224 + 8)) return fail(VKDT_CUDA_INCOMPLETE, "no colour uniform block");
+  {
+    const int off = 224;
+    if(iat(u->uniform, u->uniform_size, off + 1) != 0) return fail(VKDT_CUDA_INCOMPLETE, "colour clut mode not built");
+    if(fat(u->uniform, u->uniform_size, off + 2) != 1.0f) return fail(VKDT_CUDA_INCOMPLETE, "colour saturation != 1 not built");
+    if(iat(u->uniform, u->uniform_size, off + 3) != 0 || iat(u->uniform, u->uniform_size, off + 4) != 0)
+      return fail(VKDT_CUDA_INCOMPLETE, "colour picker / gamut not built");
+    if(fat(u->uniform, u->uniform_size, off + 7) != 0.0f) return fail(VKDT_CUDA_INCOMPLETE, "colour clip not built");
+    if(iat(u->uniform, u->uniform_size, 16) != 0) return fail(VKDT_CUDA_INCOMPLETE, "colour rbf mode not built");
+    g->colour_mul[0] = fat(u->uniform, u->uniform_size, 0);
+    g->colour_mul[1] = 1.0f;
+    g->colour_mul[2] = fat(u->uniform, u->uniform_size, 2);
+    g->colour_mulw = fat(u->uniform, u->uniform_size, 3);
+    for(int i = 0; i < 3; i++) for(int j = 0; j < 3; j++)   // f[4+4i+j] = cam[3j+i]
+      g->colour_cam[3 * j + i] = fat(u->uniform, u->uniform_size, 4 + 4 * i + j);
+  }
+  // ---- sizes: the llap depth from its reduce nodes, the output size from llap/colour
+  int reduces = 0;
+  for(int i = 0; i < count; i++) reduces += nodes[i].name == tkn("llap") && nodes[i].kernel == tkn("reduce");
+  const vkdt_cuda_node_desc_t *fin = find("llap", "colour");
+  if(!fin || !find("colour", "main") || !find("filmcurv", "main")) return fail(VKDT_CUDA_INCOMPLETE, "not the development chain");
+  int r = vkdt_cuda_graph_set_input(g, in_wd, in_ht, &ip);
+  if(r) return r;
+  for(int k = 0; k < 4; k++) { g->nblack[k] = nblack[k]; g->nwhite[k] = nwhite[k]; }
+  g->colour_given = true;
+  g->llap_levels_req = reduces + 1;
+  const int W = (int)(ip.crop_aabb[2] - ip.crop_aabb[0]), H = (int)(ip.crop_aabb[3] - ip.crop_aabb[1]);
+  const int method = g->mod("demosaic")->n("method");
+  const int fw = method == 2 ? (W + 1) / 2 : W, fh = method == 2 ? (H + 1) / 2 : H;
+  g->req_wd = (fin->wd != fw || fin->ht != fh) ? fin->wd : 0;
+  g->req_ht = (fin->wd != fw || fin->ht != fh) ? fin->ht : 0;
+  if((r = vkdt_cuda_graph_create_nodes(g))) return r;
+  // ---- the plan covers exactly these nodes
+  std::vector<std::array<int64_t, 5>> want, have;
+  for(int i = 0; i < count; i++)
+  {
+    const vkdt_cuda_node_desc_t &n = nodes[i];
+    if(n.name == tkn("filmcurv") && n.kernel == tkn("dspy")) continue;   // the display curve, not on the path
+    if(n.name == tkn("shared") && n.kernel == tkn("resample") && n.wd == g->W && n.ht == g->H && !g->halfsize) continue;
+    want.push_back({ (int64_t)n.name, (int64_t)n.kernel, n.wd, n.ht, n.dp });
+  }
+  for(auto &n : g->nodes) have.push_back({ (int64_t)n.name, (int64_t)n.kernel, (int64_t)n.wd, (int64_t)n.ht, (int64_t)n.dp });
+  std::sort(want.begin(), want.end());
+  std::sort(have.begin(), have.end());
+  if(want != have)
+  {
+    g->nodes_ready = false;
+    return fail(VKDT_CUDA_INCOMPLETE, "the library's plan (%zu nodes) does not cover the given %zu nodes", have.size(), want.size());
+  }
+  return VKDT_CUDA_SUCCESS;
+}
+
 int vkdt_cuda_graph_node(vkdt_cuda_graph_t *g, int i, vkdt_cuda_node_info_t *info)
 {
   if(!g || !info || i < 0 || i >= (int)g->nodes.size()) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "node %d", i);
@@ -1421,11 +1594,11 @@ int vkdt_cuda_graph_develop_static(vkdt_cuda_graph_t *g, const void *d_mosaic, v
   }
   cudaStream_t s = (cudaStream_t)stream;
   CU(cudaMemsetAsync(base, 0, off, s));
-  CU(launch_noop_lut((__half *)(base + g->off_lut), g->ip.black[0] / 65535.0f, g->ip.white[0] / 65535.0f, s));
+  CU(launch_noop_lut((__half *)(base + g->off_lut), g->nblack[0], g->nwhite[0], s));
   // the kernels address the scratch for this call only; the table just built is the one
   // enqueue would build, so it is marked as current (and the graph's own marks restored)
   const float keep_black = g->lut_black, keep_white = g->lut_white;
-  g->lut_black = g->ip.black[0]; g->lut_white = g->ip.white[0];
+  g->lut_black = g->nblack[0]; g->lut_white = g->nwhite[0];
   g->arena = base;
   const int r = enqueue(g, s, d_mosaic, d_rgba, false);
   g->arena = nullptr;

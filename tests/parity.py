@@ -34,6 +34,11 @@ more than 2e-3). The tolerance is max 2e-3, mean 1e-4 and CIEDE2000 < 0.5.
      than those by which the same restatement in FP64 differs from FP32: the
      CUDA path is at least as close to the FP32 reference as the reference's
      arithmetic carried in double precision is.
+   Against the FP64 build (double=True) the same rules hold, except on those
+   ill-conditioned paths: there the FP64 build's own decisions follow values
+   the FP32 arithmetic does not reproduce, and the CUDA path is held to be no
+   farther from the FP64 result than the FP32 reference is (pixels over the
+   tolerance and the mean within 25%).
 """
 import json
 import os
@@ -139,7 +144,7 @@ def check(name, v, m, ip, op, gpu, stages=("denoise", "hilite", "demosaic", "col
             rec["gauss_margin_max_differing"] = float(own["margin_gauss"][diff].max())
         elif kind == "dn_cov" and diff.any() and not double:
             problems.append(("denoise structure tensor decisions differ", differ[kind]))
-        elif kind == "dn_thr" and diff.any():
+        elif kind == "dn_thr" and diff.any() and not double:
             bits = (d ^ mine)
             mar = own["margin_dn_thr"]
             worst = 0.0
@@ -174,10 +179,15 @@ def check(name, v, m, ip, op, gpu, stages=("denoise", "hilite", "demosaic", "col
             problems.append(("node", s, r, np.unravel_index(int(np.argmax(e)), e.shape)))
     # ---- 3. end to end against the oracle with the same decisions
     ill = op.dn_strength > 0 or op.dm_method == 1
-    f64 = None
+    f64 = f32 = None
     if ill and not double:
         f64 = oracle.develop(m, oracle.img_param(ip), params=op, stages=stages, double=True,
                              force={k: dec[k] for k in dec})
+    if ill and double:
+        # against the FP64 build of an ill-conditioned path, the yardstick is the FP32
+        # reference itself: the CUDA path is to be no farther from the FP64 result than
+        # the FP32 arithmetic of the reference (with the same decisions) is
+        f32 = oracle.develop(m, oracle.img_param(ip), params=op, stages=stages, force={k: dec[k] for k in dec})
     gain = None
     for s in stages:
         a, b = gpu[s], forced[s]
@@ -198,6 +208,16 @@ def check(name, v, m, ip, op, gpu, stages=("denoise", "hilite", "demosaic", "col
             r["fp64_max"] = float(e64.max())
             if s in ("filmcurv", "llap"):
                 r["fp64_de_over"] = int((delta_e2000(f64[s], b) >= de).sum())
+        if f32 is not None:
+            e32 = rel_err(f32[s], b)
+            r["fp32_over"], r["fp32_mean"] = int((e32 > tol).sum()), float(e32.mean())
+            if s in ("filmcurv", "llap"):
+                r["fp32_de_over"] = int((delta_e2000(f32[s], b) >= de).sum())
+            if not (r["over"] <= 1.25 * r["fp32_over"] + 16 and r["mean"] <= 1.25 * r["fp32_mean"] + 1e-5
+                    and r.get("de_over", 0) <= 1.25 * r.get("fp32_de_over", 0) + 16):
+                problems.append(("farther from the FP64 build than the FP32 reference", s, r))
+            rec[s] = r
+            continue
         if not (r["mean"] <= mean):
             problems.append(("e2e mean", s, r["mean"]))
         if over.any() or r.get("de_over", 0):

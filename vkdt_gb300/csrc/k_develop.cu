@@ -253,19 +253,43 @@ DEV void gauss_exact(const float px[8], float v[4], int &dec)
   dec = (usew ? GAUSS_DEC_USEW : 0) | ((horiz ? 0 : 1) << GAUSS_DEC_SNAP_SHIFT);
 }
 
-__global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
+// The tiles whose stages see no mirrored or wrapped position (even origin, a 4
+// pixel margin to every image edge) form the rectangle of tile indices
+// [ix0, ix1] x [iy0, iy1]; the interior kernel runs those, the border kernel the
+// ring around them (two specialisations: each keeps only its own tap code).
+struct tiles_t { int nx, ny, ix0, ix1, iy0, iy1; };
+
+template<bool INTERIOR> DEV void tile_of(const tiles_t &t, int &bx, int &by)
+{
+  if(INTERIOR) { bx = t.ix0 + (int)blockIdx.x; by = t.iy0 + (int)blockIdx.y; return; }
+  // the ring, one CTA per tile: the rows above and below the interior, then the columns beside it
+  int i = blockIdx.x;
+  const int top = t.iy0 * t.nx, bot = (t.ny - 1 - t.iy1) * t.nx;
+  if(i < top) { bx = i % t.nx; by = i / t.nx; return; }
+  i -= top;
+  if(i < bot) { bx = i % t.nx; by = t.iy1 + 1 + i / t.nx; return; }
+  i -= bot;
+  const int left = t.ix0, side = t.ix0 + (t.nx - 1 - t.ix1);
+  by = t.iy0 + i / side;
+  const int k = i % side;
+  bx = k < left ? k : t.ix1 + 1 + (k - left);
+}
+
+template<bool INTERIOR> __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p, const tiles_t tiles)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   smem_t &s = *reinterpret_cast<smem_t *>(smem_raw);
   const int tid = threadIdx.x;
   const int W = p.W, H = p.H, hw = W / 2, hh = H / 2;
   // owned output range and the (possibly shifted) tile origin
-  const int OX = blockIdx.x * TX, OY = blockIdx.y * TY;
+  int tbx, tby;
+  tile_of<INTERIOR>(tiles, tbx, tby);
+  const int OX = tbx * TX, OY = tby * TY;
   const int X0 = W >= TX ? min(OX, W - TX) : 0;
   const int Y0 = H >= TY ? min(OY, H - TY) : 0;
   const int OXe = min(OX + TX, W), OYe = min(OY + TY, H);
   // no position of the tile's stages is mirrored or wrapped (even origin, 4 pixel margin)
-  const bool interior = !((X0 | Y0) & 1) && X0 >= 4 && Y0 >= 4 && X0 + TX + 4 <= W && Y0 + TY + 4 <= H;
+  constexpr bool interior = INTERIOR;
   if(p.hist) for(int i = tid; i < 257; i += NT) s.hist[i] = 0;
 
   // ---- the hilite coarse level around the tile (virtual slots, mirrored)
@@ -542,9 +566,13 @@ __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p)
 
 cudaError_t init_develop()
 {
-  cudaError_t e = cudaFuncSetAttribute(k_develop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(smem_t));
-  // the whole unified L1 as shared memory: 5 CTAs of 43.5 KB per SM
-  if(e == cudaSuccess) e = cudaFuncSetAttribute(k_develop, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+  cudaError_t e = cudaSuccess;
+  for(auto f : { k_develop<true>, k_develop<false> })
+  {
+    if(e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(smem_t));
+    // the whole unified L1 as shared memory: 5 CTAs of 43.5 KB per SM
+    if(e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+  }
   if(e == cudaSuccess) e = init_llap();
   if(e == cudaSuccess) e = init_hilite();
   return e;
@@ -552,7 +580,19 @@ cudaError_t init_develop()
 
 cudaError_t launch_develop(const dev_image_t &p, cudaStream_t s)
 {
-  dim3 grid((p.W + TX - 1) / TX, (p.H + TY - 1) / TY);
-  k_develop<<<grid, NT, sizeof(smem_t), s>>>(p);
+  tiles_t t;
+  t.nx = (p.W + TX - 1) / TX; t.ny = (p.H + TY - 1) / TY;
+  // interior tile bx: origin 32 bx >= 4 and 32 bx + TX + 4 <= W (then it is not the shifted last tile)
+  t.ix0 = 1; t.ix1 = (p.W - TX - 4) / TX;
+  t.iy0 = 1; t.iy1 = (p.H - TY - 4) / TY;
+  if(p.W < 2 * TX + 4 || p.H < 2 * TY + 4 || t.ix1 < t.ix0 || t.iy1 < t.iy0)
+  { // no interior: every tile is a border tile (the ring is the whole grid)
+    t.ix0 = t.nx; t.ix1 = t.nx - 1; t.iy0 = t.ny; t.iy1 = t.ny - 1;
+    k_develop<false><<<t.nx * t.ny, NT, sizeof(smem_t), s>>>(p, t);
+    return cudaGetLastError();
+  }
+  const int nin = (t.ix1 - t.ix0 + 1) * (t.iy1 - t.iy0 + 1);
+  k_develop<true><<<dim3(t.ix1 - t.ix0 + 1, t.iy1 - t.iy0 + 1), NT, sizeof(smem_t), s>>>(p, t);
+  k_develop<false><<<t.nx * t.ny - nin, NT, sizeof(smem_t), s>>>(p, t);
   return cudaGetLastError();
 }

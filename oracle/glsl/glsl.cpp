@@ -1,3 +1,4 @@
+#include <cstring>
 // Sampler, image and storage model of glsl.hpp (test infrastructure only).
 #include "glsl.hpp"
 #include <ucontext.h>
@@ -107,6 +108,33 @@ vec4 textureGather(const sampler2D &s, const vec2 &uv, int comp)
 ivec2 textureSize(const sampler2D &s, int) { return s.im ? ivec2(s.im->w, s.im->h) : ivec2(0); }
 ivec2 textureSize(const usampler2D &s, int) { return s.im ? ivec2(s.im->w, s.im->h) : ivec2(0); }
 ivec2 imageSize(const image2D &i) { return i.im ? ivec2(i.im->w, i.im->h) : ivec2(0); }
+ivec2 imageSize(const uimage2D &i) { return i.im ? ivec2(i.im->w, i.im->h) : ivec2(0); }
+
+uint imageAtomicAdd(const uimage2D &i, const ivec2 &p, uint v)
+{ // r32ui: the u32 stored in the float slot's bits
+  image_t *im = i.im;
+  if(!im || p.x < 0 || p.y < 0 || p.x >= im->w || p.y >= im->h) return 0;
+  float *d = im->data + ((size_t)p.y * im->w + p.x) * im->c;
+  return __atomic_fetch_add(reinterpret_cast<uint32_t *>(d), v, __ATOMIC_RELAXED);
+}
+
+float imageAtomicAdd(const image2D &i, const ivec2 &p, float v)
+{ // r32f
+  image_t *im = i.im;
+  if(!im || p.x < 0 || p.y < 0 || p.x >= im->w || p.y >= im->h) return 0.0f;
+  float *d = im->data + ((size_t)p.y * im->w + p.x) * im->c;
+  uint32_t *u = reinterpret_cast<uint32_t *>(d);
+  uint32_t cur = __atomic_load_n(u, __ATOMIC_RELAXED), nxt;
+  float f;
+  do
+  { // compare and swap of the sum
+    memcpy(&f, &cur, 4);
+    const float s = f + v;
+    memcpy(&nxt, &s, 4);
+  }
+  while(!__atomic_compare_exchange_n(u, &cur, nxt, true, __ATOMIC_RELAXED, __ATOMIC_RELAXED));
+  return f;
+}
 
 void imageStore(const image2D &i, const ivec2 &p, const vec4 &v)
 {

@@ -387,6 +387,11 @@ vec4 textureGather(const sampler2D &s, const vec2 &uv, int comp);
 ivec2 textureSize(const sampler2D &s, int lod);
 ivec2 textureSize(const usampler2D &s, int lod);
 ivec2 imageSize(const image2D &i);
+ivec2 imageSize(const uimage2D &i);
+// atomic adds (workgroups run on several threads: real atomics; float sums in any order)
+uint imageAtomicAdd(const uimage2D &i, const ivec2 &p, uint v);
+float imageAtomicAdd(const image2D &i, const ivec2 &p, float v);
+template<class V> inline uint imageAtomicAdd(const uimage2D &i, const ivec2 &p, V v) { return imageAtomicAdd(i, p, (uint)v); }
 void imageStore(const image2D &i, const ivec2 &p, const vec4 &v);
 vec4 imageLoad(const image2D &i, const ivec2 &p);
 template<class A> inline vec4 texture(const sampler2D &s, const A &uv) { return texture(s, vec2(tov(uv))); }

@@ -29,7 +29,7 @@ SHADERS = [
     ("demosaic", "halfsize"), ("demosaic", "rcd_conv"), ("demosaic", "rcd_fill"), ("shared", "resample"),
     ("colour", "main"), ("filmcurv", "main"),
     ("llap", "curve"), ("llap", "reduce"), ("llap", "assemble"), ("llap", "colour"),
-    ("i-mcraw", "decode"), ("colenc", "main"), ("grade", "main"),
+    ("i-mcraw", "decode"), ("colenc", "main"), ("grade", "main"), ("rawhist", "collect"), ("hist", "collect"),
 ]
 
 

@@ -294,3 +294,32 @@ def develop(mosaic, ip, params=None, stages=("llap",)):
         out["llap"] = res.a.copy()
     out["llap_levels"] = nl
     return out
+
+
+def rawhist(mosaic, ip, bins=1000):
+    """rawhist/collect.comp (the reference shader) on a u16 mosaic with the
+    uniforms rawhist/main.c:17-28 commits: (3, bins) counts, sums of means,
+    sums of second moments, added in dispatch order as float atomics."""
+    mosaic = np.ascontiguousarray(mosaic, np.uint16)
+    ht, wd = mosaic.shape
+    raw = Img(wd, ht, 1, UNORM16)
+    raw.a[..., 0] = mosaic.astype(np.float32) / np.float32(65535.0)
+    block = 3 if ip.filters == 9 else 2
+    out = Img(bins, 5, 1, F32)
+    uni = f32(ip.noise_a, ip.noise_b) + u32(ip.filters, max(1, int(ip.black[1])), int(ip.white[1]))
+    run("rawhist_collect", wd // block, ht // block, {0: raw, 1: out}, uniform=uni)
+    return out.a[:3, :, 0].astype(np.float64)
+
+
+def waveform(rgba, wo=1000, ho=600):
+    """hist/collect.comp (the reference shader) on an rgba f16 image: the wo x ho
+    u32 waveform (rows of (1 - value) for values in [0, 1]: the shader converts
+    negative floats to unsigned, which C++ leaves undefined, so the emulation is
+    only meaningful on values in [0, 1])"""
+    rgba = np.ascontiguousarray(rgba, np.float32)
+    ht, wd = rgba.shape[:2]
+    src = Img(wd, ht, 4)
+    src.a[...] = rgba
+    out = Img(wo, ho, 1, 3)
+    run("hist_collect", wd, ht, {0: src, 1: out})
+    return out.a[..., 0].copy().view(np.uint32)

@@ -78,3 +78,26 @@ def run(cfg, wd, ht, ip, out_wd=0, out_ht=0):
     out_m = [{"name": token_str(m.name), "inst": token_str(m.inst), "uniform": bytes(m.uniform[:m.uniform_size]),
               "param": bytes(m.param[:m.param_size]), "out": (m.out_wd, m.out_ht)} for m in mods[:nm.value]]
     return out_n, out_m
+
+
+def nprof(hist):
+    """The reference's nprof/main.c fit (its write_sink) on a rawhist histogram
+    (3 x bins: counts, sums of means, sums of second moments): (a, b) as the
+    module writes them to its .nprof file ("%g %g")."""
+    import tempfile
+    h = np.ascontiguousarray(np.asarray(hist, np.float32).reshape(3, -1))
+    fl = lib()
+    fl.hrn_nprof.restype = C.c_int
+    fl.hrn_nprof.argtypes = [C.c_char_p, C.c_void_p, C.c_int]
+    cwd = os.getcwd()
+    with tempfile.TemporaryDirectory() as td:
+        os.chdir(td)
+        try:
+            r = fl.hrn_nprof(_build.REF.encode(), h.ctypes.data, h.shape[1])
+            if r:
+                raise RuntimeError("nprof module failed with %d" % r)
+            with open(os.path.join(td, "unknown--0.nprof")) as f:
+                a, b = f.read().split()[:2]
+        finally:
+            os.chdir(cwd)
+    return a, b

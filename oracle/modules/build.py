@@ -14,6 +14,7 @@ TREE = os.environ.get("VKDT_REFERENCE", "/root/reference")
 SRC = os.path.join(TREE, "src")
 MODULES_DIR = os.path.join(SRC, "pipe", "modules")
 CHAIN = ["denoise", "hilite", "demosaic", "colour", "filmcurv", "llap"]
+EXTRA = ["nprof"]   # modules driven on their own (write_sink)
 HARNESS = os.path.join(REF, "libvkdt_modharness.so")
 
 
@@ -23,7 +24,7 @@ def flags():
 
 
 def available():
-    return os.path.exists(HARNESS) and all(os.path.exists(os.path.join(REF, "mod_%s.so" % m)) for m in CHAIN)
+    return os.path.exists(HARNESS) and all(os.path.exists(os.path.join(REF, "mod_%s.so" % m)) for m in CHAIN + EXTRA)
 
 
 def build(force=False):
@@ -33,7 +34,7 @@ def build(force=False):
         return True
     os.makedirs(REF, exist_ok=True)
     jobs = []
-    for m in CHAIN:
+    for m in CHAIN + EXTRA:
         out = os.path.join(REF, "mod_%s.so" % m)
         jobs.append(["gcc"] + flags() + ["-shared", "-o", out, os.path.join(MODULES_DIR, m, "main.c"), "-lm"])
     jobs.append(["gcc"] + flags() + ["-shared", "-o", HARNESS, os.path.join(HERE, "harness.c"),

@@ -30,6 +30,8 @@
 // the device-layer global the module host code reads (colour/main.c reads
 // float_atomics_supported); zero: no device features
 qvk_t qvk;
+// the pipeline global of src/pipe/global.c (nprof's install path reads its home directory)
+dt_pipe_global_t dt_pipe;
 
 #define HRN_MAX_MODULES 16
 #define HRN_MAX_NODES   512
@@ -484,5 +486,30 @@ int hrn_run(const char *modules_dir, const char *so_dir, const char *cfg, int wd
     const int oc = conn_of(m, tok("output"));
     if(oc >= 0) { o->out_wd = m->connector[oc].roi.wd; o->out_ht = m->connector[oc].roi.ht; }
   }
+  return 0;
+}
+
+/* nprof/main.c:82-198 write_sink on a rawhist histogram (3 rows of wd floats:
+ * counts, sums of means, sums of second moments): the module writes its fit
+ * to "unknown--0.nprof" in the working directory (the image has no maker,
+ * model or iso here). Returns 0 when the module ran. */
+int hrn_nprof(const char *so_dir, const float *hist, int wd)
+{
+  char fn[1024];
+  snprintf(fn, sizeof(fn), "%s/mod_nprof.so", so_dir);
+  void *h = dlopen(fn, RTLD_LAZY | RTLD_LOCAL);
+  if(!h) { fprintf(stderr, "harness: %s\n", dlerror()); return 1; }
+  dt_module_write_sink_t ws = (dt_module_write_sink_t)dlsym(h, "write_sink");
+  if(!ws) return 2;
+  dt_module_t *m = calloc(1, sizeof(dt_module_t));
+  m->name = tok("nprof"); m->inst = tok("np");
+  m->num_connectors = 1;
+  m->connector[0].roi.wd = wd; m->connector[0].roi.ht = 5;
+  float *buf = calloc((size_t)wd * 5, sizeof(float));
+  memcpy(buf, hist, sizeof(float) * 3 * (size_t)wd);
+  dt_write_sink_params_t p = { 0 };
+  ws(m, buf, &p);
+  free(buf);
+  free(m);
   return 0;
 }

@@ -69,3 +69,50 @@ def test_rawhist_gpu_equals_oracle(gpu, kind, filters, bins):
     got = v.rawhist(d.data_ptr(), wd, ht, ip, bins=bins)
     want = oracle.rawhist(m, filters, BLACK, WHITE, bins=bins)
     assert np.array_equal(got, want)
+
+
+# ---------------------------------------------------------------- pinned to the reference
+
+def test_nprof_fit_equals_the_reference_module():
+    # tests/golden/nprof.json: the reference's own nprof/main.c (write_sink) fit of the same
+    # histograms, as it prints them ("%g %g"); the library's fit prints the same
+    import json
+    import os
+    import sys
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    sys.path.insert(0, here)
+    import make_nprof
+    for rec in json.load(open(os.path.join(here, "nprof.json"))):
+        a, b, ok = v.nprof_fit(make_nprof.histogram(tuple(rec["case"])))
+        assert ["%g" % a, "%g" % b] == rec["ab"], (rec, a, b)
+
+
+def test_nprof_fixture_is_what_the_module_emits_now():
+    from oracle.modules import build as MB
+    import os
+    if not os.path.isdir(MB.MODULES_DIR) or not MB.build():
+        pytest.skip("no vkdt tree here")
+    from oracle import modules as M
+    import json
+    import sys
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    sys.path.insert(0, here)
+    import make_nprof
+    for rec in json.load(open(os.path.join(here, "nprof.json"))):
+        assert list(M.nprof(make_nprof.histogram(tuple(rec["case"])))) == rec["ab"]
+
+
+@pytest.mark.parametrize("filters", [BAYER, XTRANS])
+def test_oracle_rawhist_equals_the_reference_shader(filters):
+    # rawhist/collect.comp compiled for the CPU: the counts bit for bit, the float atomic sums to their
+    # rounding (the shader adds floats in any order)
+    from oracle import glsl_ref
+    if not glsl_ref.available():
+        pytest.skip("reference shaders not built (oracle/_ref)")
+    wd, ht = (600, 400) if filters == BAYER else (606, 402)
+    m = oracle.scene(wd, ht, seed=5, a=8.0, b=1.6, filters=filters)
+    ip = oracle.img_param(v.default_img_param(wd=wd, ht=ht, filters=filters))
+    ref = glsl_ref.rawhist(m, ip)
+    ours = oracle.rawhist(m, filters, BLACK, WHITE)
+    assert np.array_equal(ref[0], ours[0])
+    assert np.allclose(ref[1:], ours[1:], rtol=1e-5, atol=1e-4)

@@ -59,3 +59,15 @@ def test_waveform_of_a_develop(gpu):
     v.waveform(d.data_ptr(), wd, ht, w.data_ptr())
     torch.cuda.synchronize()
     assert np.array_equal(w.cpu().numpy().view(np.uint32), oracle.waveform(out.astype(np.float32)))
+
+
+def test_oracle_waveform_equals_the_reference_shader():
+    # hist/collect.comp compiled for the CPU, on values in [0, 1] (its float to unsigned conversion
+    # of negative values has no defined result in the C++ the shader is compiled to)
+    from oracle import glsl_ref
+    if not glsl_ref.available():
+        pytest.skip("reference shaders not built (oracle/_ref)")
+    rng = np.random.default_rng(1)
+    for (ht, wd, wo, ho) in ((90, 130, 64, 40), (300, 420, 1000, 600), (37, 19, 16, 9)):
+        img = rng.uniform(0, 1, (ht, wd, 4)).astype(np.float16).astype(np.float32)
+        assert np.array_equal(glsl_ref.waveform(img, wo, ho), oracle.waveform(img, wo, ho))

@@ -27,6 +27,7 @@ CASES = {
     "halfsize_1000x742": (1000, 742, BAYER, "param:demosaic:01:method:2\n", (0, 0)),
     "thumb_2048x1536": (2048, 1536, BAYER, "", (256, 192)),
     "xtrans_606x402": (606, 402, 9, "", (0, 0)),
+    "fixup_1000x742": (1000, 742, BAYER, "param:demosaic:01:colour:1\n", (0, 0)),
     "params_384x256": (384, 256, BAYER, "param:colour:01:exposure:0.7\nparam:llap:01:clarity:0\n"
                        "param:filmcurv:01:colour:1\nparam:filmcurv:01:contrast:1.5\nparam:hilite:01:white:0.9\n", (0, 0)),
 }

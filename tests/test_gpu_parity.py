@@ -41,6 +41,8 @@ def graph_setup(op):
             g.set_param("denoise", "strength", float(op.dn_strength))
         if op.dm_method != d.dm_method:
             g.set_param("demosaic", "method", np.int32(op.dm_method))
+        if op.dm_colour != d.dm_colour:
+            g.set_param("demosaic", "colour", np.int32(op.dm_colour))
         if op.ll_levels:
             g.set_llap_levels(op.ll_levels)
         if op.out_wd:
@@ -151,6 +153,14 @@ def test_rcd_variants(gpu, case):
     g, _ = run("rcd_" + case, m, ip, params(dm_method=1))
     want = oracle.rcd(g["hilite"], [ip.whitebalance[k] for k in range(3)])
     assert np.array_equal(g["demosaic"], want)
+
+
+@pytest.mark.parametrize("filters,wd,ht", [(BAYER, 1000, 742), (9, 606, 402)])
+def test_wide_fix_radius(gpu, filters, wd, ht):
+    # demosaic colour param 1: the fix radius clamp(fixup+1, 1, 2) = 2 on bayer (the node chain:
+    # gauss, splat, fix as separate kernels) and clamp(fixup+2, 2, 3) = 3 on x-trans
+    m, ip = scene(wd, ht, seed=wd + 13, filters=filters)
+    run("fix_radius_%dx%d_%d" % (wd, ht, filters == 9), m, ip, params(dm_colour=1), hist=True)
 
 
 def test_halfsize_method(gpu):

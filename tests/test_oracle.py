@@ -150,13 +150,13 @@ def _ref_available():
 
 
 @pytest.mark.skipif(not _ref_available(), reason="reference shaders not compiled here (oracle/_ref)")
-@pytest.mark.parametrize("seed", [101, 102, 103, 104, 105, 106, 107])
+@pytest.mark.parametrize("seed", [101, 102, 103, 104, 105, 106, 107, 108, 109])
 def test_oracle_matches_reference_shaders_random(seed):
     # 104: rcd; 105: rcd on an x-trans mosaic (the module runs it whatever the pattern);
     # 106: rcd on a cropped bayer mosaic; 107: the half size method on x-trans (resampled)
     from oracle import glsl_ref
     rng = np.random.default_rng(seed)
-    filters = gc.XTRANS if seed in (103, 105, 107) else gc.BAYER
+    filters = gc.XTRANS if seed in (103, 105, 107, 109) else gc.BAYER
     blk = 2 if filters == gc.BAYER else 6
     wd, ht = int(rng.integers(8, 40)) * blk, int(rng.integers(8, 30)) * blk
     m = v.scene_host(v.make_scene(wd, ht, seed=seed, a=gc.NOISE_A, b=gc.NOISE_B, filters=filters))
@@ -166,6 +166,7 @@ def test_oracle_matches_reference_shaders_random(seed):
     p.co_exposure = float(rng.uniform(-1, 1))
     p.ll_clarity = float(rng.uniform(0, 0.6))
     p.dm_method = {104: 1, 105: 1, 106: 1, 107: 2}.get(seed, 0)
+    p.dm_colour = {108: 1, 109: 1}.get(seed, 0)     # the wider fix radius (fix.comp:111,124)
     if seed == 106:
         ip.crop_aabb[0], ip.crop_aabb[1], ip.crop_aabb[2], ip.crop_aabb[3] = 4, 2, wd - 6, ht - 4
     st = ("denoise", "hilite", "demosaic", "colour", "filmcurv", "llap")

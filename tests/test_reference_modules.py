@@ -119,7 +119,7 @@ def test_fixture_is_what_the_reference_modules_emit_now():
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["darkroom_2048x1536", "wavelet_1000x742", "rcd_1000x742", "thumb_2048x1536",
-                                  "xtrans_606x402", "params_384x256"])
+                                  "xtrans_606x402", "params_384x256", "fixup_1000x742"])
 def test_develop_through_set_nodes_equals_cfg(gpu, name):
     case = CASES[name]
     wd, ht = case["in"]

@@ -371,7 +371,6 @@ int check_supported_params(vkdt_cuda_graph_t *g)
     for(int k = 0; k < 8; k++) id = id && c->f("perspect", k) == quad[k];
     if(!id) return fail(VKDT_CUDA_INCOMPLETE, "crop other than the identity (rotate 0, crop 0 1 0 1, the default quad) not built");
   }
-  if(g->mod("demosaic")->n("colour") != 0) return fail(VKDT_CUDA_INCOMPLETE, "demosaic colour (fixup radius) != 0 not supported");
   const int method = g->mod("demosaic")->n("method");
   if(method < 0 || method > 2) return fail(VKDT_CUDA_INCOMPLETE, "demosaic method %d not supported", method);
   const int fm = g->mod("filmcurv")->n("colour");
@@ -1045,7 +1044,9 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
   if(g->rcd && (g->W & 1)) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "rcd needs an even width");
   // bayer at full size runs fused; x-trans, rcd and reduced sizes run node by node,
   // bayer with the fused path's hilite front
-  g->unfused = xt || g->halfsize || g->rcd;
+  // a demosaic colour param >= 1 widens the bayer fix radius to 2 (fix.comp:124): node by node
+  const bool wide_fix = !xt && g->mod("demosaic")->n("colour") >= 1;
+  g->unfused = xt || g->halfsize || g->rcd || wide_fix;
   g->k1front = g->unfused && !xt;
 
   // node lists as the modules' create_nodes emit them

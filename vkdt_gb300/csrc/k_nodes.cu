@@ -11,6 +11,7 @@
 // tests) use explicit IEEE operations, as the oracle evaluates them.
 #include "common.cuh"
 #include "develop_px.cuh"
+#include "gauss.cuh"
 #include "hilite.cuh"
 #include "kernels.h"
 #include "pixel.cuh"
@@ -327,10 +328,10 @@ __global__ void __launch_bounds__(256) k_nd_splat_xt(const dev_nodes_t p)
   }
 }
 
-// demosaic/fix.comp:55-135 (x-trans): red and blue from the taps of radius 2
-// (3 with the colour param), weighted by the covariance of the block of
+// demosaic/fix.comp:55-135 (x-trans): red and blue from the taps of radius R
+// (2, or 3 with the colour param), weighted by the covariance of the block of
 // (x+1, y+1) and scaled by the splat green ratio; the centre keeps its green
-__global__ void __launch_bounds__(256) k_nd_fix_xt(const dev_nodes_t p)
+template<int R> __global__ void __launch_bounds__(256) k_nd_fix_xt(const dev_nodes_t p)
 {
   // mirrored, halo 3: hilite output, splat output and 1 / (1e-4 + splat output)
   __shared__ float shl[XT_TY + 6][XT_TX + 6 + 1], sgh[XT_TY + 6][XT_TX + 6 + 1], srg[XT_TY + 6][XT_TX + 6 + 1];
@@ -351,8 +352,8 @@ __global__ void __launch_bounds__(256) k_nd_fix_xt(const dev_nodes_t p)
     scls[sy][sx] = ((qx + qy) & 1) == 0 ? 1 : ((blue_top ^ (qy == 1)) ? 2 : 0);
   }
   __syncthreads();
-  // radius clamp(fixup + 2, 2, 3) = 2: the host admits fixup 0 only
-  constexpr int r = 2;
+  // radius clamp(fixup + 2, 2, 3) (fix.comp:111): the halo of 3 covers both
+  constexpr int r = R;
   for(int t = threadIdx.x; t < XT_TX * XT_TY; t += blockDim.x)
   {
     int lx, ly;
@@ -448,6 +449,97 @@ __global__ void __launch_bounds__(256) k_nd_resample(const dev_nodes_t p)
       for(int k = 0; k < 4; k++) res[k] += v[k] * w[0][i] * w[1][j];
     }
   p.dm[(size_t)y * p.ow + x] = mk_half4(res[0], res[1], res[2], res[3]);
+}
+
+// ---------------------------------------------------------------- bayer demosaic, node by node
+// (demosaic colour param >= 1: fix.comp:124 widens the fix radius to 2, which
+// the fused develop kernel's tile does not hold; gauss, splat and fix then run
+// as the reference's nodes, with f16 images in HBM between them)
+
+// demosaic/gauss.comp:24-75 (bayer): one thread per entry, the 8 greens at the
+// mirrored texel centres 2 pos + 0.5 + (i, j) of the hilite output
+__global__ void __launch_bounds__(256) k_nd_gauss_bayer(const dev_nodes_t p)
+{
+  const int x = blockIdx.x * 16 + threadIdx.x % 16, y = blockIdx.y * 16 + threadIdx.x / 16;
+  if(x >= p.hw || y >= p.hh) return;
+  float px[8];
+  int k = 0;
+#pragma unroll
+  for(int j = -1; j < 3; j++)
+#pragma unroll
+  for(int ii = -1; ii < 3; ii++)
+  {
+    if(((j + ii) & 1) != 1) continue;
+    px[k++] = dn_m(p, p.hl, 2 * x + ii, 2 * y + j);
+  }
+  float v[4];
+  int dec;
+  gauss_exact(px, v, dec);
+  p.cov[(size_t)y * p.hw + x] = mk_half4(v[0], v[1], v[2], v[3]);
+  if(p.dbg_gauss) p.dbg_gauss[(size_t)y * p.hw + x] = (uint8_t)dec;
+}
+
+// exp(-0.5 dot(E o / eval, E o)) for the tap offset o = (i, j), E the
+// eigenvector (c, s) and its normal (splat.comp:159-163, fix.comp:21-29)
+DEV float gauss_w(float c, float s, float e0, float e1, int i, int j)
+{
+  const float of0 = c * (float)i + s * (float)j, of1 = -s * (float)i + c * (float)j;
+  return expf(-0.5f * (of0 / e0 * of0 + of1 / e1 * of1));
+}
+
+// demosaic/splat.comp:142-266 (bayer): the greens of the 3x3 taps, centre
+// weight 666, taps past the border wrapped by the CFA period 6
+__global__ void __launch_bounds__(256) k_nd_splat_bayer(const dev_nodes_t p)
+{
+  const int x = blockIdx.x * 32 + threadIdx.x % 32, y = blockIdx.y * 8 + threadIdx.x / 32;
+  if(x >= p.W || y >= p.H) return;
+  float cov[4];
+  cov_z(p, (x + 1) / 2, (y + 1) / 2, cov);
+  const float e0 = gclamp(cov[0], 0.01f, 25.0f), e1 = gclamp(cov[1], 0.01f, 25.0f);
+  float gs = 0.0f, gw = 0.0f;
+#pragma unroll
+  for(int j = -1; j <= 1; j++)
+#pragma unroll
+    for(int i = -1; i <= 1; i++)
+    {
+      if(cfa_bayer(x + i, y + j) != 1) continue;
+      int px = x + i, py = y + j;
+      if(px < 0) px += 6;
+      if(py < 0) py += 6;
+      if(px >= p.W) px -= 6;
+      if(py >= p.H) py -= 6;
+      const float w = (i == 0 && j == 0) ? 666.0f : gclamp(gauss_w(cov[2], cov[3], e0, e1, i, j), 1e-4f, 1.0f);
+      gs += dn_z(p, p.hl, px, py) * w;
+      gw += w;
+    }
+  p.g[(size_t)y * p.W + x] = f2h(gs / fmaxf(1e-8f, gw));
+}
+
+// demosaic/fix.comp:99-135 (bayer) with radius R: red and blue from the ratio
+// of each tap to its splat green, weighted by the covariance of (x+1, y+1)/2
+template<int R> __global__ void __launch_bounds__(256) k_nd_fix_bayer(const dev_nodes_t p)
+{
+  const int x = blockIdx.x * 32 + threadIdx.x % 32, y = blockIdx.y * 8 + threadIdx.x / 32;
+  if(x >= p.W || y >= p.H) return;
+  const float gc = dn_m(p, p.g, x, y);
+  float cov[4];
+  cov_z(p, (x + 1) / 2, (y + 1) / 2, cov);
+  const float e0 = 2.0f * gclamp(cov[0], 1.0f, 49.0f), e1 = 2.0f * gclamp(cov[1], 1.0f, 49.0f);
+  float rgb[3] = { 0.0f, 0.0f, 0.0f }, w[3] = { 0.0f, 0.0f, 0.0f };
+#pragma unroll
+  for(int j = -R; j <= R; j++)
+#pragma unroll
+    for(int i = -R; i <= R; i++)
+    {
+      const int c = cfa_bayer(x + i, y + j);
+      if(c == 1) { rgb[1] = gc; w[1] = 1.0f; continue; }
+      const float gh = dn_m(p, p.g, x + i, y + j), col = dn_m(p, p.hl, x + i, y + j);
+      const float wt = gclamp(gauss_w(cov[2], cov[3], e0, e1, i, j), 1e-3f, 1.0f);
+      rgb[c] += col * (1e-4f + gc) / (1e-4f + gh) * wt;
+      w[c] += wt;
+    }
+  p.dm[(size_t)y * p.W + x] = mk_half4(rgb[0] / fmaxf(1e-8f, w[0]), rgb[1] / fmaxf(1e-8f, w[1]),
+                                       rgb[2] / fmaxf(1e-8f, w[2]), 1.0f);
 }
 
 // ---------------------------------------------------------------- post
@@ -555,9 +647,22 @@ cudaError_t launch_nodes(const dev_nodes_t &p, int stage, cudaStream_t s)
     case 0: k_nd_noop<<<dim3((p.W + 63) / 64, (p.H + 3) / 4), 256, 0, s>>>(p); break;
     case 1: if(xt) k_nd_hl_half<true><<<gh, 256, 0, s>>>(p); else k_nd_hl_half<false><<<gh, 256, 0, s>>>(p); break;
     case 2: if(xt) k_nd_hl_doub<true><<<gh, 256, 0, s>>>(p); else k_nd_hl_doub<false><<<gh, 256, 0, s>>>(p); break;
-    case 3: k_nd_gauss_xt<<<gh, 256, 0, s>>>(p); break;
-    case 4: k_nd_splat_xt<<<dim3((p.W + XT_TX - 1) / XT_TX, (p.H + XT_TY - 1) / XT_TY), 256, 0, s>>>(p); break;
-    case 5: k_nd_fix_xt<<<dim3((p.W + XT_TX - 1) / XT_TX, (p.H + XT_TY - 1) / XT_TY), 256, 0, s>>>(p); break;
+    case 3: if(xt) k_nd_gauss_xt<<<gh, 256, 0, s>>>(p); else k_nd_gauss_bayer<<<gh, 256, 0, s>>>(p); break;
+    case 4:
+      if(xt) k_nd_splat_xt<<<dim3((p.W + XT_TX - 1) / XT_TX, (p.H + XT_TY - 1) / XT_TY), 256, 0, s>>>(p);
+      else k_nd_splat_bayer<<<gf, 256, 0, s>>>(p);
+      break;
+    case 5:
+      if(xt)
+      { // fix.comp:111 radius clamp(fixup + 2, 2, 3)
+        const dim3 g((p.W + XT_TX - 1) / XT_TX, (p.H + XT_TY - 1) / XT_TY);
+        if(p.fixup >= 1) k_nd_fix_xt<3><<<g, 256, 0, s>>>(p); else k_nd_fix_xt<2><<<g, 256, 0, s>>>(p);
+      }
+      else
+      { // fix.comp:124 radius clamp(fixup + 1, 1, 2)
+        if(p.fixup >= 1) k_nd_fix_bayer<2><<<gf, 256, 0, s>>>(p); else k_nd_fix_bayer<1><<<gf, 256, 0, s>>>(p);
+      }
+      break;
     case 6: if(xt) k_nd_halfsize<true><<<gh, 256, 0, s>>>(p); else k_nd_halfsize<false><<<gh, 256, 0, s>>>(p); break;
     case 7: k_nd_resample<<<dim3((p.ow + 15) / 16, (p.oh + 15) / 16), 256, 0, s>>>(p); break;
     case 8: k_nd_hl_bayer<<<gh, 256, 0, s>>>(p); break;

@@ -64,6 +64,7 @@ typedef struct vkdt_cuda_img_param_t
   float    cam_to_rec2020[9];  /* row major camera rgb -> linear rec2020 */
   float    noise_a;            /* noise profile, gaussian part (normalised units) */
   float    noise_b;            /* noise profile, poissonian part (normalised units) */
+  uint32_t orientation;        /* exif orientation (crop's automatic rotation: 3, 6, 8) */
 }
 vkdt_cuda_img_param_t;
 
@@ -359,14 +360,18 @@ int  vkdt_cuda_nprof_fit(const double *hist, int bins, float *a, float *b);
 
 /* debug: copy an intermediate image of the last run to host floats.
  * stage 0 denoise output (1 ch), 1 hilite output (1 ch), both at the crop size;
- * 2 filmcurv output, 3 demosaic output and 4 colour output (4 ch each), at
- * the output size; with the wavelet denoise, its half size nodes (4 ch,
- * W/block x H/block): 5 half, 6 downcov, 7..9 down levels 1..3 (swizzled as
+ * 2 filmcurv output and 4 colour output (4 ch each) at the output size; 3
+ * demosaic output (4 ch) at the demosaic's size (the output size unless crop
+ * follows it); 11 crop output (4 ch, the output size; only when crop moves
+ * pixels); with the wavelet denoise, its half size nodes (4 ch, W/block x
+ * H/block): 5 half, 6 downcov, 7..9 down levels 1..3 (swizzled as
  * denoise/down.comp:102-104 stores them), 10 assemble. These are the images the reference's `-d perf` graph
  * would hold on those nodes' output connectors (graph.c:881-932).
- * requires vkdt_cuda_graph_set_debug(graph, 1) before alloc. */
+ * requires vkdt_cuda_graph_set_debug(graph, 1) before alloc (stage 2 does not).
+ * vkdt_cuda_graph_debug_stage_size gives a stage's width, height and channels. */
 int  vkdt_cuda_graph_set_debug(vkdt_cuda_graph_t *graph, int enable);
 int  vkdt_cuda_graph_debug_stage(vkdt_cuda_graph_t *graph, int stage, float *out, size_t count);
+int  vkdt_cuda_graph_debug_stage_size(vkdt_cuda_graph_t *graph, int stage, int *wd, int *ht, int *channels);
 /* debug: the discrete decisions the last run took, one element per texel of
  * a wd x ht grid (written to *wd, *ht; out may be null to ask for the size).
  * kind 0: demosaic/gauss.comp per entry (W/block x H/block), u8: bit 0 the

@@ -114,6 +114,7 @@ class Params(C.Structure):
         ("fc_blue", C.c_float), ("fc_shadows", C.c_float),
         ("ll_sigma", C.c_float), ("ll_shadows", C.c_float), ("ll_hilights", C.c_float), ("ll_clarity", C.c_float),
         ("ll_levels", C.c_int32), ("out_wd", C.c_int32), ("out_ht", C.c_int32),
+        ("cr_on", C.c_int32), ("cr_wd", C.c_int32), ("cr_ht", C.c_int32), ("cr_block", C.c_float * 20),
     ]
 
 
@@ -122,7 +123,7 @@ class Stages(C.Structure):
         ("denoise", C.POINTER(C.c_float)), ("hilite", C.POINTER(C.c_float)), ("demosaic", C.POINTER(C.c_float)),
         ("colour", C.POINTER(C.c_float)), ("filmcurv", C.POINTER(C.c_float)), ("hist", C.POINTER(C.c_uint32)),
         ("llap", C.POINTER(C.c_float)), ("out_wd", C.c_int32), ("out_ht", C.c_int32),
-        ("llap_levels", C.c_int32), ("hilite_levels", C.c_int32),
+        ("llap_levels", C.c_int32), ("hilite_levels", C.c_int32), ("crop", C.POINTER(C.c_float)),
     ]
 
 
@@ -150,6 +151,8 @@ def lib():
             f.restype = C.c_int
             f.argtypes = [C.POINTER(C.c_uint16), C.c_int, C.c_int, C.POINTER(ImgParam), C.POINTER(Params), C.POINTER(Stages)]
         l.oracle_set_perturb.argtypes = [C.c_uint32]
+        l.oracle_crop_commit.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_float, C.c_uint32, C.c_void_p,
+                                         C.POINTER(C.c_int), C.POINTER(C.c_int)]
         l.oracle_denoise_nodes.restype = C.c_int
         l.oracle_denoise_nodes.argtypes = [C.POINTER(C.c_uint16), C.c_int, C.c_int, C.POINTER(ImgParam),
                                            C.POINTER(Params), C.c_void_p * 6, C.c_void_p * 7, C.POINTER(Decisions)]
@@ -207,7 +210,7 @@ def _fptr(a):
     return a.ctypes.data_as(C.POINTER(C.c_float))
 
 
-START = {"hilite": 1, "demosaic": 2, "colour": 3, "filmcurv": 4, "llap": 5}
+START = {"hilite": 1, "demosaic": 2, "crop": 3, "colour": 4, "filmcurv": 5, "llap": 6}
 
 
 def develop(mosaic, ip, params=None, double=False, stages=("llap",), record=False, force=None, start=None,
@@ -226,8 +229,11 @@ def develop(mosaic, ip, params=None, double=False, stages=("llap",), record=Fals
     params = params or default_params()
     W = ip.crop_aabb[2] - ip.crop_aabb[0]
     H = ip.crop_aabb[3] - ip.crop_aabb[1]
-    ow = params.out_wd or (W if params.dm_method != 2 else (W + 1) // 2)   # method 2 halves the size
-    oh = params.out_ht or (H if params.dm_method != 2 else (H + 1) // 2)
+    dw = params.out_wd or (W if params.dm_method != 2 else (W + 1) // 2)   # method 2 halves the size
+    dh = params.out_ht or (H if params.dm_method != 2 else (H + 1) // 2)
+    ow, oh = (params.cr_wd, params.cr_ht) if params.cr_on else (dw, dh)   # the stages after crop
+    if "crop" in stages and not params.cr_on:
+        raise ValueError("the crop stage needs params.cr_on (set_crop)")
     st = Stages()
     bufs = {}
     for name in stages:
@@ -235,6 +241,8 @@ def develop(mosaic, ip, params=None, double=False, stages=("llap",), record=Fals
             bufs[name] = np.zeros((H, W), np.float32)
         elif name == "hist":
             bufs[name] = np.zeros(257, np.uint32)
+        elif name == "demosaic":
+            bufs[name] = np.zeros((dh, dw, 4), np.float32)
         else:
             bufs[name] = np.zeros((oh, ow, 4), np.float32)
         if name == "hist":
@@ -321,6 +329,26 @@ def denoise_nodes(mosaic, ip, params, inputs, force=None):
     res = dict(zip(DENOISE_NODES, outs[:6]))
     res["doub"] = outs[6]
     return res
+
+
+def crop_commit(wd, ht, perspect=(0.25, 0.25, 0.75, 0.25, 0.75, 0.75, 0.25, 0.75), crop=(1.0, 3.0, 3.0, 7.0),
+                rotate=1337.0, orientation=0):
+    """crop/main.c commit_params and modify_roi_out restated for an input of
+    wd x ht: (the 20 float committed block, output width, output height)"""
+    blk = (C.c_float * 20)()
+    ow, oh = C.c_int(), C.c_int()
+    pp = (C.c_float * 8)(*perspect)
+    cc = (C.c_float * 4)(*crop)
+    lib().oracle_crop_commit(wd, ht, pp, cc, float(rotate), orientation, blk, C.byref(ow), C.byref(oh))
+    return np.array(blk[:], np.float32), ow.value, oh.value
+
+
+def set_crop(params, block, wd, ht):
+    """switch the crop stage on in oracle params with a committed block and output size"""
+    params.cr_on, params.cr_wd, params.cr_ht = 1, int(wd), int(ht)
+    for i in range(20):
+        params.cr_block[i] = float(block[i])
+    return params
 
 
 def scene(wd, ht, seed=0, image_id=0, filters=0x94949494, black=512.0, white=16383.0, a=2.0, b=0.4,

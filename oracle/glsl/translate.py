@@ -27,7 +27,7 @@ SHADERS = [
     ("hilite", "half"), ("hilite", "reduce"), ("hilite", "assemble"), ("hilite", "doub"),
     ("demosaic", "down"), ("demosaic", "gauss"), ("demosaic", "splat"), ("demosaic", "fix"),
     ("demosaic", "halfsize"), ("demosaic", "rcd_conv"), ("demosaic", "rcd_fill"), ("shared", "resample"),
-    ("colour", "main"), ("filmcurv", "main"),
+    ("crop", "main"), ("colour", "main"), ("filmcurv", "main"),
     ("llap", "curve"), ("llap", "reduce"), ("llap", "assemble"), ("llap", "colour"),
     ("i-mcraw", "decode"), ("colenc", "main"), ("grade", "main"), ("rawhist", "collect"), ("hist", "collect"),
 ]
@@ -148,7 +148,11 @@ def swizzle_overloads(text):
 
 def block_struct(name, body):
     members = []
-    for decl in [d.strip() for d in body.split(";") if d.strip()]:
+    decls = []
+    for d in [d.strip() for d in body.split(";") if d.strip()]:
+        m = re.match(r"(\w+)\s+(\w+(?:\s*,\s*\w+)+)$", d)   # float a, b, c: one member each
+        decls += ["%s %s" % (m.group(1), n.strip()) for n in m.group(2).split(",")] if m else [d]
+    for decl in decls:
         m = re.match(r"(\w+)\s+(\w+)\s*(\[[^\]]*\])?$", decl)
         if not m:
             raise RuntimeError("cannot parse block member: " + decl)

@@ -212,6 +212,14 @@ def develop(mosaic, ip, params=None, stages=("llap",)):
     if "demosaic" in stages:
         out["demosaic"] = rgb.a.copy()
 
+    # ---- crop (crop/main.comp on the block crop/main.c:276-343 commits)
+    if p.cr_on:
+        cr = Img(p.cr_wd, p.cr_ht, 4)
+        run("crop_main", p.cr_wd, p.cr_ht, {0: rgb, 1: cr}, uniform=f32(*p.cr_block))
+        rgb = cr
+        if "crop" in stages:
+            out["crop"] = rgb.a.copy()
+
     # ---- colour (colour/main.c:219-365 commit_params, 415-466 create_nodes)
     cw = [0.0, 0.0, 0.0]
     pw = [float(p.co_white[k]) for k in range(3)]

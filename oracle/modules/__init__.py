@@ -15,7 +15,7 @@ HRN_MAX_NODES, HRN_MAX_MODULES = 512, 16
 class HrnImg(C.Structure):
     _fields_ = [("black", C.c_float * 4), ("white", C.c_float * 4), ("whitebalance", C.c_float * 4),
                 ("filters", C.c_uint32), ("crop_aabb", C.c_uint32 * 4), ("cam_to_rec2020", C.c_float * 9),
-                ("noise_a", C.c_float), ("noise_b", C.c_float)]
+                ("noise_a", C.c_float), ("noise_b", C.c_float), ("orientation", C.c_uint32)]
 
 
 class HrnNode(C.Structure):
@@ -66,6 +66,7 @@ def run(cfg, wd, ht, ip, out_wd=0, out_ht=0):
     for k in range(9):
         img.cam_to_rec2020[k] = ip.cam_to_rec2020[k]
     img.noise_a, img.noise_b = ip.noise_a, ip.noise_b
+    img.orientation = getattr(ip, "orientation", 0)
     nodes = (HrnNode * HRN_MAX_NODES)()
     mods = (HrnModule * HRN_MAX_MODULES)()
     nn, nm = C.c_int(0), C.c_int(0)

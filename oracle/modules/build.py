@@ -13,7 +13,7 @@ REF = os.path.join(os.path.dirname(HERE), "_ref")
 TREE = os.environ.get("VKDT_REFERENCE", "/root/reference")
 SRC = os.path.join(TREE, "src")
 MODULES_DIR = os.path.join(SRC, "pipe", "modules")
-CHAIN = ["denoise", "hilite", "demosaic", "colour", "filmcurv", "llap"]
+CHAIN = ["denoise", "hilite", "demosaic", "crop", "colour", "filmcurv", "llap"]
 EXTRA = ["nprof"]   # modules driven on their own (write_sink)
 HARNESS = os.path.join(REF, "libvkdt_modharness.so")
 
@@ -27,18 +27,24 @@ def available():
     return os.path.exists(HARNESS) and all(os.path.exists(os.path.join(REF, "mod_%s.so" % m)) for m in CHAIN + EXTRA)
 
 
+def _stale(out, srcs):
+    return not os.path.exists(out) or any(os.path.getmtime(s) > os.path.getmtime(out) for s in srcs)
+
+
 def build(force=False):
     if not os.path.isdir(MODULES_DIR):
         return available()
-    if available() and not force:
-        return True
     os.makedirs(REF, exist_ok=True)
+    shim = os.path.join(HERE, "shim", "vulkan", "vulkan.h")
     jobs = []
     for m in CHAIN + EXTRA:
         out = os.path.join(REF, "mod_%s.so" % m)
-        jobs.append(["gcc"] + flags() + ["-shared", "-o", out, os.path.join(MODULES_DIR, m, "main.c"), "-lm"])
-    jobs.append(["gcc"] + flags() + ["-shared", "-o", HARNESS, os.path.join(HERE, "harness.c"),
-                                     os.path.join(SRC, "pipe", "connector.c"), "-ldl", "-lm"])
+        src = os.path.join(MODULES_DIR, m, "main.c")
+        if force or _stale(out, [src, shim]):
+            jobs.append(["gcc"] + flags() + ["-shared", "-o", out, src, "-lm"])
+    hsrc = [os.path.join(HERE, "harness.c"), os.path.join(SRC, "pipe", "connector.c")]
+    if force or _stale(HARNESS, hsrc + [shim]):
+        jobs.append(["gcc"] + flags() + ["-shared", "-o", HARNESS] + hsrc + ["-ldl", "-lm"])
     procs = [(j, subprocess.Popen(j, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)) for j in jobs]
     for j, p in procs:
         out = p.communicate()[0].decode()

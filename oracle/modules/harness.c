@@ -43,6 +43,7 @@ typedef struct hrn_img_t
   uint32_t crop_aabb[4];
   float    cam_to_rec2020[9];
   float    noise_a, noise_b;
+  uint32_t orientation;   // exif orientation (crop's auto rotation reads it)
 }
 hrn_img_t;
 
@@ -383,6 +384,7 @@ int hrn_run(const char *modules_dir, const char *so_dir, const char *cfg, int wd
     for(int k = 0; k < 4; k++) p->crop_aabb[k] = img->crop_aabb[k];
     for(int k = 0; k < 9; k++) p->cam_to_rec2020[k] = img->cam_to_rec2020[k];
     p->noise_a = img->noise_a; p->noise_b = img->noise_b;
+    p->orientation = img->orientation;
     p->colour_primaries = s_colour_primaries_custom; p->colour_trc = s_colour_trc_linear;
     p->input_name = tok("main");
   }

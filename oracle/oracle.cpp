@@ -1051,6 +1051,148 @@ template<class T> static img_t<T> shared_resample(const img_t<T> &in, int wd, in
   return out;
 }
 
+// shared.glsl:47-96 sample_catmull_rom at normalised uv: nine bilinear taps,
+// the positions divided back to normalised coordinates as the shader does
+template<class T> static void catmull_rom_uv(const img_t<T> &in, T u, T v, T res[4])
+{
+  const T ts[2] = { T(in.w), T(in.h) };
+  const T uv[2] = { u, v };
+  T tp[3][2], w[3][2];
+  for(int k = 0; k < 2; k++)
+  {
+    const T sp = uv[k] * ts[k];
+    const T tp1 = std::floor(sp - T(0.5)) + T(0.5);
+    const T f = sp - tp1;
+    const T w0 = f * (T(-0.5) + f * (T(1.0) - T(0.5) * f));
+    const T w1 = T(1.0) + f * f * (T(-2.5) + T(1.5) * f);
+    const T w2 = f * (T(0.5) + f * (T(2.0) - T(1.5) * f));
+    const T w3 = f * f * (T(-0.5) + T(0.5) * f);
+    w[0][k] = w0; w[1][k] = w1 + w2; w[2][k] = w3;
+    tp[0][k] = (tp1 - T(1.0)) / ts[k];
+    tp[1][k] = (tp1 + w2 / (w1 + w2)) / ts[k];
+    tp[2][k] = (tp1 + T(2.0)) / ts[k];
+  }
+  for(int c = 0; c < 4; c++) res[c] = T(0);
+  for(int j = 0; j < 3; j++) for(int i = 0; i < 3; i++)
+  {
+    T t[4];
+    tex_bilinear(in, tp[i][0] * ts[0], tp[j][1] * ts[1], t);
+    for(int c = 0; c < 4; c++) res[c] += t[c] * w[i][0] * w[j][1];
+  }
+}
+
+// ------------------------------------------------------------------ crop
+
+// crop/main.comp:19-55. b is the committed block (crop/main.c:276-343): the
+// homography H as three columns padded to four floats (b[0..11]), the
+// rotation mat2(r0, r1, r2, r3) (b[12..15]) and the window x X y Y
+// (b[16..19]). Per output pixel the input position is found by undoing the
+// operations in reverse: the window's top left corner, the rotation about the
+// input's centre, then H with the homogeneous divide. Matrix products sum
+// their terms column by column, as GLSL's mat * vec. Outside [0,1)^2 the
+// output is 0; without rotation (r0 == 1) the nearest texel is fetched,
+// otherwise the Catmull-Rom filter samples. Alpha is stored as 1.
+template<class T> static img_t<T> crop_main(const img_t<T> &in, const float *b, int wd, int ht)
+{
+  img_t<T> out(wd, ht, 4);
+  const T tsx = T(in.w), tsy = T(in.h);
+  OMP_FOR
+  for(int y = 0; y < ht; y++) for(int x = 0; x < wd; x++)
+  {
+    T px = T(x) + T(0.5), py = T(y) + T(0.5);
+    px = px + T(b[16]) * tsx;
+    py = py + T(b[18]) * tsy;
+    const T vx = px - tsx * T(0.5), vy = py - tsy * T(0.5);
+    px = (T(b[12]) * vx + T(b[14]) * vy) + tsx * T(0.5);
+    py = (T(b[13]) * vx + T(b[15]) * vy) + tsy * T(0.5);
+    const T hx = (T(b[0]) * px + T(b[4]) * py) + T(b[8]);
+    const T hy = (T(b[1]) * px + T(b[5]) * py) + T(b[9]);
+    const T hz = (T(b[2]) * px + T(b[6]) * py) + T(b[10]);
+    const T rx = hx / hz / tsx, ry = hy / hz / tsy;
+    T rgba[4] = { T(0), T(0), T(0), T(0) };
+    // a position without value (hz = 0) is left undefined by the shader: 0 here
+    if(!(rx >= T(0) && ry >= T(0) && rx < T(1) && ry < T(1))) {}
+    else if(b[12] != 1.0f) catmull_rom_uv(in, rx, ry, rgba);
+    else
+    {
+      const int ix = (int)(rx * tsx), iy = (int)(ry * tsy);
+      for(int c = 0; c < 4; c++) rgba[c] = fetch_z(in, ix, iy, c);
+    }
+    rgba[3] = T(1);
+    out.store(x, y, rgba, 4);
+  }
+  return out;
+}
+
+// core/gaussian_elimination.h:40-109 (gauss_solve, after H. Spaeth,
+// "Numerik", 1994): Gaussian elimination with partial pivoting in the form of
+// LINPACK's dgefa/dgesl. A is n x n row major. Column k's pivot is the first
+// row of largest magnitude; the pivot row is swapped only right of column k,
+// the multipliers (negated) stay where they were formed, and the right hand
+// side is permuted step by step while it is reduced. The operations and their
+// order are the reference's, so the solution is the same to the last bit.
+// Returns false for a singular matrix (b untouched).
+static bool solve_pivoted(double *A, double *b, int n)
+{
+  auto a = [&](int r, int c) -> double & { return A[r * n + c]; };
+  int piv[16];
+  for(int k = 0; k < n; k++)
+  {
+    int m = k;
+    for(int r = k + 1; r < n; r++) if(std::fabs(a(r, k)) > std::fabs(a(m, k))) m = r;
+    piv[k] = m;
+    const double t = a(m, k);
+    a(m, k) = a(k, k);
+    a(k, k) = t;
+    if(t == 0.0) return false;
+    for(int r = k + 1; r < n; r++) a(r, k) /= -t;
+    if(m != k) for(int c = k + 1; c < n; c++) std::swap(a(m, c), a(k, c));
+    for(int r = k + 1; r < n; r++) for(int c = k + 1; c < n; c++) a(r, c) += a(r, k) * a(k, c);
+  }
+  for(int k = 0; k + 1 < n; k++)
+  {
+    std::swap(b[piv[k]], b[k]);
+    const double t = b[k];
+    for(int r = k + 1; r < n; r++) b[r] += a(r, k) * t;
+  }
+  for(int k = n - 1; k > 0; k--)
+  {
+    b[k] /= a(k, k);
+    const double t = b[k];
+    for(int r = 0; r < k; r++) b[r] -= a(r, k) * t;
+  }
+  b[0] /= a(0, 0);
+  return true;
+}
+
+// crop/main.c:175-226 get_crop_rot: rotation 1337 takes the exif orientation
+// (3: 180, 8: 90, 6: 270 degrees, else 0); the window 1,3,3,7 becomes a 3 px
+// margin (none at 400 px or less), transposed for the quarter turns
+static void crop_rot(uint32_t orient, double wd, double ht, const float pcrop[4], float prot, float crop[4], float *rot)
+{
+  *rot = prot;
+  for(int k = 0; k < 4; k++) crop[k] = pcrop[k];
+  if(prot == 1337.0f) *rot = orient == 3 ? 180.0f : orient == 8 ? 90.0f : orient == 6 ? 270.0f : 0.0f;
+  if(crop[0] == 1.0 && crop[1] == 3.0 && crop[2] == 3.0 && crop[3] == 7.0)
+  {
+    const double mw = wd > 400 ? 3.0 / wd : 0.0, mh = ht > 400 ? 3.0 / ht : 0.0;
+    const float r = *rot;
+    const bool quarter = (r >= 45 && r < 135) || (r >= 225 && r < 315);
+    if(quarter)
+    {
+      crop[0] = 0.5 - (.5 - mh) * ht / wd;
+      crop[2] = 0.5 - (.5 - mw) * wd / ht;
+      crop[1] = 0.5 + (.5 - mh) * ht / wd;
+      crop[3] = 0.5 + (.5 - mw) * wd / ht;
+    }
+    else
+    {
+      crop[0] = mw; crop[2] = mh;
+      crop[1] = 1.0 - mw; crop[3] = 1.0 - mh;
+    }
+  }
+}
+
 // ------------------------------------------------------------------ demosaic RCD (method 1)
 
 // demosaic/rcd_conv.comp:8-49: per pixel the vertical/horizontal
@@ -2287,18 +2429,23 @@ template<class T> static int develop(const uint16_t *mosaic, int wd, int ht,
     img_t<T> g = demosaic_splat(hl, cov, W, H, filters);
     rgb = demosaic_fix(hl, g, cov, W, H, filters, p->dm_colour);
   }
-  if(g_inj.start >= 3) rgb = from_float<T>(g_inj.img, rgb.w, rgb.h, 4);
-  if(st) { to_float(rgb, st->demosaic); st->out_wd = rgb.w; st->out_ht = rgb.h; }
+  if(g_inj.start == 3 || (g_inj.start > 3 && !p->cr_on)) rgb = from_float<T>(g_inj.img, rgb.w, rgb.h, 4);
+  if(st) to_float(rgb, st->demosaic);
+
+  // ---- crop (crop/main.comp) when connected between demosaic and colour
+  if(p->cr_on && g_inj.start >= 4) rgb = from_float<T>(g_inj.img, p->cr_wd, p->cr_ht, 4);
+  else if(p->cr_on) rgb = crop_main(rgb, p->cr_block, p->cr_wd, p->cr_ht);
+  if(st) { if(p->cr_on) to_float(rgb, st->crop); st->out_wd = rgb.w; st->out_ht = rgb.h; }
 
   // ---- colour, filmcurv (+ histogram of its input), llap
   if(p->fc_colour != 1 && p->fc_colour != 3) return 5; // filmcurv colour modes restated: 1, 3
   if(p->co_sat != 1.0f) return 6;                       // colour saturation path not restated
   img_t<T> col = colour_main(rgb, ip, p);
-  if(g_inj.start >= 4) col = from_float<T>(g_inj.img, col.w, col.h, 4);
+  if(g_inj.start >= 5) col = from_float<T>(g_inj.img, col.w, col.h, 4);
   if(st) to_float(col, st->colour);
   if(st && st->hist) hist(col, st->hist);
   img_t<T> fc = filmcurv_main(col, p);
-  if(g_inj.start >= 5) fc = from_float<T>(g_inj.img, fc.w, fc.h, 4);
+  if(g_inj.start >= 6) fc = from_float<T>(g_inj.img, fc.w, fc.h, 4);
   if(st) to_float(fc, st->filmcurv);
 
   // llap (llap/main.c:6-106)
@@ -2443,6 +2590,40 @@ void oracle_scene(int wd, int ht, uint32_t seed, uint32_t image_id, uint32_t fil
   scene_layout_make(&s, wd, ht, seed, image_id, filters, black, white, noise_a, noise_b, wb, pan_x, pan_y);
   OMP_FOR
   for(int y = 0; y < ht; y++) for(int x = 0; x < wd; x++) out[(size_t)y * wd + x] = scene_pixel(&s, x, y);
+}
+
+void oracle_crop_commit(int wd, int ht, const float perspect[8], const float pcrop[4], float rotate,
+    uint32_t orientation, float block[20], int *out_wd, int *out_ht)
+{ // crop/main.c:228-275 (modify_roi_in/out at full resolution) and :276-343 (commit_params)
+  float crop[4], rot;
+  crop_rot(orientation, (float)wd, (float)ht, pcrop, rotate, crop, &rot);
+  const float cw = crop[1] - crop[0], ch = crop[3] - crop[2];
+  *out_wd = (int)(uint32_t)std::min(32768.0f, (float)(uint32_t)wd * cw);
+  *out_ht = (int)(uint32_t)std::min(32768.0f, (float)(uint32_t)ht * ch);
+  // the homography taking the axis aligned quad (a,b) (A,b) (A,B) (a,B) to the given one
+  // (P. Heckbert, "Fundamentals of Texture Mapping and Image Warping", 1989, pp. 17-21)
+  float q[8];
+  for(int k = 0; k < 4; k++) { q[2 * k] = (float)(uint32_t)wd * perspect[2 * k]; q[2 * k + 1] = (float)(uint32_t)ht * perspect[2 * k + 1]; }
+  const float u[8] = { q[0], q[1], q[2], q[1], q[2], q[7], q[0], q[7] };
+  double M[64], r[9];
+  for(int k = 0; k < 4; k++)
+  {
+    double *ex = M + 8 * k, *ey = M + 8 * (k + 4);
+    const float ux = u[2 * k], uy = u[2 * k + 1];
+    ex[0] = ux; ex[1] = uy; ex[2] = 1; ex[3] = 0; ex[4] = 0; ex[5] = 0;
+    ex[6] = -q[2 * k] * ux; ex[7] = -q[2 * k] * uy;             // float products, as the reference
+    ey[0] = 0; ey[1] = 0; ey[2] = 0; ey[3] = ux; ey[4] = uy; ey[5] = 1;
+    ey[6] = -q[2 * k + 1] * ux; ey[7] = -q[2 * k + 1] * uy;
+    r[k] = q[2 * k]; r[k + 4] = q[2 * k + 1];
+  }
+  r[8] = 1.0;
+  solve_pivoted(M, r, 8);
+  const int col[12] = { 0, 3, 6, -1, 1, 4, 7, -1, 2, 5, 8, -1 };   // padded column major
+  for(int k = 0; k < 12; k++) block[k] = col[k] < 0 ? 0.0f : (float)r[col[k]];
+  const float rad = rot * 3.1415629 / 180.0f;
+  block[12] = cosf(rad); block[13] = sinf(rad);
+  block[14] = -sinf(rad); block[15] = cosf(rad);
+  for(int k = 0; k < 4; k++) block[16 + k] = crop[k];
 }
 
 void oracle_noop(const uint16_t *mosaic, int wd, int ht, const oracle_img_param_t *ip, float *out)

@@ -63,6 +63,11 @@ typedef struct oracle_params_t
   /* requested output size of the demosaic module (0 = full size). a smaller
    * size switches to the half-size demosaic + resample (demosaic/main.c:93-111) */
   int32_t out_wd, out_ht;
+  /* crop between demosaic and colour (crop/main.comp): 0 off, else its
+   * committed uniform block (crop/main.c:276-343: mat3 H as three padded
+   * columns, the rotation r0..r3, the window x X y Y) and its output size */
+  int32_t cr_on, cr_wd, cr_ht;
+  float   cr_block[20];
 }
 oracle_params_t;
 
@@ -79,6 +84,7 @@ typedef struct oracle_stages_t
   int32_t   out_wd, out_ht; /* written: size of the rgb stages */
   int32_t   llap_levels;    /* written: pyramid depth used */
   int32_t   hilite_levels;  /* written: number of hilite reduce nodes */
+  float    *crop;      /* crop output (when cr_on), ow*oh*4 */
 }
 oracle_stages_t;
 
@@ -116,6 +122,12 @@ void oracle_gauss_decisions(const float *mosaic, int wd, int ht, uint32_t filter
 void oracle_scene(int wd, int ht, uint32_t seed, uint32_t image_id, uint32_t filters, float black, float white,
     float noise_a, float noise_b, const float wb[3], float pan_x, float pan_y, uint16_t *out);
 
+/* crop/main.c's commit_params and modify_roi_out restated: the committed block
+ * (20 floats) and the output size for an input of wd x ht, the params
+ * perspect[8], crop[4], rotate and the image's exif orientation */
+void oracle_crop_commit(int wd, int ht, const float perspect[8], const float crop[4], float rotate,
+    uint32_t orientation, float block[20], int *out_wd, int *out_ht);
+
 /* the default parameters of the six modules plus the darkroom .cfg values
  * (bin/default-darkroom.i-raw:28-32) */
 void oracle_default_params(oracle_params_t *p);
@@ -142,10 +154,11 @@ void oracle_set_perturb(uint32_t seed);
 int oracle_denoise_nodes(const uint16_t *mosaic, int wd, int ht, const oracle_img_param_t *ip,
     const oracle_params_t *p, const float *const in[6], float *const out[7], oracle_decisions_t *dec);
 /* FP32, the path from a given stage on: start 1 hilite (input: the denoise output,
- * W*H), 2 demosaic (input: the hilite output, W*H), 3 colour (input: the demosaic
- * output, rgba), 4 filmcurv (input: the colour output), 5 llap (input: the
- * filmcurv output); the stages before it are replaced by the input (node-wise
- * checks of another implementation's stages on its own inputs) */
+ * W*H), 2 demosaic (input: the hilite output, W*H), 3 crop (input: the demosaic
+ * output, rgba; without crop the same as 4), 4 colour (input: the output of
+ * the stage before colour, rgba), 5 filmcurv (input: the colour output), 6 llap
+ * (input: the filmcurv output); the stages before it are replaced by the input
+ * (node-wise checks of another implementation's stages on its own inputs) */
 int oracle_develop_from_f32(const uint16_t *mosaic, int wd, int ht, const oracle_img_param_t *ip,
     const oracle_params_t *p, oracle_stages_t *out, oracle_decisions_t *dec, int start, const float *input);
 

@@ -37,7 +37,7 @@ def main():
         wd, ht, filters, seed, white, overrides, stages = case
         m = v.scene_host(v.make_scene(wd, ht, seed=seed, a=NOISE_A, b=NOISE_B, filters=filters))
         ip = oracle.img_param(img_param(v, wd, ht, filters, white))
-        p = oracle_params(oracle, overrides)
+        p = oracle_params(oracle, overrides, wd, ht)
         r = glsl_ref.develop(m, ip, p, stages=stages)
         arrays = {"mosaic": m}
         for s in stages:

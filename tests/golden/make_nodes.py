@@ -18,6 +18,7 @@ from oracle import modules as M            # noqa: E402
 from oracle.modules import build as MB     # noqa: E402
 
 BAYER = 0x94949494
+QUAD = (0.25, 0.25, 0.75, 0.25, 0.75, 0.75, 0.25, 0.75)   # crop/params: the default perspective quad
 # name: (wd, ht, filters, extra cfg lines, output size)
 CASES = {
     "darkroom_2048x1536": (2048, 1536, BAYER, "", (0, 0)),
@@ -31,22 +32,35 @@ CASES = {
     "params_384x256": (384, 256, BAYER, "param:colour:01:exposure:0.7\nparam:llap:01:clarity:0\n"
                        "param:filmcurv:01:colour:1\nparam:filmcurv:01:contrast:1.5\nparam:hilite:01:white:0.9\n", (0, 0)),
 }
+# with crop between demosaic and colour (the darkroom cfg's own): name: (wd, ht, filters, extra, exif orientation)
+CROP_CASES = {
+    "crop_2048x1536": (2048, 1536, BAYER, "", 0),
+    "crop_6000x4000": (6000, 4000, BAYER, "", 0),
+    "crop_orient6_1000x742": (1000, 742, BAYER, "", 6),
+    "crop_orient8_606x402": (606, 402, 9, "", 8),
+    "crop_persp_1024x768": (1024, 768, BAYER, "param:crop:01:perspect:0.2:0.22:0.8:0.25:0.77:0.8:0.21:0.75\n"
+                            "param:crop:01:crop:0.1:0.9:0.05:0.95\nparam:crop:01:rotate:3.5\n", 0),
+    "crop_rcd_1000x742": (1000, 742, BAYER, "param:demosaic:01:method:1\n", 0),
+}
 NA, NB = 2.0 / (16383 - 512) ** 2, 0.4 / (16383 - 512)
 
 
-def case_ip(wd, ht, filters):
-    return v.default_img_param(wd=wd, ht=ht, filters=filters, noise_a=NA, noise_b=NB)
+def case_ip(wd, ht, filters, orientation=0):
+    ip = v.default_img_param(wd=wd, ht=ht, filters=filters, noise_a=NA, noise_b=NB)
+    ip.orientation = orientation
+    return ip
 
 
 def generate():
     if not MB.build():
         raise SystemExit("the vkdt tree is needed (VKDT_REFERENCE)")
     out = {}
-    for name, (wd, ht, filters, extra, (ow, oh)) in CASES.items():
-        cfg = v.DARKROOM_CFG + extra
-        nodes, mods = M.run(cfg, wd, ht, case_ip(wd, ht, filters), ow, oh)
+    todo = [(n, wd, ht, f, v.DARKROOM_CFG + e, o, 0) for n, (wd, ht, f, e, o) in CASES.items()]
+    todo += [(n, wd, ht, f, v.DARKROOM_CROP_CFG + e, (0, 0), r) for n, (wd, ht, f, e, r) in CROP_CASES.items()]
+    for name, wd, ht, filters, cfg, (ow, oh), orient in todo:
+        nodes, mods = M.run(cfg, wd, ht, case_ip(wd, ht, filters, orient), ow, oh)
         out[name] = {
-            "in": [wd, ht], "filters": filters, "cfg": cfg, "out": [ow, oh],
+            "in": [wd, ht], "filters": filters, "cfg": cfg, "out": [ow, oh], "orientation": orient,
             "nodes": [{"name": n["name"], "kernel": n["kernel"], "wd": n["wd"], "ht": n["ht"], "dp": n["dp"],
                        "push": n["push"].hex(),
                        "uniform": mods[n["module"]]["uniform"].hex() if n["module"] >= 0 else ""} for n in nodes],

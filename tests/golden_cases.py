@@ -16,6 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden")
 
 BAYER, XTRANS = 0x94949494, 9
+QUAD = (0.25, 0.25, 0.75, 0.25, 0.75, 0.75, 0.25, 0.75)   # crop/params: the untouched perspective quad
 
 # noise profile of the generated mosaics, in raw DN (gaussian a, poissonian b)
 NOISE_A, NOISE_B = 8.0, 1.6
@@ -39,6 +40,15 @@ CASES = {
     "bayer_124x58_rcd_clipped": (124, 58, BAYER, 14, 9000.0, {"dm_method": 1}, ("demosaic", "llap")),
     # demosaic method 2: the half size demosaic at half the output size
     "bayer_120x90_halfsize": (120, 90, BAYER, 15, 16383.0, {"dm_method": 2}, ("demosaic", "llap")),
+    # crop after demosaic ("crop": [perspect, window, rotate, exif orientation]): a whole texel
+    # shift (nearest texel), a perspective quad with a rotation and a quarter turn (Catmull-Rom)
+    "bayer_96x64_crop_shift": (96, 64, BAYER, 16, 16383.0, {"crop": [list(QUAD), [0.03125, 0.96875, 0.0625, 0.9375], 0.0, 0]},
+                               ("crop", "llap")),
+    "bayer_112x80_crop_persp": (112, 80, BAYER, 17, 16383.0,
+                                {"crop": [[0.2, 0.22, 0.8, 0.25, 0.77, 0.8, 0.21, 0.75], [0.1, 0.9, 0.05, 0.95], 3.5, 0]},
+                                ("crop", "llap")),
+    "xtrans_132x96_crop_turn": (132, 96, XTRANS, 18, 16383.0, {"crop": [list(QUAD), [1.0, 3.0, 3.0, 7.0], 1337.0, 6]},
+                                ("crop", "llap")),
 }
 
 # i-mcraw decode cases: (rwd, ht, ox, oy, seed) of a random frame stream (every bit count)
@@ -143,11 +153,27 @@ def img_param(v, wd, ht, filters, white):
                                noise_a=NOISE_A / (16383.0 - 512.0) ** 2, noise_b=NOISE_B / (16383.0 - 512.0))
 
 
-def oracle_params(oracle, overrides):
+def oracle_params(oracle, overrides, wd=0, ht=0):
+    """oracle parameters of a case; a "crop" override commits crop for the demosaic output of
+    a full size wd x ht case (oracle.crop_commit)"""
     p = oracle.default_params()
     for k, val in overrides.items():
-        setattr(p, k, val)
+        if k == "crop":
+            persp, win, rot, orient = val
+            blk, cw, ch = oracle.crop_commit(wd, ht, perspect=persp, crop=win, rotate=rot, orientation=orient)
+            oracle.set_crop(p, blk, cw, ch)
+        else:
+            setattr(p, k, val)
     return p
+
+
+def graph_crop(v, g, ip, overrides):
+    """the crop override of a case on a graph made from v.DARKROOM_CROP_CFG"""
+    persp, win, rot, orient = overrides["crop"]
+    ip.orientation = orient
+    g.set_param("crop", "perspect", np.array(persp, np.float32))
+    g.set_param("crop", "crop", np.array(win, np.float32))
+    g.set_param("crop", "rotate", np.float32(rot))
 
 
 def path(name):

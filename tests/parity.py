@@ -74,9 +74,9 @@ def log(name, rec):
             f.write(json.dumps(rec, sort_keys=True) + "\n")
 
 
-def develop_gpu(v, m, ip, setup=None, hist=False):
+def develop_gpu(v, m, ip, setup=None, hist=False, cfg=None):
     """Develop through the C-ABI with the debug stages: every stage image and the decisions."""
-    g = v.Graph()
+    g = v.Graph(cfg) if cfg else v.Graph()
     try:
         g.set_input(m.shape[1], m.shape[0], ip)
         if setup:
@@ -89,6 +89,10 @@ def develop_gpu(v, m, ip, setup=None, hist=False):
               "demosaic": g.debug_stage(3), "colour": g.debug_stage(4)}
         if hist:
             st["hist"] = g.hist()
+        try:
+            st["crop"] = g.debug_stage(11)
+        except v._lib.VkdtError:
+            pass
         try:
             st["dn_nodes"] = {n: g.debug_stage(5 + i) for i, n in enumerate(oracle.DENOISE_NODES)}
         except v._lib.VkdtError:
@@ -118,7 +122,35 @@ def colour_gain(m, ip, op, shape):
     return float(np.abs(np.stack(cols, 1)).sum(1).max()) * 1.01
 
 
-def check(name, v, m, ip, op, gpu, stages=("denoise", "hilite", "demosaic", "colour", "filmcurv", "llap"),
+def crop_reach(op, dm_shape, out_shape, radius=2):
+    """per output pixel of the crop stage, the largest |difference| of the demosaic
+    output `d` (a 2-d map at the demosaic's size) within `radius` texels of the
+    position the pixel samples (crop/main.comp, in double precision): the
+    demosaic texels its filter can reach. Returns a function of d."""
+    b = np.array([op.cr_block[k] for k in range(20)], np.float64)
+    dh, dw = dm_shape[:2]
+    ch, cw = out_shape[:2]
+    y, x = np.mgrid[0:ch, 0:cw].astype(np.float64)
+    px, py = x + 0.5 + b[16] * dw, y + 0.5 + b[18] * dh
+    vx, vy = px - dw * 0.5, py - dh * 0.5
+    qx, qy = b[12] * vx + b[14] * vy + dw * 0.5, b[13] * vx + b[15] * vy + dh * 0.5
+    hz = b[2] * qx + b[6] * qy + b[10]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        sx = (b[0] * qx + b[4] * qy + b[8]) / hz
+        sy = (b[1] * qx + b[5] * qy + b[9]) / hz
+    inside = (sx >= 0) & (sy >= 0) & (sx < dw) & (sy < dh)
+    ix = np.clip(np.nan_to_num(sx), 0, dw - 1).astype(np.int64)
+    iy = np.clip(np.nan_to_num(sy), 0, dh - 1).astype(np.int64)
+
+    def reach(d):
+        from numpy.lib.stride_tricks import sliding_window_view
+        pad = np.pad(d, radius, mode="edge")
+        mx = sliding_window_view(pad, (2 * radius + 1, 2 * radius + 1)).max(axis=(-1, -2))
+        return np.where(inside, mx[iy, ix], 0.0)
+    return reach
+
+
+def check(name, v, m, ip, op, gpu, stages=("denoise", "hilite", "demosaic", "crop", "colour", "filmcurv", "llap"),
           tol=TOL, mean=MEAN, de=DE, double=False):
     """The CUDA path's stage images `gpu` (develop_gpu) against the oracle on the same
     mosaic and parameters; asserts the rules above and returns the record."""
@@ -160,11 +192,14 @@ def check(name, v, m, ip, op, gpu, stages=("denoise", "hilite", "demosaic", "col
                                 force={k: dec[k] for k in differ})
     # ---- 2. node-wise (FP32, the CUDA path's own inputs, its decisions)
     node = {}
-    order = ("denoise", "hilite", "demosaic", "colour", "filmcurv", "llap")
-    for prev, s in zip(order[:-1], order[1:]):
-        if s in stages and prev in gpu:
+    order = ("denoise", "hilite", "demosaic", "crop", "colour", "filmcurv", "llap")
+    prev = None
+    for s in order:
+        if s in stages and prev is not None:
             node[s] = oracle.develop(m, oracle.img_param(ip), params=op, stages=(s,), start=s, input=gpu[prev],
                                      force=dec)[s]
+        if s in gpu:
+            prev = s
     if "dn_nodes" in gpu:
         q = oracle.denoise_nodes(m, oracle.img_param(ip), op, gpu["dn_nodes"], force=dec)
         for n in oracle.DENOISE_NODES:
@@ -224,13 +259,26 @@ def check(name, v, m, ip, op, gpu, stages=("denoise", "hilite", "demosaic", "col
             if ill and f64 is not None:
                 if not (r["over"] <= r["fp64_over"] and r.get("de_over", 0) <= r.get("fp64_de_over", 0)):
                     problems.append(("e2e over the tolerance beyond the FP64 build's", s, r))
+            elif s == "crop" and "demosaic" in gpu:
+                # a resampler with weights of absolute sum below 1.3 (Catmull-Rom, or one texel):
+                # |dcrop| <= node error + 1.3 max |ddemosaic| over the texels it reaches + one f16 step
+                dcr = np.abs(a[..., :3].astype(np.float64) - b[..., :3]).max(-1)
+                ddm = np.abs(gpu["demosaic"][..., :3].astype(np.float64) - forced["demosaic"][..., :3]).max(-1)
+                dnode = np.abs(a[..., :3].astype(np.float64) - node["crop"][..., :3]).max(-1)
+                step = np.abs(np.spacing(np.abs(b[..., :3]).astype(np.float16)).astype(np.float64)).max(-1)
+                bound = dnode + 1.3 * crop_reach(op, ddm.shape, b.shape)(ddm) + step
+                bad = over & (dcr > bound * 1.0001)
+                r["over_beyond_reach_bound"] = int(bad.sum())
+                if bad.any():
+                    problems.append(("crop over the tolerance beyond the propagated bound", r))
             elif s == "colour" and "demosaic" in gpu:
-                # linear colour transform: |dcol| <= node error + gain |ddemosaic| + one f16 step
+                # linear colour transform: |dcol| <= node error + gain |dinput| + one f16 step
                 if gain is None:
                     gain = colour_gain(m, ip, op, b.shape)
                     rec["colour_gain"] = gain
                 dcol = np.abs(a[..., :3].astype(np.float64) - b[..., :3]).max(-1)
-                ddm = np.abs(gpu["demosaic"][..., :3].astype(np.float64) - forced["demosaic"][..., :3]).max(-1)
+                src = "crop" if "crop" in gpu else "demosaic"
+                ddm = np.abs(gpu[src][..., :3].astype(np.float64) - forced[src][..., :3]).max(-1)
                 dnode = np.abs(a[..., :3].astype(np.float64) - node["colour"][..., :3]).max(-1)
                 step = np.abs(np.spacing(np.abs(b[..., :3]).astype(np.float16)).astype(np.float64)).max(-1)
                 bound = dnode + gain * ddm + step

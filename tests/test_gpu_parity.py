@@ -274,19 +274,105 @@ def test_cuda_matches_reference_golden(gpu, name):
     m, case, want = gc.load(name)
     wd, ht, filters, seed, white, overrides, stages = case
     ip = gc.img_param(v, wd, ht, filters, white)
-    op = oracle.default_params()
-    for k, val in overrides.items():
-        setattr(op, k, val)
+    op = gc.oracle_params(oracle, overrides, wd, ht)
     # the oracle's own result is the fixture's
     own = oracle.develop(m, oracle.img_param(ip), params=op, stages=tuple(s for s in want if s != "hist"))
     for s in want:
         if s in own:
             a = own[s] if own[s].ndim == 2 else own[s][..., :want[s].shape[-1]]
             assert np.array_equal(a, want[s]), (name, s)
+    base = graph_setup(op)
+
+    def setup(g):
+        base(g)
+        if "crop" in overrides:
+            gc.graph_crop(v, g, ip, overrides)
+            g.set_input(wd, ht, ip)   # with its exif orientation
     try:
-        g = P.develop_gpu(v, m, ip, setup=graph_setup(op))
+        g = P.develop_gpu(v, m, ip, setup=setup, cfg=v.DARKROOM_CROP_CFG if "crop" in overrides else None)
     except v._lib.VkdtError as e:
         if e.code in (v._lib.ERROR_FORMAT_NOT_SUPPORTED, v._lib.INCOMPLETE):
             pytest.skip("not on the CUDA path: %s" % e)
         raise
     P.check("golden_" + name, v, m, ip, op, g)
+
+
+# ---------------------------------------------------------------- crop between demosaic and colour
+# bin/default-darkroom.i-raw connects crop (crop/main.c, main.comp) after demosaic: at its
+# defaults a 3 px margin (nearest texel), or with the exif orientation a half or quarter turn,
+# or a perspective quad and a rotation (Catmull-Rom); the stages after it run at its size.
+
+QUAD = (0.25, 0.25, 0.75, 0.25, 0.75, 0.75, 0.25, 0.75)
+CROP_CASES = {
+    # name: (wd, ht, filters, orientation, perspect, crop window, rotate, oracle overrides)
+    "darkroom_2048x1536": (2048, 1536, BAYER, 0, QUAD, (1, 3, 3, 7), 1337, {}),
+    "darkroom_6000x4000": (6000, 4000, BAYER, 0, QUAD, (1, 3, 3, 7), 1337, {}),
+    "orient6_1000x742": (1000, 742, BAYER, 6, QUAD, (1, 3, 3, 7), 1337, {}),
+    "orient3_1000x742": (1000, 742, BAYER, 3, QUAD, (1, 3, 3, 7), 1337, {}),
+    "perspective_1024x768": (1024, 768, BAYER, 0, (0.2, 0.22, 0.8, 0.25, 0.77, 0.8, 0.21, 0.75),
+                             (0.1, 0.9, 0.05, 0.95), 3.5, {}),
+    "window_1000x742": (1000, 742, BAYER, 0, QUAD, (0.13, 0.71, 0.2, 0.9), 0, {}),
+    "xtrans_606x402": (606, 402, 9, 0, QUAD, (1, 3, 3, 7), -7.25, {}),
+    "rcd_1000x742": (1000, 742, BAYER, 0, QUAD, (1, 3, 3, 7), 1337, {"dm_method": 1}),
+    "wavelet_1000x742": (1000, 742, BAYER, 0, QUAD, (0.05, 0.95, 0.0, 1.0), 2.0, {"dn_strength": 1.0}),
+}
+
+
+def crop_case(name):
+    wd, ht, filters, orient, persp, win, rot, kw = CROP_CASES[name]
+    m, ip = scene(wd, ht, seed=wd + orient + 77, filters=filters)
+    ip.orientation = orient
+    op = params(**kw)
+    blk, cw, ch = oracle.crop_commit(wd, ht, perspect=persp, crop=win, rotate=rot, orientation=orient)
+    oracle.set_crop(op, blk, cw, ch)
+    base = graph_setup(op)
+
+    def setup(g):
+        base(g)
+        g.set_param("crop", "perspect", np.array(persp, np.float32))
+        g.set_param("crop", "crop", np.array(win, np.float32))
+        g.set_param("crop", "rotate", np.float32(rot))
+    return m, ip, op, setup, (cw, ch), (win, rot)
+
+
+@pytest.mark.parametrize("name", sorted(CROP_CASES))
+def test_crop(gpu, name):
+    m, ip, op, setup, (cw, ch), _ = crop_case(name)
+    g = P.develop_gpu(v, m, ip, setup=setup, cfg=v.DARKROOM_CROP_CFG)
+    assert g["llap"].shape == (ch, cw, 4)
+    assert "crop" in g   # none of the cases is the identity: the crop stage ran
+    P.check("crop_" + name, v, m, ip, op, g)
+
+
+def test_crop_nearest_texel_is_a_copy(gpu):
+    # without rotation and with the default quad the crop fetches texels: its output is the
+    # demosaic output shifted by the window's corner, bit for bit
+    m, ip, op, setup, (cw, ch), _ = crop_case("darkroom_2048x1536")
+    g = P.develop_gpu(v, m, ip, setup=setup, cfg=v.DARKROOM_CROP_CFG)
+    ox, oy = int(op.cr_block[16] * 2048), int(op.cr_block[18] * 1536)
+    assert (ox, oy) == (3, 3)
+    want = g["demosaic"][oy:oy + ch, ox:ox + cw].copy()
+    want[..., 3] = 1.0
+    assert np.array_equal(g["crop"], want)
+
+
+def test_crop_identity_has_no_launch(gpu):
+    # crop at the identity (no rotation, the whole frame, the default quad) copies its input:
+    # the fused path runs, and the result equals the graph without crop
+    m, ip = scene(1000, 742, seed=3)
+
+    def setup(g):
+        g.set_param("crop", "crop", np.array((0, 1, 0, 1), np.float32))
+        g.set_param("crop", "rotate", np.float32(0))
+    with v.Graph(v.DARKROOM_CROP_CFG) as g:
+        g.set_input(1000, 742, ip)
+        setup(g)
+        g.alloc()
+        a = g.run(m)
+        fused = {(n[0], n[1]): n[5] for n in g.nodes()}
+        assert fused[("crop", "main")] == fused[("colour", "main")]   # computed by the fused launch
+    with v.Graph() as g:
+        g.set_input(1000, 742, ip)
+        g.alloc()
+        b = g.run(m)
+    assert np.array_equal(a, b)

@@ -69,22 +69,21 @@ def test_grade_oracle_matches_reference_shader(seed):
     assert np.array_equal(got.view(np.uint16), dst.a.astype(np.float16).view(np.uint16))
 
 
-def test_crop_in_the_chain_only_as_identity():
+def test_crop_and_grade_in_the_chain():
     ip = v.default_img_param(wd=420, ht=300)
     with v.Graph(cfg=_cfg()) as g:
         assert "crop" not in g.unsupported() and "grade" not in g.unsupported()
         g.set_input(420, 300, ip)
-        # crop/params defaults: rotation from the exif orientation and a 3 px margin (resampled)
+        # crop/params defaults: rotation from the exif orientation (none here) and a 3 px margin
+        # on the sides longer than 400 px
+        g.create_nodes()
+        nodes = {(n[0], n[1]): (n[2], n[3]) for n in g.nodes()}
+        assert nodes[("crop", "main")] == (414, 300) == nodes[("grade", "main")]
+        # a crop with a scaled output is not built
+        g.set_output_size(210, 150)
         with pytest.raises(VkdtError) as e:
             g.create_nodes()
         assert e.value.code == 5
-        g.set_param("crop", "rotate", 0.0)
-        g.set_param("crop", "crop", [0.0, 1.0, 0.0, 1.0])
-        g.create_nodes()
-        assert ("grade", "main") in [(n[0], n[1]) for n in g.nodes()]
-        g.set_param("crop", "rotate", 2.5)
-        with pytest.raises(VkdtError):
-            g.create_nodes()
 
 
 def _develop(cfg, wd, ht, m, params=()):

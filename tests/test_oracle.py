@@ -133,7 +133,7 @@ def test_oracle_matches_reference_golden(name):
     m, case, want = gc.load(name)
     wd, ht, filters, seed, white, overrides, stages = case
     ip = oracle.img_param(gc.img_param(v, wd, ht, filters, white))
-    got = oracle.develop(m, ip, params=gc.oracle_params(oracle, overrides), stages=stages)
+    got = oracle.develop(m, ip, params=gc.oracle_params(oracle, overrides, wd, ht), stages=stages)
     for s in stages:
         g = got[s] if got[s].ndim == 2 else got[s][..., :3]
         assert g.shape == want[s].shape, (s, g.shape, want[s].shape)
@@ -175,6 +175,32 @@ def test_oracle_matches_reference_shaders_random(seed):
     for s in st:
         x, y = (a[s], b[s]) if a[s].ndim == 2 else (a[s][..., :3], b[s][..., :3])
         assert np.array_equal(x, y), (seed, wd, ht, s)
+
+
+@pytest.mark.skipif(not _ref_available(), reason="reference shaders not compiled here (oracle/_ref)")
+@pytest.mark.parametrize("seed", [201, 202, 203, 204])
+def test_oracle_crop_matches_reference_shader_random(seed):
+    # crop/main.comp on random quads, windows and rotations (with the exif quarter and half
+    # turns): the oracle's crop stage and what follows it equal the reference's shaders
+    from oracle import glsl_ref
+    rng = np.random.default_rng(seed)
+    filters = gc.XTRANS if seed == 204 else gc.BAYER
+    blk = 2 if filters == gc.BAYER else 6
+    wd, ht = int(rng.integers(10, 40)) * blk, int(rng.integers(8, 30)) * blk
+    m = v.scene_host(v.make_scene(wd, ht, seed=seed, a=gc.NOISE_A, b=gc.NOISE_B, filters=filters))
+    ip = oracle.img_param(gc.img_param(v, wd, ht, filters, 16383.0))
+    quad = np.array(gc.QUAD) + rng.uniform(-0.06, 0.06, 8)
+    win = (1, 3, 3, 7) if seed == 203 else tuple(np.sort(rng.uniform(0, 1, 2)).tolist() + np.sort(rng.uniform(0, 1, 2)).tolist())
+    rot = 1337.0 if seed == 203 else float(rng.uniform(-20, 20))
+    b, cw, ch = oracle.crop_commit(wd, ht, perspect=quad, crop=win, rotate=rot, orientation=6 if seed == 203 else 0)
+    if cw < 4 or ch < 4:
+        pytest.skip("window too small")
+    p = oracle.set_crop(oracle.default_params(), b, cw, ch)
+    st = ("crop", "colour", "llap")
+    a = glsl_ref.develop(m, ip, p, stages=st)
+    o = oracle.develop(m, ip, params=p, stages=st)
+    for s in st:
+        assert np.array_equal(a[s][..., :3], o[s][..., :3]), (seed, s)
 
 
 def test_denoise_nodes_chain_equals_develop():

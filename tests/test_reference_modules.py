@@ -38,7 +38,7 @@ def ref_multiset(case, W, H):
 def cfg_graph(case):
     wd, ht = case["in"]
     g = v.Graph(case["cfg"])
-    g.set_input(wd, ht, MN.case_ip(wd, ht, case["filters"]))
+    g.set_input(wd, ht, MN.case_ip(wd, ht, case["filters"], case.get("orientation", 0)))
     if case["out"][0]:
         g.set_output_size(*case["out"])
     return g
@@ -82,6 +82,45 @@ def test_colour_white_written_back_as_the_reference():
     assert np.array_equal(ours, ref[8:11])
 
 
+CROP = sorted(n for n in CASES if n.startswith("crop_"))
+
+
+@pytest.mark.parametrize("name", CROP)
+def test_crop_written_back_as_the_reference(name):
+    # crop/main.c:334-342: with automatic rotation the resolved window and rotation are
+    # written back into the params; the output size is its modify_roi_out's
+    case = CASES[name]
+    with cfg_graph(case) as g:
+        g.create_nodes()
+        ours = np.concatenate([g.get_param("crop", "crop", count=4), g.get_param("crop", "rotate")])
+        size = {(n[0], n[1]): (n[2], n[3]) for n in g.nodes()}
+    ref = np.frombuffer(case["modules"]["crop"], np.float32)   # perspect[8] crop[4] rotate
+    assert np.array_equal(ours.view(np.uint32), ref[8:13].view(np.uint32))
+    want = [(n["wd"], n["ht"]) for n in case["nodes"] if n["name"] == "crop"]
+    assert [size[("crop", "main")]] == want and size[("llap", "colour")] == want[0]
+
+
+def crop_block(nodes):
+    return np.frombuffer([n for n in nodes if n["name"] == "crop"][0]["uniform"], np.float32)[:20]
+
+
+@pytest.mark.parametrize("name", CROP)
+def test_crop_block_as_the_reference_commits(name):
+    # the oracle's restatement of crop's commit_params gives the reference's block bit for bit
+    import oracle
+    case = CASES[name]
+    wd, ht = case["in"]
+    extra = {}
+    for line in case["cfg"].split("\n"):
+        f = line.split(":")
+        if f[0] == "param" and f[1] == "crop":
+            extra[f[3]] = [float(x) for x in f[4:]]
+    blk, cw, ch = oracle.crop_commit(wd, ht, perspect=extra.get("perspect", MN.QUAD), crop=extra.get("crop", (1, 3, 3, 7)),
+                                     rotate=extra.get("rotate", [1337.0])[0], orientation=case["orientation"])
+    assert np.array_equal(blk.view(np.uint32), crop_block(case["nodes"]).view(np.uint32)), name
+    assert [(cw, ch)] == [(n["wd"], n["ht"]) for n in case["nodes"] if n["name"] == "crop"]
+
+
 def test_unsupported_chains_return_incomplete():
     case = CASES["darkroom_2048x1536"]
     wd, ht = case["in"]
@@ -112,14 +151,17 @@ def test_fixture_is_what_the_reference_modules_emit_now():
         pytest.skip("no vkdt tree here")
     for name, case in CASES.items():
         wd, ht = case["in"]
-        nodes, mods = M.run(case["cfg"], wd, ht, MN.case_ip(wd, ht, case["filters"]), *case["out"])
+        nodes, mods = M.run(case["cfg"], wd, ht, MN.case_ip(wd, ht, case["filters"], case.get("orientation", 0)),
+                            *case["out"])
         assert [(n["name"], n["kernel"], n["wd"], n["ht"], n["dp"], n["push"]) for n in nodes] == \
                [(n["name"], n["kernel"], n["wd"], n["ht"], n["dp"], n["push"]) for n in case["nodes"]], name
+        assert {m["name"]: m["param"] for m in mods} == case["modules"], name
 
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["darkroom_2048x1536", "wavelet_1000x742", "rcd_1000x742", "thumb_2048x1536",
-                                  "xtrans_606x402", "params_384x256", "fixup_1000x742"])
+                                  "xtrans_606x402", "params_384x256", "fixup_1000x742", "crop_2048x1536",
+                                  "crop_orient6_1000x742", "crop_persp_1024x768", "crop_orient8_606x402"])
 def test_develop_through_set_nodes_equals_cfg(gpu, name):
     case = CASES[name]
     wd, ht = case["in"]

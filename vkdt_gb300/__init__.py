@@ -13,15 +13,16 @@ from . import _lib
 from ._lib import ImgParam, Scene, check, token, token_str, RUN_ALL, RUN_UPLOAD_SOURCE, RUN_DOWNLOAD_SINK, RUN_WAIT_DONE
 
 __all__ = ["Graph", "Server", "ImgParam", "Scene", "init", "default_img_param", "scene_host", "scene_device",
-           "DARKROOM_CFG", "CAM_TO_REC2020", "supports"]
+           "DARKROOM_CFG", "DARKROOM_CROP_CFG", "CAM_TO_REC2020", "supports"]
 
 # the synthetic camera: camera rgb -> rec2020, rows sum to one
 CAM_TO_REC2020 = (1.20, -0.15, -0.05,
                   -0.10, 1.25, -0.15,
                   0.02, -0.22, 1.20)
 
-# bin/default-darkroom.i-raw restricted to the modules of the path plus
-# the crop between demosaic and colour, with the cfg's parameter lines
+# bin/default-darkroom.i-raw restricted to the modules of the path, with the
+# cfg's parameter lines (DARKROOM_CROP_CFG: with its crop between demosaic and
+# colour, at crop's defaults: exif rotation and a 3 px margin)
 DARKROOM_CFG = """module:i-raw:main:43:400
 module:denoise:01:218:400
 module:hilite:01:393:400
@@ -41,6 +42,9 @@ param:llap:01:shadows:1
 param:llap:01:hilights:1
 param:llap:01:clarity:0.2
 """
+DARKROOM_CROP_CFG = (DARKROOM_CFG.replace("module:demosaic:01:568:400\n", "module:demosaic:01:568:400\nmodule:crop:01:743:400\n")
+                     .replace("connect:demosaic:01:output:colour:01:input\n",
+                              "connect:demosaic:01:output:crop:01:input\nconnect:crop:01:output:colour:01:input\n"))
 
 _inited = None
 
@@ -334,19 +338,17 @@ class Graph:
         return np.array(h[:], dtype=np.uint32)
 
     def debug_stage(self, stage):
-        """0 denoise, 1 hilite (crop size, one channel); 2 filmcurv, 3 demosaic,
-        4 colour (output size, rgba); wavelet denoise nodes (half size, rgba):
-        5 half, 6 downcov, 7..9 down levels 1..3, 10 assemble."""
-        if stage in (2, 3, 4):
-            out = np.empty((self.out_ht, self.out_wd, 4), np.float32)
-        elif stage >= 5:
-            block = 3 if self._filters == 9 else 2
-            out = np.empty((self.crop_ht // block, self.crop_wd // block, 4), np.float32)
-        else:
-            out = np.empty((self.crop_ht, self.crop_wd, 1), np.float32)
+        """0 denoise, 1 hilite (crop size, one channel); 2 filmcurv, 4 colour
+        (output size, rgba); 3 demosaic (its own size, rgba); 11 crop (output
+        size, rgba); wavelet denoise nodes (half size, rgba): 5 half, 6 downcov,
+        7..9 down levels 1..3, 10 assemble."""
+        w, h, c = C.c_int(), C.c_int(), C.c_int()
+        check(self._l.vkdt_cuda_graph_debug_stage_size(self._g, stage, C.byref(w), C.byref(h), C.byref(c)),
+              "debug_stage_size")
+        out = np.empty((h.value, w.value, c.value), np.float32)
         check(self._l.vkdt_cuda_graph_debug_stage(self._g, stage, out.ctypes.data_as(C.POINTER(C.c_float)), out.size),
               "debug_stage")
-        return out if stage >= 2 else out[..., 0]
+        return out if c.value == 4 else out[..., 0]
 
     DECISIONS = {"gauss": (0, np.uint8), "dn_cov": (1, np.uint32), "dn_thr": (2, np.uint8)}
 

@@ -40,6 +40,7 @@ class ImgParam(C.Structure):
         ("cam_to_rec2020", C.c_float * 9),
         ("noise_a", C.c_float),
         ("noise_b", C.c_float),
+        ("orientation", C.c_uint32),
     ]
 
 
@@ -148,6 +149,7 @@ _SIGS = {
     "vkdt_cuda_waveform_rgba_f16": (C.c_int, [_P, C.c_int, C.c_int, _P, C.c_int, C.c_int, _P]),
     "vkdt_cuda_graph_set_debug": (C.c_int, [_P, C.c_int]),
     "vkdt_cuda_graph_debug_stage": (C.c_int, [_P, C.c_int, C.POINTER(C.c_float), C.c_size_t]),
+    "vkdt_cuda_graph_debug_stage_size": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "vkdt_cuda_graph_set_nodes": (C.c_int, [_P, C.c_int, C.c_int, _P, C.c_int]),
     "vkdt_cuda_graph_debug_decisions": (C.c_int, [_P, C.c_int, _P, C.c_size_t, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "vkdt_cuda_scene_generate": (C.c_int, [C.POINTER(Scene), _P, _P]),

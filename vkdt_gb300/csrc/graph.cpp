@@ -104,7 +104,7 @@ const std::vector<module_def_t> &module_defs()
       { "lift", 'f', 4, { 0, 0, 0, 0 } }, { "gamma", 'f', 4, { 1, 1, 1, 0 } }, { "gain", 'f', 4, { 1, 1, 1, 0 } },
       { "offset", 'f', 4, { 0, 0, 0, 0 } }, { "mode", 'i', 1, { 0 } }, { "sh_pivot", 'f', 1, { 0.3f } },
       { "hi_pivot", 'f', 1, { 0.4f } } } },
-    { "crop", {                                                   // crop/params:1-3 (checked, not applied)
+    { "crop", {                                                   // crop/params:1-3
       { "perspect", 'f', 8, { 0.25f, 0.25f, 0.75f, 0.25f, 0.75f, 0.75f, 0.25f, 0.75f } },
       { "crop", 'f', 4, { 1, 3, 3, 7 } }, { "rotate", 'f', 1, { 1337 } } } },
   };
@@ -181,7 +181,12 @@ struct vkdt_cuda_graph_t
   bool halfsize = false, resample = false;  // demosaic/halfsize (+ shared/resample) for reduced sizes
   bool rcd = false;              // demosaic method 1 (rcd_conv + rcd_fill) at full size
   bool grade = false;            // llap -> grade connected: grade/main applied to the llap output
-  bool crop = false;             // demosaic -> crop -> colour connected (only as an identity)
+  bool crop = false;             // demosaic -> crop -> colour connected
+  bool crop_stage = false;       // the crop moves or resamples pixels (not the identity): its own launch
+  bool crop_given = false;       // its committed block came with the scheduler's nodes (set_nodes)
+  float crop_blk[20];            // crop's committed uniform block (crop/main.c:276-343)
+  int crop_w = 0, crop_h = 0;    // its output size
+  int dm_w = 0, dm_h = 0;        // the demosaic output size (crop's input; out_w x out_h without crop)
   bool unfused = false;          // x-trans, rcd or reduced size: the per-node chain instead of the fused kernel
   bool k1front = false;          // bayer per-node chain: the fused path's hilite front (k1, pyramid, one kernel to doub)
   std::vector<int64_t> planned_for; // what alloc planned for: a run refuses a graph changed since
@@ -193,7 +198,7 @@ struct vkdt_cuda_graph_t
   // the white balance multipliers, the exposure factor and the camera matrix as committed
   bool colour_given = false;
   float colour_mul[3] = { 1, 1, 1 }, colour_mulw = 1.0f, colour_cam[9] = { 1, 0, 0, 0, 1, 0, 0, 0, 1 };
-  size_t off_h0 = 0, off_b0 = 0, off_hl = 0, off_cov = 0, off_g = 0, off_hs = 0, off_dm = 0;
+  size_t off_h0 = 0, off_b0 = 0, off_hl = 0, off_cov = 0, off_g = 0, off_hs = 0, off_dm = 0, off_cr = 0;
   size_t off_vh = 0, off_pq = 0, off_lpf = 0;
   size_t off_dnh = 0, off_dnl[4] = { 0, 0, 0, 0 }, off_dna = 0, off_dn = 0, off_idlut = 0;
   // debug stages: demosaic (fused path) and colour outputs, the decisions of gauss and the wavelet denoise
@@ -346,6 +351,122 @@ void colour_commit(vkdt_cuda_graph_t *g, dev_image_t &d)
 
 size_t align_up(size_t v) { return (v + 255) & ~(size_t)255; }
 
+// ------------------------------------------------------------------ crop (crop/main.c)
+
+// the linear system of crop's perspective quad (core/gaussian_elimination.h:40-109, after H.
+// Spaeth, "Numerik", 1994): elimination with partial pivoting as LINPACK's dgefa/dgesl order it.
+// The operations follow the reference's order so that the homography it commits comes out to the
+// same bits: the first row of largest magnitude pivots; pivot rows swap right of the pivot column
+// only; the negated multipliers stay where they are formed; the right hand side is permuted as
+// it is reduced.
+bool solve_linpack(double *A, double *b, int n)
+{
+  std::vector<int> piv(n);
+  for(int k = 0; k < n; k++)
+  {
+    double *rk = A + (size_t)k * n;
+    int m = k;
+    for(int r = k + 1; r < n; r++) if(std::fabs(A[(size_t)r * n + k]) > std::fabs(A[(size_t)m * n + k])) m = r;
+    piv[k] = m;
+    double *rm = A + (size_t)m * n;
+    const double pv = rm[k];
+    rm[k] = rk[k];
+    rk[k] = pv;
+    if(pv == 0.0) return false;
+    for(int r = k + 1; r < n; r++) A[(size_t)r * n + k] /= -pv;
+    if(m != k) for(int c = k + 1; c < n; c++) std::swap(rm[c], rk[c]);
+    for(int r = k + 1; r < n; r++)
+    {
+      double *rr = A + (size_t)r * n;
+      for(int c = k + 1; c < n; c++) rr[c] += rr[k] * rk[c];
+    }
+  }
+  for(int k = 0; k < n - 1; k++)
+  {
+    std::swap(b[piv[k]], b[k]);
+    for(int r = k + 1; r < n; r++) b[r] += A[(size_t)r * n + k] * b[k];
+  }
+  for(int k = n - 1; k >= 0; k--)
+  {
+    b[k] /= A[(size_t)k * n + k];
+    for(int r = 0; r < k; r++) b[r] -= A[(size_t)r * n + k] * b[k];
+  }
+  return true;
+}
+
+// crop/main.c:175-226 get_crop_rot: rotation 1337 follows the exif orientation (3: 180, 8: 90,
+// 6: 270 degrees, else none); the window 1,3,3,7 is a 3 px safety margin for resampling (none at
+// 400 px or less), its axes exchanged for the quarter turns
+void crop_window(uint32_t orient, double wd, double ht, const module_t *m, float win[4], float *rot)
+{
+  const float prot = m->f("rotate");
+  *rot = prot;
+  for(int k = 0; k < 4; k++) win[k] = m->f("crop", k);
+  if(prot == 1337.0f) *rot = orient == 3 ? 180.0f : orient == 8 ? 90.0f : orient == 6 ? 270.0f : 0.0f;
+  if(!(win[0] == 1.0f && win[1] == 3.0f && win[2] == 3.0f && win[3] == 7.0f)) return;
+  const double mw = wd > 400 ? 3.0 / wd : 0.0, mh = ht > 400 ? 3.0 / ht : 0.0;
+  const float r = *rot;
+  if((r >= 45 && r < 135) || (r >= 225 && r < 315))
+  {
+    win[0] = 0.5 - (.5 - mh) * ht / wd; win[1] = 0.5 + (.5 - mh) * ht / wd;
+    win[2] = 0.5 - (.5 - mw) * wd / ht; win[3] = 0.5 + (.5 - mw) * wd / ht;
+  }
+  else { win[0] = mw; win[1] = 1.0 - mw; win[2] = mh; win[3] = 1.0 - mh; }
+}
+
+// crop's output size (crop/main.c:252-275 modify_roi_out: the window's share of the input, at
+// most 32768) and its committed block (:276-343 commit_params: the homography of the perspective
+// quad as three padded columns, the rotation matrix, the window), for a wd x ht input. With
+// automatic rotation the resolved window and rotation are written back into the params, as the
+// reference does.
+void crop_commit(vkdt_cuda_graph_t *g, int wd, int ht, float blk[20], int *ow, int *oh)
+{
+  module_t *m = g->mod("crop");
+  float win[4], rot;
+  crop_window(g->ip.orientation, (float)wd, (float)ht, m, win, &rot);
+  const float sw = win[1] - win[0], sh = win[3] - win[2];
+  *ow = (int)(uint32_t)std::fmin(32768.0f, (float)(uint32_t)wd * sw);
+  *oh = (int)(uint32_t)std::fmin(32768.0f, (float)(uint32_t)ht * sh);
+  // the homography taking the axis aligned quad (a,b) (A,b) (A,B) (a,B) to the given corners
+  // (P. Heckbert, "Fundamentals of Texture Mapping and Image Warping", 1989, pp. 17-21)
+  float c[8];
+  for(int k = 0; k < 4; k++) { c[2 * k] = (float)(uint32_t)wd * m->f("perspect", 2 * k); c[2 * k + 1] = (float)(uint32_t)ht * m->f("perspect", 2 * k + 1); }
+  const float ax = c[0], bx = c[2], ay = c[1], by = c[7];
+  const float q[8] = { ax, ay, bx, ay, bx, by, ax, by };
+  double A[64] = { 0 }, x[9];
+  for(int k = 0; k < 4; k++)
+  {
+    const float qx = q[2 * k], qy = q[2 * k + 1];
+    double *ex = A + 8 * k, *ey = A + 8 * (4 + k);
+    ex[0] = qx; ex[1] = qy; ex[2] = 1; ex[6] = -c[2 * k] * qx; ex[7] = -c[2 * k] * qy;   // float products
+    ey[3] = qx; ey[4] = qy; ey[5] = 1; ey[6] = -c[2 * k + 1] * qx; ey[7] = -c[2 * k + 1] * qy;
+    x[k] = c[2 * k]; x[4 + k] = c[2 * k + 1];
+  }
+  x[8] = 1.0;
+  solve_linpack(A, x, 8);
+  for(int col = 0; col < 3; col++)
+  {
+    for(int row = 0; row < 3; row++) blk[4 * col + row] = (float)x[3 * row + col];
+    blk[4 * col + 3] = 0.0f;
+  }
+  const float rad = rot * 3.1415629 / 180.0f;
+  blk[12] = cosf(rad); blk[13] = sinf(rad); blk[14] = -sinf(rad); blk[15] = cosf(rad);
+  for(int k = 0; k < 4; k++) blk[16 + k] = win[k];
+  if(m->f("rotate") == 1337.0f)
+  {
+    for(int k = 0; k < 4; k++) m->setf("crop", k, win[k]);
+    m->setf("rotate", 0, rot);
+  }
+}
+
+// a block that copies its input unchanged: the identity homography and rotation, the whole frame
+bool crop_identity(const float b[20], int wd, int ht, int ow, int oh)
+{
+  static const float id[20] = { 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 1, 0, 0, 1, 0, 1, 0, 1 };
+  for(int k = 0; k < 20; k++) if(b[k] != id[k]) return false;   // -0 == 0
+  return ow == wd && oh == ht;
+}
+
 // everything the node plan and the arena depend on
 std::vector<int64_t> plan_key(vkdt_cuda_graph_t *g)
 {
@@ -353,23 +474,21 @@ std::vector<int64_t> plan_key(vkdt_cuda_graph_t *g)
   const int wavelet = dn && dn->f("strength") > 0.0f;
   const int fixup = g->mod("demosaic") ? g->mod("demosaic")->n("colour") : 0;
   const int method = g->mod("demosaic") ? g->mod("demosaic")->n("method") : 0;
-  return { g->in_wd, g->in_ht, g->ip.crop_aabb[0], g->ip.crop_aabb[1], g->ip.crop_aabb[2], g->ip.crop_aabb[3],
-           g->ip.filters, g->req_wd, g->req_ht, g->llap_levels_req, wavelet, g->want_hist, g->debug, fixup, method };
+  std::vector<int64_t> k = { g->in_wd, g->in_ht, g->ip.crop_aabb[0], g->ip.crop_aabb[1], g->ip.crop_aabb[2],
+      g->ip.crop_aabb[3], g->ip.filters, g->req_wd, g->req_ht, g->llap_levels_req, wavelet, g->want_hist, g->debug,
+      fixup, method, g->crop, g->ip.orientation, g->crop_given };
+  if(const module_t *c = g->crop ? g->mod("crop") : nullptr) for(uint32_t v : c->param) k.push_back(v);
+  if(g->crop_given) for(float v : g->crop_blk) { uint32_t u; memcpy(&u, &v, 4); k.push_back(u); }
+  return k;
 }
 
 int check_supported_params(vkdt_cuda_graph_t *g)
 {
   if(g->crop)
-  { // crop/main.c:174-275: only the identity passes (no rotation, the whole frame, the untouched
-    // perspective quad); the defaults (rotation 1337 from the exif orientation, the crop 1,3,3,7
-    // margin) and every real crop resample the image, which is not built here
-    const module_t *c = g->mod("crop");
-    if(!c) return fail(VKDT_CUDA_INCOMPLETE, "crop connected but not declared");
-    static const float quad[8] = { 0.25f, 0.25f, 0.75f, 0.25f, 0.75f, 0.75f, 0.25f, 0.75f };
-    bool id = c->f("rotate") == 0.0f && c->f("crop", 0) == 0.0f && c->f("crop", 1) == 1.0f
-           && c->f("crop", 2) == 0.0f && c->f("crop", 3) == 1.0f;
-    for(int k = 0; k < 8; k++) id = id && c->f("perspect", k) == quad[k];
-    if(!id) return fail(VKDT_CUDA_INCOMPLETE, "crop other than the identity (rotate 0, crop 0 1 0 1, the default quad) not built");
+  { // crop/main.c:228-251: with a scaled output crop's input size follows its output's
+    // (modify_roi_in); only full resolution is built
+    if(!g->mod("crop")) return fail(VKDT_CUDA_INCOMPLETE, "crop connected but not declared");
+    if(g->req_wd > 0 || g->req_ht > 0) return fail(VKDT_CUDA_INCOMPLETE, "crop with a scaled output size is not built");
   }
   const int method = g->mod("demosaic")->n("method");
   if(method < 0 || method > 2) return fail(VKDT_CUDA_INCOMPLETE, "demosaic method %d not supported", method);
@@ -444,7 +563,7 @@ size_t plan_arena(vkdt_cuda_graph_t *g)
   if(g->debug)
   {
     g->off_dbg0 = take((size_t)g->W * g->H * 2); g->off_dbg1 = take((size_t)g->W * g->H * 2);
-    g->off_dbg_dm = take((size_t)g->out_w * g->out_h * 8); g->off_dbg_col = take((size_t)g->out_w * g->out_h * 8);
+    g->off_dbg_dm = take((size_t)g->dm_w * g->dm_h * 8); g->off_dbg_col = take((size_t)g->out_w * g->out_h * 8);
     g->off_dbg_gauss = take((size_t)g->hw * g->hh);
     if(g->wavelet) { g->off_dbg_cov = take((size_t)g->hw * g->hh * 4); g->off_dbg_thr = take((size_t)g->hw * g->hh); }
   }
@@ -469,7 +588,7 @@ size_t plan_arena(vkdt_cuda_graph_t *g)
     if(g->halfsize)
     {
       g->off_hs = take(hbytes);
-      g->off_dm = g->resample ? take((size_t)g->out_w * g->out_h * 8) : g->off_hs;
+      g->off_dm = g->resample ? take((size_t)g->dm_w * g->dm_h * 8) : g->off_hs;
     }
     else if(g->rcd)
     { // demosaic/main.c:113-125: vh at full size, pq and lp at half width
@@ -484,6 +603,7 @@ size_t plan_arena(vkdt_cuda_graph_t *g)
       g->off_g = take((size_t)g->W * g->H * 2);
       g->off_dm = take((size_t)g->W * g->H * 8);
     }
+    if(g->crop_stage) g->off_cr = take((size_t)g->out_w * g->out_h * 8);
   }
   return off;
 }
@@ -533,7 +653,7 @@ void fill_nodes(vkdt_cuda_graph_t *g, dev_nodes_t &p, const void *d_src)
   p.block = g->block; p.hw = g->hw; p.hh = g->hh;
   p.hl_white = g->mod("hilite")->f("white");
   p.fixup = g->mod("demosaic")->n("colour");
-  p.ow = g->out_w; p.oh = g->out_h;
+  p.ow = g->dm_w; p.oh = g->dm_h;
   p.dn = g->at<__half>(g->off_dn);
   p.h0 = g->at<half4>(g->off_h0);
   p.b0 = g->at<half4>(g->off_b0);
@@ -546,6 +666,12 @@ void fill_nodes(vkdt_cuda_graph_t *g, dev_nodes_t &p, const void *d_src)
   p.coarse = g->at<half4>(c.off); p.ccw = c.w; p.cch = c.h;
   p.hl_soft = g->mod("hilite")->f("soft");
   if(g->debug) p.dbg_gauss = g->at<uint8_t>(g->off_dbg_gauss);
+  if(g->crop_stage)
+  {
+    for(int k = 0; k < 20; k++) p.crop[k] = g->crop_blk[k];
+    p.cw = g->out_w; p.ch = g->out_h;
+    p.cr = g->at<half4>(g->off_cr);
+  }
   // the bayer front writes the noop output only for the debug stage (the wavelet writes its own)
   if(g->k1front && (g->wavelet || !g->debug)) p.dn = nullptr;
 }
@@ -680,8 +806,9 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
       rp.vh = g->at<__half>(g->off_vh); rp.pq = g->at<__half>(g->off_pq); rp.lp = g->at<__half>(g->off_lpf);
       // rcd_fill applies colour, the histogram and filmcurv to its output pixels;
       // the demosaic output itself is kept only for the debug stage
-      rp.out = g->debug ? np.dm : nullptr;
-      rp.post = 1;
+      // (with a crop stage after it, rcd_fill writes the demosaic output and k_post the rest)
+      rp.out = g->debug || g->crop_stage ? np.dm : nullptr;
+      rp.post = !g->crop_stage;
       dev_image_t dp = d;
       dp.W = g->out_w; dp.H = g->out_h;
       for(int stage = 0; stage < 2; stage++)
@@ -701,9 +828,14 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
         if((r = mark())) return r;
       }
     }
+    if(g->crop_stage)
+    { // crop/main on the demosaic output
+      CU(launch_nodes(np, 9, s));
+      if((r = mark())) return r;
+    }
     dev_image_t dp = d;
     dp.W = g->out_w; dp.H = g->out_h;
-    CU(launch_post(dp, g->rcd ? nullptr : np.dm, s));
+    CU(launch_post(dp, g->crop_stage ? np.cr : g->rcd ? nullptr : np.dm, s));
     if((r = mark())) return r;
   }
   else
@@ -972,6 +1104,7 @@ int vkdt_cuda_graph_set_input(vkdt_cuda_graph_t *g, int wd, int ht, const vkdt_c
   g->in_wd = wd; g->in_ht = ht; g->ip = *ip;
   for(int k = 0; k < 4; k++) { g->nblack[k] = ip->black[k] / 65535.0f; g->nwhite[k] = ip->white[k] / 65535.0f; }
   g->colour_given = false;
+  g->crop_given = false;
   // i-raw/main.c:214-218 normalises the white balance to green
   if(g->ip.whitebalance[1] > 0.0f && g->ip.whitebalance[1] != 1.0f)
   {
@@ -1039,6 +1172,18 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
     else if(g->resample) { g->out_w = ow; g->out_h = oh; }
     else { g->out_w = g->hw; g->out_h = g->hh; }
   }
+  // crop between demosaic and colour (crop/main.c:252-343): the stages after it run at its size;
+  // a crop that copies its input (the identity at the input's size) has no launch of its own
+  g->dm_w = g->out_w; g->dm_h = g->out_h;
+  g->crop_stage = false;
+  if(g->crop)
+  {
+    if(!g->crop_given) crop_commit(g, g->dm_w, g->dm_h, g->crop_blk, &g->crop_w, &g->crop_h);
+    if(g->crop_w < 16 || g->crop_h < 16)
+      return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "crop output %dx%d smaller than 16x16", g->crop_w, g->crop_h);
+    g->crop_stage = !crop_identity(g->crop_blk, g->dm_w, g->dm_h, g->crop_w, g->crop_h);
+    g->out_w = g->crop_w; g->out_h = g->crop_h;
+  }
   // demosaic/main.c:113: rcd at full size, whatever the pattern (its tiles need an even width)
   g->rcd = method == 1 && !g->halfsize;
   if(g->rcd && (g->W & 1)) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "rcd needs an even width");
@@ -1046,7 +1191,7 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
   // bayer with the fused path's hilite front
   // a demosaic colour param >= 1 widens the bayer fix radius to 2 (fix.comp:124): node by node
   const bool wide_fix = !xt && g->mod("demosaic")->n("colour") >= 1;
-  g->unfused = xt || g->halfsize || g->rcd || wide_fix;
+  g->unfused = xt || g->halfsize || g->rcd || wide_fix || g->crop_stage;
   g->k1front = g->unfused && !xt;
 
   // node lists as the modules' create_nodes emit them
@@ -1094,7 +1239,7 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
   if(g->halfsize)
   { // demosaic/main.c:92-111
     add_node(g, "demosaic", "halfsize", g->hw, g->hh, 1, -1);
-    if(g->resample) add_node(g, "shared", "resample", OW, OH, 1, -1);
+    if(g->resample) add_node(g, "shared", "resample", g->dm_w, g->dm_h, 1, -1);
   }
   else if(g->rcd)
   { // demosaic/main.c:113-155: one rcd_fill workgroup (8 invocations of the node size) per 58x26 tile
@@ -1108,6 +1253,7 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
     add_node(g, "demosaic", "splat", g->W, g->H, 1, -1);
     add_node(g, "demosaic", "fix", g->W, g->H, 1, -1);
   }
+  if(g->crop) add_node(g, "crop", "main", OW, OH, 1, -1);   // crop/main.c: the default create_nodes
   add_node(g, "colour", "main", OW, OH, 1, -1);
   add_node(g, "OpenDRT", "hist", (OW + 15) / 16 * 8, (OH + 15) / 16 * 8, 1, -1);
   add_node(g, "filmcurv", "main", OW, OH, 1, -1);
@@ -1139,7 +1285,7 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
   }
   std::vector<int> L_hr, L_ha, L_lr, L_la;
   int L_noop = -1, L_half = -1, L_a0 = -1, L_doub = -1, L_gauss = -1, L_splat = -1, L_fix = -1, L_hs = -1, L_rs = -1;
-  int L_rcdc = -1, L_rcdf = -1;
+  int L_rcdc = -1, L_rcdf = -1, L_crop = -1;
   int L_post, L_k1 = -1;
   const bool k1 = !g->unfused || g->k1front;
   int L_tail = -1;   // the one-CTA tail computes hr[hl_tail..] and hb[hl_tail..]
@@ -1183,6 +1329,7 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
       L_splat = launch("demosaic", "splat");
       L_fix = launch("demosaic", "fix");
     }
+    if(g->crop_stage) L_crop = launch("crop", "main");
     L_post = launch("llap", "curve");
   }
   for(size_t l = 1; l < g->lp.size(); l++) L_lr.push_back(launch("llap", "reduce"));
@@ -1199,7 +1346,8 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
     if(!g->unfused)
     {
       if(n.name == tkn("denoise") || n.kernel == tkn("doub") || n.name == tkn("demosaic") || n.name == tkn("colour")
-          || n.name == tkn("OpenDRT") || n.name == tkn("filmcurv") || n.kernel == tkn("curve")) n.fused = L_post;
+          || n.name == tkn("OpenDRT") || n.name == tkn("filmcurv") || n.kernel == tkn("curve") || n.name == tkn("crop"))
+        n.fused = L_post;
       if(n.name == tkn("hilite") && n.kernel == tkn("half")) n.fused = L_k1;
       continue;
     }
@@ -1212,6 +1360,7 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
     else if(n.kernel == tkn("gauss") || n.kernel == tkn("down")) n.fused = L_gauss;
     else if(n.kernel == tkn("splat")) n.fused = L_splat;
     else if(n.kernel == tkn("fix")) n.fused = L_fix;
+    else if(n.name == tkn("crop")) n.fused = g->crop_stage ? L_crop : L_post;
     else n.fused = L_post;   // colour, histogram, filmcurv, llap curve
   }
   // per level nodes (reduce and assemble pairs in create_nodes order)
@@ -1414,8 +1563,23 @@ int vkdt_cuda_graph_set_nodes(vkdt_cuda_graph_t *g, int in_wd, int in_ht, const 
   const int W = (int)(ip.crop_aabb[2] - ip.crop_aabb[0]), H = (int)(ip.crop_aabb[3] - ip.crop_aabb[1]);
   const int method = g->mod("demosaic")->n("method");
   const int fw = method == 2 ? (W + 1) / 2 : W, fh = method == 2 ? (H + 1) / 2 : H;
-  g->req_wd = (fin->wd != fw || fin->ht != fh) ? fin->wd : 0;
-  g->req_ht = (fin->wd != fw || fin->ht != fh) ? fin->ht : 0;
+  const vkdt_cuda_node_desc_t *cr = find("crop", "main");
+  g->crop = cr != nullptr;
+  if(cr)
+  { // crop/main.c:276-343: the committed block {mat3 H (padded columns), r0..r3, x X y Y} and its size
+    if(!cr->uniform || cr->uniform_size < 20 * 4) return fail(VKDT_CUDA_INCOMPLETE, "no crop uniform block");
+    ensure_module(g, "crop");
+    for(int k = 0; k < 20; k++) g->crop_blk[k] = fat(cr->uniform, cr->uniform_size, k);
+    g->crop_w = cr->wd; g->crop_h = cr->ht;
+    g->crop_given = true;
+    if(fin->wd != cr->wd || fin->ht != cr->ht) return fail(VKDT_CUDA_INCOMPLETE, "crop with a scaled output size is not built");
+    g->req_wd = g->req_ht = 0;
+  }
+  else
+  {
+    g->req_wd = (fin->wd != fw || fin->ht != fh) ? fin->wd : 0;
+    g->req_ht = (fin->wd != fw || fin->ht != fh) ? fin->ht : 0;
+  }
   if((r = vkdt_cuda_graph_create_nodes(g))) return r;
   // ---- the plan covers exactly these nodes
   std::vector<std::array<int64_t, 5>> want, have;
@@ -1670,6 +1834,21 @@ int vkdt_cuda_waveform_rgba_f16(const void *d_rgba, int wd, int ht, uint32_t *d_
   return 0;
 }
 
+int vkdt_cuda_graph_debug_stage_size(vkdt_cuda_graph_t *g, int stage, int *wd, int *ht, int *channels)
+{
+  if(!g || !g->allocated) return fail(VKDT_CUDA_INCOMPLETE, "graph not allocated");
+  int w, h, c = 4;
+  if(stage == 0 || stage == 1) { w = g->W; h = g->H; c = 1; }
+  else if(stage == 3) { w = g->dm_w; h = g->dm_h; }
+  else if(stage == 2 || stage == 4 || stage == 11) { w = g->out_w; h = g->out_h; }
+  else if(stage >= 5 && stage <= 10) { w = g->hw; h = g->hh; }
+  else return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "stage %d", stage);
+  if(wd) *wd = w;
+  if(ht) *ht = h;
+  if(channels) *channels = c;
+  return 0;
+}
+
 int vkdt_cuda_graph_debug_stage(vkdt_cuda_graph_t *g, int stage, float *out, size_t count)
 {
   if(!g || !g->allocated) return fail(VKDT_CUDA_INCOMPLETE, "graph not allocated");
@@ -1697,15 +1876,18 @@ int vkdt_cuda_graph_debug_stage(vkdt_cuda_graph_t *g, int stage, float *out, siz
     for(size_t i = 0; i < nh * 4; i++) out[i] = __half2float(h[i]);
     return 0;
   }
-  if(stage == 2 || stage == 3 || stage == 4)
+  if(stage == 2 || stage == 3 || stage == 4 || stage == 11)
   {
     if(stage != 2 && !g->debug) return fail(VKDT_CUDA_INCOMPLETE, "debug stages not enabled");
-    if(count < nout * 4) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "buffer too small");
-    std::vector<__half> h(nout * 4);
-    // the per-node chain keeps the demosaic output; the fused kernel and rcd_fill write debug copies
-    const size_t off = stage == 2 ? g->off_rgbf : stage == 4 ? g->off_dbg_col : (g->unfused ? g->off_dm : g->off_dbg_dm);
-    CU(cudaMemcpy(h.data(), g->arena + off, nout * 8, cudaMemcpyDeviceToHost));
-    for(size_t i = 0; i < nout * 4; i++) out[i] = __half2float(h[i]);
+    if(stage == 11 && !g->crop_stage) return fail(VKDT_CUDA_INCOMPLETE, "no crop stage in this graph");
+    const size_t n = stage == 3 ? (size_t)g->dm_w * g->dm_h : nout;
+    if(count < n * 4) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "buffer too small");
+    std::vector<__half> h(n * 4);
+    // the per-node chain keeps the demosaic and crop outputs; the fused kernel and rcd_fill write debug copies
+    const size_t off = stage == 2 ? g->off_rgbf : stage == 4 ? g->off_dbg_col : stage == 11 ? g->off_cr
+                     : (g->unfused ? g->off_dm : g->off_dbg_dm);
+    CU(cudaMemcpy(h.data(), g->arena + off, n * 8, cudaMemcpyDeviceToHost));
+    for(size_t i = 0; i < n * 4; i++) out[i] = __half2float(h[i]);
     return 0;
   }
   return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "stage %d", stage);

@@ -451,6 +451,43 @@ __global__ void __launch_bounds__(256) k_nd_resample(const dev_nodes_t p)
   p.dm[(size_t)y * p.ow + x] = mk_half4(res[0], res[1], res[2], res[3]);
 }
 
+// crop/main.comp:19-55 on the demosaic output (ow x oh): per output pixel the
+// input position, undoing in reverse order the window's corner, the rotation
+// about the input's centre and the homography with its divide (matrix
+// products summed column by column as GLSL's mat * vec; IEEE operations, as
+// the position decides the texels read); then the nearest texel when there is
+// no rotation (r0 == 1), else the Catmull-Rom filter; 0 outside the input;
+// alpha 1
+__global__ void __launch_bounds__(256) k_nd_crop(const dev_nodes_t p)
+{
+  const int x = blockIdx.x * 16 + threadIdx.x % 16, y = blockIdx.y * 16 + threadIdx.x / 16;
+  if(x >= p.cw || y >= p.ch) return;
+  const float *b = p.crop;
+  const float tsx = (float)p.ow, tsy = (float)p.oh;
+  const float px = __fadd_rn(__fadd_rn((float)x, 0.5f), __fmul_rn(b[16], tsx));
+  const float py = __fadd_rn(__fadd_rn((float)y, 0.5f), __fmul_rn(b[18], tsy));
+  const float vx = __fsub_rn(px, __fmul_rn(tsx, 0.5f)), vy = __fsub_rn(py, __fmul_rn(tsy, 0.5f));
+  const float qx = __fadd_rn(__fadd_rn(__fmul_rn(b[12], vx), __fmul_rn(b[14], vy)), __fmul_rn(tsx, 0.5f));
+  const float qy = __fadd_rn(__fadd_rn(__fmul_rn(b[13], vx), __fmul_rn(b[15], vy)), __fmul_rn(tsy, 0.5f));
+  const float hx = __fadd_rn(__fadd_rn(__fmul_rn(b[0], qx), __fmul_rn(b[4], qy)), b[8]);
+  const float hy = __fadd_rn(__fadd_rn(__fmul_rn(b[1], qx), __fmul_rn(b[5], qy)), b[9]);
+  const float hz = __fadd_rn(__fadd_rn(__fmul_rn(b[2], qx), __fmul_rn(b[6], qy)), b[10]);
+  const float rx = __fdiv_rn(__fdiv_rn(hx, hz), tsx), ry = __fdiv_rn(__fdiv_rn(hy, hz), tsy);
+  float v[4] = { 0.0f, 0.0f, 0.0f, 0.0f };
+  // outside [0,1)^2 the output is 0; so is a position without value (hz = 0), which the
+  // shader leaves undefined
+  if(rx >= 0.0f && ry >= 0.0f && rx < 1.0f && ry < 1.0f)
+  {
+    if(b[12] != 1.0f) catmull_rom_uv(p.dm, p.ow, p.oh, rx, ry, v);
+    else
+    { // texelFetch(ivec2(rd * ts)); rd * ts may round up to ts, a read outside the image: 0
+      const int ix = (int)__fmul_rn(rx, tsx), iy = (int)__fmul_rn(ry, tsy);
+      if(ix < p.ow && iy < p.oh) ld4(p.dm, p.ow, ix, iy, v);
+    }
+  }
+  p.cr[(size_t)y * p.cw + x] = mk_half4(v[0], v[1], v[2], 1.0f);
+}
+
 // ---------------------------------------------------------------- bayer demosaic, node by node
 // (demosaic colour param >= 1: fix.comp:124 widens the fix radius to 2, which
 // the fused develop kernel's tile does not hold; gauss, splat and fix then run
@@ -664,6 +701,7 @@ cudaError_t launch_nodes(const dev_nodes_t &p, int stage, cudaStream_t s)
       }
       break;
     case 6: if(xt) k_nd_halfsize<true><<<gh, 256, 0, s>>>(p); else k_nd_halfsize<false><<<gh, 256, 0, s>>>(p); break;
+    case 9: k_nd_crop<<<dim3((p.cw + 15) / 16, (p.ch + 15) / 16), 256, 0, s>>>(p); break;
     case 7: k_nd_resample<<<dim3((p.ow + 15) / 16, (p.oh + 15) / 16), 256, 0, s>>>(p); break;
     case 8: k_nd_hl_bayer<<<gh, 256, 0, s>>>(p); break;
     default: return cudaErrorInvalidValue;

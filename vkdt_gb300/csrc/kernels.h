@@ -145,9 +145,15 @@ struct dev_nodes_t
   int ccw, cch;          // its size
   float hl_soft;
   uint8_t *dbg_gauss;    // debug: demosaic/gauss decisions per entry (x-trans), or null
+  // crop/main.comp between demosaic and colour: its committed block (homography
+  // as three padded columns, rotation r0..r3, window x X y Y) and output
+  float crop[20];
+  int cw, ch;            // crop output size
+  half4 *cr;             // crop output, cw*ch
 };
 // stage: 0 noop, 1 hilite half, 2 hilite doub, 3 gauss, 4 splat, 5 fix, 6 halfsize, 7 resample,
-// 8 bayer noop + hilite half + level 0 hilite assemble + hilite doub from the mosaic (dn written when set)
+// 8 bayer noop + hilite half + level 0 hilite assemble + hilite doub from the mosaic (dn written when set),
+// 9 crop of the demosaic output (dm, ow x oh) into cr
 cudaError_t launch_nodes(const dev_nodes_t &p, int stage, cudaStream_t s);
 // colour -> histogram -> filmcurv -> llap curve -> llap level 1 reduce on the
 // demosaic output (p.W x p.H = the output size; p.mosaic unused); with dm null,

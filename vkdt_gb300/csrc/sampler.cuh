@@ -35,3 +35,41 @@ DEV void bilinear(const half4 *img, int w, int h, float x, float y, float out[4]
   for(int k = 0; k < 4; k++)
     out[k] = (t00[k] * (1.0f - ax) + t10[k] * ax) * (1.0f - ay) + (t01[k] * (1.0f - ax) + t11[k] * ax) * ay;
 }
+
+// shared.glsl:47-96 sample_catmull_rom at normalised uv on a w x h image: nine
+// texture() taps. The tap positions decide the texels read, so they are
+// formed with IEEE operations in the shader's order (including its division
+// back to normalised coordinates, which texture() scales again).
+DEV void catmull_rom_uv(const half4 *img, int w, int h, float u, float v, float res[4])
+{
+  const float ts[2] = { (float)w, (float)h }, uv[2] = { u, v };
+  float t[2][3], wt[2][3];
+#pragma unroll
+  for(int k = 0; k < 2; k++)
+  {
+    const float sp = __fmul_rn(uv[k], ts[k]);
+    const float tp1 = __fadd_rn(floorf(__fsub_rn(sp, 0.5f)), 0.5f);
+    const float f = __fsub_rn(sp, tp1);
+    const float w1 = __fadd_rn(1.0f, __fmul_rn(__fmul_rn(f, f), __fadd_rn(-2.5f, __fmul_rn(1.5f, f))));
+    const float w2 = __fmul_rn(f, __fadd_rn(0.5f, __fmul_rn(f, __fsub_rn(2.0f, __fmul_rn(1.5f, f)))));
+    const float w12 = __fadd_rn(w1, w2);
+    t[k][0] = __fmul_rn(__fdiv_rn(__fsub_rn(tp1, 1.0f), ts[k]), ts[k]);
+    t[k][1] = __fmul_rn(__fdiv_rn(__fadd_rn(tp1, __fdiv_rn(w2, w12)), ts[k]), ts[k]);
+    t[k][2] = __fmul_rn(__fdiv_rn(__fadd_rn(tp1, 2.0f), ts[k]), ts[k]);
+    wt[k][0] = f * (-0.5f + f * (1.0f - 0.5f * f));
+    wt[k][1] = w12;
+    wt[k][2] = f * f * (-0.5f + 0.5f * f);
+  }
+#pragma unroll
+  for(int c = 0; c < 4; c++) res[c] = 0.0f;
+#pragma unroll
+  for(int j = 0; j < 3; j++)
+#pragma unroll
+    for(int i = 0; i < 3; i++)
+    {
+      float q[4];
+      bilinear(img, w, h, t[0][i], t[1][j], q);
+#pragma unroll
+      for(int c = 0; c < 4; c++) res[c] += q[c] * wt[0][i] * wt[1][j];
+    }
+}

@@ -312,6 +312,10 @@ CROP_CASES = {
     "perspective_1024x768": (1024, 768, BAYER, 0, (0.2, 0.22, 0.8, 0.25, 0.77, 0.8, 0.21, 0.75),
                              (0.1, 0.9, 0.05, 0.95), 3.5, {}),
     "window_1000x742": (1000, 742, BAYER, 0, QUAD, (0.13, 0.71, 0.2, 0.9), 0, {}),
+    # no rotation but a perspective quad: nearest texels through the homography (the crop kernel)
+    "keystone_1000x742": (1000, 742, BAYER, 0, (0.24, 0.25, 0.76, 0.25, 0.75, 0.75, 0.25, 0.75), (0, 1, 0, 1), 0, {}),
+    # a window corner on half a texel: the whole texel offsets may differ between columns
+    "halftexel_1000x742": (1000, 742, BAYER, 0, QUAD, (0.0035, 0.9, 0.0, 1.0), 0, {}),
     "xtrans_606x402": (606, 402, 9, 0, QUAD, (1, 3, 3, 7), -7.25, {}),
     "rcd_1000x742": (1000, 742, BAYER, 0, QUAD, (1, 3, 3, 7), 1337, {"dm_method": 1}),
     "wavelet_1000x742": (1000, 742, BAYER, 0, QUAD, (0.05, 0.95, 0.0, 1.0), 2.0, {"dn_strength": 1.0}),
@@ -344,15 +348,22 @@ def test_crop(gpu, name):
     P.check("crop_" + name, v, m, ip, op, g)
 
 
-def test_crop_nearest_texel_is_a_copy(gpu):
-    # without rotation and with the default quad the crop fetches texels: its output is the
-    # demosaic output shifted by the window's corner, bit for bit
+def test_crop_by_whole_texels_rides_on_the_fused_kernel(gpu):
+    # without rotation and with the default quad the crop fetches texels (x + 3, y + 3): the
+    # fused develop kernel applies it, and the result equals the crop kernel's output fed to
+    # the rest of the chain (the oracle with the CUDA path's own crop as colour's input)
     m, ip, op, setup, (cw, ch), _ = crop_case("darkroom_2048x1536")
+    with v.Graph(v.DARKROOM_CROP_CFG) as g:
+        g.set_input(2048, 1536, ip)
+        setup(g)
+        g.create_nodes()
+        fused = {(n[0], n[1]): n[5] for n in g.nodes()}
+    assert fused[("crop", "main")] == fused[("demosaic", "fix")] != fused[("llap", "curve")]
     g = P.develop_gpu(v, m, ip, setup=setup, cfg=v.DARKROOM_CROP_CFG)
-    ox, oy = int(op.cr_block[16] * 2048), int(op.cr_block[18] * 1536)
+    ox, oy = int(round(op.cr_block[16] * 2048)), int(round(op.cr_block[18] * 1536))
     assert (ox, oy) == (3, 3)
-    want = g["demosaic"][oy:oy + ch, ox:ox + cw].copy()
-    want[..., 3] = 1.0
+    want = oracle.develop(m, oracle.img_param(ip), params=op, stages=("crop",), start="crop",
+                          input=g["demosaic"])["crop"]
     assert np.array_equal(g["crop"], want)
 
 

@@ -184,6 +184,8 @@ struct vkdt_cuda_graph_t
   bool crop = false;             // demosaic -> crop -> colour connected
   bool crop_stage = false;       // the crop moves or resamples pixels (not the identity): its own launch
   bool crop_given = false;       // its committed block came with the scheduler's nodes (set_nodes)
+  bool crop_shift = false;       // the crop moves the image by whole texels: applied by the fused kernel
+  int crop_dx = 0, crop_dy = 0;  // that shift
   float crop_blk[20];            // crop's committed uniform block (crop/main.c:276-343)
   int crop_w = 0, crop_h = 0;    // its output size
   int dm_w = 0, dm_h = 0;        // the demosaic output size (crop's input; out_w x out_h without crop)
@@ -459,6 +461,50 @@ void crop_commit(vkdt_cuda_graph_t *g, int wd, int ht, float blk[20], int *ow, i
   }
 }
 
+// the position crop/main.comp samples for output pixel (x, y) on a dw x dh input, normalised,
+// with the operations and rounding of k_nd_crop (IEEE single precision, nothing contracted)
+void crop_src(const float b[20], int dw, int dh, int x, int y, float &rx, float &ry)
+{
+  const float tsx = (float)dw, tsy = (float)dh;
+  const float px = ((float)x + 0.5f) + b[16] * tsx, py = ((float)y + 0.5f) + b[18] * tsy;
+  const float vx = px - tsx * 0.5f, vy = py - tsy * 0.5f;
+  const float qx = (b[12] * vx + b[14] * vy) + tsx * 0.5f, qy = (b[13] * vx + b[15] * vy) + tsy * 0.5f;
+  const float hx = (b[0] * qx + b[4] * qy) + b[8], hy = (b[1] * qx + b[5] * qy) + b[9];
+  const float hz = (b[2] * qx + b[6] * qy) + b[10];
+  rx = hx / hz / tsx; ry = hy / hz / tsy;
+}
+
+// a crop that fetches input texel (x + dx, y + dy) for every output pixel (x, y), all inside the
+// input: no rotation (r0 = 1, so texelFetch), the identity homography, and a window whose every
+// row and column lands on the same whole texel offset (checked position by position; with the
+// identity and no rotation the cross terms are exact zeros, so x and y are independent)
+bool crop_whole_texels(const float b[20], int dw, int dh, int cw, int ch, int *dx, int *dy)
+{
+  static const float id[16] = { 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 1, 0, 0, 1 };
+  for(int k = 0; k < 16; k++) if(b[k] != id[k]) return false;   // -0 == 0
+  int sx = 0, sy = 0;
+  for(int x = 0; x < cw; x++)
+  {
+    float rx, ry;
+    crop_src(b, dw, dh, x, 0, rx, ry);
+    if(!(rx >= 0.0f && rx < 1.0f)) return false;
+    const int ix = (int)(rx * (float)dw);
+    if(x == 0) sx = ix;
+    if(ix != x + sx || ix >= dw) return false;
+  }
+  for(int y = 0; y < ch; y++)
+  {
+    float rx, ry;
+    crop_src(b, dw, dh, 0, y, rx, ry);
+    if(!(ry >= 0.0f && ry < 1.0f)) return false;
+    const int iy = (int)(ry * (float)dh);
+    if(y == 0) sy = iy;
+    if(iy != y + sy || iy >= dh) return false;
+  }
+  *dx = sx; *dy = sy;
+  return true;
+}
+
 // a block that copies its input unchanged: the identity homography and rotation, the whole frame
 bool crop_identity(const float b[20], int wd, int ht, int ow, int oh)
 {
@@ -529,6 +575,8 @@ int fill_image(vkdt_cuda_graph_t *g, dev_image_t &d, const void *d_src, void *d_
   d.fc_mode = fc->n("colour");
   module_t *ll = g->mod("llap");
   d.ll_sigma = ll->f("sigma"); d.ll_shadows = ll->f("shadows"); d.ll_highlights = ll->f("hilights"); d.ll_clarity = ll->f("clarity");
+  d.crop_dx = g->crop_shift ? g->crop_dx : 0; d.crop_dy = g->crop_shift ? g->crop_dy : 0;
+  d.crop_w = g->crop_shift ? g->out_w : g->W; d.crop_h = g->crop_shift ? g->out_h : g->H;
   d.rgbf = g->at<half4>(g->off_rgbf);
   d.l1 = g->at<__half>(g->lp[0].off);
   d.l1w = g->lp[0].w; d.l1h = g->lp[0].h;
@@ -836,6 +884,17 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
     dev_image_t dp = d;
     dp.W = g->out_w; dp.H = g->out_h;
     CU(launch_post(dp, g->crop_stage ? np.cr : g->rcd ? nullptr : np.dm, s));
+    if((r = mark())) return r;
+  }
+  else if(g->crop_shift)
+  { // 4. fused develop pass to filmcurv on the crop window, then llap curve + first reduce on it
+    dev_image_t dc = d;
+    dc.l1 = nullptr;
+    CU(launch_develop(dc, s));
+    if((r = mark())) return r;
+    dev_image_t dp = d;
+    dp.W = g->out_w; dp.H = g->out_h;
+    CU(launch_post(dp, nullptr, s));
     if((r = mark())) return r;
   }
   else
@@ -1191,7 +1250,10 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
   // bayer with the fused path's hilite front
   // a demosaic colour param >= 1 widens the bayer fix radius to 2 (fix.comp:124): node by node
   const bool wide_fix = !xt && g->mod("demosaic")->n("colour") >= 1;
-  g->unfused = xt || g->halfsize || g->rcd || wide_fix || g->crop_stage;
+  // a crop by whole texels rides on the fused kernel; any other crop resamples (its own launch)
+  g->crop_shift = g->crop_stage && !xt && !g->halfsize && !g->rcd && !wide_fix
+               && crop_whole_texels(g->crop_blk, g->dm_w, g->dm_h, g->out_w, g->out_h, &g->crop_dx, &g->crop_dy);
+  g->unfused = xt || g->halfsize || g->rcd || wide_fix || (g->crop_stage && !g->crop_shift);
   g->k1front = g->unfused && !xt;
 
   // node lists as the modules' create_nodes emit them
@@ -1285,7 +1347,7 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
   }
   std::vector<int> L_hr, L_ha, L_lr, L_la;
   int L_noop = -1, L_half = -1, L_a0 = -1, L_doub = -1, L_gauss = -1, L_splat = -1, L_fix = -1, L_hs = -1, L_rs = -1;
-  int L_rcdc = -1, L_rcdf = -1, L_crop = -1;
+  int L_rcdc = -1, L_rcdf = -1, L_crop = -1, L_curve = -1;
   int L_post, L_k1 = -1;
   const bool k1 = !g->unfused || g->k1front;
   int L_tail = -1;   // the one-CTA tail computes hr[hl_tail..] and hb[hl_tail..]
@@ -1301,7 +1363,11 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
     for(size_t l = 1; l < g->hr.size(); l++) L_hr.push_back(hl_reduce(l));
     for(size_t l = 0; l < g->hb.size(); l++) L_ha.push_back(hl_assemble(l));
   }
-  if(!g->unfused) L_post = launch("demosaic", "fix");
+  if(!g->unfused)
+  {
+    L_post = launch("demosaic", "fix");
+    if(g->crop_shift) L_curve = launch("llap", "curve");   // llap curve + first reduce on the cropped image
+  }
   else
   {
     if(!k1)
@@ -1348,6 +1414,7 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
       if(n.name == tkn("denoise") || n.kernel == tkn("doub") || n.name == tkn("demosaic") || n.name == tkn("colour")
           || n.name == tkn("OpenDRT") || n.name == tkn("filmcurv") || n.kernel == tkn("curve") || n.name == tkn("crop"))
         n.fused = L_post;
+      if(n.kernel == tkn("curve") && g->crop_shift) n.fused = L_curve;
       if(n.name == tkn("hilite") && n.kernel == tkn("half")) n.fused = L_k1;
       continue;
     }
@@ -1374,7 +1441,7 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
   }
   for(size_t l = 0; l < g->lp.size(); l++)
   {
-    add_node(g, "llap", "reduce", g->lp[l].w, g->lp[l].h, 11, l == 0 ? L_post : L_lr[l - 1]);
+    add_node(g, "llap", "reduce", g->lp[l].w, g->lp[l].h, 11, l == 0 ? (g->crop_shift ? L_curve : L_post) : L_lr[l - 1]);
     const int fw = l == 0 ? OW : g->lp[l - 1].w, fh = l == 0 ? OH : g->lp[l - 1].h;
     add_node(g, "llap", "assemble", fw, fh, 1, l == 0 ? L_fin : L_la[l - 1]);
   }
@@ -1880,6 +1947,19 @@ int vkdt_cuda_graph_debug_stage(vkdt_cuda_graph_t *g, int stage, float *out, siz
   {
     if(stage != 2 && !g->debug) return fail(VKDT_CUDA_INCOMPLETE, "debug stages not enabled");
     if(stage == 11 && !g->crop_stage) return fail(VKDT_CUDA_INCOMPLETE, "no crop stage in this graph");
+    if(stage == 11 && g->crop_shift)
+    { // the fused kernel reads the window of its demosaic output: that window, alpha 1
+      if(count < nout * 4) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "buffer too small");
+      std::vector<__half> h((size_t)g->W * g->H * 4);
+      CU(cudaMemcpy(h.data(), g->arena + g->off_dbg_dm, h.size() * 2, cudaMemcpyDeviceToHost));
+      for(int y = 0; y < g->out_h; y++) for(int x = 0; x < g->out_w; x++)
+      {
+        const size_t i = (size_t)y * g->out_w + x, j = (size_t)(y + g->crop_dy) * g->W + x + g->crop_dx;
+        for(int k = 0; k < 3; k++) out[4 * i + k] = __half2float(h[4 * j + k]);
+        out[4 * i + 3] = 1.0f;
+      }
+      return 0;
+    }
     const size_t n = stage == 3 ? (size_t)g->dm_w * g->dm_h : nout;
     if(count < n * 4) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "buffer too small");
     std::vector<__half> h(n * 4);

@@ -8,6 +8,14 @@
 // mosaic in, the filmcurv output (rgba f16, needed by llap/colour) and the 11
 // level 1 planes of the llap pyramid out.
 //
+// A crop after demosaic that moves the image by whole texels (crop/main.comp
+// fetching texel (x + dx, y + dy) for every output pixel: no rotation, the
+// untouched quad) is applied on the way out: the colour, histogram and
+// filmcurv outputs of the window's pixels are written at crop coordinates. The
+// llap levels then belong to the cropped image, whose tiles do not align with
+// these (an odd shift moves them off the CFA blocks): with a crop the kernel
+// ends at filmcurv and the llap curve and first reduce run on its output.
+//
 // Tiling: one CTA computes a TX x TY tile of output pixels. Every stage is
 // evaluated on the halo its consumer needs (slots indexed by "virtual"
 // positions that hold the value of the mirrored real position, which is what
@@ -47,23 +55,26 @@ constexpr int LH = (LX + 1) / 2;
 constexpr int BX = TX / 4 + 6;       // hilite coarse level slots
 constexpr int NPL = 11;              // NUM_GAMMA curves + grey (llap/config.h:2)
 
+struct early_t
+{
+  float sw[3][CX][CX];         // splat weights, same taps as fw
+  float B1[3][BX][BX];         // hilite coarse level (rgb) around the tile
+};
 struct smem_t
 {
   float M[MX][2][MB];          // hilite output mosaic, [y][x&1][x>>1]
   float fw[3][CX][CX];         // fix weights of the taps (+-1,0), (0,+-1), (+-1,+-1)
   __half g[GX][2][GH];         // splat output (f16 values), [y][x&1][x>>1]
   float rg[GX][2][GH];         // 1 / (1e-4 + splat output)
+  uint32_t hist[257];
   union
   { // the llap level 0 planes are written after the last reads of the others
-    struct
-    {
-      float sw[3][CX][CX];     // splat weights, same taps as fw
-      float B1[3][BX][BX];     // hilite coarse level (rgb) around the tile
-    } e;
+    early_t e;
     __half L0[NPL][LX][LX + 1]; // llap level 0 planes, [y][slot] (rows of an even length)
   } u;
-  uint32_t hist[257];
 };
+// without the llap level 0 planes (the kernel ends at filmcurv)
+constexpr size_t SMEM_NO_L1 = offsetof(smem_t, u) + sizeof(early_t);
 
 DEV int mirror1(int i, int n)
 { // mirrored repeat for |overshoot| < n, clamped for slots no pixel reads
@@ -191,7 +202,7 @@ template<bool INTERIOR> DEV void tile_of(const tiles_t &t, int &bx, int &by)
   bx = k < left ? k : t.ix1 + 1 + (k - left);
 }
 
-template<bool INTERIOR> __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p, const tiles_t tiles)
+template<bool INTERIOR, bool L1> __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p, const tiles_t tiles)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   smem_t &s = *reinterpret_cast<smem_t *>(smem_raw);
@@ -386,6 +397,11 @@ template<bool INTERIOR> __global__ void __launch_bounds__(NT) k_develop(const de
       const int vx = X0 - 1 + slx, vy = Y0 - 1 + sly;
       float rr = 0.0f, rb = 0.0f, wr = 0.0f, wb = 0.0f, rg = 0.0f, wg = 0.0f;
       int px, py;
+      if(!L1)
+      { // only the pixels this tile owns: the halo fed the llap level 0 planes
+        const int qx = interior ? vx : mirror1(vx, W), qy = interior ? vy : mirror1(vy, H);
+        if(qx != vx || qy != vy || vx < OX || vx >= OXe || vy < OY || vy >= OYe) continue;
+      }
       // demosaic/fix.comp:99-135, radius clamp(fixup+1, 1, 2) = 1 for the
       // default fixup 0 (the host rejects other values for this kernel)
       if(interior)
@@ -425,19 +441,21 @@ template<bool INTERIOR> __global__ void __launch_bounds__(NT) k_develop(const de
       float co[3];
       colour_px(p, dm, co);
       const bool own = vx == px && vy == py && px >= OX && px < OXe && py >= OY && py < OYe;
-      if(own && p.dbg_colour)
-      {
-        p.dbg_demosaic[(size_t)py * W + px] = mk_half4(dm[0], dm[1], dm[2], 1.0f);
-        p.dbg_colour[(size_t)py * W + px] = mk_half4(co[0], co[1], co[2], 1.0f);
-      }
-      if(own && p.hist)
+      // the crop window's pixels, at crop coordinates (the whole image without a crop)
+      const int ccx = px - p.crop_dx, ccy = py - p.crop_dy;
+      const bool keep = own && ccx >= 0 && ccy >= 0 && ccx < p.crop_w && ccy < p.crop_h;
+      const size_t co_at = (size_t)ccy * p.crop_w + ccx;
+      if(own && p.dbg_colour) p.dbg_demosaic[(size_t)py * W + px] = mk_half4(dm[0], dm[1], dm[2], 1.0f);
+      if(keep && p.dbg_colour) p.dbg_colour[co_at] = mk_half4(co[0], co[1], co[2], 1.0f);
+      if(keep && p.hist)
       {
         const uint32_t bin = hist_bin(co[0], co[1], co[2]);
         if(bin > 0) { atomicAdd(&s.hist[bin], 1u); atomicAdd(&s.hist[256], 1u); }
       }
       float fc[3];
       filmcurv_px(p, co, fc);
-      if(own) p.rgbf[(size_t)py * W + px] = mk_half4(fc[0], fc[1], fc[2], 1.0f);
+      if(keep) p.rgbf[co_at] = mk_half4(fc[0], fc[1], fc[2], 1.0f);
+      if(!L1) continue;
       const float yv = lum2020(gclamp(fc[0], -1000.0f, 1000.0f), gclamp(fc[1], -1000.0f, 1000.0f), gclamp(fc[2], -1000.0f, 1000.0f));
       if(unit_curve)
       {
@@ -457,6 +475,7 @@ template<bool INTERIOR> __global__ void __launch_bounds__(NT) k_develop(const de
   __syncthreads();
 
   // ---- llap/reduce.comp (sample_semisoft) for level 1 outputs [X0/2, X0/2+TX/2) (llap_reduce_px)
+  if(L1)
   {
     const int lx = tid % (TX / 2), ly = tid / (TX / 2);
     const int ox = X0 / 2 + lx, oy = Y0 / 2 + ly;
@@ -483,15 +502,25 @@ template<bool INTERIOR> __global__ void __launch_bounds__(NT) k_develop(const de
 cudaError_t init_develop()
 {
   cudaError_t e = cudaSuccess;
-  for(auto f : { k_develop<true>, k_develop<false> })
+  const void *fs[4] = { (const void *)k_develop<true, true>, (const void *)k_develop<false, true>,
+                        (const void *)k_develop<true, false>, (const void *)k_develop<false, false> };
+  for(int i = 0; i < 4; i++)
   {
-    if(e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(smem_t));
-    // the whole unified L1 as shared memory: 5 CTAs of 43.5 KB per SM
-    if(e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    const int bytes = i < 2 ? (int)sizeof(smem_t) : (int)SMEM_NO_L1;
+    if(e == cudaSuccess) e = cudaFuncSetAttribute(fs[i], cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    // the whole unified L1 as shared memory: 5 CTAs of 43.5 KB per SM (with the llap planes)
+    if(e == cudaSuccess) e = cudaFuncSetAttribute(fs[i], cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
   }
   if(e == cudaSuccess) e = init_llap();
   if(e == cudaSuccess) e = init_hilite();
   return e;
+}
+
+template<bool L1> static void launch_tiles(const dev_image_t &p, const tiles_t &t, int nin, cudaStream_t s)
+{
+  const size_t bytes = L1 ? sizeof(smem_t) : SMEM_NO_L1;
+  if(nin > 0) k_develop<true, L1><<<dim3(t.ix1 - t.ix0 + 1, t.iy1 - t.iy0 + 1), NT, bytes, s>>>(p, t);
+  k_develop<false, L1><<<t.nx * t.ny - nin, NT, bytes, s>>>(p, t);
 }
 
 cudaError_t launch_develop(const dev_image_t &p, cudaStream_t s)
@@ -504,11 +533,10 @@ cudaError_t launch_develop(const dev_image_t &p, cudaStream_t s)
   if(p.W < 2 * TX + 4 || p.H < 2 * TY + 4 || t.ix1 < t.ix0 || t.iy1 < t.iy0)
   { // no interior: every tile is a border tile (the ring is the whole grid)
     t.ix0 = t.nx; t.ix1 = t.nx - 1; t.iy0 = t.ny; t.iy1 = t.ny - 1;
-    k_develop<false><<<t.nx * t.ny, NT, sizeof(smem_t), s>>>(p, t);
-    return cudaGetLastError();
   }
-  const int nin = (t.ix1 - t.ix0 + 1) * (t.iy1 - t.iy0 + 1);
-  k_develop<true><<<dim3(t.ix1 - t.ix0 + 1, t.iy1 - t.iy0 + 1), NT, sizeof(smem_t), s>>>(p, t);
-  k_develop<false><<<t.nx * t.ny - nin, NT, sizeof(smem_t), s>>>(p, t);
+  const int nin = t.ix1 < t.ix0 ? 0 : (t.ix1 - t.ix0 + 1) * (t.iy1 - t.iy0 + 1);
+  // p.l1 null: end at filmcurv (a crop follows demosaic; the llap level 1 is made from rgbf)
+  if(p.l1) launch_tiles<true>(p, t, nin, s);
+  else launch_tiles<false>(p, t, nin, s);
   return cudaGetLastError();
 }

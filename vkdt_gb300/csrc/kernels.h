@@ -44,15 +44,19 @@ struct dev_image_t
   int fc_mode;
   // llap
   float ll_sigma, ll_shadows, ll_highlights, ll_clarity;
+  // a crop after demosaic that moves the image by whole texels (crop/main.comp's
+  // texelFetch of (x + dx, y + dy)): the outputs below are the window's, at crop
+  // coordinates (dx = dy = 0 and the demosaic size without a crop)
+  int crop_dx, crop_dy, crop_w, crop_h;
   // outputs of the develop kernel
-  half4 *rgbf;          // filmcurv output, W*H rgba f16
-  __half *l1;           // llap level 1, 11 planes
+  half4 *rgbf;          // filmcurv output, crop_w*crop_h rgba f16
+  __half *l1;           // llap level 1, 11 planes (null: the develop kernel ends at filmcurv)
   int l1w, l1h;
   size_t l1plane;       // elements per plane
   uint32_t *hist;       // 257 counts or null
   // debug copies (null in production)
   __half *dbg_denoise, *dbg_hilite;
-  half4 *dbg_demosaic, *dbg_colour;   // demosaic and colour outputs at the output size
+  half4 *dbg_demosaic, *dbg_colour;   // demosaic output (W*H) and colour output (crop_w*crop_h)
   uint8_t *dbg_gauss;                 // demosaic/gauss decisions per entry (GAUSS_DEC bits)
 };
 

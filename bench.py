@@ -1,11 +1,14 @@
 """Benchmark of the raw development path on GB300.
 
-Workload (one step = one develop of one image): the 24 MP darkroom graph,
-6000x4000 RGGB uint16 holding 14-bit values (black 512, white 16383), the
-seeded synthetic scene with Poisson-Gaussian noise a=8, b=1.6 (DN) and 2% of
-the pixels clipped, white balance (2, 1, 1.6), llap at 6 pyramid levels,
-denoise -> hilite -> demosaic -> colour -> filmcurv -> llap with the module
-defaults and the darkroom .cfg values. Output rgba f16.
+Workload (one step = one develop of one image): the 24 MP full darkroom
+graph, 6000x4000 RGGB uint16 holding 14-bit values (black 512, white 16383),
+the seeded synthetic scene with Poisson-Gaussian noise a=8, b=1.6 (DN) and 2%
+of the pixels clipped, white balance (2, 1, 1.6), llap at 6 pyramid levels,
+the chain of bin/default-darkroom.i-raw: denoise -> hilite -> demosaic -> crop
+-> colour -> filmcurv -> llap -> grade with the module defaults and the .cfg's
+values (crop at its defaults: the exif rotation, none here, and a 3 px margin,
+so the output is 5993x3994). --graph chain drops crop and grade (the 6000x4000
+output of the plain chain). Output rgba f16.
 
 value: MP/s of input mosaic with the inputs resident in HBM (a ring of 4
 distinct mosaics, 192 MB > 129 MB L2, each with its own captured CUDA graph).
@@ -47,6 +50,9 @@ DENOISE = 0.0
 DEMOSAIC = 0          # demosaic method: 0 gaussian splats (the raw photo default), 1 rcd, 2 half size
 FILTERS = 0x94949494  # bayer rggb; 9: x-trans
 DEMOSAIC_NAMES = {0: "gaussian splats (method 0)", 1: "rcd (method 1)", 2: "half size (method 2)"}
+GRAPH = "darkroom"    # darkroom: bin/default-darkroom.i-raw's chain (crop, grade); chain: without them
+# grade/params defaults (the llap output graded as the darkroom cfg leaves it)
+GRADE_DEFAULTS = ((0, 0, 0, 0), (1, 1, 1, 0), (1, 1, 1, 0), (0, 0, 0, 0), 0, 0.3, 0.4)
 # the synthetic camera's matrix to rec2020 (rows sum to one), as the package's default image parameters
 CAM_TO_REC2020 = (1.20, -0.15, -0.05, -0.10, 1.25, -0.15, 0.02, -0.22, 1.20)
 # the sources of the fused develop kernel: the DRAM traffic of an ncu capture is reported only
@@ -88,13 +94,25 @@ def img_param(v, wd, ht):
                                noise_a=NOISE_A / rng ** 2, noise_b=NOISE_B / rng)
 
 
+def graph_cfg(v):
+    return v.DARKROOM_FULL_CFG if GRAPH == "darkroom" else v.DARKROOM_CFG
+
+
+def graph_name():
+    dn = "denoise(%s)" % ("wavelet" if DENOISE > 0 else "noop")
+    if GRAPH == "darkroom":
+        return dn + "->hilite->demosaic->crop->colour->filmcurv->llap->grade (bin/default-darkroom.i-raw)"
+    return dn + "->hilite->demosaic->colour->filmcurv->llap"
+
+
 def config():
-    return {"workload": "%d MP darkroom graph, one image per step%s" % (round(WD * HT / 1e6),
-                                                                       ", wavelet denoise" if DENOISE > 0 else ""),
+    return {"workload": "%d MP %s graph, one image per step%s" % (round(WD * HT / 1e6),
+                                                               "full darkroom" if GRAPH == "darkroom" else "plain chain",
+                                                               ", wavelet denoise" if DENOISE > 0 else ""),
             "wd": WD, "ht": HT, "cfa": "x-trans" if FILTERS == 9 else "rggb", "denoise_strength": DENOISE,
             "bits": 14, "black": BLACK, "white": WHITE, "noise_a_dn": NOISE_A, "noise_b_dn": NOISE_B,
             "llap_levels": LEVELS,
-            "graph": "denoise(%s)->hilite->demosaic->colour->filmcurv->llap" % ("wavelet" if DENOISE > 0 else "noop"),
+            "graph": graph_name(),
             "demosaic": DEMOSAIC_NAMES[DEMOSAIC],
             "l2": "ring of %d distinct resident mosaics (%d MB > 129 MB L2)" % (RING, RING * WD * HT * 2 // 2 ** 20)}
 
@@ -160,12 +178,38 @@ def oracle_img_param(oracle, wd, ht):
     return ip
 
 
-def oracle_params(oracle):
+def oracle_params(oracle, wd=None, ht=None):
     p = oracle.default_params()
     p.ll_levels = LEVELS
     p.dn_strength = DENOISE
     p.dm_method = DEMOSAIC
+    if GRAPH == "darkroom":   # crop/main.c's commit at its defaults for the demosaic output
+        blk, cw, ch = oracle.crop_commit(wd or WD, ht or HT)
+        oracle.set_crop(p, blk, cw, ch)
     return p
+
+
+def oracle_sink(oracle, m, ip, p, double=False):
+    """the graph's output on the oracle: the llap output, graded with grade's defaults
+    (stored as f16) on the full darkroom graph"""
+    out = oracle.develop(m, ip, params=p, double=double, stages=("llap",))["llap"]
+    if GRAPH == "darkroom":
+        out = oracle.grade(out, *GRADE_DEFAULTS).astype(np.float16).astype(np.float32)
+    return out
+
+
+def reference_sink(glsl_ref, m, ip, p):
+    """the same on the reference's shaders compiled for the CPU (grade/main.comp for the grade)"""
+    out = glsl_ref.develop(m, ip, params=p)["llap"]
+    if GRAPH == "darkroom":
+        lift, gamma, gain, off, mode, sp, hp = GRADE_DEFAULTS
+        h, w = out.shape[:2]
+        src, dst = glsl_ref.Img(w, h, 4), glsl_ref.Img(w, h, 4)
+        src.a[...] = out
+        glsl_ref.run("grade_main", w, h, {0: src, 1: dst},
+                     uniform=glsl_ref.f32(*lift, *gamma, *gain, *off) + glsl_ref.i32(mode) + glsl_ref.f32(sp, hp))
+        out = dst.a
+    return out
 
 
 def cpu_leg(args):
@@ -179,7 +223,7 @@ def cpu_leg(args):
     out = np.load(os.path.join(args.cpu_leg, "out.npy")).astype(np.float32)
     ht, wd = m.shape
     ip = oracle_img_param(oracle, wd, ht)
-    p = oracle_params(oracle)
+    p = oracle_params(oracle, wd, ht)
     res = {}
 
     def err(ref):
@@ -188,14 +232,15 @@ def cpu_leg(args):
         de = delta_e2000(out, ref)
         return {"max": float(e.max()), "mean": float(e.mean()), "px_over_2e-3": int((e > 2e-3).sum()),
                 "de2000_max": float(de.max()), "px_de_over_0.5": int((de >= 0.5).sum())}
-    res["err"] = {"stage": "llap output (the sink), rgb, |a-b|/max(1,|b|)", "window": "full %dx%d" % (wd, ht),
-                  "vs_oracle_fp32": err(oracle.develop(m, ip, params=p, stages=("llap",))["llap"]),
-                  "vs_fp64": err(oracle.develop(m, ip, params=p, double=True, stages=("llap",))["llap"]),
+    res["err"] = {"stage": "the graph's output (%s), rgb, |a-b|/max(1,|b|)" % ("grade" if GRAPH == "darkroom" else "llap"),
+                  "window": "full %dx%d" % (out.shape[1], out.shape[0]),
+                  "vs_oracle_fp32": err(oracle_sink(oracle, m, ip, p)),
+                  "vs_fp64": err(oracle_sink(oracle, m, ip, p, double=True)),
                   "tolerance": {"max": 2e-3, "mean": 1e-4, "de2000": 0.5,
                                 "note": "pixels over 2e-3 are where a branch of the reference was a near tie "
                                         "(tests/parity.py shows each such decision explained)"}}
     if not args.no_cpu:
-        run = lambda: oracle.develop(m, ip, params=p, stages=("llap",))
+        run = lambda: oracle_sink(oracle, m, ip, p)
         run()
         t0 = time.perf_counter()
         n = 0
@@ -223,12 +268,12 @@ def run_reference(args):
     try:
         from oracle import glsl_ref
         if glsl_ref.build():
-            run = lambda: glsl_ref.develop(m, ip, params=p)
+            run = lambda: reference_sink(glsl_ref, m, ip, p)
             kind = "reference"
     except Exception:
         run = None
     if run is None:
-        run = lambda: oracle.develop(m, ip, params=p, stages=("llap",))
+        run = lambda: oracle_sink(oracle, m, ip, p)
     t0 = time.perf_counter()
     run()                                   # first warm-up step: also sizes the run
     t_one = time.perf_counter() - t0
@@ -242,8 +287,9 @@ def run_reference(args):
         rows = max(64, int(HT * 180.0 / (steps * t_one)) // 2 * 2)
         mb = np.ascontiguousarray(m[:rows])
         ipb = oracle_img_param(oracle, WD, rows)
-        run = (lambda: glsl_ref.develop(mb, ipb, params=p)) if kind == "reference" else \
-              (lambda: oracle.develop(mb, ipb, params=p, stages=("llap",)))
+        pb = oracle_params(oracle, WD, rows)
+        run = (lambda: reference_sink(glsl_ref, mb, ipb, pb)) if kind == "reference" else \
+              (lambda: oracle_sink(oracle, mb, ipb, pb))
         run()
     t0 = time.perf_counter()
     for _ in range(steps):
@@ -710,7 +756,7 @@ def run_workload(args):
         torch.distributed.destroy_process_group()
 
 def main():
-    global WD, HT, RING, LEVELS, DENOISE, DEMOSAIC, FILTERS
+    global WD, HT, RING, LEVELS, DENOISE, DEMOSAIC, FILTERS, GRAPH
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
@@ -734,6 +780,9 @@ def main():
     ap.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
     ap.add_argument("--slots", type=int, default=4, help="serve/video: jobs in flight")
     ap.add_argument("--cfa", default="rggb", choices=("rggb", "xtrans"), help="single: the mosaic's colour filter array")
+    ap.add_argument("--graph", default=GRAPH, choices=("darkroom", "chain"),
+                    help="single: darkroom (bin/default-darkroom.i-raw's chain with crop and grade) or chain "
+                         "(denoise .. llap only)")
     ap.add_argument("--demosaic", type=int, default=-1, choices=(-1, 0, 1, 2),
                     help="demosaic method (-1: the workload's default: 0 for photos, 1 for the video streams)")
     args = ap.parse_args()
@@ -741,6 +790,7 @@ def main():
     RING, LEVELS, DENOISE = args.ring, args.levels, args.denoise
     DEMOSAIC = max(0, args.demosaic)
     FILTERS = 9 if args.cfa == "xtrans" else 0x94949494
+    GRAPH = args.graph
     if args.cpu_leg:
         return cpu_leg(args)
     if args.impl == "reference":
@@ -766,7 +816,7 @@ def main():
     # ring of resident inputs, one graph (and CUDA graph) per slot
     graphs = []
     for i in range(RING):
-        g = v.Graph()
+        g = v.Graph(graph_cfg(v))
         g.set_input(WD, HT, img_param(v, WD, HT))
         if LEVELS:
             g.set_llap_levels(LEVELS)
@@ -807,7 +857,7 @@ def main():
     ms = over_ranks(ms_rank, "max")
 
     # ---- per kernel durations (events around every launch, one sync per step)
-    gt = v.Graph()
+    gt = v.Graph(graph_cfg(v))
     gt.set_input(WD, HT, img_param(v, WD, HT))
     if LEVELS:
         gt.set_llap_levels(LEVELS)
@@ -837,19 +887,24 @@ def main():
     dev_idx = names.index("demosaic:fix") if fused else int(np.argmax(kms))
     dev_ms = float(kms[dev_idx])
     npx, qpx = WD * HT, (WD // 2) * (HT // 2)
+    ow, oh = gt.out_wd, gt.out_ht                       # the output size (the crop window)
+    opx, oqpx = ow * oh, ((ow + 1) // 2) * ((oh + 1) // 2)
+    crop_fused = fused and (ow, oh) != (WD, HT)         # the develop kernel ends at filmcurv
     # algorithmic bytes per launch (each buffer the launch must read or write, once):
     alg_bytes = {
         # fused develop: mosaic in (2 B/px), the hilite coarse level (8 B per (W/4 x H/4) px),
-        # filmcurv rgba f16 out (8 B/px), 11 llap level 1 planes out (11 * 2 B per (W/2 x H/2) px)
-        "demosaic:fix": npx * 2 + (WD // 4) * (HT // 4) * 8 + npx * 8 + 11 * 2 * qpx,
+        # filmcurv rgba f16 out (8 B per output px), 11 llap level 1 planes out (11 * 2 B per
+        # level 1 px) unless a crop follows demosaic (then the next launch makes them)
+        "demosaic:fix": npx * 2 + (WD // 4) * (HT // 4) * 8 + opx * 8 + (0 if crop_fused else 11 * 2 * oqpx),
         # rcd_fill: mosaic, vh, pq + lp (half width) in, rgba f16 out
         "demosaic:rcd_fill": npx * (2 + 2 + 2 + 8),
         # rcd_conv: mosaic in, vh, pq + lp out
         "demosaic:rcd_conv": npx * (2 + 2 + 2),
-        # colour .. llap curve + level 1 reduce of the per-node chain: rgba in, rgba out, 11 planes out
-        "llap:curve": npx * (8 + 8) + 11 * 2 * qpx,
-        # llap level 0 assemble + colour: rgba, 11 level 1 planes, level 1 assembled in, rgba out
-        "llap:colour": npx * (8 + 8) + 11 * 2 * qpx + 2 * qpx,
+        # colour .. llap curve + level 1 reduce of the per-node chain: rgba in, rgba out, 11 planes out;
+        # after the fused develop kernel with a crop: filmcurv rgba in, 11 planes out
+        "llap:curve": (opx * 8 if crop_fused else opx * (8 + 8)) + 11 * 2 * oqpx,
+        # llap level 0 assemble + colour (+ grade): rgba, 11 level 1 planes, level 1 assembled in, rgba out
+        "llap:colour": opx * (8 + 8) + 11 * 2 * oqpx + 2 * oqpx,
     }
     if not fused:
         alg_bytes.pop("demosaic:fix")
@@ -880,7 +935,8 @@ def main():
                      "thread_inst_per_px": tj.get("k_develop_thread_inst_per_px"), "source": "ncu capture, profiles/"}
         except Exception:
             traffic = None
-    kname = {"demosaic:fix": "k_develop (hilite doub + demosaic + colour + filmcurv + llap curve/reduce)" if fused
+    kname = {"demosaic:fix": ("k_develop (hilite doub + demosaic + crop + colour + filmcurv)" if crop_fused else
+                              "k_develop (hilite doub + demosaic + colour + filmcurv + llap curve/reduce)") if fused
              else "k_nd_fix_xt",
              "demosaic:splat": "k_nd_splat_xt",
              "demosaic:rcd_fill": "k_rcd_fill", "demosaic:rcd_conv": "k_rcd_conv",
@@ -949,7 +1005,7 @@ def main():
     reps = sorted(replica_rate(np_ * mp_step, pipelined(np_)) for _ in range(3))
     pipe_value = reps[1]
     e2e = {"value": pipe_value, "unit": "MP/s", "h2d_bytes_per_step": WD * HT * 2,
-           "d2h_bytes_per_step": WD * HT * 8, "steps": np_, "repeats_mps": [round(x, 1) for x in reps],
+           "d2h_bytes_per_step": ow * oh * 8, "steps": np_, "repeats_mps": [round(x, 1) for x in reps],
            "timing": "median of 3 repeats of %d pipelined steps each (host clock, >= 1 s each)" % np_,
            "graphs_in_flight": len(ring),
            "one_at_a_time": {"value": world * mp_step / (e2e_ms / 1e3), "unit": "MP/s"},
@@ -983,6 +1039,7 @@ def main():
             np.save(os.path.join(td, "mosaic.npy"), host_m)
             np.save(os.path.join(td, "out.npy"), np.asarray(out))
             cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--cpu-leg", td, "--size", "%dx%d" % (WD, HT),
+                   "--graph", GRAPH,
                    "--levels", str(LEVELS), "--denoise", str(DENOISE), "--cfa", "xtrans" if FILTERS == 9 else "rggb",
                    "--demosaic", str(DEMOSAIC)] + (["--no-cpu"] if args.no_cpu else [])
             r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)

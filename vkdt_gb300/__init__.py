@@ -13,7 +13,7 @@ from . import _lib
 from ._lib import ImgParam, Scene, check, token, token_str, RUN_ALL, RUN_UPLOAD_SOURCE, RUN_DOWNLOAD_SINK, RUN_WAIT_DONE
 
 __all__ = ["Graph", "Server", "ImgParam", "Scene", "init", "default_img_param", "scene_host", "scene_device",
-           "DARKROOM_CFG", "DARKROOM_CROP_CFG", "CAM_TO_REC2020", "supports"]
+           "DARKROOM_CFG", "DARKROOM_CROP_CFG", "DARKROOM_FULL_CFG", "CAM_TO_REC2020", "supports"]
 
 # the synthetic camera: camera rgb -> rec2020, rows sum to one
 CAM_TO_REC2020 = (1.20, -0.15, -0.05,
@@ -42,9 +42,13 @@ param:llap:01:shadows:1
 param:llap:01:hilights:1
 param:llap:01:clarity:0.2
 """
+# the whole chain of bin/default-darkroom.i-raw: crop after demosaic, grade after llap (the cfg's
+# histogram, zones, lens, pick and display modules are not on the path)
 DARKROOM_CROP_CFG = (DARKROOM_CFG.replace("module:demosaic:01:568:400\n", "module:demosaic:01:568:400\nmodule:crop:01:743:400\n")
                      .replace("connect:demosaic:01:output:colour:01:input\n",
                               "connect:demosaic:01:output:crop:01:input\nconnect:crop:01:output:colour:01:input\n"))
+DARKROOM_FULL_CFG = (DARKROOM_CROP_CFG.replace("module:llap:01:1269:400\n", "module:llap:01:1269:400\nmodule:grade:01:1444:400\n")
+                     + "connect:llap:01:output:grade:01:input\n")
 
 _inited = None
 

@@ -28,6 +28,10 @@ more than 2e-3). The tolerance is max 2e-3, mean 1e-4 and CIEDE2000 < 0.5.
    - the colour transform is linear: its output can move by the colour
      matrix's gain times the demosaic output's difference plus one f16 step;
      each colour pixel over 2e-3 is checked to be within that bound;
+   - after colour (filmcurv, llap) a pixel over the tolerance must come from
+     the colour input: the oracle run from colour on to the end on the CUDA
+     path's own colour input (each pixel of which meets the tolerance against
+     the reference's) meets the tolerance there;
    - on the wavelet denoise path (its detail mask raises the slope of the
      coarse levels to the 16th power) and through rcd (its gradient weights
      are 1 / (1e-5 + |difference|)), the pixels over the tolerance are fewer
@@ -224,6 +228,7 @@ def check(name, v, m, ip, op, gpu, stages=("denoise", "hilite", "demosaic", "cro
         # the FP32 arithmetic of the reference (with the same decisions) is
         f32 = oracle.develop(m, oracle.img_param(ip), params=op, stages=stages, force={k: dec[k] for k in dec})
     gain = None
+    chain = None   # the oracle from colour on, on the CUDA path's own colour input
     for s in stages:
         a, b = gpu[s], forced[s]
         assert a.shape[:2] == b.shape[:2], (name, s, a.shape, b.shape)
@@ -286,6 +291,16 @@ def check(name, v, m, ip, op, gpu, stages=("denoise", "hilite", "demosaic", "cro
                 r["over_beyond_gain_bound"] = int(bad.sum())
                 if bad.any():
                     problems.append(("colour over the tolerance beyond the propagated bound", r))
+            elif s in ("filmcurv", "llap") and ("crop" in gpu or "demosaic" in gpu):
+                if chain is None:
+                    src = "crop" if "crop" in gpu else "demosaic"
+                    chain = oracle.develop(m, oracle.img_param(ip), params=op, stages=("filmcurv", "llap"),
+                                           start="colour", input=gpu[src], force=dec)
+                bad = over & (rel_err(a, chain[s]) > tol)
+                bad |= (delta_e2000(a, b) >= de) & (delta_e2000(a, chain[s]) >= de)
+                r["over_beyond_input_chain"] = int(bad.sum())
+                if bad.any():
+                    problems.append(("%s over the tolerance not explained by the colour input" % s, r))
             else:
                 problems.append(("e2e", s, r, np.unravel_index(int(np.argmax(e)), e.shape)))
         rec[s] = r

@@ -39,6 +39,27 @@ void forget_static_scratch()
   for(auto &p : g_static_base) p = nullptr;
 }
 
+// a word of mapped pinned host memory per device in which kernels record a bounded wait that
+// ran out (bit 0: a TMA copy did not complete); the host reads it after a run without a device call
+uint32_t *g_status_host[64] = { nullptr };
+uint32_t *g_status_dev[64] = { nullptr };
+uint32_t *device_status()
+{
+  int d = -1;
+  if(cudaGetDevice(&d) != cudaSuccess || d < 0 || d >= 64) return nullptr;
+  return g_status_dev[d];
+}
+// the recorded status of the current device, cleared
+uint32_t take_device_status()
+{
+  int d = -1;
+  if(cudaGetDevice(&d) != cudaSuccess || d < 0 || d >= 64 || !g_status_host[d]) return 0;
+  volatile uint32_t *h = g_status_host[d];
+  const uint32_t v = *h;
+  if(v) *h = 0;
+  return v;
+}
+
 int fail(int code, const char *fmt, ...) __attribute__((format(printf, 2, 3)));
 int fail(int code, const char *fmt, ...)
 {
@@ -151,7 +172,7 @@ struct module_t
 };
 
 // ------------------------------------------------------------------ device buffers
-struct level_t { int w = 0, h = 0; size_t off = 0; };
+struct level_t { int w = 0, h = 0, pitch = 0; size_t off = 0; };   // pitch: texels per row (llap: 16 byte rows)
 
 } // namespace
 
@@ -210,6 +231,9 @@ struct vkdt_cuda_graph_t
   size_t src_bytes = 0, sink_bytes = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
+  // k_llap_reduce's tensor maps (input level l-1 of reduce launch l), made for the arena tm_arena
+  std::vector<CUtensorMap> tm_reduce;
+  unsigned char *tm_arena = nullptr;
   std::vector<vkdt_cuda_node_info_t> nodes;
   // launch list (fused kernels) and timing
   struct launch_t { dt_token_t name, kernel; };
@@ -548,6 +572,11 @@ int check_supported_params(vkdt_cuda_graph_t *g)
   return 0;
 }
 
+llap_level_t llap_level(vkdt_cuda_graph_t *g, const level_t &l)
+{
+  return { g->at<__half>(l.off), l.w, l.h, l.pitch, (size_t)l.pitch * l.h };
+}
+
 // fill the per image constants for the kernels (create_nodes push constants + commit_params uniforms)
 int fill_image(vkdt_cuda_graph_t *g, dev_image_t &d, const void *d_src, void *d_out)
 {
@@ -579,8 +608,8 @@ int fill_image(vkdt_cuda_graph_t *g, dev_image_t &d, const void *d_src, void *d_
   d.crop_w = g->crop_shift ? g->out_w : g->W; d.crop_h = g->crop_shift ? g->out_h : g->H;
   d.rgbf = g->at<half4>(g->off_rgbf);
   d.l1 = g->at<__half>(g->lp[0].off);
-  d.l1w = g->lp[0].w; d.l1h = g->lp[0].h;
-  d.l1plane = (size_t)g->lp[0].w * g->lp[0].h;
+  d.l1w = g->lp[0].w; d.l1h = g->lp[0].h; d.l1pitch = g->lp[0].pitch;
+  d.l1plane = (size_t)g->lp[0].pitch * g->lp[0].h;
   d.hist = g->want_hist ? g->at<uint32_t>(g->off_hist) : nullptr;
   if(g->debug)
   {
@@ -603,8 +632,8 @@ size_t plan_arena(vkdt_cuda_graph_t *g)
   for(auto &l : g->hr) l.off = take((size_t)l.w * l.h * 8);
   for(auto &l : g->hb) l.off = take((size_t)l.w * l.h * 8);
   g->off_rgbf = take((size_t)g->out_w * g->out_h * 8);
-  for(auto &l : g->lp) l.off = take((size_t)l.w * l.h * 2 * 11);
-  for(auto &l : g->la) l.off = take((size_t)l.w * l.h * 2);
+  for(auto &l : g->lp) l.off = take((size_t)l.pitch * l.h * 2 * 11);
+  for(auto &l : g->la) l.off = take((size_t)l.pitch * l.h * 2);
   g->off_out = take(g->sink_bytes);
   g->off_hist = take(257 * 4);
   g->off_lut = take(65536 * 2);
@@ -902,21 +931,21 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
     CU(launch_develop(d, s));
     if((r = mark())) return r;
   }
-  // 5. llap reduce levels 2..nl-1
+  // 5. llap reduce levels 2..nl-1 (TMA staged through the tensor maps made for this arena)
+  const bool maps = g->tm_arena == g->arena && g->tm_reduce.size() + 1 == g->lp.size();
   for(size_t l = 1; l < g->lp.size(); l++)
   {
-    const level_t &a = g->lp[l - 1], &b = g->lp[l];
-    CU(launch_llap_reduce(g->at<__half>(a.off), a.w, a.h, (size_t)a.w * a.h, g->at<__half>(b.off), b.w, b.h, (size_t)b.w * b.h, s));
+    CU(launch_llap_reduce(llap_level(g, g->lp[l - 1]), llap_level(g, g->lp[l]), maps ? &g->tm_reduce[l - 1] : nullptr,
+        maps ? device_status() : nullptr, s));
     if((r = mark())) return r;
   }
   // 6. llap assemble A[nl-2] .. A[1]
   for(int j = (int)g->la.size(); j >= 1; j--)
   { // A[j] at level j (lp index j-1), l1 = level j+1 (lp index j)
-    const level_t &l0 = g->lp[j - 1], &l1 = g->lp[j];
     const bool first = (j == (int)g->la.size());
     const __half *coarse = first ? nullptr : g->at<__half>(g->la[j].off);
-    CU(launch_llap_assemble(coarse, first ? 1 : 0, g->at<__half>(l0.off), l0.w, l0.h, (size_t)l0.w * l0.h,
-        g->at<__half>(l1.off), l1.w, l1.h, (size_t)l1.w * l1.h, g->at<__half>(g->la[j - 1].off), s));
+    CU(launch_llap_assemble(coarse, first ? 1 : 0, llap_level(g, g->lp[j - 1]), llap_level(g, g->lp[j]),
+        g->at<__half>(g->la[j - 1].off), s));
     if((r = mark())) return r;
   }
   // 7. level 0 assemble + llap colour
@@ -936,7 +965,7 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
     k3.gr_sp = m->f("sh_pivot"); k3.gr_hp = m->f("hi_pivot");
   }
   k3.rgbf = d.rgbf; k3.W = g->out_w; k3.H = g->out_h;
-  k3.l1 = d.l1; k3.l1w = d.l1w; k3.l1h = d.l1h; k3.l1plane = d.l1plane;
+  k3.l1 = d.l1; k3.l1w = d.l1w; k3.l1h = d.l1h; k3.l1pitch = d.l1pitch; k3.l1plane = d.l1plane;
   k3.coarse = g->la.empty() ? d.l1 + 10 * d.l1plane : g->at<__half>(g->la[0].off);
   k3.ll_sigma = d.ll_sigma; k3.ll_shadows = d.ll_shadows; k3.ll_highlights = d.ll_highlights; k3.ll_clarity = d.ll_clarity;
   k3.out = (half4 *)d_out;
@@ -973,6 +1002,15 @@ int vkdt_cuda_init(int device_id, uint32_t flags)
     return fail(VKDT_CUDA_ERROR_INITIALIZATION_FAILED, "device %d is sm_%d%d, the library is built for sm_103a", device_id, prop.major, prop.minor);
   CU(cudaSetDevice(device_id));
   CU(init_develop());
+  if(!g_status_host[device_id])
+  {
+    void *h = nullptr, *d = nullptr;
+    CU(cudaHostAlloc(&h, 64, cudaHostAllocMapped | cudaHostAllocPortable));
+    memset(h, 0, 64);
+    CU(cudaHostGetDevicePointer(&d, h, 0));
+    g_status_host[device_id] = (uint32_t *)h;
+    g_status_dev[device_id] = (uint32_t *)d;
+  }
   g_device = device_id;
   return VKDT_CUDA_SUCCESS;
 }
@@ -1020,6 +1058,8 @@ static void release(vkdt_cuda_graph_t *g)
   g->stream = nullptr;
   if(g->arena) cudaFree(g->arena);
   g->arena = nullptr;
+  g->tm_reduce.clear();
+  g->tm_arena = nullptr;
   if(g->h_src) cudaFreeHost(g->h_src);
   if(g->h_sink) cudaFreeHost(g->h_sink);
   g->h_src = g->h_sink = nullptr;
@@ -1327,7 +1367,7 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
     int nl = 12;
     for(int l = 1; l < nl; l++)
     {
-      level_t lv; lv.w = rw; lv.h = rh;
+      level_t lv; lv.w = rw; lv.h = rh; lv.pitch = (rw + 7) & ~7;
       g->lp.push_back(lv);
       rw = (rw - 1) / 2 + 1; rh = (rh - 1) / 2 + 1;
       if(rw <= 1 || rh <= 1) { nl = l + 1; break; }
@@ -1467,6 +1507,12 @@ int vkdt_cuda_graph_alloc(vkdt_cuda_graph_t *g, uint64_t *device_bytes)
   g->arena_bytes = plan_arena(g);
   CU(cudaMalloc((void **)&g->arena, g->arena_bytes));
   CU(cudaMemset(g->arena, 0, g->arena_bytes));
+  { // tensor maps of the llap levels the reduce launches stage by TMA (else 4 byte copies)
+    std::vector<CUtensorMap> maps(g->lp.empty() ? 0 : g->lp.size() - 1);
+    bool ok = device_status() != nullptr;
+    for(size_t l = 1; l < g->lp.size() && ok; l++) ok = llap_reduce_tensor_map(llap_level(g, g->lp[l - 1]), &maps[l - 1]) == cudaSuccess;
+    if(ok) { g->tm_reduce = maps; g->tm_arena = g->arena; }
+  }
   if(g->wavelet && (!g->unfused || g->k1front))
   {
     std::vector<uint16_t> id(65536);
@@ -1799,8 +1845,8 @@ int vkdt_cuda_graph_develop_static(vkdt_cuda_graph_t *g, const void *d_mosaic, v
   for(auto &l : g->hr) l.off = take((size_t)l.w * l.h * 8);
   for(auto &l : g->hb) l.off = take((size_t)l.w * l.h * 8);
   g->off_rgbf = take((size_t)g->W * g->H * 8);
-  for(auto &l : g->lp) l.off = take((size_t)l.w * l.h * 2 * 11);
-  for(auto &l : g->la) l.off = take((size_t)l.w * l.h * 2);
+  for(auto &l : g->lp) l.off = take((size_t)l.pitch * l.h * 2 * 11);
+  for(auto &l : g->la) l.off = take((size_t)l.pitch * l.h * 2);
   g->off_hist = take(257 * 4);
   g->off_lut = take(65536 * 2);
   if(off > VKDT_CUDA_STATIC_SCRATCH_BYTES)
@@ -1852,6 +1898,7 @@ int vkdt_cuda_graph_wait(vkdt_cuda_graph_t *g, uint32_t timeout_ms)
     if(ms > timeout_ms) return fail(VKDT_CUDA_TIMEOUT, "wait timed out after %u ms", timeout_ms);
     if(++spin > 64) std::this_thread::sleep_for(std::chrono::microseconds(20));
   }
+  if(take_device_status() & 1u) return fail(VKDT_CUDA_TIMEOUT, "a TMA copy of the llap reduce did not complete in its bounded wait");
   if(g->timing)
   {
     for(size_t i = 0; i < g->launches.size(); i++)

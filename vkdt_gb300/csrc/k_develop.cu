@@ -486,7 +486,7 @@ template<bool INTERIOR, bool L1> __global__ void __launch_bounds__(NT) k_develop
       for(int k = 0; k < NPL; k++)
       {
         const __half *const row[3] = { &s.u.L0[k][2 * ly][2 * lx], &s.u.L0[k][2 * ly + 1][2 * lx], &s.u.L0[k][2 * ly + 2][2 * lx] };
-        p.l1[k * p.l1plane + (size_t)oy * p.l1w + ox] = f2h(llap_reduce_px(row));
+        p.l1[k * p.l1plane + (size_t)oy * p.l1pitch + ox] = f2h(llap_reduce_px(row));
       }
     }
   }

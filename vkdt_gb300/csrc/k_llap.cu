@@ -14,6 +14,9 @@
 #include "kernels.h"
 #include "pixel.cuh"
 
+#include <cudaTypedefs.h>
+#include <cstring>
+
 namespace {
 
 constexpr int NPL = 11;
@@ -103,46 +106,88 @@ template<int PX, int PY, class F> DEV float2 expand2(F fetch, int kx, int ky)
 // llap/reduce.comp:17-35 (sample_semisoft), the planes of one level. The four
 // half-texel bilinear taps are the chain of pair sums scaled once by 1/16, as
 // in llap_reduce_px. A CTA makes a 32 x 16 tile of outputs for a group of
-// RPG planes (blockIdx.z): per plane it stages the 66 x 33 input texels once
-// (asynchronous 4 byte copies inside the image, mirrored single loads at its
-// border; the taps overshoot the input by at most one texel). Two plane
-// groups per tile keep the CTA at 26 KB and 32 registers: 8 CTAs per SM.
-constexpr int RT_X = 32, RT_Y = 16, RI_X = 2 * RT_X + 2, RI_Y = 2 * RT_Y + 1, RPG = (NPL + 1) / 2;
+// RPG planes (blockIdx.z): per plane it stages the input texels
+// [2 OX - 8, 2 OX + 64) x [2 OY - 1, 2 OY + 32) once (the outputs read
+// [2 OX - 1, 2 OX + 64); the box starts 16 bytes lower, where a TMA copy may
+// start). Where those texels lie inside the level, one thread stages the
+// whole box of all the group's planes with a TMA copy (cp.async.bulk.tensor on
+// a 3D tensor map over the level: x, y, plane), its completion counted on an
+// mbarrier; without a tensor map, asynchronous 4 byte copies. At the level's
+// border mirrored single loads (the taps overshoot the input by at most one
+// texel). Two plane groups per tile: 29 KB per CTA, 7 CTAs per SM.
+constexpr int RT_X = 32, RT_Y = 16, RB_X = 2 * RT_X + 8, RI_Y = 2 * RT_Y + 1, RPG = (NPL + 1) / 2;
+constexpr int RB_OFF = 6;                                        // slot of input column 2 OX - 2
+constexpr uint32_t RED_BOX_BYTES = RPG * RI_Y * RB_X * sizeof(__half);
+// bounded waits: polls of the copy's mbarrier before the CTA gives up (a completed copy takes
+// microseconds; this is seconds), and again for the copy to land before the CTA exits
+constexpr int TMA_WAIT_POLLS = 1 << 24;
 
-__global__ void __launch_bounds__(256, 8) k_llap_reduce(const __half *__restrict__ in, int iw, int ih, size_t ip,
-    __half *__restrict__ out, int ow, int oh, size_t op)
+DEV bool mbar_wait(uint32_t bar, int polls)
 {
-  __shared__ __align__(4) __half t[RPG][RI_Y][RI_X];   // the group's planes at once: every load in flight together
+  uint32_t done = 0;
+  for(int i = 0; i < polls && !done; i++)
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(done) : "r"(bar) : "memory");
+  return done != 0;
+}
+
+__global__ void __launch_bounds__(256, 7) k_llap_reduce(const __grid_constant__ CUtensorMap map, int use_map,
+    const __half *__restrict__ in, int iw, int ih, int ipitch, size_t ip,
+    __half *__restrict__ out, int ow, int oh, int opitch, size_t op, uint32_t *status)
+{
+  __shared__ __align__(128) __half t[RPG][RI_Y][RB_X];   // the group's planes at once: every load in flight together
+  __shared__ __align__(8) uint64_t bar;
   const int k0 = blockIdx.z * RPG, nk = min(RPG, NPL - k0);
-  in += k0 * ip;
-  out += k0 * op;
   const int OX = blockIdx.x * RT_X, OY = blockIdx.y * RT_Y;
-  const int gx0 = 2 * OX - 2, gy0 = 2 * OY - 1;     // input texel of t[.][0][0]
-  const bool inside = gx0 >= 0 && gy0 >= 0 && gx0 + RI_X <= iw && gy0 + RI_Y <= ih && !(iw & 1);
-  if(inside)
-  { // asynchronous copies: every word of the tile in flight at once
-    for(int i = threadIdx.x; i < RI_Y * (RI_X / 2); i += blockDim.x)
+  const int bx0 = 2 * OX - 8, gx0 = 2 * OX - 2, gy0 = 2 * OY - 1;   // box origin, first texel read
+  const bool inside = bx0 >= 0 && gy0 >= 0 && 2 * OX + RB_X - 8 <= iw && gy0 + RI_Y <= ih;
+  if(inside && use_map)
+  { // one TMA copy of the box (6 planes x 33 rows x 72 texels; planes past the last read as 0)
+    const uint32_t b = (uint32_t)__cvta_generic_to_shared(&bar), dst = (uint32_t)__cvta_generic_to_shared(&t[0][0][0]);
+    if(threadIdx.x == 0)
     {
-      const int r = i / (RI_X / 2), c = i % (RI_X / 2);
-      const size_t o = (size_t)(gy0 + r) * iw + gx0 + 2 * c;
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(b) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    }
+    __syncthreads();
+    if(threadIdx.x == 0)
+    {
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" :: "r"(b), "r"(RED_BOX_BYTES) : "memory");
+      asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n"
+                   :: "r"(dst), "l"(reinterpret_cast<uint64_t>(&map)), "r"(bx0), "r"(gy0), "r"(k0), "r"(b) : "memory");
+    }
+    if(!mbar_wait(b, TMA_WAIT_POLLS))
+    { // the copy did not complete: record it, give the copy a last bounded chance to land, leave
+      if(threadIdx.x == 0) atomicOr(status, 1u);
+      mbar_wait(b, TMA_WAIT_POLLS);
+      return;
+    }
+  }
+  else if(inside)
+  { // asynchronous 4 byte copies (even texel offsets: the row pitch is a multiple of 8 texels)
+    for(int i = threadIdx.x; i < RI_Y * (RB_X / 2 - 3); i += blockDim.x)
+    {
+      const int r = i / (RB_X / 2 - 3), c = i % (RB_X / 2 - 3);
+      const size_t o = (size_t)(gy0 + r) * ipitch + gx0 + 2 * c;
 #pragma unroll
       for(int k = 0; k < RPG; k++)
         if(k < nk)
         {
-          const unsigned dst = (unsigned)__cvta_generic_to_shared(&t[k][r][2 * c]);
-          asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" :: "r"(dst), "l"(in + k * ip + o) : "memory");
+          const unsigned dst = (unsigned)__cvta_generic_to_shared(&t[k][r][RB_OFF + 2 * c]);
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" :: "r"(dst), "l"(in + (k0 + k) * ip + o) : "memory");
         }
     }
     asm volatile("cp.async.wait_all;\n" ::: "memory");
   }
   else
-    for(int i = threadIdx.x; i < RI_Y * RI_X; i += blockDim.x)
+    for(int i = threadIdx.x; i < RI_Y * (RB_X - RB_OFF); i += blockDim.x)
     {
-      const int r = i / RI_X, c = i % RI_X;
-      const size_t o = (size_t)mirror1(gy0 + r, ih) * iw + mirror1(gx0 + c, iw);
+      const int r = i / (RB_X - RB_OFF), c = i % (RB_X - RB_OFF);
+      const size_t o = (size_t)mirror1(gy0 + r, ih) * ipitch + mirror1(gx0 + c, iw);
 #pragma unroll
       for(int k = 0; k < RPG; k++)
-        if(k < nk) t[k][r][c] = __ldg(in + k * ip + o);
+        if(k < nk) t[k][r][RB_OFF + c] = __ldg(in + (k0 + k) * ip + o);
     }
   __syncthreads();
   const int lx = threadIdx.x % RT_X, ly = threadIdx.x / RT_X;
@@ -157,12 +202,12 @@ __global__ void __launch_bounds__(256, 8) k_llap_reduce(const __half *__restrict
 #pragma unroll
       for(int b = 0; b < 3; b++)
       { // input rows 2 oy - 1 + b, columns 2 ox - 1 .. 2 ox + 1
-        const __half *row = &t[k][2 * (ly + 8 * h) + b][2 * lx + 1];
+        const __half *row = &t[k][2 * (ly + 8 * h) + b][RB_OFF + 2 * lx + 1];
         const float t0 = h2f(row[0]), t1 = h2f(row[1]), t2 = h2f(row[2]);
         P[b][0] = t0 + t1;
         P[b][1] = t1 + t2;
       }
-      out[k * op + (size_t)oy * ow + ox] =
+      out[(k0 + k) * op + (size_t)oy * opitch + ox] =
           f2h(((((P[0][0] + P[1][0]) + (P[0][1] + P[1][1])) + (P[1][0] + P[2][0])) + (P[1][1] + P[2][1])) * 0.0625f);
     }
   }
@@ -181,13 +226,13 @@ struct coarse_t
   float hc[2][FSY][NKX];          // hrow of c for even / odd outputs: [x parity][slot row][column - X0/2]
 };
 
-DEV void stage_coarse(coarse_t &sc, const __half *l1, int w1, int h1, size_t p1,
+DEV void stage_coarse(coarse_t &sc, const __half *l1, int w1, int h1, int pitch1, size_t p1,
     const __half *coarse, int bx, int by)
 { // the mirrored position once per slot, then the same texel of every plane
   for(int r = threadIdx.x; r < FSX * FSY; r += blockDim.x)
   {
     const int sx = r % FSX, sy = r / FSX;
-    const size_t o = (size_t)mirror1(by + sy, h1) * w1 + mirror1(bx + sx, w1);
+    const size_t o = (size_t)mirror1(by + sy, h1) * pitch1 + mirror1(bx + sx, w1);
     float h[NG];
 #pragma unroll
     for(int k = 0; k < NG; k++) h[k] = h2f(__ldg(l1 + k * p1 + o));
@@ -232,12 +277,12 @@ template<int PX, int PY> DEV void assemble_stored(const coarse_t &sl, const __ha
 }
 
 __global__ void __launch_bounds__(256) k_llap_assemble(const __half *__restrict__ coarse, int first,
-    const __half *__restrict__ l0, int w0, int h0, size_t p0,
-    const __half *__restrict__ l1, int w1, int h1, size_t p1, __half *__restrict__ out)
+    const __half *__restrict__ l0, int w0, int h0, int pitch0, size_t p0,
+    const __half *__restrict__ l1, int w1, int h1, int pitch1, size_t p1, __half *__restrict__ out)
 {
   __shared__ coarse_t sl;
   const int X0 = blockIdx.x * FTX, Y0 = blockIdx.y * FTY;
-  stage_coarse(sl, l1, w1, h1, p1, first ? l1 + NG * p1 : coarse, X0 / 2 - 2, Y0 / 2 - 2);
+  stage_coarse(sl, l1, w1, h1, pitch1, p1, first ? l1 + NG * p1 : coarse, X0 / 2 - 2, Y0 / 2 - 2);
   __syncthreads();
   for(int t = threadIdx.x; t < NKX * FTY; t += blockDim.x)
   { // the pair (x, x + 1) of row y; a warp takes one row
@@ -245,7 +290,7 @@ __global__ void __launch_bounds__(256) k_llap_assemble(const __half *__restrict_
     const int x = X0 + 2 * lx, y = Y0 + ry;
     if(x >= w0 || y >= h0) continue;
     const int sy = (ry >> 1) + 2;
-    const size_t o = (size_t)y * w0 + x;
+    const size_t o = (size_t)y * pitch0 + x;
     const bool two = x + 1 < w0;
     if(y & 1)
     {
@@ -331,7 +376,7 @@ __global__ void __launch_bounds__(256, 6) k_llap_final(const dev_llap_k3_t p)
 {
   __shared__ coarse_t sl;
   const int X0 = blockIdx.x * FTX, Y0 = blockIdx.y * FTY;
-  stage_coarse(sl, p.l1, p.l1w, p.l1h, p.l1plane, p.coarse, X0 / 2 - 2, Y0 / 2 - 2);
+  stage_coarse(sl, p.l1, p.l1w, p.l1h, p.l1pitch, p.l1plane, p.coarse, X0 / 2 - 2, Y0 / 2 - 2);
   __syncthreads();
   const float sig = p.ll_sigma;
   const float r2s = 1.0f / (2.0f * sig), rden = 1.0f / (2.0f * sig * sig / 3.0f);
@@ -391,19 +436,46 @@ cudaError_t init_llap()
   return e;
 }
 
-cudaError_t launch_llap_reduce(const __half *in, int iw, int ih, size_t iplane,
-    __half *out, int ow, int oh, size_t oplane, cudaStream_t s)
+// the 3D tensor map (x, y, plane) over a level's 11 planes that k_llap_reduce stages its
+// input boxes through; out of range texels and planes read 0 (the kernel uses none of them)
+cudaError_t llap_reduce_tensor_map(const llap_level_t &in, CUtensorMap *map)
 {
-  dim3 grid((ow + RT_X - 1) / RT_X, (oh + RT_Y - 1) / RT_Y, (NPL + RPG - 1) / RPG);
-  k_llap_reduce<<<grid, 256, 0, s>>>(in, iw, ih, iplane, out, ow, oh, oplane);
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if(!encode)
+  {
+    cudaDriverEntryPointQueryResult q;
+    void *fn = nullptr;
+    const cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+    if(e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn) return e != cudaSuccess ? e : cudaErrorNotSupported;
+    encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+  }
+  const cuuint64_t dim[3] = { (cuuint64_t)in.w, (cuuint64_t)in.h, (cuuint64_t)NPL };
+  const cuuint64_t stride[2] = { (cuuint64_t)in.pitch * sizeof(__half), (cuuint64_t)in.plane * sizeof(__half) };
+  const cuuint32_t box[3] = { (cuuint32_t)RB_X, (cuuint32_t)RI_Y, (cuuint32_t)RPG };
+  const cuuint32_t estride[3] = { 1, 1, 1 };
+  const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, (void *)in.p, dim, stride, box, estride,
+      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+cudaError_t launch_llap_reduce(const llap_level_t &in, const llap_level_t &out, const CUtensorMap *map,
+    uint32_t *status, cudaStream_t s)
+{
+  dim3 grid((out.w + RT_X - 1) / RT_X, (out.h + RT_Y - 1) / RT_Y, (NPL + RPG - 1) / RPG);
+  CUtensorMap none;
+  memset(&none, 0, sizeof(none));
+  k_llap_reduce<<<grid, 256, 0, s>>>(map ? *map : none, map ? 1 : 0, in.p, in.w, in.h, in.pitch, in.plane,
+                                     out.p, out.w, out.h, out.pitch, out.plane, status);
   return cudaGetLastError();
 }
 
-cudaError_t launch_llap_assemble(const __half *coarse, int first, const __half *l0, int w0, int h0, size_t p0,
-    const __half *l1, int w1, int h1, size_t p1, __half *out, cudaStream_t s)
+cudaError_t launch_llap_assemble(const __half *coarse, int first, const llap_level_t &l0, const llap_level_t &l1,
+    __half *out, cudaStream_t s)
 {
-  dim3 grid((w0 + FTX - 1) / FTX, (h0 + FTY - 1) / FTY);
-  k_llap_assemble<<<grid, 256, 0, s>>>(coarse, first, l0, w0, h0, p0, l1, w1, h1, p1, out);
+  dim3 grid((l0.w + FTX - 1) / FTX, (l0.h + FTY - 1) / FTY);
+  k_llap_assemble<<<grid, 256, 0, s>>>(coarse, first, l0.p, l0.w, l0.h, l0.pitch, l0.plane,
+                                       l1.p, l1.w, l1.h, l1.pitch, l1.plane, out);
   return cudaGetLastError();
 }
 

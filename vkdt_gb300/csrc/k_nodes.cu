@@ -663,7 +663,7 @@ template<bool FC> __global__ void __launch_bounds__(NT) k_post(const dev_image_t
       for(int k = 0; k < NPL; k++)
       { // level 0 slot of virtual x = 2ox + a - 1 is 2lx + a (llap_reduce_px)
         const __half *const row[3] = { &L0[k][2 * ly][2 * lx], &L0[k][2 * ly + 1][2 * lx], &L0[k][2 * ly + 2][2 * lx] };
-        p.l1[k * p.l1plane + (size_t)oy * p.l1w + ox] = f2h(llap_reduce_px(row));
+        p.l1[k * p.l1plane + (size_t)oy * p.l1pitch + ox] = f2h(llap_reduce_px(row));
       }
   }
   if(!FC && p.hist)

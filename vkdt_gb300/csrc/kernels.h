@@ -1,6 +1,7 @@
 // Launch interface between the host graph (graph.cpp) and the CUDA kernels.
 // Plain structs of pointers and scalars; no torch types.
 #pragma once
+#include <cuda.h>            // CUtensorMap
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
 #include <stdint.h>
@@ -52,6 +53,7 @@ struct dev_image_t
   half4 *rgbf;          // filmcurv output, crop_w*crop_h rgba f16
   __half *l1;           // llap level 1, 11 planes (null: the develop kernel ends at filmcurv)
   int l1w, l1h;
+  int l1pitch;          // elements per row (the width rounded up to 16 bytes)
   size_t l1plane;       // elements per plane
   uint32_t *hist;       // 257 counts or null
   // debug copies (null in production)
@@ -83,9 +85,9 @@ struct dev_llap_k3_t
   const half4 *rgbf;    // filmcurv output
   int W, H;
   const __half *l1;     // level 1 planes
-  int l1w, l1h;
+  int l1w, l1h, l1pitch;
   size_t l1plane;
-  const __half *coarse; // A[1] at level 1 size, or the grey plane of level 1 when the pyramid has 2 levels
+  const __half *coarse; // A[1] at level 1 size (row pitch l1pitch), or the grey plane of level 1 when the pyramid has 2 levels
   float ll_sigma, ll_shadows, ll_highlights, ll_clarity;
   // grade/main.comp after llap when the graph connects it (0 none, 1 classic, 2 zoned log):
   // lift, gamma, gain, offset with their fourth component added, sh_pivot, hi_pivot
@@ -235,11 +237,21 @@ cudaError_t launch_hilite_assemble(const half4 *fine, int fw, int fh, const half
 cudaError_t launch_develop(const dev_image_t &p, cudaStream_t s);
 cudaError_t init_develop();   // function attributes, once per device (outside stream capture)
 
-// llap pyramid (k_llap.cu)
-cudaError_t launch_llap_reduce(const __half *in, int iw, int ih, size_t iplane,
-    __half *out, int ow, int oh, size_t oplane, cudaStream_t s);
-cudaError_t launch_llap_assemble(const __half *coarse, int first, const __half *l0, int w0, int h0, size_t p0,
-    const __half *l1, int w1, int h1, size_t p1, __half *out, cudaStream_t s);
+// llap pyramid (k_llap.cu): a level is 11 f16 planes (NUM_GAMMA curves + grey) of w x h texels,
+// rows of `pitch` texels (a multiple of 8: 16 byte rows, as TMA copies want them), planes of
+// `plane` = pitch * h texels
+struct llap_level_t { __half *p; int w, h, pitch; size_t plane; };
+// the tensor map k_llap_reduce stages a level through (TMA); map lives in host memory and
+// travels as a kernel parameter
+cudaError_t llap_reduce_tensor_map(const llap_level_t &in, CUtensorMap *map);
+// map null: the kernel stages with 4 byte asynchronous copies. status (device memory, may be
+// null only with map null): bit 0 set when a TMA copy did not complete within its bounded wait
+cudaError_t launch_llap_reduce(const llap_level_t &in, const llap_level_t &out, const CUtensorMap *map,
+    uint32_t *status, cudaStream_t s);
+// assemble A[j] (out, at l0's size and pitch) from level l0, the coarse level l1 and A[j+1] (coarse,
+// at l1's size and pitch; first: the grey plane of l1 instead)
+cudaError_t launch_llap_assemble(const __half *coarse, int first, const llap_level_t &l0, const llap_level_t &l1,
+    __half *out, cudaStream_t s);
 cudaError_t launch_llap_final(const dev_llap_k3_t &p, cudaStream_t s);
 cudaError_t init_llap();      // function attributes, once per device (from init_develop)
 

@@ -189,10 +189,10 @@ def oracle_params(oracle, wd=None, ht=None):
     return p
 
 
-def oracle_sink(oracle, m, ip, p, double=False):
+def oracle_sink(oracle, m, ip, p, double=False, force=None):
     """the graph's output on the oracle: the llap output, graded with grade's defaults
-    (stored as f16) on the full darkroom graph"""
-    out = oracle.develop(m, ip, params=p, double=double, stages=("llap",))["llap"]
+    (stored as f16) on the full darkroom graph; force: decisions taken in place of its own"""
+    out = oracle.develop(m, ip, params=p, double=double, stages=("llap",), force=force)["llap"]
     if GRAPH == "darkroom":
         out = oracle.grade(out, *GRADE_DEFAULTS).astype(np.float16).astype(np.float32)
     return out
@@ -232,6 +232,11 @@ def cpu_leg(args):
         de = delta_e2000(out, ref)
         return {"max": float(e.max()), "mean": float(e.mean()), "px_over_2e-3": int((e > 2e-3).sum()),
                 "de2000_max": float(de.max()), "px_de_over_0.5": int((de >= 0.5).sum())}
+    dec = {}
+    for kind in oracle.DECISION_KINDS:
+        f = os.path.join(args.cpu_leg, "dec_%s.npy" % kind)
+        if os.path.exists(f):
+            dec[kind] = np.load(f)
     res["err"] = {"stage": "the graph's output (%s), rgb, |a-b|/max(1,|b|)" % ("grade" if GRAPH == "darkroom" else "llap"),
                   "window": "full %dx%d" % (out.shape[1], out.shape[0]),
                   "vs_oracle_fp32": err(oracle_sink(oracle, m, ip, p)),
@@ -239,6 +244,10 @@ def cpu_leg(args):
                   "tolerance": {"max": 2e-3, "mean": 1e-4, "de2000": 0.5,
                                 "note": "pixels over 2e-3 are where a branch of the reference was a near tie "
                                         "(tests/parity.py shows each such decision explained)"}}
+    if dec:
+        own = oracle.develop(m, ip, params=p, stages=("llap",), record=True)
+        res["err"]["decisions_differing"] = {k: int((dec[k] != own["dec_" + k]).sum()) for k in dec}
+        res["err"]["vs_oracle_fp32_same_decisions"] = err(oracle_sink(oracle, m, ip, p, force=dec))
     if not args.no_cpu:
         run = lambda: oracle_sink(oracle, m, ip, p)
         run()
@@ -1035,9 +1044,34 @@ def main():
         g0.source()[...] = host_in[0]
         out = g0.run(flags=v.RUN_UPLOAD_SOURCE | v.RUN_DOWNLOAD_SINK | v.RUN_WAIT_DONE, stream=sp)
         host_m = np.array(host_in[0], copy=True)
+        # the discrete decisions this image's develop took (a graph with the debug stages, whose
+        # results equal the plain graph's): the error against the oracle is also reported with the
+        # oracle taking the same decisions, which isolates the arithmetic from near-tie branches
+        dec = {}
+        gd = v.Graph(graph_cfg(v))
+        try:
+            gd.set_input(WD, HT, img_param(v, WD, HT))
+            if LEVELS:
+                gd.set_llap_levels(LEVELS)
+            if DENOISE > 0:
+                gd.set_param("denoise", "strength", DENOISE)
+            if DEMOSAIC:
+                gd.set_param("demosaic", "method", np.int32(DEMOSAIC))
+            gd.set_debug(True)
+            gd.alloc()
+            gd.run(host_m)
+            for kind in ("gauss", "dn_cov", "dn_thr"):
+                try:
+                    dec[kind] = gd.debug_decisions(kind)
+                except v._lib.VkdtError:
+                    pass
+        finally:
+            gd.close()
         with tempfile.TemporaryDirectory() as td:
             np.save(os.path.join(td, "mosaic.npy"), host_m)
             np.save(os.path.join(td, "out.npy"), np.asarray(out))
+            for kind, d in dec.items():
+                np.save(os.path.join(td, "dec_%s.npy" % kind), d)
             cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--cpu-leg", td, "--size", "%dx%d" % (WD, HT),
                    "--graph", GRAPH,
                    "--levels", str(LEVELS), "--denoise", str(DENOISE), "--cfa", "xtrans" if FILTERS == 9 else "rggb",

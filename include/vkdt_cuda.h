@@ -223,9 +223,10 @@ int  vkdt_cuda_graph_develop_static(vkdt_cuda_graph_t *graph, const void *d_mosa
 int  vkdt_cuda_graph_set_timing(vkdt_cuda_graph_t *graph, int enable);
 int  vkdt_cuda_graph_query_times(vkdt_cuda_graph_t *graph, float *ms, dt_token_t *names, dt_token_t *kernels, int max);
 
-/* replay the launch sequence of a run as a captured CUDA graph (default 1).
- * 0 launches it eagerly every run: no re-capture after the image metadata
- * changes, for graphs that develop a different image each run. */
+/* replay the launch sequence of a run as a captured CUDA graph (default 1):
+ * captured on the first run, replayed while buffers and per-image values
+ * stay the same, and updated in place (cudaGraphExecUpdate) after either
+ * changes. 0 launches it eagerly every run. */
 int  vkdt_cuda_graph_set_capture(vkdt_cuda_graph_t *graph, int enable);
 /* the graph's own stream (a cudaStream_t), valid after alloc */
 void *vkdt_cuda_graph_stream(vkdt_cuda_graph_t *graph);

@@ -135,6 +135,20 @@ def test_unsupported_chains_return_incomplete():
         with pytest.raises(v._lib.VkdtError) as e:
             g.set_nodes(wd, ht, nodes)
         assert e.value.code == v._lib.INCOMPLETE
+    # a DNG gain map on the denoise node (denoise/main.c:172-196: the noop push constant after the
+    # CFA filters, the doub push constant after the noise profile): not built
+    for name, node, at in (("darkroom_2048x1536", "noop", 17), ("wavelet_1000x742", "doub", 19)):
+        c = CASES[name]
+        nodes = [dict(n) for n in c["nodes"]]
+        for n in nodes:
+            if n["name"] == "denoise" and n["kernel"] == node:
+                u = bytearray(n["push"])
+                u[4 * at:4 * at + 4] = np.int32(1).tobytes()
+                n["push"] = bytes(u)
+        with v.Graph(None) as g:
+            with pytest.raises(v._lib.VkdtError) as e:
+                g.set_nodes(c["in"][0], c["in"][1], nodes)
+            assert e.value.code == v._lib.INCOMPLETE and "gain map" in str(e.value)
     # a node the library does not compute (an extra llap level)
     nodes = [dict(n) for n in case["nodes"]] + [dict(case["nodes"][-1], kernel="reduce", wd=2, ht=1, dp=11)]
     with v.Graph(None) as g:

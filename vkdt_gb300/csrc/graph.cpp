@@ -231,8 +231,11 @@ struct vkdt_cuda_graph_t
   size_t src_bytes = 0, sink_bytes = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
-  // k_llap_reduce's tensor maps (input level l-1 of reduce launch l), made for the arena tm_arena
+  // tensor maps made for the arena tm_arena: k_llap_reduce's (input level l-1 of reduce launch l)
+  // and k_develop's over the source mosaic and over the denoised mosaic
   std::vector<CUtensorMap> tm_reduce;
+  CUtensorMap tm_src, tm_dn;
+  bool tm_src_ok = false, tm_dn_ok = false;
   unsigned char *tm_arena = nullptr;
   std::vector<vkdt_cuda_node_info_t> nodes;
   // launch list (fused kernels) and timing
@@ -242,6 +245,8 @@ struct vkdt_cuda_graph_t
   std::vector<float> times;
   cudaGraphExec_t gexec = nullptr;
   bool graph_dirty = true;
+  const void *gsrc = nullptr;     // the buffers the captured launch sequence reads and writes
+  void *gdst = nullptr;
   const void *ext_src = nullptr;  // device buffers bound for the current run
   void *ext_dst = nullptr;
 
@@ -860,6 +865,13 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
         g->at<half4>(g->hb[l].off), white, soft, s));
     if((r = mark())) return r;
   }
+  // the develop kernel's tensor map: the buffer d.mosaic points at, where one was made for it
+  const CUtensorMap *dmap = nullptr;
+  if(g->tm_arena == g->arena)
+  {
+    if(d.codes.identity && g->tm_dn_ok && (const void *)d.mosaic == (const void *)(g->arena + g->off_dn)) dmap = &g->tm_dn;
+    else if(!d.codes.identity && g->tm_src_ok && (const void *)d.mosaic == (const void *)(g->arena + g->off_src)) dmap = &g->tm_src;
+  }
   if(g->unfused)
   { // 4'. hilite level 0 assemble, doub, demosaic, colour .. first llap reduce
     if(g->k1front)
@@ -919,7 +931,7 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
   { // 4. fused develop pass to filmcurv on the crop window, then llap curve + first reduce on it
     dev_image_t dc = d;
     dc.l1 = nullptr;
-    CU(launch_develop(dc, s));
+    CU(launch_develop(dc, dmap, dmap ? device_status() : nullptr, s));
     if((r = mark())) return r;
     dev_image_t dp = d;
     dp.W = g->out_w; dp.H = g->out_h;
@@ -928,7 +940,7 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
   }
   else
   { // 4. fused develop pass
-    CU(launch_develop(d, s));
+    CU(launch_develop(d, dmap, dmap ? device_status() : nullptr, s));
     if((r = mark())) return r;
   }
   // 5. llap reduce levels 2..nl-1 (TMA staged through the tensor maps made for this arena)
@@ -1059,6 +1071,7 @@ static void release(vkdt_cuda_graph_t *g)
   if(g->arena) cudaFree(g->arena);
   g->arena = nullptr;
   g->tm_reduce.clear();
+  g->tm_src_ok = g->tm_dn_ok = false;
   g->tm_arena = nullptr;
   if(g->h_src) cudaFreeHost(g->h_src);
   if(g->h_sink) cudaFreeHost(g->h_sink);
@@ -1512,6 +1525,11 @@ int vkdt_cuda_graph_alloc(vkdt_cuda_graph_t *g, uint64_t *device_bytes)
     bool ok = device_status() != nullptr;
     for(size_t l = 1; l < g->lp.size() && ok; l++) ok = llap_reduce_tensor_map(llap_level(g, g->lp[l - 1]), &maps[l - 1]) == cudaSuccess;
     if(ok) { g->tm_reduce = maps; g->tm_arena = g->arena; }
+    // the develop kernel's mosaic windows: the source (16 byte aligned crop origin) or the denoised mosaic
+    g->tm_src_ok = ok && !(g->ip.crop_aabb[0] & 7)
+                && develop_tensor_map(g->arena + g->off_src, g->in_wd, g->in_ht, g->in_wd, &g->tm_src) == cudaSuccess;
+    g->tm_dn_ok = ok && g->wavelet
+               && develop_tensor_map(g->arena + g->off_dn, g->W, g->H, g->W, &g->tm_dn) == cudaSuccess;
   }
   if(g->wavelet && (!g->unfused || g->k1front))
   {
@@ -1755,26 +1773,38 @@ int vkdt_cuda_graph_device_buffers(vkdt_cuda_graph_t *g, void **d_source, void *
   return 0;
 }
 
+// The launch sequence runs as a CUDA graph: captured once and replayed while nothing changes.
+// New buffers or per-image values (another image of the same shape: white balance, black and
+// white, noise) capture the sequence again and update the executable graph in place (its
+// topology is the plan's, so only kernel parameters change); a graph that cannot be updated
+// is instantiated anew.
 static int run_kernels(vkdt_cuda_graph_t *g, cudaStream_t s, const void *src, void *dst)
 {
   if(plan_key(g) != g->planned_for)
     return fail(VKDT_CUDA_INCOMPLETE, "sizes or node-changing parameters differ from the last vkdt_cuda_graph_alloc: allocate again");
-  const bool own_buffers = src == g->arena + g->off_src && dst == g->arena + g->off_out;
-  if(g->timing || !g->use_graph || !own_buffers) return enqueue(g, s, src, dst, g->timing);
-  if(g->graph_dirty || !g->gexec)
+  if(g->timing || !g->use_graph) return enqueue(g, s, src, dst, g->timing);
+  if(g->graph_dirty || !g->gexec || src != g->gsrc || dst != g->gdst)
   {
-    if(g->gexec) { cudaGraphExecDestroy(g->gexec); g->gexec = nullptr; }
-    cudaGraph_t graph;
     CU(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     const int r = enqueue(g, s, src, dst, false);
     cudaGraph_t cap = nullptr;
     const cudaError_t e = cudaStreamEndCapture(s, &cap);
     if(r) { if(cap) cudaGraphDestroy(cap); return r; }
     CU(e);
-    graph = cap;
-    cudaError_t ie = cudaGraphInstantiate(&g->gexec, graph, 0);
-    cudaGraphDestroy(graph);
+    if(g->gexec)
+    {
+      cudaGraphExecUpdateResultInfo info;
+      if(cudaGraphExecUpdate(g->gexec, cap, &info) != cudaSuccess)
+      {
+        (void)cudaGetLastError();
+        cudaGraphExecDestroy(g->gexec);
+        g->gexec = nullptr;
+      }
+    }
+    cudaError_t ie = g->gexec ? cudaSuccess : cudaGraphInstantiate(&g->gexec, cap, 0);
+    cudaGraphDestroy(cap);
     CU(ie);
+    g->gsrc = src; g->gdst = dst;
     g->graph_dirty = false;
   }
   CU(cudaGraphLaunch(g->gexec, s));

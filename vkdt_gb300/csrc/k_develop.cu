@@ -16,6 +16,12 @@
 // these (an odd shift moves them off the CFA blocks): with a crop the kernel
 // ends at filmcurv and the llap curve and first reduce run on its output.
 //
+// Staging: an interior tile's mosaic window (48 x 40 codes from 16 bytes left
+// of its 4 pixel halo) arrives by one TMA copy (cp.async.bulk.tensor on a 2D
+// tensor map over the mosaic, completion on an mbarrier) while the CTA loads
+// the hilite coarse level; border tiles and mosaics the map cannot describe
+// read the codes with plain loads.
+//
 // Tiling: one CTA computes a TX x TY tile of output pixels. Every stage is
 // evaluated on the halo its consumer needs (slots indexed by "virtual"
 // positions that hold the value of the mirrored real position, which is what
@@ -41,6 +47,8 @@
 #include "develop_px.cuh"
 #include "gauss.cuh"
 
+#include <cstring>
+
 namespace {
 
 constexpr int TX = 32, TY = 32;
@@ -55,10 +63,15 @@ constexpr int LH = (LX + 1) / 2;
 constexpr int BX = TX / 4 + 6;       // hilite coarse level slots
 constexpr int NPL = 11;              // NUM_GAMMA curves + grey (llap/config.h:2)
 
+constexpr int RAW_X = MX + 8, RAW_Y = MX;   // TMA box of mosaic codes: [X0-8, X0+TX+8) x [Y0-4, Y0+TY+4)
+constexpr uint32_t RAW_BYTES = RAW_X * RAW_Y * sizeof(uint16_t);
 struct early_t
 {
   float sw[3][CX][CX];         // splat weights, same taps as fw
   float B1[3][BX][BX];         // hilite coarse level (rgb) around the tile
+  // the mosaic codes of the tile's window (interior tiles with a tensor map), 128 byte aligned
+  // inside this array (the dynamic shared memory base is only known to be 16 byte aligned)
+  uint16_t raw[RAW_Y * RAW_X + 64];
 };
 struct smem_t
 {
@@ -67,6 +80,7 @@ struct smem_t
   __half g[GX][2][GH];         // splat output (f16 values), [y][x&1][x>>1]
   float rg[GX][2][GH];         // 1 / (1e-4 + splat output)
   uint32_t hist[257];
+  uint64_t bar;                // completion of the mosaic window's TMA copy
   union
   { // the llap level 0 planes are written after the last reads of the others
     early_t e;
@@ -202,7 +216,19 @@ template<bool INTERIOR> DEV void tile_of(const tiles_t &t, int &bx, int &by)
   bx = k < left ? k : t.ix1 + 1 + (k - left);
 }
 
-template<bool INTERIOR, bool L1> __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p, const tiles_t tiles)
+// bounded wait on an mbarrier's phase 0 (polls; a completed copy takes microseconds, this is seconds)
+constexpr int TMA_WAIT_POLLS = 1 << 24;
+DEV bool mbar_wait(uint32_t bar, int polls)
+{
+  uint32_t done = 0;
+  for(int i = 0; i < polls && !done; i++)
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(done) : "r"(bar) : "memory");
+  return done != 0;
+}
+
+template<bool INTERIOR, bool L1> __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p, const tiles_t tiles,
+    const __grid_constant__ CUtensorMap mmap, int use_map, uint32_t *status)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   smem_t &s = *reinterpret_cast<smem_t *>(smem_raw);
@@ -218,6 +244,22 @@ template<bool INTERIOR, bool L1> __global__ void __launch_bounds__(NT) k_develop
   // no position of the tile's stages is mirrored or wrapped (even origin, 4 pixel margin)
   constexpr bool interior = INTERIOR;
   if(p.hist) for(int i = tid; i < 257; i += NT) s.hist[i] = 0;
+  // the mosaic window by TMA (interior tiles): [X0-8, X0+TX+8) x [Y0-4, Y0+TY+4) of the codes,
+  // the first column 16 byte aligned (the host gives a map only where cx and the pitch allow it)
+  const uint32_t raw_addr = ((uint32_t)__cvta_generic_to_shared(s.u.e.raw) + 127u) & ~127u;
+  const uint16_t *raw = s.u.e.raw + (raw_addr - (uint32_t)__cvta_generic_to_shared(s.u.e.raw)) / 2;
+  const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&s.bar);
+  const bool tma = interior && use_map;
+  if(tma && tid == 0)
+  {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" :: "r"(bar), "r"(RAW_BYTES) : "memory");
+    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n"
+                 :: "r"(raw_addr), "l"(reinterpret_cast<uint64_t>(&mmap)), "r"(X0 - 8 + p.cx), "r"(Y0 - 4 + p.cy), "r"(bar)
+                 : "memory");
+  }
 
   // ---- the hilite coarse level around the tile (virtual slots, mirrored)
   const int bx0 = ((X0 / 2 - 2) >> 1) - 2, by0 = ((Y0 / 2 - 2) >> 1) - 2;
@@ -229,7 +271,13 @@ template<bool INTERIOR, bool L1> __global__ void __launch_bounds__(NT) k_develop
     ld_half4(p.hl_coarse + (size_t)gy * p.hcw + gx, a, b, c, d);
     s.u.e.B1[0][sy][sx] = a; s.u.e.B1[1][sy][sx] = b; s.u.e.B1[2][sy][sx] = c;
   }
-  __syncthreads();
+  __syncthreads();   // (also orders the barrier's initialisation before the waits below)
+  if(tma && !mbar_wait(bar, TMA_WAIT_POLLS))
+  { // the copy did not complete: record it, give it a last bounded chance to land, leave
+    if(tid == 0) atomicOr(status, 1u);
+    mbar_wait(bar, TMA_WAIT_POLLS);
+    return;
+  }
 
   // ---- hilite output mosaic on virtual blocks [X0/2-2, X0/2+TX/2+2):
   // denoise/noop (lut), hilite/half, level 0 hilite/assemble, hilite/doub
@@ -241,9 +289,18 @@ template<bool INTERIOR, bool L1> __global__ void __launch_bounds__(NT) k_develop
       const int vbx = hx0 + sbx, vby = hy0 + sby;
       const int rbx = mirror1(vbx, hw), rby = mirror1(vby, hh);
       const bool fx = vbx < 0 || vbx >= hw, fy = vby < 0 || vby >= hh;
-      const size_t row = (size_t)(2 * rby + p.cy) * p.pitch + 2 * rbx + p.cx;
-      const uint32_t r0 = __ldg(reinterpret_cast<const uint32_t *>(p.mosaic + row));
-      const uint32_t r1 = __ldg(reinterpret_cast<const uint32_t *>(p.mosaic + row + p.pitch));
+      uint32_t r0, r1;
+      if(tma)
+      { // window column of pixel 2 rbx = X0 - 4 + 2 sbx is 2 sbx + 4, row 2 sby
+        r0 = *reinterpret_cast<const uint32_t *>(raw + (2 * sby) * RAW_X + 2 * sbx + 4);
+        r1 = *reinterpret_cast<const uint32_t *>(raw + (2 * sby + 1) * RAW_X + 2 * sbx + 4);
+      }
+      else
+      {
+        const size_t row = (size_t)(2 * rby + p.cy) * p.pitch + 2 * rbx + p.cx;
+        r0 = __ldg(reinterpret_cast<const uint32_t *>(p.mosaic + row));
+        r1 = __ldg(reinterpret_cast<const uint32_t *>(p.mosaic + row + p.pitch));
+      }
       float m[4];
       m[0] = h2f(__ldg(p.noop_lut + (r0 & 0xffff)));
       m[1] = h2f(__ldg(p.noop_lut + (r0 >> 16)));
@@ -516,14 +573,34 @@ cudaError_t init_develop()
   return e;
 }
 
-template<bool L1> static void launch_tiles(const dev_image_t &p, const tiles_t &t, int nin, cudaStream_t s)
+template<bool L1> static void launch_tiles(const dev_image_t &p, const tiles_t &t, int nin, const CUtensorMap *map,
+    uint32_t *status, cudaStream_t s)
 {
   const size_t bytes = L1 ? sizeof(smem_t) : SMEM_NO_L1;
-  if(nin > 0) k_develop<true, L1><<<dim3(t.ix1 - t.ix0 + 1, t.iy1 - t.iy0 + 1), NT, bytes, s>>>(p, t);
-  k_develop<false, L1><<<t.nx * t.ny - nin, NT, bytes, s>>>(p, t);
+  CUtensorMap none;
+  memset(&none, 0, sizeof(none));
+  if(nin > 0) k_develop<true, L1><<<dim3(t.ix1 - t.ix0 + 1, t.iy1 - t.iy0 + 1), NT, bytes, s>>>(p, t, map ? *map : none, map ? 1 : 0, status);
+  k_develop<false, L1><<<t.nx * t.ny - nin, NT, bytes, s>>>(p, t, none, 0, status);
 }
 
-cudaError_t launch_develop(const dev_image_t &p, cudaStream_t s)
+// the 2D tensor map over a mosaic of u16 codes (or the f16 bits of the denoised mosaic) that
+// interior tiles stage their window through: base 16 byte aligned, pitch a multiple of 8 codes
+cudaError_t develop_tensor_map(const void *mosaic, int wd, int ht, int pitch, CUtensorMap *map)
+{
+  if(((uintptr_t)mosaic & 15) || (pitch & 7)) return cudaErrorInvalidValue;
+  PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+  if(!encode) return cudaErrorNotSupported;
+  const cuuint64_t dim[2] = { (cuuint64_t)wd, (cuuint64_t)ht };
+  const cuuint64_t stride[1] = { (cuuint64_t)pitch * sizeof(uint16_t) };
+  const cuuint32_t box[2] = { (cuuint32_t)RAW_X, (cuuint32_t)RAW_Y };
+  const cuuint32_t estride[2] = { 1, 1 };
+  const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, const_cast<void *>(mosaic), dim, stride, box, estride,
+      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+cudaError_t launch_develop(const dev_image_t &p, const CUtensorMap *map, uint32_t *status, cudaStream_t s)
 {
   tiles_t t;
   t.nx = (p.W + TX - 1) / TX; t.ny = (p.H + TY - 1) / TY;
@@ -536,7 +613,7 @@ cudaError_t launch_develop(const dev_image_t &p, cudaStream_t s)
   }
   const int nin = t.ix1 < t.ix0 ? 0 : (t.ix1 - t.ix0 + 1) * (t.iy1 - t.iy0 + 1);
   // p.l1 null: end at filmcurv (a crop follows demosaic; the llap level 1 is made from rgbf)
-  if(p.l1) launch_tiles<true>(p, t, nin, s);
-  else launch_tiles<false>(p, t, nin, s);
+  if(p.l1) launch_tiles<true>(p, t, nin, map, status, s);
+  else launch_tiles<false>(p, t, nin, map, status, s);
   return cudaGetLastError();
 }

@@ -335,7 +335,8 @@ DEV void grade_px(const dev_llap_k3_t &p, float rgb[3])
   {
     float v = gain[k] * rgb[k];
     v = v * (1.0f - lift[k]) + lift[k];
-    v = powf(fmaxf(v, 0.0f), 1.0f / gamma[k]);
+    // pow(x, 1) is x: the default gamma (and the mid zone's weight 0) costs no pow
+    v = gamma[k] == 1.0f ? fmaxf(v, 0.0f) : powf(fmaxf(v, 0.0f), 1.0f / gamma[k]);
     rgb[k] = v + p.gr_off[k];
   }
 }
@@ -438,7 +439,8 @@ cudaError_t init_llap()
 
 // the 3D tensor map (x, y, plane) over a level's 11 planes that k_llap_reduce stages its
 // input boxes through; out of range texels and planes read 0 (the kernel uses none of them)
-cudaError_t llap_reduce_tensor_map(const llap_level_t &in, CUtensorMap *map)
+// the driver's cuTensorMapEncodeTiled, looked up once through the runtime (no link to libcuda)
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 {
   static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
   if(!encode)
@@ -446,9 +448,15 @@ cudaError_t llap_reduce_tensor_map(const llap_level_t &in, CUtensorMap *map)
     cudaDriverEntryPointQueryResult q;
     void *fn = nullptr;
     const cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
-    if(e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn) return e != cudaSuccess ? e : cudaErrorNotSupported;
-    encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    if(e == cudaSuccess && q == cudaDriverEntryPointSuccess && fn) encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
   }
+  return encode;
+}
+
+cudaError_t llap_reduce_tensor_map(const llap_level_t &in, CUtensorMap *map)
+{
+  PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+  if(!encode) return cudaErrorNotSupported;
   const cuuint64_t dim[3] = { (cuuint64_t)in.w, (cuuint64_t)in.h, (cuuint64_t)NPL };
   const cuuint64_t stride[2] = { (cuuint64_t)in.pitch * sizeof(__half), (cuuint64_t)in.plane * sizeof(__half) };
   const cuuint32_t box[3] = { (cuuint32_t)RB_X, (cuuint32_t)RI_Y, (cuuint32_t)RPG };

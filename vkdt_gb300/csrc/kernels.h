@@ -2,6 +2,7 @@
 // Plain structs of pointers and scalars; no torch types.
 #pragma once
 #include <cuda.h>            // CUtensorMap
+#include <cudaTypedefs.h>    // PFN_cuTensorMapEncodeTiled
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
 #include <stdint.h>
@@ -234,7 +235,12 @@ cudaError_t launch_hilite_assemble(const half4 *fine, int fw, int fh, const half
     half4 *out, float white, float soft, cudaStream_t s);
 
 // develop: hilite doub + demosaic + colour + filmcurv + llap curve + level 1 reduce (k_develop.cu)
-cudaError_t launch_develop(const dev_image_t &p, cudaStream_t s);
+// map: the tensor map of develop_tensor_map over p.mosaic (interior tiles stage their window by
+// TMA), or null (plain loads). status: as launch_llap_reduce's (may be null with map null)
+cudaError_t launch_develop(const dev_image_t &p, const CUtensorMap *map, uint32_t *status, cudaStream_t s);
+cudaError_t develop_tensor_map(const void *mosaic, int wd, int ht, int pitch, CUtensorMap *map);
+// the driver's cuTensorMapEncodeTiled (null where the driver has none)
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder();
 cudaError_t init_develop();   // function attributes, once per device (outside stream capture)
 
 // llap pyramid (k_llap.cu): a level is 11 f16 planes (NUM_GAMMA curves + grey) of w x h texels,

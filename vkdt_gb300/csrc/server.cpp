@@ -126,8 +126,8 @@ struct vkdt_cuda_server_t
       release(lru);
     }
     uint64_t got = 0;
-    rc = vkdt_cuda_graph_set_capture(g, 0);      // a different image every run: launch eagerly
-    if(!rc) rc = vkdt_cuda_graph_alloc(g, &got);
+    // every job replays the graph's captured launch sequence, updated in place for its buffers and metadata
+    rc = vkdt_cuda_graph_alloc(g, &got);
     pooled_t p;
     if(!rc) rc = vkdt_cuda_graph_device_buffers(g, &p.d_src, &p.d_dst);
     if(!rc && cudaEventCreateWithFlags(&p.done, cudaEventDisableTiming) != cudaSuccess) rc = VKDT_CUDA_ERROR_UNKNOWN;

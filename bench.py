@@ -57,7 +57,7 @@ GRADE_DEFAULTS = ((0, 0, 0, 0), (1, 1, 1, 0), (1, 1, 1, 0), (0, 0, 0, 0), 0, 0.3
 CAM_TO_REC2020 = (1.20, -0.15, -0.05, -0.10, 1.25, -0.15, 0.02, -0.22, 1.20)
 # the sources of the fused develop kernel: the DRAM traffic of an ncu capture is reported only
 # while they are the ones that capture measured (profiles/traffic.json holds their hash)
-K_DEVELOP_SOURCES = ["k_develop.cu", "common.cuh", "hilite.cuh", "pixel.cuh", "develop_px.cuh", "kernels.h"]
+K_DEVELOP_SOURCES = ["k_develop.cu", "common.cuh", "hilite.cuh", "pixel.cuh", "develop_px.cuh", "gauss.cuh", "kernels.h"]
 
 
 def source_hash(files):
@@ -488,8 +488,10 @@ def _replay(v, s, trace, pool, outs):
 
 
 def workload_serve(args, v, torch, sp, clk):
-    """Poisson arrivals at 200 requests/s: 70% full size, 30% 1/8 thumbnails, admission capped at 120 GB."""
-    trace = _request_trace(args.duration, 200.0, 3)
+    """Poisson arrivals (200 requests/s, the configuration's rate, or --rate): 70% full size, 30% 1/8
+    thumbnails, admission capped at 120 GB. Above one GPU's capacity (about 1 000/s) both forms fall
+    behind and their MP/s is what they develop, not the offered rate."""
+    trace = _request_trace(args.duration, args.rate, 3)
     pool = {}
     for i, (wd, ht) in enumerate(MIX_SIZES):
         # two resident mosaics per size, each with its own noise and white balance
@@ -524,8 +526,9 @@ def workload_serve(args, v, torch, sp, clk):
                      "failed": st["failed"], "p50_ms": st["latency_p50_ms"], "p99_ms": st["latency_p99_ms"],
                      "peak_device_bytes": st["peak_device_bytes"], "slots": slots}
         s.close()
-    return {"workload": "served request stream: Poisson arrivals 200/s for %g s (%d requests), 70%% full size "
-                        "(sizes of the mixed batch), 30%% 1/8 thumbnails, HBM admission cap 120 GB" % (args.duration, len(trace)),
+    return {"workload": "served request stream: Poisson arrivals %g/s for %g s (%d requests), 70%% full size "
+                        "(sizes of the mixed batch), 30%% 1/8 thumbnails, HBM admission cap 120 GB"
+                        % (args.rate, args.duration, len(trace)),
             "requests": len(trace), "offered_mpix_per_s": mp / args.duration}, \
         res["served"]["value"], res["served"]["wall_s"] * 1e3, {
             "per_image": res["per_image"], "served": res["served"],
@@ -787,6 +790,7 @@ def main():
                          "ingest: device unpack/decode of packed raw video frames")
     ap.add_argument("--images", type=int, default=64, help="batch: mosaics in the batch")
     ap.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
+    ap.add_argument("--rate", type=float, default=200.0, help="serve: requests per second (Poisson)")
     ap.add_argument("--slots", type=int, default=4, help="serve/video: jobs in flight")
     ap.add_argument("--cfa", default="rggb", choices=("rggb", "xtrans"), help="single: the mosaic's colour filter array")
     ap.add_argument("--graph", default=GRAPH, choices=("darkroom", "chain"),

@@ -84,7 +84,11 @@ struct smem_t
   union
   { // the llap level 0 planes are written after the last reads of the others
     early_t e;
-    __half L0[NPL][LX][LX + 1]; // llap level 0 planes, [y][slot] (rows of an even length)
+    struct
+    {
+      __half2 p[LLAP_PAIRS][LX][2][LH]; // the curve planes in pairs, [y][x & 1][x >> 1]
+      __half g[LX][LX + 1];             // the grey plane, [y][slot] (rows of an even length)
+    } L0;
   } u;
 };
 // without the llap level 0 planes (the kernel ends at filmcurv)
@@ -227,7 +231,12 @@ DEV bool mbar_wait(uint32_t bar, int polls)
   return done != 0;
 }
 
-template<bool INTERIOR, bool L1> __global__ void __launch_bounds__(NT) k_develop(const dev_image_t p, const tiles_t tiles,
+// CTAs per SM the register budget is cut for: 5 with the llap planes (their shared memory allows
+// no more), VKDT_DEVELOP_CTAS_NO_L1 without them (shared memory allows 7)
+#ifndef VKDT_DEVELOP_CTAS_NO_L1
+#define VKDT_DEVELOP_CTAS_NO_L1 6
+#endif
+template<bool INTERIOR, bool L1> __global__ void __launch_bounds__(NT, L1 ? 5 : VKDT_DEVELOP_CTAS_NO_L1) k_develop(const dev_image_t p, const tiles_t tiles,
     const __grid_constant__ CUtensorMap mmap, int use_map, uint32_t *status)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -516,35 +525,53 @@ template<bool INTERIOR, bool L1> __global__ void __launch_bounds__(NT) k_develop
       const float yv = lum2020(gclamp(fc[0], -1000.0f, 1000.0f), gclamp(fc[1], -1000.0f, 1000.0f), gclamp(fc[2], -1000.0f, 1000.0f));
       if(unit_curve)
       {
+        const float2 X = make_float2(yv, yv), nr = make_float2(-rden, -rden), cl = make_float2(cla, cla);
 #pragma unroll
-        for(int k = 0; k < NPL - 1; k++)
-          s.u.L0[k][sly][slx] = f2h(llap_curve_unit(yv, kLlapGamma[k], rden, cla));
+        for(int j = 0; j < LLAP_PAIRS; j++) s.u.L0.p[j][sly][slx & 1][slx >> 1] = llap_curve_unit2(X, j, nr, cl);
       }
       else
       {
 #pragma unroll
-        for(int k = 0; k < NPL - 1; k++)
-          s.u.L0[k][sly][slx] = f2h(llap_curve_rcp(yv, kLlapGamma[k], sig, r2s, rden, shd, hil, cla));
+        for(int j = 0; j < LLAP_PAIRS; j++)
+          s.u.L0.p[j][sly][slx & 1][slx >> 1] = __floats2half2_rn(
+              llap_curve_rcp(yv, kLlapGamma[2 * j], sig, r2s, rden, shd, hil, cla),
+              llap_curve_rcp(yv, kLlapGamma[2 * j + 1], sig, r2s, rden, shd, hil, cla));
       }
-      s.u.L0[NPL - 1][sly][slx] = f2h(yv);
+      s.u.L0.g[sly][slx] = f2h(yv);
     }
   }
   __syncthreads();
 
-  // ---- llap/reduce.comp (sample_semisoft) for level 1 outputs [X0/2, X0/2+TX/2) (llap_reduce_px)
+  // ---- llap/reduce.comp (sample_semisoft) for level 1 outputs [X0/2, X0/2+TX/2) (llap_reduce_px2/_px).
+  // A warp takes 16 outputs of row ly and 16 of row ly + 4: its two halves read level 0 rows 8
+  // apart, 16 banks apart in the pair arrays
   if(L1)
   {
-    const int lx = tid % (TX / 2), ly = tid / (TX / 2);
+    const int w = tid >> 5, lx = tid & 15;
+    const int ly = (w & 3) + 8 * (w >> 2) + 4 * ((tid >> 4) & 1);
     const int ox = X0 / 2 + lx, oy = Y0 / 2 + ly;
     const bool own = ox >= OX / 2 && ox < min(OX / 2 + TX / 2, p.l1w) && oy >= OY / 2 && oy < min(OY / 2 + TY / 2, p.l1h);
     if(own)
     {
-      // level 0 slot of virtual x = 2ox + a - 1 is 2lx + a
-      for(int k = 0; k < NPL; k++)
+      // level 0 slot of virtual x = 2ox + a - 1 is 2lx + a: pair words [.][0][lx], [.][1][lx], [.][0][lx + 1]
+      const size_t o = (size_t)oy * p.l1pitch + ox;
+#pragma unroll
+      for(int j = 0; j < LLAP_PAIRS; j++)
       {
-        const __half *const row[3] = { &s.u.L0[k][2 * ly][2 * lx], &s.u.L0[k][2 * ly + 1][2 * lx], &s.u.L0[k][2 * ly + 2][2 * lx] };
-        p.l1[k * p.l1plane + (size_t)oy * p.l1pitch + ox] = f2h(llap_reduce_px(row));
+        const __half2 *a[3], *b[3], *c[3];
+#pragma unroll
+        for(int r = 0; r < 3; r++)
+        {
+          a[r] = &s.u.L0.p[j][2 * ly + r][0][lx];
+          b[r] = &s.u.L0.p[j][2 * ly + r][1][lx];
+          c[r] = &s.u.L0.p[j][2 * ly + r][0][lx + 1];
+        }
+        const float2 v = llap_reduce_px2(a, b, c);
+        p.l1[(2 * j) * p.l1plane + o] = f2h(v.x);
+        p.l1[(2 * j + 1) * p.l1plane + o] = f2h(v.y);
       }
+      const __half *const row[3] = { &s.u.L0.g[2 * ly][2 * lx], &s.u.L0.g[2 * ly + 1][2 * lx], &s.u.L0.g[2 * ly + 2][2 * lx] };
+      p.l1[(NPL - 1) * p.l1plane + o] = f2h(llap_reduce_px(row));
     }
   }
   if(p.hist)

@@ -78,29 +78,28 @@ template<int PY, class R> DEV float vcol(R rowsum, int ky)
 }
 
 // expand of two planes at once (fetch returns both texels as a float2): the
-// same sums in the same order as hrow and vcol for each of the two
+// same sums in the same order as hrow and vcol for each of the two, as paired
+// FP32 operations (one instruction for both planes; the weights are powers of
+// two, so each fused step rounds only its sum, as the separate ones do)
 template<int PX, int PY, class F> DEV float2 expand2(F fetch, int kx, int ky)
 {
   constexpr int NX = PX ? 4 : 5, NY = PY ? 4 : 5;
   constexpr int BXO = PX ? -1 : -2, BYO = PY ? -1 : -2;
-  float r0 = 0.0f, r1 = 0.0f;
+  float2 r = make_float2(0.0f, 0.0f);
 #pragma unroll
   for(int b = 0; b < NY; b++)
   {
-    float row0 = 0.0f, row1 = 0.0f;
+    float2 row = make_float2(0.0f, 0.0f);
 #pragma unroll
     for(int a = 0; a < NX; a++)
     {
       const float w = PX ? ((a == 0 || a == 3) ? 1.0f : 0.5f) : (a == 2 ? 1.0f : 0.5f);
-      const float2 f = fetch(kx + BXO + a, ky + BYO + b);
-      row0 += w * f.x;
-      row1 += w * f.y;
+      row = __ffma2_rn(make_float2(w, w), fetch(kx + BXO + a, ky + BYO + b), row);
     }
     const float wy = PY ? ((b == 0 || b == 3) ? 1.0f : 0.5f) : (b == 2 ? 1.0f : 0.5f);
-    r0 += wy * row0;
-    r1 += wy * row1;
+    r = __ffma2_rn(make_float2(wy, wy), row, r);
   }
-  return make_float2(r0 / 9.0f, r1 / 9.0f);
+  return make_float2(r.x / 9.0f, r.y / 9.0f);
 }
 
 // llap/reduce.comp:17-35 (sample_semisoft), the planes of one level. The four

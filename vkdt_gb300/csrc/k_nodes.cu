@@ -584,7 +584,7 @@ template<int R> __global__ void __launch_bounds__(256) k_nd_fix_bayer(const dev_
 // [X0-1, X0+TX) of a tile and the first llap/reduce level of its outputs
 // (the arithmetic of the tail of the fused develop kernel)
 constexpr int TX = 32, TY = 32, NT = 256, NPL = 11;
-constexpr int LX = TX + 1;
+constexpr int LX = TX + 1, LH = (LX + 1) / 2;
 
 DEV int mirror1(int i, int n)
 {
@@ -597,7 +597,8 @@ DEV int mirror1(int i, int n)
 // (p.rgbf holds the filmcurv output); this kernel reads it for the llap curves
 template<bool FC> __global__ void __launch_bounds__(NT) k_post(const dev_image_t p, const half4 *__restrict__ dm)
 {
-  __shared__ __align__(4) __half L0[NPL][LX][LX + 1];   // [y][slot], rows of an even length
+  __shared__ __half2 L0p[LLAP_PAIRS][LX][2][LH];        // the curve planes in pairs, [y][x & 1][x >> 1]
+  __shared__ __align__(4) __half L0g[LX][LX + 1];       // the grey plane, [y][slot], rows of an even length
   __shared__ uint32_t hist[257];
   const int tid = threadIdx.x;
   const int W = p.W, H = p.H;
@@ -641,30 +642,48 @@ template<bool FC> __global__ void __launch_bounds__(NT) k_post(const dev_image_t
     const float yv = lum2020(gclamp(fc[0], -1000.0f, 1000.0f), gclamp(fc[1], -1000.0f, 1000.0f), gclamp(fc[2], -1000.0f, 1000.0f));
     if(unit_curve)
     {
+      const float2 X = make_float2(yv, yv), nr = make_float2(-rden, -rden), cl = make_float2(cla, cla);
 #pragma unroll
-      for(int k = 0; k < NPL - 1; k++)
-        L0[k][sly][slx] = f2h(llap_curve_unit(yv, kLlapGamma[k], rden, cla));
+      for(int j = 0; j < LLAP_PAIRS; j++) L0p[j][sly][slx & 1][slx >> 1] = llap_curve_unit2(X, j, nr, cl);
     }
     else
     {
 #pragma unroll
-      for(int k = 0; k < NPL - 1; k++)
-        L0[k][sly][slx] = f2h(llap_curve_rcp(yv, kLlapGamma[k], sig, r2s, rden, shd, hil, cla));
+      for(int j = 0; j < LLAP_PAIRS; j++)
+        L0p[j][sly][slx & 1][slx >> 1] = __floats2half2_rn(llap_curve_rcp(yv, kLlapGamma[2 * j], sig, r2s, rden, shd, hil, cla),
+                                                           llap_curve_rcp(yv, kLlapGamma[2 * j + 1], sig, r2s, rden, shd, hil, cla));
     }
-    L0[NPL - 1][sly][slx] = f2h(yv);
+    L0g[sly][slx] = f2h(yv);
   }
   __syncthreads();
-  // llap/reduce.comp (sample_semisoft) for level 1 outputs [X0/2, X0/2+TX/2)
+  // llap/reduce.comp (sample_semisoft) for level 1 outputs [X0/2, X0/2+TX/2): a warp takes 16
+  // outputs of row ly and 16 of row ly + 4 (its halves read pair words 16 banks apart)
   {
-    const int lx = tid % (TX / 2), ly = tid / (TX / 2);
+    const int w = tid >> 5, lx = tid & 15;
+    const int ly = (w & 3) + 8 * (w >> 2) + 4 * ((tid >> 4) & 1);
     const int ox = X0 / 2 + lx, oy = Y0 / 2 + ly;
     const bool own = ox >= OX / 2 && ox < min(OX / 2 + TX / 2, p.l1w) && oy >= OY / 2 && oy < min(OY / 2 + TY / 2, p.l1h);
     if(own)
-      for(int k = 0; k < NPL; k++)
-      { // level 0 slot of virtual x = 2ox + a - 1 is 2lx + a (llap_reduce_px)
-        const __half *const row[3] = { &L0[k][2 * ly][2 * lx], &L0[k][2 * ly + 1][2 * lx], &L0[k][2 * ly + 2][2 * lx] };
-        p.l1[k * p.l1plane + (size_t)oy * p.l1pitch + ox] = f2h(llap_reduce_px(row));
+    { // level 0 slot of virtual x = 2ox + a - 1 is 2lx + a: pair words [.][0][lx], [.][1][lx], [.][0][lx + 1]
+      const size_t o = (size_t)oy * p.l1pitch + ox;
+#pragma unroll
+      for(int j = 0; j < LLAP_PAIRS; j++)
+      {
+        const __half2 *a[3], *b[3], *c[3];
+#pragma unroll
+        for(int r = 0; r < 3; r++)
+        {
+          a[r] = &L0p[j][2 * ly + r][0][lx];
+          b[r] = &L0p[j][2 * ly + r][1][lx];
+          c[r] = &L0p[j][2 * ly + r][0][lx + 1];
+        }
+        const float2 v = llap_reduce_px2(a, b, c);
+        p.l1[(2 * j) * p.l1plane + o] = f2h(v.x);
+        p.l1[(2 * j + 1) * p.l1plane + o] = f2h(v.y);
       }
+      const __half *const row[3] = { &L0g[2 * ly][2 * lx], &L0g[2 * ly + 1][2 * lx], &L0g[2 * ly + 2][2 * lx] };
+      p.l1[(NPL - 1) * p.l1plane + o] = f2h(llap_reduce_px(row));
+    }
   }
   if(!FC && p.hist)
   {

@@ -90,6 +90,40 @@ DEV float llap_reduce_px(const __half *const row[3])
   return (((((P[0][0] + P[1][0]) + (P[0][1] + P[1][1])) + (P[1][0] + P[2][0])) + (P[1][1] + P[2][1]))) * 0.0625f;
 }
 
+// The 10 curve planes of llap level 0 kept as five pairs (2j, 2j+1) of f16 in
+// one 32 bit word: the curves of a pair and the level 1 reduce of a pair run
+// as paired FP32 operations (add/mul/fma.f32x2, one instruction for both
+// planes, each component rounded as the scalar operation rounds it).
+constexpr int LLAP_PAIRS = 5;
+
+// llap_curve_unit for planes 2j and 2j+1 of value x, rounded to f16
+DEV __half2 llap_curve_unit2(float2 X, int j, float2 nrden, float2 cla)
+{
+  const float2 c = __fadd2_rn(X, make_float2(-kLlapGamma[2 * j], -kLlapGamma[2 * j + 1]));
+  const float2 a = __fmul2_rn(__fmul2_rn(c, c), nrden);               // -c c rden
+  const float2 e = make_float2(curve_exp(a.x), curve_exp(a.y));
+  const float2 v = __ffma2_rn(__fmul2_rn(cla, c), e, X);             // x + clarity c e
+  return __floats2half2_rn(v.x, v.y);
+}
+
+// llap_reduce_px for a pair of planes: r[k] points at the pair word of row k
+// (virtual y = 2 oy - 1 + k) at virtual x = 2 ox - 1, r1[k] at 2 ox and r0[k]
+// at 2 ox + 1 (the three taps of the row); the same sums in the same order
+DEV float2 llap_reduce_px2(const __half2 *const a[3], const __half2 *const b[3], const __half2 *const c[3])
+{
+  float2 P[3][2];
+#pragma unroll
+  for(int r = 0; r < 3; r++)
+  {
+    const float2 t0 = __half22float2(*a[r]), t1 = __half22float2(*b[r]), t2 = __half22float2(*c[r]);
+    P[r][0] = __fadd2_rn(t0, t1);
+    P[r][1] = __fadd2_rn(t1, t2);
+  }
+  const float2 s = __fadd2_rn(__fadd2_rn(__fadd2_rn(__fadd2_rn(P[0][0], P[1][0]), __fadd2_rn(P[0][1], P[1][1])),
+                                          __fadd2_rn(P[1][0], P[2][0])), __fadd2_rn(P[1][1], P[2][1]));
+  return __fmul2_rn(s, make_float2(0.0625f, 0.0625f));
+}
+
 // histogram bin, bit exact with the oracle (see hist_log there for the method)
 DEV float hist_log(float x)
 {

@@ -33,3 +33,19 @@ def test_rcp_f16v_and_div_ry_equal_ieee(tmp_path):
     assert r.returncode == 0, r.stdout + r.stderr
     assert "0 of 65536 f16 values differ, 0 of their squares" in r.stdout, r.stdout
     assert "noop_code: 0 of" in r.stdout, r.stdout
+
+
+@pytest.mark.gpu
+def test_paired_fp32_intrinsics_against_scalar(tmp_path):
+    # records, per class of operand, how often the paired forms (add/mul/fma.f32x2) differ from the
+    # scalar IEEE operations; the kernels use them only where a value feeds continuous arithmetic
+    # (the llap planes, the llap expand), so any difference found here is reported, not asserted
+    nvcc = _nvcc()
+    assert nvcc, "nvcc not found"
+    exe = str(tmp_path / "check_paired")
+    subprocess.run([nvcc, "-gencode=arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-o", exe,
+                    os.path.join(HERE, "cuda", "check_paired.cu")], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    print(r.stdout)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "normal " in r.stdout and "quotient remainders" in r.stdout, r.stdout

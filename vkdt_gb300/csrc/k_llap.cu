@@ -380,8 +380,9 @@ __global__ void __launch_bounds__(256, 6) k_llap_final(const dev_llap_k3_t p)
   __syncthreads();
   const float sig = p.ll_sigma;
   const float r2s = 1.0f / (2.0f * sig), rden = 1.0f / (2.0f * sig * sig / 3.0f);
-  // the pair as one 16 byte word where rows have even length and both images are 16 byte aligned
-  const bool vec = !(p.W & 1) && !((reinterpret_cast<uintptr_t>(p.rgbf) | reinterpret_cast<uintptr_t>(p.out)) & 15);
+  // the pair as one 16 byte word where it starts 16 byte aligned in both images (every pair of
+  // rows of even length; every other row of odd length, the crop window's 5993 for one)
+  const bool vec_base = !((reinterpret_cast<uintptr_t>(p.rgbf) | reinterpret_cast<uintptr_t>(p.out)) & 15);
   for(int t = threadIdx.x; t < NKX * FTY; t += blockDim.x)
   { // the pair (x, x + 1) of row y; a warp takes one row
     const int lx = t % NKX, ry = t / NKX;
@@ -390,6 +391,7 @@ __global__ void __launch_bounds__(256, 6) k_llap_final(const dev_llap_k3_t p)
     const int sy = (ry >> 1) + 2;
     const size_t o = (size_t)y * p.W + x;
     const bool two = x + 1 < p.W;
+    const bool vec = vec_base && two && !(o & 1);
     uint4 u = make_uint4(0u, 0u, 0u, 0u);
     if(vec) u = __ldg(reinterpret_cast<const uint4 *>(p.rgbf + o));
     else

@@ -205,7 +205,7 @@ struct vkdt_cuda_graph_t
   bool crop = false;             // demosaic -> crop -> colour connected
   bool crop_stage = false;       // the crop moves or resamples pixels (not the identity): its own launch
   bool crop_given = false;       // its committed block came with the scheduler's nodes (set_nodes)
-  bool crop_shift = false;       // the crop moves the image by whole texels: applied by the fused kernel
+  bool crop_shift = false;       // the crop moves the image by whole texels: the next launch reads the window
   int crop_dx = 0, crop_dy = 0;  // that shift
   float crop_blk[20];            // crop's committed uniform block (crop/main.c:276-343)
   int crop_w = 0, crop_h = 0;    // its output size
@@ -685,7 +685,7 @@ size_t plan_arena(vkdt_cuda_graph_t *g)
       g->off_g = take((size_t)g->W * g->H * 2);
       g->off_dm = take((size_t)g->W * g->H * 8);
     }
-    if(g->crop_stage) g->off_cr = take((size_t)g->out_w * g->out_h * 8);
+    if(g->crop_stage && !g->crop_shift) g->off_cr = take((size_t)g->out_w * g->out_h * 8);
   }
   return off;
 }
@@ -917,14 +917,18 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
         if((r = mark())) return r;
       }
     }
-    if(g->crop_stage)
+    if(g->crop_stage && !g->crop_shift)
     { // crop/main on the demosaic output
       CU(launch_nodes(np, 9, s));
       if((r = mark())) return r;
     }
     dev_image_t dp = d;
     dp.W = g->out_w; dp.H = g->out_h;
-    CU(launch_post(dp, g->crop_stage ? np.cr : g->rcd ? nullptr : np.dm, s));
+    // the post kernel's input: the crop output, the window of the demosaic output, the demosaic
+    // output, or nothing (rcd_fill applied colour and filmcurv itself)
+    const half4 *pin = g->crop_stage ? (g->crop_shift ? np.dm + (size_t)g->crop_dy * g->dm_w + g->crop_dx : np.cr)
+                     : g->rcd ? nullptr : np.dm;
+    CU(launch_post(dp, pin, g->crop_shift ? g->dm_w : g->out_w, s));
     if((r = mark())) return r;
   }
   else if(g->crop_shift)
@@ -935,7 +939,7 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
     if((r = mark())) return r;
     dev_image_t dp = d;
     dp.W = g->out_w; dp.H = g->out_h;
-    CU(launch_post(dp, nullptr, s));
+    CU(launch_post(dp, nullptr, g->out_w, s));
     if((r = mark())) return r;
   }
   else
@@ -1303,8 +1307,9 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
   // bayer with the fused path's hilite front
   // a demosaic colour param >= 1 widens the bayer fix radius to 2 (fix.comp:124): node by node
   const bool wide_fix = !xt && g->mod("demosaic")->n("colour") >= 1;
-  // a crop by whole texels rides on the fused kernel; any other crop resamples (its own launch)
-  g->crop_shift = g->crop_stage && !xt && !g->halfsize && !g->rcd && !wide_fix
+  // a crop by whole texels rides on the fused kernel, or on the post kernel of the per-node chain
+  // (it reads the window of the demosaic output); any other crop resamples (its own launch)
+  g->crop_shift = g->crop_stage
                && crop_whole_texels(g->crop_blk, g->dm_w, g->dm_h, g->out_w, g->out_h, &g->crop_dx, &g->crop_dy);
   g->unfused = xt || g->halfsize || g->rcd || wide_fix || (g->crop_stage && !g->crop_shift);
   g->k1front = g->unfused && !xt;
@@ -1448,7 +1453,7 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
       L_splat = launch("demosaic", "splat");
       L_fix = launch("demosaic", "fix");
     }
-    if(g->crop_stage) L_crop = launch("crop", "main");
+    if(g->crop_stage && !g->crop_shift) L_crop = launch("crop", "main");
     L_post = launch("llap", "curve");
   }
   for(size_t l = 1; l < g->lp.size(); l++) L_lr.push_back(launch("llap", "reduce"));
@@ -1480,7 +1485,7 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
     else if(n.kernel == tkn("gauss") || n.kernel == tkn("down")) n.fused = L_gauss;
     else if(n.kernel == tkn("splat")) n.fused = L_splat;
     else if(n.kernel == tkn("fix")) n.fused = L_fix;
-    else if(n.name == tkn("crop")) n.fused = g->crop_stage ? L_crop : L_post;
+    else if(n.name == tkn("crop")) n.fused = g->crop_stage && !g->crop_shift ? L_crop : L_post;
     else n.fused = L_post;   // colour, histogram, filmcurv, llap curve
   }
   // per level nodes (reduce and assemble pairs in create_nodes order)
@@ -1494,7 +1499,7 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
   }
   for(size_t l = 0; l < g->lp.size(); l++)
   {
-    add_node(g, "llap", "reduce", g->lp[l].w, g->lp[l].h, 11, l == 0 ? (g->crop_shift ? L_curve : L_post) : L_lr[l - 1]);
+    add_node(g, "llap", "reduce", g->lp[l].w, g->lp[l].h, 11, l == 0 ? (!g->unfused && g->crop_shift ? L_curve : L_post) : L_lr[l - 1]);
     const int fw = l == 0 ? OW : g->lp[l - 1].w, fh = l == 0 ? OH : g->lp[l - 1].h;
     add_node(g, "llap", "assemble", fw, fh, 1, l == 0 ? L_fin : L_la[l - 1]);
   }
@@ -2025,13 +2030,13 @@ int vkdt_cuda_graph_debug_stage(vkdt_cuda_graph_t *g, int stage, float *out, siz
     if(stage != 2 && !g->debug) return fail(VKDT_CUDA_INCOMPLETE, "debug stages not enabled");
     if(stage == 11 && !g->crop_stage) return fail(VKDT_CUDA_INCOMPLETE, "no crop stage in this graph");
     if(stage == 11 && g->crop_shift)
-    { // the fused kernel reads the window of its demosaic output: that window, alpha 1
+    { // the kernel after demosaic reads the window of its output: that window, alpha 1
       if(count < nout * 4) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "buffer too small");
-      std::vector<__half> h((size_t)g->W * g->H * 4);
-      CU(cudaMemcpy(h.data(), g->arena + g->off_dbg_dm, h.size() * 2, cudaMemcpyDeviceToHost));
+      std::vector<__half> h((size_t)g->dm_w * g->dm_h * 4);
+      CU(cudaMemcpy(h.data(), g->arena + (g->unfused ? g->off_dm : g->off_dbg_dm), h.size() * 2, cudaMemcpyDeviceToHost));
       for(int y = 0; y < g->out_h; y++) for(int x = 0; x < g->out_w; x++)
       {
-        const size_t i = (size_t)y * g->out_w + x, j = (size_t)(y + g->crop_dy) * g->W + x + g->crop_dx;
+        const size_t i = (size_t)y * g->out_w + x, j = (size_t)(y + g->crop_dy) * g->dm_w + x + g->crop_dx;
         for(int k = 0; k < 3; k++) out[4 * i + k] = __half2float(h[4 * j + k]);
         out[4 * i + 3] = 1.0f;
       }

@@ -511,7 +511,7 @@ __global__ void __launch_bounds__(256) k_nd_gauss_bayer(const dev_nodes_t p)
   }
   float v[4];
   int dec;
-  gauss_exact(px, v, dec);
+  gauss_entry(px, v, dec);
   p.cov[(size_t)y * p.hw + x] = mk_half4(v[0], v[1], v[2], v[3]);
   if(p.dbg_gauss) p.dbg_gauss[(size_t)y * p.hw + x] = (uint8_t)dec;
 }
@@ -595,7 +595,7 @@ DEV int mirror1(int i, int n)
 
 // FC: the demosaic kernel applied colour, the histogram and filmcurv already
 // (p.rgbf holds the filmcurv output); this kernel reads it for the llap curves
-template<bool FC> __global__ void __launch_bounds__(NT) k_post(const dev_image_t p, const half4 *__restrict__ dm)
+template<bool FC> __global__ void __launch_bounds__(NT) k_post(const dev_image_t p, const half4 *__restrict__ dm, int dm_pitch)
 {
   __shared__ __half2 L0p[LLAP_PAIRS][LX][2][LH];        // the curve planes in pairs, [y][x & 1][x >> 1]
   __shared__ __align__(4) __half L0g[LX][LX + 1];       // the grey plane, [y][slot], rows of an even length
@@ -626,7 +626,7 @@ template<bool FC> __global__ void __launch_bounds__(NT) k_post(const dev_image_t
     else
     {
       float d[4];
-      ld_half4(dm + (size_t)py * W + px, d[0], d[1], d[2], d[3]);
+      ld_half4(dm + (size_t)py * dm_pitch + px, d[0], d[1], d[2], d[3]);
       float co[3];
       colour_px(p, d, co);
       const bool own = vx == px && vy == py && px >= OX && px < OXe && py >= OY && py < OYe;
@@ -728,9 +728,9 @@ cudaError_t launch_nodes(const dev_nodes_t &p, int stage, cudaStream_t s)
   return cudaGetLastError();
 }
 
-cudaError_t launch_post(const dev_image_t &p, const half4 *dm, cudaStream_t s)
+cudaError_t launch_post(const dev_image_t &p, const half4 *dm, int dm_pitch, cudaStream_t s)
 {
-  if(dm) k_post<false><<<dim3((p.W + TX - 1) / TX, (p.H + TY - 1) / TY), NT, 0, s>>>(p, dm);
-  else    k_post<true><<<dim3((p.W + TX - 1) / TX, (p.H + TY - 1) / TY), NT, 0, s>>>(p, dm);
+  if(dm) k_post<false><<<dim3((p.W + TX - 1) / TX, (p.H + TY - 1) / TY), NT, 0, s>>>(p, dm, dm_pitch);
+  else    k_post<true><<<dim3((p.W + TX - 1) / TX, (p.H + TY - 1) / TY), NT, 0, s>>>(p, dm, dm_pitch);
   return cudaGetLastError();
 }

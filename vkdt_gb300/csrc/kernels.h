@@ -165,7 +165,9 @@ cudaError_t launch_nodes(const dev_nodes_t &p, int stage, cudaStream_t s);
 // colour -> histogram -> filmcurv -> llap curve -> llap level 1 reduce on the
 // demosaic output (p.W x p.H = the output size; p.mosaic unused); with dm null,
 // llap curve -> level 1 reduce on the filmcurv output p.rgbf
-cudaError_t launch_post(const dev_image_t &p, const half4 *dm, cudaStream_t s);
+// dm: the demosaic output read at rows of dm_pitch texels (a crop by whole texels passes the window's
+// first texel and the demosaic output's width)
+cudaError_t launch_post(const dev_image_t &p, const half4 *dm, int dm_pitch, cudaStream_t s);
 
 // demosaic RCD (k_rcd.cu): rcd_conv (stage 0) and rcd_fill (stage 1) on the
 // bayer hilite output, W x H (even W)

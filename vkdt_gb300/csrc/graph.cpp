@@ -926,8 +926,8 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
     dp.W = g->out_w; dp.H = g->out_h;
     // the post kernel's input: the crop output, the window of the demosaic output, the demosaic
     // output, or nothing (rcd_fill applied colour and filmcurv itself)
-    const half4 *pin = g->crop_stage ? (g->crop_shift ? np.dm + (size_t)g->crop_dy * g->dm_w + g->crop_dx : np.cr)
-                     : g->rcd ? nullptr : np.dm;
+    const half4 *window = g->at<half4>(g->off_dm + ((size_t)g->crop_dy * g->dm_w + g->crop_dx) * 8);
+    const half4 *pin = g->crop_stage ? (g->crop_shift ? window : np.cr) : g->rcd ? nullptr : np.dm;
     CU(launch_post(dp, pin, g->crop_shift ? g->dm_w : g->out_w, s));
     if((r = mark())) return r;
   }

@@ -6,7 +6,12 @@
 // them bit for bit per operation and class of operand: normal operands across
 // the exponent range, operands near the subnormal range, subnormal operands,
 // and zeros, infinities and NaN; and the Markstein remainder a - q b of a
-// correctly rounded quotient, which is exact only when the fma is fused.
+// correctly rounded quotient, which is exact only when the fma is fused. Two
+// more lines compare a product followed by a sum, a b + c, written as two
+// paired operations: through the intrinsics, which the compiler may contract
+// into one fma (-fmad=true), and through the inline PTX add/mul.rn.f32x2 of
+// gauss.cuh, whose separate roundings it keeps.
+#include "gauss.cuh"
 #include <cuda_runtime.h>
 #include <cstdio>
 #include <cstdint>
@@ -33,13 +38,15 @@ __global__ void k_pair(const float2 *a, const float2 *b, const float2 *c, float2
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if(i >= n) return;
   const float2 x = a[i], y = b[i], z = c[i];
-  o[i] = op == 0 ? __fadd2_rn(x, y) : op == 1 ? __fmul2_rn(x, y) : __ffma2_rn(x, y, z);
+  o[i] = op == 0 ? __fadd2_rn(x, y) : op == 1 ? __fmul2_rn(x, y) : op == 2 ? __ffma2_rn(x, y, z)
+       : op == 3 ? __fadd2_rn(__fmul2_rn(x, y), z) : add2_rn(mul2_rn(x, y), z);
 }
 __global__ void k_scalar(const float *a, const float *b, const float *c, float *o, int n, int op)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if(i >= n) return;
-  o[i] = op == 0 ? __fadd_rn(a[i], b[i]) : op == 1 ? __fmul_rn(a[i], b[i]) : __fmaf_rn(a[i], b[i], c[i]);
+  o[i] = op == 0 ? __fadd_rn(a[i], b[i]) : op == 1 ? __fmul_rn(a[i], b[i]) : op == 2 ? __fmaf_rn(a[i], b[i], c[i])
+       : __fadd_rn(__fmul_rn(a[i], b[i]), c[i]);
 }
 
 static bool same(float x, float y)
@@ -58,7 +65,7 @@ int main()
   if(cudaMalloc(&da, bytes) || cudaMalloc(&db, bytes) || cudaMalloc(&dc, bytes) || cudaMalloc(&dp, bytes) || cudaMalloc(&ds, bytes))
   { printf("device allocation failed\n"); return 2; }
   const char *cls[5] = { "normal", "near subnormal", "subnormal", "special", "remainder" };
-  const char *ops[3] = { "add", "mul", "fma" };
+  const char *ops[5] = { "add", "mul", "fma", "mul+add (intrinsics)", "mul+add (ptx)" };
   for(int c = 0; c < 5; c++)
   {
     uint32_t h = 12345u + 977u * c;
@@ -79,7 +86,7 @@ int main()
     cudaMemcpy(db, hb.data(), bytes, cudaMemcpyHostToDevice);
     cudaMemcpy(dc, hc.data(), bytes, cudaMemcpyHostToDevice);
     printf("%-15s of %d components:", cls[c], 2 * n);
-    for(int op = (c < 4 ? 0 : 2); op < 3; op++)
+    for(int op = (c < 4 ? 0 : 2); op < (c == 0 ? 5 : 3); op++)
     {
       k_pair<<<(n + 255) / 256, 256>>>((const float2 *)da, (const float2 *)db, (const float2 *)dc, (float2 *)dp, n, op);
       k_scalar<<<(2 * n + 255) / 256, 256>>>(da, db, dc, ds, 2 * n, op);

@@ -43,9 +43,12 @@ def test_paired_fp32_intrinsics_against_scalar(tmp_path):
     nvcc = _nvcc()
     assert nvcc, "nvcc not found"
     exe = str(tmp_path / "check_paired")
-    subprocess.run([nvcc, "-gencode=arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-o", exe,
+    subprocess.run([nvcc, "-gencode=arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
+                    "-I" + os.path.join(ROOT, "vkdt_gb300", "csrc"), "-o", exe,
                     os.path.join(HERE, "cuda", "check_paired.cu")], check=True)
     r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     print(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "normal " in r.stdout and "remainder" in r.stdout, r.stdout
+    # the inline PTX forms the covariance is built with round every operation on its own
+    assert "mul+add (ptx) 0 " in r.stdout, r.stdout

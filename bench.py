@@ -937,15 +937,15 @@ def main():
         try:
             tj = json.load(open(tp))
             if tj.get("k_develop_source_sha") == source_hash(K_DEVELOP_SOURCES) and (WD, HT) == (6000, 4000) \
-                    and DENOISE == 0:
+                    and DENOISE == 0 and tj.get("graph", "chain") == GRAPH:
                 traffic = tj.get("k_develop_bytes_per_launch")
                 traffic_note = "ncu capture of this kernel source at this size (" + tj.get("source", "") + ")"
+                # the kernel is bound by instruction issue, not by HBM: the same capture's issue
+                # utilisation and instructions per pixel are reported beside the HBM fraction
+                issue = {"issue_active": tj.get("k_develop_issue_active"),
+                         "thread_inst_per_px": tj.get("k_develop_thread_inst_per_px"), "source": "ncu capture, profiles/"}
             else:
-                traffic_note = "no ncu capture of this kernel source and size"
-            # the kernel is bound by instruction issue, not by HBM: the ncu capture's issue
-            # utilisation and instructions per pixel are reported beside the HBM fraction
-            issue = {"issue_active": tj.get("k_develop_issue_active"),
-                     "thread_inst_per_px": tj.get("k_develop_thread_inst_per_px"), "source": "ncu capture, profiles/"}
+                traffic_note = "no ncu capture of this kernel source, size and graph"
         except Exception:
             traffic = None
     kname = {"demosaic:fix": ("k_develop (hilite doub + demosaic + crop + colour + filmcurv)" if crop_fused else

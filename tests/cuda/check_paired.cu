@@ -7,11 +7,10 @@
 // the exponent range, operands near the subnormal range, subnormal operands,
 // and zeros, infinities and NaN; and the Markstein remainder a - q b of a
 // correctly rounded quotient, which is exact only when the fma is fused. Two
-// more lines compare a product followed by a sum, a b + c, written as two
-// paired operations: through the intrinsics, which the compiler may contract
-// into one fma (-fmad=true), and through the inline PTX add/mul.rn.f32x2 of
-// gauss.cuh, whose separate roundings it keeps.
-#include "gauss.cuh"
+// more lines compare a product followed by a sum, a b + c: as two paired
+// operations, which the code generator contracts into one paired fma (one
+// rounding instead of two), and as the demosaic covariance writes it, the
+// paired product followed by scalar IEEE adds, which are never contracted.
 #include <cuda_runtime.h>
 #include <cstdio>
 #include <cstdint>
@@ -39,7 +38,8 @@ __global__ void k_pair(const float2 *a, const float2 *b, const float2 *c, float2
   if(i >= n) return;
   const float2 x = a[i], y = b[i], z = c[i];
   o[i] = op == 0 ? __fadd2_rn(x, y) : op == 1 ? __fmul2_rn(x, y) : op == 2 ? __ffma2_rn(x, y, z)
-       : op == 3 ? __fadd2_rn(__fmul2_rn(x, y), z) : add2_rn(mul2_rn(x, y), z);
+       : op == 3 ? __fadd2_rn(__fmul2_rn(x, y), z) : [&] { const float2 t = __fmul2_rn(x, y);
+                                                             return make_float2(__fadd_rn(t.x, z.x), __fadd_rn(t.y, z.y)); }();
 }
 __global__ void k_scalar(const float *a, const float *b, const float *c, float *o, int n, int op)
 {
@@ -65,7 +65,7 @@ int main()
   if(cudaMalloc(&da, bytes) || cudaMalloc(&db, bytes) || cudaMalloc(&dc, bytes) || cudaMalloc(&dp, bytes) || cudaMalloc(&ds, bytes))
   { printf("device allocation failed\n"); return 2; }
   const char *cls[5] = { "normal", "near subnormal", "subnormal", "special", "remainder" };
-  const char *ops[5] = { "add", "mul", "fma", "mul+add (intrinsics)", "mul+add (ptx)" };
+  const char *ops[5] = { "add", "mul", "fma", "paired mul+add", "paired mul, scalar add" };
   for(int c = 0; c < 5; c++)
   {
     uint32_t h = 12345u + 977u * c;

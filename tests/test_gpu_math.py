@@ -37,18 +37,18 @@ def test_rcp_f16v_and_div_ry_equal_ieee(tmp_path):
 
 @pytest.mark.gpu
 def test_paired_fp32_intrinsics_against_scalar(tmp_path):
-    # records, per class of operand, how often the paired forms (add/mul/fma.f32x2) differ from the
-    # scalar IEEE operations; the kernels use them only where a value feeds continuous arithmetic
-    # (the llap planes, the llap expand), so any difference found here is reported, not asserted
+    # per class of operand, how often the paired forms (add/mul/fma.f32x2) differ from the scalar IEEE
+    # operations; and a product followed by a sum, paired throughout (contracted into one fma by the
+    # code generator: reported, not asserted) and in the covariance's form
     nvcc = _nvcc()
     assert nvcc, "nvcc not found"
     exe = str(tmp_path / "check_paired")
-    subprocess.run([nvcc, "-gencode=arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
-                    "-I" + os.path.join(ROOT, "vkdt_gb300", "csrc"), "-o", exe,
+    subprocess.run([nvcc, "-gencode=arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-o", exe,
                     os.path.join(HERE, "cuda", "check_paired.cu")], check=True)
     r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     print(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "normal " in r.stdout and "remainder" in r.stdout, r.stdout
-    # the inline PTX forms the covariance is built with round every operation on its own
-    assert "mul+add (ptx) 0 " in r.stdout, r.stdout
+    # single paired operations round as the scalar ones; a paired product summed by scalar IEEE adds
+    # (the covariance's form) keeps both roundings
+    assert "add 0 mul 0 fma 0" in r.stdout and "paired mul, scalar add 0 " in r.stdout, r.stdout

@@ -4,39 +4,14 @@
 #include "common.cuh"
 #include "kernels.h"
 
-// paired FP32 operations as PTX instructions, each component rounded to nearest on its own
-DEV unsigned long long f2_bits(float2 v)
-{
-  return (unsigned long long)__float_as_uint(v.x) | ((unsigned long long)__float_as_uint(v.y) << 32);
-}
-DEV float2 f2_of(unsigned long long u) { return make_float2(__uint_as_float((unsigned)u), __uint_as_float((unsigned)(u >> 32))); }
-DEV float2 add2_rn(float2 a, float2 b)
-{
-  unsigned long long r;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_bits(a)), "l"(f2_bits(b)));
-  return f2_of(r);
-}
-DEV float2 mul2_rn(float2 a, float2 b)
-{
-  unsigned long long r;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_bits(a)), "l"(f2_bits(b)));
-  return f2_of(r);
-}
-DEV float2 fma2_rn(float2 a, float2 b, float2 c)
-{
-  unsigned long long r;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(f2_bits(a)), "l"(f2_bits(b)), "l"(f2_bits(c)));
-  return f2_of(r);
-}
-
 // x / b for both components of a pair as div_ry does each (one reciprocal per
 // component shared by its quotients; IEEE division outside div_ok's range)
 DEV float2 div2_ry(float2 a, float2 b, float2 y, bool okx, bool oky)
 {
   if(okx && oky && div_ok(a.x) && div_ok(a.y))
   {
-    const float2 q = mul2_rn(a, y);
-    return fma2_rn(fma2_rn(make_float2(-q.x, -q.y), b, a), y, q);
+    const float2 q = __fmul2_rn(a, y);
+    return __ffma2_rn(__ffma2_rn(make_float2(-q.x, -q.y), b, a), y, q);
   }
   return make_float2(div_ry(a.x, b.x, y.x, okx), div_ry(a.y, b.y, y.y, oky));
 }
@@ -48,13 +23,15 @@ DEV float2 div2_ry(float2 a, float2 b, float2 y, bool okx, bool oky)
 // covariance (1.25 -0.25; -0.25 1.25), eigenvectors at 45 degrees, so the snap
 // there follows the last bits of the sums and is evaluated exactly. The two
 // structure tensors (Sw of the greens, Sb of their reciprocals) are built side
-// by side as pairs (w, b): each pair operation is one paired FP32 instruction
-// (add/mul/fma.rn.f32x2, inline PTX: the compiler neither contracts nor folds
-// them, as it may the paired intrinsics) whose components round as the scalar
-// IEEE operations do. The greens are f16 values (the hilite output), so their
-// reciprocals and those of their squares come from rcp_f16v; the quotients by
-// the four sums share one correctly rounded reciprocal each (div_ry): the same
-// IEEE results.
+// by side as pairs (w, b) where a paired FP32 instruction (add/mul/fma.f32x2)
+// rounds each component as the scalar IEEE operation does: the weighted sums of
+// the means (exact products), the differences to the means, the products, and
+// the quotients. A paired product that a paired sum consumes may be contracted
+// into one fma by the code generator, so every sum of products is a scalar
+// IEEE add (never contracted), as is the determinant. The greens are f16
+// values (the hilite output), so their reciprocals and those of their squares
+// come from rcp_f16v; the quotients by the four sums share one correctly
+// rounded reciprocal each (div_ry): the same IEEE results.
 DEV void gauss_exact(const float px[8], float v[4], int &dec)
 {
   // sample values with their reciprocals: (px, 1/px)
@@ -72,9 +49,9 @@ DEV void gauss_exact(const float px[8], float v[4], int &dec)
   for(int ii = -1; ii < 3; ii++)
   {
     if(((j + ii) & 1) != 1) continue;
-    m0 = fma2_rn(make_float2((float)ii, (float)ii), pv[k], m0);
-    m1 = fma2_rn(make_float2((float)j, (float)j), pv[k], m1);
-    sm = add2_rn(sm, pv[k]);
+    m0 = __ffma2_rn(make_float2((float)ii, (float)ii), pv[k], m0);
+    m1 = __ffma2_rn(make_float2((float)j, (float)j), pv[k], m1);
+    sm = __fadd2_rn(sm, pv[k]);
     k++;
   }
   {
@@ -94,14 +71,15 @@ DEV void gauss_exact(const float px[8], float v[4], int &dec)
     if(((j + ii) & 1) != 1) continue;
     const float p2 = __fmul_rn(px[k], px[k]);
     const float2 P = make_float2(p2, rcp_f16v(p2));                  // (p2, 1/p2)
-    const float2 q0 = add2_rn(make_float2((float)ii, (float)ii), n0);
-    const float2 q1 = add2_rn(make_float2((float)j, (float)j), n1);
-    const float2 a = mul2_rn(P, q0), b = mul2_rn(P, q1);
-    S00 = add2_rn(S00, mul2_rn(a, q0));
-    S01 = add2_rn(S01, mul2_rn(a, q1));
-    S10 = add2_rn(S10, mul2_rn(b, q0));
-    S11 = add2_rn(S11, mul2_rn(b, q1));
-    ss = add2_rn(ss, P);
+    const float2 q0 = __fadd2_rn(make_float2((float)ii, (float)ii), n0);
+    const float2 q1 = __fadd2_rn(make_float2((float)j, (float)j), n1);
+    const float2 a = __fmul2_rn(P, q0), b = __fmul2_rn(P, q1);
+    const float2 t00 = __fmul2_rn(a, q0), t01 = __fmul2_rn(a, q1), t10 = __fmul2_rn(b, q0), t11 = __fmul2_rn(b, q1);
+    S00 = make_float2(__fadd_rn(S00.x, t00.x), __fadd_rn(S00.y, t00.y));
+    S01 = make_float2(__fadd_rn(S01.x, t01.x), __fadd_rn(S01.y, t01.y));
+    S10 = make_float2(__fadd_rn(S10.x, t10.x), __fadd_rn(S10.y, t10.y));
+    S11 = make_float2(__fadd_rn(S11.x, t11.x), __fadd_rn(S11.y, t11.y));
+    ss = __fadd2_rn(ss, P);
     k++;
   }
   {
@@ -110,9 +88,9 @@ DEV void gauss_exact(const float px[8], float v[4], int &dec)
     S00 = div2_ry(S00, ss, y, okw, okb); S01 = div2_ry(S01, ss, y, okw, okb);
     S10 = div2_ry(S10, ss, y, okw, okb); S11 = div2_ry(S11, ss, y, okw, okb);
   }
-  // (detw, detb) = S00 S11 - S10 S01, the difference as a sum with the negated product
-  const float2 d1 = mul2_rn(S00, S11), d2 = mul2_rn(S10, S01);
-  const float2 det = add2_rn(d1, make_float2(-d2.x, -d2.y));
+  // (detw, detb) = S00 S11 - S10 S01 (scalar: a difference of products)
+  const float2 det = make_float2(__fsub_rn(__fmul_rn(S00.x, S11.x), __fmul_rn(S10.x, S01.x)),
+                                 __fsub_rn(__fmul_rn(S00.y, S11.y), __fmul_rn(S10.y, S01.y)));
   float eval[2], evec0[2], evec1[2];
   const bool usew = det.x < det.y;
   if(usew) evd2x2(eval, evec0, evec1, S00.x, S10.x, S11.x);

@@ -2,11 +2,13 @@
 // against the IEEE intrinsics: rcp_f16v on every f16 encoding and on the
 // squares of all of them (every input it is used on), div_ry on random
 // operands across the exponent range and on zeros, infinities, NaN and
-// subnormals, and noop_code against the code table's IEEE formula on every
-// u16 code for several black and white levels. Prints the counts and exits
+// subnormals, noop_code against the code table's IEEE formula on every u16
+// code for several black and white levels, and unorm16_exact (denoise.cuh)
+// against the IEEE quotient on every u16 code. Prints the counts and exits
 // non-zero on any difference.
 #include "common.cuh"
 #include "hilite.cuh"
+#include "denoise.cuh"
 #include <cstdio>
 
 __device__ bool same(float a, float b) { return __float_as_uint(a) == __float_as_uint(b) || (a != a && b != b); }
@@ -68,17 +70,26 @@ __global__ void k_noop(unsigned *bad)
   if(__half_as_ushort(want) != __half_as_ushort(got)) atomicAdd(bad, 1u);
 }
 
+// every u16 code: unorm16_exact against the IEEE quotient of an R16_UNORM read
+__global__ void k_unorm(unsigned *bad)
+{
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if(v >= 65536) return;
+  if(!same(unorm16_exact((uint32_t)v), __fdiv_rn((float)v, 65535.0f))) atomicAdd(bad, 1u);
+}
+
 int main()
 {
   unsigned *d_bad;
   unsigned long long *d_cnt;
-  if(cudaMalloc(&d_bad, 3 * sizeof(unsigned)) || cudaMalloc(&d_cnt, 2 * sizeof(unsigned long long))) return 2;
-  cudaMemset(d_bad, 0, 3 * sizeof(unsigned));
+  if(cudaMalloc(&d_bad, 4 * sizeof(unsigned)) || cudaMalloc(&d_cnt, 2 * sizeof(unsigned long long))) return 2;
+  cudaMemset(d_bad, 0, 4 * sizeof(unsigned));
   cudaMemset(d_cnt, 0, 2 * sizeof(unsigned long long));
   k_rcp<<<256, 256>>>(d_bad);
   k_div<<<152 * 4, 256>>>(d_cnt, 2048);
   k_noop<<<65536 * 6 / 256, 256>>>(d_bad + 2);
-  unsigned bad[3];
+  k_unorm<<<256, 256>>>(d_bad + 3);
+  unsigned bad[4];
   unsigned long long cnt[2];
   cudaMemcpy(bad, d_bad, sizeof(bad), cudaMemcpyDeviceToHost);
   cudaMemcpy(cnt, d_cnt, sizeof(cnt), cudaMemcpyDeviceToHost);
@@ -86,6 +97,7 @@ int main()
   printf("rcp_f16v: %u of 65536 f16 values differ, %u of their squares\n", bad[0], bad[1]);
   printf("div_ry: %llu quotients on the corrected path, %llu differ from __fdiv_rn\n", cnt[0], cnt[1]);
   printf("noop_code: %u of 6 x 65536 codes differ from the code table\n", bad[2]);
+  printf("unorm16_exact: %u of 65536 codes differ\n", bad[3]);
   printf("cuda: %s\n", cudaGetErrorString(e));
-  return (e != cudaSuccess || bad[0] || bad[1] || bad[2] || cnt[1] || cnt[0] == 0) ? 1 : 0;
+  return (e != cudaSuccess || bad[0] || bad[1] || bad[2] || bad[3] || cnt[1] || cnt[0] == 0) ? 1 : 0;
 }

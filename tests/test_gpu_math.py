@@ -1,7 +1,8 @@
 """The exact arithmetic shortcuts of the kernels (common.cuh, hilite.cuh):
 rcp_f16v must equal the IEEE reciprocal on every input the kernels give it
-(all f16 values and their squares), div_ry the IEEE quotient and noop_code
-the denoise/noop code table on every u16 code. The check is
+(all f16 values and their squares), div_ry the IEEE quotient, noop_code
+the denoise/noop code table on every u16 code and unorm16_exact the IEEE
+quotient v / 65535 of every u16 code. The check is
 a small CUDA program built against the kernels' own header; it runs on the
 device and compares bit for bit."""
 import os
@@ -33,6 +34,7 @@ def test_rcp_f16v_and_div_ry_equal_ieee(tmp_path):
     assert r.returncode == 0, r.stdout + r.stderr
     assert "0 of 65536 f16 values differ, 0 of their squares" in r.stdout, r.stdout
     assert "noop_code: 0 of" in r.stdout, r.stdout
+    assert "unorm16_exact: 0 of 65536 codes differ" in r.stdout, r.stdout
 
 
 @pytest.mark.gpu

@@ -198,6 +198,7 @@ struct vkdt_cuda_graph_t
   int nl = 0;
   size_t off_src = 0, off_rgbf = 0, off_out = 0, off_hist = 0, off_dbg0 = 0, off_dbg1 = 0, off_lut = 0, arena_bytes = 0;
   bool wavelet = false;          // denoise strength > 0: the wavelet nodes run before hilite
+  bool doub_fixed = false;       // bayer: denoise/doub's bilinear taps at fixed places in every row and column
   int block = 2;                 // CFA block: 2 bayer, 3 x-trans
   bool halfsize = false, resample = false;  // demosaic/halfsize (+ shared/resample) for reduced sizes
   bool rcd = false;              // demosaic method 1 (rcd_conv + rcd_fill) at full size
@@ -690,6 +691,30 @@ size_t plan_arena(vkdt_cuda_graph_t *g)
   return off;
 }
 
+// denoise/doub.comp:35-40 samples the coarse levels by texture() at the
+// normalised centre of output position x of n, on a level of size h = n / 2.
+// True when, in the kernel's IEEE single operations and the sampler's 8 bit
+// sub-texel position, that is texel x/2 - 1 at fraction 0.75 for even x and
+// texel x/2 at 0.25 for odd x, for every x (the fixed taps of k_dn_doub_quad).
+bool doub_taps_fixed(int n, int h)
+{
+  if(n != 2 * h) return false;
+  for(int x = 0; x < n; x++)
+  {
+    volatile float u = ((float)x + 0.5f) / (float)n;
+    volatile float t = u * (float)h;
+    volatile float v = t - 0.5f;
+    volatile float s = v * 256.0f;
+    volatile float r = s + 0.5f;
+    volatile float xs = std::floor(r) * 0.00390625f;
+    const float fx = std::floor(xs);
+    const float ax = xs - fx;
+    const int want = (x & 1) ? x / 2 : x / 2 - 1;
+    if((int)fx != want || ax != ((x & 1) ? 0.25f : 0.75f)) return false;
+  }
+  return true;
+}
+
 // the push constants and uniforms of the wavelet denoise nodes (denoise/main.c:133-333)
 void fill_denoise(vkdt_cuda_graph_t *g, dev_denoise_t &p, const void *d_src)
 {
@@ -704,6 +729,8 @@ void fill_denoise(vkdt_cuda_graph_t *g, dev_denoise_t &p, const void *d_src)
     p.black[k] = g->nblack[k];
     p.white[k] = g->nwhite[k];
     p.wb[k] = g->ip.whitebalance[k];
+    p.wb_norm[k] = p.wb[k] / (p.white[k] - p.black[k]);
+    p.wb_denorm[k] = (p.white[k] - p.black[k]) / p.wb[k];
   }
   p.na = g->ip.noise_a; p.nb = g->ip.noise_b;
   module_t *dn = g->mod("denoise");
@@ -711,6 +738,8 @@ void fill_denoise(vkdt_cuda_graph_t *g, dev_denoise_t &p, const void *d_src)
   p.strength = dn->f("strength"); p.luma = dn->f("luma"); p.detail = dn->f("detail");
   p.thrs0 = std::pow(p.strength, 4.0f);
   p.block_f = g->ip.filters == 9u ? 2.23607f : 1.414213f;   // denoise/main.c:235-238 (block 3 / 2)
+  p.doub_fixed = g->doub_fixed;
+  p.fuse_half = g->ip.filters != 9u;
   const float bl[4] = { 0.7000f, 0.4900f, 0.3430f, 0.2401f };
   for(int l = 0; l < 4; l++) p.bscale[l] = bl[l] / p.block_f;
   for(int l = 0; l < 4; l++) p.pl[l] = std::pow(0.7f, (float)l);
@@ -793,7 +822,7 @@ int enqueue(vkdt_cuda_graph_t *g, cudaStream_t s, const void *d_src, void *d_out
   if((r = mark())) return r;
   // 0. wavelet denoise (strength > 0): half, downcov, down x3, assemble, doub
   if(g->wavelet)
-    for(int stage = 0; stage < 7; stage++)
+    for(int stage = dd.fuse_half ? 1 : 0; stage < 7; stage++)
     {
       CU(launch_denoise(dd, stage, s));
       if((r = mark())) return r;
@@ -1272,6 +1301,7 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
     return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "bayer mosaic width and crop window must be even");
   if(g->W < 16 || g->H < 16) return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "image smaller than 16x16");
   g->hw = g->W / g->block; g->hh = g->H / g->block;
+  g->doub_fixed = !xt && doub_taps_fixed(g->W, g->hw) && doub_taps_fixed(g->H, g->hh);
   // demosaic/main.c:18-41, 92-111: a requested size of 1/(1.5 block) or less
   // takes the half size demosaic, resampled unless the scale is the block
   const int method = g->mod("demosaic")->n("method");
@@ -1401,7 +1431,9 @@ int vkdt_cuda_graph_create_nodes(vkdt_cuda_graph_t *g)
   if(g->wavelet)
   {
     const char *dk[7] = { "half", "downcov", "down", "down", "down", "assemble", "doub" };
-    for(int i = 0; i < 7; i++) L_dn[i] = launch("denoise", dk[i]);
+    // bayer: the downcov launch makes the half image as well
+    for(int i = g->ip.filters != 9u ? 1 : 0; i < 7; i++) L_dn[i] = launch("denoise", dk[i]);
+    if(L_dn[0] < 0) L_dn[0] = L_dn[1];
   }
   std::vector<int> L_hr, L_ha, L_lr, L_la;
   int L_noop = -1, L_half = -1, L_a0 = -1, L_doub = -1, L_gauss = -1, L_splat = -1, L_fix = -1, L_hs = -1, L_rs = -1;

@@ -107,10 +107,13 @@ struct dev_denoise_t
   int hw, hh;            // half size (W/block, H/block)
   uint32_t filters;      // 9 x-trans, else bayer
   float black[3], white[3], wb[3];  // unorm black/white per channel, camera white balance
+  float wb_norm[3], wb_denorm[3];   // wb / (white - black) and its inverse (assemble)
   float na, nb;          // noise profile (normalised)
   float edge_gain[3];    // exp2(12 edges.rgb + edges.a) of noise_sigma
   float strength, luma, detail, thrs0;  // params; thrs0 = strength^4
   float block_f;         // 1.414213 (bayer), 2.23607 (x-trans)
+  int doub_fixed;        // bayer, W = 2 hw, H = 2 hh, doub's taps at fixed places (checked on the host)
+  int fuse_half;         // bayer: the downcov launch makes the half image (no half launch)
   float bscale[4];       // 0.7^(l+1) / block_f, l = 0..3 (assemble.comp)
   float pl[4];           // 0.7^level
   float rgb_to_yuv[9], yuv_to_rgb[9];
@@ -124,7 +127,8 @@ struct dev_denoise_t
   uint32_t *dbg_cov;
   uint8_t *dbg_thr;
 };
-// stage 0 half, 1 downcov, 2..4 down levels 1..3, 5 assemble, 6 doub (k_denoise.cu)
+// stage 0 half, 1 downcov, 2..4 down levels 1..3, 5 assemble, 6 doub (k_denoise.cu);
+// with fuse_half stage 0 is not launched: stage 1 makes the half image too
 cudaError_t launch_denoise(const dev_denoise_t &p, int stage, cudaStream_t s);
 
 // the per-node chain for what the fused develop kernel does not cover

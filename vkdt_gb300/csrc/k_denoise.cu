@@ -10,7 +10,6 @@
 // operations in the shader's order, as the oracle evaluates them.
 #include "common.cuh"
 #include "kernels.h"
-#include "launch.cuh"
 #include "sampler.cuh"
 #include "denoise.cuh"
 #include "gauss.cuh"
@@ -112,7 +111,6 @@ DEV void half_bayer(const dev_denoise_t &p, int x, int y, float v[3]) { half_bay
 // replaced by the other one), B of the 2x2 block, on the raw unorm values
 __global__ void __launch_bounds__(256) k_dn_half(const dev_denoise_t p)
 {
-  pdl_begin();
   const int x = blockIdx.x * 16 + threadIdx.x % 16, y = blockIdx.y * 16 + threadIdx.x / 16;
   if(x >= p.hw || y >= p.hh) return;
   if(p.filters == 9u)
@@ -163,7 +161,6 @@ constexpr int DC_T = 16, DC_N = DC_T + 4;
 template<bool HALF>
 __global__ void __launch_bounds__(256, 5) k_dn_downcov(const dev_denoise_t p)
 {
-  pdl_begin();
   __shared__ float2 s_l[DC_N][DC_N];    // (l, 1/l)
   __shared__ float4 s_q[DC_N][DC_N];    // (l^2, 1/l^2, l/25, -)
   __shared__ float4 s_c[DC_N][DC_N];    // (r, g, b, -)
@@ -322,7 +319,6 @@ __global__ void __launch_bounds__(256, 5) k_dn_downcov(const dev_denoise_t p)
 __global__ void __launch_bounds__(256) k_dn_down(const dev_denoise_t p, const half4 *__restrict__ in,
     half4 *__restrict__ out, float pl)
 {
-  pdl_begin();
   const int x = blockIdx.x * 16 + threadIdx.x % 16, y = blockIdx.y * 16 + threadIdx.x / 16;
   if(x >= p.hw || y >= p.hh) return;
   const float t = 0.2f;
@@ -377,7 +373,6 @@ constexpr int DW_T = 16, DW_N = DW_T + 4;
 __global__ void __launch_bounds__(256, 6) k_dn_down_tile(const dev_denoise_t p, const half4 *__restrict__ in,
     half4 *__restrict__ out, float pl)
 {
-  pdl_begin();
   __shared__ float4 win[DW_N][DW_N];
   const int X0 = blockIdx.x * DW_T, Y0 = blockIdx.y * DW_T;
   // the window's slots, two per thread: both loads issued before the first is used
@@ -467,7 +462,6 @@ DEV void m3v(const float *A, const float v[3], float o[3])
 
 __global__ void __launch_bounds__(256) k_dn_assemble(const dev_denoise_t p)
 {
-  pdl_begin();
   const int x = blockIdx.x * 16 + threadIdx.x % 16, y = blockIdx.y * 16 + threadIdx.x / 16;
   if(x >= p.hw || y >= p.hh) return;
   const int szx = p.hw + 1, szy = p.hh + 1;
@@ -547,7 +541,6 @@ __global__ void __launch_bounds__(256) k_dn_assemble(const dev_denoise_t p)
 // level, protected by the detail mask, and normalise to [0, 1]
 __global__ void __launch_bounds__(256) k_dn_doub(const dev_denoise_t p)
 {
-  pdl_begin();
   const int x = blockIdx.x * 32 + threadIdx.x % 32, y = blockIdx.y * 8 + threadIdx.x / 32;
   if(x >= p.W || y >= p.H) return;
   const float ux = __fdiv_rn(__fadd_rn((float)x, 0.5f), (float)p.W);
@@ -589,7 +582,6 @@ __global__ void __launch_bounds__(256) k_dn_doub(const dev_denoise_t p)
 // the rest is continuous and takes the fast quotients.
 __global__ void __launch_bounds__(256) k_dn_doub_quad(const dev_denoise_t p)
 {
-  pdl_begin();
   const int i = blockIdx.x * 32 + threadIdx.x % 32, j = blockIdx.y * 8 + threadIdx.x / 32;
   if(i >= p.hw || j >= p.hh) return;
   // MIRRORED_REPEAT of i - 1 >= -1 and i + 1 <= hw
@@ -654,24 +646,24 @@ cudaError_t launch_denoise(const dev_denoise_t &p, int stage, cudaStream_t s)
   const dim3 gh((p.hw + 15) / 16, (p.hh + 15) / 16);
   switch(stage)
   {
-    case 0: if(p.fuse_half) return cudaErrorInvalidValue; launch_pdl(k_dn_half, gh, 256, 0, s, p); break;
+    case 0: if(p.fuse_half) return cudaErrorInvalidValue; k_dn_half<<<gh, 256, 0, s>>>(p); break;
     case 1:
     {
       const dim3 grid((p.hw + DC_T - 1) / DC_T, (p.hh + DC_T - 1) / DC_T);
-      if(p.fuse_half) launch_pdl(k_dn_downcov<true>, grid, 256, 0, s, p);
-      else launch_pdl(k_dn_downcov<false>, grid, 256, 0, s, p);
+      if(p.fuse_half) k_dn_downcov<true><<<grid, 256, 0, s>>>(p);
+      else k_dn_downcov<false><<<grid, 256, 0, s>>>(p);
       break;
     }
     case 2: case 3: case 4:
       if(p.hw < 8192 && p.hh < 8192)
-        launch_pdl(k_dn_down_tile, dim3((p.hw + DW_T - 1) / DW_T, (p.hh + DW_T - 1) / DW_T), 256, 0, s, 
+        k_dn_down_tile<<<dim3((p.hw + DW_T - 1) / DW_T, (p.hh + DW_T - 1) / DW_T), 256, 0, s>>>(
             p, p.lvl[stage - 2], p.lvl[stage - 1], p.pl[stage - 1]);
-      else launch_pdl(k_dn_down, gh, 256, 0, s, p, p.lvl[stage - 2], p.lvl[stage - 1], p.pl[stage - 1]);
+      else k_dn_down<<<gh, 256, 0, s>>>(p, p.lvl[stage - 2], p.lvl[stage - 1], p.pl[stage - 1]);
       break;
-    case 5: launch_pdl(k_dn_assemble, gh, 256, 0, s, p); break;
+    case 5: k_dn_assemble<<<gh, 256, 0, s>>>(p); break;
     case 6:
-      if(p.doub_fixed) launch_pdl(k_dn_doub_quad, dim3((p.hw + 31) / 32, (p.hh + 7) / 8), 256, 0, s, p);
-      else launch_pdl(k_dn_doub, dim3((p.W + 31) / 32, (p.H + 7) / 8), 256, 0, s, p);
+      if(p.doub_fixed) k_dn_doub_quad<<<dim3((p.hw + 31) / 32, (p.hh + 7) / 8), 256, 0, s>>>(p);
+      else k_dn_doub<<<dim3((p.W + 31) / 32, (p.H + 7) / 8), 256, 0, s>>>(p);
       break;
     default: return cudaErrorInvalidValue;
   }

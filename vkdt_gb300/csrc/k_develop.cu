@@ -43,7 +43,6 @@
 #include "common.cuh"
 #include "hilite.cuh"
 #include "kernels.h"
-#include "launch.cuh"
 #include "pixel.cuh"
 #include "develop_px.cuh"
 #include "gauss.cuh"
@@ -240,7 +239,6 @@ DEV bool mbar_wait(uint32_t bar, int polls)
 template<bool INTERIOR, bool L1> __global__ void __launch_bounds__(NT, L1 ? 5 : VKDT_DEVELOP_CTAS_NO_L1) k_develop(const dev_image_t p, const tiles_t tiles,
     const __grid_constant__ CUtensorMap mmap, int use_map, uint32_t *status)
 {
-  pdl_begin();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   smem_t &s = *reinterpret_cast<smem_t *>(smem_raw);
   const int tid = threadIdx.x;
@@ -608,8 +606,8 @@ template<bool L1> static void launch_tiles(const dev_image_t &p, const tiles_t &
   const size_t bytes = L1 ? sizeof(smem_t) : SMEM_NO_L1;
   CUtensorMap none;
   memset(&none, 0, sizeof(none));
-  if(nin > 0) launch_pdl(k_develop<true, L1>, dim3(t.ix1 - t.ix0 + 1, t.iy1 - t.iy0 + 1), NT, bytes, s, p, t, map ? *map : none, map ? 1 : 0, status);
-  launch_pdl(k_develop<false, L1>, t.nx * t.ny - nin, NT, bytes, s, p, t, none, 0, status);
+  if(nin > 0) k_develop<true, L1><<<dim3(t.ix1 - t.ix0 + 1, t.iy1 - t.iy0 + 1), NT, bytes, s>>>(p, t, map ? *map : none, map ? 1 : 0, status);
+  k_develop<false, L1><<<t.nx * t.ny - nin, NT, bytes, s>>>(p, t, none, 0, status);
 }
 
 // the 2D tensor map over a mosaic of u16 codes (or the f16 bits of the denoised mosaic) that

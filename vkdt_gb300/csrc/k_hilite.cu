@@ -3,7 +3,6 @@
 #include "common.cuh"
 #include "hilite.cuh"
 #include "kernels.h"
-#include "launch.cuh"
 
 namespace {
 
@@ -21,7 +20,6 @@ DEV int mirror1c(int i, int n)
 
 __global__ void __launch_bounds__(256) k_hilite_k1(const dev_hilite_k1_t p)
 {
-  pdl_begin();
   // the reduce terms of every h0 texel of the tile (hilite_reduce_texel)
   __shared__ float st[5][K1_N][K1_N + 1];
   const int OX0 = blockIdx.x * K1_T, OY0 = blockIdx.y * K1_T;
@@ -66,7 +64,6 @@ struct reduce_args_t { float white, desat, wb[3]; };
 __global__ void __launch_bounds__(256) k_hilite_reduce(const half4 *__restrict__ in, int iw, int ih,
     half4 *__restrict__ out, int ow, int oh, const reduce_args_t a)
 {
-  pdl_begin();
   __shared__ float st[5][K1_N][K1_N + 1];
   const int OX0 = blockIdx.x * K1_T, OY0 = blockIdx.y * K1_T;
   const int bx0 = 2 * OX0 - 2, by0 = 2 * OY0 - 2;
@@ -120,7 +117,6 @@ template<int DX, int DY> DEV void assemble_one(const half4 *__restrict__ fine, i
 __global__ void __launch_bounds__(256) k_hilite_assemble(const half4 *__restrict__ fine, int fw, int fh,
     const half4 *__restrict__ coarse, int cw, int ch, half4 *__restrict__ out, float white, float soft)
 {
-  pdl_begin();
   const int ph = threadIdx.x >> 6, b = threadIdx.x & 63;      // parity class, position in it
   const int x = blockIdx.x * 16 + 2 * (b & 7) + (ph & 1), y = blockIdx.y * 16 + 2 * (b >> 3) + (ph >> 1);
   if(x >= fw || y >= fh) return;
@@ -152,7 +148,6 @@ DEV void lds_half4(const half4 *p, float &a, float &b, float &c, float &d)
 
 __global__ void __launch_bounds__(HT_NT) k_hilite_tail(const dev_hilite_tail_t p)
 {
-  pdl_begin();
   extern __shared__ __align__(16) unsigned char tail_raw[];
   const int nr = p.nr;
   const int n0 = p.lw[0] * p.lh[0];
@@ -250,14 +245,14 @@ cudaError_t launch_hilite_tail(const dev_hilite_tail_t &p, cudaStream_t s)
   if(p.nr < 2 || p.nr >= HL_TAIL_MAX) return cudaErrorInvalidValue;
   const size_t smem = hilite_tail_smem_bytes(p.lw, p.lh, p.nr);
   if(smem > HL_TAIL_SMEM) return cudaErrorInvalidValue;
-  launch_pdl(k_hilite_tail, 1, HT_NT, smem, s, p);
+  k_hilite_tail<<<1, HT_NT, smem, s>>>(p);
   return cudaGetLastError();
 }
 
 cudaError_t launch_hilite_k1(const dev_hilite_k1_t &p, cudaStream_t s)
 {
   dim3 grid((p.s1w + K1_T - 1) / K1_T, (p.s1h + K1_T - 1) / K1_T);
-  launch_pdl(k_hilite_k1, grid, 256, 0, s, p);
+  k_hilite_k1<<<grid, 256, 0, s>>>(p);
   return cudaGetLastError();
 }
 
@@ -266,7 +261,7 @@ cudaError_t launch_hilite_reduce(const half4 *in, int iw, int ih, half4 *out, in
 {
   reduce_args_t a = { white, desat, { wb[0], wb[1], wb[2] } };
   dim3 grid((ow + K1_T - 1) / K1_T, (oh + K1_T - 1) / K1_T);
-  launch_pdl(k_hilite_reduce, grid, 256, 0, s, in, iw, ih, out, ow, oh, a);
+  k_hilite_reduce<<<grid, 256, 0, s>>>(in, iw, ih, out, ow, oh, a);
   return cudaGetLastError();
 }
 
@@ -274,6 +269,6 @@ cudaError_t launch_hilite_assemble(const half4 *fine, int fw, int fh, const half
     half4 *out, float white, float soft, cudaStream_t s)
 {
   dim3 grid((fw + 15) / 16, (fh + 15) / 16);
-  launch_pdl(k_hilite_assemble, grid, 256, 0, s, fine, fw, fh, coarse, cw, ch, out, white, soft);
+  k_hilite_assemble<<<grid, 256, 0, s>>>(fine, fw, fh, coarse, cw, ch, out, white, soft);
   return cudaGetLastError();
 }

@@ -12,7 +12,6 @@
 #include "common.cuh"
 #include "hilite.cuh"
 #include "kernels.h"
-#include "launch.cuh"
 #include "pixel.cuh"
 
 #include <cudaTypedefs.h>
@@ -135,7 +134,6 @@ __global__ void __launch_bounds__(256, 7) k_llap_reduce(const __grid_constant__ 
     const __half *__restrict__ in, int iw, int ih, int ipitch, size_t ip,
     __half *__restrict__ out, int ow, int oh, int opitch, size_t op, uint32_t *status)
 {
-  pdl_begin();
   __shared__ __align__(128) __half t[RPG][RI_Y][RB_X];   // the group's planes at once: every load in flight together
   __shared__ __align__(8) uint64_t bar;
   const int k0 = blockIdx.z * RPG, nk = min(RPG, NPL - k0);
@@ -281,7 +279,6 @@ __global__ void __launch_bounds__(256) k_llap_assemble(const __half *__restrict_
     const __half *__restrict__ l0, int w0, int h0, int pitch0, size_t p0,
     const __half *__restrict__ l1, int w1, int h1, int pitch1, size_t p1, __half *__restrict__ out)
 {
-  pdl_begin();
   __shared__ coarse_t sl;
   const int X0 = blockIdx.x * FTX, Y0 = blockIdx.y * FTY;
   stage_coarse(sl, l1, w1, h1, pitch1, p1, first ? l1 + NG * p1 : coarse, X0 / 2 - 2, Y0 / 2 - 2);
@@ -377,7 +374,6 @@ DEV uint2 pack_half4(half4 h) { return *reinterpret_cast<const uint2 *>(&h); }
 
 __global__ void __launch_bounds__(256, 6) k_llap_final(const dev_llap_k3_t p)
 {
-  pdl_begin();
   __shared__ coarse_t sl;
   const int X0 = blockIdx.x * FTX, Y0 = blockIdx.y * FTY;
   stage_coarse(sl, p.l1, p.l1w, p.l1h, p.l1pitch, p.l1plane, p.coarse, X0 / 2 - 2, Y0 / 2 - 2);
@@ -478,7 +474,7 @@ cudaError_t launch_llap_reduce(const llap_level_t &in, const llap_level_t &out, 
   dim3 grid((out.w + RT_X - 1) / RT_X, (out.h + RT_Y - 1) / RT_Y, (NPL + RPG - 1) / RPG);
   CUtensorMap none;
   memset(&none, 0, sizeof(none));
-  launch_pdl(k_llap_reduce, grid, 256, 0, s, map ? *map : none, map ? 1 : 0, in.p, in.w, in.h, in.pitch, in.plane,
+  k_llap_reduce<<<grid, 256, 0, s>>>(map ? *map : none, map ? 1 : 0, in.p, in.w, in.h, in.pitch, in.plane,
                                      out.p, out.w, out.h, out.pitch, out.plane, status);
   return cudaGetLastError();
 }
@@ -487,7 +483,7 @@ cudaError_t launch_llap_assemble(const __half *coarse, int first, const llap_lev
     __half *out, cudaStream_t s)
 {
   dim3 grid((l0.w + FTX - 1) / FTX, (l0.h + FTY - 1) / FTY);
-  launch_pdl(k_llap_assemble, grid, 256, 0, s, coarse, first, l0.p, l0.w, l0.h, l0.pitch, l0.plane,
+  k_llap_assemble<<<grid, 256, 0, s>>>(coarse, first, l0.p, l0.w, l0.h, l0.pitch, l0.plane,
                                        l1.p, l1.w, l1.h, l1.pitch, l1.plane, out);
   return cudaGetLastError();
 }
@@ -495,6 +491,6 @@ cudaError_t launch_llap_assemble(const __half *coarse, int first, const llap_lev
 cudaError_t launch_llap_final(const dev_llap_k3_t &p, cudaStream_t s)
 {
   dim3 grid((p.W + FTX - 1) / FTX, (p.H + FTY - 1) / FTY);
-  launch_pdl(k_llap_final, grid, 256, 0, s, p);
+  k_llap_final<<<grid, 256, 0, s>>>(p);
   return cudaGetLastError();
 }

@@ -14,7 +14,6 @@
 #include "gauss.cuh"
 #include "hilite.cuh"
 #include "kernels.h"
-#include "launch.cuh"
 #include "pixel.cuh"
 #include "sampler.cuh"
 
@@ -461,7 +460,6 @@ __global__ void __launch_bounds__(256) k_nd_resample(const dev_nodes_t p)
 // alpha 1
 __global__ void __launch_bounds__(256) k_nd_crop(const dev_nodes_t p)
 {
-  pdl_begin();
   const int x = blockIdx.x * 16 + threadIdx.x % 16, y = blockIdx.y * 16 + threadIdx.x / 16;
   if(x >= p.cw || y >= p.ch) return;
   const float *b = p.crop;
@@ -599,7 +597,6 @@ DEV int mirror1(int i, int n)
 // (p.rgbf holds the filmcurv output); this kernel reads it for the llap curves
 template<bool FC> __global__ void __launch_bounds__(NT) k_post(const dev_image_t p, const half4 *__restrict__ dm, int dm_pitch)
 {
-  pdl_begin();
   __shared__ __half2 L0p[LLAP_PAIRS][LX][2][LH];        // the curve planes in pairs, [y][x & 1][x >> 1]
   __shared__ __align__(4) __half L0g[LX][LX + 1];       // the grey plane, [y][slot], rows of an even length
   __shared__ uint32_t hist[257];
@@ -723,7 +720,7 @@ cudaError_t launch_nodes(const dev_nodes_t &p, int stage, cudaStream_t s)
       }
       break;
     case 6: if(xt) k_nd_halfsize<true><<<gh, 256, 0, s>>>(p); else k_nd_halfsize<false><<<gh, 256, 0, s>>>(p); break;
-    case 9: launch_pdl(k_nd_crop, dim3((p.cw + 15) / 16, (p.ch + 15) / 16), 256, 0, s, p); break;
+    case 9: k_nd_crop<<<dim3((p.cw + 15) / 16, (p.ch + 15) / 16), 256, 0, s>>>(p); break;
     case 7: k_nd_resample<<<dim3((p.ow + 15) / 16, (p.oh + 15) / 16), 256, 0, s>>>(p); break;
     case 8: k_nd_hl_bayer<<<gh, 256, 0, s>>>(p); break;
     default: return cudaErrorInvalidValue;
@@ -733,7 +730,7 @@ cudaError_t launch_nodes(const dev_nodes_t &p, int stage, cudaStream_t s)
 
 cudaError_t launch_post(const dev_image_t &p, const half4 *dm, int dm_pitch, cudaStream_t s)
 {
-  if(dm) launch_pdl(k_post<false>, dim3((p.W + TX - 1) / TX, (p.H + TY - 1) / TY), NT, 0, s, p, dm, dm_pitch);
-  else    launch_pdl(k_post<true>, dim3((p.W + TX - 1) / TX, (p.H + TY - 1) / TY), NT, 0, s, p, dm, dm_pitch);
+  if(dm) k_post<false><<<dim3((p.W + TX - 1) / TX, (p.H + TY - 1) / TY), NT, 0, s>>>(p, dm, dm_pitch);
+  else    k_post<true><<<dim3((p.W + TX - 1) / TX, (p.H + TY - 1) / TY), NT, 0, s>>>(p, dm, dm_pitch);
   return cudaGetLastError();
 }

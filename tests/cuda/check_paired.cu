@@ -10,7 +10,10 @@
 // more lines compare a product followed by a sum, a b + c: as two paired
 // operations, which the code generator contracts into one paired fma (one
 // rounding instead of two), and as the demosaic covariance writes it, the
-// paired product followed by scalar IEEE adds, which are never contracted.
+// paired product followed by scalar IEEE adds, which are never contracted;
+// and the denoise structure tensor's form: the product as a paired fma whose
+// addend is a -0 the compiler cannot see (exact: x + -0 = x), then a paired
+// add, which has no product to contract with.
 #include <cuda_runtime.h>
 #include <cstdio>
 #include <cstdint>
@@ -32,14 +35,16 @@ static float operand(uint32_t h, int cls)
   return f;
 }
 
-__global__ void k_pair(const float2 *a, const float2 *b, const float2 *c, float2 *o, int n, int op)
+__global__ void k_pair(const float2 *a, const float2 *b, const float2 *c, float2 *o, int n, int op, float nz)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if(i >= n) return;
   const float2 x = a[i], y = b[i], z = c[i];
   o[i] = op == 0 ? __fadd2_rn(x, y) : op == 1 ? __fmul2_rn(x, y) : op == 2 ? __ffma2_rn(x, y, z)
-       : op == 3 ? __fadd2_rn(__fmul2_rn(x, y), z) : [&] { const float2 t = __fmul2_rn(x, y);
-                                                             return make_float2(__fadd_rn(t.x, z.x), __fadd_rn(t.y, z.y)); }();
+       : op == 3 ? __fadd2_rn(__fmul2_rn(x, y), z)
+       : op == 4 ? [&] { const float2 t = __fmul2_rn(x, y); return make_float2(__fadd_rn(t.x, z.x), __fadd_rn(t.y, z.y)); }()
+       // the product as a paired fma with an addend of -0 the compiler cannot see (x + -0 = x for every x)
+       : __fadd2_rn(__ffma2_rn(x, y, make_float2(nz, nz)), z);
 }
 __global__ void k_scalar(const float *a, const float *b, const float *c, float *o, int n, int op)
 {
@@ -65,7 +70,7 @@ int main()
   if(cudaMalloc(&da, bytes) || cudaMalloc(&db, bytes) || cudaMalloc(&dc, bytes) || cudaMalloc(&dp, bytes) || cudaMalloc(&ds, bytes))
   { printf("device allocation failed\n"); return 2; }
   const char *cls[5] = { "normal", "near subnormal", "subnormal", "special", "remainder" };
-  const char *ops[5] = { "add", "mul", "fma", "paired mul+add", "paired mul, scalar add" };
+  const char *ops[6] = { "add", "mul", "fma", "paired mul+add", "paired mul, scalar add", "paired fma -0, paired add" };
   for(int c = 0; c < 5; c++)
   {
     uint32_t h = 12345u + 977u * c;
@@ -86,10 +91,10 @@ int main()
     cudaMemcpy(db, hb.data(), bytes, cudaMemcpyHostToDevice);
     cudaMemcpy(dc, hc.data(), bytes, cudaMemcpyHostToDevice);
     printf("%-15s of %d components:", cls[c], 2 * n);
-    for(int op = (c < 4 ? 0 : 2); op < (c == 0 ? 5 : 3); op++)
+    for(int op = (c < 4 ? 0 : 2); op < (c == 0 ? 6 : 3); op++)
     {
-      k_pair<<<(n + 255) / 256, 256>>>((const float2 *)da, (const float2 *)db, (const float2 *)dc, (float2 *)dp, n, op);
-      k_scalar<<<(2 * n + 255) / 256, 256>>>(da, db, dc, ds, 2 * n, op);
+      k_pair<<<(n + 255) / 256, 256>>>((const float2 *)da, (const float2 *)db, (const float2 *)dc, (float2 *)dp, n, op, -0.0f);
+      k_scalar<<<(2 * n + 255) / 256, 256>>>(da, db, dc, ds, 2 * n, op > 4 ? 3 : op);
       if(cudaDeviceSynchronize() != cudaSuccess) { printf(" device error\n"); return 2; }
       cudaMemcpy(hp.data(), dp, bytes, cudaMemcpyDeviceToHost);
       cudaMemcpy(hs.data(), ds, bytes, cudaMemcpyDeviceToHost);

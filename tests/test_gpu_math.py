@@ -54,3 +54,5 @@ def test_paired_fp32_intrinsics_against_scalar(tmp_path):
     # single paired operations round as the scalar ones; a paired product summed by scalar IEEE adds
     # (the covariance's form) keeps both roundings
     assert "add 0 mul 0 fma 0" in r.stdout and "paired mul, scalar add 0 " in r.stdout, r.stdout
+    # the denoise structure tensor: a product by a paired fma with an opaque -0 addend, then a paired add
+    assert "paired fma -0, paired add 0 " in r.stdout, r.stdout

@@ -740,6 +740,7 @@ void fill_denoise(vkdt_cuda_graph_t *g, dev_denoise_t &p, const void *d_src)
   p.block_f = g->ip.filters == 9u ? 2.23607f : 1.414213f;   // denoise/main.c:235-238 (block 3 / 2)
   p.doub_fixed = g->doub_fixed;
   p.fuse_half = g->ip.filters != 9u;
+  p.neg_zero = -0.0f;
   const float bl[4] = { 0.7000f, 0.4900f, 0.3430f, 0.2401f };
   for(int l = 0; l < 4; l++) p.bscale[l] = bl[l] / p.block_f;
   for(int l = 0; l < 4; l++) p.pl[l] = std::pow(0.7f, (float)l);

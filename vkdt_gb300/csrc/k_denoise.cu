@@ -153,13 +153,17 @@ constexpr int DC_T = 16, DC_N = DC_T + 4;
 // gauss.cuh): i (l, 1/l) + m is one paired fma, exact as the product by the
 // integer offset i in [-2, 2] is; the differences to the means, the products
 // and the quotients (div2_ry from one correctly rounded reciprocal per sum)
-// are paired; the sums of products are scalar IEEE adds, as the code
-// generator may contract a paired product into a paired sum.
+// are paired. The code generator contracts a paired product into the paired
+// sum that takes it, so the products the sums take are paired fmas with an
+// opaque -0 addend (exact), checked against the scalar IEEE form on the device.
 // HALF (bayer): the window is made from the mosaic here (half_bayer, rounded to
 // f16 as the stored half image) and the tile's own texels of the half image are
 // written, in place of a launch of k_dn_half.
+#ifndef VKDT_DOWNCOV_CTAS
+#define VKDT_DOWNCOV_CTAS 5    // CTAs per SM the register budget is cut for
+#endif
 template<bool HALF>
-__global__ void __launch_bounds__(256, 5) k_dn_downcov(const dev_denoise_t p)
+__global__ void __launch_bounds__(256, VKDT_DOWNCOV_CTAS) k_dn_downcov(const dev_denoise_t p)
 {
   __shared__ float2 s_l[DC_N][DC_N];    // (l, 1/l)
   __shared__ float4 s_q[DC_N][DC_N];    // (l^2, 1/l^2, l/25, -)
@@ -167,6 +171,7 @@ __global__ void __launch_bounds__(256, 5) k_dn_downcov(const dev_denoise_t p)
   const int X0 = blockIdx.x * DC_T, Y0 = blockIdx.y * DC_T;
   // the window's slots, two per thread: all loads issued before the first is used
   constexpr int NS = (DC_N * DC_N + 255) / 256;
+  const bool inner = X0 >= 2 && Y0 >= 2 && X0 + DC_N - 2 <= p.hw && Y0 + DC_N - 2 <= p.hh;
   bayer_block_t blk[NS];
   uint2 tex[NS];
 #pragma unroll
@@ -175,10 +180,13 @@ __global__ void __launch_bounds__(256, 5) k_dn_downcov(const dev_denoise_t p)
     const int i = threadIdx.x + 256 * r;
     if(i >= DC_N * DC_N) break;
     const int tx = i % DC_N, ty = i / DC_N;
-    // slots an output reads are within 2 of the image (mirror exact); the
-    // clamp only keeps the unused slots of images narrower than a tile in bounds
-    const int x = min(max(mirror(X0 - 2 + tx, p.hw), 0), p.hw - 1);
-    const int y = min(max(mirror(Y0 - 2 + ty, p.hh), 0), p.hh - 1);
+    int x = X0 - 2 + tx, y = Y0 - 2 + ty;
+    if(!inner)
+    { // slots an output reads are within 2 of the image (mirror exact); the
+      // clamp only keeps the unused slots of images narrower than a tile in bounds
+      x = min(max(mirror(x, p.hw), 0), p.hw - 1);
+      y = min(max(mirror(y, p.hh), 0), p.hh - 1);
+    }
     if(HALF) blk[r] = half_bayer_load(p, x, y);
     else tex[r] = __ldg(reinterpret_cast<const uint2 *>(p.half_img + (size_t)y * p.hw + x));
   }
@@ -229,9 +237,12 @@ __global__ void __launch_bounds__(256, 5) k_dn_downcov(const dev_denoise_t p)
   }
   // second moments
   const float2 n0 = make_float2(-m0.x, -m0.y), n1 = make_float2(-m1.x, -m1.y);   // i - m as i + (-m): exact
+  // the last products as paired fmas with an addend of -0 the compiler cannot see
+  // (p.neg_zero; x + -0 = x for every x): the sums that take them are paired adds
+  // with no product to contract with
+  const float2 nz = make_float2(p.neg_zero, p.neg_zero);
   float mean_b = 0.0f;
-  float Sw00 = 0.0f, Sw01 = 0.0f, Sw10 = 0.0f, Sw11 = 0.0f, Sb00 = 0.0f, Sb01 = 0.0f, Sb10 = 0.0f, Sb11 = 0.0f;
-  float2 ss = make_float2(0.0f, 0.0f);
+  float2 S00 = make_float2(0.0f, 0.0f), S01 = S00, S10 = S00, S11 = S00, ss = S00;   // (w, b)
 #pragma unroll
   for(int j = -2; j <= 2; j++)
 #pragma unroll
@@ -243,21 +254,21 @@ __global__ void __launch_bounds__(256, 5) k_dn_downcov(const dev_denoise_t p)
       const float2 q0 = __fadd2_rn(make_float2((float)i, (float)i), n0);
       const float2 q1 = __fadd2_rn(make_float2((float)j, (float)j), n1);
       const float2 a = __fmul2_rn(P, q0), b = __fmul2_rn(P, q1);
-      const float2 t00 = __fmul2_rn(a, q0), t01 = __fmul2_rn(a, q1), t10 = __fmul2_rn(b, q0), t11 = __fmul2_rn(b, q1);
-      Sw00 = __fadd_rn(Sw00, t00.x); Sb00 = __fadd_rn(Sb00, t00.y);
-      Sw01 = __fadd_rn(Sw01, t01.x); Sb01 = __fadd_rn(Sb01, t01.y);
-      Sw10 = __fadd_rn(Sw10, t10.x); Sb10 = __fadd_rn(Sb10, t10.y);
-      Sw11 = __fadd_rn(Sw11, t11.x); Sb11 = __fadd_rn(Sb11, t11.y);
+      S00 = __fadd2_rn(S00, __ffma2_rn(a, q0, nz));
+      S01 = __fadd2_rn(S01, __ffma2_rn(a, q1, nz));
+      S10 = __fadd2_rn(S10, __ffma2_rn(b, q0, nz));
+      S11 = __fadd2_rn(S11, __ffma2_rn(b, q1, nz));
       ss = __fadd2_rn(ss, P);
     }
+  float Sw00, Sw01, Sw10, Sw11, Sb00, Sb01, Sb10, Sb11;
   {
     const bool okw = div_ok(ss.x), okb = div_ok(ss.y);
     const float2 ys = make_float2(__frcp_rn(ss.x), __frcp_rn(ss.y));
     float2 r;
-    r = div2_ry(make_float2(Sw00, Sb00), ss, ys, okw, okb); Sw00 = r.x; Sb00 = r.y;
-    r = div2_ry(make_float2(Sw01, Sb01), ss, ys, okw, okb); Sw01 = r.x; Sb01 = r.y;
-    r = div2_ry(make_float2(Sw10, Sb10), ss, ys, okw, okb); Sw10 = r.x; Sb10 = r.y;
-    r = div2_ry(make_float2(Sw11, Sb11), ss, ys, okw, okb); Sw11 = r.x; Sb11 = r.y;
+    r = div2_ry(S00, ss, ys, okw, okb); Sw00 = r.x; Sb00 = r.y;
+    r = div2_ry(S01, ss, ys, okw, okb); Sw01 = r.x; Sb01 = r.y;
+    r = div2_ry(S10, ss, ys, okw, okb); Sw10 = r.x; Sb10 = r.y;
+    r = div2_ry(S11, ss, ys, okw, okb); Sw11 = r.x; Sb11 = r.y;
   }
   // cov.glsl: the form with the smaller determinant
   const float detw = __fsub_rn(__fmul_rn(Sw00, Sw11), __fmul_rn(Sw10, Sw01));
@@ -377,6 +388,7 @@ __global__ void __launch_bounds__(256, 6) k_dn_down_tile(const dev_denoise_t p, 
   const int X0 = blockIdx.x * DW_T, Y0 = blockIdx.y * DW_T;
   // the window's slots, two per thread: both loads issued before the first is used
   constexpr int NS = (DW_N * DW_N + 255) / 256;
+  const bool inner = X0 >= 2 && Y0 >= 2 && X0 + DW_N - 2 <= p.hw && Y0 + DW_N - 2 <= p.hh;
   uint2 tex[NS];
 #pragma unroll
   for(int r = 0; r < NS; r++)
@@ -384,10 +396,13 @@ __global__ void __launch_bounds__(256, 6) k_dn_down_tile(const dev_denoise_t p, 
     const int k = threadIdx.x + 256 * r;
     if(k >= DW_N * DW_N) break;
     const int tx = k % DW_N, ty = k / DW_N;
-    // slots an output reads are within 2 of the image (mirror exact); the clamp
-    // only keeps the unused slots of images narrower than a tile in bounds
-    const int x = min(max(mirror(X0 - 2 + tx, p.hw), 0), p.hw - 1);
-    const int y = min(max(mirror(Y0 - 2 + ty, p.hh), 0), p.hh - 1);
+    int x = X0 - 2 + tx, y = Y0 - 2 + ty;
+    if(!inner)
+    { // slots an output reads are within 2 of the image (mirror exact); the clamp
+      // only keeps the unused slots of images narrower than a tile in bounds
+      x = min(max(mirror(x, p.hw), 0), p.hw - 1);
+      y = min(max(mirror(y, p.hh), 0), p.hh - 1);
+    }
     tex[r] = __ldg(reinterpret_cast<const uint2 *>(in + (size_t)y * p.hw + x));
   }
 #pragma unroll

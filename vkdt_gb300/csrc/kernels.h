@@ -114,6 +114,7 @@ struct dev_denoise_t
   float block_f;         // 1.414213 (bayer), 2.23607 (x-trans)
   int doub_fixed;        // bayer, W = 2 hw, H = 2 hh, doub's taps at fixed places (checked on the host)
   int fuse_half;         // bayer: the downcov launch makes the half image (no half launch)
+  float neg_zero;        // -0.0f (an addend the compiler cannot fold, k_dn_downcov)
   float bscale[4];       // 0.7^(l+1) / block_f, l = 0..3 (assemble.comp)
   float pl[4];           // 0.7^level
   float rgb_to_yuv[9], yuv_to_rgb[9];

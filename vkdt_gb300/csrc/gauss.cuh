@@ -25,15 +25,18 @@ DEV float2 div2_ry(float2 a, float2 b, float2 y, bool okx, bool oky)
 // structure tensors (Sw of the greens, Sb of their reciprocals) are built side
 // by side as pairs (w, b) where a paired FP32 instruction (add/mul/fma.f32x2)
 // rounds each component as the scalar IEEE operation does: the weighted sums of
-// the means (exact products), the differences to the means, the products, and
-// the quotients. A paired product that a paired sum consumes may be contracted
-// into one fma by the code generator, so every sum of products is a scalar
-// IEEE add (never contracted), as is the determinant. The greens are f16
+// the means (exact products), the differences to the means, the products, the
+// sums and the quotients. A paired product that a paired sum consumes may be
+// contracted into one fma by the code generator, so the products the sums take
+// are paired fmas with an addend of -0 the compiler cannot see (nz, a kernel
+// parameter; x + -0 = x for every x), which leave it nothing to contract; the
+// determinant is scalar. The greens are f16
 // values (the hilite output), so their reciprocals and those of their squares
 // come from rcp_f16v; the quotients by the four sums share one correctly
 // rounded reciprocal each (div_ry): the same IEEE results.
-DEV void gauss_exact(const float px[8], float v[4], int &dec)
+DEV void gauss_exact(const float px[8], float v[4], int &dec, float nz)
 {
+  const float2 z = make_float2(nz, nz);
   // sample values with their reciprocals: (px, 1/px)
   float2 pv[8];
 #pragma unroll
@@ -74,11 +77,10 @@ DEV void gauss_exact(const float px[8], float v[4], int &dec)
     const float2 q0 = __fadd2_rn(make_float2((float)ii, (float)ii), n0);
     const float2 q1 = __fadd2_rn(make_float2((float)j, (float)j), n1);
     const float2 a = __fmul2_rn(P, q0), b = __fmul2_rn(P, q1);
-    const float2 t00 = __fmul2_rn(a, q0), t01 = __fmul2_rn(a, q1), t10 = __fmul2_rn(b, q0), t11 = __fmul2_rn(b, q1);
-    S00 = make_float2(__fadd_rn(S00.x, t00.x), __fadd_rn(S00.y, t00.y));
-    S01 = make_float2(__fadd_rn(S01.x, t01.x), __fadd_rn(S01.y, t01.y));
-    S10 = make_float2(__fadd_rn(S10.x, t10.x), __fadd_rn(S10.y, t10.y));
-    S11 = make_float2(__fadd_rn(S11.x, t11.x), __fadd_rn(S11.y, t11.y));
+    S00 = __fadd2_rn(S00, __ffma2_rn(a, q0, z));
+    S01 = __fadd2_rn(S01, __ffma2_rn(a, q1, z));
+    S10 = __fadd2_rn(S10, __ffma2_rn(b, q0, z));
+    S11 = __fadd2_rn(S11, __ffma2_rn(b, q1, z));
     ss = __fadd2_rn(ss, P);
     k++;
   }

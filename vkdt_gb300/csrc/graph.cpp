@@ -587,6 +587,7 @@ llap_level_t llap_level(vkdt_cuda_graph_t *g, const level_t &l)
 int fill_image(vkdt_cuda_graph_t *g, dev_image_t &d, const void *d_src, void *d_out)
 {
   memset(&d, 0, sizeof(d));
+  d.neg_zero = -0.0f;
   d.mosaic = (const uint16_t *)d_src;
   d.noop_lut = g->at<__half>(g->off_lut);
   d.pitch = g->in_wd;
@@ -757,6 +758,7 @@ void fill_denoise(vkdt_cuda_graph_t *g, dev_denoise_t &p, const void *d_src)
 void fill_nodes(vkdt_cuda_graph_t *g, dev_nodes_t &p, const void *d_src)
 {
   memset(&p, 0, sizeof(p));
+  p.neg_zero = -0.0f;
   p.mosaic = (const uint16_t *)d_src;
   p.noop_lut = g->at<__half>(g->off_lut);
   p.pitch = g->in_wd; p.cx = (int)g->ip.crop_aabb[0]; p.cy = (int)g->ip.crop_aabb[1];

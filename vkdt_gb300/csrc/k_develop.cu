@@ -375,7 +375,7 @@ template<bool INTERIOR, bool L1> __global__ void __launch_bounds__(NT, L1 ? 5 : 
         const int xs = 2 * scx + 2 + ii;
         px[k++] = s.M[2 * scy + 2 + j][xs & 1][xs >> 1];
       }
-      gauss_exact(px, v, dec);
+      gauss_exact(px, v, dec, p.neg_zero);
       // debug: the entry's decisions, written by the CTA whose outputs own it
       if(p.dbg_gauss && cx >= OX / 2 && cx < OX / 2 + TX / 2 && cy >= OY / 2 && cy < OY / 2 + TY / 2)
         p.dbg_gauss[(size_t)cy * hw + cx] = (uint8_t)dec;

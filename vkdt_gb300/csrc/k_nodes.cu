@@ -511,7 +511,7 @@ __global__ void __launch_bounds__(256) k_nd_gauss_bayer(const dev_nodes_t p)
   }
   float v[4];
   int dec;
-  gauss_exact(px, v, dec);
+  gauss_exact(px, v, dec, p.neg_zero);
   p.cov[(size_t)y * p.hw + x] = mk_half4(v[0], v[1], v[2], v[3]);
   if(p.dbg_gauss) p.dbg_gauss[(size_t)y * p.hw + x] = (uint8_t)dec;
 }

@@ -30,6 +30,7 @@ struct dev_image_t
   uint32_t filters;
   // denoise noop, channel 0, unorm units
   float black, white;
+  float neg_zero;       // -0.0f: an fma addend the compiler cannot fold (gauss_exact)
   // hilite/params
   float hl_white, hl_desat, hl_soft;
   float wb[3];
@@ -136,6 +137,7 @@ cudaError_t launch_denoise(const dev_denoise_t &p, int stage, cudaStream_t s);
 // (x-trans mosaics, reduced output sizes): buffers and sizes (k_nodes.cu)
 struct dev_nodes_t
 {
+  float neg_zero;        // -0.0f: an fma addend the compiler cannot fold (gauss_exact)
   const uint16_t *mosaic;
   const __half *noop_lut; // denoise/noop of every u16 code (L1 resident in these kernels)
   int pitch, cx, cy;     // source layout and crop offset

@@ -142,6 +142,20 @@ def test_create_nodes_xtrans():
     assert min(fused) >= 0 and len(set(fused)) >= 20
 
 
+def test_create_nodes_xtrans_wavelet_denoise():
+    # x-trans with the wavelet denoise: the half node keeps a launch of its own (3x3 blocks)
+    g = v.Graph()
+    g.set_input(6240, 4160, v.default_img_param(wd=6240, ht=4160, filters=9))
+    g.set_param("denoise", "strength", 1.0)
+    g.create_nodes()
+    n = g.nodes()
+    g.close()
+    dn = [x for x in n if x[0] == "denoise"]
+    assert [x[1] for x in dn] == ["downcov", "down", "down", "down", "assemble", "half", "doub"]
+    assert all(x[2:4] == (2080, 1386) for x in dn[:6]) and dn[6][2:4] == (6240, 4160)
+    assert len({x[5] for x in dn}) == 7
+
+
 def test_create_nodes_rcd():
     # demosaic method 1 (demosaic/main.c:113-155): rcd_conv at full size, one rcd_fill
     # workgroup per 58x26 tile, no gaussian splat nodes; method 2: always half size

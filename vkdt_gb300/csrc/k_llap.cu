@@ -251,8 +251,8 @@ DEV void stage_coarse(coarse_t &sc, const __half *l1, int w1, int h1, int pitch1
 }
 
 // llap/assemble.comp:89-123 at one output of parity (PX, PY) centred on coarse
-// column slot lx + 2 and row slot sy. l0(k, g) returns the fine level plane k
-// at the output.
+// column slot lx + 2 and row slot sy. l0(hi, glo, ghi) returns the fine level
+// planes hi - 1 and hi (of gamma glo and ghi) at the output.
 template<int PX, int PY, class L0> DEV float assemble_px(L0 l0, float v, const coarse_t &sc, int lx, int sy)
 {
   const float res = vcol<PY>([&](int iy) { return sc.hc[PX][iy][lx]; }, sy);
@@ -261,8 +261,9 @@ template<int PX, int PY, class L0> DEV float assemble_px(L0 l0, float v, const c
   const float a = gclamp((v - glo) / (ghi - glo), 0.0f, 1.0f);
   const float2 (*pr)[FSX] = sc.pr[hi - 1];
   const float2 e = expand2<PX, PY>([&](int ix, int iy) { return pr[iy][ix]; }, lx + 2, sy);
-  const float la = l0(hi - 1, glo) - e.x;
-  const float lb = l0(hi, ghi) - e.y;
+  const float2 f = l0(hi, glo, ghi);
+  const float la = f.x - e.x;
+  const float lb = f.y - e.y;
   return res + la * (1.0f - a) + lb * a;
 }
 
@@ -271,7 +272,8 @@ template<int PX, int PY> DEV void assemble_stored(const coarse_t &sl, const __ha
     size_t o, int lx, int sy, __half *out)
 {
   const float v = h2f(l0[NG * p0 + o]);
-  const float r = assemble_px<PX, PY>([&](int k, float) { return h2f(l0[k * p0 + o]); }, v, sl, lx, sy);
+  const float r = assemble_px<PX, PY>([&](int hi, float, float) {
+      return make_float2(h2f(l0[(hi - 1) * p0 + o]), h2f(l0[hi * p0 + o])); }, v, sl, lx, sy);
   out[o] = f2h(r);
 }
 
@@ -349,13 +351,24 @@ template<int PX, int PY> DEV half4 final_px(const dev_llap_k3_t &p, const coarse
   const float yv = lum2020(gclamp(rgb[0], -1000.0f, 1000.0f), gclamp(rgb[1], -1000.0f, 1000.0f), gclamp(rgb[2], -1000.0f, 1000.0f));
   const float v = f16r(yv);
   const bool unit_curve = p.ll_shadows == 1.0f && p.ll_highlights == 1.0f;
-  float yo_ = f16r(assemble_px<PX, PY>([&](int, float g) {
-      return f16r(unit_curve ? llap_curve_unit(yv, g, rden, p.ll_clarity)
-                             : llap_curve_rcp(yv, g, p.ll_sigma, r2s, rden, p.ll_shadows, p.ll_highlights, p.ll_clarity)); },
+  float yo_ = f16r(assemble_px<PX, PY>([&](int, float glo, float ghi) {
+      if(unit_curve)
+      { // both planes as one pair, as k_post makes the level-0 planes (llap_curve_unit2)
+        const float2 X = make_float2(yv, yv);
+        const float2 c = __fadd2_rn(X, make_float2(-glo, -ghi));
+        const float2 na = __fmul2_rn(__fmul2_rn(c, c), make_float2(-rden, -rden));
+        const float2 e = make_float2(curve_exp(na.x), curve_exp(na.y));
+        const float2 r = __ffma2_rn(__fmul2_rn(make_float2(p.ll_clarity, p.ll_clarity), c), e, X);
+        return make_float2(f16r(r.x), f16r(r.y));
+      }
+      return make_float2(f16r(llap_curve_rcp(yv, glo, p.ll_sigma, r2s, rden, p.ll_shadows, p.ll_highlights, p.ll_clarity)),
+                         f16r(llap_curve_rcp(yv, ghi, p.ll_sigma, r2s, rden, p.ll_shadows, p.ll_highlights, p.ll_clarity))); },
     v, sl, lx, sy));
+  // llap/colour.comp: the output luminance over the input's (continuous: the fast exponential and one quotient)
   const float yo = fmaxf(lum2020(rgb[0], rgb[1], rgb[2]), 1e-8f);
-  if(yo_ < yo) yo_ = yo * expf(1.0f * (yo_ - yo));
-  float o[3] = { fmaxf(0.0f, rgb[0] * yo_ / yo), fmaxf(0.0f, rgb[1] * yo_ / yo), fmaxf(0.0f, rgb[2] * yo_ / yo) };
+  if(yo_ < yo) yo_ = yo * __expf(yo_ - yo);
+  const float s = __fdividef(yo_, yo);
+  float o[3] = { fmaxf(0.0f, rgb[0] * s), fmaxf(0.0f, rgb[1] * s), fmaxf(0.0f, rgb[2] * s) };
   if(p.grade)
   { // grade reads the llap output as stored (f16)
     for(int k = 0; k < 3; k++) o[k] = f16r(o[k]);

@@ -16,7 +16,8 @@
 
 namespace {
 
-DEV float unorm16(uint16_t v) { return __fdiv_rn((float)v, 65535.0f); }
+// R16_UNORM: v / 65535 correctly rounded (unorm16_exact, equal to the IEEE quotient on every code)
+DEV float unorm16(uint16_t v) { return unorm16_exact(v); }
 
 // R16_UNORM mosaic read with MIRRORED_REPEAT over the full input
 DEV float raw_m(const dev_denoise_t &p, int x, int y)

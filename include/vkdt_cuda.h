@@ -303,6 +303,16 @@ int  vkdt_cuda_hist_rgba_f16(const void *d_rgba, int wd, int ht, uint32_t *d_his
 int  vkdt_cuda_waveform_rgba_f16(const void *d_rgba, int wd, int ht, uint32_t *d_out, int out_wd, int out_ht,
     void *stream);
 
+/* lens/main.comp:22-57 (the lens module, declared in bin/default-darkroom.i-raw; no host
+ * code: its params file is the uniform block): a device rgba f16 image of wd x ht resampled
+ * into a device rgba f16 image of out_wd x out_ht (the module's output has the input's size)
+ * through the double sphere camera model. params in the params file's order: centre x, y,
+ * scale x, y, squish0, squish1, ca red, ca blue (lens/params; defaults 0 0 1 1 0 0 1 1).
+ * Catmull-Rom sampling (shared.glsl sample_catmull_rom), alpha 1. 8-byte aligned buffers.
+ * Asynchronous on `stream`. */
+int  vkdt_cuda_lens_rgba_f16(const void *d_in, int wd, int ht, void *d_out, int out_wd, int out_ht,
+                             const float params[8], void *stream);
+
 /* Ingestion of packed raw video (replaces the host unpack of i-mlv/video_mlv.c:254-274,
  * called from read_source at i-mlv/main.c:204-211 through read_frame at main.c:76-85):
  * d_packed holds an uncompressed magic lantern frame of `bytes` bytes (16-bit aligned) with

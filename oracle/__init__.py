@@ -85,6 +85,21 @@ def grade(rgba, lift=(0, 0, 0, 0), gamma=(1, 1, 1, 0), gain=(1, 1, 1, 0), offset
     return out
 
 
+LENS_DEFAULTS = (0.0, 0.0, 1.0, 1.0, 0.0, 0.0, 1.0, 1.0)   # lens/params: centre, scale, squish0/1, ca red/blue
+
+
+def lens(rgba, par=LENS_DEFAULTS, out_size=None):
+    """lens/main.comp restated: H x W x 4 float rgba in (as stored), f16-rounded rgba out of out_size (W, H)"""
+    rgba = np.ascontiguousarray(rgba, np.float32)
+    ht, wd = rgba.shape[:2]
+    owd, oht = out_size or (wd, ht)
+    par = np.ascontiguousarray(par, np.float32)
+    assert par.size == 8
+    out = np.zeros((oht, owd, 4), np.float32)
+    lib().oracle_lens(rgba.ctypes.data, wd, ht, owd, oht, par.ctypes.data, out.ctypes.data)
+    return out
+
+
 def bc1_encode(rgba):
     """o-bc1 restated: BC1 blocks of an rgba u8 image (H x W x 4), 8 bytes per whole 4x4 block"""
     rgba = np.ascontiguousarray(rgba, np.uint8)
@@ -188,6 +203,7 @@ def lib():
         l.oracle_colenc.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
         l.oracle_bc1_encode.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p]
         l.oracle_grade.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_void_p]
+        l.oracle_lens.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
         l.oracle_rcd.argtypes = [C.POINTER(C.c_float), C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
         _lib = l
     return _lib

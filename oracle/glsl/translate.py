@@ -27,7 +27,7 @@ SHADERS = [
     ("hilite", "half"), ("hilite", "reduce"), ("hilite", "assemble"), ("hilite", "doub"),
     ("demosaic", "down"), ("demosaic", "gauss"), ("demosaic", "splat"), ("demosaic", "fix"),
     ("demosaic", "halfsize"), ("demosaic", "rcd_conv"), ("demosaic", "rcd_fill"), ("shared", "resample"),
-    ("crop", "main"), ("colour", "main"), ("filmcurv", "main"),
+    ("crop", "main"), ("lens", "main"), ("colour", "main"), ("filmcurv", "main"),
     ("llap", "curve"), ("llap", "reduce"), ("llap", "assemble"), ("llap", "colour"),
     ("i-mcraw", "decode"), ("colenc", "main"), ("grade", "main"), ("rawhist", "collect"), ("hist", "collect"),
 ]

@@ -1996,6 +1996,57 @@ static void block(const uint8_t *px, uint8_t *out)
 }
 } // namespace bc1
 
+// lens/main.comp:22-57, the double sphere camera model (V. Usenko, N. Demmel, D.
+// Cremers, "The Double Sphere Camera Model", 2018): the output position, centred
+// and scaled by the output's aspect, is unprojected with the two sphere radii
+// r = (squish0, squish1), projected back to a pinhole, moved by the centre and
+// sampled with the Catmull-Rom filter; with chromatic aberration factors other
+// than (1, 1) red and blue sample at positions scaled about the image centre.
+// par is the uniform block: centre (2), scale (2), squish0, squish1, ca red, ca
+// blue. GLSL's component-wise operations in the shader's order; out stores f16.
+template<class T> static img_t<T> lens_main(const img_t<T> &in, const float *par, int wd, int ht)
+{
+  img_t<T> out(wd, ht, 4);
+  const T aspx = T(wd) / T(ht);
+  const T cx = par[0], cy = par[1], fx = par[2], fy = par[3], r0 = par[4], r1 = par[5];
+  const T cax = par[6], cay = par[7];
+  const bool plain = par[6] == 1.0f && par[7] == 1.0f;
+  OMP_FOR
+  for(int y = 0; y < ht; y++) for(int x = 0; x < wd; x++)
+  {
+    const T px = ((T(x) + T(0.5)) / T(wd) - T(0.5)) * aspx;
+    const T py = ((T(y) + T(0.5)) / T(ht) - T(0.5)) * T(1);
+    const T mx = px / fx, my = py / fy;
+    const T r2 = T(0) + mx * mx + my * my;                       // dot(m, m)
+    const T mz = (T(1) - r0 * r0 * r2) / (r0 * std::sqrt(T(1) - (T(2) * r0 - T(1)) * r2) + T(1) - r0);
+    const T s = (mz * r1 + std::sqrt(mz * mz + (T(1) - r1 * r1))) / (mz * mz + r2);
+    const T X = s * mx - T(0), Y = s * my - T(0), Z = s * mz - r1;
+    const T ux = X / Z / aspx + T(0.5) + cx;
+    const T uy = Y / Z / T(1) + T(0.5) + cy;
+    T rgba[4], t[4];
+    catmull_rom_uv(in, ux, uy, t);
+    rgba[0] = t[0]; rgba[1] = t[1]; rgba[2] = t[2];
+    if(!plain)
+    {
+      catmull_rom_uv(in, (ux - T(0.5)) * cax + T(0.5), (uy - T(0.5)) * cax + T(0.5), t);
+      rgba[0] = t[0];
+      catmull_rom_uv(in, (ux - T(0.5)) * cay + T(0.5), (uy - T(0.5)) * cay + T(0.5), t);
+      rgba[2] = t[2];
+    }
+    rgba[3] = T(1);
+    out.store(x, y, rgba, 4);
+  }
+  return out;
+}
+
+extern "C" void oracle_lens(const float *rgba, int wd, int ht, int owd, int oht, const float *par, float *out)
+{
+  img_t<float> in(wd, ht, 4);
+  std::copy(rgba, rgba + (size_t)wd * ht * 4, in.d.begin());
+  const img_t<float> o = lens_main(in, par, owd, oht);
+  std::copy(o.d.begin(), o.d.end(), out);
+}
+
 // colenc/main.comp:15-80: rec2020 linear rgb to the output primaries
 // (matrices.h, row major) and transfer curve; out: rgba with alpha 1, as FP32
 // values (the f16 store rounds them; an 8-bit sink rounds them to 1/255)

@@ -191,6 +191,9 @@ size_t oracle_mcraw_encode(const uint16_t *img, int rwd, int ht, int force_cnt,
     uint8_t *bitcnt, uint16_t *refval, uint8_t *data, size_t cap);
 /* colenc/main.comp: rec2020 rgba (floats) to the output primaries and transfer curve, FP32 out */
 void oracle_colenc(const float *rgba, int wd, int ht, int prim, int trc, float *out);
+/* lens/main.comp: a wd x ht rgba image (floats, as stored) resampled to owd x oht through the
+ * double sphere model; par = centre (2), scale (2), squish0, squish1, ca red, ca blue; out f16-rounded */
+void oracle_lens(const float *rgba, int wd, int ht, int owd, int oht, const float *par, float *out);
 // grade/main.comp: rgba (float) in, rgba out; par = lift, gamma, gain, offset (4 floats each)
 void oracle_grade(const float *rgba, int wd, int ht, const float *par, int mode, float sh_pivot, float hi_pivot,
                   float *out);

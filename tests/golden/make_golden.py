@@ -23,8 +23,9 @@ sys.path.insert(0, os.path.join(ROOT, "tests"))
 import oracle                      # noqa: E402
 import vkdt_gb300 as v             # noqa: E402
 from oracle import glsl_ref        # noqa: E402
-from golden_cases import (CASES, ENCODE_COLENC, GRADE_CASES, MCRAW_BYTES, MCRAW_CASES, NOISE_A,   # noqa: E402
-                          NOISE_B, encode_inputs, grade_input, img_param, mcraw_stream, oracle_params, path)
+from golden_cases import (CASES, ENCODE_COLENC, GRADE_CASES, LENS_CASES, MCRAW_BYTES, MCRAW_CASES,   # noqa: E402
+                          NOISE_A, NOISE_B, encode_inputs, grade_input, img_param, lens_input, mcraw_stream,
+                          oracle_params, path)
 
 
 def main():
@@ -92,6 +93,17 @@ def main():
             outs.append(dst.a.astype(np.float16))
         np.savez_compressed(path("grade"), out=np.stack(outs))
         print("%-24s grade" % "grade")
+    if not only or "lens" in only:
+        # lens/main.comp on the f16 input, the output as stored (f16), at the input's size
+        f = lens_input()
+        outs = []
+        for par in LENS_CASES:
+            src, dst = glsl_ref.Img(f.shape[1], f.shape[0], 4), glsl_ref.Img(f.shape[1], f.shape[0], 4)
+            src.a[...] = f
+            glsl_ref.run("lens_main", f.shape[1], f.shape[0], {0: src, 1: dst}, uniform=glsl_ref.f32(*par))
+            outs.append(dst.a.astype(np.float16))
+        np.savez_compressed(path("lens"), out=np.stack(outs))
+        print("%-24s lens" % "lens")
 
 
 if __name__ == "__main__":

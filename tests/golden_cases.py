@@ -134,6 +134,31 @@ def load_grade():
     return np.load(path("grade"))["out"]
 
 
+# lens (lens/main.comp): the uniform block centre (2), scale (2), squish0, squish1, ca red, ca blue;
+# the first is the params file's default (close to the identity)
+LENS_CASES = [
+    (0.0, 0.0, 1.0, 1.0, 0.0, 0.0, 1.0, 1.0),
+    (0.0, 0.0, 1.0, 1.0, 0.3, 0.1, 1.0, 1.0),
+    (0.02, -0.01, 1.1, 0.95, 0.5, -0.2, 1.0, 1.0),
+    (0.0, 0.0, 0.9, 0.9, 0.2, 0.4, 1.003, 0.996),
+    (-0.03, 0.02, 1.2, 1.2, -0.3, 0.6, 0.99, 1.01),
+]
+
+
+def lens_input(seed=6):
+    """the f16 rgba image of the lens fixture (an input as stored: f16, a smooth field plus noise)"""
+    rng = np.random.default_rng(seed)
+    ht, wd = 36, 52
+    y, x = np.mgrid[0:ht, 0:wd].astype(np.float32)
+    f = np.stack([0.5 + 0.4 * np.sin(x / 5.0), 0.5 + 0.4 * np.cos(y / 4.0), (x + y) / (wd + ht), np.ones_like(x)], -1)
+    f[..., :3] += rng.normal(0, 0.03, (ht, wd, 3)).astype(np.float32)
+    return f.astype(np.float16).astype(np.float32)
+
+
+def load_lens():
+    return np.load(path("lens"))["out"]
+
+
 # oracle parameter field -> (module, parameter) of the graph configuration
 PARAM_MAP = {
     "dn_strength": ("denoise", "strength"),

@@ -166,6 +166,17 @@ def waveform(d_rgba_f16, wd, ht, d_out_u32, out_wd=1000, out_ht=600, stream=0):
                                                  C.c_void_p(stream)), "waveform")
 
 
+LENS_DEFAULTS = (0.0, 0.0, 1.0, 1.0, 0.0, 0.0, 1.0, 1.0)   # lens/params: centre, scale, squish0/1, ca red/blue
+
+
+def lens(d_in_rgba_f16, wd, ht, d_out_rgba_f16, params=LENS_DEFAULTS, out_wd=0, out_ht=0, stream=0):
+    """vkdt_cuda_lens_rgba_f16: the lens module (lens/main.comp, the double sphere model) from a
+    device rgba f16 image of wd x ht into one of out_wd x out_ht (default: the input's size)."""
+    par = (C.c_float * 8)(*[float(x) for x in params])
+    check(_lib.lib().vkdt_cuda_lens_rgba_f16(C.c_void_p(d_in_rgba_f16), wd, ht, C.c_void_p(d_out_rgba_f16),
+                                             out_wd or wd, out_ht or ht, par, C.c_void_p(stream)), "lens")
+
+
 def nprof_fit(hist):
     """vkdt_cuda_nprof_fit: the noise profile (a, b) of a rawhist histogram (nprof module)."""
     h = np.ascontiguousarray(np.asarray(hist, np.float64).reshape(-1))

@@ -147,6 +147,7 @@ _SIGS = {
     "vkdt_cuda_graph_hist": (C.c_int, [_P, C.POINTER(C.c_uint32)]),
     "vkdt_cuda_hist_rgba_f16": (C.c_int, [_P, C.c_int, C.c_int, _P, _P]),
     "vkdt_cuda_waveform_rgba_f16": (C.c_int, [_P, C.c_int, C.c_int, _P, C.c_int, C.c_int, _P]),
+    "vkdt_cuda_lens_rgba_f16": (C.c_int, [_P, C.c_int, C.c_int, _P, C.c_int, C.c_int, C.POINTER(C.c_float), _P]),
     "vkdt_cuda_graph_set_debug": (C.c_int, [_P, C.c_int]),
     "vkdt_cuda_graph_debug_stage": (C.c_int, [_P, C.c_int, C.POINTER(C.c_float), C.c_size_t]),
     "vkdt_cuda_graph_debug_stage_size": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),

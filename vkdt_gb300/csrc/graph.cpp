@@ -5,6 +5,7 @@
 #include "vkdt_cuda.h"
 #include "internal.h"
 #include "kernels.h"
+#include "lens.h"
 #include "scene.h"
 
 #include <cuda_fp16.h>
@@ -2015,6 +2016,19 @@ int vkdt_cuda_waveform_rgba_f16(const void *d_rgba, int wd, int ht, uint32_t *d_
   if(((uintptr_t)d_rgba & 7) || ((uintptr_t)d_out & 3))
     return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "waveform: unaligned buffer");
   CU(launch_waveform((const half4 *)d_rgba, wd, ht, d_out, out_wd, out_ht, (cudaStream_t)stream));
+  return 0;
+}
+
+int vkdt_cuda_lens_rgba_f16(const void *d_in, int wd, int ht, void *d_out, int out_wd, int out_ht,
+    const float params[8], void *stream)
+{
+  if(!d_in || !d_out || !params || wd <= 0 || ht <= 0 || out_wd <= 0 || out_ht <= 0)
+    return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "bad lens arguments");
+  if(((uintptr_t)d_in & 7) || ((uintptr_t)d_out & 7))
+    return fail(VKDT_CUDA_ERROR_FORMAT_NOT_SUPPORTED, "lens: unaligned buffer");
+  lens_par_t q;
+  memcpy(&q, params, sizeof(q));
+  CU(launch_lens((const half4 *)d_in, wd, ht, (half4 *)d_out, out_wd, out_ht, q, (cudaStream_t)stream));
   return 0;
 }
 

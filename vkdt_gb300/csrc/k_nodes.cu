@@ -14,6 +14,7 @@
 #include "gauss.cuh"
 #include "hilite.cuh"
 #include "kernels.h"
+#include "lens.h"
 #include "pixel.cuh"
 #include "sampler.cuh"
 
@@ -488,6 +489,51 @@ __global__ void __launch_bounds__(256) k_nd_crop(const dev_nodes_t p)
   p.cr[(size_t)y * p.cw + x] = mk_half4(v[0], v[1], v[2], 1.0f);
 }
 
+// ---------------------------------------------------------------- lens
+// lens/main.comp:22-57, the double sphere camera model (V. Usenko, N. Demmel, D.
+// Cremers, "The Double Sphere Camera Model", 2018): each output position,
+// centred and scaled by the output's aspect, is unprojected with the two sphere
+// radii (squish0, squish1), projected back to a pinhole, moved by the centre and
+// sampled with the Catmull-Rom filter; with chromatic aberration factors other
+// than (1, 1) red and blue sample at positions scaled about the image centre.
+// The positions decide the texels the filter reads: IEEE operations in the
+// shader's order (its divisions by 1 and additions of 0 are exact and left out).
+// Extreme parameters can put a position anywhere (or make it NaN): every texel
+// index is wrapped by the sampler's mirrored repeat, so no read leaves the image.
+__global__ void __launch_bounds__(256) k_lens(const half4 *__restrict__ in, int w, int h, half4 *__restrict__ out,
+    int ow, int oh, const lens_par_t q)
+{
+  const int x = blockIdx.x * 16 + threadIdx.x % 16, y = blockIdx.y * 16 + threadIdx.x / 16;
+  if(x >= ow || y >= oh) return;
+  const float aspx = __fdiv_rn((float)ow, (float)oh);
+  const float px = __fmul_rn(__fsub_rn(__fdiv_rn(__fadd_rn((float)x, 0.5f), (float)ow), 0.5f), aspx);
+  const float py = __fsub_rn(__fdiv_rn(__fadd_rn((float)y, 0.5f), (float)oh), 0.5f);
+  const float mx = __fdiv_rn(px, q.f[0]), my = __fdiv_rn(py, q.f[1]);
+  const float r2 = __fadd_rn(__fmul_rn(mx, mx), __fmul_rn(my, my));
+  const float r0 = q.r[0], r1 = q.r[1];
+  const float num = __fsub_rn(1.0f, __fmul_rn(__fmul_rn(r0, r0), r2));
+  const float sq = __fsqrt_rn(__fsub_rn(1.0f, __fmul_rn(__fsub_rn(__fmul_rn(2.0f, r0), 1.0f), r2)));
+  const float mz = __fdiv_rn(num, __fsub_rn(__fadd_rn(__fmul_rn(r0, sq), 1.0f), r0));
+  const float a = __fadd_rn(__fmul_rn(mz, r1), __fsqrt_rn(__fadd_rn(__fmul_rn(mz, mz), __fsub_rn(1.0f, __fmul_rn(r1, r1)))));
+  const float sc = __fdiv_rn(a, __fadd_rn(__fmul_rn(mz, mz), r2));
+  const float X = __fmul_rn(sc, mx), Y = __fmul_rn(sc, my), Z = __fsub_rn(__fmul_rn(sc, mz), r1);
+  const float ux = __fadd_rn(__fadd_rn(__fdiv_rn(__fdiv_rn(X, Z), aspx), 0.5f), q.c[0]);
+  const float uy = __fadd_rn(__fadd_rn(__fdiv_rn(Y, Z), 0.5f), q.c[1]);
+  float t[4];
+  catmull_rom_uv<true>(in, w, h, ux, uy, t);
+  float rgb[3] = { t[0], t[1], t[2] };
+  if(!(q.ca[0] == 1.0f && q.ca[1] == 1.0f))
+  {
+    catmull_rom_uv<true>(in, w, h, __fadd_rn(__fmul_rn(__fsub_rn(ux, 0.5f), q.ca[0]), 0.5f),
+                   __fadd_rn(__fmul_rn(__fsub_rn(uy, 0.5f), q.ca[0]), 0.5f), t);
+    rgb[0] = t[0];
+    catmull_rom_uv<true>(in, w, h, __fadd_rn(__fmul_rn(__fsub_rn(ux, 0.5f), q.ca[1]), 0.5f),
+                   __fadd_rn(__fmul_rn(__fsub_rn(uy, 0.5f), q.ca[1]), 0.5f), t);
+    rgb[2] = t[2];
+  }
+  out[(size_t)y * ow + x] = mk_half4(rgb[0], rgb[1], rgb[2], 1.0f);
+}
+
 // ---------------------------------------------------------------- bayer demosaic, node by node
 // (demosaic colour param >= 1: fix.comp:124 widens the fix radius to 2, which
 // the fused develop kernel's tile does not hold; gauss, splat and fix then run
@@ -725,6 +771,12 @@ cudaError_t launch_nodes(const dev_nodes_t &p, int stage, cudaStream_t s)
     case 8: k_nd_hl_bayer<<<gh, 256, 0, s>>>(p); break;
     default: return cudaErrorInvalidValue;
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lens(const half4 *in, int w, int h, half4 *out, int ow, int oh, const lens_par_t &q, cudaStream_t s)
+{
+  k_lens<<<dim3((ow + 15) / 16, (oh + 15) / 16), 256, 0, s>>>(in, w, h, out, ow, oh, q);
   return cudaGetLastError();
 }
 

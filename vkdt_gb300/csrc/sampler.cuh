@@ -21,14 +21,27 @@ DEV void bilinear_at(const half4 *img, int w, int h, int x0, int y0, float ax, f
     out[k] = (t00[k] * (1.0f - ax) + t10[k] * ax) * (1.0f - ay) + (t01[k] * (1.0f - ax) + t11[k] * ax) * ay;
 }
 
-// texture() with LINEAR + MIRRORED_REPEAT at texel-space position (x, y)
-DEV void bilinear(const half4 *img, int w, int h, float x, float y, float out[4])
+// MIRRORED_REPEAT for any texel index (the period 2n), every index in [0, n)
+DEV int mirror_any(int i, int n)
+{
+  const int m = 2 * n;
+  int t = i % m;
+  if(t < 0) t += m;
+  return t < n ? t : m - 1 - t;
+}
+
+// texture() with LINEAR + MIRRORED_REPEAT at texel-space position (x, y). ANY:
+// positions anywhere (a NaN or a position past +-1e9 texels read as +-1e9 before
+// the conversion, every index wrapped by mirror_any), else within one image size
+// of the image (mirror)
+template<bool ANY = false> DEV void bilinear(const half4 *img, int w, int h, float x, float y, float out[4])
 {
   const float xs = subtexel(__fsub_rn(x, 0.5f)), ys = subtexel(__fsub_rn(y, 0.5f));
   const float fx = floorf(xs), fy = floorf(ys);
-  const int x0 = (int)fx, y0 = (int)fy;
+  const int x0 = ANY ? (int)fminf(fmaxf(fx, -1e9f), 1e9f) : (int)fx, y0 = ANY ? (int)fminf(fmaxf(fy, -1e9f), 1e9f) : (int)fy;
   const float ax = xs - fx, ay = ys - fy;
-  const int X0 = mirror(x0, w), X1 = mirror(x0 + 1, w), Y0 = mirror(y0, h), Y1 = mirror(y0 + 1, h);
+  const int X0 = ANY ? mirror_any(x0, w) : mirror(x0, w), X1 = ANY ? mirror_any(x0 + 1, w) : mirror(x0 + 1, w);
+  const int Y0 = ANY ? mirror_any(y0, h) : mirror(y0, h), Y1 = ANY ? mirror_any(y0 + 1, h) : mirror(y0 + 1, h);
   float t00[4], t10[4], t01[4], t11[4];
   ld4(img, w, X0, Y0, t00); ld4(img, w, X1, Y0, t10); ld4(img, w, X0, Y1, t01); ld4(img, w, X1, Y1, t11);
 #pragma unroll
@@ -40,7 +53,7 @@ DEV void bilinear(const half4 *img, int w, int h, float x, float y, float out[4]
 // texture() taps. The tap positions decide the texels read, so they are
 // formed with IEEE operations in the shader's order (including its division
 // back to normalised coordinates, which texture() scales again).
-DEV void catmull_rom_uv(const half4 *img, int w, int h, float u, float v, float res[4])
+template<bool ANY = false> DEV void catmull_rom_uv(const half4 *img, int w, int h, float u, float v, float res[4])
 {
   const float ts[2] = { (float)w, (float)h }, uv[2] = { u, v };
   float t[2][3], wt[2][3];
@@ -68,7 +81,7 @@ DEV void catmull_rom_uv(const half4 *img, int w, int h, float u, float v, float 
     for(int i = 0; i < 3; i++)
     {
       float q[4];
-      bilinear(img, w, h, t[0][i], t[1][j], q);
+      bilinear<ANY>(img, w, h, t[0][i], t[1][j], q);
 #pragma unroll
       for(int c = 0; c < 4; c++) res[c] += q[c] * wt[0][i] * wt[1][j];
     }

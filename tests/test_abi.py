@@ -214,3 +214,19 @@ def test_create_nodes_rejects_bad_input():
     with pytest.raises(_lib.VkdtError):
         g.create_nodes()
     g.close()
+
+
+def test_standalone_nodes_reject_bad_arguments():
+    # the standalone node entries check their arguments before any device work
+    with pytest.raises(_lib.VkdtError) as e:
+        v.lens(0, 64, 48, 0)
+    assert e.value.code == _lib.ERROR_FORMAT_NOT_SUPPORTED
+    with pytest.raises(_lib.VkdtError) as e:
+        v.lens(256, 0, 48, 512)
+    assert e.value.code == _lib.ERROR_FORMAT_NOT_SUPPORTED
+    with pytest.raises(_lib.VkdtError) as e:
+        v.lens(260, 64, 48, 512)                       # an rgba f16 image is 8-byte aligned
+    assert e.value.code == _lib.ERROR_FORMAT_NOT_SUPPORTED
+    with pytest.raises(_lib.VkdtError) as e:
+        v.waveform(0, 64, 48, 0)
+    assert e.value.code == _lib.ERROR_FORMAT_NOT_SUPPORTED

@@ -106,7 +106,8 @@ def graph_name():
 
 
 def config():
-    return {"workload": "%d MP %s graph, one image per step%s" % (round(WD * HT / 1e6),
+    mp = WD * HT / 1e6
+    return {"workload": "%s MP %s graph, one image per step%s" % ("%d" % round(mp) if mp >= 10 else "%.2g" % mp,
                                                                "full darkroom" if GRAPH == "darkroom" else "plain chain",
                                                                ", wavelet denoise" if DENOISE > 0 else ""),
             "wd": WD, "ht": HT, "cfa": "x-trans" if FILTERS == 9 else "rggb", "denoise_strength": DENOISE,
